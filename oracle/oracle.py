@@ -1,0 +1,267 @@
+"""ctypes front end of the CPU FP64 oracle (test infrastructure only).
+
+The oracle restates galax's potentials, Hamiltonian field and the diffrax
+Runge-Kutta / PID-controller arithmetic in C++ (``galax_oracle.cpp``). Only the
+test suite, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` use it, as the checker; the ``galax_gb300`` package never does.
+
+Component records use the same 56-byte layout as the CUDA library's
+``gal_component`` (kind, flags, mass, l1, l2, origin[3]).
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build_oracle
+
+KEPLER, HERNQUIST, MIYAMOTO_NAGAI, NFW, PLUMMER = range(5)
+
+G_GALACTIC = 4.498502151469553e-12  # kpc^3 / (Msun Myr^2), astropy CODATA-2018 G
+
+COMP_DTYPE = np.dtype(
+    [("kind", "<i4"), ("flags", "<i4"), ("m", "<f8"), ("l1", "<f8"), ("l2", "<f8"), ("origin", "<f8", (3,))],
+    align=True,
+)
+assert COMP_DTYPE.itemsize == 56
+
+
+class SolverCfg(C.Structure):
+    _fields_ = [
+        ("method", C.c_int32),
+        ("adaptive", C.c_int32),
+        ("max_steps", C.c_int64),
+        ("dt0", C.c_double),
+        ("rtol", C.c_double),
+        ("atol", C.c_double),
+        ("dtmin", C.c_double),
+        ("dtmax", C.c_double),
+        ("pcoeff", C.c_double),
+        ("icoeff", C.c_double),
+        ("dcoeff", C.c_double),
+        ("safety", C.c_double),
+        ("factormin", C.c_double),
+        ("factormax", C.c_double),
+        ("force_dtmin", C.c_int32),
+        ("lockstep", C.c_int32),
+    ]
+
+
+def solver_cfg(
+    method: int = 8,
+    adaptive: bool = True,
+    *,
+    dt0: float = 0.0,
+    rtol: float = 1e-7,
+    atol: float = 1e-7,
+    dtmin: float = 0.0,
+    dtmax: float = 0.0,
+    pcoeff: float = 0.0,
+    icoeff: float = 1.0,
+    dcoeff: float = 0.0,
+    safety: float = 0.9,
+    factormin: float = 0.2,
+    factormax: float = 10.0,
+    force_dtmin: bool = True,
+    max_steps: int = 2**62,
+    lockstep: bool = False,
+) -> SolverCfg:
+    return SolverCfg(
+        method, int(adaptive), max_steps, dt0, rtol, atol, dtmin, dtmax, pcoeff, icoeff, dcoeff, safety,
+        factormin, factormax, int(force_dtmin), int(lockstep),
+    )
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        path = build_oracle.build()
+        L = C.CDLL(str(path))
+        dp = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+        cp = np.ctypeslib.ndpointer(COMP_DTYPE, flags="C_CONTIGUOUS")
+        i64p = np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")
+        i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+        for name in ("orc_potential", "orc_gradient", "orc_hessian"):
+            getattr(L, name).argtypes = [cp, C.c_int, C.c_double, dp, C.c_int64, dp]
+            getattr(L, name).restype = None
+        L.orc_dgrad_dparams.argtypes = [cp, C.c_int, C.c_double, dp, dp, C.c_int64, dp]
+        L.orc_tableau.argtypes = [C.c_int, dp, dp, dp, dp]
+        L.orc_tableau.restype = C.c_int
+        L.orc_dopri5_cmid.argtypes = [dp]
+        L.orc_integrate.argtypes = [
+            cp, C.c_int, C.c_double, C.POINTER(SolverCfg), dp, dp, dp, i64p, dp, dp, i32p, i64p, i64p,
+            C.c_int64, C.c_int,
+        ]
+        L.orc_integrate.restype = C.c_int
+        L.orc_count_ops.argtypes = [cp, C.c_int, C.c_double, C.c_int, dp, i64p]
+        L.orc_adjoint_fixed.argtypes = [
+            cp, C.c_int, C.c_double, C.POINTER(SolverCfg), dp, C.c_double, C.c_double, dp, dp, dp, dp,
+            C.c_int64, C.c_int,
+        ]
+        L.orc_adjoint_fixed.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def comps(records) -> np.ndarray:
+    """Build a component array from (kind, m, l1, l2, origin) tuples."""
+    a = np.zeros(len(records), COMP_DTYPE)
+    for i, r in enumerate(records):
+        kind, m, l1, l2 = r[:4]
+        origin = r[4] if len(r) > 4 else (0.0, 0.0, 0.0)
+        a[i]["kind"] = kind
+        a[i]["m"] = m
+        a[i]["l1"] = l1
+        a[i]["l2"] = l2
+        a[i]["origin"] = origin
+    return a
+
+
+def milky_way(**over) -> np.ndarray:
+    """galax MilkyWayPotential defaults, component order disk, halo, bulge, nucleus
+    (src/galax/potential/_src/builtin/milkyway.py:203-229)."""
+    d = dict(disk=(6.8e10, 3.0, 0.28), halo=(5.4e11, 15.62), bulge=(5e9, 1.0), nucleus=(1.71e9, 0.07))
+    d.update(over)
+    return comps([
+        (MIYAMOTO_NAGAI, d["disk"][0], d["disk"][1], d["disk"][2]),
+        (NFW, d["halo"][0], d["halo"][1], 0.0),
+        (HERNQUIST, d["bulge"][0], d["bulge"][1], 0.0),
+        (HERNQUIST, d["nucleus"][0], d["nucleus"][1], 0.0),
+    ])
+
+
+def _xyz(x):
+    x = np.ascontiguousarray(np.atleast_2d(np.asarray(x, np.float64)))
+    assert x.shape[-1] == 3
+    return x.reshape(-1, 3)
+
+
+def potential(c: np.ndarray, x, G: float = G_GALACTIC) -> np.ndarray:
+    x = _xyz(x)
+    out = np.empty(len(x))
+    lib().orc_potential(np.ascontiguousarray(c), len(c), G, x, len(x), out)
+    return out
+
+
+def gradient(c: np.ndarray, x, G: float = G_GALACTIC) -> np.ndarray:
+    x = _xyz(x)
+    out = np.empty((len(x), 3))
+    lib().orc_gradient(np.ascontiguousarray(c), len(c), G, x, len(x), out)
+    return out
+
+
+def hessian(c: np.ndarray, x, G: float = G_GALACTIC) -> np.ndarray:
+    x = _xyz(x)
+    out = np.empty((len(x), 3, 3))
+    lib().orc_hessian(np.ascontiguousarray(c), len(c), G, x, len(x), out)
+    return out
+
+
+def dgrad_dparams(c: np.ndarray, x, v, G: float = G_GALACTIC) -> np.ndarray:
+    """d(grad Phi(x) . v)/d(m, l1, l2) per component: shape (n, ncomp, 3)."""
+    x = _xyz(x)
+    v = _xyz(v)
+    out = np.empty((len(x), len(c), 3))
+    lib().orc_dgrad_dparams(np.ascontiguousarray(c), len(c), G, x, v, len(x), out)
+    return out
+
+
+def tableau(method: int):
+    c = np.zeros(13); a = np.zeros(169); b = np.zeros(13); e = np.zeros(13)
+    s = lib().orc_tableau(method, c, a, b, e)
+    return c[:s], a.reshape(13, 13)[:s, :s], b[:s], e[:s]
+
+
+def dopri5_cmid() -> np.ndarray:
+    out = np.zeros(7)
+    lib().orc_dopri5_cmid(out)
+    return out
+
+
+def integrate(
+    c: np.ndarray,
+    y0,
+    t0,
+    t1,
+    save_ts,
+    cfg: SolverCfg,
+    *,
+    G: float = G_GALACTIC,
+    nthreads: int = 0,
+):
+    """Integrate orbits. ``save_ts`` is a list of per-orbit 1-D arrays or a
+    single 1-D array shared by all orbits. Returns (saves list of (T_i, 6),
+    status, accepted, rejected); in lockstep mode saves is (T, n, 6)."""
+    y0 = np.ascontiguousarray(np.atleast_2d(np.asarray(y0, np.float64)))
+    n = len(y0)
+    t0 = np.ascontiguousarray(np.broadcast_to(np.asarray(t0, np.float64), (n,)))
+    t1 = np.ascontiguousarray(np.broadcast_to(np.asarray(t1, np.float64), (n,)))
+    if isinstance(save_ts, np.ndarray) and save_ts.ndim == 1:
+        save_list = [save_ts] * n
+    else:
+        save_list = [np.asarray(s, np.float64).ravel() for s in save_ts]
+    offs = np.zeros(n + 1, np.int64)
+    offs[1:] = np.cumsum([len(s) for s in save_list])
+    flat = np.ascontiguousarray(np.concatenate(save_list) if n else np.zeros(0))
+    status = np.zeros(n, np.int32)
+    acc = np.zeros(n, np.int64)
+    rej = np.zeros(n, np.int64)
+    if cfg.lockstep:
+        ns = len(save_list[0])
+        out = np.empty((ns, n, 6))
+    else:
+        out = np.empty((int(offs[-1]), 6))
+    lib().orc_integrate(
+        np.ascontiguousarray(c), len(c), G, C.byref(cfg), y0, t0, t1, offs, flat, out, status, acc, rej, n,
+        nthreads,
+    )
+    if cfg.lockstep:
+        return out, status, acc, rej
+    return [out[offs[i]:offs[i + 1]] for i in range(n)], status, acc, rej
+
+
+def adjoint_fixed(
+    c: np.ndarray,
+    y0,
+    t0: float,
+    t1: float,
+    target,
+    cfg: SolverCfg,
+    *,
+    G: float = G_GALACTIC,
+    nthreads: int = 0,
+):
+    """Discrete adjoint of constant steps ``cfg.dt0`` from t0 to t1 for the loss
+    L = sum_i |y_i(t1) - target_i|^2. Returns (yT (n,6), dL/dy0 (n,6),
+    dL/dparams (ncomp,3), L)."""
+    y0 = np.ascontiguousarray(np.atleast_2d(np.asarray(y0, np.float64)))
+    target = np.ascontiguousarray(np.asarray(target, np.float64).reshape(y0.shape))
+    n = len(y0)
+    yT = np.empty_like(y0)
+    gy = np.empty_like(y0)
+    gp = np.zeros((len(c), 3))
+    loss = np.zeros(1)
+    lib().orc_adjoint_fixed(
+        np.ascontiguousarray(c), len(c), G, C.byref(cfg), y0, float(t0), float(t1), target, yT, gy,
+        gp.reshape(-1), n, nthreads,
+    )
+    L = float(np.sum((yT - target) ** 2))
+    return yT, gy, gp, L
+
+
+def count_ops(c: np.ndarray, method: int, y=(8.0, 1.0, 0.5, 0.0, 0.2, 0.01), G: float = G_GALACTIC):
+    """Algorithmic FP64 operation counts: dict for one gradient and one step."""
+    out = np.zeros(10, np.int64)
+    lib().orc_count_ops(np.ascontiguousarray(c), len(c), G, method, np.asarray(y, np.float64), out)
+    keys = ("add", "mul", "div", "sqrt", "log1p")
+    return dict(zip(keys, out[:5].tolist())), dict(zip(keys, out[5:].tolist()))
+
+
+def nthreads_default() -> int:
+    return os.cpu_count() or 1

@@ -1,0 +1,157 @@
+"""Extract golden vectors from the reference's tests and doctests.
+
+The reference (GalacticDynamics/galax) cannot be imported here (it needs JAX,
+diffrax, unxt, ...), so its golden values are read as text from the cited lines
+of its test files and docstrings and written, with the inputs each one belongs
+to, into ``reference_goldens.json`` beside this script. Run:
+
+    python tests/golden/make_goldens.py /root/reference
+
+Only this generator reads the reference tree; the tests read the JSON.
+"""
+
+from __future__ import annotations
+
+import json
+import re
+import sys
+from pathlib import Path
+
+NUM = re.compile(r"[-+]?(?:\d+\.\d*|\.\d+|\d+)(?:[eE][-+]?\d+)?")
+KMS = 0.001022712165045695  # 1 km/s in kpc/Myr
+
+# (name, file, [line numbers]): every number on those lines, in order.
+POTENTIAL_SPECS = [
+    ("hernquist", "tests/unit/potential/builtin/test_hernquist.py", [31], [35], [46, 47, 48]),
+    ("miyamoto_nagai", "tests/unit/potential/builtin/test_miyamotonagai.py", [40], [44], [55, 56, 57]),
+    ("nfw", "tests/unit/potential/builtin/test_nfw.py", [40], [44], [56, 57, 58]),
+    ("plummer", "tests/unit/potential/builtin/test_plummer.py", [38], [42], [53, 54, 55]),
+    ("milky_way", "tests/unit/potential/builtin/test_milkywaypotential.py", [43], [48], [61, 62, 63]),
+]
+# parameters of each fixture: tests/unit/potential/builtin/test_common.py
+# (m_tot = m = 1e12 Msun, r_s = a = b = 1 kpc); MilkyWay uses its defaults.
+POTENTIAL_PARAMS = {
+    "hernquist": {"kind": "hernquist", "m": 1e12, "l1": 1.0, "l2": 0.0},
+    "miyamoto_nagai": {"kind": "miyamoto_nagai", "m": 1e12, "l1": 1.0, "l2": 1.0},
+    "nfw": {"kind": "nfw", "m": 1e12, "l1": 1.0, "l2": 0.0},
+    "plummer": {"kind": "plummer", "m": 1e12, "l1": 1.0, "l2": 0.0},
+    "milky_way": {"kind": "milky_way"},
+}
+
+
+def numbers(root: Path, rel: str, lines: list[int]) -> list[float]:
+    text = (root / rel).read_text().splitlines()
+    out: list[float] = []
+    for ln in lines:
+        line = text[ln - 1]
+        # drop unit strings such as "kpc2 / Myr2" before scanning numbers
+        line = re.sub(r'"[^"]*"', "", line)
+        # drop identifiers (dtype=float64, CartesianPos3D, ...) so only literals remain
+        line = re.sub(r"\b[A-Za-z_][A-Za-z_0-9]*", " ", line)
+        out += [float(x) for x in NUM.findall(line)]
+    return out
+
+
+def main(root: Path) -> None:
+    g: dict = {"source": "GalacticDynamics/galax tests and doctests (see 'cite' fields)", "potentials": {}, "orbits": {}}
+    for name, rel, lphi, lgrad, lhess in POTENTIAL_SPECS:
+        phi = numbers(root, rel, lphi)
+        grad = numbers(root, rel, lgrad)
+        hess = numbers(root, rel, lhess)
+        assert len(phi) == 1 and len(grad) == 3 and len(hess) == 9, (name, phi, grad, hess)
+        g["potentials"][name] = {
+            "cite": f"{rel}:{lphi[0]},{lgrad[0]},{lhess[0]}-{lhess[-1]}",
+            "params": POTENTIAL_PARAMS[name],
+            "x": [1.0, 2.0, 3.0],
+            "t": 0.0,
+            "potential": phi[0],
+            "gradient": grad,
+            "hessian": hess,
+            "tol": {"atol": 1e-8, "rtol": 1e-5},
+        }
+
+    f = "src/galax/dynamics/_src/orbit/solver.py"
+    v220 = 220 * KMS
+    step = numbers(root, f, [318, 319, 320, 321])
+    g["orbits"]["dopri8_single_step"] = {
+        "cite": f"{f}:290-321",
+        "potential": {"kind": "hernquist", "m": 1e12, "l1": 5.0, "l2": 0.0},
+        "solver": {"method": 8, "adaptive": False, "dt0": 10.0},
+        "y0": [[8, 0, 9, 0, v220, 0], [9, 0, 3, 0, v220, 0]],
+        "t0": 0.0, "t1": 10.0, "save_ts": [10.0],
+        "expect_q": [step[0:3], step[3:6]], "expect_p": [step[6:9], step[9:12]],
+        "digits": 8,
+    }
+    run = numbers(root, f, [376, 377, 378, 379])
+    g["orbits"]["dopri8_pid_lockstep_run"] = {
+        "cite": f"{f}:348-379",
+        "potential": {"kind": "hernquist", "m": 1e12, "l1": 5.0, "l2": 0.0},
+        "solver": {"method": 8, "adaptive": True, "rtol": 1e-8, "atol": 1e-8, "lockstep": True},
+        "y0": [[8, 0, 9, 0, v220, 0], [9, 0, 3, 0, v220, 0]],
+        "t0": 0.0, "t1": 1000.0, "save_ts": [1000.0],
+        "expect_q": [run[0:3], run[3:6]], "expect_p": [run[6:9], run[9:12]],
+        "digits": 8,
+    }
+    s1 = numbers(root, f, [441, 442])
+    g["orbits"]["dopri8_pid_solve_220kms"] = {
+        "cite": f"{f}:431-442",
+        "potential": {"kind": "hernquist", "m": 1e12, "l1": 5.0, "l2": 0.0},
+        "solver": {"method": 8, "adaptive": True, "rtol": 1e-8, "atol": 1e-8},
+        "y0": [[8, 0, 0, 0, v220, 0]], "t0": 0.0, "t1": 1000.0, "save_ts": [1000.0],
+        "expect_q": [s1[0:3]], "expect_p": [s1[3:6]], "digits": 8,
+    }
+    s2 = numbers(root, f, [456, 457])
+    g["orbits"]["dopri8_pid_solve_array"] = {
+        "cite": f"{f}:451-457",
+        "potential": {"kind": "hernquist", "m": 1e12, "l1": 5.0, "l2": 0.0},
+        "solver": {"method": 8, "adaptive": True, "rtol": 1e-8, "atol": 1e-8},
+        "y0": [[8, 0, 0, 0, 0.22499669, 0]], "t0": 0.0, "t1": 1000.0, "save_ts": [1000.0],
+        "expect_q": [s2[0:3]], "expect_p": [s2[3:6]], "digits": 8,
+    }
+
+    f = "src/galax/dynamics/_src/solver.py"
+    for key, lines_q, lines_p, v in (
+        ("kepler_integrate_field_array", [356, 357, 359, 360], [361, 362, 364, 365], 0.22499668),
+        ("kepler_integrate_field_quantity", [378, 379, 381, 382], [383, 384, 386, 387], v220),
+    ):
+        q = numbers(root, f, lines_q)
+        p = numbers(root, f, lines_p)
+        g["orbits"][key] = {
+            "cite": f"{f}:{lines_q[0]}-{lines_p[-1]} (solver defaults {f}:226-232)",
+            "potential": {"kind": "kepler", "m": 1e11, "l1": 0.0, "l2": 0.0},
+            "solver": {"method": 8, "adaptive": True, "rtol": 1e-7, "atol": 1e-7, "dtmin": 0.05},
+            "y0": [[8, 0, 0, 0, v, 0]], "t0": 0.0, "t1": 1000.0,
+            "save_ts_linspace": [0.0, 1000.0, 100], "rows": [0, 1, 98, 99],
+            "expect_q": [q[0:3], q[3:6], q[6:9], q[9:12]], "expect_p": [p[0:3], p[3:6], p[6:9], p[9:12]],
+        }
+
+    f = "src/galax/dynamics/_src/experimental/integrate.py"
+    q = numbers(root, f, [175, 176, 178])
+    p = numbers(root, f, [179, 180, 182])
+    g["orbits"]["nfw_integrate_orbit"] = {
+        "cite": f"{f}:157-182 (solver defaults {f}:28-35)",
+        "potential": {"kind": "nfw", "m": 1e12, "l1": 15.0, "l2": 0.0},
+        "solver": {"method": 8, "adaptive": True, "rtol": 1e-7, "atol": 1e-7, "dtmin": 0.3},
+        "y0": [[15.0, 0, 0, 0, 0.225, 0]], "t0": 0.0, "t1": 10.0,
+        "save_ts_linspace": [0.0, 10.0, 100], "rows": [0, 1, 99],
+        "expect_q": [q[0:3], q[3:6], q[6:9]], "expect_p": [p[0:3], p[3:6], p[6:9]], "digits": 8,
+    }
+
+    f = "src/galax/dynamics/_src/legacy/integrator.py"
+    q = numbers(root, f, [92])
+    p = numbers(root, f, [94])
+    g["orbits"]["legacy_integrator_1gyr"] = {
+        "cite": f"{f}:76-95 (defaults {f}:161-168)",
+        "potential": {"kind": "hernquist", "m": 1e12, "l1": 5.0, "l2": 0.0},
+        "solver": {"method": 8, "adaptive": True, "rtol": 1e-7, "atol": 1e-7},
+        "y0": [[10, 0, 0, 0, 200 * KMS, 0]], "t0": 0.0, "t1": 1000.0, "save_ts": [1000.0],
+        "expect_q": [q[0:3]], "expect_p": [p[0:3]], "digits": 3,
+    }
+
+    out = Path(__file__).with_name("reference_goldens.json")
+    out.write_text(json.dumps(g, indent=1) + "\n")
+    print(f"wrote {out}")
+
+
+if __name__ == "__main__":
+    main(Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference"))

@@ -1,0 +1,282 @@
+"""The CPU oracle against the reference's golden vectors and known-answer tests.
+
+These pin the oracle before it is trusted as the checker of the CUDA library:
+every potential / gradient / Hessian golden of the reference's unit tests, the
+Dopri8 single-step doctest, the PID-controlled doctests, and self-consistency
+(order conditions of both tableaux, finite differences of the Hessians, the
+parameter derivatives and the discrete adjoint).
+"""
+
+from __future__ import annotations
+
+import itertools
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests._helpers import golden_cfg, golden_comps, golden_save_ts
+
+
+# ---------------------------------------------------------------- potentials
+@pytest.mark.parametrize("name", ["hernquist", "miyamoto_nagai", "nfw", "plummer", "milky_way"])
+def test_potential_goldens(goldens, name):
+    g = goldens["potentials"][name]
+    c = golden_comps(g["params"])
+    x = np.array([g["x"]])
+    tol = g["tol"]
+    np.testing.assert_allclose(O.potential(c, x)[0], g["potential"], **tol)
+    np.testing.assert_allclose(O.gradient(c, x)[0], g["gradient"], **tol)
+    np.testing.assert_allclose(O.hessian(c, x)[0].ravel(), g["hessian"], **tol)
+    if name != "milky_way":
+        # single components match every printed digit, not just the reference's tolerance
+        np.testing.assert_allclose(O.potential(c, x)[0], g["potential"], rtol=0, atol=5e-9)
+        np.testing.assert_allclose(O.gradient(c, x)[0], g["gradient"], rtol=0, atol=5e-9)
+
+
+def test_gradient_is_finite_at_origin():
+    c = O.milky_way()
+    g = O.gradient(c, np.zeros((1, 3)))
+    assert np.all(np.isfinite(g)) and np.all(g == 0)
+
+
+def _mixed_points(n=64, seed=5):
+    rng = np.random.default_rng(seed)
+    return rng.normal(size=(n, 3)) * np.exp(rng.uniform(np.log(0.05), np.log(60), (n, 1)))
+
+
+def _all_kinds():
+    return O.comps([
+        (O.KEPLER, 3e10, 0, 0, (0.3, -0.2, 0.1)),
+        (O.HERNQUIST, 5e9, 1.0, 0),
+        (O.MIYAMOTO_NAGAI, 6.8e10, 3.0, 0.28),
+        (O.NFW, 5.4e11, 15.62, 0),
+        (O.PLUMMER, 1e8, 0.5, 0, (4.0, 1.0, -2.0)),
+    ])
+
+
+def test_gradient_matches_finite_difference_of_potential():
+    c = _all_kinds()
+    x = _mixed_points()
+    g = O.gradient(c, x)
+    for k in range(3):
+        h = 1e-6 * np.maximum(1.0, np.abs(x[:, k]))
+        e = np.zeros(3); e[k] = 1
+        fd = (O.potential(c, x + h[:, None] * e) - O.potential(c, x - h[:, None] * e)) / (2 * h)
+        np.testing.assert_allclose(g[:, k], fd, rtol=1e-6, atol=1e-9)
+
+
+def test_hessian_matches_finite_difference_of_gradient():
+    c = _all_kinds()
+    x = _mixed_points()
+    H = O.hessian(c, x)
+    for k in range(3):
+        h = 1e-6 * np.maximum(1.0, np.abs(x[:, k]))
+        e = np.zeros(3); e[k] = 1
+        fd = (O.gradient(c, x + h[:, None] * e) - O.gradient(c, x - h[:, None] * e)) / (2 * h[:, None])
+        np.testing.assert_allclose(H[:, :, k], fd, rtol=1e-5, atol=1e-10)
+    np.testing.assert_allclose(H, np.swapaxes(H, 1, 2), rtol=1e-12, atol=1e-18)
+
+
+def test_param_derivatives_match_finite_difference():
+    c = _all_kinds()
+    x = _mixed_points(32)
+    v = np.random.default_rng(1).normal(size=x.shape)
+    d = O.dgrad_dparams(c, x, v)
+    for ci, field in itertools.product(range(len(c)), ("m", "l1", "l2")):
+        if field == "l2" and c[ci]["kind"] != O.MIYAMOTO_NAGAI:
+            continue
+        if field == "l1" and c[ci]["kind"] == O.KEPLER:
+            continue
+        j = {"m": 0, "l1": 1, "l2": 2}[field]
+        p0 = float(c[ci][field])
+        h = 1e-5 * p0
+        one = c[ci:ci + 1]  # difference the component alone (no cancellation against the others)
+        cp, cm = one.copy(), one.copy()
+        cp[0][field] = p0 + h
+        cm[0][field] = p0 - h
+        fd = ((O.gradient(cp, x) - O.gradient(cm, x)) / (2 * h) * v).sum(1)
+        np.testing.assert_allclose(d[:, ci, j], fd, rtol=1e-6, atol=1e-6 * np.abs(fd).max())
+
+
+# ---------------------------------------------------------------- tableaux
+def _trees(n):
+    if n == 1:
+        return [()]
+    out = set()
+
+    def parts(m, mx):
+        if m == 0:
+            yield []
+            return
+        for p in range(min(m, mx), 0, -1):
+            for rest in parts(m - p, p):
+                yield [p] + rest
+
+    for p in parts(n - 1, n - 1):
+        for combo in itertools.product(*[_trees(k) for k in p]):
+            out.add(tuple(sorted(combo)))
+    return sorted(out)
+
+
+def _size(t):
+    return 1 + sum(_size(c) for c in t)
+
+
+def _gamma(t):
+    g = _size(t)
+    for c in t:
+        g *= _gamma(c)
+    return g
+
+
+def _phi(t, A):
+    v = np.ones(A.shape[0], dtype=np.longdouble)
+    for ch in t:
+        v = v * (A @ _phi(ch, A))
+    return v
+
+
+@pytest.mark.parametrize("method,p,phat", [(5, 5, 4), (8, 8, 7)])
+def test_tableau_order_conditions(method, p, phat):
+    """Every rooted-tree condition up to the method's order holds for b, and up
+    to the embedded order for b - e; the next order fails (so the count is exact)."""
+    c, a, b, e = O.tableau(method)
+    A = a.astype(np.longdouble)
+    np.testing.assert_allclose(A.sum(1), c, atol=2e-15)
+    for w, order in ((b, p), (b - e, phat)):
+        w = w.astype(np.longdouble)
+        worst = max(abs(float(w @ _phi(t, A) - 1 / np.longdouble(_gamma(t))))
+                    for n in range(1, order + 1) for t in _trees(n))
+        assert worst < 1e-14
+        nxt = max(abs(float(w @ _phi(t, A) - 1 / np.longdouble(_gamma(t)))) for t in _trees(order + 1))
+        assert nxt > 1e-7
+
+
+def test_dopri5_midpoint_weights():
+    """Shampine's midpoint weights are a 4th-order (or better) quadrature at 1/2."""
+    c, a, b, e = O.tableau(5)
+    w = O.dopri5_cmid()
+    for k in range(4):
+        assert abs(w @ c**k - 0.5 ** (k + 1) / (k + 1)) < 1e-15
+
+
+# ---------------------------------------------------------------- integration KATs
+EXACT = ["dopri8_single_step", "dopri8_pid_lockstep_run", "dopri8_pid_solve_220kms", "dopri8_pid_solve_array",
+         "nfw_integrate_orbit", "legacy_integrator_1gyr"]
+
+
+@pytest.mark.parametrize("name", EXACT)
+def test_integration_kats_exact(goldens, name):
+    """Doctest values reproduced to every printed digit (half a unit in the last
+    place, plus 1e-9 of floating-point slack for the long PID runs)."""
+    g = goldens["orbits"][name]
+    c = golden_comps(g["potential"])
+    cfg = golden_cfg(g["solver"])
+    ts = golden_save_ts(g)
+    saves, status, acc, rej = O.integrate(c, np.array(g["y0"], float), g["t0"], g["t1"], ts, cfg)
+    assert np.all(status == 0)
+    rows = g.get("rows", [-1])
+    if cfg.lockstep:
+        got = saves[-1]  # (n, 6)
+    else:
+        got = np.stack([saves[i][rows] for i in range(len(saves))]).reshape(-1, 6)
+    want = np.concatenate([np.asarray(g["expect_q"]), np.asarray(g["expect_p"])], axis=-1).reshape(-1, 6)
+    tol = 0.5 * 10.0 ** (-g["digits"]) + 1e-9
+    np.testing.assert_allclose(got, want, rtol=0, atol=tol)
+
+
+@pytest.mark.parametrize("name", ["kepler_integrate_field_array", "kepler_integrate_field_quantity"])
+def test_kepler_integrate_field_within_ten_rtol(goldens, name):
+    """integrate_field's Kepler doctest (PID 1e-7, dtmin 0.05).
+
+    The final row is a step endpoint. With the initial-step rule that reproduces
+    every Hernquist doctest digit, it agrees within 20 x rtol (the whole gap comes
+    from the first step: starting at dt0 = dtmin reproduces all printed digits,
+    so diffrax's first step here was <= dtmin). The t=10.1 Myr row lies inside a
+    step, where diffrax's 7th-order Dopri8 interpolant carries ~3e-6 of its own
+    error; the oracle's sub-step is checked against a converged solution."""
+    g = goldens["orbits"][name]
+    c = golden_comps(g["potential"])
+    cfg = golden_cfg(g["solver"])
+    ts = golden_save_ts(g)
+    y0 = np.array(g["y0"], float)
+    saves, status, acc, rej = O.integrate(c, y0, g["t0"], g["t1"], ts, cfg)
+    got = saves[0][g["rows"]]
+    want = np.concatenate([np.asarray(g["expect_q"]), np.asarray(g["expect_p"])], axis=-1)
+    np.testing.assert_allclose(got[0], want[0], atol=1e-12)
+    scale = np.abs(want[-1]).max()
+    assert np.abs(got[-1] - want[-1]).max() <= 20 * 1e-7 * scale
+    first_dtmin = golden_cfg(dict(g["solver"], dt0=0.05))
+    s2, *_ = O.integrate(c, y0, g["t0"], g["t1"], ts, first_dtmin)
+    np.testing.assert_allclose(s2[0][-1], want[-1], rtol=0, atol=0.5e-8 + 1e-9)
+    # interpolated row: oracle within 1e-7 of the converged solution, reference within 5e-6
+    fine, *_ = O.integrate(c, y0, g["t0"], ts[1], np.array([ts[1]]), O.solver_cfg(8, False, dt0=ts[1] / 2000))
+    assert np.abs(got[1] - fine[0][0]).max() < 1e-7
+    assert np.abs(want[1] - fine[0][0]).max() < 5e-6
+
+
+def test_dopri8_substep_save_is_order_eight():
+    """A save inside a step equals the Dopri8 step of the partial length: halving
+    dt shrinks the save error ~2^8."""
+    c = O.milky_way()
+    y0 = np.array([[8.0, 0.5, 0.3, 0.02, 0.21, 0.01]])
+    ts = np.array([37.3])
+    ref, *_ = O.integrate(c, y0, 0.0, 40.0, ts, O.solver_cfg(8, False, dt0=0.05))
+    errs = []
+    for dt in (4.0, 2.0):
+        s, *_ = O.integrate(c, y0, 0.0, 40.0, ts, O.solver_cfg(8, False, dt0=dt))
+        errs.append(np.abs(s[0] - ref[0]).max())
+    assert errs[1] < errs[0] / 100
+
+
+def test_reverse_time_matches_forward():
+    c = O.milky_way()
+    y0 = np.array([[8.0, 0.5, 0.3, 0.02, 0.21, 0.01]])
+    fwd, *_ = O.integrate(c, y0, 0.0, 200.0, np.array([200.0]), O.solver_cfg(8, False, dt0=0.5))
+    back, *_ = O.integrate(c, fwd[0], 200.0, 0.0, np.array([0.0]), O.solver_cfg(8, False, dt0=0.5))
+    np.testing.assert_allclose(back[0][0], y0[0], rtol=1e-10, atol=1e-12)
+
+
+def test_max_steps_status():
+    c = O.milky_way()
+    y0 = np.array([[8.0, 0.0, 0.0, 0.0, 0.2, 0.0]])
+    s, st, acc, rej = O.integrate(c, y0, 0.0, 100.0, np.array([50.0, 100.0]),
+                                  O.solver_cfg(5, True, rtol=1e-8, atol=1e-10, max_steps=5))
+    assert st[0] == 1 and acc[0] + rej[0] == 5
+    assert np.all(np.isnan(s[0][-1]))
+
+
+# ---------------------------------------------------------------- adjoint
+def test_adjoint_matches_central_differences():
+    c = O.milky_way()
+    rng = np.random.default_rng(7)
+    y0 = np.array([[8.0, 0.5, 0.3, 0.02, 0.21, 0.01], [12.0, -3.0, 1.0, 0.1, 0.15, -0.02]])
+    cfg = O.solver_cfg(8, False, dt0=1.0)
+    yT, *_ = O.integrate(c, y0, 0.0, 50.0, np.array([50.0]), cfg)
+    target = np.stack([s[0] for s in yT]) + rng.normal(0, 0.1, (2, 6))
+    yT2, gy, gp, L = O.adjoint_fixed(c, y0, 0.0, 50.0, target, cfg)
+
+    def loss(cc, yy):
+        s, *_ = O.integrate(cc, yy, 0.0, 50.0, np.array([50.0]), cfg)
+        return float(sum(((s[i][0] - target[i]) ** 2).sum() for i in range(len(s))))
+
+    assert abs(loss(c, y0) - L) < 1e-12 * max(1, L)
+    for i, j in itertools.product(range(2), range(6)):
+        h = 1e-6
+        yp, ym = y0.copy(), y0.copy()
+        yp[i, j] += h
+        ym[i, j] -= h
+        fd = (loss(c, yp) - loss(c, ym)) / (2 * h)
+        assert abs(gy[i, j] - fd) <= 1e-5 * max(1.0, abs(fd))
+    for ci in range(len(c)):
+        for field, j in (("m", 0), ("l1", 1), ("l2", 2)):
+            if field == "l2" and c[ci]["kind"] != O.MIYAMOTO_NAGAI:
+                continue
+            p0 = float(c[ci][field])
+            h = 1e-6 * p0
+            cp, cm = c.copy(), c.copy()
+            cp[ci][field] = p0 + h
+            cm[ci][field] = p0 - h
+            fd = (loss(cp, y0) - loss(cm, y0)) / (2 * h)
+            assert abs(gp[ci, j] - fd) <= 1e-5 * max(abs(fd), 1e-12 / p0), (ci, field, gp[ci, j], fd)

@@ -1,0 +1,390 @@
+"""Benchmark of the orbit-integration hot path (one JSON line on rank 0).
+
+Default workload (the headline configuration): MilkyWayPotential, 262,144
+orbits, radii log-uniform 0.5-100 kpc, Dopri5 with the PID controller (rtol 1e-8,
+atol 1e-10, max_steps 2**16), per-orbit durations log-uniform 0.1-5 Gyr and
+10-1000 saves per orbit, all in one persistent launch. One "step" is one pass
+of the integrator over the whole batch. Metric: orbit-steps/s = accepted RK
+steps (counted by the kernel) per second.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload uneven|plain|grad] [--orbits N]
+
+--impl reference times the reference path's CPU implementation on the host
+cores: galax itself needs JAX, which is absent, so this is the C++ FP64
+restatement of the same arithmetic (oracle/), with every host thread.
+Multi-GPU: orbits shard across ranks with no collective (weak scaling).
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "uneven": "batched uneven plain: MilkyWayPotential, Dopri5 PID rtol=1e-8 atol=1e-10 max_steps=2**16, "
+              "radii log-uniform 0.5-100 kpc, durations log-uniform 0.1-5 Gyr, 10-1000 saves/orbit, "
+              "one persistent launch",
+    "plain": "plain small: MilkyWayPotential, Dopri8 fixed dt=1 Myr over 1 Gyr, 100 uniform saves",
+    "grad": "differentiation: MilkyWayPotential, Dopri8 fixed dt=0.5 Myr over 2 Gyr, squared-distance loss, "
+            "adjoint with checkpoints every 256 steps",
+}
+DEFAULT_ORBITS = {"uneven": 262_144, "plain": 1024, "grad": 65_536}
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:  # noqa: BLE001
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:  # noqa: BLE001
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def fp64_peak() -> dict:
+    """Measured FP64 FMA throughput of this GPU (MEASURED_PEAKS.json has no FP64 entry)."""
+    import ctypes as C
+
+    import torch
+
+    from galax_gb300 import _lib
+
+    L = _lib.load()
+    ms, fl = C.c_double(), C.c_double()
+    best = 0.0
+    for _ in range(3):
+        _lib.check(L.gal_fp64_peak_probe(20000, C.byref(ms), C.byref(fl), torch.cuda.current_stream().cuda_stream),
+                   "gal_fp64_peak_probe")
+        best = max(best, fl.value / (ms.value * 1e-3))
+    return {"tflops": best / 1e12, "how": "dependent-chain DFMA probe, 8 chains/thread, full-device grid, best of 3"}
+
+
+def measured_peaks() -> dict:
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except Exception:  # noqa: BLE001
+        return {}
+
+
+def flops_per_step(method: int) -> int:
+    from galax_gb300.flops import STEP_FLOPS_MW
+
+    return STEP_FLOPS_MW[method]
+
+
+# ------------------------------------------------------------------ workloads
+def make_uneven(n: int, seed: int):
+    import galax_gb300 as gx
+    from galax_gb300 import workloads as W
+
+    mw = gx.MilkyWayPotential()
+    return mw, W.uneven_ics(lambda x: mw.gradient(x), n, seed=seed)
+
+
+def run_ours(args) -> dict | None:
+    import torch
+
+    import galax_gb300 as gx
+    from galax_gb300 import _lib
+    from galax_gb300.dynamics import Workspace, integrate
+
+    rank, local_rank, world = dist_env()
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    n = args.orbits or DEFAULT_ORBITS[args.workload]
+    if args.workload != "uneven":
+        raise SystemExit(f"workload {args.workload} is reported by bench_configs.py")
+    mw, b = make_uneven(n, seed=1 + rank)  # weak scaling: every rank its own shard
+    cfg = gx.Integrator(solver=gx.Dopri5(), stepsize_controller=gx.PIDController(rtol=1e-8, atol=1e-10),
+                        max_steps=2**16).config()
+    dev = "cuda"
+    y0 = torch.as_tensor(b.y0, device=dev).t().contiguous()
+    t0 = torch.as_tensor(b.t0, device=dev)
+    t1 = torch.as_tensor(b.t1, device=dev)
+    offs = torch.as_tensor(b.save_offsets, device=dev)
+    sts = torch.as_tensor(b.save_ts, device=dev)
+    total_saves = int(b.save_offsets[-1])
+    # longest-first order: cost estimate = duration x local orbital frequency
+    r = torch.linalg.vector_norm(y0[:3], dim=0)
+    a = torch.linalg.vector_norm(torch.as_tensor(mw.gradient(y0[:3].t())), dim=1)
+    order = torch.argsort(t1 * torch.sqrt(a / r), descending=True).to(torch.int32).contiguous()
+    ws = Workspace()
+    stream = torch.cuda.current_stream()
+
+    def step():
+        return integrate(mw, y0, t0, t1, sts, cfg, save_offsets=offs, order=order, soa=True, workspace=ws)
+
+    for _ in range(args.warmup):
+        out, status, steps = step()
+    torch.cuda.synchronize()
+    accepted = int(steps.sum())
+    n_bad = int((status != 0).sum())
+    del out
+    clocks = ClockSampler(local_rank)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    launches = 0
+    for _ in range(args.steps):
+        out, status, steps = step()
+        launches += 1
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_total = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    ms = ms_total / args.steps
+    if dist:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t)
+        acc_t = torch.tensor([accepted], device=dev, dtype=torch.float64)
+        dist.all_reduce(acc_t)
+        accepted_all = float(acc_t)
+    else:
+        accepted_all = accepted
+    value = accepted_all / (ms * 1e-3)
+
+    # ---- end to end through the public call with pinned host buffers
+    h_y0 = torch.as_tensor(b.y0.T.copy()).pin_memory()
+    h_t0 = torch.as_tensor(b.t0).pin_memory()
+    h_t1 = torch.as_tensor(b.t1).pin_memory()
+    h_offs = torch.as_tensor(b.save_offsets).pin_memory()
+    h_ts = torch.as_tensor(b.save_ts).pin_memory()
+    h_out = torch.empty((6, total_saves), dtype=torch.float64).pin_memory()
+    h_status = torch.empty(n, dtype=torch.int32).pin_memory()
+    h2d = sum(x.numel() * x.element_size() for x in (h_y0, h_t0, h_t1, h_offs, h_ts))
+    d2h = h_out.numel() * 8 + h_status.numel() * 4
+
+    def e2e_step():
+        dy0 = h_y0.to(dev, non_blocking=True)
+        dt0 = h_t0.to(dev, non_blocking=True)
+        dt1 = h_t1.to(dev, non_blocking=True)
+        doffs = h_offs.to(dev, non_blocking=True)
+        dts = h_ts.to(dev, non_blocking=True)
+        o, s, _ = integrate(mw, dy0, dt0, dt1, dts, cfg, save_offsets=doffs, order=order, soa=True, workspace=ws)
+        h_out.copy_(o, non_blocking=True)
+        h_status.copy_(s, non_blocking=True)
+
+    e2e_step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    t_start = time.perf_counter()
+    e2e_steps = max(1, min(args.steps, 3))
+    for _ in range(e2e_steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_ms = (time.perf_counter() - t_start) * 1e3 / e2e_steps
+    if dist:
+        t = torch.tensor([e2e_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t)
+    e2e_value = accepted_all / (e2e_ms * 1e-3)
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return None
+    peak = fp64_peak()
+    f_step = flops_per_step(5)
+    achieved = accepted * f_step / (ms * 1e-3) / 1e12
+    traffic = traffic_from_profiles()
+    save_bytes = total_saves * 6 * 8
+    line = {
+        "metric": "orbit-steps/s", "value": value, "unit": "orbit-steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded numpy, galactic units)",
+        "config": {"workload": WORKLOADS["uneven"], "orbits_per_gpu": n, "accepted_steps_per_gpu": accepted,
+                   "orbits_not_finished": n_bad, "saves_per_gpu": total_saves,
+                   "save_bytes_per_step": save_bytes,
+                   "l2": "inputs larger than L2: 1.0 GB save-time grid read and 6.3 GB of saves written per step",
+                   "parallelism": f"orbit shards x{world}, no collective"},
+        "e2e": {"value": e2e_value, "unit": "orbit-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": e2e_ms, "path": "pinned host -> gal_integrate -> pinned host"},
+        "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak["tflops"], "unit": "TFLOP/s",
+                     "frac": achieved / peak["tflops"], "traffic": traffic,
+                     "flops_per_accepted_step": f_step,
+                     "note": "FP64 pipe bound; achieved counts accepted steps only (rejected attempts, saves and "
+                             "initial-step selection are extra work, so frac is a lower bound); peak measured live "
+                             "(" + peak["how"] + ")",
+                     "hbm": {"achieved_gbs": save_bytes / (ms * 1e-3) / 1e9,
+                             "peak_gbs": measured_peaks().get("hbm_gbs"),
+                             "note": "save writes only; of measured"}},
+        "clocks": clk,
+        "gpu_launches": launches,
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(b, target_s=args.cpu_seconds)
+    if dist:
+        dist.destroy_process_group()
+    return line
+
+
+def traffic_from_profiles():
+    """DRAM bytes per launch of the integrate kernel, from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "integrate_dopri5_uneven.md")
+    try:
+        for ln in open(p):
+            if ln.startswith("traffic_bytes_per_full_launch:"):
+                return float(ln.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+def cpu_baseline(b, target_s: float = 15.0) -> dict:
+    """The oracle (C++ FP64, OpenMP over orbits, all host threads) on a bounded
+    sample of the same orbits; value = accepted steps per second."""
+    from oracle import oracle as O
+
+    cores = os.cpu_count() or 1
+    cfg = O.solver_cfg(5, True, rtol=1e-8, atol=1e-10, max_steps=2**16)
+    comps = O.milky_way()
+    rng = np.random.default_rng(99)
+    idx_all = rng.permutation(len(b.t1))
+
+    def run(idx):
+        grids = [b.save_ts[b.save_offsets[i]:b.save_offsets[i + 1]] for i in idx]
+        t = time.perf_counter()
+        _, st, acc, _ = O.integrate(comps, b.y0[idx], b.t0[idx], b.t1[idx], grids, cfg, nthreads=cores)
+        return time.perf_counter() - t, int(acc.sum())
+
+    m = max(64, 4 * cores)
+    dt, acc = run(idx_all[:m])
+    while dt < 1.0 and m < len(idx_all):
+        m = min(len(idx_all), m * 4)
+        dt, acc = run(idx_all[:m])
+    m2 = int(min(len(idx_all), max(m, m * target_s / max(dt, 1e-3))))
+    if m2 > m:
+        dt, acc = run(idx_all[:m2])
+        m = m2
+    return {"value": acc / dt, "unit": "orbit-steps/s", "cores": cores, "kind": "port",
+            "sample": f"{m} randomly chosen orbits of the same workload ({acc} accepted steps, {dt:.1f} s wall)"}
+
+
+def run_reference(args) -> dict | None:
+    """CPU implementation of the path on the host cores (the oracle port; galax needs JAX, absent here)."""
+    rank, _, world = dist_env()
+    if rank != 0:
+        return None
+    from oracle import oracle as O
+    from galax_gb300 import workloads as W
+
+    n = args.orbits or DEFAULT_ORBITS["uneven"]
+    b = W.uneven_ics(lambda x: O.gradient(O.milky_way(), x), n, seed=1)
+    cores = os.cpu_count() or 1
+    cfg = O.solver_cfg(5, True, rtol=1e-8, atol=1e-10, max_steps=2**16)
+    comps = O.milky_way()
+    rng = np.random.default_rng(99)
+    per_step = args.ref_orbits
+    times, accs = [], []
+    for i in range(args.warmup + args.steps):
+        idx = rng.choice(n, per_step, replace=False)
+        grids = [b.save_ts[b.save_offsets[j]:b.save_offsets[j + 1]] for j in idx]
+        t = time.perf_counter()
+        _, st, acc, _ = O.integrate(comps, b.y0[idx], b.t0[idx], b.t1[idx], grids, cfg, nthreads=cores)
+        dt = time.perf_counter() - t
+        if i >= args.warmup:
+            times.append(dt)
+            accs.append(int(acc.sum()))
+    value = sum(accs) / sum(times)
+    sample = f"{per_step} random orbits of the workload per step, {cores} threads"
+    return {"impl": "reference", "metric": "orbit-steps/s", "value": value, "unit": "orbit-steps/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded numpy, galactic units)",
+            "config": {"workload": WORKLOADS["uneven"], "orbits_per_step": per_step},
+            "cpu_baseline": {"value": value, "unit": "orbit-steps/s", "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "orbit-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "galax (JAX) is not installed on this machine; this is the C++ FP64 restatement of its "
+                    "orbit arithmetic (oracle/) on every host thread"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--workload", choices=tuple(WORKLOADS), default="uneven")
+    ap.add_argument("--orbits", type=int, default=0)
+    ap.add_argument("--ref-orbits", type=int, default=8192)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        print("note: fewer than 3 warm-up steps", file=sys.stderr)
+    line = run_reference(args) if args.impl == "reference" else run_ours(args)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,39 @@
+"""galax_gb300: the orbit-integration hot path of GalacticDynamics/galax on GB300.
+
+Potentials (``galax_gb300.potential``) and orbit integration
+(``galax_gb300.dynamics``) with galax's interface, run by a CUDA library for
+sm_103a through the C ABI in ``include/galax_gb300.h``. There is no CPU path:
+without the built library or a CUDA device, calls raise.
+"""
+
+from . import dynamics, potential
+from ._lib import GalaxGB300Error
+from .dynamics import (
+    ConstantStepSize,
+    Dopri5,
+    Dopri8,
+    Integrator,
+    Orbit,
+    OrbitSolver,
+    PhaseSpaceCoordinate,
+    PIDController,
+    evaluate_orbit,
+    integrate_orbit,
+)
+from .potential import (
+    CompositePotential,
+    HernquistPotential,
+    KeplerPotential,
+    MilkyWayPotential,
+    MiyamotoNagaiPotential,
+    NFWPotential,
+    PlummerPotential,
+    TranslatedPotential,
+)
+
+__all__ = [
+    "GalaxGB300Error", "dynamics", "potential", "ConstantStepSize", "Dopri5", "Dopri8", "Integrator", "Orbit",
+    "OrbitSolver", "PhaseSpaceCoordinate", "PIDController", "evaluate_orbit", "integrate_orbit",
+    "CompositePotential", "HernquistPotential", "KeplerPotential", "MilkyWayPotential", "MiyamotoNagaiPotential",
+    "NFWPotential", "PlummerPotential", "TranslatedPotential",
+]

@@ -1,0 +1,453 @@
+// C ABI of the galax_gb300 library (declared in include/galax_gb300.h):
+// potential handles, batched potential / gradient / Hessian evaluation, the
+// orbit-integration entry point and small utilities.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/galax_gb300.h"
+#include "handle.h"
+#include "launch.h"
+
+namespace gal {
+
+thread_local std::string g_last_error;
+static LaunchShape g_shape[2][2] = {{{0, 0}, {0, 0}}, {{0, 0}, {0, 0}}};  // [method 5/8][adaptive]
+
+gal_status fail(gal_status st, const std::string& msg) {
+  g_last_error = msg;
+  return st;
+}
+
+gal_status cuda_fail(cudaError_t e, const char* where) {
+  return fail(GAL_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+int device_sm_count() {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return sms > 0 ? sms : 1;
+}
+
+static DevComp fold(const gal_component& c, double G) {
+  DevComp d{};
+  d.kind = c.kind;
+  d.centered = (c.origin[0] == 0.0 && c.origin[1] == 0.0 && c.origin[2] == 0.0) ? 1 : 0;
+  d.Gm = G * c.m;
+  d.l1 = c.l1;
+  d.l2 = c.l2;
+  d.l2sq = (c.kind == PLUMMER) ? c.l1 * c.l1 : c.l2 * c.l2;
+  d.inv_l1 = (c.kind == NFW) ? 1.0 / c.l1 : 0.0;
+  d.inv_m = (c.m != 0.0) ? 1.0 / c.m : 0.0;
+  d.ox = c.origin[0];
+  d.oy = c.origin[1];
+  d.oz = c.origin[2];
+  return d;
+}
+
+static bool milky_way_shape(const gal_component* c, int n) {
+  if (n != 4) return false;
+  const int32_t want[4] = {MIYAMOTO_NAGAI, NFW, HERNQUIST, HERNQUIST};
+  for (int i = 0; i < 4; ++i) {
+    if (c[i].kind != want[i]) return false;
+    if (c[i].origin[0] != 0.0 || c[i].origin[1] != 0.0 || c[i].origin[2] != 0.0) return false;
+  }
+  return true;
+}
+
+static MWParams mw_params(const gal_component* c, double G) {
+  MWParams p{};
+  p.Gm_d = G * c[0].m;
+  p.a_d = c[0].l1;
+  p.b2_d = c[0].l2 * c[0].l2;
+  p.Gm_h = G * c[1].m;
+  p.rs_h = c[1].l1;
+  p.irs_h = 1.0 / c[1].l1;
+  p.Gm_b = G * c[2].m;
+  p.rs_b = c[2].l1;
+  p.Gm_n = G * c[3].m;
+  p.rs_n = c[3].l1;
+  return p;
+}
+
+static gal_status validate_components(const gal_component* comps, int32_t n) {
+  if (!comps || n < 1) return fail(GAL_ERR_INVALID_ARGUMENT, "need at least one component");
+  if (n > GAL_MAX_COMPONENTS) return fail(GAL_ERR_TOO_LARGE, "too many components (max GAL_MAX_COMPONENTS)");
+  for (int i = 0; i < n; ++i) {
+    const gal_component& c = comps[i];
+    if (c.kind < GAL_KEPLER || c.kind > GAL_PLUMMER) return fail(GAL_ERR_UNSUPPORTED, "unsupported component kind");
+    if (c.flags != 0) return fail(GAL_ERR_INVALID_ARGUMENT, "component flags must be 0");
+    const double v[6] = {c.m, c.l1, c.l2, c.origin[0], c.origin[1], c.origin[2]};
+    for (double x : v)
+      if (!std::isfinite(x)) return fail(GAL_ERR_INVALID_ARGUMENT, "non-finite component parameter");
+    if ((c.kind == GAL_HERNQUIST || c.kind == GAL_NFW) && !(c.l1 > 0.0))
+      return fail(GAL_ERR_INVALID_ARGUMENT, "r_s must be > 0");
+    if (c.kind == GAL_MIYAMOTO_NAGAI && (c.l1 < 0.0 || !(c.l2 > 0.0)))
+      return fail(GAL_ERR_INVALID_ARGUMENT, "Miyamoto-Nagai needs a >= 0 and b > 0");
+    if (c.kind == GAL_PLUMMER && c.l1 < 0.0) return fail(GAL_ERR_INVALID_ARGUMENT, "Plummer r_s must be >= 0");
+  }
+  return GAL_OK;
+}
+
+// ----------------------------------------------------------------- eval kernels
+template <class Pot>
+__global__ void k_eval_gradient(Pot pot, const double* __restrict__ x, int64_t n, double* __restrict__ out,
+                                double sign) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double gx, gy, gz;
+    pot.grad(x[i], x[n + i], x[2 * n + i], gx, gy, gz);
+    out[i] = sign * gx;
+    out[n + i] = sign * gy;
+    out[2 * n + i] = sign * gz;
+  }
+}
+
+__global__ void k_eval_gradient_table(const DevComp* comps, int ncomp, const double* __restrict__ x, int64_t n,
+                                      double* __restrict__ out, double sign) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  DevComp* s = reinterpret_cast<DevComp*>(smem_raw);
+  for (int i = threadIdx.x; i < ncomp; i += blockDim.x) s[i] = comps[i];
+  __syncthreads();
+  const TablePot pot{s, ncomp};
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double gx, gy, gz;
+    pot.grad(x[i], x[n + i], x[2 * n + i], gx, gy, gz);
+    out[i] = sign * gx;
+    out[n + i] = sign * gy;
+    out[2 * n + i] = sign * gz;
+  }
+}
+
+__global__ void k_eval_phi(const DevComp* comps, int ncomp, const double* __restrict__ x, int64_t n,
+                           double* __restrict__ out) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  DevComp* s = reinterpret_cast<DevComp*>(smem_raw);
+  for (int i = threadIdx.x; i < ncomp; i += blockDim.x) s[i] = comps[i];
+  __syncthreads();
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double phi = 0.0;
+    for (int c = 0; c < ncomp; ++c) phi += comp_phi(s[c], x[i], x[n + i], x[2 * n + i]);
+    out[i] = phi;
+  }
+}
+
+__global__ void k_eval_hessian(const DevComp* comps, int ncomp, const double* __restrict__ x, int64_t n,
+                               double* __restrict__ out) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  DevComp* s = reinterpret_cast<DevComp*>(smem_raw);
+  for (int i = threadIdx.x; i < ncomp; i += blockDim.x) s[i] = comps[i];
+  __syncthreads();
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double H[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int c = 0; c < ncomp; ++c) comp_hessian(s[c], x[i], x[n + i], x[2 * n + i], H);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) out[k * n + i] = H[k];
+  }
+}
+
+__global__ void k_fp64_probe(int64_t iters, double seed, double* sink) {
+  double a0 = seed + threadIdx.x, a1 = a0 + 1, a2 = a0 + 2, a3 = a0 + 3, a4 = a0 + 4, a5 = a0 + 5, a6 = a0 + 6,
+         a7 = a0 + 7;
+  const double m = 0.999999999, c = 1e-9;
+  for (int64_t i = 0; i < iters; ++i) {
+    a0 = fma(a0, m, c); a1 = fma(a1, m, c); a2 = fma(a2, m, c); a3 = fma(a3, m, c);
+    a4 = fma(a4, m, c); a5 = fma(a5, m, c); a6 = fma(a6, m, c); a7 = fma(a7, m, c);
+  }
+  const double s = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+  if (s == 12345.678) sink[threadIdx.x] = s;  // keep the chain alive
+}
+
+gal_status validate_cfg(const gal_solver_config* c) {
+  if (!c) return fail(GAL_ERR_INVALID_ARGUMENT, "config is NULL");
+  if (c->method != 5 && c->method != 8) return fail(GAL_ERR_UNSUPPORTED, "method must be 5 (Dopri5) or 8 (Dopri8)");
+  if (c->reserved != 0) return fail(GAL_ERR_INVALID_ARGUMENT, "reserved must be 0");
+  if (c->max_steps < 1) return fail(GAL_ERR_INVALID_ARGUMENT, "max_steps must be >= 1");
+  if (!c->adaptive && !(c->dt0 > 0.0)) return fail(GAL_ERR_INVALID_ARGUMENT, "constant step needs dt0 > 0");
+  if (c->adaptive) {
+    if (!(c->rtol >= 0.0) || !(c->atol >= 0.0) || (c->rtol == 0.0 && c->atol == 0.0))
+      return fail(GAL_ERR_INVALID_ARGUMENT, "rtol/atol must be >= 0 and not both 0");
+    if (!(c->safety > 0.0) || !(c->factormin > 0.0) || !(c->factormax >= 1.0))
+      return fail(GAL_ERR_INVALID_ARGUMENT, "bad safety/factormin/factormax");
+  }
+  return GAL_OK;
+}
+
+static void grid_for(int64_t n, int block, unsigned* grid) {
+  int64_t g = (n + block - 1) / block;
+  const int64_t cap = (int64_t)device_sm_count() * 16;
+  if (g > cap) g = cap;
+  if (g < 1) g = 1;
+  *grid = (unsigned)g;
+}
+
+}  // namespace gal
+
+using namespace gal;
+
+
+extern "C" {
+
+int32_t gal_abi_version(void) { return 1; }
+
+const char* gal_last_error(void) { return g_last_error.c_str(); }
+
+const char* gal_status_string(int32_t st) {
+  switch (st) {
+    case GAL_OK: return "ok";
+    case GAL_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case GAL_ERR_UNSUPPORTED: return "unsupported";
+    case GAL_ERR_CUDA: return "CUDA error";
+    case GAL_ERR_WORKSPACE: return "workspace too small";
+    case GAL_ERR_TOO_LARGE: return "size beyond the supported maximum";
+    default: return "unknown status";
+  }
+}
+
+gal_status gal_potential_create(const gal_component* comps, int32_t n, double G, gal_potential** out) {
+  if (!out) return fail(GAL_ERR_INVALID_ARGUMENT, "out is NULL");
+  *out = nullptr;
+  gal_status st = validate_components(comps, n);
+  if (st != GAL_OK) return st;
+  if (!(G > 0.0) || !std::isfinite(G)) return fail(GAL_ERR_INVALID_ARGUMENT, "G must be finite and > 0");
+  gal_potential* p = new gal_potential();
+  p->comps.assign(comps, comps + n);
+  p->G = G;
+  p->n = n;
+  p->is_mw = milky_way_shape(comps, n);
+  p->mw = p->is_mw ? mw_params(comps, G) : MWParams{};
+  std::vector<DevComp> h(n);
+  for (int i = 0; i < n; ++i) h[i] = fold(comps[i], G);
+  cudaError_t e = cudaMalloc(&p->d_comps, sizeof(DevComp) * n);
+  if (e != cudaSuccess) {
+    delete p;
+    return cuda_fail(e, "cudaMalloc(component table)");
+  }
+  e = cudaMemcpy(p->d_comps, h.data(), sizeof(DevComp) * n, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaFree(p->d_comps);
+    delete p;
+    return cuda_fail(e, "cudaMemcpy(component table)");
+  }
+  *out = p;
+  return GAL_OK;
+}
+
+gal_status gal_potential_destroy(gal_potential* p) {
+  if (!p) return GAL_OK;
+  cudaError_t e = cudaFree(p->d_comps);
+  delete p;
+  return e == cudaSuccess ? GAL_OK : cuda_fail(e, "cudaFree(component table)");
+}
+
+gal_status gal_potential_update(gal_potential* p, const gal_component* comps, int32_t n, gal_stream_t stream) {
+  if (!p) return fail(GAL_ERR_INVALID_ARGUMENT, "potential is NULL");
+  if (n != p->n) return fail(GAL_ERR_INVALID_ARGUMENT, "component count differs from the handle's");
+  gal_status st = validate_components(comps, n);
+  if (st != GAL_OK) return st;
+  for (int i = 0; i < n; ++i)
+    if (comps[i].kind != p->comps[i].kind) return fail(GAL_ERR_INVALID_ARGUMENT, "component kinds differ");
+  std::vector<DevComp> h(n);
+  for (int i = 0; i < n; ++i) h[i] = fold(comps[i], p->G);
+  // pageable source: the call returns once the bytes are staged, so h may go out of scope
+  cudaError_t e = cudaMemcpyAsync(p->d_comps, h.data(), sizeof(DevComp) * n, cudaMemcpyHostToDevice,
+                                  (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(component table)");
+  e = cudaStreamSynchronize((cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
+  p->comps.assign(comps, comps + n);
+  p->is_mw = milky_way_shape(comps, n);
+  p->mw = p->is_mw ? mw_params(comps, p->G) : MWParams{};
+  return GAL_OK;
+}
+
+int32_t gal_potential_num_components(const gal_potential* p) { return p ? p->n : 0; }
+int32_t gal_potential_is_milky_way(const gal_potential* p) { return p && p->is_mw ? 1 : 0; }
+
+static gal_status eval_grad_common(const gal_potential* p, const double* x, int64_t n, double* out, double sign,
+                                   gal_stream_t stream) {
+  if (!p || (!x && n) || (!out && n) || n < 0) return fail(GAL_ERR_INVALID_ARGUMENT, "bad pointer or size");
+  if (n == 0) return GAL_OK;
+  const int block = 256;
+  unsigned grid;
+  grid_for(n, block, &grid);
+  if (p->is_mw) {
+    k_eval_gradient<MWPot><<<grid, block, 0, (cudaStream_t)stream>>>(MWPot{p->mw}, x, n, out, sign);
+  } else {
+    const size_t smem = sizeof(DevComp) * p->n;
+    if (smem > 48 * 1024)
+      cudaFuncSetAttribute(k_eval_gradient_table, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_eval_gradient_table<<<grid, block, smem, (cudaStream_t)stream>>>(p->d_comps, p->n, x, n, out, sign);
+  }
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? GAL_OK : cuda_fail(e, "gradient kernel launch");
+}
+
+gal_status gal_eval_gradient(const gal_potential* p, const double* x, double t, int64_t n, double* out,
+                             gal_stream_t stream) {
+  (void)t;
+  return eval_grad_common(p, x, n, out, 1.0, stream);
+}
+
+gal_status gal_eval_acceleration(const gal_potential* p, const double* x, double t, int64_t n, double* out,
+                                 gal_stream_t stream) {
+  (void)t;
+  return eval_grad_common(p, x, n, out, -1.0, stream);
+}
+
+gal_status gal_eval_potential(const gal_potential* p, const double* x, double t, int64_t n, double* phi,
+                              gal_stream_t stream) {
+  (void)t;
+  if (!p || (!x && n) || (!phi && n) || n < 0) return fail(GAL_ERR_INVALID_ARGUMENT, "bad pointer or size");
+  if (n == 0) return GAL_OK;
+  const int block = 256;
+  unsigned grid;
+  grid_for(n, block, &grid);
+  const size_t smem = sizeof(DevComp) * p->n;
+  if (smem > 48 * 1024) cudaFuncSetAttribute(k_eval_phi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_eval_phi<<<grid, block, smem, (cudaStream_t)stream>>>(p->d_comps, p->n, x, n, phi);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? GAL_OK : cuda_fail(e, "potential kernel launch");
+}
+
+gal_status gal_eval_hessian(const gal_potential* p, const double* x, double t, int64_t n, double* out,
+                            gal_stream_t stream) {
+  (void)t;
+  if (!p || (!x && n) || (!out && n) || n < 0) return fail(GAL_ERR_INVALID_ARGUMENT, "bad pointer or size");
+  if (n == 0) return GAL_OK;
+  const int block = 128;
+  unsigned grid;
+  grid_for(n, block, &grid);
+  const size_t smem = sizeof(DevComp) * p->n;
+  if (smem > 48 * 1024)
+    cudaFuncSetAttribute(k_eval_hessian, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_eval_hessian<<<grid, block, smem, (cudaStream_t)stream>>>(p->d_comps, p->n, x, n, out);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? GAL_OK : cuda_fail(e, "hessian kernel launch");
+}
+
+gal_status gal_integrate_workspace_size(const gal_solver_config* cfg, int64_t n, size_t* bytes) {
+  (void)cfg;
+  (void)n;
+  if (!bytes) return fail(GAL_ERR_INVALID_ARGUMENT, "bytes is NULL");
+  *bytes = 256;  // one 8-byte work-queue counter, padded
+  return GAL_OK;
+}
+
+gal_status gal_set_launch(int32_t method, int32_t adaptive, int32_t block_threads, int32_t blocks_per_sm) {
+  if ((method != 5 && method != 8) || block_threads < 0 || block_threads > 256 || (block_threads % 32) ||
+      blocks_per_sm < 0)
+    return fail(GAL_ERR_INVALID_ARGUMENT, "bad launch shape");
+  g_shape[method == 8][adaptive ? 1 : 0] = LaunchShape{block_threads, blocks_per_sm};
+  return GAL_OK;
+}
+
+gal_status gal_integrate(const gal_potential* p, const gal_solver_config* cfg, const double* y0, const double* t0,
+                         const double* t1, const int64_t* save_offsets, const double* save_ts, int64_t n_saves,
+                         double* out, int32_t* status, int64_t* steps, const int32_t* order, int64_t n,
+                         void* workspace, size_t workspace_bytes, gal_stream_t stream) {
+  if (!p) return fail(GAL_ERR_INVALID_ARGUMENT, "potential is NULL");
+  gal_status st = validate_cfg(cfg);
+  if (st != GAL_OK) return st;
+  if (n < 0) return fail(GAL_ERR_INVALID_ARGUMENT, "n < 0");
+  if (n == 0) return GAL_OK;
+  if (n > (int64_t)2147483647) return fail(GAL_ERR_TOO_LARGE, "at most 2^31-1 orbits per call");
+  if (!y0 || !t0 || !t1) return fail(GAL_ERR_INVALID_ARGUMENT, "y0/t0/t1 NULL");
+  if (n_saves < 0) return fail(GAL_ERR_INVALID_ARGUMENT, "n_saves < 0");
+  if ((save_offsets || n_saves > 0) && (!save_ts || !out)) return fail(GAL_ERR_INVALID_ARGUMENT, "saves need save_ts and out");
+  size_t need = 0;
+  gal_integrate_workspace_size(cfg, n, &need);
+  if (!workspace || workspace_bytes < need) return fail(GAL_ERR_WORKSPACE, "workspace too small");
+  // CSR saves: n_saves is the total count (save_offsets[n]); shared grid: saves per orbit
+  const int64_t total = save_offsets ? n_saves : n_saves * n;
+  IntegrateArgs a{};
+  a.adaptive = cfg->adaptive;
+  a.force_dtmin = cfg->force_dtmin;
+  a.max_steps = cfg->max_steps;
+  a.dt0 = cfg->dt0;
+  a.rtol = cfg->rtol;
+  a.atol = cfg->atol;
+  a.dtmin = cfg->dtmin;
+  a.dtmax = cfg->dtmax;
+  const double morder = cfg->method == 8 ? 8.0 : 5.0;
+  a.c1 = (cfg->icoeff + cfg->pcoeff + cfg->dcoeff) / morder;
+  a.c2 = -(cfg->pcoeff + 2.0 * cfg->dcoeff) / morder;
+  a.c3 = cfg->dcoeff / morder;
+  a.safety = cfg->safety;
+  a.factormin = cfg->factormin;
+  a.factormax = cfg->factormax;
+  a.y0 = y0;
+  a.t0 = t0;
+  a.t1 = t1;
+  a.save_offsets = save_offsets;
+  a.save_ts = save_ts;
+  a.n_saves = n_saves;
+  a.out = out;
+  a.out_stride = total;
+  a.status = status;
+  a.steps = steps;
+  a.order = order;
+  a.n = n;
+  a.queue = reinterpret_cast<unsigned long long*>(workspace);
+  cudaError_t e = cudaMemsetAsync(workspace, 0, sizeof(unsigned long long), (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "clearing the work queue");
+  const LaunchShape shape = g_shape[cfg->method == 8][cfg->adaptive ? 1 : 0];
+  if (cfg->method == 8)
+    e = launch_integrate_dopri8(a, p->is_mw, p->mw, p->d_comps, p->n, shape, (cudaStream_t)stream);
+  else
+    e = launch_integrate_dopri5(a, p->is_mw, p->mw, p->d_comps, p->n, shape, (cudaStream_t)stream);
+  return e == cudaSuccess ? GAL_OK : cuda_fail(e, "integrate kernel launch");
+}
+
+int32_t gal_tableau(int32_t method, double* c, double* a, double* b, double* e) {
+  if (method != 5 && method != 8) return 0;
+  for (int i = 0; i < 13; ++i) {
+    c[i] = b[i] = e[i] = 0.0;
+    for (int j = 0; j < 13; ++j) a[13 * i + j] = 0.0;
+  }
+  auto copy = [&](auto tb) {
+    using TB = decltype(tb);
+    for (int i = 0; i < TB::S; ++i) {
+      c[i] = TB::C[i];
+      b[i] = TB::B[i];
+      e[i] = TB::E[i];
+      for (int j = 0; j < TB::S; ++j) a[13 * i + j] = TB::A[i][j];
+    }
+    return TB::S;
+  };
+  return method == 5 ? copy(Dopri5{}) : copy(Dopri8{});
+}
+
+gal_status gal_fp64_peak_probe(int64_t iters, double* ms, double* flops, gal_stream_t stream) {
+  if (iters < 1 || !ms || !flops) return fail(GAL_ERR_INVALID_ARGUMENT, "bad probe arguments");
+  const int block = 256;
+  const unsigned grid = (unsigned)device_sm_count() * 8;
+  double* sink = nullptr;
+  cudaError_t e = cudaMalloc(&sink, block * sizeof(double));
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(probe)");
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  k_fp64_probe<<<grid, block, 0, (cudaStream_t)stream>>>(iters / 8 + 1, 1.0, sink);  // warm-up
+  cudaEventRecord(a, (cudaStream_t)stream);
+  k_fp64_probe<<<grid, block, 0, (cudaStream_t)stream>>>(iters, 1.0, sink);
+  cudaEventRecord(b, (cudaStream_t)stream);
+  e = cudaEventSynchronize(b);
+  float t = 0.f;
+  cudaEventElapsedTime(&t, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(sink);
+  if (e != cudaSuccess) return cuda_fail(e, "probe");
+  *ms = t;
+  *flops = 2.0 * 8.0 * (double)iters * (double)grid * (double)block;
+  return GAL_OK;
+}
+
+// The adjoint entry points live in adjoint.cu.
+
+}  // extern "C"

@@ -1,0 +1,216 @@
+// Device-side potentials: value, gradient and Hessian of the closed-form
+// components galax's orbit path uses, and of their sums.
+//
+// Formulas (r = sqrt(x^2 + y^2 + z^2 + DBL_MIN) as galax's r_spherical /
+// safe_sqrt, src/galax/potential/_src/utils.py:45-125):
+//   Kepler          Phi = -G m / r                       builtin/kepler.py
+//   Hernquist       Phi = -G m / (r + r_s)               builtin/hernquist.py:80-82
+//   Miyamoto-Nagai  Phi = -G m / sqrt(R^2 + (sqrt(z^2 + b^2) + a)^2)   builtin/miyamotonagai.py:73-78
+//   NFW             Phi = -G m log1p(r / r_s) / r        builtin/nfw/base.py:326-338
+//   Plummer         Phi = -G m / sqrt(r^2 + b^2)         builtin/plummer.py:122-133
+// galax differentiates these with jax.grad (src/galax/potential/_src/base.py:170-179);
+// here the derivatives are written out analytically and arranged for the FP64
+// pipe: reciprocal square roots instead of sqrt + divide, one shared radius for
+// all centred spherical components, and one reciprocal for the three
+// (r + r_s) factors of the Milky Way model.
+#pragma once
+
+#include <cstdint>
+
+namespace gal {
+
+enum Kind : int32_t { KEPLER = 0, HERNQUIST = 1, MIYAMOTO_NAGAI = 2, NFW = 3, PLUMMER = 4 };
+
+constexpr double TINY = 2.2250738585072014e-308;  // DBL_MIN, galax's safe_sqrt offset
+
+// Component with parameters folded for evaluation (80 bytes).
+struct DevComp {
+  int32_t kind;
+  int32_t centered;  // 1 when origin == 0
+  double Gm;         // G * m
+  double l1;         // a (MN) or r_s
+  double l2;         // b (MN)
+  double l2sq;       // b^2 (MN) or r_s^2 (Plummer)
+  double inv_l1;     // 1 / r_s (NFW)
+  double ox, oy, oz;
+  double inv_m;      // 1 / m (parameter derivatives)
+};
+static_assert(sizeof(DevComp) == 80, "DevComp layout");
+
+// ----------------------------------------------------------- single components
+__device__ __forceinline__ void comp_grad(const DevComp& c, double x, double y, double z, double& gx, double& gy,
+                                          double& gz) {
+  const double dx = x - c.ox, dy = y - c.oy, dz = z - c.oz;
+  if (c.kind == MIYAMOTO_NAGAI) {
+    const double zb2 = fma(dz, dz, c.l2sq);
+    const double izb = rsqrt(zb2);
+    const double zb = zb2 * izb;
+    const double s = zb + c.l1;
+    const double D2 = fma(dx, dx, fma(dy, dy, s * s));
+    const double iD = rsqrt(D2);
+    const double u = c.Gm * (iD * iD) * iD;
+    gx = fma(u, dx, gx);
+    gy = fma(u, dy, gy);
+    gz = fma(u * s * izb, dz, gz);
+    return;
+  }
+  const double r2 = fma(dx, dx, fma(dy, dy, fma(dz, dz, TINY)));
+  const double ir = rsqrt(r2);
+  double f;
+  switch (c.kind) {
+    case KEPLER:
+      f = c.Gm * (ir * ir) * ir;
+      break;
+    case HERNQUIST: {
+      const double d = fma(r2, ir, c.l1);
+      f = c.Gm * ir / (d * d);
+      break;
+    }
+    case NFW: {
+      const double r = r2 * ir;
+      const double L = log1p(r * c.inv_l1);
+      f = c.Gm * (ir * ir) * fma(L, ir, -1.0 / (c.l1 + r));
+      break;
+    }
+    default: {  // PLUMMER
+      const double s2 = r2 + c.l2sq;
+      const double is = rsqrt(s2);
+      f = c.Gm * (is * is) * is;
+      break;
+    }
+  }
+  gx = fma(f, dx, gx);
+  gy = fma(f, dy, gy);
+  gz = fma(f, dz, gz);
+}
+
+__device__ __forceinline__ double comp_phi(const DevComp& c, double x, double y, double z) {
+  const double dx = x - c.ox, dy = y - c.oy, dz = z - c.oz;
+  switch (c.kind) {
+    case MIYAMOTO_NAGAI: {
+      const double zp = sqrt(fma(dz, dz, c.l2sq)) + c.l1;
+      return -c.Gm / sqrt(fma(dx, dx, fma(dy, dy, zp * zp)));
+    }
+    case KEPLER:
+      return -c.Gm / sqrt(fma(dx, dx, fma(dy, dy, fma(dz, dz, TINY))));
+    case HERNQUIST:
+      return -c.Gm / (sqrt(fma(dx, dx, fma(dy, dy, fma(dz, dz, TINY)))) + c.l1);
+    case NFW: {
+      const double r = sqrt(fma(dx, dx, fma(dy, dy, fma(dz, dz, TINY))));
+      const double s = r * c.inv_l1;
+      return -c.Gm * c.inv_l1 * log1p(s) / s;
+    }
+    default: {
+      const double r = sqrt(fma(dx, dx, fma(dy, dy, fma(dz, dz, TINY))));
+      return -c.Gm / sqrt(fma(r, r, c.l2sq));
+    }
+  }
+}
+
+// Hessian accumulated into H[9] (row-major, symmetric).
+__device__ __forceinline__ void comp_hessian(const DevComp& c, double x, double y, double z, double* H) {
+  const double d[3] = {x - c.ox, y - c.oy, z - c.oz};
+  if (c.kind == MIYAMOTO_NAGAI) {
+    const double zb = sqrt(fma(d[2], d[2], c.l2sq));
+    const double s = zb + c.l1;
+    const double D2 = fma(d[0], d[0], fma(d[1], d[1], s * s));
+    const double D = sqrt(D2);
+    const double u = c.Gm / (D2 * D);
+    const double w = 3.0 * c.Gm / (D2 * D2 * D);
+    const double v[3] = {d[0], d[1], d[2] * s / zb};
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) H[3 * i + j] -= w * v[i] * v[j];
+    H[0] += u;
+    H[4] += u;
+    H[8] += u * (1.0 + c.l1 * c.l2sq / (zb * zb * zb));
+    return;
+  }
+  const double r2 = fma(d[0], d[0], fma(d[1], d[1], fma(d[2], d[2], TINY)));
+  const double r = sqrt(r2);
+  double g, gpr;  // g(r) with grad = g x, and g'(r)/r
+  switch (c.kind) {
+    case KEPLER:
+      g = c.Gm / (r2 * r);
+      gpr = -3.0 * c.Gm / (r2 * r2 * r);
+      break;
+    case HERNQUIST: {
+      const double dd = r + c.l1;
+      g = c.Gm / (r * dd * dd);
+      gpr = -c.Gm * (3.0 * r + c.l1) / (r2 * r * dd * dd * dd);
+      break;
+    }
+    case NFW: {
+      const double L = log1p(r * c.inv_l1), q = c.l1 + r;
+      g = c.Gm * (L / (r2 * r) - 1.0 / (r2 * q));
+      gpr = c.Gm * (3.0 / (r2 * r2 * q) - 3.0 * L / (r2 * r2 * r) + 1.0 / (r2 * r * q * q));
+      break;
+    }
+    default: {
+      const double s2 = r2 + c.l2sq, s = sqrt(s2);
+      g = c.Gm / (s2 * s);
+      gpr = -3.0 * c.Gm / (s2 * s2 * s);
+      break;
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) H[3 * i + j] += gpr * d[i] * d[j];
+  H[0] += g;
+  H[4] += g;
+  H[8] += g;
+}
+
+// ----------------------------------------------------------- potential models
+// General composite: a table of components (in shared memory inside kernels).
+struct TablePot {
+  const DevComp* c;
+  int n;
+  __device__ __forceinline__ void grad(double x, double y, double z, double& gx, double& gy, double& gz) const {
+    gx = gy = gz = 0.0;
+    for (int i = 0; i < n; ++i) comp_grad(c[i], x, y, z, gx, gy, gz);
+  }
+};
+
+// galax's MilkyWayPotential structure: Miyamoto-Nagai disk, NFW halo and two
+// Hernquist spheres (bulge, nucleus), all centred on the origin
+// (src/galax/potential/_src/builtin/milkyway.py:203-229).
+struct MWParams {
+  double Gm_d, a_d, b2_d;   // disk
+  double Gm_h, rs_h, irs_h; // halo
+  double Gm_b, rs_b;        // bulge
+  double Gm_n, rs_n;        // nucleus
+};
+
+struct MWPot {
+  MWParams p;
+  __device__ __forceinline__ void grad(double x, double y, double z, double& gx, double& gy, double& gz) const {
+    // disk
+    const double zb2 = fma(z, z, p.b2_d);
+    const double izb = rsqrt(zb2);
+    const double s = fma(zb2, izb, p.a_d);
+    const double R2 = fma(x, x, y * y);
+    const double iD = rsqrt(fma(s, s, R2));
+    const double u = p.Gm_d * (iD * iD) * iD;
+    // centred spheres share r
+    const double r2 = fma(z, z, R2 + TINY);
+    const double ir = rsqrt(r2);
+    const double r = r2 * ir;
+    const double dh = p.rs_h + r, db = r + p.rs_b, dn = r + p.rs_n;
+    const double db2 = db * db, dn2 = dn * dn;
+    const double q = db2 * dn2;
+    const double iP = 1.0 / (dh * q);  // one reciprocal for 1/dh, 1/db^2, 1/dn^2
+    const double inv_dh = iP * q;
+    const double inv_db2 = iP * dh * dn2;
+    const double inv_dn2 = iP * dh * db2;
+    const double L = log1p(r * p.irs_h);
+    const double f = p.Gm_h * (ir * ir) * fma(L, ir, -inv_dh) + ir * fma(p.Gm_b, inv_db2, p.Gm_n * inv_dn2);
+    gx = (u + f) * x;
+    gy = (u + f) * y;
+    gz = fma(u * s, izb, f) * z;
+  }
+};
+
+}  // namespace gal

@@ -1,0 +1,361 @@
+"""Orbit integration with galax's public interface, run by the CUDA library.
+
+Mirrors ``galax.dynamics.evaluate_orbit`` (src/galax/dynamics/_src/legacy/funcs.py:42-213),
+the legacy ``Integrator`` (legacy/integrator.py:42-245), ``OrbitSolver``'s
+defaults (orbit/solver.py:121-141) and the per-orbit save grids of
+``experimental.integrate_orbit`` (experimental/integrate.py:301-575). The
+solver and step-size-controller objects carry diffrax's names and fields
+(``Dopri5``, ``Dopri8``, ``ConstantStepSize``, ``PIDController``).
+
+Every orbit gets its own step-size controller (galax's per-orbit dispatch,
+legacy/integrator.py:449-527); galax's batched ``evaluate_orbit`` with shared
+start and end times instead advances the whole batch with one step size, so
+adaptive results agree per orbit within the controller tolerance, not bitwise.
+Fixed-step results agree to rounding.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from typing import Any, Sequence
+
+import numpy as np
+
+from . import _lib
+from .potential import KMS_TO_KPC_MYR, AbstractPotential
+
+# galax's legacy Integrator passes max_steps=None (unbounded); a GPU loop must end,
+# so "unbounded" becomes this per-orbit bound on step attempts.
+UNBOUNDED_MAX_STEPS = 2**20
+
+
+def _torch():
+    import torch
+
+    return torch
+
+
+# ---------------------------------------------------------------- solver objects
+@dataclass(frozen=True)
+class Dopri5:
+    """Dormand-Prince 5(4), 7 stages, FSAL (diffrax.Dopri5)."""
+
+    order: int = 5
+
+
+@dataclass(frozen=True)
+class Dopri8:
+    """Prince-Dormand 8(7) 13-stage pair (diffrax.Dopri8)."""
+
+    order: int = 8
+
+
+@dataclass(frozen=True)
+class ConstantStepSize:
+    """Fixed step dt0 (diffrax.ConstantStepSize)."""
+
+
+@dataclass(frozen=True)
+class PIDController:
+    """diffrax.PIDController fields, with diffrax's defaults."""
+
+    rtol: float
+    atol: float
+    pcoeff: float = 0.0
+    icoeff: float = 1.0
+    dcoeff: float = 0.0
+    dtmin: float | None = None
+    dtmax: float | None = None
+    force_dtmin: bool = True
+    safety: float = 0.9
+    factormin: float = 0.2
+    factormax: float = 10.0
+    step_ts: Any = None
+    jump_ts: Any = None
+
+    def __post_init__(self):
+        if self.step_ts is not None or self.jump_ts is not None:
+            raise NotImplementedError("step_ts / jump_ts are not supported on the GPU path")
+
+
+def _method(solver) -> int:
+    if isinstance(solver, (Dopri5, Dopri8)):
+        return solver.order
+    name = type(solver).__name__ if not isinstance(solver, str) else solver
+    if name in ("Dopri5", "dopri5", "5"):
+        return 5
+    if name in ("Dopri8", "dopri8", "8"):
+        return 8
+    raise NotImplementedError(f"solver {name!r}: only Dopri5 and Dopri8 are implemented")
+
+
+@dataclass
+class Integrator:
+    """galax's legacy Integrator (src/galax/dynamics/_src/legacy/integrator.py:161-168):
+    Dopri8 with PIDController(rtol=1e-7, atol=1e-7) and no step limit by default."""
+
+    solver: Any = field(default_factory=Dopri8)
+    stepsize_controller: Any = field(default_factory=lambda: PIDController(rtol=1e-7, atol=1e-7))
+    dt0: float | None = None
+    max_steps: int | None = None
+
+    def config(self) -> _lib.SolverConfig:
+        method = _method(self.solver)
+        max_steps = UNBOUNDED_MAX_STEPS if self.max_steps is None else int(self.max_steps)
+        c = self.stepsize_controller
+        if isinstance(c, ConstantStepSize):
+            if not self.dt0 or self.dt0 <= 0:
+                raise ValueError("ConstantStepSize needs dt0 > 0")
+            return _lib.solver_config(method, False, dt0=self.dt0, max_steps=max_steps)
+        if isinstance(c, PIDController):
+            return _lib.solver_config(
+                method, True, dt0=self.dt0 or 0.0, rtol=c.rtol, atol=c.atol, dtmin=c.dtmin, dtmax=c.dtmax,
+                pcoeff=c.pcoeff, icoeff=c.icoeff, dcoeff=c.dcoeff, safety=c.safety, factormin=c.factormin,
+                factormax=c.factormax, force_dtmin=c.force_dtmin, max_steps=max_steps,
+            )
+        raise NotImplementedError(f"step-size controller {type(c).__name__} is not supported")
+
+
+def OrbitSolver(solver=None, stepsize_controller=None, *, max_steps: int = 2**16, dt0=None) -> Integrator:
+    """galax's OrbitSolver defaults (src/galax/dynamics/_src/orbit/solver.py:121-141):
+    Dopri8, PIDController(rtol=1e-8, atol=1e-8), max_steps=2**16."""
+    return Integrator(
+        solver=solver or Dopri8(),
+        stepsize_controller=stepsize_controller or PIDController(rtol=1e-8, atol=1e-8),
+        dt0=dt0,
+        max_steps=max_steps,
+    )
+
+
+# ---------------------------------------------------------------- containers
+@dataclass
+class PhaseSpaceCoordinate:
+    """Host-side stand-in for gc.PhaseSpaceCoordinate: q (...,3) kpc, p (...,3) kpc/Myr, t (...) Myr."""
+
+    q: Any
+    p: Any
+    t: Any = None
+
+
+@dataclass
+class Orbit:
+    """Result of evaluate_orbit: q, p of shape (B, T, 3) (or (T, 3) for one orbit), times t (T,)."""
+
+    q: Any
+    p: Any
+    t: Any
+    status: Any = None
+    steps: Any = None
+    interpolant: Any = None
+
+    @property
+    def shape(self):
+        return tuple(self.q.shape[:-1])
+
+    @property
+    def w(self):
+        torch = _torch()
+        if isinstance(self.q, torch.Tensor):
+            return torch.cat([self.q, self.p], dim=-1)
+        return np.concatenate([self.q, self.p], axis=-1)
+
+
+def kms(v):
+    """km/s -> kpc/Myr."""
+    return np.asarray(v, np.float64) * KMS_TO_KPC_MYR
+
+
+# ---------------------------------------------------------------- low level
+class Workspace:
+    """Device scratch reused across calls (grown on demand)."""
+
+    def __init__(self):
+        self._buf = None
+
+    def get(self, nbytes: int):
+        torch = _torch()
+        if self._buf is None or self._buf.numel() < nbytes or self._buf.device.index != torch.cuda.current_device():
+            self._buf = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device="cuda")
+        return self._buf
+
+
+_WS = Workspace()
+
+
+def _as_cuda(x, dtype):
+    torch = _torch()
+    if isinstance(x, torch.Tensor):
+        return x.to(device="cuda", dtype=dtype)
+    return torch.as_tensor(np.asarray(x), dtype=dtype, device="cuda")
+
+
+def integrate(
+    pot: AbstractPotential,
+    y0,
+    t0,
+    t1,
+    save_ts,
+    cfg: _lib.SolverConfig,
+    *,
+    save_offsets=None,
+    order=None,
+    soa: bool = False,
+    stream=None,
+    workspace: Workspace | None = None,
+):
+    """Integrate n orbits on the current CUDA device.
+
+    y0: (n, 6) (or (6, n) with ``soa=True``); t0, t1: scalars or (n,);
+    save_ts: (T,) shared by all orbits, or the flat CSR values with
+    ``save_offsets`` (n+1,). Returns (out, status, steps) with out of shape
+    (6, T, n) for a shared grid or (6, total) for CSR saves. Asynchronous.
+    """
+    torch = _torch()
+    y = _as_cuda(y0, torch.float64)
+    if not soa:
+        y = y.reshape(-1, 6).t()
+    y = y.contiguous()
+    n = y.shape[1]
+    t0v = _as_cuda(t0, torch.float64).reshape(-1).expand(n).contiguous()
+    t1v = _as_cuda(t1, torch.float64).reshape(-1).expand(n).contiguous()
+    ts = _as_cuda(save_ts, torch.float64).reshape(-1).contiguous()
+    if save_offsets is not None:
+        offs = _as_cuda(save_offsets, torch.int64).reshape(-1).contiguous()
+        if offs.numel() != n + 1:
+            raise ValueError("save_offsets must have n + 1 entries")
+        total = int(ts.numel())
+        # the kernel indexes saves through these offsets: reject inconsistent ones before launch
+        if int(offs[0]) != 0 or int(offs[-1]) != total or bool((offs[1:] < offs[:-1]).any()):
+            raise ValueError("save_offsets must start at 0, be non-decreasing and end at len(save_ts)")
+        out = torch.empty((6, total), dtype=torch.float64, device="cuda")
+        offs_ptr, n_saves = offs.data_ptr(), total
+    else:
+        out = torch.empty((6, ts.numel(), n), dtype=torch.float64, device="cuda")
+        offs_ptr, n_saves = None, ts.numel()
+    status = torch.empty(n, dtype=torch.int32, device="cuda")
+    steps = torch.empty(n, dtype=torch.int64, device="cuda")
+    ordp = None
+    if order is not None:
+        ordt = _as_cuda(order, torch.int32).reshape(-1).contiguous()
+        if ordt.numel() != n or (n and (int(ordt.min()) < 0 or int(ordt.max()) >= n)):
+            raise ValueError("order must be a permutation of range(n)")
+        ordp = ordt.data_ptr()
+    L = _lib.load()
+    nbytes = C.c_size_t()
+    _lib.check(L.gal_integrate_workspace_size(C.byref(cfg), n, C.byref(nbytes)), "gal_integrate_workspace_size")
+    ws = (workspace or _WS).get(nbytes.value)
+    st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+    _lib.check(
+        L.gal_integrate(
+            pot.handle(), C.byref(cfg), y.data_ptr(), t0v.data_ptr(), t1v.data_ptr(), offs_ptr, ts.data_ptr(),
+            n_saves, out.data_ptr(), status.data_ptr(), steps.data_ptr(), ordp, n, ws.data_ptr(), ws.numel(), st,
+        ),
+        "gal_integrate",
+    )
+    return out, status, steps
+
+
+def _raise_on_status(status, what: str) -> None:
+    torch = _torch()
+    bad = status != 0
+    if bool(bad.any()):
+        s = status.cpu().numpy()
+        idx = np.nonzero(s)[0]
+        first = int(idx[0])
+        raise _lib.GalaxGB300Error(
+            f"{what}: {len(idx)} orbit(s) did not finish; orbit {first}: {_lib.ORBIT_STATUS.get(int(s[first]), s[first])}"
+        )
+    del torch
+
+
+def _split_w0(w0):
+    torch = _torch()
+    if isinstance(w0, PhaseSpaceCoordinate) or (hasattr(w0, "q") and hasattr(w0, "p")):
+        q = _as_cuda(w0.q, torch.float64)
+        p = _as_cuda(w0.p, torch.float64)
+        q, p = torch.broadcast_tensors(q, p)
+        t = getattr(w0, "t", None)
+        return torch.cat([q, p], dim=-1), t
+    w = _as_cuda(w0, torch.float64)
+    if w.shape[-1] != 6:
+        raise ValueError("w0 must be (..., 6) phase-space points or have q and p")
+    return w, None
+
+
+# ---------------------------------------------------------------- front doors
+def evaluate_orbit(pot: AbstractPotential, w0, t, /, *, integrator: Integrator | None = None, dense: bool = False,
+                   throw: bool = True) -> Orbit:
+    """Compute orbits in ``pot`` saved at times ``t`` (galax legacy/funcs.py:42-213).
+
+    As in galax, a ``w0`` that carries its own time is first integrated from
+    ``w0.t`` to ``t[0]``, then from ``t[0]`` to ``t[-1]`` with saves at every
+    ``t``; without a time, ``w0`` is taken to be at ``t[0]``.
+    """
+    torch = _torch()
+    if dense:
+        raise NotImplementedError("dense=True (interpolated orbits) is not implemented on the GPU path")
+    integrator = integrator or Integrator()
+    cfg = integrator.config()
+    is_np = not isinstance(t, torch.Tensor) and not isinstance(w0, torch.Tensor)
+    ts = _as_cuda(t, torch.float64).reshape(-1)
+    if ts.numel() == 0:
+        raise ValueError("t must hold at least one time")
+    w, tw0 = _split_w0(w0)
+    batch = w.shape[:-1]
+    y = w.reshape(-1, 6)
+    n = y.shape[0]
+    t_first, t_last = ts[0], ts[-1]
+    if tw0 is not None:
+        tw = _as_cuda(tw0, torch.float64).reshape(-1).expand(n).contiguous()
+        out0, st0, _ = integrate(pot, y, tw, t_first.reshape(1), t_first.reshape(1), cfg)
+        if throw:
+            _raise_on_status(st0, "evaluate_orbit (w0.t -> t[0])")
+        y = out0[:, 0, :].t()
+    out, status, steps = integrate(pot, y, t_first.reshape(1), t_last.reshape(1), ts, cfg)
+    if throw:
+        _raise_on_status(status, "evaluate_orbit")
+    w_btk = out.permute(2, 1, 0)  # (n, T, 6)
+    q = w_btk[..., :3].reshape(*batch, ts.numel(), 3)
+    p = w_btk[..., 3:].reshape(*batch, ts.numel(), 3)
+    orb = Orbit(q=q, p=p, t=ts, status=status.reshape(batch), steps=steps.reshape(batch))
+    if is_np:
+        orb = Orbit(q=q.cpu().numpy(), p=p.cpu().numpy(), t=ts.cpu().numpy(), status=orb.status.cpu().numpy(),
+                    steps=orb.steps.cpu().numpy())
+    return orb
+
+
+def integrate_orbit(pot: AbstractPotential, w0, t0, t1, saveat: Sequence | None = None, *,
+                    integrator: Integrator | None = None, throw: bool = True):
+    """Per-orbit start/end times and save grids (galax experimental/integrate.py:301-575).
+
+    ``saveat`` is a list of 1-D arrays, one per orbit (ragged allowed), or None
+    for the final state only. Returns (list of (T_i, 6) arrays or a (n, 6)
+    array, status, steps).
+    """
+    torch = _torch()
+    integrator = integrator or Integrator(solver=Dopri8(), stepsize_controller=PIDController(rtol=1e-7, atol=1e-7))
+    cfg = integrator.config()
+    w, _ = _split_w0(w0)
+    y = w.reshape(-1, 6)
+    n = y.shape[0]
+    t0v = _as_cuda(t0, torch.float64).reshape(-1).expand(n)
+    t1v = _as_cuda(t1, torch.float64).reshape(-1).expand(n)
+    if saveat is None:
+        offs = torch.arange(n + 1, dtype=torch.int64, device="cuda")
+        flat = t1v.contiguous()
+    else:
+        lens = [len(s) for s in saveat]
+        if len(lens) != n:
+            raise ValueError("saveat needs one grid per orbit")
+        offs = torch.zeros(n + 1, dtype=torch.int64)
+        offs[1:] = torch.cumsum(torch.as_tensor(lens, dtype=torch.int64), 0)
+        flat = torch.cat([_as_cuda(s, torch.float64).reshape(-1) for s in saveat])
+    out, status, steps = integrate(pot, y, t0v, t1v, flat, cfg, save_offsets=offs)
+    if throw:
+        _raise_on_status(status, "integrate_orbit")
+    res = out.t()
+    if saveat is None:
+        return res, status, steps
+    o = offs.cpu().numpy()
+    return [res[o[i]:o[i + 1]] for i in range(n)], status, steps

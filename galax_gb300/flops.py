@@ -1,0 +1,12 @@
+"""Algorithmic FP64 operation counts used for roofline reporting.
+
+Counted by executing the CPU restatement of the arithmetic with an
+operation-counting number type (every add, multiply, divide, square root and
+log1p counts as one flop); a test keeps these constants equal to that count.
+One Milky Way gradient (disk + halo + bulge + nucleus) is 92 flops; a step
+is every new stage evaluation plus the stage combinations, solution and error
+estimate (Dopri5: 6 new evaluations thanks to FSAL; Dopri8: 13).
+"""
+
+GRADIENT_FLOPS_MW = 92
+STEP_FLOPS_MW = {5: 1002, 8: 2276}

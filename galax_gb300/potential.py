@@ -1,0 +1,373 @@
+"""Potentials with galax's public interface, evaluated by the CUDA library.
+
+Mirrors the part of ``galax.potential`` on the orbit path:
+``HernquistPotential``, ``MiyamotoNagaiPotential``, ``NFWPotential``,
+``PlummerPotential``, ``KeplerPotential``, ``MilkyWayPotential`` and
+``CompositePotential`` (src/galax/potential/_src/builtin/*.py,
+composite.py:32-108, builtin/milkyway.py:172-236) with the methods
+``potential``, ``gradient``, ``acceleration``, ``hessian``,
+``local_circular_velocity`` and ``evaluate_orbit``
+(src/galax/potential/_src/base.py:138-143, 181-186, 250-255, 384-456;
+register_funcs.py:327-340, 384-400).
+
+Inputs are arrays in galax's "galactic" unit system (kpc, Myr, Msun; velocities
+in kpc/Myr) with positions on the last axis, as galax accepts bare arrays. NumPy
+inputs give NumPy outputs; CUDA torch tensors stay on the device. Parameters
+must be constants (galax's ConstantParameter): time-dependent or callable
+parameters are rejected, as are unit systems other than "galactic".
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import math
+from collections.abc import Mapping
+from typing import Any
+
+import numpy as np
+
+from . import _lib
+
+G_GALACTIC = 4.498502151469553e-12  # kpc^3 / (Msun Myr^2): astropy's CODATA-2018 G in galactic units
+KMS_TO_KPC_MYR = 0.001022712165045695
+
+
+def _torch():
+    import torch
+
+    return torch
+
+
+def _param(name: str, v: Any) -> float:
+    if callable(v):
+        raise NotImplementedError(f"{name}: only constant parameters are supported on the GPU path")
+    try:
+        f = float(v)
+    except Exception as e:  # noqa: BLE001
+        raise TypeError(f"{name} must be a number in galactic units, got {type(v).__name__}") from e
+    if not math.isfinite(f):
+        raise ValueError(f"{name} must be finite")
+    return f
+
+
+def _check_units(units: Any) -> None:
+    if units not in (None, "galactic"):
+        raise NotImplementedError("only the 'galactic' unit system (kpc, Myr, Msun) is supported")
+
+
+class AbstractPotential:
+    """Base class: a sum of closed-form components evaluated on the GPU."""
+
+    units = "galactic"
+
+    def __init__(self, *, units: Any = "galactic", constants: Mapping[str, float] | None = None):
+        _check_units(units)
+        self.constants = {"G": G_GALACTIC}
+        if constants:
+            self.constants.update({k: float(v) for k, v in constants.items()})
+        self._handle = None
+        self._handle_device = None
+        self._handle_key = None
+
+    # ---- component table -------------------------------------------------
+    def components(self) -> list[tuple[int, float, float, float, tuple[float, float, float]]]:
+        raise NotImplementedError
+
+    def component_array(self) -> np.ndarray:
+        recs = self.components()
+        a = np.zeros(len(recs), _lib.COMPONENT_DTYPE)
+        for i, (kind, m, l1, l2, origin) in enumerate(recs):
+            a[i]["kind"], a[i]["m"], a[i]["l1"], a[i]["l2"] = kind, m, l1, l2
+            a[i]["origin"] = origin
+        return a
+
+    def parameter_names(self) -> list[tuple[str, str, str]]:
+        """(component, mass-name, length names) per component, for gradients."""
+        return [(f"c{i}", "m", "l1", "l2") for i in range(len(self.components()))]
+
+    @property
+    def G(self) -> float:
+        return self.constants["G"]
+
+    def handle(self) -> int:
+        """The device-side ``gal_potential`` for the current CUDA device."""
+        torch = _torch()
+        if not torch.cuda.is_available():
+            raise _lib.GalaxGB300Error("no CUDA device: the galax_gb300 path has no CPU fallback")
+        dev = torch.cuda.current_device()
+        arr = self.component_array()
+        key = arr.tobytes() + np.float64(self.G).tobytes()
+        if self._handle is not None and self._handle_device == dev and self._handle_key == key:
+            return self._handle
+        self._release()
+        L = _lib.load()
+        h = C.c_void_p()
+        _lib.check(L.gal_potential_create(arr.ctypes.data, len(arr), self.G, C.byref(h)), "gal_potential_create")
+        self._handle, self._handle_device, self._handle_key, self._arr = h.value, dev, key, arr
+        return self._handle
+
+    def _release(self) -> None:
+        if getattr(self, "_handle", None):
+            try:
+                torch = _torch()
+                with torch.cuda.device(self._handle_device):
+                    _lib.load().gal_potential_destroy(self._handle)
+            except Exception:  # noqa: BLE001  (interpreter shutdown)
+                pass
+        self._handle = None
+
+    def __del__(self):
+        self._release()
+
+    def is_milky_way_kernel(self) -> bool:
+        return bool(_lib.load().gal_potential_is_milky_way(self.handle()))
+
+    # ---- evaluation --------------------------------------------------------
+    def _positions(self, x):
+        torch = _torch()
+        is_np = not isinstance(x, torch.Tensor)
+        xt = torch.as_tensor(np.asarray(x, dtype=np.float64) if is_np else x)
+        if xt.shape[-1] != 3:
+            raise ValueError(f"positions must have a last axis of size 3, got shape {tuple(xt.shape)}")
+        batch = xt.shape[:-1]
+        soa = xt.reshape(-1, 3).to(device="cuda", dtype=torch.float64).t().contiguous()
+        return soa, batch, is_np
+
+    @staticmethod
+    def _out(t, is_np):
+        return t.cpu().numpy() if is_np else t
+
+    def _eval(self, fn: str, x, t, ncomp_out: int):
+        torch = _torch()
+        soa, batch, is_np = self._positions(x)
+        n = soa.shape[1]
+        out = torch.empty((ncomp_out, n), dtype=torch.float64, device="cuda")
+        L = _lib.load()
+        stream = torch.cuda.current_stream().cuda_stream
+        _lib.check(getattr(L, fn)(self.handle(), soa.data_ptr(), float(t or 0.0), n, out.data_ptr(), stream), fn)
+        return out, batch, is_np
+
+    def potential(self, x, t=0.0):
+        out, batch, is_np = self._eval("gal_eval_potential", x, t, 1)
+        return self._out(out.reshape(batch), is_np)
+
+    def gradient(self, x, t=0.0):
+        out, batch, is_np = self._eval("gal_eval_gradient", x, t, 3)
+        return self._out(out.t().reshape(*batch, 3), is_np)
+
+    def acceleration(self, x, t=0.0):
+        out, batch, is_np = self._eval("gal_eval_acceleration", x, t, 3)
+        return self._out(out.t().reshape(*batch, 3), is_np)
+
+    def hessian(self, x, t=0.0):
+        out, batch, is_np = self._eval("gal_eval_hessian", x, t, 9)
+        return self._out(out.t().reshape(*batch, 3, 3), is_np)
+
+    def local_circular_velocity(self, x, t=0.0):
+        """sqrt(r |dPhi/dr|) at x (src/galax/potential/_src/register_funcs.py:384-400)."""
+        torch = _torch()
+        is_np = not isinstance(x, torch.Tensor)
+        xt = torch.as_tensor(np.asarray(x, np.float64) if is_np else x).to("cuda", torch.float64)
+        g = self.gradient(xt, t)
+        r = torch.linalg.vector_norm(xt, dim=-1)
+        dphidr = (g * xt / r[..., None]).sum(-1)
+        return self._out(torch.sqrt(r * dphidr.abs()), is_np)
+
+    def evaluate_orbit(self, w0, t, *, integrator=None, dense: bool = False):
+        from .dynamics import evaluate_orbit
+
+        return evaluate_orbit(self, w0, t, integrator=integrator, dense=dense)
+
+    def __or__(self, other: "AbstractPotential") -> "CompositePotential":
+        return CompositePotential(_flatten(self) + _flatten(other))
+
+    def __repr__(self) -> str:
+        return f"{type(self).__name__}({self._repr_params()})"
+
+    def _repr_params(self) -> str:
+        return ""
+
+
+class AbstractSinglePotential(AbstractPotential):
+    kind: int
+    _names: tuple[str, ...]
+
+    def __init__(self, *, origin=(0.0, 0.0, 0.0), units: Any = "galactic", constants=None, **params):
+        super().__init__(units=units, constants=constants)
+        for name in self._names:
+            if name not in params:
+                raise TypeError(f"{type(self).__name__} needs parameter {name!r}")
+            setattr(self, name, _param(name, params.pop(name)))
+        if params:
+            raise TypeError(f"unexpected parameters {sorted(params)}")
+        self.origin = tuple(float(v) for v in origin)
+        if len(self.origin) != 3:
+            raise ValueError("origin must have 3 entries")
+
+    def _repr_params(self) -> str:
+        return ", ".join(f"{k}={getattr(self, k)!r}" for k in self._names)
+
+
+class KeplerPotential(AbstractSinglePotential):
+    """Point mass: Phi = -G m_tot / r."""
+
+    kind = _lib.GAL_KEPLER
+    _names = ("m_tot",)
+
+    def components(self):
+        return [(self.kind, self.m_tot, 0.0, 0.0, self.origin)]
+
+
+class HernquistPotential(AbstractSinglePotential):
+    """Phi = -G m_tot / (r + r_s) (src/galax/potential/_src/builtin/hernquist.py:80-82)."""
+
+    kind = _lib.GAL_HERNQUIST
+    _names = ("m_tot", "r_s")
+
+    def components(self):
+        return [(self.kind, self.m_tot, self.r_s, 0.0, self.origin)]
+
+
+class MiyamotoNagaiPotential(AbstractSinglePotential):
+    """Phi = -G m_tot / sqrt(R^2 + (sqrt(z^2 + b^2) + a)^2) (builtin/miyamotonagai.py:73-78)."""
+
+    kind = _lib.GAL_MIYAMOTO_NAGAI
+    _names = ("m_tot", "a", "b")
+
+    def components(self):
+        return [(self.kind, self.m_tot, self.a, self.b, self.origin)]
+
+
+class NFWPotential(AbstractSinglePotential):
+    """Phi = -G m log(1 + r/r_s) / r (builtin/nfw/base.py:326-338)."""
+
+    kind = _lib.GAL_NFW
+    _names = ("m", "r_s")
+
+    def components(self):
+        return [(self.kind, self.m, self.r_s, 0.0, self.origin)]
+
+
+class PlummerPotential(AbstractSinglePotential):
+    """Phi = -G m_tot / sqrt(r^2 + r_s^2) (builtin/plummer.py:122-133)."""
+
+    kind = _lib.GAL_PLUMMER
+    _names = ("m_tot", "r_s")
+
+    def components(self):
+        return [(self.kind, self.m_tot, self.r_s, 0.0, self.origin)]
+
+
+def _flatten(p: AbstractPotential) -> list[AbstractPotential]:
+    if isinstance(p, CompositePotential):
+        out = []
+        for v in p.values():
+            out += _flatten(v)
+        return out
+    return [p]
+
+
+class CompositePotential(AbstractPotential):
+    """Sum of potentials (src/galax/potential/_src/composite.py:32-108): a mapping
+    name -> potential whose Phi, gradient and Hessian are the component sums."""
+
+    def __init__(self, potentials=None, /, *, units: Any = "galactic", constants=None, **kw):
+        super().__init__(units=units, constants=constants)
+        if potentials is None:
+            items = list(kw.items())
+        elif isinstance(potentials, Mapping):
+            items = list(potentials.items()) + list(kw.items())
+        else:
+            items = [(f"p{i}", p) for i, p in enumerate(potentials)] + list(kw.items())
+        for k, v in items:
+            if not isinstance(v, AbstractPotential):
+                raise TypeError(f"component {k!r} is not a potential")
+        self._items = dict(items)
+
+    def keys(self):
+        return self._items.keys()
+
+    def values(self):
+        return self._items.values()
+
+    def items(self):
+        return self._items.items()
+
+    def __getitem__(self, k):
+        return self._items[k]
+
+    def __len__(self):
+        return len(self._items)
+
+    def __iter__(self):
+        return iter(self._items)
+
+    def components(self):
+        out = []
+        for v in self._items.values():
+            out += v.components()
+        return out
+
+    def _repr_params(self) -> str:
+        return ", ".join(f"{k}={v!r}" for k, v in self._items.items())
+
+
+class MilkyWayPotential(CompositePotential):
+    """galax's MilkyWayPotential (src/galax/potential/_src/builtin/milkyway.py:172-236):
+    Miyamoto-Nagai disk, NFW halo, Hernquist bulge and nucleus, in that order."""
+
+    DEFAULTS = {
+        "disk": {"m_tot": 6.8e10, "a": 3.0, "b": 0.28},
+        "halo": {"m": 5.4e11, "r_s": 15.62},
+        "bulge": {"m_tot": 5e9, "r_s": 1.0},
+        "nucleus": {"m_tot": 1.71e9, "r_s": 0.07},
+    }
+
+    def __init__(self, disk=None, halo=None, bulge=None, nucleus=None, *, units: Any = "galactic", constants=None):
+        def part(name, cls, given):
+            if isinstance(given, AbstractPotential):
+                return given
+            kw = dict(self.DEFAULTS[name])
+            kw.update(given or {})
+            return cls(**kw, units=units, constants=constants)
+
+        super().__init__(
+            {
+                "disk": part("disk", MiyamotoNagaiPotential, disk),
+                "halo": part("halo", NFWPotential, halo),
+                "bulge": part("bulge", HernquistPotential, bulge),
+                "nucleus": part("nucleus", HernquistPotential, nucleus),
+            },
+            units=units,
+            constants=constants,
+        )
+
+
+class TranslatedPotential(CompositePotential):
+    """A potential shifted by a constant translation (src/galax/potential/_src/xfm/translate.py:28-87,
+    constant translations only)."""
+
+    def __init__(self, original: AbstractPotential, translation, *, units: Any = "galactic"):
+        super().__init__({"original": original}, units=units, constants=original.constants)
+        self.translation = tuple(float(v) for v in translation)
+        if callable(translation):
+            raise NotImplementedError("time-dependent translations are not supported on the GPU path")
+
+    def components(self):
+        tx, ty, tz = self.translation
+        return [(k, m, l1, l2, (o[0] + tx, o[1] + ty, o[2] + tz))
+                for (k, m, l1, l2, o) in self["original"].components()]
+
+
+def from_component_array(arr: np.ndarray, G: float = G_GALACTIC) -> CompositePotential:
+    """Composite built from a ``gal_component`` record array."""
+    cls = {_lib.GAL_KEPLER: KeplerPotential, _lib.GAL_HERNQUIST: HernquistPotential,
+           _lib.GAL_MIYAMOTO_NAGAI: MiyamotoNagaiPotential, _lib.GAL_NFW: NFWPotential,
+           _lib.GAL_PLUMMER: PlummerPotential}
+    parts = {}
+    for i, rec in enumerate(arr):
+        k = int(rec["kind"])
+        names = cls[k]._names
+        vals = [float(rec["m"]), float(rec["l1"]), float(rec["l2"])][: len(names)]
+        parts[f"c{i}"] = cls[k](**dict(zip(names, vals)), origin=tuple(rec["origin"]), constants={"G": G})
+    return CompositePotential(parts, constants={"G": G})

@@ -1,0 +1,95 @@
+"""Seeded synthetic workloads with the shapes and distributions of the
+benchmark configurations (there is no dataset: galax benchmarks synthetic
+orbits). Everything is drawn with ``numpy.random.default_rng(seed)`` in float64
+galactic units; velocities use the local circular speed sqrt(r |dPhi/dr|)
+(galax's local_circular_velocity, src/galax/potential/_src/register_funcs.py:384-400)
+computed from a caller-supplied gradient function ``grad(x (n,3)) -> (n,3)``.
+"""
+
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+KMS = 0.001022712165045695  # kpc/Myr per km/s
+
+
+def isotropic(rng: np.random.Generator, n: int) -> np.ndarray:
+    v = rng.normal(size=(n, 3))
+    return v / np.linalg.norm(v, axis=1, keepdims=True)
+
+
+def circular_speed(grad, x: np.ndarray) -> np.ndarray:
+    g = np.asarray(grad(x))
+    r = np.linalg.norm(x, axis=1)
+    dphidr = np.sum(g * x / r[:, None], axis=1)
+    return np.sqrt(r * np.abs(dphidr))
+
+
+def disk_like_ics(grad, n: int, seed: int, rmin: float = 4.0, rmax: float = 20.0) -> np.ndarray:
+    """Orbits of the small plain workload: r ~ U(rmin, rmax), isotropic direction,
+    v = v_c(r) phi_hat * N(1, 0.1) per component + z_hat * N(0, 20 km/s). Returns (n, 6)."""
+    rng = np.random.default_rng(seed)
+    r = rng.uniform(rmin, rmax, n)
+    x = isotropic(rng, n) * r[:, None]
+    vc = circular_speed(grad, x)
+    R = np.hypot(x[:, 0], x[:, 1])
+    phi_hat = np.stack([-x[:, 1] / R, x[:, 0] / R, np.zeros(n)], axis=1)
+    v = vc[:, None] * phi_hat * rng.normal(1.0, 0.1, (n, 3))
+    v[:, 2] += rng.normal(0.0, 20.0 * KMS, n)
+    return np.concatenate([x, v], axis=1)
+
+
+@dataclass
+class UnevenBatch:
+    y0: np.ndarray          # (n, 6)
+    t0: np.ndarray          # (n,)
+    t1: np.ndarray          # (n,)
+    save_offsets: np.ndarray  # (n+1,) int64
+    save_ts: np.ndarray     # (total,)
+
+
+def uneven_ics(grad, n: int, seed: int = 1, rmin: float = 0.5, rmax: float = 100.0, tmin: float = 100.0,
+               tmax: float = 5000.0, smin: int = 10, smax: int = 1000) -> UnevenBatch:
+    """The batched uneven workload: r log-uniform [rmin, rmax], isotropic
+    direction, v = v_c * U(0.3, 1.1) along a random tangential direction,
+    duration log-uniform [tmin, tmax] Myr, save count uniform in [smin, smax],
+    saves evenly spaced over each orbit's span."""
+    rng = np.random.default_rng(seed)
+    r = np.exp(rng.uniform(np.log(rmin), np.log(rmax), n))
+    rhat = isotropic(rng, n)
+    x = rhat * r[:, None]
+    vc = circular_speed(grad, x)
+    a = isotropic(rng, n)
+    tang = a - np.sum(a * rhat, axis=1, keepdims=True) * rhat
+    tang /= np.linalg.norm(tang, axis=1, keepdims=True)
+    v = tang * (vc * rng.uniform(0.3, 1.1, n))[:, None]
+    dur = np.exp(rng.uniform(np.log(tmin), np.log(tmax), n))
+    ns = rng.integers(smin, smax + 1, n)
+    offs = np.zeros(n + 1, np.int64)
+    offs[1:] = np.cumsum(ns)
+    # evenly spaced saves over [0, dur_i] for every orbit, vectorised
+    orbit_of = np.repeat(np.arange(n), ns)
+    k = np.arange(offs[-1]) - offs[orbit_of]
+    save_ts = dur[orbit_of] * (k / (ns[orbit_of] - 1))
+    last = offs[1:] - 1
+    save_ts[last] = dur  # exact end times
+    return UnevenBatch(np.concatenate([x, v], axis=1), np.zeros(n), dur, offs, save_ts)
+
+
+def subhalo_table(seed: int = 3, n: int = 512):
+    """Plummer subhalos: m log-uniform [1e6, 1e8] Msun, r_s ~ U(0.1, 1) kpc,
+    centres isotropic at radius U(5, 50) kpc. Returns (m, r_s, centres (n,3))."""
+    rng = np.random.default_rng(seed)
+    m = np.exp(rng.uniform(np.log(1e6), np.log(1e8), n))
+    b = rng.uniform(0.1, 1.0, n)
+    c = isotropic(rng, n) * rng.uniform(5.0, 50.0, n)[:, None]
+    return m, b, c
+
+
+def training_points(n: int, seed: int = 30, rmin: float = 0.1, rmax: float = 200.0) -> np.ndarray:
+    """Positions log-uniform in radius over [rmin, rmax] kpc with isotropic directions."""
+    rng = np.random.default_rng(seed)
+    r = np.exp(rng.uniform(np.log(rmin), np.log(rmax), n))
+    return isotropic(rng, n) * r[:, None]

@@ -1,0 +1,193 @@
+/*
+ * galax_gb300 — C ABI of the GB300 (sm_103a) orbit-integration library.
+ *
+ * The library replaces, for static composites of Kepler / Hernquist /
+ * Miyamoto-Nagai / NFW / Plummer components, the part of GalacticDynamics/galax
+ * that runs below `gd.evaluate_orbit` and `gp.AbstractPotential.gradient`:
+ * the field, potential-gradient, Runge-Kutta stepping, step-size control and
+ * save-time interpolation that galax hands to diffrax.
+ *
+ * Conventions
+ *   - Units are galax's "galactic" system: kpc, Myr, Msun (G passed in).
+ *   - Arrays are caller-owned device memory, structure-of-arrays float64:
+ *     positions x[3][n] (x[0..n) = all x, then y, then z); phase-space
+ *     y[6][n] (x, y, z, vx, vy, vz).
+ *   - Every call is asynchronous on the given stream (cudaStream_t; NULL = legacy
+ *     default stream) and returns a gal_status. Nothing synchronises the device.
+ *   - Scratch memory is caller-provided: size it with the matching
+ *     *_workspace_size query. The library allocates device memory only inside
+ *     gal_potential_create (its component table) and frees it in
+ *     gal_potential_destroy.
+ *   - No C++ exception crosses this boundary.
+ */
+#ifndef GALAX_GB300_H
+#define GALAX_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* gal_stream_t; /* identical to cudaStream_t */
+
+#if defined(__GNUC__)
+#define GAL_API __attribute__((visibility("default")))
+#else
+#define GAL_API
+#endif
+
+/* ------------------------------------------------------------------ status */
+typedef enum gal_status {
+  GAL_OK = 0,
+  GAL_ERR_INVALID_ARGUMENT = 1,
+  GAL_ERR_UNSUPPORTED = 2,
+  GAL_ERR_CUDA = 3,
+  GAL_ERR_WORKSPACE = 4,
+  GAL_ERR_TOO_LARGE = 5
+} gal_status;
+
+/* Per-orbit outcome; mirrors diffrax.RESULTS as raised by galax's solvers
+ * (src/galax/dynamics/_src/solver.py:69-72). */
+typedef enum gal_orbit_status {
+  GAL_ORBIT_OK = 0,
+  GAL_ORBIT_MAX_STEPS = 1, /* diffrax RESULTS.max_steps_reached */
+  GAL_ORBIT_DT_MIN = 2,    /* diffrax RESULTS.dt_min_reached (force_dtmin = 0) */
+  GAL_ORBIT_NONFINITE = 3  /* state became NaN/inf; integration stopped */
+} gal_orbit_status;
+
+/* ------------------------------------------------------------------ potential */
+typedef enum gal_kind {
+  GAL_KEPLER = 0,         /* Phi = -G m / r                src/galax/potential/_src/builtin/kepler.py */
+  GAL_HERNQUIST = 1,      /* Phi = -G m / (r + r_s)        .../builtin/hernquist.py:80-82 */
+  GAL_MIYAMOTO_NAGAI = 2, /* Phi = -G m / sqrt(R^2 + (sqrt(z^2+b^2)+a)^2)  .../miyamotonagai.py:73-78 */
+  GAL_NFW = 3,            /* Phi = -G m log(1 + r/r_s) / r .../builtin/nfw/base.py:326-338 */
+  GAL_PLUMMER = 4         /* Phi = -G m / sqrt(r^2 + b^2)  .../builtin/plummer.py:122-133 */
+} gal_kind;
+
+/* One component of a composite potential (src/galax/potential/_src/base_multi.py:39-55).
+ * m  : m_tot (Kepler, Hernquist, Miyamoto-Nagai, Plummer) or m (NFW)
+ * l1 : r_s (Hernquist, NFW, Plummer) or a (Miyamoto-Nagai); unused for Kepler
+ * l2 : b (Miyamoto-Nagai); unused otherwise
+ * origin : constant translation of the component centre
+ *          (src/galax/potential/_src/xfm/translate.py:28-87 with a constant shift). */
+typedef struct gal_component {
+  int32_t kind;
+  int32_t flags; /* must be 0 */
+  double m;
+  double l1;
+  double l2;
+  double origin[3];
+} gal_component;
+
+typedef struct gal_potential gal_potential; /* opaque */
+
+/* Build a device-resident composite. Replaces the construction of
+ * gp.CompositePotential / gp.MilkyWayPotential (src/galax/potential/_src/composite.py:32-108,
+ * builtin/milkyway.py:172-236). n in [1, GAL_MAX_COMPONENTS]. */
+#define GAL_MAX_COMPONENTS 1024
+GAL_API gal_status gal_potential_create(const gal_component* comps, int32_t n, double G, gal_potential** out);
+GAL_API gal_status gal_potential_destroy(gal_potential* pot);
+/* Replace the parameters (same count and kinds), e.g. between optimiser steps. */
+GAL_API gal_status gal_potential_update(gal_potential* pot, const gal_component* comps, int32_t n, gal_stream_t stream);
+GAL_API int32_t gal_potential_num_components(const gal_potential* pot);
+/* 1 when the composite is evaluated by the specialised MilkyWayPotential kernel. */
+GAL_API int32_t gal_potential_is_milky_way(const gal_potential* pot);
+
+/* Batched evaluation at n positions x[3][n] (time t is accepted for API parity:
+ * all supported parameters are constant in time).
+ *   gal_eval_potential    : phi[n]       replaces AbstractPotential._potential   (base.py:113-136)
+ *   gal_eval_gradient     : out[3][n]    replaces AbstractPotential._gradient    (base.py:170-179)
+ *   gal_eval_acceleration : out[3][n]    replaces api.acceleration = -gradient   (register_funcs.py:327-340)
+ *   gal_eval_hessian      : out[9][n]    replaces AbstractPotential._hessian     (base.py:230-239) */
+GAL_API gal_status gal_eval_potential(const gal_potential* pot, const double* x, double t, int64_t n, double* phi,
+                              gal_stream_t stream);
+GAL_API gal_status gal_eval_gradient(const gal_potential* pot, const double* x, double t, int64_t n, double* out,
+                             gal_stream_t stream);
+GAL_API gal_status gal_eval_acceleration(const gal_potential* pot, const double* x, double t, int64_t n, double* out,
+                                 gal_stream_t stream);
+GAL_API gal_status gal_eval_hessian(const gal_potential* pot, const double* x, double t, int64_t n, double* out,
+                            gal_stream_t stream);
+
+/* ------------------------------------------------------------------ integration */
+/* Solver configuration; field meanings follow diffrax's Dopri5/Dopri8,
+ * ConstantStepSize and PIDController as configured by galax
+ * (src/galax/dynamics/_src/legacy/integrator.py:161-168, orbit/solver.py:121-141). */
+typedef struct gal_solver_config {
+  int32_t method;    /* 5 = Dopri5, 8 = Dopri8 */
+  int32_t adaptive;  /* 0 = ConstantStepSize(dt0), 1 = PIDController */
+  int64_t max_steps; /* bound on step attempts per orbit (accepted + rejected) */
+  double dt0;        /* constant step; for PID the initial step (<= 0: automatic selection) */
+  double rtol, atol;
+  double dtmin, dtmax; /* <= 0 means None */
+  double pcoeff, icoeff, dcoeff;
+  double safety, factormin, factormax;
+  int32_t force_dtmin;
+  int32_t reserved; /* must be 0 */
+} gal_solver_config;
+
+/* Scratch bytes gal_integrate needs for n orbits (work-queue counters). */
+GAL_API gal_status gal_integrate_workspace_size(const gal_solver_config* cfg, int64_t n, size_t* bytes);
+
+/* Integrate n orbits from t0[i] to t1[i] (t1 < t0 integrates backwards) and
+ * write the state at each orbit's save times. Replaces diffrax.diffeqsolve with
+ * SaveAt(ts=...) as driven by galax's Integrator / OrbitSolver
+ * (src/galax/dynamics/_src/legacy/integrator.py:179-245, orbit/solver.py:774-803),
+ * one independent controller per orbit (the per-orbit dispatch of
+ * legacy/integrator.py:449-527).
+ *
+ * y0        : [6][n] initial states at t0
+ * t0, t1    : [n]
+ * save_offsets : NULL  -> every orbit uses save_ts[0..n_saves) and out is [6][n_saves][n]
+ *                !NULL -> [n+1] CSR offsets into save_ts; n_saves must equal save_offsets[n]
+ *                         (the total) and out is [6][n_saves]
+ * save_ts   : save times, increasing along the direction of integration, within [t0, t1]
+ * out       : saved states; saves never reached (see status) are NaN
+ * status    : [n] gal_orbit_status (may be NULL)
+ * steps     : [n] accepted steps per orbit (may be NULL)
+ * order     : optional [n] permutation: the work queue hands orbits out in this order
+ * workspace : device scratch of at least gal_integrate_workspace_size bytes */
+GAL_API gal_status gal_integrate(const gal_potential* pot, const gal_solver_config* cfg, const double* y0, const double* t0,
+                         const double* t1, const int64_t* save_offsets, const double* save_ts, int64_t n_saves,
+                         double* out, int32_t* status, int64_t* steps, const int32_t* order, int64_t n,
+                         void* workspace, size_t workspace_bytes, gal_stream_t stream);
+
+/* Launch shape used by gal_integrate (0 = automatic). Tunable per method. */
+GAL_API gal_status gal_set_launch(int32_t method, int32_t adaptive, int32_t block_threads, int32_t blocks_per_sm);
+
+/* ------------------------------------------------------------------ adjoint */
+/* Scratch bytes gal_adjoint needs for n orbits with checkpoints every k_ckpt steps. */
+GAL_API gal_status gal_adjoint_workspace_size(const gal_potential* pot, const gal_solver_config* cfg, double t0, double t1,
+                                      int32_t k_ckpt, int64_t n, size_t* bytes);
+
+/* Discrete adjoint of the constant-step map y(t0) -> y(t1) (cfg->adaptive must be
+ * 0; step cfg->dt0) for terminal cotangents: given lambda = dL/dy(t1) [6][n],
+ * returns the final states yT [6][n], dL/dy0 [6][n] and dL/d(m, l1, l2) for
+ * every component, summed over orbits, [ncomp][3]. The forward pass stores the
+ * state every k_ckpt steps; the reverse pass recomputes each segment from its
+ * checkpoint. Replaces reverse-mode differentiation through diffeqsolve with
+ * RecursiveCheckpointAdjoint (src/galax/dynamics/_src/orbit/solver.py:99-108)
+ * and the forward-mode jacfwd path (ForwardMode, orbit/solver.py:133).
+ * If lambda is NULL, the loss L = sum |yT - target|^2 is used (target [6][n]). */
+GAL_API gal_status gal_adjoint(const gal_potential* pot, const gal_solver_config* cfg, const double* y0, double t0,
+                       double t1, const double* lambda, const double* target, double* yT, double* grad_y0,
+                       double* grad_params, int32_t k_ckpt, int64_t n, void* workspace, size_t workspace_bytes,
+                       gal_stream_t stream);
+
+/* ------------------------------------------------------------------ utilities */
+/* Copy the library's Butcher tableau (c[13], a[13][13], b[13], e[13] = b - bhat);
+ * returns the number of stages, or 0 for an unknown method. Host only. */
+GAL_API int32_t gal_tableau(int32_t method, double* c, double* a, double* b, double* e);
+/* FP64 FMA throughput probe: runs `iters` dependent-chain FMAs on every thread of
+ * a full-device grid and writes the elapsed device time (ms) to *ms. Used to
+ * measure the chip's FP64 peak for roofline reporting. */
+GAL_API gal_status gal_fp64_peak_probe(int64_t iters, double* ms, double* flops, gal_stream_t stream);
+GAL_API const char* gal_status_string(int32_t status);
+GAL_API const char* gal_last_error(void);
+GAL_API int32_t gal_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GALAX_GB300_H */

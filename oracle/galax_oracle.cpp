@@ -590,6 +590,7 @@ static SolveOut solve_group(const Pot& P, const OrcSolverCfg& cfg, const double*
     // diffrax _clip_to_end
     if (next_t1 > tau1 - tol) next_t1 = keep ? tau1 : tprev + 0.5 * (tau1 - tprev);
     tnext = next_t1;
+    if (R.status == ORC_DT_MIN) break;  // an unsuccessful result ends diffrax's loop after this step
   }
   if (R.status == ORC_OK && tprev < tau1) R.status = ORC_MAX_STEPS;
   // Unreached saves stay NaN.

@@ -1,0 +1,136 @@
+"""The C-ABI library without a GPU: it loads, exports every symbol the header
+declares, and carries the same tableaux as the oracle (host-only calls)."""
+
+from __future__ import annotations
+
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+ROOT = Path(__file__).resolve().parents[1]
+HEADER = ROOT / "include" / "galax_gb300.h"
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from galax_gb300 import _lib
+    from galax_gb300.build import build
+
+    build()
+    return _lib.load()
+
+
+def declared_symbols() -> list[str]:
+    text = HEADER.read_text()
+    return re.findall(r"^GAL_API\s+[\w\s\*]+?\b(gal_\w+)\(", text, flags=re.M)
+
+
+def test_header_declares_the_api():
+    syms = declared_symbols()
+    assert len(syms) >= 19
+    for s in ("gal_potential_create", "gal_eval_gradient", "gal_integrate", "gal_adjoint"):
+        assert s in syms
+
+
+def test_library_exports_every_declared_symbol(lib):
+    from galax_gb300 import _lib
+
+    for s in declared_symbols():
+        assert hasattr(lib, s), s
+        assert s in _lib.SIGNATURES, f"{s} has no ctypes signature"
+
+
+def test_abi_version_and_status_strings(lib):
+    assert lib.gal_abi_version() == 1
+    assert lib.gal_status_string(0) == b"ok"
+    assert lib.gal_status_string(4) == b"workspace too small"
+
+
+@pytest.mark.parametrize("method", [5, 8])
+def test_tableau_matches_oracle_bitwise(lib, method):
+    c = np.zeros(13); a = np.zeros(169); b = np.zeros(13); e = np.zeros(13)
+    s = lib.gal_tableau(method, c.ctypes.data, a.ctypes.data, b.ctypes.data, e.ctypes.data)
+    oc, oa, ob, oe = O.tableau(method)
+    assert s == len(oc)
+    assert np.array_equal(c[:s], oc)
+    assert np.array_equal(a.reshape(13, 13)[:s, :s], oa)
+    assert np.array_equal(b[:s], ob)
+    assert np.array_equal(e[:s], oe)
+    assert lib.gal_tableau(7, c.ctypes.data, a.ctypes.data, b.ctypes.data, e.ctypes.data) == 0
+
+
+def test_struct_layouts_match_oracle():
+    from galax_gb300 import _lib
+
+    assert _lib.COMPONENT_DTYPE == O.COMP_DTYPE
+    assert C.sizeof(_lib.SolverConfig) == C.sizeof(O.SolverCfg)
+
+
+def test_validation_without_gpu(lib):
+    """Argument checks run on the host and fail before any device work."""
+    from galax_gb300 import _lib
+
+    h = C.c_void_p()
+    bad = np.zeros(1, _lib.COMPONENT_DTYPE)
+    bad[0]["kind"] = 9
+    assert lib.gal_potential_create(bad.ctypes.data, 1, 1.0, C.byref(h)) == 2
+    assert b"unsupported" in lib.gal_last_error()
+    bad[0]["kind"] = _lib.GAL_NFW
+    bad[0]["m"] = 1.0
+    bad[0]["l1"] = 0.0
+    assert lib.gal_potential_create(bad.ctypes.data, 1, 1.0, C.byref(h)) == 1
+    assert lib.gal_potential_create(bad.ctypes.data, 0, 1.0, C.byref(h)) == 1
+    nbytes = C.c_size_t()
+    cfg = _lib.solver_config(8, False, dt0=1.0)
+    assert lib.gal_integrate_workspace_size(C.byref(cfg), 10, C.byref(nbytes)) == 0 and nbytes.value >= 8
+    assert lib.gal_set_launch(8, 0, 100, 0) == 1  # not a multiple of 32
+
+
+def test_python_api_rejects_unsupported_inputs():
+    import galax_gb300 as gx
+
+    with pytest.raises(NotImplementedError):
+        gx.HernquistPotential(m_tot=1e12, r_s=5.0, units="solarsystem")
+    with pytest.raises(NotImplementedError):
+        gx.HernquistPotential(m_tot=lambda t: 1e12, r_s=5.0)
+    with pytest.raises(NotImplementedError):
+        gx.Integrator(solver="Tsit5").config()
+    with pytest.raises(NotImplementedError):
+        gx.PIDController(rtol=1e-7, atol=1e-7, jump_ts=[1.0])
+    mw = gx.MilkyWayPotential()
+    arr = mw.component_array()
+    assert list(arr["kind"]) == [2, 3, 1, 1]
+    np.testing.assert_array_equal(arr, O.milky_way())
+
+
+def test_workloads_follow_their_distributions():
+    from galax_gb300 import workloads as W
+
+    grad = lambda x: O.gradient(O.milky_way(), x)  # noqa: E731
+    y = W.disk_like_ics(grad, 2000, seed=0)
+    r = np.linalg.norm(y[:, :3], axis=1)
+    assert r.min() >= 4 and r.max() <= 20
+    vz_kms = y[:, 5] / W.KMS
+    assert 10 < np.std(vz_kms) < 40
+    b = W.uneven_ics(grad, 3000, seed=1)
+    ns = np.diff(b.save_offsets)
+    assert ns.min() >= 10 and ns.max() <= 1000
+    assert np.all(b.t1 >= 100 - 1e-9) and np.all(b.t1 <= 5000 + 1e-9)
+    assert np.allclose(b.save_ts[b.save_offsets[1:] - 1], b.t1)
+    assert np.all(b.save_ts[b.save_offsets[:-1]] == 0)
+    r = np.linalg.norm(b.y0[:, :3], axis=1)
+    assert np.allclose(np.sum(b.y0[:, :3] * b.y0[:, 3:], axis=1) / r, 0, atol=1e-12)  # tangential
+
+
+def test_flop_constants_match_counted_oracle():
+    from galax_gb300 import flops
+
+    for method in (5, 8):
+        g, s = O.count_ops(O.milky_way(), method)
+        assert sum(g.values()) == flops.GRADIENT_FLOPS_MW
+        assert sum(s.values()) == flops.STEP_FLOPS_MW[method]

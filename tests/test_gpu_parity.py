@@ -1,0 +1,328 @@
+"""Parity of the CUDA library with the CPU oracle (needs a GB300).
+
+Every case runs the same seeded inputs through the C ABI (via the package's
+ctypes front end) and through the oracle, and compares with the tolerances the
+orbit path promises: 1e-9 relative in position and velocity for fixed steps,
+10 x rtol for adaptive runs (per-orbit controllers on both sides, so most
+orbits agree far tighter), rounding level for potential evaluation.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests._helpers import golden_cfg, golden_comps, golden_save_ts
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def gx():
+    import torch
+
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA device")
+    from galax_gb300.build import build
+
+    build()
+    import galax_gb300
+
+    return galax_gb300
+
+
+def _pot(gx, comps):
+    from galax_gb300.potential import from_component_array
+
+    return from_component_array(comps)
+
+
+def _rel(a, b):
+    """max over points of |a-b| / |b| per 3-vector block (position, velocity)."""
+    a = np.asarray(a).reshape(-1, 6)
+    b = np.asarray(b).reshape(-1, 6)
+    out = 0.0
+    for sl in (slice(0, 3), slice(3, 6)):
+        d = np.linalg.norm(a[:, sl] - b[:, sl], axis=1)
+        s = np.linalg.norm(b[:, sl], axis=1)
+        out = max(out, float(np.max(d / np.maximum(s, 1e-300))))
+    return out
+
+
+def _rel_each(a, b):
+    a = np.asarray(a).reshape(-1, 6)
+    b = np.asarray(b).reshape(-1, 6)
+    r = []
+    for sl in (slice(0, 3), slice(3, 6)):
+        r.append(np.linalg.norm(a[:, sl] - b[:, sl], axis=1) / np.maximum(np.linalg.norm(b[:, sl], axis=1), 1e-300))
+    return np.maximum(*r)
+
+
+def _mixed_points(n, seed):
+    rng = np.random.default_rng(seed)
+    return rng.normal(size=(n, 3)) * np.exp(rng.uniform(np.log(0.02), np.log(150), (n, 1)))
+
+
+def _kinds():
+    return O.comps([
+        (O.KEPLER, 3e10, 0, 0, (0.3, -0.2, 0.1)),
+        (O.HERNQUIST, 5e9, 1.0, 0),
+        (O.MIYAMOTO_NAGAI, 6.8e10, 3.0, 0.28),
+        (O.NFW, 5.4e11, 15.62, 0),
+        (O.PLUMMER, 1e8, 0.5, 0, (4.0, 1.0, -2.0)),
+    ])
+
+
+def _subhalos(n=512, seed=3):
+    from galax_gb300 import workloads as W
+
+    m, b, c = W.subhalo_table(seed, n)
+    return np.concatenate([O.milky_way(), O.comps([(O.PLUMMER, m[i], b[i], 0, tuple(c[i])) for i in range(n)])])
+
+
+# ------------------------------------------------------------------ evaluation
+@pytest.mark.parametrize("which", ["kinds", "milky_way", "subhalos"])
+def test_potential_gradient_hessian_match_oracle(gx, which):
+    comps = {"kinds": _kinds, "milky_way": O.milky_way, "subhalos": _subhalos}[which]()
+    pot = _pot(gx, comps)
+    x = _mixed_points(4096, 11)
+    np.testing.assert_allclose(pot.potential(x), O.potential(comps, x), rtol=1e-13, atol=0)
+    g_ref = O.gradient(comps, x)
+    g = pot.gradient(x)
+    scale = np.linalg.norm(g_ref, axis=1, keepdims=True)
+    assert np.max(np.abs(g - g_ref) / scale) < 1e-13
+    np.testing.assert_array_equal(pot.acceleration(x), -g)
+    H_ref = O.hessian(comps, x)
+    Hs = np.abs(H_ref).max(axis=(1, 2), keepdims=True)
+    assert np.max(np.abs(pot.hessian(x) - H_ref) / Hs) < 1e-12
+
+
+def test_reference_potential_goldens_on_gpu(gx, goldens):
+    for name, g in goldens["potentials"].items():
+        pot = _pot(gx, golden_comps(g["params"]))
+        x = np.array([g["x"]])
+        np.testing.assert_allclose(pot.potential(x)[0], g["potential"], **g["tol"])
+        np.testing.assert_allclose(pot.gradient(x)[0], g["gradient"], **g["tol"])
+        np.testing.assert_allclose(pot.hessian(x)[0].ravel(), g["hessian"], **g["tol"])
+
+
+def test_milky_way_kernel_matches_general_table(gx):
+    mw = gx.MilkyWayPotential()
+    assert mw.is_milky_way_kernel()
+    arr = O.milky_way()[[1, 0, 2, 3]]  # same components, order the specialised kernel does not take
+    other = _pot(gx, arr)
+    assert not other.is_milky_way_kernel()
+    x = _mixed_points(8192, 12)
+    g1, g2 = mw.gradient(x), other.gradient(x)
+    assert np.max(np.abs(g1 - g2) / np.linalg.norm(g2, axis=1, keepdims=True)) < 1e-14
+
+
+def test_gradient_at_origin_is_zero(gx):
+    mw = gx.MilkyWayPotential()
+    g = mw.gradient(np.zeros((3, 3)))
+    assert np.all(g == 0)
+
+
+# ------------------------------------------------------------------ fixed step
+def _ics(n, seed):
+    from galax_gb300 import workloads as W
+
+    return W.disk_like_ics(lambda x: O.gradient(O.milky_way(), x), n, seed)
+
+
+@pytest.mark.parametrize("method,dt", [(8, 1.0), (5, 0.5)])
+def test_fixed_step_matches_oracle_within_1e9(gx, method, dt):
+    """The small plain workload: MW, 1,024 orbits, 1 Gyr, 100 uniform saves."""
+    y0 = _ics(1024, 0)
+    ts = np.linspace(0.0, 1000.0, 100)
+    integ = gx.Integrator(solver=gx.Dopri8() if method == 8 else gx.Dopri5(),
+                          stepsize_controller=gx.ConstantStepSize(), dt0=dt)
+    orb = gx.evaluate_orbit(gx.MilkyWayPotential(), y0, ts, integrator=integ)
+    assert orb.q.shape == (1024, 100, 3)
+    assert np.all(orb.steps == int(round(1000 / dt)))
+    ref, st, acc, rej = O.integrate(O.milky_way(), y0, 0.0, 1000.0, ts, O.solver_cfg(method, False, dt0=dt))
+    assert np.all(st == 0)
+    got = orb.w.reshape(-1, 6)
+    want = np.stack(ref).reshape(-1, 6)
+    assert _rel(got, want) < 1e-9
+    np.testing.assert_array_equal(orb.w[:, 0], y0)  # the first save is t0 itself
+
+
+def test_fixed_step_general_table_matches_oracle(gx):
+    comps = _kinds()
+    y0 = _ics(256, 5)
+    y0[:, :3] += 0.7  # keep clear of the Kepler point mass
+    ts = np.linspace(0.0, 300.0, 37)
+    integ = gx.Integrator(solver=gx.Dopri8(), stepsize_controller=gx.ConstantStepSize(), dt0=0.5)
+    orb = gx.evaluate_orbit(_pot(gx, comps), y0, ts, integrator=integ)
+    ref, st, *_ = O.integrate(comps, y0, 0.0, 300.0, ts, O.solver_cfg(8, False, dt0=0.5))
+    assert _rel(orb.w.reshape(-1, 6), np.stack(ref).reshape(-1, 6)) < 1e-9
+
+
+# ------------------------------------------------------------------ adaptive
+@pytest.mark.parametrize("method,rtol,atol", [(8, 1e-7, 1e-7), (5, 1e-8, 1e-10)])
+def test_adaptive_matches_oracle(gx, method, rtol, atol):
+    y0 = _ics(512, 7)
+    ts = np.linspace(0.0, 500.0, 51)
+    integ = gx.Integrator(solver=gx.Dopri8() if method == 8 else gx.Dopri5(),
+                          stepsize_controller=gx.PIDController(rtol=rtol, atol=atol), max_steps=2**16)
+    orb = gx.evaluate_orbit(gx.MilkyWayPotential(), y0, ts, integrator=integ)
+    ref, st, acc, rej = O.integrate(O.milky_way(), y0, 0.0, 500.0, ts,
+                                    O.solver_cfg(method, True, rtol=rtol, atol=atol, max_steps=2**16))
+    assert np.all(st == 0)
+    rel = _rel_each(orb.w.reshape(-1, 6), np.stack(ref).reshape(-1, 6))
+    assert rel.max() <= 10 * rtol
+    assert np.median(rel) < 1e-11  # identical step sequences: rounding-level agreement
+    same_steps = np.mean(np.asarray(orb.steps) == acc)
+    assert same_steps > 0.95
+
+
+def test_uneven_batch_csr_matches_oracle(gx):
+    """The batched uneven workload at reduced size: ragged save grids, per-orbit
+    durations, Dopri5 PID rtol=1e-8 atol=1e-10, one persistent launch."""
+    from galax_gb300 import workloads as W
+
+    b = W.uneven_ics(lambda x: O.gradient(O.milky_way(), x), 384, seed=1, tmax=800.0, smax=200)
+    integ = gx.Integrator(solver=gx.Dopri5(), stepsize_controller=gx.PIDController(rtol=1e-8, atol=1e-10),
+                          max_steps=2**16)
+    grids = [b.save_ts[b.save_offsets[i]:b.save_offsets[i + 1]] for i in range(len(b.t1))]
+    res, status, steps = gx.integrate_orbit(gx.MilkyWayPotential(), b.y0, b.t0, b.t1, grids, integrator=integ,
+                                            throw=False)
+    ref, st, acc, rej = O.integrate(O.milky_way(), b.y0, b.t0, b.t1, grids,
+                                    O.solver_cfg(5, True, rtol=1e-8, atol=1e-10, max_steps=2**16))
+    st_gpu = status.cpu().numpy()
+    np.testing.assert_array_equal(st_gpu, st)
+    ok = st == 0
+    got = np.concatenate([res[i].cpu().numpy() for i in np.nonzero(ok)[0]])
+    want = np.concatenate([ref[i] for i in np.nonzero(ok)[0]])
+    rel = _rel_each(got, want)
+    assert rel.max() <= 10 * 1e-8
+    assert np.median(rel) < 1e-11
+    # orbits that ran out of steps report it and leave unreached saves NaN
+    for i in np.nonzero(~ok)[0]:
+        assert np.isnan(res[i].cpu().numpy()[-1]).all()
+
+
+# ------------------------------------------------------------------ reference KATs on the GPU
+@pytest.mark.parametrize("name", ["dopri8_single_step", "dopri8_pid_solve_220kms", "dopri8_pid_solve_array",
+                                  "nfw_integrate_orbit", "legacy_integrator_1gyr"])
+def test_reference_kats_on_gpu(gx, goldens, name):
+    g = goldens["orbits"][name]
+    comps = golden_comps(g["potential"])
+    cfgd = dict(g["solver"])
+    method = cfgd.pop("method")
+    adaptive = cfgd.pop("adaptive")
+    if adaptive:
+        ctrl = gx.PIDController(rtol=cfgd["rtol"], atol=cfgd["atol"], dtmin=cfgd.get("dtmin"))
+        integ = gx.Integrator(solver=gx.Dopri8() if method == 8 else gx.Dopri5(), stepsize_controller=ctrl)
+    else:
+        integ = gx.Integrator(solver=gx.Dopri8(), stepsize_controller=gx.ConstantStepSize(), dt0=cfgd["dt0"])
+    ts = golden_save_ts(g)
+    rows = g.get("rows", [-1])
+    orb = gx.evaluate_orbit(_pot(gx, comps), np.array(g["y0"], float), ts, integrator=integ)
+    got = orb.w[:, rows].reshape(-1, 6)
+    want = np.concatenate([np.asarray(g["expect_q"]), np.asarray(g["expect_p"])], axis=-1).reshape(-1, 6)
+    np.testing.assert_allclose(got, want, rtol=0, atol=0.5 * 10.0 ** (-g["digits"]) + 1e-9)
+
+
+# ------------------------------------------------------------------ semantics and edge cases
+def test_reverse_time_round_trip(gx):
+    y0 = _ics(128, 9)
+    integ = gx.Integrator(solver=gx.Dopri8(), stepsize_controller=gx.ConstantStepSize(), dt0=0.5)
+    mw = gx.MilkyWayPotential()
+    fwd = gx.evaluate_orbit(mw, y0, np.array([0.0, 200.0]), integrator=integ).w[:, -1]
+    back = gx.evaluate_orbit(mw, fwd, np.array([200.0, 0.0]), integrator=integ).w[:, -1]
+    assert _rel(back, y0) < 1e-10
+    ref, *_ = O.integrate(O.milky_way(), fwd, 200.0, 0.0, np.array([0.0]), O.solver_cfg(8, False, dt0=0.5))
+    assert _rel(back, np.stack(ref).reshape(-1, 6)) < 1e-12
+
+
+def test_two_phase_evaluate_orbit(gx):
+    """w0 carrying its own time is first moved to t[0] (galax legacy/funcs.py:186-213)."""
+    y0 = _ics(64, 13)
+    tw = np.linspace(-150.0, -50.0, 64)
+    ts = np.linspace(0.0, 300.0, 31)
+    integ = gx.Integrator(solver=gx.Dopri8(), stepsize_controller=gx.PIDController(rtol=1e-8, atol=1e-8))
+    w0 = gx.PhaseSpaceCoordinate(q=y0[:, :3], p=y0[:, 3:], t=tw)
+    orb = gx.evaluate_orbit(gx.MilkyWayPotential(), w0, ts, integrator=integ)
+    cfg = O.solver_cfg(8, True, rtol=1e-8, atol=1e-8)
+    mid, *_ = O.integrate(O.milky_way(), y0, tw, 0.0, np.array([0.0]), cfg)
+    ref, *_ = O.integrate(O.milky_way(), np.stack(mid).reshape(-1, 6), 0.0, 300.0, ts, cfg)
+    assert _rel_each(orb.w.reshape(-1, 6), np.stack(ref).reshape(-1, 6)).max() < 1e-7
+
+
+def test_edge_cases(gx):
+    import torch
+
+    mw = gx.MilkyWayPotential()
+    y0 = _ics(8, 21)
+    # t0 == t1: every save is the initial state
+    integ = gx.Integrator(solver=gx.Dopri8(), stepsize_controller=gx.ConstantStepSize(), dt0=1.0)
+    orb = gx.evaluate_orbit(mw, y0, np.array([5.0, 5.0]), integrator=integ)
+    np.testing.assert_array_equal(orb.w[:, 1], y0)
+    # max_steps: status, unreached saves NaN, no exception with throw=False
+    integ = gx.Integrator(solver=gx.Dopri5(), stepsize_controller=gx.PIDController(rtol=1e-8, atol=1e-10),
+                          max_steps=5)
+    orb = gx.evaluate_orbit(mw, y0, np.linspace(0, 500, 5), integrator=integ, throw=False)
+    assert np.all(orb.status == 1) and np.all(np.isnan(orb.w[:, -1]))
+    with pytest.raises(gx.GalaxGB300Error, match="max_steps_reached"):
+        gx.evaluate_orbit(mw, y0, np.linspace(0, 500, 5), integrator=integ)
+    # a non-finite start stops with status 3
+    bad = y0.copy()
+    bad[3, 0] = np.nan
+    integ = gx.Integrator(solver=gx.Dopri8(), stepsize_controller=gx.ConstantStepSize(), dt0=1.0)
+    orb = gx.evaluate_orbit(mw, bad, np.linspace(0, 50, 3), integrator=integ, throw=False)
+    assert orb.status[3] == 3 and np.all(orb.status[[0, 1, 2, 4, 5, 6, 7]] == 0)
+    # empty batch
+    from galax_gb300.dynamics import integrate
+
+    out, st, steps = integrate(mw, np.zeros((0, 6)), 0.0, 1.0, np.array([1.0]),
+                               gx.Integrator(stepsize_controller=gx.ConstantStepSize(), dt0=0.5).config())
+    assert out.shape == (6, 1, 0)
+    torch.cuda.synchronize()
+
+
+def test_launch_shapes_give_identical_results(gx):
+    """The work queue makes results independent of block size and grid."""
+    from galax_gb300 import _lib
+    from galax_gb300.dynamics import integrate
+
+    L = _lib.load()
+    mw = gx.MilkyWayPotential()
+    y0 = _ics(3000, 23)
+    cfg = gx.Integrator(solver=gx.Dopri5(), stepsize_controller=gx.PIDController(rtol=1e-8, atol=1e-10)).config()
+    outs = []
+    for block, per_sm in ((128, 0), (64, 1), (256, 2), (32, 3)):
+        _lib.check(L.gal_set_launch(5, 1, block, per_sm), "gal_set_launch")
+        out, st, steps = integrate(mw, y0, 0.0, 300.0, np.linspace(0, 300, 11), cfg)
+        outs.append(out.cpu().numpy())
+    _lib.check(L.gal_set_launch(5, 1, 0, 0), "gal_set_launch")
+    for o in outs[1:]:
+        np.testing.assert_array_equal(o, outs[0])
+
+
+# ------------------------------------------------------------------ adjoint
+@pytest.mark.parametrize("which", ["milky_way", "table"])
+def test_adjoint_matches_oracle(gx, which):
+    import torch
+
+    from galax_gb300.adjoint import orbit_adjoint
+
+    comps = O.milky_way() if which == "milky_way" else np.concatenate(
+        [O.milky_way(), O.comps([(O.PLUMMER, 1e9, 0.8, 0, (6.0, 2.0, 0.5))])])
+    pot = _pot(gx, comps)
+    y0 = _ics(96, 31)
+    rng = np.random.default_rng(20)
+    cfg = O.solver_cfg(8, False, dt0=1.0)
+    yT_ref, *_ = O.integrate(comps, y0, 0.0, 150.0, np.array([150.0]), cfg)
+    target = np.stack(yT_ref).reshape(-1, 6) + np.concatenate(
+        [rng.normal(0, 0.1, (96, 3)), rng.normal(0, 2 * 0.001022712165045695, (96, 3))], axis=1)
+    yT_o, gy_o, gp_o, L_o = O.adjoint_fixed(comps, y0, 0.0, 150.0, target, cfg)
+    res = orbit_adjoint(pot, y0, 0.0, 150.0, dt=1.0, target=target, method=8, k_ckpt=16)
+    torch.cuda.synchronize()
+    assert _rel(res.yT, yT_o) < 1e-12
+    np.testing.assert_allclose(res.grad_y0, gy_o, rtol=1e-8, atol=1e-12 * np.abs(gy_o).max())
+    mask = gp_o != 0
+    np.testing.assert_allclose(res.grad_params[mask], gp_o[mask], rtol=1e-8)
+    assert abs(res.loss - L_o) <= 1e-10 * L_o

@@ -44,7 +44,7 @@ class SolverConfig(C.Structure):
         ("factormin", C.c_double),
         ("factormax", C.c_double),
         ("force_dtmin", C.c_int32),
-        ("reserved", C.c_int32),
+        ("schedule", C.c_int32),
     ]
 
 
@@ -67,7 +67,7 @@ SIGNATURES = {
     "gal_integrate_workspace_size": (C.c_int, [C.POINTER(SolverConfig), C.c_int64, C.POINTER(C.c_size_t)]),
     "gal_integrate": (C.c_int, [C.c_void_p, C.POINTER(SolverConfig), _DP, _DP, _DP, _I64P, _DP, C.c_int64, _DP,
                                 _I32P, _I64P, _I32P, C.c_int64, _VP, C.c_size_t, C.c_void_p]),
-    "gal_set_launch": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
+    "gal_set_launch": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
     "gal_adjoint_workspace_size": (C.c_int, [C.c_void_p, C.POINTER(SolverConfig), C.c_double, C.c_double,
                                              C.c_int32, C.c_int64, C.POINTER(C.c_size_t)]),
     "gal_adjoint": (C.c_int, [C.c_void_p, C.POINTER(SolverConfig), _DP, C.c_double, C.c_double, _DP, _DP, _DP, _DP,
@@ -128,9 +128,10 @@ def solver_config(
     factormax: float = 10.0,
     force_dtmin: bool = True,
     max_steps: int = 2**62,
+    schedule: bool = False,
 ) -> SolverConfig:
     return SolverConfig(
         int(method), int(bool(adaptive)), int(max_steps), float(dt0 or 0.0), float(rtol), float(atol),
         float(dtmin or 0.0), float(dtmax or 0.0), float(pcoeff), float(icoeff), float(dcoeff), float(safety),
-        float(factormin), float(factormax), int(bool(force_dtmin)), 0,
+        float(factormin), float(factormax), int(bool(force_dtmin)), int(bool(schedule)),
     )

@@ -16,7 +16,7 @@
 namespace gal {
 
 thread_local std::string g_last_error;
-static LaunchShape g_shape[2][2] = {{{0, 0}, {0, 0}}, {{0, 0}, {0, 0}}};  // [method 5/8][adaptive]
+static LaunchShape g_shape[2][2] = {{{0, 0, 0}, {0, 0, 0}}, {{0, 0, 0}, {0, 0, 0}}};  // [method 5/8][adaptive]
 
 gal_status fail(gal_status st, const std::string& msg) {
   g_last_error = msg;
@@ -165,7 +165,7 @@ __global__ void k_fp64_probe(int64_t iters, double seed, double* sink) {
 gal_status validate_cfg(const gal_solver_config* c) {
   if (!c) return fail(GAL_ERR_INVALID_ARGUMENT, "config is NULL");
   if (c->method != 5 && c->method != 8) return fail(GAL_ERR_UNSUPPORTED, "method must be 5 (Dopri5) or 8 (Dopri8)");
-  if (c->reserved != 0) return fail(GAL_ERR_INVALID_ARGUMENT, "reserved must be 0");
+  if (c->schedule != 0 && c->schedule != 1) return fail(GAL_ERR_INVALID_ARGUMENT, "schedule must be 0 or 1");
   if (c->max_steps < 1) return fail(GAL_ERR_INVALID_ARGUMENT, "max_steps must be >= 1");
   if (!c->adaptive && !(c->dt0 > 0.0)) return fail(GAL_ERR_INVALID_ARGUMENT, "constant step needs dt0 > 0");
   if (c->adaptive) {
@@ -175,6 +175,62 @@ gal_status validate_cfg(const gal_solver_config* c) {
       return fail(GAL_ERR_INVALID_ARGUMENT, "bad safety/factormin/factormax");
   }
   return GAL_OK;
+}
+
+// ---- two-phase schedule: order parked orbits by estimated remaining work
+constexpr int kBuckets = 64;
+constexpr double kSplitFrac = 0.1;
+
+__global__ void k_sched_keys(const OrbitResume* __restrict__ r, int64_t n, unsigned* __restrict__ hist,
+                             int* __restrict__ bucket) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    if (r[i].paused) {
+      const double p = r[i].progress;
+      const double key = (double)r[i].nsteps * (1.0 - p) / fmax(p, 1e-12);
+      int b = (int)(2.0f * log2f(1.0f + (float)key));  // half-octave buckets
+      b = b < 0 ? 0 : (b >= kBuckets ? kBuckets - 1 : b);
+      bucket[i] = b;
+      atomicAdd(&hist[b], 1u);
+    } else {
+      bucket[i] = -1;
+    }
+  }
+}
+
+__global__ void k_sched_scan(const unsigned* __restrict__ hist, unsigned* __restrict__ cursor,
+                             unsigned long long* __restrict__ qlen) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    unsigned acc = 0;
+    for (int b = kBuckets - 1; b >= 0; --b) {  // most remaining work first
+      cursor[b] = acc;
+      acc += hist[b];
+    }
+    *qlen = acc;
+  }
+}
+
+__global__ void k_sched_scatter(const int* __restrict__ bucket, int64_t n, unsigned* __restrict__ cursor,
+                                int32_t* __restrict__ order) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int b = bucket[i];
+    if (b >= 0) order[atomicAdd(&cursor[b], 1u)] = (int32_t)i;
+  }
+}
+
+struct SchedLayout {
+  size_t header, resume, bucket, order, total;
+};
+
+static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+static SchedLayout sched_layout(int64_t n) {
+  SchedLayout L{};
+  L.header = 0;  // [0] queue counter, [8] queue length, [16] hist[64], [272] cursor[64]
+  L.resume = 1024;
+  L.bucket = L.resume + align256(sizeof(OrbitResume) * (size_t)n);
+  L.order = L.bucket + align256(sizeof(int) * (size_t)n);
+  L.total = L.order + align256(sizeof(int32_t) * (size_t)n);
+  return L;
 }
 
 static void grid_for(int64_t n, int block, unsigned* grid) {
@@ -331,18 +387,17 @@ gal_status gal_eval_hessian(const gal_potential* p, const double* x, double t, i
 }
 
 gal_status gal_integrate_workspace_size(const gal_solver_config* cfg, int64_t n, size_t* bytes) {
-  (void)cfg;
-  (void)n;
-  if (!bytes) return fail(GAL_ERR_INVALID_ARGUMENT, "bytes is NULL");
-  *bytes = 256;  // one 8-byte work-queue counter, padded
+  if (!bytes || !cfg || n < 0) return fail(GAL_ERR_INVALID_ARGUMENT, "bad workspace query");
+  *bytes = cfg->schedule ? sched_layout(n).total : 256;  // one 8-byte work-queue counter, padded
   return GAL_OK;
 }
 
-gal_status gal_set_launch(int32_t method, int32_t adaptive, int32_t block_threads, int32_t blocks_per_sm) {
+gal_status gal_set_launch(int32_t method, int32_t adaptive, int32_t block_threads, int32_t blocks_per_sm,
+                          int32_t variant) {
   if ((method != 5 && method != 8) || block_threads < 0 || block_threads > 256 || (block_threads % 32) ||
-      blocks_per_sm < 0)
+      blocks_per_sm < 0 || variant < 0 || variant > 1)
     return fail(GAL_ERR_INVALID_ARGUMENT, "bad launch shape");
-  g_shape[method == 8][adaptive ? 1 : 0] = LaunchShape{block_threads, blocks_per_sm};
+  g_shape[method == 8][adaptive ? 1 : 0] = LaunchShape{block_threads, blocks_per_sm, variant};
   return GAL_OK;
 }
 
@@ -377,6 +432,7 @@ gal_status gal_integrate(const gal_potential* p, const gal_solver_config* cfg, c
   a.c1 = (cfg->icoeff + cfg->pcoeff + cfg->dcoeff) / morder;
   a.c2 = -(cfg->pcoeff + 2.0 * cfg->dcoeff) / morder;
   a.c3 = cfg->dcoeff / morder;
+  a.i_controller = (cfg->pcoeff == 0.0 && cfg->dcoeff == 0.0 && cfg->icoeff == 1.0) ? 1 : 0;
   a.safety = cfg->safety;
   a.factormin = cfg->factormin;
   a.factormax = cfg->factormax;
@@ -392,15 +448,51 @@ gal_status gal_integrate(const gal_potential* p, const gal_solver_config* cfg, c
   a.steps = steps;
   a.order = order;
   a.n = n;
-  a.queue = reinterpret_cast<unsigned long long*>(workspace);
-  cudaError_t e = cudaMemsetAsync(workspace, 0, sizeof(unsigned long long), (cudaStream_t)stream);
-  if (e != cudaSuccess) return cuda_fail(e, "clearing the work queue");
+  cudaStream_t s = (cudaStream_t)stream;
+  char* ws = static_cast<char*>(workspace);
+  a.queue = reinterpret_cast<unsigned long long*>(ws);
+  a.phase = 0;
+  a.split_frac = 0.0;
+  a.resume = nullptr;
+  a.queue_len = nullptr;
   const LaunchShape shape = g_shape[cfg->method == 8][cfg->adaptive ? 1 : 0];
-  if (cfg->method == 8)
-    e = launch_integrate_dopri8(a, p->is_mw, p->mw, p->d_comps, p->n, shape, (cudaStream_t)stream);
-  else
-    e = launch_integrate_dopri5(a, p->is_mw, p->mw, p->d_comps, p->n, shape, (cudaStream_t)stream);
-  return e == cudaSuccess ? GAL_OK : cuda_fail(e, "integrate kernel launch");
+  auto launch = [&]() {
+    return cfg->method == 8 ? launch_integrate_dopri8(a, p->is_mw, p->mw, p->d_comps, p->n, shape, s)
+                            : launch_integrate_dopri5(a, p->is_mw, p->mw, p->d_comps, p->n, shape, s);
+  };
+  if (!cfg->schedule) {
+    cudaError_t e = cudaMemsetAsync(ws, 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return cuda_fail(e, "clearing the work queue");
+    e = launch();
+    return e == cudaSuccess ? GAL_OK : cuda_fail(e, "integrate kernel launch");
+  }
+  // two phases: first tenth of every span, then longest remaining work first
+  const SchedLayout L = sched_layout(n);
+  auto* qlen = reinterpret_cast<unsigned long long*>(ws + 8);
+  auto* hist = reinterpret_cast<unsigned*>(ws + 16);
+  auto* cursor = reinterpret_cast<unsigned*>(ws + 16 + 4 * kBuckets);
+  auto* resume = reinterpret_cast<OrbitResume*>(ws + L.resume);
+  auto* bucket = reinterpret_cast<int*>(ws + L.bucket);
+  auto* order2 = reinterpret_cast<int32_t*>(ws + L.order);
+  cudaError_t e = cudaMemsetAsync(ws, 0, L.resume + sizeof(OrbitResume) * (size_t)n, s);
+  if (e != cudaSuccess) return cuda_fail(e, "clearing the schedule scratch");
+  a.split_frac = kSplitFrac;
+  a.resume = resume;
+  e = launch();
+  if (e != cudaSuccess) return cuda_fail(e, "integrate kernel launch (first pass)");
+  unsigned grid;
+  grid_for(n, 256, &grid);
+  k_sched_keys<<<grid, 256, 0, s>>>(resume, n, hist, bucket);
+  k_sched_scan<<<1, 32, 0, s>>>(hist, cursor, qlen);
+  k_sched_scatter<<<grid, 256, 0, s>>>(bucket, n, cursor, order2);
+  e = cudaMemsetAsync(ws, 0, sizeof(unsigned long long), s);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "ordering the parked orbits");
+  a.phase = 1;
+  a.order = order2;
+  a.queue_len = qlen;
+  e = launch();
+  return e == cudaSuccess ? GAL_OK : cuda_fail(e, "integrate kernel launch (second pass)");
 }
 
 int32_t gal_tableau(int32_t method, double* c, double* a, double* b, double* e) {

@@ -36,6 +36,16 @@ namespace gal {
 
 enum { ORBIT_OK = 0, ORBIT_MAX_STEPS = 1, ORBIT_DT_MIN = 2, ORBIT_NONFINITE = 3 };
 
+// Everything needed to continue an orbit exactly where a first pass parked it
+// (state, step times, controller memory, counters, save cursor). 128 bytes.
+struct OrbitResume {
+  double y[6];
+  double tau, tnext, prev_inv, prev_prev_inv, progress;
+  int64_t nsteps, naccepted, save_i;
+  int32_t at_dtmin, status, paused, pad;
+};
+static_assert(sizeof(OrbitResume) == 128, "OrbitResume layout");
+
 struct IntegrateArgs {
   // solver
   int32_t adaptive;
@@ -43,6 +53,7 @@ struct IntegrateArgs {
   int64_t max_steps;
   double dt0, rtol, atol, dtmin, dtmax;
   double c1, c2, c3;  // PID exponents (i+p+d)/order, -(p+2d)/order, d/order
+  int32_t i_controller;  // 1 when pcoeff = dcoeff = 0 and icoeff = 1 (diffrax's default)
   double safety, factormin, factormax;
   // data
   const double* y0;  // [6][n]
@@ -58,6 +69,12 @@ struct IntegrateArgs {
   const int32_t* order;
   int64_t n;
   unsigned long long* queue;  // work-queue counter (scratch)
+  // two-phase schedule: phase 0 parks every orbit once it has covered split_frac
+  // of its span; phase 1 resumes the parked orbits from `resume` in `order`
+  int32_t phase;
+  double split_frac;                     // <= 0: single pass
+  OrbitResume* resume;                   // [n]
+  const unsigned long long* queue_len;   // phase 1: number of entries in order (device)
 };
 
 // Hamiltonian field without the time-direction sign: F = (p, -grad Phi(q)).
@@ -151,7 +168,7 @@ struct OrbitState {
   int64_t save_i, save_end;
   int64_t nsteps, naccepted;
   double y[6], F0[6];
-  double tau, tnext, tau1, dir;
+  double tau, tnext, tau0, tau1, dir;
   double prev_inv, prev_prev_inv;
   int32_t at_dtmin;
   int32_t status;      // sticky: set when the controller reports dt < dtmin
@@ -216,29 +233,46 @@ __device__ __forceinline__ double initial_step(const IntegrateArgs& a, const Pot
 // Returns false when the queue is empty.
 template <class TB, class Pot>
 __device__ __forceinline__ bool start_orbit(const IntegrateArgs& a, const Pot& pot, OrbitState& s) {
+  const unsigned long long qlen = a.queue_len ? *a.queue_len : (unsigned long long)a.n;
   while (true) {
     const unsigned long long k = atomicAdd(a.queue, 1ULL);
-    if ((int64_t)k >= a.n) return false;
+    if (k >= qlen) return false;
     const int64_t o = a.order ? (int64_t)a.order[k] : (int64_t)k;
     s.orbit = o;
-#pragma unroll
-    for (int j = 0; j < 6; ++j) s.y[j] = a.y0[j * a.n + o];
     const double t0 = a.t0[o], t1 = a.t1[o];
     if (a.save_offsets) {
       s.save_base = a.save_offsets[o];
-      s.save_i = 0;
       s.save_end = a.save_offsets[o + 1] - s.save_base;
     } else {
       s.save_base = o;
-      s.save_i = 0;
       s.save_end = a.n_saves;
     }
-    s.nsteps = 0;
-    s.naccepted = 0;
     s.pending = 0;
     s.dir = (t0 < t1) ? 1.0 : -1.0;
-    s.tau = s.dir * t0;
+    s.tau0 = s.dir * t0;
     s.tau1 = s.dir * t1;
+    if (a.phase == 1) {  // continue a parked orbit exactly
+      const OrbitResume& r = a.resume[o];
+#pragma unroll
+      for (int j = 0; j < 6; ++j) s.y[j] = r.y[j];
+      s.tau = r.tau;
+      s.tnext = r.tnext;
+      s.prev_inv = r.prev_inv;
+      s.prev_prev_inv = r.prev_prev_inv;
+      s.nsteps = r.nsteps;
+      s.naccepted = r.naccepted;
+      s.save_i = r.save_i;
+      s.at_dtmin = r.at_dtmin;
+      s.status = r.status;
+      field(pot, s.y, s.F0);
+      return true;
+    }
+#pragma unroll
+    for (int j = 0; j < 6; ++j) s.y[j] = a.y0[j * a.n + o];
+    s.save_i = 0;
+    s.nsteps = 0;
+    s.naccepted = 0;
+    s.tau = s.tau0;
     s.prev_inv = 1.0;
     s.prev_prev_inv = 1.0;
     s.at_dtmin = 0;
@@ -265,27 +299,108 @@ __device__ __forceinline__ bool start_orbit(const IntegrateArgs& a, const Pot& p
   }
 }
 
+// Phase 0 of the two-phase schedule: park the orbit once it has covered
+// split_frac of its span (only between steps, never with saves pending).
+__device__ __forceinline__ bool maybe_park(const IntegrateArgs& a, OrbitState& s) {
+  if (a.phase != 0 || a.split_frac <= 0.0) return false;
+  const double span = s.tau1 - s.tau0;
+  const double done = s.tau - s.tau0;
+  if (done < a.split_frac * span) return false;
+  OrbitResume& r = a.resume[s.orbit];
+#pragma unroll
+  for (int j = 0; j < 6; ++j) r.y[j] = s.y[j];
+  r.tau = s.tau;
+  r.tnext = s.tnext;
+  r.prev_inv = s.prev_inv;
+  r.prev_prev_inv = s.prev_prev_inv;
+  r.progress = done / span;
+  r.nsteps = s.nsteps;
+  r.naccepted = s.naccepted;
+  r.save_i = s.save_i;
+  r.at_dtmin = s.at_dtmin;
+  r.status = s.status;
+  r.paused = 1;
+  if (a.steps) a.steps[s.orbit] = s.naccepted;
+  s.orbit = -1;
+  return true;
+}
+
+// y = ms^(-1/(2*ORDER)) to FP64 accuracy: an FP32 seed and two FP64 Newton
+// steps on ms * y^(2*ORDER) = 1 (y <- y (1 + e / (2*ORDER)), e = 1 - ms y^(2*ORDER);
+// the error squares each step). Valid for ms in [1e-30, 1e30].
+template <int ORDER>
+__device__ __forceinline__ double inv_root(double ms) {
+  constexpr int P = 2 * ORDER;
+  double y = (double)powf((float)ms, -1.0f / P);
+#pragma unroll
+  for (int it = 0; it < 2; ++it) {
+    double p = y;  // y^P by repeated multiplication (P = 10 or 16)
+    if constexpr (P == 16) {
+      p = p * p; p = p * p; p = p * p; p = p * p;
+    } else {
+      const double y2 = y * y, y4 = y2 * y2, y8 = y4 * y4;
+      p = y8 * y2;
+    }
+    const double e = fma(-ms, p, 1.0);
+    y = fma(y * (1.0 / P), e, y);
+  }
+  return y;
+}
+
 // Controller after a step of length h = tnext - tau with error estimate err.
 // Sets keep, the next (t0, t1) and the controller state.
+template <int ORDER>
 __device__ __forceinline__ bool pid_adapt(const IntegrateArgs& a, OrbitState& s, const double* y1,
                                           const double* err, double h, double& next_t0, double& next_t1) {
-  double q[6];
+  // RMS of err_j / d_j with d_j = atol + rtol max(|y0_j|, |y1_j|); the six
+  // reciprocals come from one division (prefix/suffix products).
+  double d[6];
 #pragma unroll
   for (int j = 0; j < 6; ++j) {
     const double y1c = isnan(y1[j]) ? s.y[j] : y1[j];
-    q[j] = err[j] / fma(fmax(fabs(s.y[j]), fabs(y1c)), a.rtol, a.atol);
+    d[j] = fma(fmax(fabs(s.y[j]), fabs(y1c)), a.rtol, a.atol);
   }
-  const double scaled = rms6(q);
-  bool keep = scaled < 1.0;
+  const double p01 = d[0] * d[1], p23 = d[2] * d[3], p45 = d[4] * d[5];
+  const double p0123 = p01 * p23;
+  const double P = p0123 * p45;
+  double ms = 0.0;
+  if (P > 1e-280 && P < 1e280) {
+    const double iP = 1.0 / P;
+    const double i01 = iP * p23 * p45, i23 = iP * p01 * p45, i45 = iP * p0123;
+    const double r[6] = {i01 * d[1], i01 * d[0], i23 * d[3], i23 * d[2], i45 * d[5], i45 * d[4]};
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      const double q = err[j] * r[j];
+      ms = fma(q, q, ms);
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      const double q = err[j] / d[j];
+      ms = fma(q, q, ms);
+    }
+  }
+  ms = ms / 6.0;
+  bool keep = ms < 1.0;  // scaled error = sqrt(ms) < 1
   if (a.dtmin > 0.0) keep = keep || s.at_dtmin;
-  double inv = 1.0 / scaled;
-  double f1 = (a.c1 == 0.0) ? 1.0 : pow(inv, a.c1);
-  const double f2 = (a.c2 == 0.0) ? 1.0 : pow(s.prev_inv, a.c2);
-  const double f3 = (a.c3 == 0.0) ? 1.0 : pow(s.prev_prev_inv, a.c3);
   const double fmin_ = keep ? 1.0 : a.factormin;
-  const double factor = fmin(fmax(a.safety * f1 * f2 * f3, fmin_), a.factormax);
+  double factor;
+  if (a.i_controller && ms >= 1e-30 && ms <= 1e30) {
+    // integral controller: factor = safety * (1/scaled)^(1/order) = safety * ms^(-1/(2 order))
+    factor = fmin(fmax(a.safety * inv_root<ORDER>(ms), fmin_), a.factormax);
+  } else {
+    double inv = 1.0 / sqrt(ms);
+    const double f1 = (a.c1 == 0.0) ? 1.0 : pow(inv, a.c1);
+    const double f2 = (a.c2 == 0.0) ? 1.0 : pow(s.prev_inv, a.c2);
+    const double f3 = (a.c3 == 0.0) ? 1.0 : pow(s.prev_prev_inv, a.c3);
+    factor = fmin(fmax(a.safety * f1 * f2 * f3, fmin_), a.factormax);
+    if (inv == 0.0 || isinf(inv)) inv = 1.0;
+    if (keep) {
+      s.prev_prev_inv = s.prev_inv;
+      s.prev_inv = inv;
+    }
+  }
   double dt = h * factor;
-  if (inv == 0.0 || isinf(inv)) inv = 1.0;
   if (a.dtmax > 0.0) dt = fmin(dt, a.dtmax);
   if (a.dtmin > 0.0) {
     if (!a.force_dtmin && dt < a.dtmin) s.status = ORBIT_DT_MIN;
@@ -294,10 +409,6 @@ __device__ __forceinline__ bool pid_adapt(const IntegrateArgs& a, OrbitState& s,
   }
   next_t0 = keep ? s.tnext : s.tau;
   next_t1 = next_t0 + dt;
-  if (keep) {
-    s.prev_prev_inv = s.prev_inv;
-    s.prev_inv = inv;
-  }
   return keep;
 }
 
@@ -343,6 +454,10 @@ __device__ void integrate_loop(const IntegrateArgs& a, const Pot& pot) {
       if (s.status != ORBIT_OK) { done = true; st = s.status; }
       else if (s.tau >= s.tau1) done = true;
       else if (s.nsteps >= a.max_steps) { done = true; st = ORBIT_MAX_STEPS; }
+      else if (maybe_park(a, s)) {
+        if (!start_orbit<TB>(a, pot, s)) return;
+        continue;
+      }
     } else {
       rk_combine<TB>(s.y, hs, F, y1, a.adaptive ? err : nullptr);
       ++s.nsteps;
@@ -350,7 +465,7 @@ __device__ void integrate_loop(const IntegrateArgs& a, const Pot& pot) {
       double next_t0, next_t1;
       bool keep;
       if (a.adaptive) {
-        keep = pid_adapt(a, s, y1, err, h, next_t0, next_t1);
+        keep = pid_adapt<TB::ORDER>(a, s, y1, err, h, next_t0, next_t1);
       } else {
         keep = true;
         next_t0 = s.tnext;
@@ -381,8 +496,9 @@ __device__ void integrate_loop(const IntegrateArgs& a, const Pot& pot) {
                 C4[j] = F1 - 4.0 * F0 - 11.0 * Y0 - 5.0 * Y1 + 16.0 * ymid[j];
                 f0[j] = F0;
               }
+              const double ih = 1.0 / h;
               do {
-                const double th = (save_tau(a, s, s.save_i) - s.tau) / h;
+                const double th = (save_tau(a, s, s.save_i) - s.tau) * ih;
                 double v[6];
 #pragma unroll
                 for (int j = 0; j < 6; ++j) v[j] = fma(fma(fma(fma(A4[j], th, B4[j]), th, C4[j]), th, f0[j]), th, s.y[j]);
@@ -420,6 +536,10 @@ __device__ void integrate_loop(const IntegrateArgs& a, const Pot& pot) {
         if (s.status != ORBIT_OK) { done = true; st = s.status; }
         else if (s.tau >= s.tau1) done = true;
         else if (s.nsteps >= a.max_steps) { done = true; st = ORBIT_MAX_STEPS; }
+        else if (maybe_park(a, s)) {
+          if (!start_orbit<TB>(a, pot, s)) return;
+          continue;
+        }
       }
     }
     if (done) {

@@ -8,8 +8,10 @@ namespace gal {
 
 constexpr int kMaxBlock = 256;
 
-template <class TB>
-__global__ void __launch_bounds__(kMaxBlock) k_integrate_mw(IntegrateArgs a, MWParams p) {
+// MINB = 1: registers up to 255 (no spills); MINB = 2: at most 128 registers per
+// thread for more resident warps (a few spills). The autotuner picks per workload.
+template <class TB, int MINB>
+__global__ void __launch_bounds__(kMaxBlock, MINB) k_integrate_mw(IntegrateArgs a, MWParams p) {
   const MWPot pot{p};
   integrate_loop<TB>(a, pot);
 }
@@ -32,9 +34,11 @@ cudaError_t launch_integrate(const IntegrateArgs& a, bool mw, const MWParams& p,
   const size_t smem = mw ? 0 : sizeof(DevComp) * (size_t)ncomp;
   int per_sm = shape.blocks_per_sm;
   cudaError_t err;
+  const bool dense = shape.variant == 1;
   if (per_sm <= 0) {
     if (mw)
-      err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_integrate_mw<TB>, block, 0);
+      err = dense ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_integrate_mw<TB, 2>, block, 0)
+                  : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_integrate_mw<TB, 1>, block, 0);
     else
       err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_integrate_table<TB>, block, smem);
     if (err != cudaSuccess) return err;
@@ -45,7 +49,10 @@ cudaError_t launch_integrate(const IntegrateArgs& a, bool mw, const MWParams& p,
   if (grid > need) grid = need;
   if (grid < 1) grid = 1;
   if (mw) {
-    k_integrate_mw<TB><<<(unsigned)grid, block, 0, stream>>>(a, p);
+    if (dense)
+      k_integrate_mw<TB, 2><<<(unsigned)grid, block, 0, stream>>>(a, p);
+    else
+      k_integrate_mw<TB, 1><<<(unsigned)grid, block, 0, stream>>>(a, p);
   } else {
     if (smem > 48 * 1024) {
       err = cudaFuncSetAttribute(k_integrate_table<TB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -10,6 +10,7 @@ namespace gal {
 struct LaunchShape {
   int block_threads;  // 0 = default
   int blocks_per_sm;  // 0 = occupancy maximum
+  int variant;        // Milky Way kernel: 0 = up to 255 registers, 1 = at most 128 (more warps)
 };
 
 cudaError_t launch_integrate_dopri5(const IntegrateArgs& a, bool mw, const MWParams& p, const DevComp* comps,

@@ -99,6 +99,8 @@ class Integrator:
     stepsize_controller: Any = field(default_factory=lambda: PIDController(rtol=1e-7, atol=1e-7))
     dt0: float | None = None
     max_steps: int | None = None
+    # two-pass longest-remaining-first scheduling (identical results); None = on for adaptive runs
+    schedule: bool | None = None
 
     def config(self) -> _lib.SolverConfig:
         method = _method(self.solver)
@@ -107,12 +109,14 @@ class Integrator:
         if isinstance(c, ConstantStepSize):
             if not self.dt0 or self.dt0 <= 0:
                 raise ValueError("ConstantStepSize needs dt0 > 0")
-            return _lib.solver_config(method, False, dt0=self.dt0, max_steps=max_steps)
+            return _lib.solver_config(method, False, dt0=self.dt0, max_steps=max_steps,
+                                      schedule=bool(self.schedule))
         if isinstance(c, PIDController):
             return _lib.solver_config(
                 method, True, dt0=self.dt0 or 0.0, rtol=c.rtol, atol=c.atol, dtmin=c.dtmin, dtmax=c.dtmax,
                 pcoeff=c.pcoeff, icoeff=c.icoeff, dcoeff=c.dcoeff, safety=c.safety, factormin=c.factormin,
                 factormax=c.factormax, force_dtmin=c.force_dtmin, max_steps=max_steps,
+                schedule=True if self.schedule is None else self.schedule,
             )
         raise NotImplementedError(f"step-size controller {type(c).__name__} is not supported")
 

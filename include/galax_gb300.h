@@ -124,10 +124,16 @@ typedef struct gal_solver_config {
   double pcoeff, icoeff, dcoeff;
   double safety, factormin, factormax;
   int32_t force_dtmin;
-  int32_t reserved; /* must be 0 */
+  /* 0: one pass. 1: two passes over the batch with identical results: every
+   * orbit first covers the first tenth of its time span, then the orbits are
+   * resumed in order of decreasing estimated remaining work (steps so far x
+   * remaining fraction), so the longest orbits start early instead of forming a
+   * tail. Useful for adaptive batches with uneven lengths. */
+  int32_t schedule;
 } gal_solver_config;
 
-/* Scratch bytes gal_integrate needs for n orbits (work-queue counters). */
+/* Scratch bytes gal_integrate needs for n orbits (work-queue counters, and with
+ * cfg->schedule = 1 a 128-byte resume record per orbit plus ordering arrays). */
 GAL_API gal_status gal_integrate_workspace_size(const gal_solver_config* cfg, int64_t n, size_t* bytes);
 
 /* Integrate n orbits from t0[i] to t1[i] (t1 < t0 integrates backwards) and
@@ -153,8 +159,13 @@ GAL_API gal_status gal_integrate(const gal_potential* pot, const gal_solver_conf
                          double* out, int32_t* status, int64_t* steps, const int32_t* order, int64_t n,
                          void* workspace, size_t workspace_bytes, gal_stream_t stream);
 
-/* Launch shape used by gal_integrate (0 = automatic). Tunable per method. */
-GAL_API gal_status gal_set_launch(int32_t method, int32_t adaptive, int32_t block_threads, int32_t blocks_per_sm);
+/* Launch shape used by gal_integrate for one (method, adaptive) pair: threads per
+ * block (multiple of 32, <= 256; 0 = 128), blocks per SM (0 = occupancy maximum)
+ * and register variant of the Milky Way kernel (0 = up to 255 registers per
+ * thread, 1 = at most 128 for more resident warps). Process-wide setting, used
+ * by the autotuner; results never depend on it. */
+GAL_API gal_status gal_set_launch(int32_t method, int32_t adaptive, int32_t block_threads, int32_t blocks_per_sm,
+                                  int32_t variant);
 
 /* ------------------------------------------------------------------ adjoint */
 /* Scratch bytes gal_adjoint needs for n orbits with checkpoints every k_ckpt steps. */

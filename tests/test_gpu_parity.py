@@ -194,11 +194,19 @@ def test_uneven_batch_csr_matches_oracle(gx):
     st_gpu = status.cpu().numpy()
     np.testing.assert_array_equal(st_gpu, st)
     ok = st == 0
-    got = np.concatenate([res[i].cpu().numpy() for i in np.nonzero(ok)[0]])
-    want = np.concatenate([ref[i] for i in np.nonzero(ok)[0]])
-    rel = _rel_each(got, want)
-    assert rel.max() <= 10 * 1e-8
-    assert np.median(rel) < 1e-11
+    rel = np.array([_rel_each(res[i].cpu().numpy(), ref[i]).max() if ok[i] else 0.0 for i in range(len(ok))])
+    same = ok & (rel < 1e-10)
+    # nearly every orbit takes the identical step sequence: rounding-level agreement
+    assert same.sum() >= 0.95 * ok.sum()
+    # a borderline accept/reject that rounds the other way changes the step
+    # sequence; such an orbit must then agree within its own integration error
+    diff = np.nonzero(ok & ~same)[0]
+    if len(diff):
+        fine, *_ = O.integrate(O.milky_way(), b.y0[diff], b.t0[diff], b.t1[diff], [grids[i] for i in diff],
+                               O.solver_cfg(5, True, rtol=1e-11, atol=1e-13, max_steps=2**20))
+        for k, i in enumerate(diff):
+            err_ref = np.abs(ref[i] - fine[k]).max()
+            assert np.abs(res[i].cpu().numpy() - ref[i]).max() <= 10 * max(err_ref, 1e-8 * np.abs(ref[i]).max())
     # orbits that ran out of steps report it and leave unreached saves NaN
     for i in np.nonzero(~ok)[0]:
         assert np.isnan(res[i].cpu().numpy()[-1]).all()
@@ -220,6 +228,8 @@ def test_reference_kats_on_gpu(gx, goldens, name):
         integ = gx.Integrator(solver=gx.Dopri8(), stepsize_controller=gx.ConstantStepSize(), dt0=cfgd["dt0"])
     ts = golden_save_ts(g)
     rows = g.get("rows", [-1])
+    if "save_ts" in g:  # a single end time: evaluate_orbit starts from t[0], so prepend t0
+        ts = np.concatenate([[g["t0"]], ts])
     orb = gx.evaluate_orbit(_pot(gx, comps), np.array(g["y0"], float), ts, integrator=integ)
     got = orb.w[:, rows].reshape(-1, 6)
     want = np.concatenate([np.asarray(g["expect_q"]), np.asarray(g["expect_p"])], axis=-1).reshape(-1, 6)
@@ -233,7 +243,7 @@ def test_reverse_time_round_trip(gx):
     mw = gx.MilkyWayPotential()
     fwd = gx.evaluate_orbit(mw, y0, np.array([0.0, 200.0]), integrator=integ).w[:, -1]
     back = gx.evaluate_orbit(mw, fwd, np.array([200.0, 0.0]), integrator=integ).w[:, -1]
-    assert _rel(back, y0) < 1e-10
+    assert _rel(back, y0) < 1e-8  # Dopri8 truncation error over 2 x 200 Myr
     ref, *_ = O.integrate(O.milky_way(), fwd, 200.0, 0.0, np.array([0.0]), O.solver_cfg(8, False, dt0=0.5))
     assert _rel(back, np.stack(ref).reshape(-1, 6)) < 1e-12
 
@@ -293,11 +303,11 @@ def test_launch_shapes_give_identical_results(gx):
     y0 = _ics(3000, 23)
     cfg = gx.Integrator(solver=gx.Dopri5(), stepsize_controller=gx.PIDController(rtol=1e-8, atol=1e-10)).config()
     outs = []
-    for block, per_sm in ((128, 0), (64, 1), (256, 2), (32, 3)):
-        _lib.check(L.gal_set_launch(5, 1, block, per_sm), "gal_set_launch")
+    for block, per_sm, variant in ((128, 0, 0), (64, 1, 1), (256, 2, 0), (32, 3, 1), (128, 0, 1)):
+        _lib.check(L.gal_set_launch(5, 1, block, per_sm, variant), "gal_set_launch")
         out, st, steps = integrate(mw, y0, 0.0, 300.0, np.linspace(0, 300, 11), cfg)
         outs.append(out.cpu().numpy())
-    _lib.check(L.gal_set_launch(5, 1, 0, 0), "gal_set_launch")
+    _lib.check(L.gal_set_launch(5, 1, 0, 0, 0), "gal_set_launch")
     for o in outs[1:]:
         np.testing.assert_array_equal(o, outs[0])
 
@@ -326,3 +336,24 @@ def test_adjoint_matches_oracle(gx, which):
     mask = gp_o != 0
     np.testing.assert_allclose(res.grad_params[mask], gp_o[mask], rtol=1e-8)
     assert abs(res.loss - L_o) <= 1e-10 * L_o
+
+
+@pytest.mark.parametrize("method", [5, 8])
+def test_two_pass_schedule_is_bitwise_identical(gx, method):
+    """Longest-remaining-first rescheduling parks and resumes orbits from their
+    exact state, so every save and step count is unchanged."""
+    from galax_gb300 import workloads as W
+    from galax_gb300.dynamics import integrate
+
+    b = W.uneven_ics(lambda x: O.gradient(O.milky_way(), x), 2000, seed=4, tmax=600.0, smax=60)
+    mw = gx.MilkyWayPotential()
+    res = []
+    for sched in (False, True):
+        cfg = gx.Integrator(solver=gx.Dopri8() if method == 8 else gx.Dopri5(),
+                            stepsize_controller=gx.PIDController(rtol=1e-8, atol=1e-10), max_steps=2**16,
+                            schedule=sched).config()
+        out, st, steps = integrate(mw, b.y0, b.t0, b.t1, b.save_ts, cfg, save_offsets=b.save_offsets)
+        res.append((out.cpu().numpy(), st.cpu().numpy(), steps.cpu().numpy()))
+    np.testing.assert_array_equal(res[0][1], res[1][1])
+    np.testing.assert_array_equal(res[0][2], res[1][2])
+    np.testing.assert_array_equal(res[0][0], res[1][0])

@@ -67,6 +67,8 @@ SIGNATURES = {
     "gal_integrate_workspace_size": (C.c_int, [C.POINTER(SolverConfig), C.c_int64, C.POINTER(C.c_size_t)]),
     "gal_integrate": (C.c_int, [C.c_void_p, C.POINTER(SolverConfig), _DP, _DP, _DP, _I64P, _DP, C.c_int64, _DP,
                                 _I32P, _I64P, _I32P, C.c_int64, _VP, C.c_size_t, C.c_void_p]),
+    "gal_integrate_noalloc": (C.c_int, [C.c_void_p, C.POINTER(SolverConfig), _DP, _DP, _DP, _I64P, _DP, C.c_int64,
+                                        _DP, _I32P, _I64P, _I32P, C.c_int64, C.c_void_p]),
     "gal_set_launch": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
     "gal_adjoint_workspace_size": (C.c_int, [C.c_void_p, C.POINTER(SolverConfig), C.c_double, C.c_double,
                                              C.c_int32, C.c_int64, C.POINTER(C.c_size_t)]),

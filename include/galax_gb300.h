@@ -159,6 +159,31 @@ GAL_API gal_status gal_integrate(const gal_potential* pot, const gal_solver_conf
                          double* out, int32_t* status, int64_t* steps, const int32_t* order, int64_t n,
                          void* workspace, size_t workspace_bytes, gal_stream_t stream);
 
+/* gal_integrate without a workspace (no counterpart in the reference: galax runs
+ * under XLA, which manages all device memory).
+ *
+ * For callers that cannot allocate device memory: code running while a CUDA
+ * graph is captured, plugins that are handed only their input and output
+ * buffers, services that forbid allocation after start-up. The scratch that
+ * gal_integrate takes from its workspace comes instead from a fixed array of
+ * GAL_NOALLOC_SCRATCH_BYTES (4 MiB) in the library's own device memory, which
+ * every GPU that loads the library holds until the process exits. Inputs and
+ * outputs are the caller's, exactly as for gal_integrate, and the results are
+ * the same. This function allocates and frees nothing.
+ *  - Limit: a call whose gal_integrate_workspace_size exceeds the array is
+ *    rejected with GAL_ERR_TOO_LARGE (with schedule = 1 that is about 30,000
+ *    orbits per call; with schedule = 0 only 8 bytes are needed, so any n).
+ *  - The first call on each device looks up the array's device address with
+ *    that device current; make that first call before any stream capture.
+ *  - All calls share the one array and it keeps the previous call's contents
+ *    (each call clears what must start at zero). Calls that overlap on the GPU,
+ *    from different streams or threads, race on it: serialise them. */
+#define GAL_NOALLOC_SCRATCH_BYTES (4 * 1024 * 1024)
+GAL_API gal_status gal_integrate_noalloc(const gal_potential* pot, const gal_solver_config* cfg, const double* y0,
+                                         const double* t0, const double* t1, const int64_t* save_offsets,
+                                         const double* save_ts, int64_t n_saves, double* out, int32_t* status,
+                                         int64_t* steps, const int32_t* order, int64_t n, gal_stream_t stream);
+
 /* Launch shape used by gal_integrate for one (method, adaptive) pair: threads per
  * block (multiple of 32, <= 256; 0 = 128), blocks per SM (0 = occupancy maximum)
  * and register variant of the Milky Way kernel (0 = up to 255 registers per

@@ -18,7 +18,7 @@ DEFAULT_CANDIDATES = (
     (128, 0, 0),
     (128, 0, 1),
     (64, 0, 0),
-    (256, 0, 1),
+    (128, 0, 2),
 )
 
 

@@ -16,7 +16,9 @@
 namespace gal {
 
 thread_local std::string g_last_error;
-static LaunchShape g_shape[2][2] = {{{0, 0, 0}, {0, 0, 0}}, {{0, 0, 0}, {0, 0, 0}}};  // [method 5/8][adaptive]
+// [method 5/8][adaptive]: Dopri5 fits 3 blocks of 128 per SM without spills
+// (variant 0); Dopri8 needs the uncapped variant 2 to avoid spilling.
+static LaunchShape g_shape[2][2] = {{{0, 0, 0}, {0, 0, 0}}, {{0, 0, 2}, {0, 0, 2}}};
 
 gal_status fail(gal_status st, const std::string& msg) {
   g_last_error = msg;
@@ -395,7 +397,7 @@ gal_status gal_integrate_workspace_size(const gal_solver_config* cfg, int64_t n,
 gal_status gal_set_launch(int32_t method, int32_t adaptive, int32_t block_threads, int32_t blocks_per_sm,
                           int32_t variant) {
   if ((method != 5 && method != 8) || block_threads < 0 || block_threads > 256 || (block_threads % 32) ||
-      blocks_per_sm < 0 || variant < 0 || variant > 1)
+      blocks_per_sm < 0 || variant < 0 || variant > 2 || (variant != 2 && block_threads > 128))
     return fail(GAL_ERR_INVALID_ARGUMENT, "bad launch shape");
   g_shape[method == 8][adaptive ? 1 : 0] = LaunchShape{block_threads, blocks_per_sm, variant};
   return GAL_OK;

@@ -155,6 +155,44 @@ __device__ __forceinline__ void rk_combine(const double* y, double hs, const dou
   if (err != nullptr) weighted<TB, W_ERROR>(nullptr, hs, F, err);
 }
 
+// Dopri5 dense output at theta in [0, 1] of a step of signed length hs: the
+// quartic p with p(0) = y0, p(1) = y1, p(1/2) = y_mid (Shampine's weights),
+// p'(0) = hs F0, p'(1) = hs F6 (diffrax's FourthOrderPolynomialInterpolation),
+// written in its basis form
+//   p = y0 + H1 (y1 - y0) + Hm (y_mid - y0) + Hf0 hs F0 + Hf1 hs F6,
+//   H1 = th^2 (-8 th^2 + 14 th - 5), Hm = 16 th^2 (1 - th)^2,
+//   Hf0 = th (1 - th)^2 (1 - 2 th), Hf1 = th^2 (th - 1) (2 th - 1),
+// so that p = y0 + hs sum_i W_i F_i with W_i = H1 b_i + Hm cmid_i (+ Hf0, Hf1).
+// One weight vector per save time; no per-step set-up.
+__device__ __forceinline__ void dopri5_dense(const double* y0, double hs, const double (&F)[Dopri5::S][6],
+                                             double th, double* out) {
+  const double t2 = th * th;
+  const double u = 1.0 - th;
+  const double H1 = t2 * fma(th, fma(-8.0, th, 14.0), -5.0);
+  const double Hm = 16.0 * t2 * (u * u);
+  const double Hf0 = th * (u * u) * fma(-2.0, th, 1.0);
+  const double Hf1 = t2 * (-u) * fma(2.0, th, -1.0);
+  double W[Dopri5::S];
+  static_for<0, Dopri5::S>([&](auto i) {
+    constexpr int I = decltype(i)::value;
+    constexpr double b = Dopri5::B[I], c = Dopri5::CMID[I];
+    double w = (b != 0.0) ? H1 * b : 0.0;
+    if constexpr (c != 0.0) w = fma(Hm, c, w);
+    if constexpr (I == 0) w += Hf0;
+    if constexpr (I == Dopri5::S - 1) w += Hf1;
+    W[I] = w;
+  });
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    double acc = W[0] * F[0][j];
+    static_for<1, Dopri5::S>([&](auto i) {
+      constexpr int I = decltype(i)::value;
+      if constexpr (I != 1) acc = fma(W[I], F[I][j], acc);  // b_1 = cmid_1 = 0
+    });
+    out[j] = fma(hs, acc, y0[j]);
+  }
+}
+
 __device__ __forceinline__ double rms6(const double* q) {
   double s = 0.0;
 #pragma unroll
@@ -485,23 +523,11 @@ __device__ void integrate_loop(const IntegrateArgs& a, const Pot& pot) {
           if constexpr (TB::FSAL) {
             // Dopri5: saves in (tau, tnext] from the quartic dense output
             if (s.save_i < s.save_end && save_tau(a, s, s.save_i) <= next_t0) {
-              double A4[6], B4[6], C4[6], f0[6], ymid[6];
-              weighted<TB, W_MIDPOINT>(s.y, hs, F, ymid);
-#pragma unroll
-              for (int j = 0; j < 6; ++j) {
-                const double F0 = hs * F[0][j], F1 = hs * F[TB::S - 1][j];
-                const double Y0 = s.y[j], Y1 = y1[j];
-                A4[j] = 2.0 * (F1 - F0) - 8.0 * (Y1 + Y0) + 16.0 * ymid[j];
-                B4[j] = 5.0 * F0 - 3.0 * F1 + 18.0 * Y0 + 14.0 * Y1 - 32.0 * ymid[j];
-                C4[j] = F1 - 4.0 * F0 - 11.0 * Y0 - 5.0 * Y1 + 16.0 * ymid[j];
-                f0[j] = F0;
-              }
               const double ih = 1.0 / h;
               do {
                 const double th = (save_tau(a, s, s.save_i) - s.tau) * ih;
                 double v[6];
-#pragma unroll
-                for (int j = 0; j < 6; ++j) v[j] = fma(fma(fma(fma(A4[j], th, B4[j]), th, C4[j]), th, f0[j]), th, s.y[j]);
+                dopri5_dense(s.y, hs, F, th, v);
                 write_save(a, s, s.save_i, v);
                 ++s.save_i;
               } while (s.save_i < s.save_end && save_tau(a, s, s.save_i) <= next_t0);

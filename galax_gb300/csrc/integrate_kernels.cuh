@@ -8,12 +8,33 @@ namespace gal {
 
 constexpr int kMaxBlock = 256;
 
-// MINB = 1: registers up to 255 (no spills); MINB = 2: at most 128 registers per
-// thread for more resident warps (a few spills). The autotuner picks per workload.
-template <class TB, int MINB>
-__global__ void __launch_bounds__(kMaxBlock, MINB) k_integrate_mw(IntegrateArgs a, MWParams p) {
+// Register variants of the Milky Way kernel (threads per block <= MAXT):
+//   0: 128 threads, 3 blocks per SM  -> at most 168 registers, 12 warps per SM
+//   1: 128 threads, 4 blocks per SM  -> at most 128 registers, 16 warps per SM (spills)
+//   2: 256 threads, 1 block per SM   -> up to 255 registers
+// The autotuner picks per workload; results do not depend on it.
+template <class TB, int MAXT, int MINB>
+__global__ void __launch_bounds__(MAXT, MINB) k_integrate_mw(IntegrateArgs a, MWParams p) {
   const MWPot pot{p};
   integrate_loop<TB>(a, pot);
+}
+
+template <class TB>
+cudaError_t mw_occupancy(int variant, int block, int* per_sm) {
+  switch (variant) {
+    case 1: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_integrate_mw<TB, 128, 4>, block, 0);
+    case 2: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_integrate_mw<TB, 256, 1>, block, 0);
+    default: return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_integrate_mw<TB, 128, 3>, block, 0);
+  }
+}
+
+template <class TB>
+void mw_launch(int variant, unsigned grid, int block, cudaStream_t stream, const IntegrateArgs& a, const MWParams& p) {
+  switch (variant) {
+    case 1: k_integrate_mw<TB, 128, 4><<<grid, block, 0, stream>>>(a, p); break;
+    case 2: k_integrate_mw<TB, 256, 1><<<grid, block, 0, stream>>>(a, p); break;
+    default: k_integrate_mw<TB, 128, 3><<<grid, block, 0, stream>>>(a, p); break;
+  }
 }
 
 template <class TB>
@@ -34,11 +55,10 @@ cudaError_t launch_integrate(const IntegrateArgs& a, bool mw, const MWParams& p,
   const size_t smem = mw ? 0 : sizeof(DevComp) * (size_t)ncomp;
   int per_sm = shape.blocks_per_sm;
   cudaError_t err;
-  const bool dense = shape.variant == 1;
+  if (mw && shape.variant != 2 && block > 128) return cudaErrorInvalidValue;
   if (per_sm <= 0) {
     if (mw)
-      err = dense ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_integrate_mw<TB, 2>, block, 0)
-                  : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_integrate_mw<TB, 1>, block, 0);
+      err = mw_occupancy<TB>(shape.variant, block, &per_sm);
     else
       err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_integrate_table<TB>, block, smem);
     if (err != cudaSuccess) return err;
@@ -49,10 +69,7 @@ cudaError_t launch_integrate(const IntegrateArgs& a, bool mw, const MWParams& p,
   if (grid > need) grid = need;
   if (grid < 1) grid = 1;
   if (mw) {
-    if (dense)
-      k_integrate_mw<TB, 2><<<(unsigned)grid, block, 0, stream>>>(a, p);
-    else
-      k_integrate_mw<TB, 1><<<(unsigned)grid, block, 0, stream>>>(a, p);
+    mw_launch<TB>(shape.variant, (unsigned)grid, block, stream, a, p);
   } else {
     if (smem > 48 * 1024) {
       err = cudaFuncSetAttribute(k_integrate_table<TB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

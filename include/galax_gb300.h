@@ -186,9 +186,11 @@ GAL_API gal_status gal_integrate_noalloc(const gal_potential* pot, const gal_sol
 
 /* Launch shape used by gal_integrate for one (method, adaptive) pair: threads per
  * block (multiple of 32, <= 256; 0 = 128), blocks per SM (0 = occupancy maximum)
- * and register variant of the Milky Way kernel (0 = up to 255 registers per
- * thread, 1 = at most 128 for more resident warps). Process-wide setting, used
- * by the autotuner; results never depend on it. */
+ * and register variant of the Milky Way kernel (0 = at most 168 registers per
+ * thread, 3 blocks of 128 per SM; 1 = at most 128 registers, 4 blocks of 128;
+ * 2 = up to 255 registers, blocks up to 256 threads; variants 0 and 1 need
+ * block_threads <= 128). Process-wide setting, used by the autotuner; results
+ * never depend on it. */
 GAL_API gal_status gal_set_launch(int32_t method, int32_t adaptive, int32_t block_threads, int32_t blocks_per_sm,
                                   int32_t variant);
 

@@ -89,7 +89,8 @@ def test_validation_without_gpu(lib):
     cfg = _lib.solver_config(8, False, dt0=1.0)
     assert lib.gal_integrate_workspace_size(C.byref(cfg), 10, C.byref(nbytes)) == 0 and nbytes.value >= 8
     assert lib.gal_set_launch(8, 0, 100, 0, 0) == 1  # not a multiple of 32
-    assert lib.gal_set_launch(8, 0, 128, 0, 2) == 1  # unknown register variant
+    assert lib.gal_set_launch(8, 0, 128, 0, 3) == 1  # unknown register variant
+    assert lib.gal_set_launch(8, 0, 256, 0, 0) == 1  # variant 0 takes at most 128 threads
 
 
 def test_python_api_rejects_unsupported_inputs():

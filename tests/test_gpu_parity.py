@@ -303,7 +303,7 @@ def test_launch_shapes_give_identical_results(gx):
     y0 = _ics(3000, 23)
     cfg = gx.Integrator(solver=gx.Dopri5(), stepsize_controller=gx.PIDController(rtol=1e-8, atol=1e-10)).config()
     outs = []
-    for block, per_sm, variant in ((128, 0, 0), (64, 1, 1), (256, 2, 0), (32, 3, 1), (128, 0, 1)):
+    for block, per_sm, variant in ((128, 0, 0), (64, 1, 1), (256, 2, 2), (32, 3, 1), (128, 0, 2)):
         _lib.check(L.gal_set_launch(5, 1, block, per_sm, variant), "gal_set_launch")
         out, st, steps = integrate(mw, y0, 0.0, 300.0, np.linspace(0, 300, 11), cfg)
         outs.append(out.cpu().numpy())

@@ -155,8 +155,10 @@ def run_ours(args) -> dict | None:
 
         dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
     n = args.orbits or DEFAULT_ORBITS[args.workload]
-    if args.workload != "uneven":
-        raise SystemExit(f"workload {args.workload} is reported by bench_configs.py")
+    if args.workload == "grad":
+        return run_grad(args, n, rank, world, dist)
+    if args.workload == "plain":
+        return run_plain(args, n, rank, world, dist)
     mw, b = make_uneven(n, seed=1 + rank)  # weak scaling: every rank its own shard
     cfg = gx.Integrator(solver=gx.Dopri5(), stepsize_controller=gx.PIDController(rtol=1e-8, atol=1e-10),
                         max_steps=2**16).config()
@@ -295,6 +297,147 @@ def run_ours(args) -> dict | None:
     return line
 
 
+def _timed(fn, steps, stream):
+    import torch
+
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def _max_over_ranks(x, dist):
+    import torch
+
+    if not dist:
+        return x
+    t = torch.tensor([x], device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t)
+
+
+def run_grad(args, n, rank, world, dist) -> dict | None:
+    """Differentiation workload: MW, Dopri8 dt=0.5 Myr over 2 Gyr, loss = sum of
+    squared distances of the final points to perturbed targets, gradients with
+    respect to the 6 initial conditions of every orbit and the component
+    parameters, checkpoints every 256 steps. Metric: gradients (orbits) per second."""
+    import torch
+
+    import galax_gb300 as gx
+    from galax_gb300 import workloads as W
+    from galax_gb300.adjoint import _run as adjoint_run
+    from galax_gb300.dynamics import integrate
+
+    mw = gx.MilkyWayPotential()
+    y0h = W.disk_like_ics(lambda x: mw.gradient(x), n, seed=2 + rank)
+    dt, t1 = 0.5, float(args.t1 or 2000.0)
+    cfg = gx.Integrator(solver=gx.Dopri8(), stepsize_controller=gx.ConstantStepSize(), dt0=dt).config()
+    y0 = torch.as_tensor(y0h, device="cuda").t().contiguous()
+    out, _, _ = integrate(mw, y0, 0.0, t1, torch.tensor([t1]), cfg, soa=True)
+    rng = np.random.default_rng(20 + rank)
+    pert = np.concatenate([rng.normal(0, 0.1, (n, 3)), rng.normal(0, 2 * 0.001022712165045695, (n, 3))], axis=1)
+    target = (out[:, 0, :] + torch.as_tensor(pert.T, device="cuda")).contiguous()
+    stream = torch.cuda.current_stream()
+
+    def step():
+        return adjoint_run(mw, y0, 0.0, t1, dt, 8, 256, target_soa=target)
+
+    for _ in range(args.warmup):
+        step()
+    if dist:
+        dist.barrier()
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", 0)))
+    clocks.start()
+    ms = _max_over_ranks(_timed(step, args.steps, stream), dist)
+    clk = clocks.stop()
+    yT, gy, gp = step()
+    value = n * world / (ms * 1e-3)
+    # end to end: pinned host inputs, gradients back to pinned host
+    h_y0 = torch.as_tensor(y0h.T.copy()).pin_memory()
+    h_tg = target.cpu().pin_memory()
+    h_gy = torch.empty((6, n), dtype=torch.float64).pin_memory()
+    h_gp = torch.empty((4, 3), dtype=torch.float64).pin_memory()
+
+    def e2e():
+        dy = h_y0.to("cuda", non_blocking=True)
+        dtg = h_tg.to("cuda", non_blocking=True)
+        _, g1, g2 = adjoint_run(mw, dy, 0.0, t1, dt, 8, 256, target_soa=dtg)
+        h_gy.copy_(g1, non_blocking=True)
+        h_gp.copy_(g2, non_blocking=True)
+
+    e2e()
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        e2e()
+    torch.cuda.synchronize()
+    e2e_ms = _max_over_ranks((time.perf_counter() - t) * 1e3 / args.steps, dist)
+    if rank != 0:
+        return None
+    from galax_gb300.flops import STEP_FLOPS_MW
+
+    nsteps = int(round(t1 / dt))
+    flops = n * nsteps * STEP_FLOPS_MW[8] * 4  # forward, segment recompute, stage recompute, reverse sweep
+    peak = fp64_peak()
+    achieved = flops / (ms * 1e-3) / 1e12
+    return {
+        "metric": "grads/s", "value": value, "unit": "grads/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded numpy, galactic units)",
+        "config": {"workload": WORKLOADS["grad"], "orbits_per_gpu": n, "steps_per_orbit": nsteps,
+                   "gradient": "6 initial conditions per orbit + (m, l1, l2) of the 4 components",
+                   "l2": "checkpoints (n x 16 x 48 B) and segment buffer (n x 256 x 48 B = 0.8 GB) exceed L2"},
+        "e2e": {"value": n * world / (e2e_ms * 1e-3), "unit": "grads/s", "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": 2 * 6 * n * 8, "d2h_bytes_per_step": 6 * n * 8 + 12 * 8},
+        "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak["tflops"], "unit": "TFLOP/s",
+                     "frac": achieved / peak["tflops"], "traffic": None,
+                     "note": "algorithmic flops = 4 x Dopri8 forward step flops per step; peak measured live"},
+        "clocks": clk, "gpu_launches": 2 * args.steps,
+    }
+
+
+def run_plain(args, n, rank, world, dist) -> dict | None:
+    """Plain small workload: MW, 1,024 orbits, Dopri8 dt=1 Myr over 1 Gyr, 100 saves."""
+    import torch
+
+    import galax_gb300 as gx
+    from galax_gb300 import workloads as W
+    from galax_gb300.dynamics import integrate
+
+    mw = gx.MilkyWayPotential()
+    y0h = W.disk_like_ics(lambda x: mw.gradient(x), n, seed=0 + rank)
+    cfg = gx.Integrator(solver=gx.Dopri8(), stepsize_controller=gx.ConstantStepSize(), dt0=1.0).config()
+    y0 = torch.as_tensor(y0h, device="cuda").t().contiguous()
+    ts = torch.linspace(0, 1000, 100, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def step():
+        return integrate(mw, y0, 0.0, 1000.0, ts, cfg, soa=True)
+
+    for _ in range(args.warmup):
+        step()
+    ms = _max_over_ranks(_timed(step, args.steps, stream), dist)
+    if rank != 0:
+        return None
+    value = n * world * 1000 / (ms * 1e-3)
+    from galax_gb300.flops import STEP_FLOPS_MW
+
+    peak = fp64_peak()
+    achieved = n * 1000 * STEP_FLOPS_MW[8] / (ms * 1e-3) / 1e12
+    return {"metric": "orbit-steps/s", "value": value, "unit": "orbit-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOADS["plain"], "orbits_per_gpu": n},
+            "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak["tflops"], "unit": "TFLOP/s",
+                         "frac": achieved / peak["tflops"],
+                         "note": "1,024 orbits occupy 8 of 152 SMs: latency-bound by construction"},
+            "gpu_launches": args.steps}
+
+
 def traffic_from_profiles():
     """DRAM bytes per launch of the integrate kernel, from the committed ncu summary."""
     p = os.path.join(ROOT, "profiles", "integrate_dopri5_uneven.md")
@@ -388,6 +531,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--t1", type=float, default=0.0, help="grad workload: end time in Myr (default 2000)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("note: fewer than 3 warm-up steps", file=sys.stderr)

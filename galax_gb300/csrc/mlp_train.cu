@@ -1,0 +1,359 @@
+// Training of the potential-surrogate MLP on the GPU (FP32 CUDA cores).
+//
+// One call, gal_mlp_train_step, runs for a batch of B points: the forward pass,
+// the input-gradient (backward) pass, the loss on potential and gradient
+// targets, the exact parameter gradient of that loss (backpropagation through
+// the backward pass, which needs SiLU'' terms), and an Adam update. Weights and
+// the activations that enter the 256x256 products are rounded to bfloat16 in
+// the forward and backward passes, as the tensor-core inference kernel does, so
+// the trained network is the one that will be run (gradients pass the rounding
+// straight through). gal_mlp_loss_grads returns the loss and gradient without
+// updating (checked against a NumPy restatement).
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "handle.h"
+#include "mlp.cuh"
+
+namespace gal {
+namespace mlp {
+
+// C[M,N] = alpha * op(A)[M,K] op(B)[K,N] + beta * C + bias[n], row-major storage.
+// op(A)(m,k) = TA ? A[k*lda+m] : A[m*lda+k]; op(B)(k,n) = TB ? B[n*ldb+k] : B[k*ldb+n].
+// qa / qb round the loaded operand to bfloat16.
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(256) k_gemm(int M, int N, int K, const float* __restrict__ A, int lda,
+                                              const float* __restrict__ B, int ldb, float* __restrict__ C, int ldc,
+                                              float alpha, float beta, const float* __restrict__ bias, int qa,
+                                              int qb) {
+  __shared__ float As[16][64 + 1];
+  __shared__ float Bs[16][64 + 1];
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  const int m0 = blockIdx.y * 64, n0 = blockIdx.x * 64;
+  float acc[4][4] = {};
+  for (int k0 = 0; k0 < K; k0 += 16) {
+    for (int i = threadIdx.x; i < 1024; i += 256) {
+      int mm, kk;
+      if (TA) { kk = i / 64; mm = i % 64; } else { mm = i / 16; kk = i % 16; }
+      const int m = m0 + mm, k = k0 + kk;
+      float v = 0.0f;
+      if (m < M && k < K) v = TA ? A[(int64_t)k * lda + m] : A[(int64_t)m * lda + k];
+      As[kk][mm] = qa ? bf16r(v) : v;
+      int nn, kb;
+      if (TB) { nn = i / 16; kb = i % 16; } else { kb = i / 64; nn = i % 64; }
+      const int n = n0 + nn, kq = k0 + kb;
+      float w = 0.0f;
+      if (n < N && kq < K) w = TB ? B[(int64_t)n * ldb + kq] : B[(int64_t)kq * ldb + n];
+      Bs[kb][nn] = qb ? bf16r(w) : w;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < 16; ++kk) {
+      float a[4], b[4];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) a[r] = As[kk][ty * 4 + r];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) b[c] = Bs[kk][tx * 4 + c];
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc[r][c] = fmaf(a[r], b[c], acc[r][c]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int m = m0 + ty * 4 + r;
+    if (m >= M) continue;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const int n = n0 + tx * 4 + c;
+      if (n >= N) continue;
+      float v = alpha * acc[r][c];
+      if (beta != 0.0f) v += beta * C[(int64_t)m * ldc + n];
+      if (bias) v += bias[n];
+      C[(int64_t)m * ldc + n] = v;
+    }
+  }
+}
+
+#define GRID_STRIDE(i, n) for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < (n); i += (int64_t)gridDim.x * blockDim.x)
+
+// H = silu(Z), optionally rounded to bfloat16
+__global__ void k_silu(const float* Z, float* Hout, int64_t n, int q) {
+  GRID_STRIDE(i, n) {
+    const float h = silu(Z[i]);
+    Hout[i] = q ? bf16r(h) : h;
+  }
+}
+
+// D = s(Z) * U with s = silu' (optionally bf16-rounded, as stored by the inference kernel), D optionally rounded
+__global__ void k_dmul(const float* Z, const float* U, float* D, int64_t n, int qs, int qd) {
+  GRID_STRIDE(i, n) {
+    float s = dsilu(Z[i]);
+    if (qs) s = bf16r(s);
+    const float d = s * U[i];
+    D[i] = qd ? bf16r(d) : d;
+  }
+}
+
+// D4[b, c] = silu'(Z4[b, c]) * w5[c]
+__global__ void k_d4(const float* Z, const float* w5, float* D, int64_t n, int q) {
+  GRID_STRIDE(i, n) {
+    const float d = dsilu(Z[i]) * w5[i % H];
+    D[i] = q ? bf16r(d) : d;
+  }
+}
+
+// Ub = s(Z) * Db;  Zb = silu''(Z) * U * Db   (the z-dependence of the backward pass)
+__global__ void k_dd(const float* Z, const float* U, const float* Db, float* Ub, float* Zb, int64_t n, int qs) {
+  GRID_STRIDE(i, n) {
+    const float z = Z[i];
+    float s = dsilu(z);
+    if (qs) s = bf16r(s);
+    Ub[i] = s * Db[i];
+    Zb[i] = d2silu(z) * U[i] * Db[i];
+  }
+}
+
+// Zb4 = silu''(Z4) * w5 * Db4 + silu'(Z4) * Pb[b] * w5
+__global__ void k_zb4(const float* Z, const float* Db, const float* Pb, const float* w5, float* Zb, int64_t n) {
+  GRID_STRIDE(i, n) {
+    const float z = Z[i];
+    const float w = w5[i % H];
+    Zb[i] = d2silu(z) * w * Db[i] + dsilu(z) * Pb[i / H] * w;
+  }
+}
+
+// Zb += silu'(Z) * Hb
+__global__ void k_zb_acc(const float* Z, const float* Hb, float* Zb, int64_t n) {
+  GRID_STRIDE(i, n) { Zb[i] += dsilu(Z[i]) * Hb[i]; }
+}
+
+// out[c] (+)= sum_b f(b, c) over rows; mode 0: X[b,c]; 1: X[b,c]*v[b]; 2: silu'(X[b,c]) * Y[b,c]
+__global__ void k_colsum(const float* X, const float* Y, const float* v, int64_t rows, int cols, float* out, int mode,
+                         int accumulate) {
+  const int c = blockIdx.x;
+  float s = 0.0f;
+  for (int64_t b = threadIdx.x; b < rows; b += blockDim.x) {
+    const float x = X[b * cols + c];
+    s += mode == 0 ? x : (mode == 1 ? x * v[b] : dsilu(x) * Y[b * cols + c]);
+  }
+  __shared__ float red[256];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[c] = accumulate ? out[c] + red[0] : red[0];
+}
+
+// residuals, their loss weights and the loss value
+__global__ void k_loss(const float* out, const float* G, const float* phi_t, const float* g_t, int64_t B,
+                       float alpha, float beta, float* Pb, float* Eb, float* loss) {
+  float s = 0.0f;
+  GRID_STRIDE(b, B) {
+    const float r = out[b] - phi_t[b];
+    Pb[b] = 2.0f * alpha * r / (float)B;
+    s += alpha * r * r;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const float e = G[b * 3 + j] - g_t[b * 3 + j];
+      Eb[b * 3 + j] = 2.0f * beta * e / (float)B;
+      s += beta * e * e;
+    }
+  }
+  __shared__ float red[256];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) atomicAdd(loss, red[0] / (float)B);
+}
+
+__global__ void k_adam(float* p, const float* g, float* m, float* v, int64_t n, float lr, float b1, float b2,
+                       float eps, float c1, float c2) {
+  GRID_STRIDE(i, n) {
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.0f - b1) * gi;
+    const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+  }
+}
+
+struct Ws {
+  float *Z[5], *Hh[5], *D[5], *U[4], *Zb[5], *Db, *Ub, *Hb, *out, *G, *Pb, *Eb;
+};
+
+static size_t ws_bytes(int64_t B) {
+  const size_t big = sizeof(float) * (size_t)B * H;
+  return big * (4 + 4 + 4 + 3 + 4 + 3) + sizeof(float) * (size_t)B * (1 + 3 + 1 + 3) + 64 * 256;
+}
+
+static Ws carve(void* ws, int64_t B) {
+  Ws w{};
+  char* p = static_cast<char*>(ws);
+  const size_t big = sizeof(float) * (size_t)B * H;
+  auto take = [&](size_t bytes) {
+    float* r = reinterpret_cast<float*>(p);
+    p += (bytes + 255) & ~(size_t)255;
+    return r;
+  };
+  for (int k = 1; k <= 4; ++k) w.Z[k] = take(big);
+  for (int k = 1; k <= 4; ++k) w.Hh[k] = take(big);
+  for (int k = 1; k <= 4; ++k) w.D[k] = take(big);
+  for (int k = 1; k <= 3; ++k) w.U[k] = take(big);
+  for (int k = 1; k <= 4; ++k) w.Zb[k] = take(big);
+  w.Db = take(big);
+  w.Ub = take(big);
+  w.Hb = take(big);
+  w.out = take(sizeof(float) * B);
+  w.G = take(sizeof(float) * B * 3);
+  w.Pb = take(sizeof(float) * B);
+  w.Eb = take(sizeof(float) * B * 3);
+  return w;
+}
+
+template <bool TA, bool TB>
+static void gemm(cudaStream_t s, int M, int N, int K, const float* A, int lda, const float* B, int ldb, float* C,
+                 int ldc, float beta = 0.0f, const float* bias = nullptr, int qa = 0, int qb = 0) {
+  dim3 grid((N + 63) / 64, (M + 63) / 64);
+  k_gemm<TA, TB><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc, 1.0f, beta, bias, qa, qb);
+}
+
+static unsigned ew_grid(int64_t n) {
+  int64_t g = (n + 255) / 256;
+  return (unsigned)(g > 4096 ? 4096 : (g < 1 ? 1 : g));
+}
+
+// forward and input-gradient pass; leaves Z, H, D, U, out, G in the workspace
+static void forward_backward(cudaStream_t s, const float* P, const float* x, int64_t B, const Ws& w, int q) {
+  const int64_t n = B * H;
+  const int Bi = (int)B;
+  gemm<false, true>(s, Bi, H, 3, x, 3, P + OFF_W1, 3, w.Z[1], H, 0.0f, P + OFF_B1);
+  k_silu<<<ew_grid(n), 256, 0, s>>>(w.Z[1], w.Hh[1], n, q);
+  gemm<false, true>(s, Bi, H, H, w.Hh[1], H, P + OFF_W2, H, w.Z[2], H, 0.0f, P + OFF_B2, 0, q);
+  k_silu<<<ew_grid(n), 256, 0, s>>>(w.Z[2], w.Hh[2], n, q);
+  gemm<false, true>(s, Bi, H, H, w.Hh[2], H, P + OFF_W3, H, w.Z[3], H, 0.0f, P + OFF_B3, 0, q);
+  k_silu<<<ew_grid(n), 256, 0, s>>>(w.Z[3], w.Hh[3], n, q);
+  gemm<false, true>(s, Bi, H, H, w.Hh[3], H, P + OFF_W4, H, w.Z[4], H, 0.0f, P + OFF_B4, 0, q);
+  k_silu<<<ew_grid(n), 256, 0, s>>>(w.Z[4], w.Hh[4], n, 0);
+  gemm<false, false>(s, Bi, 1, H, w.Hh[4], H, P + OFF_W5, 1, w.out, 1, 0.0f, P + OFF_B5);
+  // input gradient
+  k_d4<<<ew_grid(n), 256, 0, s>>>(w.Z[4], P + OFF_W5, w.D[4], n, q);
+  gemm<false, false>(s, Bi, H, H, w.D[4], H, P + OFF_W4, H, w.U[3], H, 0.0f, nullptr, 0, q);
+  k_dmul<<<ew_grid(n), 256, 0, s>>>(w.Z[3], w.U[3], w.D[3], n, q, q);
+  gemm<false, false>(s, Bi, H, H, w.D[3], H, P + OFF_W3, H, w.U[2], H, 0.0f, nullptr, 0, q);
+  k_dmul<<<ew_grid(n), 256, 0, s>>>(w.Z[2], w.U[2], w.D[2], n, q, q);
+  gemm<false, false>(s, Bi, H, H, w.D[2], H, P + OFF_W2, H, w.U[1], H, 0.0f, nullptr, 0, q);
+  k_dmul<<<ew_grid(n), 256, 0, s>>>(w.Z[1], w.U[1], w.D[1], n, 0, 0);
+  gemm<false, false>(s, Bi, 3, H, w.D[1], H, P + OFF_W1, 3, w.G, 3);
+}
+
+static void loss_grads(cudaStream_t s, const float* P, const float* x, const float* phi_t, const float* g_t, int64_t B,
+                       float alpha, float beta, float* grad, float* loss, const Ws& w, int q) {
+  const int64_t n = B * H;
+  const int Bi = (int)B;
+  forward_backward(s, P, x, B, w, q);
+  cudaMemsetAsync(loss, 0, sizeof(float), s);
+  k_loss<<<ew_grid(B), 256, 0, s>>>(w.out, w.G, phi_t, g_t, B, alpha, beta, w.Pb, w.Eb, loss);
+  // ---- through the input-gradient graph, layer 1 up to 4
+  gemm<true, false>(s, H, 3, Bi, w.D[1], H, w.Eb, 3, grad + OFF_W1, 3);                       // gW1 = D1^T Eb
+  gemm<false, true>(s, Bi, H, 3, w.Eb, 3, P + OFF_W1, 3, w.Db, H);                           // Db1 = Eb W1^T
+  k_dd<<<ew_grid(n), 256, 0, s>>>(w.Z[1], w.U[1], w.Db, w.Ub, w.Zb[1], n, 0);
+  gemm<true, false>(s, H, H, Bi, w.D[2], H, w.Ub, H, grad + OFF_W2, H);                      // gW2 = D2^T Ub1
+  gemm<false, true>(s, Bi, H, H, w.Ub, H, P + OFF_W2, H, w.Db, H, 0.0f, nullptr, 0, q);      // Db2 = Ub1 W2^T
+  k_dd<<<ew_grid(n), 256, 0, s>>>(w.Z[2], w.U[2], w.Db, w.Ub, w.Zb[2], n, q);
+  gemm<true, false>(s, H, H, Bi, w.D[3], H, w.Ub, H, grad + OFF_W3, H);                      // gW3 = D3^T Ub2
+  gemm<false, true>(s, Bi, H, H, w.Ub, H, P + OFF_W3, H, w.Db, H, 0.0f, nullptr, 0, q);      // Db3 = Ub2 W3^T
+  k_dd<<<ew_grid(n), 256, 0, s>>>(w.Z[3], w.U[3], w.Db, w.Ub, w.Zb[3], n, q);
+  gemm<true, false>(s, H, H, Bi, w.D[4], H, w.Ub, H, grad + OFF_W4, H);                      // gW4 = D4^T Ub3
+  gemm<false, true>(s, Bi, H, H, w.Ub, H, P + OFF_W4, H, w.Db, H, 0.0f, nullptr, 0, q);      // Db4 = Ub3 W4^T
+  k_colsum<<<H, 256, 0, s>>>(w.Z[4], w.Db, nullptr, B, H, grad + OFF_W5, 2, 0);              // gw5 = sum silu'(Z4) Db4
+  k_zb4<<<ew_grid(n), 256, 0, s>>>(w.Z[4], w.Db, w.Pb, P + OFF_W5, w.Zb[4], n);
+  // ---- potential term and the forward graph, layer 4 down to 1
+  k_colsum<<<H, 256, 0, s>>>(w.Hh[4], nullptr, w.Pb, B, H, grad + OFF_W5, 1, 1);             // gw5 += H4^T Pb
+  k_colsum<<<1, 256, 0, s>>>(w.Pb, nullptr, nullptr, B, 1, grad + OFF_B5, 0, 0);             // gb5
+  gemm<true, false>(s, H, H, Bi, w.Zb[4], H, w.Hh[3], H, grad + OFF_W4, H, 1.0f);            // gW4 += Zb4^T H3
+  k_colsum<<<H, 256, 0, s>>>(w.Zb[4], nullptr, nullptr, B, H, grad + OFF_B4, 0, 0);
+  gemm<false, false>(s, Bi, H, H, w.Zb[4], H, P + OFF_W4, H, w.Hb, H, 0.0f, nullptr, 0, q);  // Hb3 = Zb4 W4
+  k_zb_acc<<<ew_grid(n), 256, 0, s>>>(w.Z[3], w.Hb, w.Zb[3], n);
+  gemm<true, false>(s, H, H, Bi, w.Zb[3], H, w.Hh[2], H, grad + OFF_W3, H, 1.0f);
+  k_colsum<<<H, 256, 0, s>>>(w.Zb[3], nullptr, nullptr, B, H, grad + OFF_B3, 0, 0);
+  gemm<false, false>(s, Bi, H, H, w.Zb[3], H, P + OFF_W3, H, w.Hb, H, 0.0f, nullptr, 0, q);
+  k_zb_acc<<<ew_grid(n), 256, 0, s>>>(w.Z[2], w.Hb, w.Zb[2], n);
+  gemm<true, false>(s, H, H, Bi, w.Zb[2], H, w.Hh[1], H, grad + OFF_W2, H, 1.0f);
+  k_colsum<<<H, 256, 0, s>>>(w.Zb[2], nullptr, nullptr, B, H, grad + OFF_B2, 0, 0);
+  gemm<false, false>(s, Bi, H, H, w.Zb[2], H, P + OFF_W2, H, w.Hb, H, 0.0f, nullptr, 0, q);
+  k_zb_acc<<<ew_grid(n), 256, 0, s>>>(w.Z[1], w.Hb, w.Zb[1], n);
+  gemm<true, false>(s, H, 3, Bi, w.Zb[1], H, x, 3, grad + OFF_W1, 3, 1.0f);                  // gW1 += Zb1^T X
+  k_colsum<<<H, 256, 0, s>>>(w.Zb[1], nullptr, nullptr, B, H, grad + OFF_B1, 0, 0);
+}
+
+}  // namespace mlp
+}  // namespace gal
+
+using namespace gal;
+using namespace gal::mlp;
+
+extern "C" {
+
+int64_t gal_mlp_num_params(void) { return NPARAM; }
+
+gal_status gal_mlp_workspace_size(int64_t batch, size_t* bytes) {
+  if (!bytes || batch < 1) return fail(GAL_ERR_INVALID_ARGUMENT, "batch >= 1 required");
+  if (batch > (int64_t)1 << 24) return fail(GAL_ERR_TOO_LARGE, "batch above 2^24 points");
+  *bytes = ws_bytes(batch);
+  return GAL_OK;
+}
+
+gal_status gal_mlp_forward_f32(const float* params, const float* x, int64_t batch, float* phi, float* grad,
+                               int32_t quantize, void* workspace, size_t workspace_bytes, gal_stream_t stream) {
+  if (!params || !x || batch < 1) return fail(GAL_ERR_INVALID_ARGUMENT, "bad MLP arguments");
+  if (batch > (int64_t)1 << 24) return fail(GAL_ERR_TOO_LARGE, "batch above 2^24 points");
+  if (!workspace || workspace_bytes < ws_bytes(batch)) return fail(GAL_ERR_WORKSPACE, "workspace too small");
+  cudaStream_t s = (cudaStream_t)stream;
+  const Ws w = carve(workspace, batch);
+  forward_backward(s, params, x, batch, w, quantize ? 1 : 0);
+  cudaError_t e = cudaSuccess;
+  if (phi) e = cudaMemcpyAsync(phi, w.out, sizeof(float) * batch, cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess && grad) e = cudaMemcpyAsync(grad, w.G, sizeof(float) * batch * 3, cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  return e == cudaSuccess ? GAL_OK : cuda_fail(e, "MLP forward");
+}
+
+gal_status gal_mlp_loss_grads(const float* params, const float* x, const float* phi_t, const float* g_t, int64_t batch,
+                              float alpha, float beta, int32_t quantize, float* grad, float* loss, void* workspace,
+                              size_t workspace_bytes, gal_stream_t stream) {
+  if (!params || !x || !phi_t || !g_t || !grad || !loss || batch < 1)
+    return fail(GAL_ERR_INVALID_ARGUMENT, "bad MLP arguments");
+  if (batch > (int64_t)1 << 24) return fail(GAL_ERR_TOO_LARGE, "batch above 2^24 points");
+  if (!workspace || workspace_bytes < ws_bytes(batch)) return fail(GAL_ERR_WORKSPACE, "workspace too small");
+  cudaStream_t s = (cudaStream_t)stream;
+  loss_grads(s, params, x, phi_t, g_t, batch, alpha, beta, grad, loss, carve(workspace, batch), quantize ? 1 : 0);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? GAL_OK : cuda_fail(e, "MLP loss/gradient");
+}
+
+gal_status gal_mlp_train_step(float* params, float* grad, float* adam_m, float* adam_v, const float* x,
+                              const float* phi_t, const float* g_t, int64_t batch, float alpha, float beta, float lr,
+                              float beta1, float beta2, float eps, int32_t step, int32_t quantize, float* loss,
+                              void* workspace, size_t workspace_bytes, gal_stream_t stream) {
+  gal_status st = gal_mlp_loss_grads(params, x, phi_t, g_t, batch, alpha, beta, quantize, grad, loss, workspace,
+                                     workspace_bytes, stream);
+  if (st != GAL_OK) return st;
+  if (!adam_m || !adam_v || step < 1) return fail(GAL_ERR_INVALID_ARGUMENT, "Adam state and step >= 1 required");
+  const float c1 = 1.0f - powf(beta1, (float)step), c2 = 1.0f - powf(beta2, (float)step);
+  k_adam<<<ew_grid(NPARAM), 256, 0, (cudaStream_t)stream>>>(params, grad, adam_m, adam_v, NPARAM, lr, beta1, beta2,
+                                                            eps, c1, c2);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? GAL_OK : cuda_fail(e, "MLP Adam update");
+}
+
+}  // extern "C"

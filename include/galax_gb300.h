@@ -213,6 +213,54 @@ GAL_API gal_status gal_adjoint(const gal_potential* pot, const gal_solver_config
                        double* grad_params, int32_t k_ckpt, int64_t n, void* workspace, size_t workspace_bytes,
                        gal_stream_t stream);
 
+/* ------------------------------------------------------------------ learned surrogate */
+/* A small MLP, 3 -> 256 -> 256 -> 256 -> 256 -> 1 with SiLU activations, that
+ * stands in for an expensive composite (the north-star's MilkyWayPotential plus
+ * hundreds of Plummer subhalos; no counterpart class in galax). Input
+ * u = x / length_scale, potential = phi_scale * out(u), gradient =
+ * (phi_scale / length_scale) grad_u out. Parameters are one float32 vector of
+ * gal_mlp_num_params() values: W1[256][3], b1, W2[256][256], b2, W3, b3, W4,
+ * b4, w5[256], b5 (W rows are output units). */
+typedef struct gal_mlp gal_mlp; /* opaque, device-resident inference weights */
+GAL_API int64_t gal_mlp_num_params(void);
+/* Training-side scratch for a batch of `batch` points. */
+GAL_API gal_status gal_mlp_workspace_size(int64_t batch, size_t* bytes);
+/* FP32 forward and input gradient of `batch` points u[batch][3] (network units):
+ * phi[batch] = out(u), grad[batch][3] = grad_u out. quantize = 1 rounds weights
+ * and the activations entering the 256x256 products to bfloat16, as inference does. */
+GAL_API gal_status gal_mlp_forward_f32(const float* params, const float* u, int64_t batch, float* phi, float* grad,
+                                       int32_t quantize, void* workspace, size_t workspace_bytes, gal_stream_t stream);
+/* Loss L = alpha/B sum (out - phi_t)^2 + beta/B sum |grad_u out - g_t|^2 (network
+ * units) and its exact gradient with respect to every parameter (grad[num_params]). */
+GAL_API gal_status gal_mlp_loss_grads(const float* params, const float* u, const float* phi_t, const float* g_t,
+                                      int64_t batch, float alpha, float beta, int32_t quantize, float* grad,
+                                      float* loss, void* workspace, size_t workspace_bytes, gal_stream_t stream);
+/* One Adam step on that loss (step counts from 1). */
+GAL_API gal_status gal_mlp_train_step(float* params, float* grad, float* adam_m, float* adam_v, const float* u,
+                                      const float* phi_t, const float* g_t, int64_t batch, float alpha, float beta,
+                                      float lr, float beta1, float beta2, float eps, int32_t step, int32_t quantize,
+                                      float* loss, void* workspace, size_t workspace_bytes, gal_stream_t stream);
+/* Build inference weights (bfloat16 operand images) from a host parameter vector. */
+GAL_API gal_status gal_mlp_create(const float* params_host, double length_scale, double phi_scale, gal_mlp** out);
+GAL_API gal_status gal_mlp_destroy(gal_mlp* mlp);
+/* Tensor-core inference at n positions x[3][n] (physical units): grad[3][n]
+ * (= or += grad_sign * grad Phi) and optionally phi[n]. */
+GAL_API gal_status gal_mlp_eval(const gal_mlp* mlp, const double* x, int64_t n, double* grad, int32_t accumulate,
+                                double grad_sign, double* phi, gal_stream_t stream);
+/* Error code the inference kernel recorded (0 = none; non-zero = a bounded wait gave up). */
+GAL_API gal_status gal_mlp_error(const gal_mlp* mlp, int32_t* code);
+
+/* Orbit integration with a surrogate: acceleration = -grad Phi_analytic (FP64,
+ * `pot`) - grad Phi_mlp (tensor cores; NULL = analytic only). Dopri5 with the
+ * constant step dt from t0 to t1 (the last step clipped onto t1, as
+ * gal_integrate), advancing y[6][n] in place to the final state. use_graph = 1
+ * replays one captured CUDA graph per step. Scratch from
+ * gal_surrogate_workspace_size (seven stage slopes and the stage positions). */
+GAL_API gal_status gal_surrogate_workspace_size(int64_t n, size_t* bytes);
+GAL_API gal_status gal_integrate_surrogate(const gal_potential* pot, const gal_mlp* mlp, double dt, double t0,
+                                           double t1, double* y, int64_t n, int32_t use_graph, void* workspace,
+                                           size_t workspace_bytes, gal_stream_t stream);
+
 /* ------------------------------------------------------------------ utilities */
 /* Copy the library's Butcher tableau (c[13], a[13][13], b[13], e[13] = b - bhat);
  * returns the number of stages, or 0 for an unknown method. Host only. */

@@ -1,0 +1,149 @@
+"""The learned-surrogate kernels on a GB300: training gradients against the NumPy
+restatement, tensor-core inference against the FP32 path, and the surrogate
+integrator against the plain integrator."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from oracle import mlp_oracle as M
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def env():
+    import torch
+
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA device")
+    from galax_gb300.build import build
+
+    build()
+    import galax_gb300 as gx
+    from galax_gb300 import surrogate as S
+
+    return gx, S
+
+
+def _params(S, seed=1, scale=1.0):
+    p = S.init_params(seed)
+    d = S.unpack(p)
+    rng = np.random.default_rng(seed + 100)
+    for k in ("b1", "b2", "b3", "b4"):
+        d[k][:] = rng.normal(0, 0.1, d[k].shape)
+    d["b5"][:] = 0.3
+    return p * np.float32(scale) if scale != 1.0 else p
+
+
+def _as_oracle(S, p):
+    return {k: v.astype(np.float64) for k, v in S.unpack(p).items()}
+
+
+def test_training_gradient_matches_numpy(env):
+    gx, S = env
+    p = _params(S)
+    rng = np.random.default_rng(3)
+    u = rng.normal(size=(96, 3)).astype(np.float32)
+    pt = rng.normal(size=96).astype(np.float32)
+    gt = rng.normal(size=(96, 3)).astype(np.float32)
+    loss, grad = S.loss_grads(p, u, pt, gt, 0.7, 1.3, quantize=False)
+    L_ref, g_ref = M.loss_and_grads(_as_oracle(S, p), u.astype(np.float64), pt.astype(np.float64),
+                                    gt.astype(np.float64), 0.7, 1.3)
+    assert abs(loss - L_ref) <= 1e-4 * abs(L_ref)
+    gd = S.unpack(grad)
+    for k in M.NAMES:
+        ref = g_ref[k].reshape(-1)
+        got = gd[k].reshape(-1).astype(np.float64)
+        assert np.linalg.norm(got - ref) <= 2e-4 * np.linalg.norm(ref) + 1e-7, k
+
+
+def test_quantised_fp32_forward_matches_numpy_bf16(env):
+    gx, S = env
+    p = _params(S)
+    rng = np.random.default_rng(4)
+    u = rng.normal(size=(512, 3)).astype(np.float32)
+    mlp = S.MLPSurrogate(p, 1.0, 1.0)
+    phi, g = mlp.forward_f32(u, quantize=True)
+    out_ref, g_ref = M.forward_bf16(_as_oracle(S, p), u.astype(np.float64))
+    phi, g = phi.cpu().numpy(), g.cpu().numpy()
+    # bfloat16 rounding ties can fall differently with a different summation order
+    assert np.median(np.abs(phi - out_ref)) < 1e-3 * np.abs(out_ref).mean()
+    rel = np.linalg.norm(g - g_ref, axis=1) / np.linalg.norm(g_ref, axis=1)
+    assert np.median(rel) < 5e-3 and rel.max() < 5e-2
+
+
+@pytest.mark.parametrize("n", [300, 20000])
+def test_tensor_core_inference_matches_fp32(env, n):
+    import torch
+
+    gx, S = env
+    p = _params(S)
+    length, pscale = 50.0, 3e-3
+    mlp = S.MLPSurrogate(p, length, pscale)
+    rng = np.random.default_rng(5)
+    x = rng.normal(size=(n, 3)) * 30.0
+    g, phi = mlp.evaluate(x, potential=True)
+    phi_r, g_r = mlp.forward_f32(x / length, quantize=True)
+    g_r = g_r.double().cpu().numpy() * (pscale / length)
+    phi_r = phi_r.double().cpu().numpy() * pscale
+    rel = np.linalg.norm(g - g_r, axis=1) / np.linalg.norm(g_r, axis=1)
+    assert np.median(rel) < 5e-3 and np.percentile(rel, 99) < 3e-2
+    assert np.median(np.abs(phi - phi_r)) < 2e-3 * np.abs(phi_r).mean()
+    torch.cuda.synchronize()
+
+
+def test_zero_network_surrogate_equals_plain_integrator(env):
+    """With an MLP whose output is identically zero the surrogate integrator must
+    reproduce the plain constant-step Dopri5 kernel on the analytic part."""
+    gx, S = env
+    from galax_gb300 import workloads as W
+    from galax_gb300.dynamics import integrate
+
+    p = _params(S)
+    d = S.unpack(p)
+    d["w5"][:] = 0.0
+    d["b5"][:] = 0.0
+    mlp = S.MLPSurrogate(p, 50.0, 1e-3)
+    mw = gx.MilkyWayPotential()
+    y0 = W.disk_like_ics(lambda x: O.gradient(O.milky_way(), x), 1000, seed=8)
+    for use_graph in (True, False):
+        yT = S.integrate(mw, mlp, y0, 0.0, 100.0, 1.0, use_graph=use_graph).cpu().numpy()
+        cfg = gx.Integrator(solver=gx.Dopri5(), stepsize_controller=gx.ConstantStepSize(), dt0=1.0).config()
+        out, st, steps = integrate(mw, y0, 0.0, 100.0, np.array([100.0]), cfg)
+        ref = out[:, 0, :].t().cpu().numpy()
+        np.testing.assert_allclose(yT, ref, rtol=1e-13, atol=1e-15)
+
+
+def test_surrogate_integrator_with_table_potential(env):
+    """Analytic part as a general component table: the MLP term shifts the orbits."""
+    gx, S = env
+    from galax_gb300 import workloads as W
+
+    p = _params(S, scale=0.5)
+    mlp = S.MLPSurrogate(p, 50.0, 1e-4)
+    kinds = gx.potential.from_component_array(O.milky_way()[[1, 0, 2, 3]])
+    y0 = W.disk_like_ics(lambda x: O.gradient(O.milky_way(), x), 777, seed=9)
+    a = S.integrate(kinds, None, y0, 0.0, 50.0, 1.0).cpu().numpy()
+    b = S.integrate(kinds, mlp, y0, 0.0, 50.0, 1.0).cpu().numpy()
+    ref, *_ = O.integrate(O.milky_way(), y0, 0.0, 50.0, np.array([50.0]), O.solver_cfg(5, False, dt0=1.0))
+    np.testing.assert_allclose(a, np.stack(ref).reshape(-1, 6), rtol=1e-11, atol=1e-13)
+    assert np.abs(b - a).max() > 1e-6
+
+
+def test_training_reduces_the_loss(env):
+    gx, S = env
+    rng = np.random.default_rng(6)
+    plum = O.comps([(O.PLUMMER, 5e9, 2.0, 0, (3.0, -1.0, 0.5))])
+    r = np.exp(rng.uniform(np.log(0.5), np.log(40), 32768))
+    v = rng.normal(size=(32768, 3))
+    x = v / np.linalg.norm(v, axis=1, keepdims=True) * r[:, None]
+    mlp, rep = S.train(x, O.potential(plum, x), O.gradient(plum, x), length_scale=20.0, epochs=6, batch=4096,
+                       lr=2e-3)
+    assert rep.loss[-1] < 0.25 * rep.loss[0]
+    g = mlp.evaluate(x[:4096])
+    g_ref = O.gradient(plum, x[:4096])
+    rel = np.linalg.norm(g - g_ref, axis=1) / np.linalg.norm(g_ref, axis=1)
+    assert np.median(rel) < 0.2

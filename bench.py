@@ -39,8 +39,11 @@ WORKLOADS = {
     "plain": "plain small: MilkyWayPotential, Dopri8 fixed dt=1 Myr over 1 Gyr, 100 uniform saves",
     "grad": "differentiation: MilkyWayPotential, Dopri8 fixed dt=0.5 Myr over 2 Gyr, squared-distance loss, "
             "adjoint with checkpoints every 256 steps",
+    "surrogate": "learned surrogate: MilkyWayPotential + 512 Plummer subhalos (m log-uniform 1e6-1e8 Msun, "
+                 "r_s U(0.1,1) kpc, centres at U(5,50) kpc); MLP 3-256-256-256-256-1 SiLU on the subhalo part, "
+                 "BF16 weights, FP32 accumulation, trained on 4M FP64 samples; Dopri5 dt=1 Myr over 1 Gyr",
 }
-DEFAULT_ORBITS = {"uneven": 262_144, "plain": 1024, "grad": 65_536}
+DEFAULT_ORBITS = {"uneven": 262_144, "plain": 1024, "grad": 65_536, "surrogate": 1_048_576}
 
 
 def dist_env():
@@ -159,6 +162,8 @@ def run_ours(args) -> dict | None:
         return run_grad(args, n, rank, world, dist)
     if args.workload == "plain":
         return run_plain(args, n, rank, world, dist)
+    if args.workload == "surrogate":
+        return run_surrogate(args, n, rank, world, dist)
     mw, b = make_uneven(n, seed=1 + rank)  # weak scaling: every rank its own shard
     cfg = gx.Integrator(solver=gx.Dopri5(), stepsize_controller=gx.PIDController(rtol=1e-8, atol=1e-10),
                         max_steps=2**16).config()
@@ -438,6 +443,100 @@ def run_plain(args, n, rank, world, dist) -> dict | None:
             "gpu_launches": args.steps}
 
 
+def run_surrogate(args, n, rank, world, dist) -> dict | None:
+    """Learned-surrogate workload: orbit-steps/s of the surrogate path (analytic Milky
+    Way in FP64 + MLP subhalo term on the tensor cores) against the plain FP64
+    direct sum over all 516 components, and the surrogate's median relative
+    position error after 1 Gyr (judged by the plain path)."""
+    import torch
+
+    import galax_gb300 as gx
+    from galax_gb300 import surrogate as S
+    from galax_gb300 import workloads as W
+    from galax_gb300.dynamics import integrate
+    from galax_gb300.potential import from_component_array
+
+    mw = gx.MilkyWayPotential()
+    m, b, c = W.subhalo_table(3, 512)
+    sub_arr = np.zeros(512, mw.component_array().dtype)
+    sub_arr["kind"] = 4
+    sub_arr["m"], sub_arr["l1"], sub_arr["origin"] = m, b, c
+    sub = from_component_array(sub_arr)
+    full = from_component_array(np.concatenate([mw.component_array(), sub_arr]))
+    # training set: positions log-uniform in radius, FP64 targets from the direct sum
+    npts = args.train_points
+    xt = torch.as_tensor(W.training_points(npts, seed=30), device="cuda")
+    phi_t, g_t = sub.potential(xt), sub.gradient(xt)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    mlp, rep = S.train(xt, phi_t, g_t, length_scale=50.0, epochs=args.train_epochs, batch=8192, lr=2e-3)
+    train_s = time.perf_counter() - t
+    # initial conditions as the small plain workload, radii 4-20 kpc
+    y0 = torch.as_tensor(W.disk_like_ics(lambda x: mw.gradient(x), n, seed=31 + rank), device="cuda")
+    dt, t1 = 1.0, 1000.0
+    stream = torch.cuda.current_stream()
+
+    def surrogate_step():
+        return S.integrate(mw, mlp, y0, 0.0, t1, dt)
+
+    for _ in range(args.warmup):
+        surrogate_step()
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", 0)))
+    clocks.start()
+    ms = _max_over_ranks(_timed(surrogate_step, args.steps, stream), dist)
+    clk = clocks.stop()
+    yT_sur = surrogate_step()
+    nsteps = int(round(t1 / dt))
+    value = n * world * nsteps / (ms * 1e-3)
+    # MLP kernel alone on 1M points (one stage evaluation)
+    xq = y0[:, :3].t().contiguous()
+    mlp.evaluate(xq.t())
+    mlp_ms = _timed(lambda: mlp.evaluate(xq.t()), 10, stream)
+    mlp_flops = 2.0 * (3 * 256 * 2 + 6 * 256 * 256 + 256)  # forward + input gradient per point
+    # plain FP64 direct sum over all 516 components, on a subsample
+    ns = min(n, args.plain_orbits)
+    cfg = gx.Integrator(solver=gx.Dopri5(), stepsize_controller=gx.ConstantStepSize(), dt0=dt).config()
+    ys = y0[:ns].t().contiguous()
+
+    def plain_step():
+        return integrate(full, ys, 0.0, t1, torch.tensor([t1]), cfg, soa=True)
+
+    plain_step()
+    plain_ms = _timed(plain_step, 1, stream)
+    out, st, _ = plain_step()
+    yT_plain = out[:, 0, :].t()
+    yT_mw = S.integrate(mw, None, y0[:ns], 0.0, t1, dt)
+    err = lambda a: (torch.linalg.vector_norm(a[:, :3] - yT_plain[:, :3], dim=1)  # noqa: E731
+                     / torch.linalg.vector_norm(yT_plain[:, :3], dim=1))
+    e_sur = err(yT_sur[:ns])
+    e_mw = err(yT_mw)
+    plain_value = ns * nsteps / (plain_ms * 1e-3)
+    if rank != 0:
+        return None
+    peaks = measured_peaks()
+    achieved_tf = n * mlp_flops / (mlp_ms * 1e-3) / 1e12
+    return {
+        "metric": "orbit-steps/s (surrogate)", "value": value, "unit": "orbit-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64 state, bf16 MLP", "data": "synthetic",
+        "config": {"workload": WORKLOADS["surrogate"], "orbits_per_gpu": n, "steps_per_orbit": nsteps,
+                   "train_points": npts, "train_epochs": args.train_epochs, "train_seconds": round(train_s, 2),
+                   "train_loss_first_last": [rep.loss[0], rep.loss[-1]]},
+        "plain_fp64_direct_sum": {"value": plain_value, "unit": "orbit-steps/s", "orbits": ns, "ms": plain_ms},
+        "speedup_vs_plain": value / plain_value,
+        "median_rel_pos_err_1gyr": {"surrogate": float(e_sur.median()), "analytic_mw_only": float(e_mw.median()),
+                                    "surrogate_p90": float(torch.quantile(e_sur, 0.9)),
+                                    "judged_on_orbits": ns},
+        "roofline": {"bound": "tensor", "kernel": "k_mlp_infer", "achieved": achieved_tf,
+                     "peak": peaks.get("bf16_tflops"), "unit": "TFLOP/s",
+                     "frac": achieved_tf / peaks["bf16_tflops"] if peaks.get("bf16_tflops") else None,
+                     "traffic": None, "ms_per_1M_points": mlp_ms,
+                     "note": "MLP forward + input gradient on 1,048,576 points, algorithmic flops; peak = measured "
+                             "burst BF16 (cuBLAS) from MEASURED_PEAKS.json"},
+        "clocks": clk, "gpu_launches": args.steps * (1 + 2 * 6 * nsteps),
+    }
+
+
 def traffic_from_profiles():
     """DRAM bytes per launch of the integrate kernel, from the committed ncu summary."""
     p = os.path.join(ROOT, "profiles", "integrate_dopri5_uneven.md")
@@ -532,6 +631,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--t1", type=float, default=0.0, help="grad workload: end time in Myr (default 2000)")
+    ap.add_argument("--train-points", type=int, default=4_194_304, help="surrogate workload: training samples")
+    ap.add_argument("--train-epochs", type=int, default=30, help="surrogate workload: training epochs")
+    ap.add_argument("--plain-orbits", type=int, default=65_536, help="surrogate workload: orbits for the plain path")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("note: fewer than 3 warm-up steps", file=sys.stderr)

@@ -29,11 +29,19 @@ gal_status cuda_fail(cudaError_t e, const char* where) {
   return fail(GAL_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
 }
 
+// SM count of the current device, looked up once per device (so that launches
+// made while a stream is being captured query nothing)
 int device_sm_count() {
-  int dev = 0, sms = 0;
+  static int cache[64] = {0};
+  int dev = 0;
   cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  return sms > 0 ? sms : 1;
+  if (dev < 0 || dev >= 64) dev = 0;
+  if (cache[dev] <= 0) {
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cache[dev] = sms > 0 ? sms : 1;
+  }
+  return cache[dev];
 }
 
 static DevComp fold(const gal_component& c, double G) {

@@ -131,7 +131,29 @@ gal_status gal_integrate_surrogate(const gal_potential* pot, const gal_mlp* mlp,
   if (!workspace || workspace_bytes < need) return fail(GAL_ERR_WORKSPACE, "workspace too small");
   double* F = static_cast<double*>(workspace);
   double* Yq = reinterpret_cast<double*>(static_cast<char*>(workspace) + align256(sizeof(double) * 7 * 6 * (size_t)n));
-  cudaStream_t s = (cudaStream_t)stream;
+  cudaStream_t caller = (cudaStream_t)stream;
+  // graphs are captured on a private non-blocking stream (the legacy default
+  // stream cannot be captured), ordered after and before the caller's stream
+  cudaStream_t s = caller;
+  cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+  if (use_graph) {
+    cudaError_t e0 = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    if (e0 == cudaSuccess) e0 = cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming);
+    if (e0 == cudaSuccess) e0 = cudaEventCreateWithFlags(&ev_out, cudaEventDisableTiming);
+    if (e0 == cudaSuccess) e0 = cudaEventRecord(ev_in, caller);
+    if (e0 == cudaSuccess) e0 = cudaStreamWaitEvent(s, ev_in, 0);
+    if (e0 != cudaSuccess) return cuda_fail(e0, "setting up the capture stream");
+  }
+  auto finish = [&](gal_status st) -> gal_status {
+    if (use_graph) {
+      cudaEventRecord(ev_out, s);
+      cudaStreamWaitEvent(caller, ev_out, 0);
+      cudaEventDestroy(ev_in);
+      cudaEventDestroy(ev_out);
+      cudaStreamDestroy(s);  // returns at once; queued work still completes
+    }
+    return st;
+  };
   const double dir = (t0 < t1) ? 1.0 : -1.0;
   // constant-step time grid as for gal_integrate: the step that would pass t1 - 1e-10 ends on t1
   const double tau1 = dir * t1;
@@ -152,7 +174,7 @@ gal_status gal_integrate_surrogate(const gal_potential* pot, const gal_mlp* mlp,
     return pot->is_mw ? launch_step(MWPot{pot->mw}, y, F, Yq, hs, n, mlp, s, grid)
                       : launch_step(TablePot{pot->d_comps, pot->n}, y, F, Yq, hs, n, mlp, s, grid);
   };
-  if ((e = run_slope0()) != cudaSuccess) return cuda_fail(e, "surrogate first slope");
+  if ((e = run_slope0()) != cudaSuccess) return finish(cuda_fail(e, "surrogate first slope"));
   cudaGraphExec_t exec = nullptr;
   double graph_hs = 0.0;
   while (tprev < tau1) {
@@ -170,7 +192,7 @@ gal_status gal_integrate_surrogate(const gal_potential* pot, const gal_mlp* mlp,
         }
         if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, g, 0);
         if (e == cudaSuccess) cudaGraphDestroy(g);
-        if (e != cudaSuccess) return cuda_fail(e, "capturing the surrogate step");
+        if (e != cudaSuccess) return finish(cuda_fail(e, "capturing the surrogate step"));
         graph_hs = hs;
       }
       e = cudaGraphLaunch(exec, s);
@@ -179,7 +201,7 @@ gal_status gal_integrate_surrogate(const gal_potential* pot, const gal_mlp* mlp,
     }
     if (e != cudaSuccess) {
       if (exec) cudaGraphExecDestroy(exec);
-      return cuda_fail(e, "surrogate step");
+      return finish(cuda_fail(e, "surrogate step"));
     }
     double nt1 = tnext + dt;
     tprev = fmin(tnext, tau1);
@@ -187,7 +209,7 @@ gal_status gal_integrate_surrogate(const gal_potential* pot, const gal_mlp* mlp,
     tnext = nt1;
   }
   if (exec) cudaGraphExecDestroy(exec);
-  return GAL_OK;
+  return finish(GAL_OK);
 }
 
 }  // extern "C"

@@ -140,7 +140,7 @@ def test_training_reduces_the_loss(env):
     r = np.exp(rng.uniform(np.log(0.5), np.log(40), 32768))
     v = rng.normal(size=(32768, 3))
     x = v / np.linalg.norm(v, axis=1, keepdims=True) * r[:, None]
-    mlp, rep = S.train(x, O.potential(plum, x), O.gradient(plum, x), length_scale=20.0, epochs=6, batch=4096,
+    mlp, rep = S.train(x, O.potential(plum, x), O.gradient(plum, x), length_scale=20.0, epochs=40, batch=2048,
                        lr=2e-3)
     assert rep.loss[-1] < 0.25 * rep.loss[0]
     g = mlp.evaluate(x[:4096])

@@ -42,8 +42,10 @@ WORKLOADS = {
     "surrogate": "learned surrogate: MilkyWayPotential + 512 Plummer subhalos (m log-uniform 1e6-1e8 Msun, "
                  "r_s U(0.1,1) kpc, centres at U(5,50) kpc); MLP 3-256-256-256-256-1 SiLU on the subhalo part, "
                  "BF16 weights, FP32 accumulation, trained on 4M FP64 samples; Dopri5 dt=1 Myr over 1 Gyr",
+    "mlp": "surrogate MLP inference alone: forward + input gradient of 3-256-256-256-256-1 SiLU at n points "
+           "(random weights), fused tensor-core kernel",
 }
-DEFAULT_ORBITS = {"uneven": 262_144, "plain": 1024, "grad": 65_536, "surrogate": 1_048_576}
+DEFAULT_ORBITS = {"uneven": 262_144, "plain": 1024, "grad": 65_536, "surrogate": 1_048_576, "mlp": 1_048_576}
 
 
 def dist_env():
@@ -164,6 +166,8 @@ def run_ours(args) -> dict | None:
         return run_plain(args, n, rank, world, dist)
     if args.workload == "surrogate":
         return run_surrogate(args, n, rank, world, dist)
+    if args.workload == "mlp":
+        return run_mlp(args, n, rank, world, dist)
     mw, b = make_uneven(n, seed=1 + rank)  # weak scaling: every rank its own shard
     cfg = gx.Integrator(solver=gx.Dopri5(), stepsize_controller=gx.PIDController(rtol=1e-8, atol=1e-10),
                         max_steps=2**16).config()
@@ -535,6 +539,33 @@ def run_surrogate(args, n, rank, world, dist) -> dict | None:
                              "burst BF16 (cuBLAS) from MEASURED_PEAKS.json"},
         "clocks": clk, "gpu_launches": args.steps * (1 + 2 * 6 * nsteps),
     }
+
+
+def run_mlp(args, n, rank, world, dist) -> dict | None:
+    """The tensor-core MLP kernel alone (one stage evaluation of the surrogate)."""
+    import torch
+
+    from galax_gb300 import surrogate as S
+
+    mlp = S.MLPSurrogate(S.init_params(0), 50.0, 1e-3)
+    rng = np.random.default_rng(1)
+    x = torch.as_tensor(rng.normal(size=(n, 3)) * 20.0, device="cuda")
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        mlp.evaluate(x)
+    ms = _max_over_ranks(_timed(lambda: mlp.evaluate(x), args.steps, stream), dist)
+    if rank != 0:
+        return None
+    flops = 2.0 * (3 * 256 * 2 + 6 * 256 * 256 + 256)
+    achieved = n * flops / (ms * 1e-3) / 1e12
+    peaks = measured_peaks()
+    return {"metric": "MLP evaluations/s", "value": n * world / (ms * 1e-3), "unit": "points/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+            "config": {"workload": WORKLOADS["mlp"], "points": n},
+            "roofline": {"bound": "tensor", "achieved": achieved, "peak": peaks.get("bf16_tflops"), "unit": "TFLOP/s",
+                         "frac": achieved / peaks["bf16_tflops"] if peaks.get("bf16_tflops") else None},
+            "gpu_launches": args.steps}
 
 
 def traffic_from_profiles():

@@ -106,7 +106,7 @@ __device__ __forceinline__ bool issue_gemm(const Ring& r, int64_t j0, uint32_t a
   return true;
 }
 
-__device__ __forceinline__ float sig(float z) { return __frcp_rn(1.0f + __expf(-z)); }
+__device__ __forceinline__ float sig(float z) { return tc::rcp_approx(1.0f + __expf(-z)); }
 
 // write 32 consecutive hidden units [c, c+32) of row `row` into the operand tile
 __device__ __forceinline__ void store_row32(uint8_t* tile, int row, int c, const float (&v)[32]) {

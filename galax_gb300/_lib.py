@@ -48,6 +48,21 @@ class SolverConfig(C.Structure):
     ]
 
 
+class StreamConfig(C.Structure):
+    """``gal_stream_config``."""
+
+    _fields_ = [
+        ("method", C.c_int32),
+        ("k_ckpt", C.c_int32),
+        ("n_release", C.c_int64),
+        ("dt", C.c_double),
+        ("t_now", C.c_double),
+        ("prog_m", C.c_double),
+        ("prog_b", C.c_double),
+        ("w_now", C.c_double * 6),
+    ]
+
+
 class GalaxGB300Error(RuntimeError):
     """A call into the CUDA library failed."""
 
@@ -74,6 +89,12 @@ SIGNATURES = {
                                              C.c_int32, C.c_int64, C.POINTER(C.c_size_t)]),
     "gal_adjoint": (C.c_int, [C.c_void_p, C.POINTER(SolverConfig), _DP, C.c_double, C.c_double, _DP, _DP, _DP, _DP,
                               _DP, C.c_int32, C.c_int64, _VP, C.c_size_t, C.c_void_p]),
+    "gal_stream_workspace_size": (C.c_int, [C.c_void_p, C.POINTER(StreamConfig), C.c_int32,
+                                            C.POINTER(C.c_size_t)]),
+    "gal_stream_run": (C.c_int, [C.c_void_p, C.POINTER(StreamConfig), _DP, _DP, _DP, _DP, _VP, C.c_size_t,
+                                 C.c_void_p]),
+    "gal_stream_grad": (C.c_int, [C.c_void_p, C.POINTER(StreamConfig), _DP, _DP, _DP, _DP, _DP, _DP, _VP,
+                                  C.c_size_t, C.c_void_p]),
     "gal_mlp_num_params": (C.c_int64, []),
     "gal_mlp_workspace_size": (C.c_int, [C.c_int64, C.POINTER(C.c_size_t)]),
     "gal_mlp_forward_f32": (C.c_int, [_VP, _VP, C.c_int64, _VP, _VP, C.c_int32, _VP, C.c_size_t, C.c_void_p]),

@@ -1,0 +1,878 @@
+// Mock stream with a moving progenitor: the forward simulation and the
+// discrete adjoint of the whole pipeline (progenitor orbit -> release
+// conditions -> particle orbits -> loss).
+//
+// Reference pipeline: src/galax/dynamics/_src/experimental/stream.py:121-230
+// (StreamSimulator.init: integrate the progenitor back to the first release
+// time, then forwards through the release times), stream.py:380-446 (run: every
+// particle from its release time to the present), with the progenitor's own
+// potential moved along its orbit as legacy/mockstream/_moving.py:20-42 does
+// (TimeDependentSpatialTranslationOperator), and the release model built on the
+// King (1962) tidal radius (dynamics/_src/cluster/radius.py:198-214,
+// r_t = cbrt(G M / (Omega^2 - d2Phi/dr2)); Omega = |x x v| / r^2,
+// dynamics/_src/register_api.py:82-88; d2Phi/dr2 = rhat . H . rhat,
+// potential/_src/register_funcs.py:444-457). galax differentiates all of it
+// with jax (diffrax ForwardMode); here the reverse pass is written out.
+//
+// Grid. Constant steps dt. The progenitor starts at w_now (time t_now), is
+// integrated n_rel steps backwards, then n_rel steps forwards; the forward pass
+// records its state P[k] at every grid point and its position Q[k][i] at every
+// Runge-Kutta stage i of every step k. Release r (r = 0..n_rel-1) happens at
+// grid point r and sends two particles, p = 2r (leading) and 2r + 1 (trailing):
+//     x_p = x_r + s r_t rhat + 0.1 r_t xi_p,   v_p = v_r + 0.1 Omega r_t eta_p,
+// s = -1 / +1, xi and eta caller-given standard-normal draws. Each particle is
+// integrated from grid point r to n_rel in the host potential plus a Plummer
+// sphere centred on Q[k][i] at stage i of step k: since the progenitor does not
+// feel the particles, this is exactly the particle half of the coupled
+// (particle, progenitor) system, with no interpolation of the progenitor track.
+//
+// Kernels. The progenitor runs on one thread (it is one serial orbit); the
+// release map on one thread per release; the particles on one thread each, one
+// warp per block. The particle adjoint walks the global step grid backwards in
+// lockstep across the warp (a lane joins once the walk reaches its release
+// step), so that at every step and stage the warp can sum its lanes'
+// cotangents on the progenitor's stage position (mu) with shuffles and write
+// one partial per warp; a fixed-order reduction over warps follows, then the
+// release-map adjoint (forward-mode dual numbers for d(d2Phi/dr2)) and the
+// progenitor adjoint (forwards track with the mu and release cotangents
+// injected, then the backwards track). Parameter gradients are written per
+// column and summed in a fixed order, so results are bitwise reproducible.
+#include <cuda_runtime.h>
+
+#include <climits>
+#include <vector>
+
+#include "handle.h"
+#include "integrate.cuh"
+#include "vjp.cuh"
+
+namespace gal {
+
+struct StreamDev {
+  int64_t n_rel, np, nwarps, ncol;
+  double dt, GMp, b2;
+  double w_now[6];
+  int32_t k_ckpt, ncomp;
+  double* B;             // [n_rel + 1][6] backwards progenitor track, B[0] = w_now
+  double* P;             // [n_rel + 1][6] forwards progenitor track
+  double* Q;             // [n_rel][S][3] progenitor stage positions
+  double* rt_om;         // [2][n_rel] tidal radius, angular frequency
+  const double* noise;   // [12][n_rel]: xi_lead, eta_lead, xi_trail, eta_trail
+  double* ics;           // [6][np]
+  double* fin;           // [6][np]
+  double* ckpt;          // [nseg][6][np] (gradient only)
+  double* seg;           // [K][6][np]
+  const double* target;  // [6][np]
+  double* lam_rel;       // [6][np] dL/dy_p at the release step
+  double* mu_warp;       // [nwarps][n_rel][S * 3]
+  double* mu;            // [n_rel][S * 3]
+  double* nu;            // [n_rel][6] dL/dP[r] through the release map
+  double* gp_all;        // [ncomp * 3 + 1][ncol]: parameter partials per column, last row the loss
+  double* grad_w_now;    // [6] or NULL
+};
+
+__device__ __forceinline__ MWPot bind_shared(const MWPot& p, const DevComp*) { return p; }
+__device__ __forceinline__ TablePot bind_shared(const TablePot& p, const DevComp* s) { return TablePot{s, p.n}; }
+
+__device__ __forceinline__ void stage_comps(const DevComp* comps, int ncomp, DevComp* s_comps) {
+  for (int i = threadIdx.x; i < ncomp; i += blockDim.x) s_comps[i] = comps[i];
+  __syncthreads();
+}
+
+// Particle field: host potential plus the progenitor's Plummer sphere at q.
+template <class Host>
+__device__ __forceinline__ void pfield(const Host& host, double GMp, double b2, const double* q, const double* Y,
+                                       double* F) {
+  double gx, gy, gz;
+  host.grad(Y[0], Y[1], Y[2], gx, gy, gz);
+  const double d0 = Y[0] - q[0], d1 = Y[1] - q[1], d2 = Y[2] - q[2];
+  const double r2 = fma(d0, d0, fma(d1, d1, fma(d2, d2, TINY)));
+  const double is = rsqrt(r2 + b2);
+  const double f = GMp * (is * is) * is;
+  F[0] = Y[3];
+  F[1] = Y[4];
+  F[2] = Y[5];
+  F[3] = -fma(f, d0, gx);
+  F[4] = -fma(f, d1, gy);
+  F[5] = -fma(f, d2, gz);
+}
+
+template <class TB, class Host>
+__device__ __forceinline__ void particle_step(const Host& host, double GMp, double b2, const double* Qk, double* y,
+                                              double hs) {
+  double F[TB::S][6];
+  pfield(host, GMp, b2, Qk, y, F[0]);
+  static_for<1, TB::S>([&](auto i) {
+    constexpr int I = decltype(i)::value;
+    double Y[6];
+    stage_state<TB, I>(y, hs, F, Y);
+    pfield(host, GMp, b2, Qk + 3 * I, Y, F[I]);
+  });
+  double y1[6];
+  rk_combine<TB>(y, hs, F, y1, nullptr);
+#pragma unroll
+  for (int j = 0; j < 6; ++j) y[j] = y1[j];
+}
+
+// H v of the Plummer sphere GMp / sqrt(|d|^2 + b^2) at offset d.
+__device__ __forceinline__ void plummer_hv(double GMp, double b2, const double* d, const double* v, double* Hv) {
+  const double r2 = fma(d[0], d[0], fma(d[1], d[1], fma(d[2], d[2], TINY)));
+  const double is = rsqrt(r2 + b2), is2 = is * is;
+  const double g = GMp * is2 * is;
+  const double gpr = -3.0 * g * is2;
+  const double dv = fma(d[0], v[0], fma(d[1], v[1], d[2] * v[2]));
+#pragma unroll
+  for (int j = 0; j < 3; ++j) Hv[j] = fma(g, v[j], gpr * dv * d[j]);
+}
+
+// ------------------------------------------------------------------ forward
+template <class TB, class Host>
+__global__ void __launch_bounds__(32) k_stream_progenitor(StreamDev a, Host host, const DevComp* comps) {
+  __shared__ DevComp s_comps[kAdjMaxComps];
+  stage_comps(comps, a.ncomp, s_comps);
+  const Host h = bind_shared(host, s_comps);
+  if (threadIdx.x != 0) return;
+  double y[6];
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    y[j] = a.w_now[j];
+    a.B[j] = y[j];
+  }
+  for (int64_t k = 0; k < a.n_rel; ++k) {
+    rk_step_plain<TB>(h, y, -a.dt);
+#pragma unroll
+    for (int j = 0; j < 6; ++j) a.B[(k + 1) * 6 + j] = y[j];
+  }
+#pragma unroll
+  for (int j = 0; j < 6; ++j) a.P[j] = y[j];
+  for (int64_t k = 0; k < a.n_rel; ++k) {
+    double* Qk = a.Q + k * TB::S * 3;
+    double F[TB::S][6];
+    field(h, y, F[0]);
+    Qk[0] = y[0];
+    Qk[1] = y[1];
+    Qk[2] = y[2];
+    static_for<1, TB::S>([&](auto i) {
+      constexpr int I = decltype(i)::value;
+      double Y[6];
+      stage_state<TB, I>(y, a.dt, F, Y);
+      Qk[3 * I + 0] = Y[0];
+      Qk[3 * I + 1] = Y[1];
+      Qk[3 * I + 2] = Y[2];
+      field(h, Y, F[I]);
+    });
+    double y1[6];
+    rk_combine<TB>(y, a.dt, F, y1, nullptr);
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      y[j] = y1[j];
+      a.P[(k + 1) * 6 + j] = y[j];
+    }
+  }
+}
+
+__global__ void __launch_bounds__(128) k_stream_release(StreamDev a, const DevComp* comps) {
+  __shared__ DevComp s_comps[kAdjMaxComps];
+  stage_comps(comps, a.ncomp, s_comps);
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= a.n_rel) return;
+  const double* w = a.P + 6 * r;
+  const double x[3] = {w[0], w[1], w[2]}, v[3] = {w[3], w[4], w[5]};
+  const double rr = sqrt(fma(x[0], x[0], fma(x[1], x[1], x[2] * x[2])));
+  const double rh[3] = {x[0] / rr, x[1] / rr, x[2] / rr};
+  const double L[3] = {x[1] * v[2] - x[2] * v[1], x[2] * v[0] - x[0] * v[2], x[0] * v[1] - x[1] * v[0]};
+  const double om = sqrt(fma(L[0], L[0], fma(L[1], L[1], L[2] * L[2]))) / (rr * rr);
+  double H[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  for (int c = 0; c < a.ncomp; ++c) comp_hessian(s_comps[c], x[0], x[1], x[2], H);
+  double prr = 0.0;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) prr = fma(rh[i] * H[3 * i + j], rh[j], prr);
+  const double rt = cbrt(a.GMp / (om * om - prr));
+  a.rt_om[r] = rt;
+  a.rt_om[a.n_rel + r] = om;
+  for (int side = 0; side < 2; ++side) {
+    const double s = side ? 1.0 : -1.0;
+    const int64_t p = 2 * r + side;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const double xi = a.noise[(6 * side + j) * a.n_rel + r];
+      const double eta = a.noise[(6 * side + 3 + j) * a.n_rel + r];
+      a.ics[j * a.np + p] = x[j] + s * rt * rh[j] + 0.1 * rt * xi;
+      a.ics[(3 + j) * a.np + p] = v[j] + 0.1 * om * rt * eta;
+    }
+  }
+}
+
+template <class TB, class Host>
+__global__ void __launch_bounds__(32) k_stream_particles(StreamDev a, Host host, const DevComp* comps) {
+  __shared__ DevComp s_comps[kAdjMaxComps];
+  stage_comps(comps, a.ncomp, s_comps);
+  const Host h = bind_shared(host, s_comps);
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= a.np) return;
+  const int64_t n = a.np, r = p >> 1;
+  const int K = a.k_ckpt;
+  double y[6];
+#pragma unroll
+  for (int j = 0; j < 6; ++j) y[j] = a.ics[j * n + p];
+  for (int64_t k = r; k < a.n_rel; ++k) {
+    if (a.ckpt && (k == r || k % K == 0)) {
+      const int64_t g = k / K;
+#pragma unroll
+      for (int j = 0; j < 6; ++j) a.ckpt[(g * 6 + j) * n + p] = y[j];
+    }
+    particle_step<TB>(h, a.GMp, a.b2, a.Q + k * TB::S * 3, y, a.dt);
+  }
+#pragma unroll
+  for (int j = 0; j < 6; ++j) a.fin[j * n + p] = y[j];
+}
+
+// ------------------------------------------------------------------ adjoint
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+  return v;
+}
+
+template <class TB, class Host>
+__global__ void __launch_bounds__(32) k_stream_particles_adj(StreamDev a, Host host, const DevComp* comps) {
+  __shared__ DevComp s_comps[kAdjMaxComps];
+  stage_comps(comps, a.ncomp, s_comps);
+  const Host h = bind_shared(host, s_comps);
+  constexpr int S = TB::S;
+  const int lane = threadIdx.x;
+  const int64_t w = blockIdx.x;
+  const int64_t p = w * 32 + lane;
+  const int64_t n = a.np;
+  const bool valid = p < n;
+  const int64_t rp = valid ? (p >> 1) : LLONG_MAX;
+  const int64_t rmin = (w * 32) >> 1;
+  const int K = a.k_ckpt;
+  const int ncomp = a.ncomp;
+  const double dt = a.dt;
+  double lam[6], loss = 0.0;
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    const double d = valid ? a.fin[j * n + p] - a.target[j * n + p] : 0.0;
+    lam[j] = 2.0 * d;
+    loss = fma(d, d, loss);
+  }
+  double gp[kAdjMaxComps * 3];
+#pragma unroll
+  for (int i = 0; i < kAdjMaxComps * 3; ++i) gp[i] = 0.0;
+  const int64_t nseg = (a.n_rel + K - 1) / K;
+  for (int64_t g = nseg - 1; g >= rmin / K; --g) {
+    const int64_t k0 = g * K;
+    const int64_t k1 = (k0 + K < a.n_rel) ? k0 + K : a.n_rel;
+    if (valid && rp < k1) {
+      const int64_t ks = rp > k0 ? rp : k0;
+      double y[6];
+#pragma unroll
+      for (int j = 0; j < 6; ++j) y[j] = a.ckpt[(g * 6 + j) * n + p];
+      for (int64_t k = ks; k < k1; ++k) {
+#pragma unroll
+        for (int j = 0; j < 6; ++j) a.seg[((k - k0) * 6 + j) * n + p] = y[j];
+        if (k + 1 < k1) particle_step<TB>(h, a.GMp, a.b2, a.Q + k * S * 3, y, dt);
+      }
+    }
+    const int64_t kstop = k0 > rmin ? k0 : rmin;
+    for (int64_t k = k1 - 1; k >= kstop; --k) {
+      const bool act = valid && k >= rp;
+      const double* Qk = a.Q + k * S * 3;
+      double yk[6] = {8.0, 0.0, 0.0, 0.0, 0.2, 0.0};  // finite stand-in for lanes not yet released
+      if (act) {
+#pragma unroll
+        for (int j = 0; j < 6; ++j) yk[j] = a.seg[((k - k0) * 6 + j) * n + p];
+      }
+      double F[S][6], Yq[S][3];
+      pfield(h, a.GMp, a.b2, Qk, yk, F[0]);
+      Yq[0][0] = yk[0];
+      Yq[0][1] = yk[1];
+      Yq[0][2] = yk[2];
+      static_for<1, S>([&](auto i) {
+        constexpr int I = decltype(i)::value;
+        double Y[6];
+        stage_state<TB, I>(yk, dt, F, Y);
+        Yq[I][0] = Y[0];
+        Yq[I][1] = Y[1];
+        Yq[I][2] = Y[2];
+        pfield(h, a.GMp, a.b2, Qk + 3 * I, Y, F[I]);
+      });
+      static_for<0, S>([&](auto i) {
+        constexpr int I = decltype(i)::value;
+        constexpr double bi = TB::B[I];
+#pragma unroll
+        for (int j = 0; j < 6; ++j) F[I][j] = dt * bi * lam[j];
+      });
+      double* mw_out = a.mu_warp + (w * a.n_rel + k) * (S * 3);
+      static_for<0, S>([&](auto rr) {
+        constexpr int I = S - 1 - decltype(rr)::value;
+        const double v[3] = {F[I][3], F[I][4], F[I][5]};
+        double Hv[3] = {0.0, 0.0, 0.0};
+        for (int c = 0; c < ncomp; ++c) {
+          double dp[3] = {0.0, 0.0, 0.0};
+          comp_vjp(s_comps[c], Yq[I], v, Hv, dp);
+          if (act) {
+            gp[3 * c + 0] -= dp[0];
+            gp[3 * c + 1] -= dp[1];
+            gp[3 * c + 2] -= dp[2];
+          }
+        }
+        const double d[3] = {Yq[I][0] - Qk[3 * I], Yq[I][1] - Qk[3 * I + 1], Yq[I][2] - Qk[3 * I + 2]};
+        double Hp[3];
+        plummer_hv(a.GMp, a.b2, d, v, Hp);
+        // cotangent on the progenitor's stage position: +H_prog v, summed over the warp
+        const double m0 = warp_sum(act ? Hp[0] : 0.0);
+        const double m1 = warp_sum(act ? Hp[1] : 0.0);
+        const double m2 = warp_sum(act ? Hp[2] : 0.0);
+        if (lane == 0) {
+          mw_out[3 * I + 0] = m0;
+          mw_out[3 * I + 1] = m1;
+          mw_out[3 * I + 2] = m2;
+        }
+        const double Yb[6] = {-(Hv[0] + Hp[0]), -(Hv[1] + Hp[1]), -(Hv[2] + Hp[2]), F[I][0], F[I][1], F[I][2]};
+        if (act) {
+#pragma unroll
+          for (int j = 0; j < 6; ++j) lam[j] += Yb[j];
+        }
+        static_for<0, I>([&](auto l) {
+          constexpr int L = decltype(l)::value;
+          constexpr double c = TB::A[I][L];
+          if constexpr (c != 0.0) {
+#pragma unroll
+            for (int j = 0; j < 6; ++j) F[L][j] = fma(dt * c, Yb[j], F[L][j]);
+          }
+        });
+      });
+      if (valid && k == rp) {
+#pragma unroll
+        for (int j = 0; j < 6; ++j) a.lam_rel[j * n + p] = lam[j];
+      }
+    }
+  }
+  if (valid) {
+    for (int c = 0; c < 3 * ncomp; ++c) a.gp_all[(int64_t)c * a.ncol + p] = gp[c];
+    a.gp_all[(int64_t)(3 * ncomp) * a.ncol + p] = loss;
+  }
+}
+
+// mu[k][:] = sum over the warps that had released particles by step k, in warp order.
+__global__ void k_stream_mu_reduce(StreamDev a, int S3) {
+  const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (idx >= a.n_rel * S3) return;
+  const int64_t k = idx / S3;
+  int64_t wmax = k / 16;
+  if (wmax > a.nwarps - 1) wmax = a.nwarps - 1;
+  double s = 0.0;
+  for (int64_t w = 0; w <= wmax; ++w) s += a.mu_warp[w * a.n_rel * S3 + idx];
+  a.mu[idx] = s;
+}
+
+// Forward-mode dual numbers (value + N tangents) for the release-map adjoint.
+template <int N>
+struct Dual {
+  double v, d[N];
+  __device__ Dual() : v(0.0) {
+#pragma unroll
+    for (int i = 0; i < N; ++i) d[i] = 0.0;
+  }
+  __device__ Dual(double x) : v(x) {  // NOLINT: implicit promotion of constants
+#pragma unroll
+    for (int i = 0; i < N; ++i) d[i] = 0.0;
+  }
+};
+template <int N>
+__device__ Dual<N> operator+(const Dual<N>& a, const Dual<N>& b) {
+  Dual<N> r(a.v + b.v);
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] + b.d[i];
+  return r;
+}
+template <int N>
+__device__ Dual<N> operator-(const Dual<N>& a, const Dual<N>& b) {
+  Dual<N> r(a.v - b.v);
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] - b.d[i];
+  return r;
+}
+template <int N>
+__device__ Dual<N> operator-(const Dual<N>& a) {
+  Dual<N> r(-a.v);
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = -a.d[i];
+  return r;
+}
+template <int N>
+__device__ Dual<N> operator*(const Dual<N>& a, const Dual<N>& b) {
+  Dual<N> r(a.v * b.v);
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = fma(a.d[i], b.v, a.v * b.d[i]);
+  return r;
+}
+template <int N>
+__device__ Dual<N> operator/(const Dual<N>& a, const Dual<N>& b) {
+  const double ib = 1.0 / b.v;
+  Dual<N> r(a.v * ib);
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = (a.d[i] - r.v * b.d[i]) * ib;
+  return r;
+}
+template <int N>
+__device__ Dual<N> operator+(const Dual<N>& a, double b) { return a + Dual<N>(b); }
+template <int N>
+__device__ Dual<N> operator+(double a, const Dual<N>& b) { return Dual<N>(a) + b; }
+template <int N>
+__device__ Dual<N> operator-(const Dual<N>& a, double b) { return a - Dual<N>(b); }
+template <int N>
+__device__ Dual<N> operator-(double a, const Dual<N>& b) { return Dual<N>(a) - b; }
+template <int N>
+__device__ Dual<N> operator*(const Dual<N>& a, double b) { return a * Dual<N>(b); }
+template <int N>
+__device__ Dual<N> operator*(double a, const Dual<N>& b) { return Dual<N>(a) * b; }
+template <int N>
+__device__ Dual<N> operator/(const Dual<N>& a, double b) { return a / Dual<N>(b); }
+template <int N>
+__device__ Dual<N> operator/(double a, const Dual<N>& b) { return Dual<N>(a) / b; }
+template <int N>
+__device__ Dual<N> sqrt(const Dual<N>& a) {
+  const double s = ::sqrt(a.v);
+  Dual<N> r(s);
+  const double f = 0.5 / s;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = f * a.d[i];
+  return r;
+}
+template <int N>
+__device__ Dual<N> log1p(const Dual<N>& a) {
+  Dual<N> r(::log1p(a.v));
+  const double f = 1.0 / (1.0 + a.v);
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = f * a.d[i];
+  return r;
+}
+
+// Hessian of one component at offset d from its centre (same closed forms as
+// comp_hessian), generic in the number type so parameters and positions can
+// carry tangents.
+template <class T>
+__device__ void comp_hessian_t(int kind, const T& Gm, const T& l1, const T& l2, const T* d, T* H) {
+  if (kind == MIYAMOTO_NAGAI) {
+    const T zb = sqrt(d[2] * d[2] + l2 * l2);
+    const T s = zb + l1;
+    const T D2 = d[0] * d[0] + d[1] * d[1] + s * s;
+    const T D = sqrt(D2);
+    const T u = Gm / (D2 * D);
+    const T w = 3.0 * Gm / (D2 * D2 * D);
+    const T v[3] = {d[0], d[1], d[2] * s / zb};
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) H[3 * i + j] = H[3 * i + j] - w * v[i] * v[j];
+    H[0] = H[0] + u;
+    H[4] = H[4] + u;
+    H[8] = H[8] + u * (1.0 + l1 * l2 * l2 / (zb * zb * zb));
+    return;
+  }
+  const T r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2] + TINY;
+  const T r = sqrt(r2);
+  T g, gpr;
+  if (kind == KEPLER) {
+    g = Gm / (r2 * r);
+    gpr = -3.0 * Gm / (r2 * r2 * r);
+  } else if (kind == HERNQUIST) {
+    const T dd = r + l1;
+    g = Gm / (r * dd * dd);
+    gpr = -Gm * (3.0 * r + l1) / (r2 * r * dd * dd * dd);
+  } else if (kind == NFW) {
+    const T Lg = log1p(r / l1), q = l1 + r;
+    g = Gm * (Lg / (r2 * r) - 1.0 / (r2 * q));
+    gpr = Gm * (3.0 / (r2 * r2 * q) - 3.0 * Lg / (r2 * r2 * r) + 1.0 / (r2 * r * q * q));
+  } else {  // PLUMMER
+    const T s2 = r2 + l1 * l1, s = sqrt(s2);
+    g = Gm / (s2 * s);
+    gpr = -3.0 * Gm / (s2 * s2 * s);
+  }
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) H[3 * i + j] = H[3 * i + j] + gpr * d[i] * d[j];
+  H[0] = H[0] + g;
+  H[4] = H[4] + g;
+  H[8] = H[8] + g;
+}
+
+template <class T>
+__device__ T contract_rhat(const T* H, const T* rh) {
+  T s(0.0);
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) s = s + rh[i] * H[3 * i + j] * rh[j];
+  return s;
+}
+
+// The release map's transpose: (dL/dx_p, dL/dv_p) of both particles ->
+// dL/dP[r] (nu) and dL/d(component parameters) through d2Phi/dr2.
+__global__ void __launch_bounds__(128) k_stream_release_adj(StreamDev a, const DevComp* comps) {
+  __shared__ DevComp s_comps[kAdjMaxComps];
+  stage_comps(comps, a.ncomp, s_comps);
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= a.n_rel) return;
+  const double* w = a.P + 6 * r;
+  const double x[3] = {w[0], w[1], w[2]}, v[3] = {w[3], w[4], w[5]};
+  const double rt = a.rt_om[r], om = a.rt_om[a.n_rel + r];
+  const double rr = ::sqrt(fma(x[0], x[0], fma(x[1], x[1], x[2] * x[2])));
+  const double rh[3] = {x[0] / rr, x[1] / rr, x[2] / rr};
+  double g_rt = 0.0, g_om = 0.0, g_rh[3] = {0, 0, 0}, xb[3] = {0, 0, 0}, vb[3] = {0, 0, 0};
+  for (int side = 0; side < 2; ++side) {
+    const double s = side ? 1.0 : -1.0;
+    const int64_t p = 2 * r + side;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const double lx = a.lam_rel[j * a.np + p], lv = a.lam_rel[(3 + j) * a.np + p];
+      const double xi = a.noise[(6 * side + j) * a.n_rel + r];
+      const double eta = a.noise[(6 * side + 3 + j) * a.n_rel + r];
+      g_rt += lx * (s * rh[j] + 0.1 * xi) + lv * (0.1 * om * eta);
+      g_om += lv * (0.1 * rt * eta);
+      g_rh[j] += s * rt * lx;
+      xb[j] += lx;
+      vb[j] += lv;
+    }
+  }
+  // d2Phi/dr2 and its gradient in x (three tangents)
+  Dual<3> X[3], RH[3], Hd[9];
+  for (int j = 0; j < 3; ++j) {
+    X[j] = Dual<3>(x[j]);
+    X[j].d[j] = 1.0;
+  }
+  const Dual<3> R = sqrt(X[0] * X[0] + X[1] * X[1] + X[2] * X[2]);
+  for (int j = 0; j < 3; ++j) RH[j] = X[j] / R;
+  for (int c = 0; c < a.ncomp; ++c) {
+    const DevComp& cc = s_comps[c];
+    const Dual<3> dd[3] = {X[0] - cc.ox, X[1] - cc.oy, X[2] - cc.oz};
+    comp_hessian_t<Dual<3>>(cc.kind, Dual<3>(cc.Gm), Dual<3>(cc.l1), Dual<3>(cc.l2), dd, Hd);
+  }
+  const Dual<3> prr = contract_rhat(Hd, RH);
+  const double D = om * om - prr.v;
+  const double Db = g_rt * (-rt / (3.0 * D));
+  g_om += 2.0 * om * Db;
+  const double prr_b = -Db;
+#pragma unroll
+  for (int j = 0; j < 3; ++j) xb[j] += prr_b * prr.d[j];
+  // parameters: d2Phi/dr2 is linear in each mass; (l1, l2) by two tangents
+  for (int c = 0; c < a.ncomp; ++c) {
+    const DevComp& cc = s_comps[c];
+    Dual<2> l1(cc.l1), l2(cc.l2), Hc[9], dd[3], rhd[3];
+    l1.d[0] = 1.0;
+    l2.d[1] = 1.0;
+    dd[0] = Dual<2>(x[0] - cc.ox);
+    dd[1] = Dual<2>(x[1] - cc.oy);
+    dd[2] = Dual<2>(x[2] - cc.oz);
+    for (int j = 0; j < 3; ++j) rhd[j] = Dual<2>(rh[j]);
+    comp_hessian_t<Dual<2>>(cc.kind, Dual<2>(cc.Gm), l1, l2, dd, Hc);
+    const Dual<2> pc = contract_rhat(Hc, rhd);
+    a.gp_all[(int64_t)(3 * c + 0) * a.ncol + a.np + r] = prr_b * pc.v * cc.inv_m;
+    a.gp_all[(int64_t)(3 * c + 1) * a.ncol + a.np + r] = prr_b * pc.d[0];
+    a.gp_all[(int64_t)(3 * c + 2) * a.ncol + a.np + r] = prr_b * pc.d[1];
+  }
+  a.gp_all[(int64_t)(3 * a.ncomp) * a.ncol + a.np + r] = 0.0;
+  // rhat = x / |x|
+  const double rg = rh[0] * g_rh[0] + rh[1] * g_rh[1] + rh[2] * g_rh[2];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) xb[j] += (g_rh[j] - rg * rh[j]) / rr;
+  // Omega = |x x v| / |x|^2
+  const double L[3] = {x[1] * v[2] - x[2] * v[1], x[2] * v[0] - x[0] * v[2], x[0] * v[1] - x[1] * v[0]};
+  const double Lm = ::sqrt(L[0] * L[0] + L[1] * L[1] + L[2] * L[2]);
+  const double Lh[3] = {L[0] / Lm, L[1] / Lm, L[2] / Lm};
+  const double ir2 = 1.0 / (rr * rr);
+  const double vxL[3] = {v[1] * Lh[2] - v[2] * Lh[1], v[2] * Lh[0] - v[0] * Lh[2], v[0] * Lh[1] - v[1] * Lh[0]};
+  const double Lxx[3] = {Lh[1] * x[2] - Lh[2] * x[1], Lh[2] * x[0] - Lh[0] * x[2], Lh[0] * x[1] - Lh[1] * x[0]};
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    xb[j] += g_om * (vxL[j] * ir2 - 2.0 * om * x[j] * ir2);
+    vb[j] += g_om * Lxx[j] * ir2;
+  }
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    a.nu[6 * r + j] = xb[j];
+    a.nu[6 * r + 3 + j] = vb[j];
+  }
+}
+
+// Reverse sweep of one host-potential step of signed length hs from y with
+// extra cotangents mu (S x 3, may be NULL) on the stage positions.
+template <class TB, class Host>
+__device__ void prog_reverse_step(const Host& h, const DevComp* comps, int ncomp, const double* yk, double hs,
+                                  const double* mu, double* lam, double* gp) {
+  constexpr int S = TB::S;
+  double F[S][6], Yq[S][3];
+  field(h, yk, F[0]);
+  Yq[0][0] = yk[0];
+  Yq[0][1] = yk[1];
+  Yq[0][2] = yk[2];
+  static_for<1, S>([&](auto i) {
+    constexpr int I = decltype(i)::value;
+    double Y[6];
+    stage_state<TB, I>(yk, hs, F, Y);
+    Yq[I][0] = Y[0];
+    Yq[I][1] = Y[1];
+    Yq[I][2] = Y[2];
+    field(h, Y, F[I]);
+  });
+  static_for<0, S>([&](auto i) {
+    constexpr int I = decltype(i)::value;
+    constexpr double bi = TB::B[I];
+#pragma unroll
+    for (int j = 0; j < 6; ++j) F[I][j] = hs * bi * lam[j];
+  });
+  static_for<0, S>([&](auto rr) {
+    constexpr int I = S - 1 - decltype(rr)::value;
+    const double v[3] = {F[I][3], F[I][4], F[I][5]};
+    double Hv[3] = {0.0, 0.0, 0.0};
+    for (int c = 0; c < ncomp; ++c) {
+      double dp[3] = {0.0, 0.0, 0.0};
+      comp_vjp(comps[c], Yq[I], v, Hv, dp);
+      gp[3 * c + 0] -= dp[0];
+      gp[3 * c + 1] -= dp[1];
+      gp[3 * c + 2] -= dp[2];
+    }
+    double Yb[6] = {-Hv[0], -Hv[1], -Hv[2], F[I][0], F[I][1], F[I][2]};
+    if (mu) {
+      Yb[0] += mu[3 * I + 0];
+      Yb[1] += mu[3 * I + 1];
+      Yb[2] += mu[3 * I + 2];
+    }
+#pragma unroll
+    for (int j = 0; j < 6; ++j) lam[j] += Yb[j];
+    static_for<0, I>([&](auto l) {
+      constexpr int L = decltype(l)::value;
+      constexpr double c = TB::A[I][L];
+      if constexpr (c != 0.0) {
+#pragma unroll
+        for (int j = 0; j < 6; ++j) F[L][j] = fma(hs * c, Yb[j], F[L][j]);
+      }
+    });
+  });
+}
+
+template <class TB, class Host>
+__global__ void __launch_bounds__(32) k_stream_progenitor_adj(StreamDev a, Host host, const DevComp* comps) {
+  __shared__ DevComp s_comps[kAdjMaxComps];
+  stage_comps(comps, a.ncomp, s_comps);
+  const Host h = bind_shared(host, s_comps);
+  if (threadIdx.x != 0) return;
+  constexpr int S = TB::S;
+  double lam[6] = {0, 0, 0, 0, 0, 0};
+  double gp[kAdjMaxComps * 3];
+  for (int i = 0; i < kAdjMaxComps * 3; ++i) gp[i] = 0.0;
+  for (int64_t k = a.n_rel - 1; k >= 0; --k) {
+    prog_reverse_step<TB>(h, s_comps, a.ncomp, a.P + 6 * k, a.dt, a.mu + k * S * 3, lam, gp);
+#pragma unroll
+    for (int j = 0; j < 6; ++j) lam[j] += a.nu[6 * k + j];
+  }
+  for (int64_t k = a.n_rel - 1; k >= 0; --k)
+    prog_reverse_step<TB>(h, s_comps, a.ncomp, a.B + 6 * k, -a.dt, nullptr, lam, gp);
+  if (a.grad_w_now)
+    for (int j = 0; j < 6; ++j) a.grad_w_now[j] = lam[j];
+  const int64_t col = a.np + a.n_rel;
+  for (int c = 0; c < 3 * a.ncomp; ++c) a.gp_all[(int64_t)c * a.ncol + col] = gp[c];
+  a.gp_all[(int64_t)(3 * a.ncomp) * a.ncol + col] = 0.0;
+}
+
+__global__ void k_stream_reduce_rows(const double* __restrict__ in, int64_t n, double* __restrict__ out) {
+  __shared__ double red[256];
+  const double* row = in + (int64_t)blockIdx.x * n;
+  double s = 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s += row[i];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[blockIdx.x] = red[0];
+}
+
+// ------------------------------------------------------------------ host side
+static size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+struct StreamLayout {
+  size_t B, P, Q, rt_om, ics, fin, ckpt, seg, lam_rel, mu_warp, mu, nu, gp_all, red, total;
+  int64_t np, nwarps, nseg, ncol;
+  int S;
+};
+
+static StreamLayout stream_layout(int ncomp, const gal_stream_config& c, bool grad) {
+  StreamLayout L{};
+  L.S = c.method == 5 ? Dopri5::S : Dopri8::S;
+  L.np = 2 * c.n_release;
+  L.nwarps = (L.np + 31) / 32;
+  const int K = c.k_ckpt > 0 ? c.k_ckpt : 1;
+  L.nseg = (c.n_release + K - 1) / K;
+  L.ncol = L.np + c.n_release + 1;
+  const size_t d = sizeof(double);
+  const size_t nr = (size_t)c.n_release;
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    const size_t o = off;
+    off += al256(bytes);
+    return o;
+  };
+  L.B = take(d * 6 * (nr + 1));
+  L.P = take(d * 6 * (nr + 1));
+  L.Q = take(d * 3 * L.S * nr);
+  L.rt_om = take(d * 2 * nr);
+  L.ics = take(d * 6 * L.np);
+  L.fin = take(d * 6 * L.np);
+  if (grad) {
+    L.ckpt = take(d * 6 * L.nseg * L.np);
+    L.seg = take(d * 6 * (size_t)K * L.np);
+    L.lam_rel = take(d * 6 * L.np);
+    L.mu_warp = take(d * 3 * L.S * nr * L.nwarps);
+    L.mu = take(d * 3 * L.S * nr);
+    L.nu = take(d * 6 * nr);
+    L.gp_all = take(d * (3 * (size_t)ncomp + 1) * L.ncol);
+    L.red = take(d * (3 * (size_t)ncomp + 1));
+  }
+  L.total = off;
+  return L;
+}
+
+static gal_status stream_validate(const gal_potential* pot, const gal_stream_config* c) {
+  if (!pot || !c) return fail(GAL_ERR_INVALID_ARGUMENT, "NULL potential or stream configuration");
+  if (c->method != 5 && c->method != 8) return fail(GAL_ERR_INVALID_ARGUMENT, "method must be 5 or 8");
+  if (!(c->dt > 0.0)) return fail(GAL_ERR_INVALID_ARGUMENT, "dt must be > 0");
+  if (c->n_release < 1) return fail(GAL_ERR_INVALID_ARGUMENT, "n_release must be >= 1");
+  if (c->k_ckpt < 1) return fail(GAL_ERR_INVALID_ARGUMENT, "k_ckpt must be >= 1");
+  if (!(c->prog_m > 0.0) || !(c->prog_b > 0.0)) return fail(GAL_ERR_INVALID_ARGUMENT, "progenitor m, b must be > 0");
+  if (pot->n > kAdjMaxComps) return fail(GAL_ERR_UNSUPPORTED, "stream host potentials have at most 8 components");
+  return GAL_OK;
+}
+
+static StreamDev stream_args(const gal_potential* pot, const gal_stream_config* c, const StreamLayout& L, char* ws,
+                             const double* noise, bool grad) {
+  StreamDev a{};
+  a.n_rel = c->n_release;
+  a.np = L.np;
+  a.nwarps = L.nwarps;
+  a.ncol = L.ncol;
+  a.dt = c->dt;
+  a.GMp = pot->G * c->prog_m;
+  a.b2 = c->prog_b * c->prog_b;
+  for (int j = 0; j < 6; ++j) a.w_now[j] = c->w_now[j];
+  a.k_ckpt = c->k_ckpt;
+  a.ncomp = pot->n;
+  auto at = [&](size_t o) { return reinterpret_cast<double*>(ws + o); };
+  a.B = at(L.B);
+  a.P = at(L.P);
+  a.Q = at(L.Q);
+  a.rt_om = at(L.rt_om);
+  a.noise = noise;
+  a.ics = at(L.ics);
+  a.fin = at(L.fin);
+  if (grad) {
+    a.ckpt = at(L.ckpt);
+    a.seg = at(L.seg);
+    a.lam_rel = at(L.lam_rel);
+    a.mu_warp = at(L.mu_warp);
+    a.mu = at(L.mu);
+    a.nu = at(L.nu);
+    a.gp_all = at(L.gp_all);
+  }
+  return a;
+}
+
+template <class TB, class Host>
+static cudaError_t stream_forward(const StreamDev& a, const Host& host, const DevComp* comps, cudaStream_t s) {
+  k_stream_progenitor<TB, Host><<<1, 32, 0, s>>>(a, host, comps);
+  k_stream_release<<<(unsigned)((a.n_rel + 127) / 128), 128, 0, s>>>(a, comps);
+  k_stream_particles<TB, Host><<<(unsigned)((a.np + 31) / 32), 32, 0, s>>>(a, host, comps);
+  return cudaGetLastError();
+}
+
+template <class TB, class Host>
+static cudaError_t stream_backward(const StreamDev& a, const Host& host, const DevComp* comps, cudaStream_t s) {
+  k_stream_particles_adj<TB, Host><<<(unsigned)a.nwarps, 32, 0, s>>>(a, host, comps);
+  const int S3 = 3 * TB::S;
+  k_stream_mu_reduce<<<(unsigned)((a.n_rel * S3 + 255) / 256), 256, 0, s>>>(a, S3);
+  k_stream_release_adj<<<(unsigned)((a.n_rel + 127) / 128), 128, 0, s>>>(a, comps);
+  k_stream_progenitor_adj<TB, Host><<<1, 32, 0, s>>>(a, host, comps);
+  return cudaGetLastError();
+}
+
+template <class Fn>
+static cudaError_t dispatch(const gal_potential* pot, int method, Fn&& fn) {
+  if (method == 8) {
+    if (pot->is_mw) return fn(Dopri8{}, MWPot{pot->mw});
+    return fn(Dopri8{}, TablePot{pot->d_comps, pot->n});
+  }
+  if (pot->is_mw) return fn(Dopri5{}, MWPot{pot->mw});
+  return fn(Dopri5{}, TablePot{pot->d_comps, pot->n});
+}
+
+}  // namespace gal
+
+using namespace gal;
+
+extern "C" {
+
+gal_status gal_stream_workspace_size(const gal_potential* pot, const gal_stream_config* cfg, int32_t with_grad,
+                                     size_t* bytes) {
+  gal_status st = stream_validate(pot, cfg);
+  if (st != GAL_OK) return st;
+  if (!bytes) return fail(GAL_ERR_INVALID_ARGUMENT, "bytes is NULL");
+  *bytes = stream_layout(pot->n, *cfg, with_grad != 0).total;
+  return GAL_OK;
+}
+
+gal_status gal_stream_run(const gal_potential* pot, const gal_stream_config* cfg, const double* noise,
+                          double* final_states, double* ics, double* prog_track, void* workspace,
+                          size_t workspace_bytes, gal_stream_t stream) {
+  gal_status st = stream_validate(pot, cfg);
+  if (st != GAL_OK) return st;
+  if (!noise || !final_states) return fail(GAL_ERR_INVALID_ARGUMENT, "NULL noise or output");
+  const StreamLayout L = stream_layout(pot->n, *cfg, false);
+  if (!workspace || workspace_bytes < L.total) return fail(GAL_ERR_WORKSPACE, "workspace too small");
+  char* ws = static_cast<char*>(workspace);
+  StreamDev a = stream_args(pot, cfg, L, ws, noise, false);
+  a.fin = final_states;
+  if (ics) a.ics = ics;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e = dispatch(pot, cfg->method, [&](auto tb, auto host) {
+    return stream_forward<decltype(tb)>(a, host, pot->d_comps, s);
+  });
+  if (e != cudaSuccess) return cuda_fail(e, "stream kernels");
+  if (prog_track) {
+    e = cudaMemcpyAsync(prog_track, a.P, sizeof(double) * 6 * (size_t)(cfg->n_release + 1), cudaMemcpyDeviceToDevice,
+                        s);
+    if (e != cudaSuccess) return cuda_fail(e, "copying the progenitor track");
+  }
+  return GAL_OK;
+}
+
+gal_status gal_stream_grad(const gal_potential* pot, const gal_stream_config* cfg, const double* noise,
+                           const double* target, double* final_states, double* grad_params, double* grad_w_now,
+                           double* loss, void* workspace, size_t workspace_bytes, gal_stream_t stream) {
+  gal_status st = stream_validate(pot, cfg);
+  if (st != GAL_OK) return st;
+  if (!noise || !target || !grad_params) return fail(GAL_ERR_INVALID_ARGUMENT, "NULL noise, target or gradient");
+  const StreamLayout L = stream_layout(pot->n, *cfg, true);
+  if (!workspace || workspace_bytes < L.total) return fail(GAL_ERR_WORKSPACE, "workspace too small");
+  char* ws = static_cast<char*>(workspace);
+  StreamDev a = stream_args(pot, cfg, L, ws, noise, true);
+  if (final_states) a.fin = final_states;
+  a.target = target;
+  a.grad_w_now = grad_w_now;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e = dispatch(pot, cfg->method, [&](auto tb, auto host) {
+    cudaError_t e1 = stream_forward<decltype(tb)>(a, host, pot->d_comps, s);
+    if (e1 != cudaSuccess) return e1;
+    return stream_backward<decltype(tb)>(a, host, pot->d_comps, s);
+  });
+  if (e != cudaSuccess) return cuda_fail(e, "stream gradient kernels");
+  double* red = reinterpret_cast<double*>(ws + L.red);
+  k_stream_reduce_rows<<<(unsigned)(3 * pot->n + 1), 256, 0, s>>>(a.gp_all, L.ncol, red);
+  e = cudaGetLastError();
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(grad_params, red, sizeof(double) * 3 * pot->n, cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess && loss) e = cudaMemcpyAsync(loss, red + 3 * pot->n, sizeof(double), cudaMemcpyDeviceToDevice, s);
+  return e == cudaSuccess ? GAL_OK : cuda_fail(e, "stream gradient reduction");
+}
+
+}  // extern "C"

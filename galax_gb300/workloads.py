@@ -93,3 +93,34 @@ def training_points(n: int, seed: int = 30, rmin: float = 0.1, rmax: float = 200
     rng = np.random.default_rng(seed)
     r = np.exp(rng.uniform(np.log(rmin), np.log(rmax), n))
     return isotropic(rng, n) * r[:, None]
+
+
+@dataclass
+class StreamSetup:
+    w_now: np.ndarray     # (6,) progenitor phase-space point at t_now
+    t_now: float
+    dt: float
+    n_release: int        # release times t_now - (n_release - r) dt, r = 0..n_release-1
+    prog_m: float
+    prog_b: float
+    noise: np.ndarray     # (n_release, 12): xi_lead, eta_lead, xi_trail, eta_trail ~ N(0, 1)
+    pert: np.ndarray      # (2 n_release, 6): target offsets (N(0, 0.1 kpc), N(0, 2 km/s))
+
+
+def stream_setup(grad, n_release: int = 3000, dt: float = 1.0, seed: int = 4, apocentre: float = 20.0,
+                 speed_frac: float = 0.6, incl_deg: float = 30.0, prog_m: float = 1e5,
+                 prog_b: float = 0.02) -> StreamSetup:
+    """The stream-like batched-gradient workload: a Plummer progenitor (1e5 Msun,
+    b = 20 pc) at apocentre (x = apocentre kpc, velocity speed_frac v_c
+    tangential, inclined incl_deg to the x-y plane) at t_now = 0, released
+    over n_release dt before the present, two particles per release with
+    seeded Gaussian offsets, and seeded target perturbations for the loss."""
+    rng = np.random.default_rng(seed)
+    x = np.array([[apocentre, 0.0, 0.0]])
+    vc = float(circular_speed(grad, x)[0])
+    inc = np.deg2rad(incl_deg)
+    w_now = np.array([apocentre, 0.0, 0.0, 0.0, speed_frac * vc * np.cos(inc), speed_frac * vc * np.sin(inc)])
+    noise = rng.normal(size=(n_release, 12))
+    pert = np.concatenate([rng.normal(0.0, 0.1, (2 * n_release, 3)), rng.normal(0.0, 2 * KMS, (2 * n_release, 3))],
+                          axis=1)
+    return StreamSetup(w_now, 0.0, dt, n_release, prog_m, prog_b, noise, pert)

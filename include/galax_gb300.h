@@ -213,6 +213,56 @@ GAL_API gal_status gal_adjoint(const gal_potential* pot, const gal_solver_config
                        double* grad_params, int32_t k_ckpt, int64_t n, void* workspace, size_t workspace_bytes,
                        gal_stream_t stream);
 
+/* ------------------------------------------------------------------ mock stream */
+/* A stream released by a Plummer progenitor that moves along its own orbit in
+ * the host potential `pot` (at most 8 components). Replaces galax's
+ * StreamSimulator.init/run (src/galax/dynamics/_src/experimental/stream.py:121-230,
+ * 380-446) and MockStreamGenerator.run with a moving progenitor potential
+ * (legacy/mockstream/mockstream_generator.py:160-275, legacy/mockstream/_moving.py:20-42)
+ * for releases on a constant-step grid:
+ *  - the progenitor starts at w_now (time t_now), is integrated n_release steps
+ *    of dt backwards, then forwards again to t_now;
+ *  - release r = 0..n_release-1 happens at t_now - (n_release - r) dt with the
+ *    King (1962) tidal radius r_t = cbrt(G prog_m / (Omega^2 - d2Phi/dr2))
+ *    (dynamics/_src/cluster/radius.py:198-214) and sends particle 2r (leading)
+ *    and 2r+1 (trailing): x = x_prog -/+ r_t rhat + 0.1 r_t xi,
+ *    v = v_prog + 0.1 Omega r_t eta (xi, eta from `noise`);
+ *  - every particle is integrated to t_now in pot + Plummer(prog_m, prog_b)
+ *    centred on the progenitor's position at every Runge-Kutta stage.
+ * Constant steps (Dopri5 or Dopri8). noise: [12][n_release] device array, rows
+ * xi_lead(3), eta_lead(3), xi_trail(3), eta_trail(3). */
+typedef struct gal_stream_config {
+  int32_t method;    /* 5 = Dopri5, 8 = Dopri8 */
+  int32_t k_ckpt;    /* gradient: particle checkpoint interval in steps (>= 1) */
+  int64_t n_release; /* releases (>= 1); particles = 2 n_release */
+  double dt;         /* constant step (> 0) */
+  double t_now;      /* present time (the potential is static: only labels times) */
+  double prog_m;     /* progenitor Plummer mass */
+  double prog_b;     /* progenitor Plummer scale radius */
+  double w_now[6];   /* progenitor phase-space point at t_now (host values) */
+} gal_stream_config;
+
+/* Scratch bytes for gal_stream_run (with_grad = 0) or gal_stream_grad (1). */
+GAL_API gal_status gal_stream_workspace_size(const gal_potential* pot, const gal_stream_config* cfg,
+                                             int32_t with_grad, size_t* bytes);
+/* Forward simulation: final_states [6][2 n_release] at t_now; optionally the
+ * release conditions ics [6][2 n_release] and the progenitor's forwards track
+ * prog_track [n_release + 1][6] (NULL to skip). */
+GAL_API gal_status gal_stream_run(const gal_potential* pot, const gal_stream_config* cfg, const double* noise,
+                                  double* final_states, double* ics, double* prog_track, void* workspace,
+                                  size_t workspace_bytes, gal_stream_t stream);
+/* Gradient of L = sum_p |y_p(t_now) - target_p|^2 (target [6][2 n_release])
+ * with respect to (m, l1, l2) of every host component, grad_params [ncomp][3],
+ * through the particle orbits, the release conditions (tidal radius included)
+ * and the progenitor's orbit, by a hand-written discrete adjoint (galax takes
+ * jax derivatives through the same pipeline; diffrax ForwardMode is the
+ * stream solver's default, experimental/stream.py:35-43). Optional outputs:
+ * final_states [6][2 n_release], grad_w_now [6] = dL/dw_now, loss [1] (device). */
+GAL_API gal_status gal_stream_grad(const gal_potential* pot, const gal_stream_config* cfg, const double* noise,
+                                   const double* target, double* final_states, double* grad_params,
+                                   double* grad_w_now, double* loss, void* workspace, size_t workspace_bytes,
+                                   gal_stream_t stream);
+
 /* ------------------------------------------------------------------ learned surrogate */
 /* A small MLP, 3 -> 256 -> 256 -> 256 -> 256 -> 1 with SiLU activations, that
  * stands in for an expensive composite (the north-star's MilkyWayPotential plus

@@ -788,6 +788,186 @@ int orc_adjoint_fixed(const Comp* comps, int ncomp, double G, const OrcSolverCfg
   return 0;
 }
 
+// ---------------------------------------------------------------------------
+// Stream with a moving progenitor (test infrastructure for the stream row).
+//
+// Follows the reference's mock-stream pipeline
+// (src/galax/dynamics/_src/experimental/stream.py:121-230 init: integrate the
+// progenitor to the first release time, then along the release times;
+// stream.py:380-446 run: every particle from its release time to the present;
+// legacy/mockstream/mockstream_generator.py:160-275 with a progenitor potential
+// moved along the progenitor's orbit, legacy/mockstream/_moving.py:20-42),
+// with the release model of the King (1962) tidal radius
+// (src/galax/dynamics/_src/cluster/radius.py:198-214:
+// r_t = cbrt(G M / (Omega^2 - d2Phi/dr2)), Omega = |x x v| / r^2 from
+// dynamics/_src/register_api.py:82-88, d2Phi/dr2 = rhat . H . rhat from
+// potential/_src/register_funcs.py:444-457).
+//
+// Grid: constant steps dt. The progenitor is integrated backwards from
+// (w_now, t_now) to t_now - n_rel dt, then forwards to t_now, recording its
+// state at every grid time and its position at every stage of every forward
+// step. Release r happens at grid time r; its two particles are integrated
+// from there to t_now in the host potential plus a Plummer sphere (mass
+// prog_m, radius prog_b) centred on the progenitor's stage positions, i.e.
+// exactly the particle half of the coupled particle + progenitor system.
+// Particle ICs (p = 2 r + side, side 0 = leading, 1 = trailing):
+//   x = x_prog + s r_t rhat + 0.1 r_t xi_p,  v = v_prog + 0.1 Omega r_t eta_p,
+//   s = -1 (leading) / +1 (trailing), xi, eta = given standard-normal draws.
+// ---------------------------------------------------------------------------
+namespace orc {
+
+static void stage_positions_step(const Pot& P, const Tableau& TB, const double* y, double h, double sign,
+                                 double* ynew, double* Q /* s x 3 */) {
+  double F[13 * 6], Y[6];
+  field<double>(P, sign, y, F);
+  for (int j = 0; j < 3; ++j) Q[j] = y[j];
+  for (int i = 1; i < TB.s; ++i) {
+    for (int j = 0; j < 6; ++j) {
+      double acc = 0;
+      bool first = true;
+      for (int l = 0; l < i; ++l)
+        if (TB.a[i][l] != 0.0) {
+          double t = TB.a[i][l] * F[6 * l + j];
+          acc = first ? t : acc + t;
+          first = false;
+        }
+      Y[j] = y[j] + h * acc;
+    }
+    for (int j = 0; j < 3; ++j) Q[3 * i + j] = Y[j];
+    field<double>(P, sign, Y, F + 6 * i);
+  }
+  for (int j = 0; j < 6; ++j) {
+    double acc = 0;
+    bool first = true;
+    for (int l = 0; l < TB.s; ++l)
+      if (TB.b[l] != 0.0) {
+        double t = TB.b[l] * F[6 * l + j];
+        acc = first ? t : acc + t;
+        first = false;
+      }
+    ynew[j] = y[j] + h * acc;
+  }
+}
+
+// field of a particle: host potential + Plummer(prog_m, prog_b) at Qi
+static void particle_field(const Pot& P, double Gmp, double b2, const double* Qi, const double* y, double* dy) {
+  double g[3];
+  gradient<double>(P, y, g);
+  double d[3] = {y[0] - Qi[0], y[1] - Qi[1], y[2] - Qi[2]};
+  double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2] + TINY;
+  double s2 = r2 + b2;
+  double f = Gmp / (s2 * std::sqrt(s2));
+  for (int j = 0; j < 3; ++j) g[j] += f * d[j];
+  dy[0] = y[3]; dy[1] = y[4]; dy[2] = y[5];
+  dy[3] = -g[0]; dy[4] = -g[1]; dy[5] = -g[2];
+}
+
+static void particle_step(const Pot& P, const Tableau& TB, double Gmp, double b2, const double* Qk, double* y,
+                          double h) {
+  double F[13 * 6], Y[6];
+  particle_field(P, Gmp, b2, Qk, y, F);
+  for (int i = 1; i < TB.s; ++i) {
+    for (int j = 0; j < 6; ++j) {
+      double acc = 0;
+      bool first = true;
+      for (int l = 0; l < i; ++l)
+        if (TB.a[i][l] != 0.0) {
+          double t = TB.a[i][l] * F[6 * l + j];
+          acc = first ? t : acc + t;
+          first = false;
+        }
+      Y[j] = y[j] + h * acc;
+    }
+    particle_field(P, Gmp, b2, Qk + 3 * i, Y, F + 6 * i);
+  }
+  double y1[6];
+  for (int j = 0; j < 6; ++j) {
+    double acc = 0;
+    bool first = true;
+    for (int l = 0; l < TB.s; ++l)
+      if (TB.b[l] != 0.0) {
+        double t = TB.b[l] * F[6 * l + j];
+        acc = first ? t : acc + t;
+        first = false;
+      }
+    y1[j] = y[j] + h * acc;
+  }
+  for (int j = 0; j < 6; ++j) y[j] = y1[j];
+}
+
+}  // namespace orc
+
+// prog_track: (n_rel + 1) x 6 forward states; ics, final_: 2 n_rel x 6;
+// noise: n_rel x 12 (xi_lead, eta_lead, xi_trail, eta_trail); rt_om: n_rel x 2 (r_t, Omega).
+int orc_stream_forward(const Comp* comps, int ncomp, double G, int method, double prog_m, double prog_b,
+                       const double* w_now, double t_now, double dt, int64_t n_rel, const double* noise,
+                       double* prog_track, double* rt_om, double* ics, double* final_, int nthreads) {
+  Pot P{comps, ncomp, G};
+  const Tableau& TB = (method == 5) ? DOPRI5 : DOPRI8;
+  const int S = TB.s;
+  // backwards from t_now (reversed time, tau = -t, constant steps dt)
+  double y[6], ynew[6];
+  std::vector<double> Qb((size_t)S * 3);
+  for (int j = 0; j < 6; ++j) y[j] = w_now[j];
+  for (int64_t k = 0; k < n_rel; ++k) {
+    stage_positions_step(P, TB, y, dt, -1.0, ynew, Qb.data());
+    for (int j = 0; j < 6; ++j) y[j] = ynew[j];
+  }
+  // forwards, recording states and stage positions
+  std::vector<double> Q((size_t)n_rel * S * 3);
+  for (int j = 0; j < 6; ++j) prog_track[j] = y[j];
+  for (int64_t k = 0; k < n_rel; ++k) {
+    stage_positions_step(P, TB, y, dt, 1.0, ynew, Q.data() + (size_t)k * S * 3);
+    for (int j = 0; j < 6; ++j) {
+      y[j] = ynew[j];
+      prog_track[6 * (k + 1) + j] = y[j];
+    }
+  }
+  const double GM = G * prog_m, b2 = prog_b * prog_b;
+  // release: King tidal radius and the particle ICs
+  for (int64_t r = 0; r < n_rel; ++r) {
+    const double* w = prog_track + 6 * r;
+    const double* x = w;
+    const double* v = w + 3;
+    double rr = std::sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+    double rh[3] = {x[0] / rr, x[1] / rr, x[2] / rr};
+    double L[3] = {x[1] * v[2] - x[2] * v[1], x[2] * v[0] - x[0] * v[2], x[0] * v[1] - x[1] * v[0]};
+    double om = std::sqrt(L[0] * L[0] + L[1] * L[1] + L[2] * L[2]) / (rr * rr);
+    double H[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int c = 0; c < ncomp; ++c) comp_hessian(comps[c], G, x, H);
+    double prr = 0;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) prr += rh[i] * H[3 * i + j] * rh[j];
+    double rt = std::cbrt(GM / (om * om - prr));
+    rt_om[2 * r] = rt;
+    rt_om[2 * r + 1] = om;
+    for (int side = 0; side < 2; ++side) {
+      const double s = side == 0 ? -1.0 : 1.0;
+      const double* xi = noise + 12 * r + 6 * side;
+      const double* eta = xi + 3;
+      double* o = ics + 6 * (2 * r + side);
+      for (int j = 0; j < 3; ++j) {
+        o[j] = x[j] + s * rt * rh[j] + 0.1 * rt * xi[j];
+        o[3 + j] = v[j] + 0.1 * om * rt * eta[j];
+      }
+    }
+  }
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+  (void)nthreads;
+#endif
+#pragma omp parallel for schedule(dynamic, 4)
+  for (int64_t p = 0; p < 2 * n_rel; ++p) {
+    const int64_t r = p / 2;
+    double yp[6];
+    for (int j = 0; j < 6; ++j) yp[j] = ics[6 * p + j];
+    for (int64_t k = r; k < n_rel; ++k) particle_step(P, TB, GM, b2, Q.data() + (size_t)k * S * 3, yp, dt);
+    for (int j = 0; j < 6; ++j) final_[6 * p + j] = yp[j];
+  }
+  return 0;
+}
+
 // Count algorithmic FP64 operations of one gradient evaluation and one RK step
 // (without the controller). out: [add, mul, div, sqrt, log1p] for the
 // gradient, then the same five for a full step of `method`.

@@ -265,3 +265,51 @@ def count_ops(c: np.ndarray, method: int, y=(8.0, 1.0, 0.5, 0.0, 0.2, 0.01), G: 
 
 def nthreads_default() -> int:
     return os.cpu_count() or 1
+
+
+def stream_forward(c: np.ndarray, setup, *, method: int = 8, G: float = G_GALACTIC, nthreads: int = 0):
+    """The stream pipeline with a moving progenitor on the CPU (see
+    orc_stream_forward). ``setup`` carries w_now, t_now, dt, n_release,
+    prog_m, prog_b, noise. Returns dict(track (n_rel+1, 6), rt_om (n_rel, 2),
+    ics (2 n_rel, 6), final (2 n_rel, 6))."""
+    L = lib()
+    if not hasattr(L, "_stream_bound"):
+        dp = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+        cp = np.ctypeslib.ndpointer(COMP_DTYPE, flags="C_CONTIGUOUS")
+        L.orc_stream_forward.argtypes = [cp, C.c_int, C.c_double, C.c_int, C.c_double, C.c_double, dp, C.c_double,
+                                         C.c_double, C.c_int64, dp, dp, dp, dp, dp, C.c_int]
+        L.orc_stream_forward.restype = C.c_int
+        L._stream_bound = True
+    n = int(setup.n_release)
+    track = np.empty((n + 1, 6))
+    rt_om = np.empty((n, 2))
+    ics = np.empty((2 * n, 6))
+    final = np.empty((2 * n, 6))
+    L.orc_stream_forward(np.ascontiguousarray(c), len(c), G, method, float(setup.prog_m), float(setup.prog_b),
+                         np.ascontiguousarray(setup.w_now, np.float64), float(setup.t_now), float(setup.dt), n,
+                         np.ascontiguousarray(setup.noise, np.float64), track, rt_om, ics, final, nthreads)
+    return dict(track=track, rt_om=rt_om, ics=ics, final=final)
+
+
+def stream_loss(c: np.ndarray, setup, target, **kw) -> float:
+    f = stream_forward(c, setup, **kw)["final"]
+    return float(np.sum((f - target) ** 2))
+
+
+def stream_fd_grad(c: np.ndarray, setup, target, params, *, rel_h: float = 1e-5, **kw) -> np.ndarray:
+    """Central finite differences of the stream loss with one Richardson
+    extrapolation, for parameters given as (component, field) pairs with field
+    in ("m", "l1", "l2"). Returns an array of len(params)."""
+    out = []
+    for ci, fld in params:
+        x0 = float(c[ci][fld])
+
+        def d(h):
+            cp_, cm_ = c.copy(), c.copy()
+            cp_[ci][fld] = x0 + h
+            cm_[ci][fld] = x0 - h
+            return (stream_loss(cp_, setup, target, **kw) - stream_loss(cm_, setup, target, **kw)) / (2 * h)
+
+        h = rel_h * abs(x0)
+        out.append((4.0 * d(h / 2) - d(h)) / 3.0)
+    return np.array(out)

@@ -136,3 +136,6 @@ def test_flop_constants_match_counted_oracle():
         g, s = O.count_ops(O.milky_way(), method)
         assert sum(g.values()) == flops.GRADIENT_FLOPS_MW
         assert sum(s.values()) == flops.STEP_FLOPS_MW[method]
+        c = np.concatenate([O.milky_way(), O.comps([(O.PLUMMER, 1e5, 0.02, 0.0, (1.0, 2.0, 3.0))])])
+        _, s = O.count_ops(c, method)
+        assert sum(s.values()) == flops.STEP_FLOPS_MW_PLUMMER[method]

@@ -1,8 +1,8 @@
 // Tensor-core inference of the potential-surrogate MLP: potential and its
 // gradient (the acceleration) at n positions, one fused kernel.
 //
-// One CTA per SM, persistent over tiles of 128 points, 256 threads (two per
-// point: each handles 128 of the 256 hidden units). Per tile:
+// One CTA per SM, persistent over tiles of 128 points, warp-specialised (a
+// weight-copy warp, a tensor-core warp, eight epilogue warps). Per tile:
 //   layer 1 (3 -> 256) on CUDA cores -> h1 (bf16) into the shared-memory
 //   operand tile; then six 128x256x256 products on the tensor cores
 //   (tcgen05.mma kind::f16, bf16 x bf16 -> f32 accumulator in TMEM):
@@ -11,8 +11,8 @@
 //   with d4 = silu'(z4) w5, d3 = silu'(z3) u3, d2 = silu'(z2) u2 (bf16), and
 //   grad_u out = (silu'(z1) u1) W1 on CUDA cores. silu'(z2), silu'(z3) wait in
 //   TMEM as packed bf16 pairs; every operand tile is rewritten in place.
-// Weights stream through a three-stage ring of 32 KB K-blocks (bulk copies from
-// pre-swizzled global images) overlapping the products. The numerics are those
+// Weights stream through a four-stage ring of 32 KB K-blocks (bulk copies from
+// pre-swizzled global images) run by their own warp ahead of the products. The numerics are those
 // of the training kernels' quantised forward/backward (mlp_train.cu).
 //
 // Every mbarrier wait is bounded: on timeout the kernel records an error code,
@@ -30,8 +30,9 @@ namespace gal {
 namespace mlp {
 
 constexpr int TILE = 128;
-constexpr int NTHREADS = 256;
-constexpr int STAGES = 3;
+constexpr int EPI_WARPS = 8;                            // two per TMEM lane quadrant: column halves
+constexpr int NTHREADS = 64 + 32 * EPI_WARPS;           // warp 0 copies weights, warp 1 issues products
+constexpr int STAGES = 4;
 constexpr uint32_t KBLOCK_BYTES = 256 * 128;           // 256 rows x 64 bf16
 constexpr int KBLOCKS_PER_GEMM = 4;
 constexpr int GEMMS = 6;
@@ -39,15 +40,17 @@ constexpr int KBLOCKS_PER_TILE = GEMMS * KBLOCKS_PER_GEMM;  // 24
 constexpr uint32_t A_BYTES = TILE * 256 * 2;            // 64 KB
 constexpr uint32_t SMEM_A = 0;
 constexpr uint32_t SMEM_RING = A_BYTES;
-constexpr uint32_t SMEM_SMALL = SMEM_RING + STAGES * KBLOCK_BYTES;  // 160 KB
+constexpr uint32_t SMEM_SMALL = SMEM_RING + STAGES * KBLOCK_BYTES;  // 192 KB
 constexpr int SMALL_FLOATS = H * 3 + 5 * H + 1;         // W1, b1, b2, b3, b4, w5, b5
 constexpr uint32_t SMEM_PART = SMEM_SMALL + ((SMALL_FLOATS * 4 + 255) / 256) * 256;
-constexpr uint32_t SMEM_BAR = SMEM_PART + TILE * 4 * 4;
+constexpr uint32_t SMEM_READY = SMEM_PART + TILE * 4 * 4;
+constexpr uint32_t SMEM_BAR = SMEM_READY + TILE * 4;
 constexpr uint32_t SMEM_TOTAL = SMEM_BAR + 256;
 constexpr uint32_t SMEM_ALLOC = SMEM_TOTAL + 1024;      // room to align the base to 1024
 constexpr uint32_t WAIT_LIMIT = 1u << 24;
 constexpr uint32_t TMEM_COLS = 512;
 constexpr uint32_t COL_S2 = 256, COL_S3 = 384;          // packed silu'(z2), silu'(z3)
+static_assert(SMEM_ALLOC <= 227 * 1024, "shared memory budget");
 
 struct InferArgs {
   const double* x;       // [3][n]
@@ -63,50 +66,22 @@ struct InferArgs {
   int* err;
 };
 
-struct Ring {
-  uint64_t* full;
-  uint64_t* empty;
-  uint8_t* buf;
-  const uint8_t* wimg;
-  int64_t total;  // K-blocks this CTA will consume
-};
-
-// issue the bulk copy of K-block jj (thread 0 only)
-__device__ __forceinline__ bool produce(const Ring& r, int64_t jj) {
-  if (jj >= r.total) return true;
-  const int s = (int)(jj % STAGES);
-  const int64_t use = jj / STAGES;
-  if (use > 0 && !tc::mbar_wait(&r.empty[s], (uint32_t)((use - 1) & 1), WAIT_LIMIT)) return false;
-  tc::mbar_expect_tx(&r.full[s], KBLOCK_BYTES);
-  tc::bulk_g2s(r.buf + (size_t)s * KBLOCK_BYTES, r.wimg + (size_t)(jj % KBLOCKS_PER_TILE) * KBLOCK_BYTES,
-               KBLOCK_BYTES, &r.full[s]);
-  return true;
-}
-
-// one 128x256x256 product: D[tmem] = A[smem tile] x (K-blocks j0..j0+3)^T
-__device__ __forceinline__ bool issue_gemm(const Ring& r, int64_t j0, uint32_t a_base, uint32_t tmem,
-                                           uint64_t* mma_bar) {
-  constexpr uint32_t idesc = tc::idesc_bf16(TILE, 256);
-  for (int kb = 0; kb < KBLOCKS_PER_GEMM; ++kb) {
-    const int64_t j = j0 + kb;
-    const int s = (int)(j % STAGES);
-    if (!tc::mbar_wait(&r.full[s], (uint32_t)((j / STAGES) & 1), WAIT_LIMIT)) return false;
-    tc::tc_fence_after();
-    const uint32_t b_base = tc::smem_u32(r.buf + (size_t)s * KBLOCK_BYTES);
-#pragma unroll
-    for (int ks = 0; ks < 4; ++ks) {
-      const uint64_t ad = tc::desc_sw128(a_base + kb * (TILE * 128) + ks * 32);
-      const uint64_t bd = tc::desc_sw128(b_base + ks * 32);
-      tc::mma_bf16(tmem, ad, bd, idesc, (kb | ks) != 0);
-    }
-    tc::mma_commit(&r.empty[s]);       // stage free once these products complete
-    if (!produce(r, j + 2)) return false;
+// Bounded wait that also gives up as soon as another role has aborted.
+__device__ __forceinline__ bool wait_bar(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
+  for (uint32_t i = 0; i < WAIT_LIMIT; ++i) {
+    if (tc::mbar_try_wait(bar, parity)) return true;
+    if ((i & 255) == 255 && *abort_flag) return false;
   }
-  tc::mma_commit(mma_bar);
-  return true;
+  return false;
 }
 
-__device__ __forceinline__ float sig(float z) { return tc::rcp_approx(1.0f + __expf(-z)); }
+__device__ __forceinline__ void set_abort(volatile int* abort_flag, int* err, int code) {
+  *abort_flag = 1;
+  if (err) atomicExch(err, code);
+}
+
+// sigmoid from one SFU operation: 1 / (1 + e^-z) = (1 + tanh(z / 2)) / 2
+__device__ __forceinline__ float sig(float z) { return fmaf(0.5f, tc::tanh_approx(0.5f * z), 0.5f); }
 
 // write 32 consecutive hidden units [c, c+32) of row `row` into the operand tile
 __device__ __forceinline__ void store_row32(uint8_t* tile, int row, int c, const float (&v)[32]) {
@@ -121,10 +96,18 @@ __device__ __forceinline__ void store_row32(uint8_t* tile, int row, int c, const
   }
 }
 
+// Warp-specialised, persistent over 128-point tiles:
+//   warp 0   : streams the 24 weight K-blocks of every tile through a 4-stage ring (bulk copies)
+//   warp 1   : allocates TMEM and issues the six 128x256x256 products per tile (tcgen05.mma)
+//   warps 2-9: epilogues, one thread per (point, half of the 256 hidden units); a warp may only
+//              touch its TMEM lane quadrant (warp id % 4), so each quadrant has two warps
+// Synchronisation: full/empty (ring), acc_full (products -> epilogue), op_ready (epilogue ->
+// products: operand tile rewritten and accumulator drained). Every wait is bounded.
 __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = smem_raw + ((1024 - (tc::smem_u32(smem_raw) & 1023)) & 1023);
   uint8_t* tileA = smem + SMEM_A;
+  uint8_t* ring = smem + SMEM_RING;
   float* sm = reinterpret_cast<float*>(smem + SMEM_SMALL);
   const float* sW1 = sm;
   const float* sb1 = sm + 3 * H;
@@ -133,30 +116,33 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
   const float* sb4 = sb3 + H;
   const float* sw5 = sb4 + H;
   float* part = reinterpret_cast<float*>(smem + SMEM_PART);  // [TILE][4]
+  volatile int* ready = reinterpret_cast<volatile int*>(smem + SMEM_READY);  // [TILE]
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + SMEM_BAR);
   uint64_t* full = bars;
   uint64_t* empty = bars + STAGES;
-  uint64_t* mma_bar = bars + 2 * STAGES;
-  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 1);
-  __shared__ int abort_flag;
+  uint64_t* acc_full = bars + 2 * STAGES;
+  uint64_t* op_ready = acc_full + 1;
+  uint64_t* drain = op_ready + 1;
+  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(drain + 1);
+  __shared__ int abort_s;
+  volatile int* abort_flag = &abort_s;
 
   const int t = threadIdx.x;
-  const int row = t & (TILE - 1);
-  const int half = t >> 7;
-  const int c0 = half * 128;
-  const int warp = t >> 5;
-
+  const int warp = t >> 5, lane = t & 31;
   for (int i = t; i < SMALL_FLOATS; i += NTHREADS) sm[i] = a.small[i];
+  for (int i = t; i < TILE; i += NTHREADS) ready[i] = 0;
   if (t == 0) {
-    abort_flag = 0;
+    abort_s = 0;
     for (int s = 0; s < STAGES; ++s) {
       tc::mbar_init(&full[s], 1);
       tc::mbar_init(&empty[s], 1);
     }
-    tc::mbar_init(mma_bar, 1);
+    tc::mbar_init(acc_full, 1);
+    tc::mbar_init(op_ready, EPI_WARPS);
+    tc::mbar_init(drain, 1);
     tc::fence_barrier_init();
   }
-  if (warp == 0) {
+  if (warp == 1) {
     tc::tmem_alloc(tmem_holder, TMEM_COLS);
     tc::tmem_relinquish();
   }
@@ -164,140 +150,214 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
   __syncthreads();
   tc::tc_fence_after();
   const uint32_t tmem = *tmem_holder;
-  const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;  // this warp's TMEM lanes
-
   const int64_t ntiles = (a.n + TILE - 1) / TILE;
   const int64_t my_tiles = ntiles > blockIdx.x ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
-  Ring ring{full, empty, smem + SMEM_RING, a.wimg, my_tiles * KBLOCKS_PER_TILE};
-  const uint32_t a_base = tc::smem_u32(tileA);
-  if (t == 0) {
-    if (!produce(ring, 0) || !produce(ring, 1)) abort_flag = 1;
-  }
-  __syncthreads();
-  int64_t gemm_count = 0;   // products waited for
-  int64_t gemm_issued = 0;  // products issued (thread 0)
 
-  for (int64_t it = 0; it < my_tiles && !abort_flag; ++it) {
-    const int64_t tile = blockIdx.x + it * gridDim.x;
-    const int64_t gi = tile * TILE + row;
-    const bool valid = gi < a.n;
-    float u[3] = {0.f, 0.f, 0.f};
-    if (valid) {
-#pragma unroll
-      for (int j = 0; j < 3; ++j) u[j] = (float)(a.x[j * a.n + gi] * a.inv_length);
-    }
-    // layer 1 on CUDA cores: h1 = silu(W1 u + b1) -> operand tile
-    for (int c = c0; c < c0 + 128; c += 32) {
-      float v[32];
-#pragma unroll
-      for (int q = 0; q < 32; ++q) {
-        const int cc = c + q;
-        const float z = fmaf(sW1[3 * cc], u[0], fmaf(sW1[3 * cc + 1], u[1], fmaf(sW1[3 * cc + 2], u[2], sb1[cc])));
-        v[q] = z * sig(z);
+  if (warp == 0) {
+    // ------------------------------------------------------------ weight producer
+    if (lane == 0) {
+      const int64_t total = my_tiles * KBLOCKS_PER_TILE;
+      int64_t j = 0;
+      for (; j < total; ++j) {
+        const int s = (int)(j % STAGES);
+        const int64_t use = j / STAGES;
+        if (use > 0 && !wait_bar(&empty[s], (uint32_t)((use - 1) & 1), abort_flag)) {
+          if (!*abort_flag) set_abort(abort_flag, a.err, 3);
+          break;
+        }
+        tc::mbar_expect_tx(&full[s], KBLOCK_BYTES);
+        tc::bulk_g2s(ring + (size_t)s * KBLOCK_BYTES, a.wimg + (size_t)(j % KBLOCKS_PER_TILE) * KBLOCK_BYTES,
+                     KBLOCK_BYTES, &full[s]);
       }
-      store_row32(tileA, row, c, v);
+      // every copy issued must have landed before the CTA can exit (bounded)
+      for (int64_t q = (j > STAGES ? j - STAGES : 0); q < j; ++q)
+        tc::mbar_wait(&full[q % STAGES], (uint32_t)((q / STAGES) & 1), WAIT_LIMIT);
     }
-    float gpart[3] = {0.f, 0.f, 0.f};
-    float ppart = 0.f;
-    for (int g = 0; g < GEMMS; ++g) {
-      tc::fence_proxy_async_smem();
-      tc::tc_fence_before();
-      __syncthreads();
-      if (abort_flag) break;
-      if (t == 0) {
-        tc::tc_fence_after();
-        if (!issue_gemm(ring, (it * GEMMS + g) * KBLOCKS_PER_GEMM, a_base, tmem, mma_bar)) {
-          abort_flag = 1;
-          if (a.err) atomicExch(a.err, 1);
-        } else {
-          ++gemm_issued;
+  } else if (warp == 1) {
+    // ------------------------------------------------------------ tensor-core products
+    if (lane == 0) {
+      constexpr uint32_t idesc = tc::idesc_bf16(TILE, 256);
+      const uint32_t a_base = tc::smem_u32(tileA);
+      int64_t j = 0, q = 0;
+      bool ok = true;
+      for (int64_t it = 0; it < my_tiles && ok; ++it) {
+        for (int g = 0; g < GEMMS && ok; ++g, ++q) {
+          if (!wait_bar(op_ready, (uint32_t)(q & 1), abort_flag)) {
+            ok = false;
+            break;
+          }
+          tc::tc_fence_after();
+          for (int kb = 0; kb < KBLOCKS_PER_GEMM; ++kb, ++j) {
+            const int s = (int)(j % STAGES);
+            if (!wait_bar(&full[s], (uint32_t)((j / STAGES) & 1), abort_flag)) {
+              ok = false;
+              break;
+            }
+            tc::tc_fence_after();
+            const uint32_t b_base = tc::smem_u32(ring + (size_t)s * KBLOCK_BYTES);
+#pragma unroll
+            for (int ks = 0; ks < 4; ++ks) {
+              const uint64_t ad = tc::desc_sw128(a_base + kb * (TILE * 128) + ks * 32);
+              const uint64_t bd = tc::desc_sw128(b_base + ks * 32);
+              tc::mma_bf16(tmem, ad, bd, idesc, (kb | ks) != 0);
+            }
+            tc::mma_commit(&empty[s]);  // stage free once these products complete
+          }
+          if (ok) tc::mma_commit(acc_full);
         }
       }
-      if (!tc::mbar_wait(mma_bar, (uint32_t)(gemm_count & 1), WAIT_LIMIT)) {
-        abort_flag = 1;
-        if (a.err) atomicExch(a.err, 2);
+      if (!ok && !*abort_flag) set_abort(abort_flag, a.err, 4);
+      // no product may still be writing TMEM when it is released
+      tc::mma_commit(drain);
+      tc::mbar_wait(drain, 0, WAIT_LIMIT);
+    }
+  } else {
+    // ------------------------------------------------------------ epilogues
+    const int e = warp - 2;
+    const int quad = warp & 3;
+    const int row = quad * 32 + lane;
+    const int hh = e >= 4 ? 1 : 0;
+    const int c0 = hh * 128;
+    const uint32_t lane_base = (uint32_t)(quad * 32) << 16;
+    int64_t q = 0;
+    for (int64_t it = 0; it < my_tiles; ++it) {
+      if (*abort_flag) break;
+      const int64_t tile = blockIdx.x + it * gridDim.x;
+      const int64_t gi = tile * TILE + row;
+      const bool valid = gi < a.n;
+      float u[3] = {0.f, 0.f, 0.f};
+      if (valid) {
+#pragma unroll
+        for (int j = 0; j < 3; ++j) u[j] = (float)(a.x[j * a.n + gi] * a.inv_length);
       }
-      ++gemm_count;
-      __syncthreads();
-      if (abort_flag) break;
-      tc::tc_fence_after();
-      // epilogue over this thread's 128 columns, 32 at a time
+      // layer 1 on CUDA cores: h1 = silu(W1 u + b1) -> operand tile
       for (int c = c0; c < c0 + 128; c += 32) {
-        uint32_t acc[32];
-        tc::tmem_ld32(tmem + lane_base + (uint32_t)c, acc);
-        uint32_t sp[16];
-        if (g == 3 || g == 4) tc::tmem_ld16(tmem + lane_base + (uint32_t)((g == 3 ? COL_S3 : COL_S2) + c / 2), sp);
-        tc::tmem_wait_ld();
         float v[32];
-        if (g <= 1) {  // z2 / z3: h = silu(z) -> tile, silu'(z) -> TMEM
-          const float* bb = g == 0 ? sb2 : sb3;
-          uint32_t spk[16];
 #pragma unroll
-          for (int q = 0; q < 32; q += 2) {
-            const float z0 = __uint_as_float(acc[q]) + bb[c + q];
-            const float z1 = __uint_as_float(acc[q + 1]) + bb[c + q + 1];
-            const float s0 = sig(z0), s1 = sig(z1);
-            v[q] = z0 * s0;
-            v[q + 1] = z1 * s1;
-            spk[q / 2] = tc::pack_bf16x2(s0 * (1.f + z0 * (1.f - s0)), s1 * (1.f + z1 * (1.f - s1)));
+        for (int k = 0; k < 32; ++k) {
+          const int cc = c + k;
+          const float z = fmaf(sW1[3 * cc], u[0], fmaf(sW1[3 * cc + 1], u[1], fmaf(sW1[3 * cc + 2], u[2], sb1[cc])));
+          v[k] = z * sig(z);
+        }
+        store_row32(tileA, row, c, v);
+      }
+      tc::fence_proxy_async_smem();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(op_ready);
+      float gpart[3] = {0.f, 0.f, 0.f};
+      float ppart = 0.f;
+      bool ok = true;
+      for (int g = 0; g < GEMMS; ++g, ++q) {
+        if (!wait_bar(acc_full, (uint32_t)(q & 1), abort_flag)) {
+          if (!*abort_flag) set_abort(abort_flag, a.err, 2);
+          ok = false;
+          break;
+        }
+        tc::tc_fence_after();
+        // two 32-column chunks per TMEM round trip
+        for (int c = c0; c < c0 + 128; c += 64) {
+          uint32_t acc0[32], acc1[32], sp0[16], sp1[16];
+          tc::tmem_ld32(tmem + lane_base + (uint32_t)c, acc0);
+          tc::tmem_ld32(tmem + lane_base + (uint32_t)(c + 32), acc1);
+          if (g == 3 || g == 4) {
+            const uint32_t cs = (g == 3 ? COL_S3 : COL_S2) + c / 2;
+            tc::tmem_ld16(tmem + lane_base + cs, sp0);
+            tc::tmem_ld16(tmem + lane_base + cs + 16, sp1);
           }
-          tc::tmem_st16(tmem + lane_base + (uint32_t)((g == 0 ? COL_S2 : COL_S3) + c / 2), spk);
-          store_row32(tileA, row, c, v);
-        } else if (g == 2) {  // z4: d4 = silu'(z4) w5 -> tile; out = w5 . silu(z4)
+          tc::tmem_wait_ld();
 #pragma unroll
-          for (int q = 0; q < 32; ++q) {
-            const float z = __uint_as_float(acc[q]) + sb4[c + q];
-            const float s = sig(z);
-            ppart = fmaf(z * s, sw5[c + q], ppart);
-            v[q] = s * (1.f + z * (1.f - s)) * sw5[c + q];
-          }
-          store_row32(tileA, row, c, v);
-        } else if (g <= 4) {  // u3 / u2: d = silu'(z) u -> tile
+          for (int half = 0; half < 2; ++half) {
+            const uint32_t(&acc)[32] = half ? acc1 : acc0;
+            const uint32_t(&sp)[16] = half ? sp1 : sp0;
+            const int cc0 = c + 32 * half;
+            float v[32];
+            if (g <= 1) {  // z2 / z3: h = silu(z) -> tile, silu'(z) -> TMEM
+              const float* bb = g == 0 ? sb2 : sb3;
+              uint32_t spk[16];
 #pragma unroll
-          for (int q = 0; q < 32; q += 2) {
-            v[q] = tc::bf16_lo(sp[q / 2]) * __uint_as_float(acc[q]);
-            v[q + 1] = tc::bf16_hi(sp[q / 2]) * __uint_as_float(acc[q + 1]);
-          }
-          store_row32(tileA, row, c, v);
-        } else {  // u1: grad_u out = sum_c silu'(z1_c) u1_c W1[c]
+              for (int k = 0; k < 32; k += 2) {
+                const float z0 = __uint_as_float(acc[k]) + bb[cc0 + k];
+                const float z1 = __uint_as_float(acc[k + 1]) + bb[cc0 + k + 1];
+                const float s0 = sig(z0), s1 = sig(z1);
+                v[k] = z0 * s0;
+                v[k + 1] = z1 * s1;
+                spk[k / 2] = tc::pack_bf16x2(s0 * fmaf(z0, 1.f - s0, 1.f), s1 * fmaf(z1, 1.f - s1, 1.f));
+              }
+              tc::tmem_st16(tmem + lane_base + (uint32_t)((g == 0 ? COL_S2 : COL_S3) + cc0 / 2), spk);
+              store_row32(tileA, row, cc0, v);
+            } else if (g == 2) {  // z4: d4 = silu'(z4) w5 -> tile; out = w5 . silu(z4)
 #pragma unroll
-          for (int q = 0; q < 32; ++q) {
-            const int cc = c + q;
-            const float z = fmaf(sW1[3 * cc], u[0], fmaf(sW1[3 * cc + 1], u[1], fmaf(sW1[3 * cc + 2], u[2], sb1[cc])));
-            const float s = sig(z);
-            const float d1 = s * (1.f + z * (1.f - s)) * __uint_as_float(acc[q]);
-            gpart[0] = fmaf(d1, sW1[3 * cc], gpart[0]);
-            gpart[1] = fmaf(d1, sW1[3 * cc + 1], gpart[1]);
-            gpart[2] = fmaf(d1, sW1[3 * cc + 2], gpart[2]);
+              for (int k = 0; k < 32; ++k) {
+                const float z = __uint_as_float(acc[k]) + sb4[cc0 + k];
+                const float sg = sig(z);
+                ppart = fmaf(z * sg, sw5[cc0 + k], ppart);
+                v[k] = sg * fmaf(z, 1.f - sg, 1.f) * sw5[cc0 + k];
+              }
+              store_row32(tileA, row, cc0, v);
+            } else if (g <= 4) {  // u3 / u2: d = silu'(z) u -> tile
+#pragma unroll
+              for (int k = 0; k < 32; k += 2) {
+                v[k] = tc::bf16_lo(sp[k / 2]) * __uint_as_float(acc[k]);
+                v[k + 1] = tc::bf16_hi(sp[k / 2]) * __uint_as_float(acc[k + 1]);
+              }
+              store_row32(tileA, row, cc0, v);
+            } else {  // u1: grad_u out = sum_c silu'(z1_c) u1_c W1[c]
+#pragma unroll
+              for (int k = 0; k < 32; ++k) {
+                const int cc = cc0 + k;
+                const float z =
+                    fmaf(sW1[3 * cc], u[0], fmaf(sW1[3 * cc + 1], u[1], fmaf(sW1[3 * cc + 2], u[2], sb1[cc])));
+                const float sg = sig(z);
+                const float d1 = sg * fmaf(z, 1.f - sg, 1.f) * __uint_as_float(acc[k]);
+                gpart[0] = fmaf(d1, sW1[3 * cc], gpart[0]);
+                gpart[1] = fmaf(d1, sW1[3 * cc + 1], gpart[1]);
+                gpart[2] = fmaf(d1, sW1[3 * cc + 2], gpart[2]);
+              }
+            }
           }
         }
+        if (g <= 1) tc::tmem_wait_st();
+        if (g < GEMMS - 1) {
+          tc::fence_proxy_async_smem();
+          tc::tc_fence_before();
+          __syncwarp();
+          if (lane == 0) tc::mbar_arrive(op_ready);
+        }
       }
-      if (g <= 1) tc::tmem_wait_st();
-    }
-    if (abort_flag) break;
-    // combine the two halves of each row and write the outputs
-    if (half == 1) {
-      part[row * 4 + 0] = gpart[0];
-      part[row * 4 + 1] = gpart[1];
-      part[row * 4 + 2] = gpart[2];
-      part[row * 4 + 3] = ppart;
-    }
-    __syncthreads();
-    if (half == 0 && valid) {
+      if (!ok) break;
+      // combine the two halves of each row (bounded hand-off through shared memory)
+      if (hh == 1) {
+        part[row * 4 + 0] = gpart[0];
+        part[row * 4 + 1] = gpart[1];
+        part[row * 4 + 2] = gpart[2];
+        part[row * 4 + 3] = ppart;
+        __threadfence_block();
+        ready[row] = (int)(it + 1);
+      } else {
+        uint32_t spins = 0;
+        while (ready[row] != (int)(it + 1) && spins < WAIT_LIMIT && !*abort_flag) ++spins;
+        if (ready[row] != (int)(it + 1)) {
+          if (!*abort_flag) set_abort(abort_flag, a.err, 5);
+          break;
+        }
+        __threadfence_block();
+        if (valid) {
 #pragma unroll
-      for (int j = 0; j < 3; ++j) {
-        const double gj = a.gscale * (double)(gpart[j] + part[row * 4 + j]);
-        if (a.grad) a.grad[j * a.n + gi] = a.accumulate ? a.grad[j * a.n + gi] + gj : gj;
+          for (int j = 0; j < 3; ++j) {
+            const double gj = a.gscale * (double)(gpart[j] + part[row * 4 + j]);
+            if (a.grad) a.grad[j * a.n + gi] = a.accumulate ? a.grad[j * a.n + gi] + gj : gj;
+          }
+          if (a.phi) a.phi[gi] = a.pscale * (double)(ppart + part[row * 4 + 3] + sw5[H]);
+        }
       }
-      if (a.phi) a.phi[gi] = a.pscale * (double)(ppart + part[row * 4 + 3] + sw5[H]);
     }
   }
-  // release TMEM, making sure no product is still running on it
-  if (abort_flag && t == 0 && gemm_issued > gemm_count)
-    tc::mbar_wait(mma_bar, (uint32_t)((gemm_issued - 1) & 1), WAIT_LIMIT);
   tc::tc_fence_before();
   __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tmem, TMEM_COLS);
+  if (warp == 1) {
+    tc::tc_fence_after();
+    tc::tmem_dealloc(tmem, TMEM_COLS);
+  }
 }
 
 }  // namespace mlp

@@ -22,6 +22,8 @@ namespace mlp {
 // C[M,N] = alpha * op(A)[M,K] op(B)[K,N] + beta * C + bias[n], row-major storage.
 // op(A)(m,k) = TA ? A[k*lda+m] : A[m*lda+k]; op(B)(k,n) = TB ? B[n*ldb+k] : B[k*ldb+n].
 // qa / qb round the loaded operand to bfloat16.
+// With gridDim.z > 1 the K range is split across blockIdx.z and every block adds
+// alpha * (its partial product) into C with atomics (C prepared by the caller).
 template <bool TA, bool TB>
 __global__ void __launch_bounds__(256) k_gemm(int M, int N, int K, const float* __restrict__ A, int lda,
                                               const float* __restrict__ B, int ldb, float* __restrict__ C, int ldc,
@@ -31,20 +33,24 @@ __global__ void __launch_bounds__(256) k_gemm(int M, int N, int K, const float* 
   __shared__ float Bs[16][64 + 1];
   const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
   const int m0 = blockIdx.y * 64, n0 = blockIdx.x * 64;
+  const bool split = gridDim.z > 1;
+  const int kchunk = split ? ((K + gridDim.z - 1) / gridDim.z + 15) / 16 * 16 : K;
+  const int kbeg = split ? (int)blockIdx.z * kchunk : 0;
+  const int kend = split ? min(K, kbeg + kchunk) : K;
   float acc[4][4] = {};
-  for (int k0 = 0; k0 < K; k0 += 16) {
+  for (int k0 = kbeg; k0 < kend; k0 += 16) {
     for (int i = threadIdx.x; i < 1024; i += 256) {
       int mm, kk;
       if (TA) { kk = i / 64; mm = i % 64; } else { mm = i / 16; kk = i % 16; }
       const int m = m0 + mm, k = k0 + kk;
       float v = 0.0f;
-      if (m < M && k < K) v = TA ? A[(int64_t)k * lda + m] : A[(int64_t)m * lda + k];
+      if (m < M && k < kend) v = TA ? A[(int64_t)k * lda + m] : A[(int64_t)m * lda + k];
       As[kk][mm] = qa ? bf16r(v) : v;
       int nn, kb;
       if (TB) { nn = i / 16; kb = i % 16; } else { kb = i / 64; nn = i % 64; }
       const int n = n0 + nn, kq = k0 + kb;
       float w = 0.0f;
-      if (n < N && kq < K) w = TB ? B[(int64_t)n * ldb + kq] : B[(int64_t)kq * ldb + n];
+      if (n < N && kq < kend) w = TB ? B[(int64_t)n * ldb + kq] : B[(int64_t)kq * ldb + n];
       Bs[kb][nn] = qb ? bf16r(w) : w;
     }
     __syncthreads();
@@ -70,6 +76,10 @@ __global__ void __launch_bounds__(256) k_gemm(int M, int N, int K, const float* 
     for (int c = 0; c < 4; ++c) {
       const int n = n0 + tx * 4 + c;
       if (n >= N) continue;
+      if (split) {
+        atomicAdd(&C[(int64_t)m * ldc + n], alpha * acc[r][c]);
+        continue;
+      }
       float v = alpha * acc[r][c];
       if (beta != 0.0f) v += beta * C[(int64_t)m * ldc + n];
       if (bias) v += bias[n];
@@ -151,18 +161,20 @@ __global__ void k_colsum(const float* X, const float* Y, const float* v, int64_t
 }
 
 // residuals, their loss weights and the loss value
-__global__ void k_loss(const float* out, const float* G, const float* phi_t, const float* g_t, int64_t B,
-                       float alpha, float beta, float* Pb, float* Eb, float* loss) {
+// (optional per-point weights wt[b] multiply both terms of point b)
+__global__ void k_loss(const float* out, const float* G, const float* phi_t, const float* g_t, const float* wt,
+                       int64_t B, float alpha, float beta, float* Pb, float* Eb, float* loss) {
   float s = 0.0f;
   GRID_STRIDE(b, B) {
+    const float w = wt ? wt[b] : 1.0f;
     const float r = out[b] - phi_t[b];
-    Pb[b] = 2.0f * alpha * r / (float)B;
-    s += alpha * r * r;
+    Pb[b] = 2.0f * alpha * w * r / (float)B;
+    s += alpha * w * r * r;
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
       const float e = G[b * 3 + j] - g_t[b * 3 + j];
-      Eb[b * 3 + j] = 2.0f * beta * e / (float)B;
-      s += beta * e * e;
+      Eb[b * 3 + j] = 2.0f * beta * w * e / (float)B;
+      s += beta * w * e * e;
     }
   }
   __shared__ float red[256];
@@ -224,6 +236,21 @@ template <bool TA, bool TB>
 static void gemm(cudaStream_t s, int M, int N, int K, const float* A, int lda, const float* B, int ldb, float* C,
                  int ldc, float beta = 0.0f, const float* bias = nullptr, int qa = 0, int qb = 0) {
   dim3 grid((N + 63) / 64, (M + 63) / 64);
+  // few output tiles and a long K (the weight gradients, K = batch): split K over
+  // enough blocks to fill the GPU and accumulate with atomics
+  const int tiles = (int)(grid.x * grid.y);
+  if (!bias && (beta == 0.0f || beta == 1.0f) && tiles < 2 * device_sm_count() && K >= 1024) {
+    int splits = 4 * device_sm_count() / tiles;
+    if (splits > K / 256) splits = K / 256;
+    if (splits > 1) {
+      if (beta == 0.0f && ldc == N) cudaMemsetAsync(C, 0, sizeof(float) * (size_t)M * N, s);
+      if (beta == 0.0f && ldc != N) {
+        k_gemm<TA, TB><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc, 1.0f, beta, bias, qa, qb);
+        return;
+      }
+      grid.z = splits;
+    }
+  }
   k_gemm<TA, TB><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc, 1.0f, beta, bias, qa, qb);
 }
 
@@ -256,13 +283,14 @@ static void forward_backward(cudaStream_t s, const float* P, const float* x, int
   gemm<false, false>(s, Bi, 3, H, w.D[1], H, P + OFF_W1, 3, w.G, 3);
 }
 
-static void loss_grads(cudaStream_t s, const float* P, const float* x, const float* phi_t, const float* g_t, int64_t B,
-                       float alpha, float beta, float* grad, float* loss, const Ws& w, int q) {
+static void loss_grads(cudaStream_t s, const float* P, const float* x, const float* phi_t, const float* g_t,
+                       const float* wt, int64_t B, float alpha, float beta, float* grad, float* loss, const Ws& w,
+                       int q) {
   const int64_t n = B * H;
   const int Bi = (int)B;
   forward_backward(s, P, x, B, w, q);
   cudaMemsetAsync(loss, 0, sizeof(float), s);
-  k_loss<<<ew_grid(B), 256, 0, s>>>(w.out, w.G, phi_t, g_t, B, alpha, beta, w.Pb, w.Eb, loss);
+  k_loss<<<ew_grid(B), 256, 0, s>>>(w.out, w.G, phi_t, g_t, wt, B, alpha, beta, w.Pb, w.Eb, loss);
   // ---- through the input-gradient graph, layer 1 up to 4
   gemm<true, false>(s, H, 3, Bi, w.D[1], H, w.Eb, 3, grad + OFF_W1, 3);                       // gW1 = D1^T Eb
   gemm<false, true>(s, Bi, H, 3, w.Eb, 3, P + OFF_W1, 3, w.Db, H);                           // Db1 = Eb W1^T
@@ -328,25 +356,27 @@ gal_status gal_mlp_forward_f32(const float* params, const float* x, int64_t batc
   return e == cudaSuccess ? GAL_OK : cuda_fail(e, "MLP forward");
 }
 
-gal_status gal_mlp_loss_grads(const float* params, const float* x, const float* phi_t, const float* g_t, int64_t batch,
-                              float alpha, float beta, int32_t quantize, float* grad, float* loss, void* workspace,
-                              size_t workspace_bytes, gal_stream_t stream) {
+gal_status gal_mlp_loss_grads(const float* params, const float* x, const float* phi_t, const float* g_t,
+                              const float* weights, int64_t batch, float alpha, float beta, int32_t quantize,
+                              float* grad, float* loss, void* workspace, size_t workspace_bytes, gal_stream_t stream) {
   if (!params || !x || !phi_t || !g_t || !grad || !loss || batch < 1)
     return fail(GAL_ERR_INVALID_ARGUMENT, "bad MLP arguments");
   if (batch > (int64_t)1 << 24) return fail(GAL_ERR_TOO_LARGE, "batch above 2^24 points");
   if (!workspace || workspace_bytes < ws_bytes(batch)) return fail(GAL_ERR_WORKSPACE, "workspace too small");
   cudaStream_t s = (cudaStream_t)stream;
-  loss_grads(s, params, x, phi_t, g_t, batch, alpha, beta, grad, loss, carve(workspace, batch), quantize ? 1 : 0);
+  loss_grads(s, params, x, phi_t, g_t, weights, batch, alpha, beta, grad, loss, carve(workspace, batch),
+             quantize ? 1 : 0);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? GAL_OK : cuda_fail(e, "MLP loss/gradient");
 }
 
 gal_status gal_mlp_train_step(float* params, float* grad, float* adam_m, float* adam_v, const float* x,
-                              const float* phi_t, const float* g_t, int64_t batch, float alpha, float beta, float lr,
-                              float beta1, float beta2, float eps, int32_t step, int32_t quantize, float* loss,
-                              void* workspace, size_t workspace_bytes, gal_stream_t stream) {
-  gal_status st = gal_mlp_loss_grads(params, x, phi_t, g_t, batch, alpha, beta, quantize, grad, loss, workspace,
-                                     workspace_bytes, stream);
+                              const float* phi_t, const float* g_t, const float* weights, int64_t batch, float alpha,
+                              float beta, float lr, float beta1, float beta2, float eps, int32_t step,
+                              int32_t quantize, float* loss, void* workspace, size_t workspace_bytes,
+                              gal_stream_t stream) {
+  gal_status st = gal_mlp_loss_grads(params, x, phi_t, g_t, weights, batch, alpha, beta, quantize, grad, loss,
+                                     workspace, workspace_bytes, stream);
   if (st != GAL_OK) return st;
   if (!adam_m || !adam_v || step < 1) return fail(GAL_ERR_INVALID_ARGUMENT, "Adam state and step >= 1 required");
   const float c1 = 1.0f - powf(beta1, (float)step), c2 = 1.0f - powf(beta2, (float)step);

@@ -149,13 +149,14 @@ class MLPSurrogate:
         return phi, g
 
 
-def loss_grads(params, u, phi_t, g_t, alpha: float, beta: float, *, quantize: bool = False):
+def loss_grads(params, u, phi_t, g_t, alpha: float, beta: float, *, quantize: bool = False, weights=None):
     """Loss and its parameter gradient on the GPU (FP32), for checking."""
     torch = _torch()
     P = _as_cuda(params, torch.float32).contiguous()
     U = _as_cuda(u, torch.float32).reshape(-1, 3).contiguous()
     pt = _as_cuda(phi_t, torch.float32).reshape(-1).contiguous()
     gt = _as_cuda(g_t, torch.float32).reshape(-1, 3).contiguous()
+    wt = _as_cuda(weights, torch.float32).reshape(-1).contiguous() if weights is not None else None
     B = U.shape[0]
     grad = torch.empty_like(P)
     loss = torch.zeros(1, dtype=torch.float32, device="cuda")
@@ -164,19 +165,25 @@ def loss_grads(params, u, phi_t, g_t, alpha: float, beta: float, *, quantize: bo
     _lib.check(L.gal_mlp_workspace_size(B, C.byref(nb)), "gal_mlp_workspace_size")
     ws = torch.empty(nb.value, dtype=torch.uint8, device="cuda")
     st = torch.cuda.current_stream().cuda_stream
-    _lib.check(L.gal_mlp_loss_grads(P.data_ptr(), U.data_ptr(), pt.data_ptr(), gt.data_ptr(), B, alpha, beta,
-                                    int(quantize), grad.data_ptr(), loss.data_ptr(), ws.data_ptr(), ws.numel(), st),
+    _lib.check(L.gal_mlp_loss_grads(P.data_ptr(), U.data_ptr(), pt.data_ptr(), gt.data_ptr(),
+                                    wt.data_ptr() if wt is not None else None, B, alpha, beta, int(quantize),
+                                    grad.data_ptr(), loss.data_ptr(), ws.data_ptr(), ws.numel(), st),
                "gal_mlp_loss_grads")
     return float(loss), grad.cpu().numpy()
 
 
 def train(x, phi, grad, *, length_scale: float, epochs: int = 30, batch: int = 8192, lr: float = 2e-3,
           lr_final: float = 2e-5, alpha: float = 0.1, seed: int = 0, quantize: bool = True,
-          log_every: int = 0) -> tuple[MLPSurrogate, TrainReport]:
+          far_field_weight: bool = False, log_every: int = 0) -> tuple[MLPSurrogate, TrainReport]:
     """Fit the MLP to FP64 samples (x (n,3), Phi (n,), grad Phi (n,3), physical
     units) with the GPU training kernels. phi_scale is set so the potential
     targets have unit variance; the gradient term is weighted by the inverse
-    variance of its targets. Cosine learning-rate decay from lr to lr_final."""
+    variance of its targets. Cosine learning-rate decay from lr to lr_final.
+
+    far_field_weight: weight every point by 1 / (|g|^2 + g_med^2) (g_med the
+    median gradient norm, the weights normalised to mean 1), so the squared
+    error becomes a relative one: without it the few points next to a compact
+    component, whose gradients are ~1000x the typical one, dominate the loss."""
     import time
 
     torch = _torch()
@@ -189,6 +196,12 @@ def train(x, phi, grad, *, length_scale: float, epochs: int = 30, batch: int = 8
     pt = (ph / phi_scale).to(torch.float32)
     gt = (gr * (length_scale / phi_scale)).to(torch.float32)
     beta = 1.0 / float((gt ** 2).sum(1).mean())
+    wts = None
+    if far_field_weight:
+        g2 = (gt.double() ** 2).sum(1)
+        w = 1.0 / (g2 + g2.median())
+        wts = (w / w.mean()).to(torch.float32)
+        beta = 1.0 / float((wts.double() * g2).mean())
     P = torch.as_tensor(init_params(seed), device="cuda")
     G = torch.zeros_like(P)
     M = torch.zeros_like(P)
@@ -211,11 +224,13 @@ def train(x, phi, grad, *, length_scale: float, epochs: int = 30, batch: int = 8
         for b in range(steps_per_epoch):
             idx = perm[b * batch:(b + 1) * batch]
             ub, pb, gb = u[idx].contiguous(), pt[idx].contiguous(), gt[idx].contiguous()
+            wb = wts[idx].contiguous() if wts is not None else None
             step += 1
             lr_t = lr_final + 0.5 * (lr - lr_final) * (1 + math.cos(math.pi * step / total))
             _lib.check(L.gal_mlp_train_step(P.data_ptr(), G.data_ptr(), M.data_ptr(), V.data_ptr(), ub.data_ptr(),
-                                            pb.data_ptr(), gb.data_ptr(), batch, alpha, beta, lr_t, 0.9, 0.999, 1e-8,
-                                            step, int(quantize), loss.data_ptr(), ws.data_ptr(), ws.numel(), st),
+                                            pb.data_ptr(), gb.data_ptr(), wb.data_ptr() if wb is not None else None,
+                                            batch, alpha, beta, lr_t, 0.9, 0.999, 1e-8, step, int(quantize),
+                                            loss.data_ptr(), ws.data_ptr(), ws.numel(), st),
                        "gal_mlp_train_step")
             ep_loss += loss
         rep.loss.append(float(ep_loss) / steps_per_epoch)

@@ -280,16 +280,19 @@ GAL_API gal_status gal_mlp_workspace_size(int64_t batch, size_t* bytes);
  * and the activations entering the 256x256 products to bfloat16, as inference does. */
 GAL_API gal_status gal_mlp_forward_f32(const float* params, const float* u, int64_t batch, float* phi, float* grad,
                                        int32_t quantize, void* workspace, size_t workspace_bytes, gal_stream_t stream);
-/* Loss L = alpha/B sum (out - phi_t)^2 + beta/B sum |grad_u out - g_t|^2 (network
- * units) and its exact gradient with respect to every parameter (grad[num_params]). */
+/* Loss L = 1/B sum_b w_b [alpha (out_b - phi_t,b)^2 + beta |grad_u out_b - g_t,b|^2]
+ * (network units; weights[batch] = w_b, NULL for w_b = 1) and its exact gradient
+ * with respect to every parameter (grad[num_params]). */
 GAL_API gal_status gal_mlp_loss_grads(const float* params, const float* u, const float* phi_t, const float* g_t,
-                                      int64_t batch, float alpha, float beta, int32_t quantize, float* grad,
-                                      float* loss, void* workspace, size_t workspace_bytes, gal_stream_t stream);
+                                      const float* weights, int64_t batch, float alpha, float beta,
+                                      int32_t quantize, float* grad, float* loss, void* workspace,
+                                      size_t workspace_bytes, gal_stream_t stream);
 /* One Adam step on that loss (step counts from 1). */
 GAL_API gal_status gal_mlp_train_step(float* params, float* grad, float* adam_m, float* adam_v, const float* u,
-                                      const float* phi_t, const float* g_t, int64_t batch, float alpha, float beta,
-                                      float lr, float beta1, float beta2, float eps, int32_t step, int32_t quantize,
-                                      float* loss, void* workspace, size_t workspace_bytes, gal_stream_t stream);
+                                      const float* phi_t, const float* g_t, const float* weights, int64_t batch,
+                                      float alpha, float beta, float lr, float beta1, float beta2, float eps,
+                                      int32_t step, int32_t quantize, float* loss, void* workspace,
+                                      size_t workspace_bytes, gal_stream_t stream);
 /* Build inference weights (bfloat16 operand images) from a host parameter vector. */
 GAL_API gal_status gal_mlp_create(const float* params_host, double length_scale, double phi_scale, gal_mlp** out);
 GAL_API gal_status gal_mlp_destroy(gal_mlp* mlp);

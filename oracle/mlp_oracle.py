@@ -81,14 +81,17 @@ def forward(p: dict, u: np.ndarray):
     return out, g, cache
 
 
-def loss_and_grads(p: dict, u, phi_t, g_t, alpha: float, beta: float):
+def loss_and_grads(p: dict, u, phi_t, g_t, alpha: float, beta: float, w=None):
+    """Loss 1/B sum_b w_b [alpha (out_b - phi_t,b)^2 + beta |g_b - g_t,b|^2] (w_b = 1
+    when w is None) and its exact gradient with respect to every parameter."""
     B = len(u)
+    w = np.ones(B) if w is None else np.asarray(w, np.float64)
     out, g, c = forward(p, u)
     rphi = out - phi_t
     rg = g - g_t
-    L = alpha * np.sum(rphi**2) / B + beta * np.sum(rg**2) / B
-    Pb = 2.0 * alpha * rphi / B          # dL/dout
-    Eb = 2.0 * beta * rg / B             # dL/dg
+    L = alpha * np.sum(w * rphi**2) / B + beta * np.sum(w[:, None] * rg**2) / B
+    Pb = 2.0 * alpha * w * rphi / B          # dL/dout
+    Eb = 2.0 * beta * w[:, None] * rg / B    # dL/dg
     gr = {k: np.zeros_like(v) for k, v in p.items()}
     # ---- through the input-gradient (backward) graph
     gr["W1"] += c["d1"].T @ Eb

@@ -60,6 +60,27 @@ def test_training_gradient_matches_numpy(env):
         assert np.linalg.norm(got - ref) <= 2e-4 * np.linalg.norm(ref) + 1e-7, k
 
 
+def test_weighted_training_gradient_matches_numpy(env):
+    """Per-point loss weights (used to weight the far field) enter the exact gradient."""
+    gx, S = env
+    p = _params(S, seed=2)
+    rng = np.random.default_rng(13)
+    B = 2048  # above the split-K threshold of the weight-gradient products
+    u = rng.normal(size=(B, 3)).astype(np.float32)
+    pt = rng.normal(size=B).astype(np.float32)
+    gt = rng.normal(size=(B, 3)).astype(np.float32)
+    w = rng.uniform(0.1, 3.0, B).astype(np.float32)
+    loss, grad = S.loss_grads(p, u, pt, gt, 0.4, 0.9, quantize=False, weights=w)
+    L_ref, g_ref = M.loss_and_grads(_as_oracle(S, p), u.astype(np.float64), pt.astype(np.float64),
+                                    gt.astype(np.float64), 0.4, 0.9, w.astype(np.float64))
+    assert abs(loss - L_ref) <= 1e-4 * abs(L_ref)
+    gd = S.unpack(grad)
+    for k in M.NAMES:
+        ref = g_ref[k].reshape(-1)
+        got = gd[k].reshape(-1).astype(np.float64)
+        assert np.linalg.norm(got - ref) <= 3e-4 * np.linalg.norm(ref) + 1e-7, k
+
+
 def test_quantised_fp32_forward_matches_numpy_bf16(env):
     gx, S = env
     p = _params(S)

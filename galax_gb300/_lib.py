@@ -108,8 +108,11 @@ SIGNATURES = {
     "gal_mlp_eval": (C.c_int, [_VP, _DP, C.c_int64, _DP, C.c_int32, C.c_double, _DP, C.c_void_p]),
     "gal_mlp_error": (C.c_int, [_VP, C.POINTER(C.c_int32)]),
     "gal_surrogate_workspace_size": (C.c_int, [C.c_int64, C.POINTER(C.c_size_t)]),
-    "gal_integrate_surrogate": (C.c_int, [_VP, _VP, C.c_double, C.c_double, C.c_double, _DP, C.c_int64, C.c_int32,
-                                          _VP, C.c_size_t, C.c_void_p]),
+    "gal_split_create": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_double, C.POINTER(C.c_void_p)]),
+    "gal_split_destroy": (C.c_int, [_VP]),
+    "gal_split_eval": (C.c_int, [_VP, _DP, C.c_int64, _DP, _DP, C.c_void_p]),
+    "gal_integrate_surrogate": (C.c_int, [_VP, _VP, _VP, C.c_double, C.c_double, C.c_double, _DP, C.c_int64,
+                                          C.c_int32, _VP, C.c_size_t, C.c_void_p]),
     "gal_tableau": (C.c_int32, [C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "gal_fp64_peak_probe": (C.c_int, [C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_void_p]),
     "gal_status_string": (C.c_char_p, [C.c_int32]),

@@ -34,9 +34,11 @@
 // cotangents on the progenitor's stage position (mu) with shuffles and write
 // one partial per warp; a fixed-order reduction over warps follows, then the
 // release-map adjoint (forward-mode dual numbers for d(d2Phi/dr2)) and the
-// progenitor adjoint (forwards track with the mu and release cotangents
-// injected, then the backwards track). Parameter gradients are written per
-// column and summed in a fixed order, so results are bitwise reproducible.
+// progenitor adjoint: Hessians at all its stage points in parallel, the serial
+// reverse recurrence on one warp (a lane per state component, no potential
+// evaluations), and the parameter terms of all stage points in parallel.
+// Parameter gradients are written per column and summed in a fixed order, so
+// results are bitwise reproducible.
 #include <cuda_runtime.h>
 
 #include <climits>
@@ -55,7 +57,10 @@ struct StreamDev {
   int32_t k_ckpt, ncomp;
   double* B;             // [n_rel + 1][6] backwards progenitor track, B[0] = w_now
   double* P;             // [n_rel + 1][6] forwards progenitor track
-  double* Q;             // [n_rel][S][3] progenitor stage positions
+  double* Q;             // [n_rel][S][3] progenitor stage positions (forwards track)
+  double* Qb;            // [n_rel][S][3] stage positions of the backwards track (gradient only)
+  double* Hst;           // [2][n_rel][S][6] host Hessians at both tracks' stage points (xx xy xz yy yz zz)
+  double* vst;           // [2][n_rel][S][3] velocity cotangents at those stage points
   double* rt_om;         // [2][n_rel] tidal radius, angular frequency
   const double* noise;   // [12][n_rel]: xi_lead, eta_lead, xi_trail, eta_trail
   double* ics;           // [6][np]
@@ -68,6 +73,7 @@ struct StreamDev {
   double* mu;            // [n_rel][S * 3]
   double* nu;            // [n_rel][6] dL/dP[r] through the release map
   double* gp_all;        // [ncomp * 3 + 1][ncol]: parameter partials per column, last row the loss
+                         // (columns: particles, releases, progenitor stage points)
   double* grad_w_now;    // [6] or NULL
 };
 
@@ -139,7 +145,29 @@ __global__ void __launch_bounds__(32) k_stream_progenitor(StreamDev a, Host host
     a.B[j] = y[j];
   }
   for (int64_t k = 0; k < a.n_rel; ++k) {
-    rk_step_plain<TB>(h, y, -a.dt);
+    if (a.Qb) {  // the same step as rk_step_plain, keeping the stage positions
+      double* Qk = a.Qb + k * TB::S * 3;
+      double F[TB::S][6];
+      field(h, y, F[0]);
+      Qk[0] = y[0];
+      Qk[1] = y[1];
+      Qk[2] = y[2];
+      static_for<1, TB::S>([&](auto i) {
+        constexpr int I = decltype(i)::value;
+        double Y[6];
+        stage_state<TB, I>(y, -a.dt, F, Y);
+        Qk[3 * I + 0] = Y[0];
+        Qk[3 * I + 1] = Y[1];
+        Qk[3 * I + 2] = Y[2];
+        field(h, Y, F[I]);
+      });
+      double y1[6];
+      rk_combine<TB>(y, -a.dt, F, y1, nullptr);
+#pragma unroll
+      for (int j = 0; j < 6; ++j) y[j] = y1[j];
+    } else {
+      rk_step_plain<TB>(h, y, -a.dt);
+    }
 #pragma unroll
     for (int j = 0; j < 6; ++j) a.B[(k + 1) * 6 + j] = y[j];
   }
@@ -595,83 +623,115 @@ __global__ void __launch_bounds__(128) k_stream_release_adj(StreamDev a, const D
   }
 }
 
-// Reverse sweep of one host-potential step of signed length hs from y with
-// extra cotangents mu (S x 3, may be NULL) on the stage positions.
-template <class TB, class Host>
-__device__ void prog_reverse_step(const Host& h, const DevComp* comps, int ncomp, const double* yk, double hs,
-                                  const double* mu, double* lam, double* gp) {
-  constexpr int S = TB::S;
-  double F[S][6], Yq[S][3];
-  field(h, yk, F[0]);
-  Yq[0][0] = yk[0];
-  Yq[0][1] = yk[1];
-  Yq[0][2] = yk[2];
-  static_for<1, S>([&](auto i) {
-    constexpr int I = decltype(i)::value;
-    double Y[6];
-    stage_state<TB, I>(yk, hs, F, Y);
-    Yq[I][0] = Y[0];
-    Yq[I][1] = Y[1];
-    Yq[I][2] = Y[2];
-    field(h, Y, F[I]);
-  });
-  static_for<0, S>([&](auto i) {
-    constexpr int I = decltype(i)::value;
-    constexpr double bi = TB::B[I];
-#pragma unroll
-    for (int j = 0; j < 6; ++j) F[I][j] = hs * bi * lam[j];
-  });
-  static_for<0, S>([&](auto rr) {
-    constexpr int I = S - 1 - decltype(rr)::value;
-    const double v[3] = {F[I][3], F[I][4], F[I][5]};
-    double Hv[3] = {0.0, 0.0, 0.0};
-    for (int c = 0; c < ncomp; ++c) {
-      double dp[3] = {0.0, 0.0, 0.0};
-      comp_vjp(comps[c], Yq[I], v, Hv, dp);
-      gp[3 * c + 0] -= dp[0];
-      gp[3 * c + 1] -= dp[1];
-      gp[3 * c + 2] -= dp[2];
-    }
-    double Yb[6] = {-Hv[0], -Hv[1], -Hv[2], F[I][0], F[I][1], F[I][2]};
-    if (mu) {
-      Yb[0] += mu[3 * I + 0];
-      Yb[1] += mu[3 * I + 1];
-      Yb[2] += mu[3 * I + 2];
-    }
-#pragma unroll
-    for (int j = 0; j < 6; ++j) lam[j] += Yb[j];
-    static_for<0, I>([&](auto l) {
-      constexpr int L = decltype(l)::value;
-      constexpr double c = TB::A[I][L];
-      if constexpr (c != 0.0) {
-#pragma unroll
-        for (int j = 0; j < 6; ++j) F[L][j] = fma(hs * c, Yb[j], F[L][j]);
-      }
-    });
-  });
-}
-
-template <class TB, class Host>
-__global__ void __launch_bounds__(32) k_stream_progenitor_adj(StreamDev a, Host host, const DevComp* comps) {
+// Progenitor adjoint, in three kernels. Its stage positions are known from the
+// forward pass, so the Hessians there are computed for all stage points at
+// once (k_stream_prog_hess); the serial reverse recurrence then needs no
+// potential evaluations, only H v and the Runge-Kutta combinations, and runs on
+// one warp with a lane per state component (k_stream_prog_sweep), recording the
+// velocity cotangent v of every stage; the parameter gradient
+// -sum d(grad Phi . v)/dtheta over all stage points is again parallel
+// (k_stream_prog_pgrad).
+__global__ void __launch_bounds__(128) k_stream_prog_hess(StreamDev a, const DevComp* comps, int S) {
   __shared__ DevComp s_comps[kAdjMaxComps];
   stage_comps(comps, a.ncomp, s_comps);
-  const Host h = bind_shared(host, s_comps);
-  if (threadIdx.x != 0) return;
+  const int64_t npts = 2 * a.n_rel * S;
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= npts) return;
+  const int64_t per = a.n_rel * S;
+  const double* Y = (p < per ? a.Q + 3 * p : a.Qb + 3 * (p - per));
+  double H[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  for (int c = 0; c < a.ncomp; ++c) comp_hessian(s_comps[c], Y[0], Y[1], Y[2], H);
+  double* o = a.Hst + 6 * p;
+  o[0] = H[0];
+  o[1] = H[1];
+  o[2] = H[2];
+  o[3] = H[4];
+  o[4] = H[5];
+  o[5] = H[8];
+}
+
+// One track of the reverse recurrence (track 0: forwards, hs = +dt, with the
+// particles' cotangents mu on the stage positions and the release-map
+// cotangents nu on the grid states; track 1: backwards, hs = -dt). Lane j < 6
+// owns component j of lambda and of every stage cotangent Fbar_i.
+template <class TB>
+__device__ __forceinline__ void prog_sweep_track(const StreamDev& a, int track, double hs, double& lam, int lane) {
   constexpr int S = TB::S;
-  double lam[6] = {0, 0, 0, 0, 0, 0};
-  double gp[kAdjMaxComps * 3];
-  for (int i = 0; i < kAdjMaxComps * 3; ++i) gp[i] = 0.0;
+  const bool mine = lane < 6;
+  const int hrow = lane < 3 ? lane : 0;
+  const int h0 = hrow == 0 ? 0 : (hrow == 1 ? 1 : 2);
+  const int h1 = hrow == 0 ? 1 : (hrow == 1 ? 3 : 4);
+  const int h2 = hrow == 0 ? 2 : (hrow == 1 ? 4 : 5);
+  const int src = (lane >= 3 && lane < 6) ? lane - 3 : lane;
   for (int64_t k = a.n_rel - 1; k >= 0; --k) {
-    prog_reverse_step<TB>(h, s_comps, a.ncomp, a.P + 6 * k, a.dt, a.mu + k * S * 3, lam, gp);
-#pragma unroll
-    for (int j = 0; j < 6; ++j) lam[j] += a.nu[6 * k + j];
+    const int64_t base = (int64_t)track * a.n_rel * S + k * S;  // stage-point index of (k, 0)
+    double Hr[S][3], Mu[S];
+    // all of this step's inputs in flight together
+    static_for<0, S>([&](auto i) {
+      constexpr int I = decltype(i)::value;
+      const double* Hp = a.Hst + 6 * (base + I);
+      Hr[I][0] = lane < 3 ? Hp[h0] : 0.0;
+      Hr[I][1] = lane < 3 ? Hp[h1] : 0.0;
+      Hr[I][2] = lane < 3 ? Hp[h2] : 0.0;
+      Mu[I] = (track == 0 && lane < 3) ? a.mu[(k * S + I) * 3 + lane] : 0.0;
+    });
+    const double nu = (track == 0 && mine) ? a.nu[6 * k + lane] : 0.0;
+    double Fb[S];
+    static_for<0, S>([&](auto i) {
+      constexpr int I = decltype(i)::value;
+      constexpr double bi = TB::B[I];
+      Fb[I] = hs * bi * lam;
+    });
+    static_for<0, S>([&](auto rr) {
+      constexpr int I = S - 1 - decltype(rr)::value;
+      const double f = Fb[I];
+      const double v0 = __shfl_sync(0xffffffffu, f, 3);
+      const double v1 = __shfl_sync(0xffffffffu, f, 4);
+      const double v2 = __shfl_sync(0xffffffffu, f, 5);
+      const double pos = __shfl_sync(0xffffffffu, f, src);
+      if (lane >= 3 && mine) a.vst[3 * (base + I) + (lane - 3)] = f;
+      double Yb;
+      if (lane < 3)
+        Yb = Mu[I] - fma(Hr[I][0], v0, fma(Hr[I][1], v1, Hr[I][2] * v2));
+      else
+        Yb = mine ? pos : 0.0;
+      lam += Yb;
+      static_for<0, I>([&](auto l) {
+        constexpr int L = decltype(l)::value;
+        constexpr double c = TB::A[I][L];
+        if constexpr (c != 0.0) Fb[L] = fma(hs * c, Yb, Fb[L]);
+      });
+    });
+    lam += nu;
   }
-  for (int64_t k = a.n_rel - 1; k >= 0; --k)
-    prog_reverse_step<TB>(h, s_comps, a.ncomp, a.B + 6 * k, -a.dt, nullptr, lam, gp);
-  if (a.grad_w_now)
-    for (int j = 0; j < 6; ++j) a.grad_w_now[j] = lam[j];
-  const int64_t col = a.np + a.n_rel;
-  for (int c = 0; c < 3 * a.ncomp; ++c) a.gp_all[(int64_t)c * a.ncol + col] = gp[c];
+}
+
+template <class TB>
+__global__ void __launch_bounds__(32) k_stream_prog_sweep(StreamDev a) {
+  const int lane = threadIdx.x;
+  double lam = 0.0;
+  prog_sweep_track<TB>(a, 0, a.dt, lam, lane);
+  prog_sweep_track<TB>(a, 1, -a.dt, lam, lane);
+  if (a.grad_w_now && lane < 6) a.grad_w_now[lane] = lam;
+}
+
+__global__ void __launch_bounds__(128) k_stream_prog_pgrad(StreamDev a, const DevComp* comps, int S) {
+  __shared__ DevComp s_comps[kAdjMaxComps];
+  stage_comps(comps, a.ncomp, s_comps);
+  const int64_t npts = 2 * a.n_rel * S;
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= npts) return;
+  const int64_t per = a.n_rel * S;
+  const double* Y = (p < per ? a.Q + 3 * p : a.Qb + 3 * (p - per));
+  const double* v = a.vst + 3 * p;
+  const int64_t col = a.np + a.n_rel + p;
+  for (int c = 0; c < a.ncomp; ++c) {
+    double Hv[3] = {0.0, 0.0, 0.0}, dp[3] = {0.0, 0.0, 0.0};
+    comp_vjp(s_comps[c], Y, v, Hv, dp);
+    a.gp_all[(int64_t)(3 * c + 0) * a.ncol + col] = -dp[0];
+    a.gp_all[(int64_t)(3 * c + 1) * a.ncol + col] = -dp[1];
+    a.gp_all[(int64_t)(3 * c + 2) * a.ncol + col] = -dp[2];
+  }
   a.gp_all[(int64_t)(3 * a.ncomp) * a.ncol + col] = 0.0;
 }
 
@@ -693,7 +753,7 @@ __global__ void k_stream_reduce_rows(const double* __restrict__ in, int64_t n, d
 static size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 struct StreamLayout {
-  size_t B, P, Q, rt_om, ics, fin, ckpt, seg, lam_rel, mu_warp, mu, nu, gp_all, red, total;
+  size_t B, P, Q, Qb, Hst, vst, rt_om, ics, fin, ckpt, seg, lam_rel, mu_warp, mu, nu, gp_all, red, total;
   int64_t np, nwarps, nseg, ncol;
   int S;
 };
@@ -705,7 +765,7 @@ static StreamLayout stream_layout(int ncomp, const gal_stream_config& c, bool gr
   L.nwarps = (L.np + 31) / 32;
   const int K = c.k_ckpt > 0 ? c.k_ckpt : 1;
   L.nseg = (c.n_release + K - 1) / K;
-  L.ncol = L.np + c.n_release + 1;
+  L.ncol = L.np + c.n_release + 2 * c.n_release * L.S;
   const size_t d = sizeof(double);
   const size_t nr = (size_t)c.n_release;
   size_t off = 0;
@@ -721,6 +781,9 @@ static StreamLayout stream_layout(int ncomp, const gal_stream_config& c, bool gr
   L.ics = take(d * 6 * L.np);
   L.fin = take(d * 6 * L.np);
   if (grad) {
+    L.Qb = take(d * 3 * L.S * nr);
+    L.Hst = take(d * 6 * 2 * L.S * nr);
+    L.vst = take(d * 3 * 2 * L.S * nr);
     L.ckpt = take(d * 6 * L.nseg * L.np);
     L.seg = take(d * 6 * (size_t)K * L.np);
     L.lam_rel = take(d * 6 * L.np);
@@ -767,6 +830,9 @@ static StreamDev stream_args(const gal_potential* pot, const gal_stream_config* 
   a.ics = at(L.ics);
   a.fin = at(L.fin);
   if (grad) {
+    a.Qb = at(L.Qb);
+    a.Hst = at(L.Hst);
+    a.vst = at(L.vst);
     a.ckpt = at(L.ckpt);
     a.seg = at(L.seg);
     a.lam_rel = at(L.lam_rel);
@@ -792,7 +858,10 @@ static cudaError_t stream_backward(const StreamDev& a, const Host& host, const D
   const int S3 = 3 * TB::S;
   k_stream_mu_reduce<<<(unsigned)((a.n_rel * S3 + 255) / 256), 256, 0, s>>>(a, S3);
   k_stream_release_adj<<<(unsigned)((a.n_rel + 127) / 128), 128, 0, s>>>(a, comps);
-  k_stream_progenitor_adj<TB, Host><<<1, 32, 0, s>>>(a, host, comps);
+  const int64_t npts = 2 * a.n_rel * TB::S;
+  k_stream_prog_hess<<<(unsigned)((npts + 127) / 128), 128, 0, s>>>(a, comps, TB::S);
+  k_stream_prog_sweep<TB><<<1, 32, 0, s>>>(a);
+  k_stream_prog_pgrad<<<(unsigned)((npts + 127) / 128), 128, 0, s>>>(a, comps, TB::S);
   return cudaGetLastError();
 }
 

@@ -14,6 +14,7 @@
 
 #include "handle.h"
 #include "integrate.cuh"
+#include "split.cuh"
 
 struct gal_mlp;
 extern "C" gal_status gal_mlp_eval(const gal_mlp* mlp, const double* x, int64_t n, double* grad, int32_t accumulate,
@@ -121,9 +122,9 @@ gal_status gal_surrogate_workspace_size(int64_t n, size_t* bytes) {
   return GAL_OK;
 }
 
-gal_status gal_integrate_surrogate(const gal_potential* pot, const gal_mlp* mlp, double dt, double t0, double t1,
-                                   double* y, int64_t n, int32_t use_graph, void* workspace, size_t workspace_bytes,
-                                   gal_stream_t stream) {
+gal_status gal_integrate_surrogate(const gal_potential* pot, const gal_mlp* mlp, const gal_split* near, double dt,
+                                   double t0, double t1, double* y, int64_t n, int32_t use_graph, void* workspace,
+                                   size_t workspace_bytes, gal_stream_t stream) {
   if (!pot || !y || n < 0 || !(dt > 0.0)) return fail(GAL_ERR_INVALID_ARGUMENT, "bad surrogate arguments");
   if (n == 0 || t0 == t1) return GAL_OK;
   size_t need = 0;
@@ -162,17 +163,27 @@ gal_status gal_integrate_surrogate(const gal_potential* pot, const gal_mlp* mlp,
   const int64_t cap = (int64_t)device_sm_count() * 8;
   const unsigned grid = (unsigned)(grid64 > cap ? cap : grid64);
   cudaError_t e;
+  // the analytic part, with the exact short-range Plummer sum when a split is given
+  const SplitDev* spd = gal_split_device(near);
+  auto with_pot = [&](auto&& fn) -> cudaError_t {
+    if (pot->is_mw) {
+      const MWPot base{pot->mw};
+      return spd ? fn(WithShort<MWPot>{base, *spd}) : fn(base);
+    }
+    const TablePot base{pot->d_comps, pot->n};
+    return spd ? fn(WithShort<TablePot>{base, *spd}) : fn(base);
+  };
   auto run_slope0 = [&]() -> cudaError_t {
-    if (pot->is_mw)
-      k_slope0<<<grid, 256, 0, s>>>(MWPot{pot->mw}, y, F, Yq, n);
-    else
-      k_slope0<<<grid, 256, 0, s>>>(TablePot{pot->d_comps, pot->n}, y, F, Yq, n);
+    cudaError_t e0 = with_pot([&](auto P) -> cudaError_t {
+      k_slope0<<<grid, 256, 0, s>>>(P, y, F, Yq, n);
+      return cudaSuccess;
+    });
+    if (e0 != cudaSuccess) return e0;
     if (mlp && gal_mlp_eval(mlp, Yq, n, F + 3 * n, 1, -1.0, nullptr, s) != GAL_OK) return cudaErrorLaunchFailure;
     return cudaGetLastError();
   };
   auto run_step = [&](double hs) -> cudaError_t {
-    return pot->is_mw ? launch_step(MWPot{pot->mw}, y, F, Yq, hs, n, mlp, s, grid)
-                      : launch_step(TablePot{pot->d_comps, pot->n}, y, F, Yq, hs, n, mlp, s, grid);
+    return with_pot([&](auto P) -> cudaError_t { return launch_step(P, y, F, Yq, hs, n, mlp, s, grid); });
   };
   if ((e = run_slope0()) != cudaSuccess) return finish(cuda_fail(e, "surrogate first slope"));
   cudaGraphExec_t exec = nullptr;

@@ -241,13 +241,66 @@ def train(x, phi, grad, *, length_scale: float, epochs: int = 30, batch: int = 8
     return MLPSurrogate(P.cpu().numpy(), length_scale, phi_scale), rep
 
 
+class ShortRange:
+    """Exact FP64 short-range part of a set of Plummer spheres (``gal_split_*``).
+
+    Every sphere is split as Phi S(d / r_cut) + Phi (1 - S), S(q) = (1 - q^2)^3
+    for q < 1 (0 beyond): ``evaluate`` returns the short-range sum, which the
+    surrogate integrator adds exactly; an MLP trained on ``total - short`` only
+    has to learn the remainder, which is smooth on the scale r_cut."""
+
+    def __init__(self, plummers: AbstractPotential, r_cut: float):
+        arr = plummers.component_array()
+        if np.any(arr["kind"] != _lib.GAL_PLUMMER):
+            raise NotImplementedError("the short-range split takes Plummer components only")
+        self.r_cut = float(r_cut)
+        self._arr = np.ascontiguousarray(arr)
+        self._G = plummers.G
+        self._handle = None
+        self._dev = None
+
+    def handle(self) -> int:
+        torch = _torch()
+        dev = torch.cuda.current_device()
+        if self._handle is None or self._dev != dev:
+            self.release()
+            h = C.c_void_p()
+            _lib.check(_lib.load().gal_split_create(self._arr.ctypes.data, len(self._arr), self._G, self.r_cut,
+                                                    C.byref(h)), "gal_split_create")
+            self._handle, self._dev = h.value, dev
+        return self._handle
+
+    def release(self):
+        if getattr(self, "_handle", None):
+            try:
+                _lib.load().gal_split_destroy(self._handle)
+            except Exception:  # noqa: BLE001
+                pass
+        self._handle = None
+
+    def __del__(self):
+        self.release()
+
+    def evaluate(self, x):
+        """(phi (n,), grad (n, 3)) of the short-range part at x (n, 3), on the GPU."""
+        torch = _torch()
+        xs = _as_cuda(x, torch.float64).reshape(-1, 3).t().contiguous()
+        n = xs.shape[1]
+        phi = torch.empty(n, dtype=torch.float64, device="cuda")
+        g = torch.empty((3, n), dtype=torch.float64, device="cuda")
+        _lib.check(_lib.load().gal_split_eval(self.handle(), xs.data_ptr(), n, phi.data_ptr(), g.data_ptr(),
+                                              torch.cuda.current_stream().cuda_stream), "gal_split_eval")
+        return phi, g.t()
+
+
 _WS = Workspace()
 
 
 def integrate(analytic: AbstractPotential, mlp: MLPSurrogate | None, y0, t0: float, t1: float, dt: float, *,
-              use_graph: bool = True, soa: bool = False):
-    """Dopri5 with constant step dt under -grad(Phi_analytic + Phi_mlp); returns the
-    final states (n, 6) (or (6, n) with soa=True), on the GPU."""
+              near: ShortRange | None = None, use_graph: bool = True, soa: bool = False):
+    """Dopri5 with constant step dt under -grad(Phi_analytic + Phi_short + Phi_mlp)
+    (``near`` the exact short-range part, or None); returns the final states
+    (n, 6) (or (6, n) with soa=True), on the GPU."""
     torch = _torch()
     y = _as_cuda(y0, torch.float64)
     y = (y if soa else y.reshape(-1, 6).t()).contiguous().clone()
@@ -257,7 +310,8 @@ def integrate(analytic: AbstractPotential, mlp: MLPSurrogate | None, y0, t0: flo
     _lib.check(L.gal_surrogate_workspace_size(n, C.byref(nb)), "gal_surrogate_workspace_size")
     ws = _WS.get(nb.value)
     st = torch.cuda.current_stream().cuda_stream
-    _lib.check(L.gal_integrate_surrogate(analytic.handle(), mlp.handle() if mlp is not None else None, float(dt),
-                                         float(t0), float(t1), y.data_ptr(), n, int(use_graph), ws.data_ptr(),
-                                         ws.numel(), st), "gal_integrate_surrogate")
+    _lib.check(L.gal_integrate_surrogate(analytic.handle(), mlp.handle() if mlp is not None else None,
+                                         near.handle() if near is not None else None, float(dt), float(t0),
+                                         float(t1), y.data_ptr(), n, int(use_graph), ws.data_ptr(), ws.numel(), st),
+               "gal_integrate_surrogate")
     return y if soa else y.t()

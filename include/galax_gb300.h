@@ -303,16 +303,31 @@ GAL_API gal_status gal_mlp_eval(const gal_mlp* mlp, const double* x, int64_t n, 
 /* Error code the inference kernel recorded (0 = none; non-zero = a bounded wait gave up). */
 GAL_API gal_status gal_mlp_error(const gal_mlp* mlp, int32_t* code);
 
+/* Short-range / long-range split of a set of Plummer spheres for the surrogate
+ * (no counterpart in galax). Each sphere Phi_i = -G m_i / sqrt(d^2 + b_i^2)
+ * (builtin/plummer.py:122-133, centred at its origin) is written as
+ * Phi_i S(d / r_cut) + Phi_i (1 - S) with S(q) = (1 - q^2)^3 for q < 1, 0
+ * beyond: the MLP learns the smooth remainder, the short-range part is summed
+ * exactly in FP64 from per-cell neighbour lists built here (device memory
+ * allocated here, freed by gal_split_destroy). comps must all be GAL_PLUMMER. */
+typedef struct gal_split gal_split; /* opaque */
+GAL_API gal_status gal_split_create(const gal_component* comps, int32_t n, double G, double r_cut, gal_split** out);
+GAL_API gal_status gal_split_destroy(gal_split* split);
+/* Short-range potential phi[n] and gradient grad[3][n] at x[3][n] (either output may be NULL). */
+GAL_API gal_status gal_split_eval(const gal_split* split, const double* x, int64_t n, double* phi, double* grad,
+                                  gal_stream_t stream);
+
 /* Orbit integration with a surrogate: acceleration = -grad Phi_analytic (FP64,
- * `pot`) - grad Phi_mlp (tensor cores; NULL = analytic only). Dopri5 with the
- * constant step dt from t0 to t1 (the last step clipped onto t1, as
- * gal_integrate), advancing y[6][n] in place to the final state. use_graph = 1
- * replays one captured CUDA graph per step. Scratch from
- * gal_surrogate_workspace_size (seven stage slopes and the stage positions). */
+ * `pot`) - grad Phi_short (FP64, `near`; NULL = none) - grad Phi_mlp (tensor
+ * cores; NULL = none). Dopri5 with the constant step dt from t0 to t1 (the
+ * last step clipped onto t1, as gal_integrate), advancing y[6][n] in place to
+ * the final state. use_graph = 1 replays one captured CUDA graph per step.
+ * Scratch from gal_surrogate_workspace_size (seven stage slopes and the stage
+ * positions). */
 GAL_API gal_status gal_surrogate_workspace_size(int64_t n, size_t* bytes);
-GAL_API gal_status gal_integrate_surrogate(const gal_potential* pot, const gal_mlp* mlp, double dt, double t0,
-                                           double t1, double* y, int64_t n, int32_t use_graph, void* workspace,
-                                           size_t workspace_bytes, gal_stream_t stream);
+GAL_API gal_status gal_integrate_surrogate(const gal_potential* pot, const gal_mlp* mlp, const gal_split* near,
+                                           double dt, double t0, double t1, double* y, int64_t n, int32_t use_graph,
+                                           void* workspace, size_t workspace_bytes, gal_stream_t stream);
 
 /* ------------------------------------------------------------------ utilities */
 /* Copy the library's Butcher tableau (c[13], a[13][13], b[13], e[13] = b - bhat);

@@ -313,3 +313,27 @@ def stream_fd_grad(c: np.ndarray, setup, target, params, *, rel_h: float = 1e-5,
         h = rel_h * abs(x0)
         out.append((4.0 * d(h / 2) - d(h)) / 3.0)
     return np.array(out)
+
+
+def plummer_short_range(c: np.ndarray, x, r_cut: float, G: float = G_GALACTIC):
+    """Short-range part sum_i Phi_i S(d_i / r_cut), S(q) = (1 - q^2)^3 for q < 1,
+    of Plummer components (direct sum over all of them, no cell lists): returns
+    (phi (n,), grad (n, 3)). Restates the surrogate's split of
+    Phi_i = -G m_i / sqrt(d^2 + b_i^2) (galax builtin/plummer.py:122-133)."""
+    x = _xyz(x)
+    phi = np.zeros(len(x))
+    g = np.zeros((len(x), 3))
+    for comp in c:
+        d = x - np.asarray(comp["origin"])
+        d2 = np.sum(d * d, axis=1)
+        q2 = d2 / r_cut**2
+        inside = q2 < 1.0
+        t = np.where(inside, 1.0 - q2, 0.0)
+        S = t**3
+        s2 = d2 + np.finfo(float).tiny + comp["l1"] ** 2
+        Gm = G * comp["m"]
+        ph = -Gm / np.sqrt(s2)
+        phi += ph * S
+        # grad(Phi S) = S grad Phi + Phi grad S, grad S = -6 t^2 d / r_cut^2
+        g += (S * Gm / s2**1.5)[:, None] * d + (ph * (-6.0 * t**2 / r_cut**2))[:, None] * d
+    return phi, g

@@ -168,3 +168,65 @@ def test_training_reduces_the_loss(env):
     g_ref = O.gradient(plum, x[:4096])
     rel = np.linalg.norm(g - g_ref, axis=1) / np.linalg.norm(g_ref, axis=1)
     assert np.median(rel) < 0.2
+
+
+def _subhalos(n=64, seed=11):
+    rng = np.random.default_rng(seed)
+    m = np.exp(rng.uniform(np.log(1e6), np.log(1e8), n))
+    b = rng.uniform(0.1, 1.0, n)
+    v = rng.normal(size=(n, 3))
+    c = v / np.linalg.norm(v, axis=1, keepdims=True) * rng.uniform(5.0, 30.0, n)[:, None]
+    return O.comps([(O.PLUMMER, m[i], b[i], 0.0, tuple(c[i])) for i in range(n)])
+
+
+def test_short_range_split_matches_direct_taper_sum(env):
+    """The cell-list short-range sum equals the direct sum of the tapered spheres
+    everywhere: next to centres, across cell faces and outside the grid."""
+    gx, S = env
+    subs = _subhalos()
+    near = S.ShortRange(gx.potential.from_component_array(subs), 3.0)
+    rng = np.random.default_rng(12)
+    x = np.concatenate([
+        rng.normal(size=(4000, 3)) * 20.0,                                              # spread out
+        subs["origin"][rng.integers(0, len(subs), 4000)] + rng.normal(size=(4000, 3)),  # next to centres
+        rng.normal(size=(50, 3)) * 200.0,                                               # mostly outside the grid
+    ])
+    phi, g = near.evaluate(x)
+    phi_r, g_r = O.plummer_short_range(subs, x, 3.0)
+    phi, g = phi.cpu().numpy(), g.cpu().numpy()
+    assert np.count_nonzero(phi_r) > 4000
+    np.testing.assert_allclose(phi, phi_r, rtol=1e-12, atol=1e-18)
+    np.testing.assert_allclose(g, g_r, rtol=1e-11, atol=1e-18)
+
+
+def test_surrogate_integrator_adds_the_exact_short_range_field(env):
+    """Zero MLP plus the split: the orbit is Dopri5 under Milky Way + short-range
+    sum (checked against a NumPy constant-step Dopri5 on the oracle's fields)."""
+    gx, S = env
+    from galax_gb300 import workloads as W
+
+    subs = _subhalos(seed=14)
+    near = S.ShortRange(gx.potential.from_component_array(subs), 4.0)
+    p = _params(S)
+    d = S.unpack(p)
+    d["w5"][:] = 0.0
+    d["b5"][:] = 0.0
+    mlp = S.MLPSurrogate(p, 50.0, 1e-3)
+    mw = gx.MilkyWayPotential()
+    y0 = W.disk_like_ics(lambda x: O.gradient(O.milky_way(), x), 64, seed=15)
+    got = S.integrate(mw, mlp, y0, 0.0, 60.0, 1.0, near=near).cpu().numpy()
+    c, a, b, _ = O.tableau(5)
+
+    def f(y):
+        g = O.gradient(O.milky_way(), y[:, :3]) + O.plummer_short_range(subs, y[:, :3], 4.0)[1]
+        return np.concatenate([y[:, 3:], -g], axis=1)
+
+    y = y0.copy()
+    for _ in range(60):
+        F = [f(y)]
+        for i in range(1, len(c)):
+            F.append(f(y + sum(a[i][j] * F[j] for j in range(i)) * 1.0))
+        y = y + sum(b[i] * F[i] for i in range(len(c))) * 1.0
+    np.testing.assert_allclose(got, y, rtol=1e-10, atol=1e-12)
+    plain = S.integrate(mw, mlp, y0, 0.0, 60.0, 1.0).cpu().numpy()
+    assert np.abs(plain - got).max() > 1e-8  # the short-range field does act

@@ -599,7 +599,7 @@ def run_stream(args, n_rel, rank, world, dist) -> dict | None:
     mw = gx.MilkyWayPotential()
     s = W.stream_setup(lambda x: mw.gradient(x), n_release=n_rel, seed=4 + rank)
     cfg = ST.config(n_release=n_rel, dt=s.dt, w_now=s.w_now, prog_m=s.prog_m, prog_b=s.prog_b, method=8,
-                    k_ckpt=256)
+                    k_ckpt=args.stream_ckpt)
     noise = torch.as_tensor(s.noise, device="cuda")
     base = ST.simulate(mw, cfg, noise)
     target = (base.final + torch.as_tensor(s.pert, device="cuda")).contiguous()
@@ -652,12 +652,16 @@ def run_stream(args, n_rel, rank, world, dist) -> dict | None:
                    "particle_steps": particle_steps, "forward_ms": fwd_ms,
                    "forward_particle_steps_per_s": particle_steps / (fwd_ms * 1e-3),
                    "halo_grad_m_rs": [float(g.grad_params[1][0]), float(g.grad_params[1][1])],
-                   "l2": "each step recomputes everything from the inputs; mu partials (176 MB) exceed L2"},
+                   "adjoint_storage": "every particle stage stored (k_ckpt=0)" if args.stream_ckpt == 0 else
+                   f"checkpoints every {args.stream_ckpt} steps",
+                   "l2": "each step recomputes everything from the inputs; stored stages (17 GB) and mu partials "
+                         "(176 MB) exceed L2"},
         "e2e": {"value": world / (e2e_ms * 1e-3), "unit": "gradients/s", "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": int(s.noise.size * 8 + target.numel() * 8), "d2h_bytes_per_step": 12 * 8},
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak["tflops"], "unit": "TFLOP/s",
                      "frac": achieved / peak["tflops"], "traffic": None,
-                     "note": "algorithmic flops = 4 x forward (particle steps x 2,562 + progenitor 2 x n_rel x 2,276); "
+                     "note": "algorithmic flops = 4 x forward (particle steps x 2,562 + progenitor 2 x n_rel x 2,276), "
+                             "the checkpointed adjoint's count, kept as the unit of work for both storage modes; "
                              "6,000 particles fill 188 warps, and the progenitor is one serial orbit, so the "
                              "pipeline is bound by FP64 latency along its longest chains, not by the FP64 pipe"},
         "clocks": clk, "gpu_launches": 9 * args.steps,
@@ -782,8 +786,10 @@ def main():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--t1", type=float, default=0.0, help="grad workload: end time in Myr (default 2000)")
     ap.add_argument("--train-points", type=int, default=4_194_304, help="surrogate workload: training samples")
-    ap.add_argument("--train-epochs", type=int, default=30, help="surrogate workload: training epochs")
+    ap.add_argument("--train-epochs", type=int, default=200, help="surrogate workload: training epochs")
     ap.add_argument("--plain-orbits", type=int, default=65_536, help="surrogate workload: orbits for the plain path")
+    ap.add_argument("--stream-ckpt", type=int, default=0,
+                    help="stream workload: particle checkpoint interval (0 = store every stage, no recompute)")
     ap.add_argument("--split-radius", type=float, default=4.0,
                     help="surrogate workload: short-range split radius in kpc (0 = the MLP learns the whole sum)")
     args = ap.parse_args()

@@ -65,7 +65,11 @@ struct StreamDev {
   const double* noise;   // [12][n_rel]: xi_lead, eta_lead, xi_trail, eta_trail
   double* ics;           // [6][np]
   double* fin;           // [6][np]
-  double* ckpt;          // [nseg][6][np] (gradient only)
+  double* ckpt;          // [nseg][6][np] (gradient with k_ckpt >= 1)
+  double* Ys;            // particle stage positions, Hessians and velocity cotangents at every
+  double* Hs;            // stage point (gradient with k_ckpt = 0); step k holds the 2(k+1) released
+  double* vs;            // particles: [S][E][2(k+1)] after k(k+1) S E earlier entries (E = 3, 12, 3)
+  int64_t pg_col0;       // first gp_all column of the stored-stage parameter partials
   double* seg;           // [K][6][np]
   const double* target;  // [6][np]
   double* lam_rel;       // [6][np] dL/dy_p at the release step
@@ -129,6 +133,34 @@ __device__ __forceinline__ void plummer_hv(double GMp, double b2, const double* 
   const double dv = fma(d[0], v[0], fma(d[1], v[1], d[2] * v[2]));
 #pragma unroll
   for (int j = 0; j < 3; ++j) Hv[j] = fma(g, v[j], gpr * dv * d[j]);
+}
+
+// Stored-stage layout: entry e of stage i of particle p at step k.
+__host__ __device__ __forceinline__ int64_t stage_idx(int64_t k, int i, int e, int64_t p, int S, int E) {
+  return k * (k + 1) * S * E + ((int64_t)i * E + e) * (2 * (k + 1)) + p;
+}
+
+// particle step that also records its stage positions
+template <class TB, class Host>
+__device__ __forceinline__ void particle_step_store(const Host& host, double GMp, double b2, const double* Qk,
+                                                    double* y, double hs, double* Ys, int64_t k, int64_t p) {
+  constexpr int S = TB::S;
+  double F[S][6];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) Ys[stage_idx(k, 0, c, p, S, 3)] = y[c];
+  pfield(host, GMp, b2, Qk, y, F[0]);
+  static_for<1, S>([&](auto i) {
+    constexpr int I = decltype(i)::value;
+    double Y[6];
+    stage_state<TB, I>(y, hs, F, Y);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) Ys[stage_idx(k, I, c, p, S, 3)] = Y[c];
+    pfield(host, GMp, b2, Qk + 3 * I, Y, F[I]);
+  });
+  double y1[6];
+  rk_combine<TB>(y, hs, F, y1, nullptr);
+#pragma unroll
+  for (int j = 0; j < 6; ++j) y[j] = y1[j];
 }
 
 // ------------------------------------------------------------------ forward
@@ -246,6 +278,10 @@ __global__ void __launch_bounds__(32) k_stream_particles(StreamDev a, Host host,
 #pragma unroll
   for (int j = 0; j < 6; ++j) y[j] = a.ics[j * n + p];
   for (int64_t k = r; k < a.n_rel; ++k) {
+    if (a.Ys) {
+      particle_step_store<TB>(h, a.GMp, a.b2, a.Q + k * TB::S * 3, y, a.dt, a.Ys, k, p);
+      continue;
+    }
     if (a.ckpt && (k == r || k % K == 0)) {
       const int64_t g = k / K;
 #pragma unroll
@@ -384,6 +420,178 @@ __global__ void __launch_bounds__(32) k_stream_particles_adj(StreamDev a, Host h
     for (int c = 0; c < 3 * ncomp; ++c) a.gp_all[(int64_t)c * a.ncol + p] = gp[c];
     a.gp_all[(int64_t)(3 * ncomp) * a.ncol + p] = loss;
   }
+}
+
+// ---- stored-stage particle adjoint (k_ckpt = 0)
+// (k, p) of particle-step q in the stored layout: step k holds particles 0 .. 2k+1
+__device__ __forceinline__ void particle_step_of(int64_t q, int64_t& k, int64_t& p) {
+  int64_t kk = (int64_t)((sqrt(4.0 * (double)q + 1.0) - 1.0) * 0.5);
+  while ((kk + 1) * (kk + 2) <= q) ++kk;
+  while (kk * (kk + 1) > q) --kk;
+  k = kk;
+  p = q - kk * (kk + 1);
+}
+
+// Hessians at every particle stage point: host + progenitor (0..5) and progenitor alone (6..11).
+template <class TB>
+__global__ void __launch_bounds__(128) k_stream_particle_hess(StreamDev a, const DevComp* comps) {
+  __shared__ DevComp s_comps[kAdjMaxComps];
+  stage_comps(comps, a.ncomp, s_comps);
+  constexpr int S = TB::S;
+  const int64_t nq = a.n_rel * (a.n_rel + 1);
+  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q >= nq) return;
+  int64_t k, p;
+  particle_step_of(q, k, p);
+  for (int i = 0; i < S; ++i) {
+    const double Y[3] = {a.Ys[stage_idx(k, i, 0, p, S, 3)], a.Ys[stage_idx(k, i, 1, p, S, 3)],
+                         a.Ys[stage_idx(k, i, 2, p, S, 3)]};
+    double H[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int c = 0; c < a.ncomp; ++c) comp_hessian(s_comps[c], Y[0], Y[1], Y[2], H);
+    const double* Qi = a.Q + (k * S + i) * 3;
+    const double d[3] = {Y[0] - Qi[0], Y[1] - Qi[1], Y[2] - Qi[2]};
+    const double r2 = fma(d[0], d[0], fma(d[1], d[1], fma(d[2], d[2], TINY)));
+    const double is = rsqrt(r2 + a.b2), is2 = is * is;
+    const double g = a.GMp * is2 * is, gpr = -3.0 * g * is2;
+    const double Hp[6] = {fma(gpr * d[0], d[0], g), gpr * d[0] * d[1], gpr * d[0] * d[2],
+                          fma(gpr * d[1], d[1], g), gpr * d[1] * d[2], fma(gpr * d[2], d[2], g)};
+    const double Ht[6] = {H[0] + Hp[0], H[1] + Hp[1], H[2] + Hp[2], H[4] + Hp[3], H[5] + Hp[4], H[8] + Hp[5]};
+#pragma unroll
+    for (int e = 0; e < 6; ++e) {
+      a.Hs[stage_idx(k, i, e, p, S, 12)] = Ht[e];
+      a.Hs[stage_idx(k, i, 6 + e, p, S, 12)] = Hp[e];
+    }
+  }
+}
+
+__device__ __forceinline__ void sym_mv(const double* H, const double* v, double* o) {
+  o[0] = fma(H[0], v[0], fma(H[1], v[1], H[2] * v[2]));
+  o[1] = fma(H[1], v[0], fma(H[3], v[1], H[4] * v[2]));
+  o[2] = fma(H[2], v[0], fma(H[4], v[1], H[5] * v[2]));
+}
+
+// Reverse sweep with the stored Hessians: no potential evaluations on the serial chain.
+template <class TB>
+__global__ void __launch_bounds__(32) k_stream_particles_sweep(StreamDev a) {
+  constexpr int S = TB::S;
+  const int lane = threadIdx.x;
+  const int64_t w = blockIdx.x;
+  const int64_t p = w * 32 + lane;
+  const int64_t n = a.np;
+  const bool valid = p < n;
+  const int64_t rp = valid ? (p >> 1) : LLONG_MAX;
+  const int64_t rmin = (w * 32) >> 1;
+  const double dt = a.dt;
+  double lam[6], loss = 0.0;
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    const double d = valid ? a.fin[j * n + p] - a.target[j * n + p] : 0.0;
+    lam[j] = 2.0 * d;
+    loss = fma(d, d, loss);
+  }
+  for (int64_t k = a.n_rel - 1; k >= rmin; --k) {
+    const bool act = valid && k >= rp;
+    double F[S][6];
+    static_for<0, S>([&](auto i) {
+      constexpr int I = decltype(i)::value;
+      constexpr double bi = TB::B[I];
+#pragma unroll
+      for (int j = 0; j < 6; ++j) F[I][j] = dt * bi * lam[j];
+    });
+    double* mw_out = a.mu_warp + (w * a.n_rel + k) * (S * 3);
+    static_for<0, S>([&](auto rr) {
+      constexpr int I = S - 1 - decltype(rr)::value;
+      const double v[3] = {F[I][3], F[I][4], F[I][5]};
+      double Ht[6] = {0, 0, 0, 0, 0, 0}, Hp[6] = {0, 0, 0, 0, 0, 0};
+      if (act) {
+#pragma unroll
+        for (int e = 0; e < 6; ++e) {
+          Ht[e] = a.Hs[stage_idx(k, I, e, p, S, 12)];
+          Hp[e] = a.Hs[stage_idx(k, I, 6 + e, p, S, 12)];
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) a.vs[stage_idx(k, I, c, p, S, 3)] = v[c];
+      }
+      double Hv[3], Hpv[3];
+      sym_mv(Ht, v, Hv);
+      sym_mv(Hp, v, Hpv);
+      const double m0 = warp_sum(act ? Hpv[0] : 0.0);
+      const double m1 = warp_sum(act ? Hpv[1] : 0.0);
+      const double m2 = warp_sum(act ? Hpv[2] : 0.0);
+      if (lane == 0) {
+        mw_out[3 * I + 0] = m0;
+        mw_out[3 * I + 1] = m1;
+        mw_out[3 * I + 2] = m2;
+      }
+      const double Yb[6] = {-Hv[0], -Hv[1], -Hv[2], F[I][0], F[I][1], F[I][2]};
+      if (act) {
+#pragma unroll
+        for (int j = 0; j < 6; ++j) lam[j] += Yb[j];
+      }
+      static_for<0, I>([&](auto l) {
+        constexpr int L = decltype(l)::value;
+        constexpr double c = TB::A[I][L];
+        if constexpr (c != 0.0) {
+#pragma unroll
+          for (int j = 0; j < 6; ++j) F[L][j] = fma(dt * c, Yb[j], F[L][j]);
+        }
+      });
+    });
+    if (valid && k == rp) {
+#pragma unroll
+      for (int j = 0; j < 6; ++j) a.lam_rel[j * n + p] = lam[j];
+    }
+  }
+  if (valid) {
+    for (int c = 0; c < 3 * a.ncomp; ++c) a.gp_all[(int64_t)c * a.ncol + p] = 0.0;
+    a.gp_all[(int64_t)(3 * a.ncomp) * a.ncol + p] = loss;
+  }
+}
+
+// Parameter terms -sum d(grad Phi_host . v)/dtheta over all particle stage points,
+// one column of partial sums per block.
+template <class TB>
+__global__ void __launch_bounds__(256) k_stream_particles_pgrad(StreamDev a, const DevComp* comps) {
+  __shared__ DevComp s_comps[kAdjMaxComps];
+  __shared__ double red[kAdjMaxComps * 3][8];
+  stage_comps(comps, a.ncomp, s_comps);
+  constexpr int S = TB::S;
+  const int64_t nq = a.n_rel * (a.n_rel + 1);
+  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int nc3 = 3 * a.ncomp;
+  double acc[kAdjMaxComps * 3];
+#pragma unroll
+  for (int i = 0; i < kAdjMaxComps * 3; ++i) acc[i] = 0.0;
+  if (q < nq) {
+    int64_t k, p;
+    particle_step_of(q, k, p);
+    for (int i = 0; i < S; ++i) {
+      const double Y[3] = {a.Ys[stage_idx(k, i, 0, p, S, 3)], a.Ys[stage_idx(k, i, 1, p, S, 3)],
+                           a.Ys[stage_idx(k, i, 2, p, S, 3)]};
+      const double v[3] = {a.vs[stage_idx(k, i, 0, p, S, 3)], a.vs[stage_idx(k, i, 1, p, S, 3)],
+                           a.vs[stage_idx(k, i, 2, p, S, 3)]};
+      for (int c = 0; c < a.ncomp; ++c) {
+        double Hv[3] = {0, 0, 0}, dp[3] = {0, 0, 0};
+        comp_vjp(s_comps[c], Y, v, Hv, dp);
+        acc[3 * c + 0] -= dp[0];
+        acc[3 * c + 1] -= dp[1];
+        acc[3 * c + 2] -= dp[2];
+      }
+    }
+  }
+  // warp sums, then the block's eight warps in order
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int c = 0; c < nc3; ++c) {
+    const double v = warp_sum(acc[c]);
+    if (lane == 0) red[c][wid] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < nc3) {
+    double t = 0.0;
+    for (int j = 0; j < (int)(blockDim.x >> 5); ++j) t += red[threadIdx.x][j];
+    a.gp_all[(int64_t)threadIdx.x * a.ncol + a.pg_col0 + blockIdx.x] = t;
+  }
+  if (threadIdx.x == 0) a.gp_all[(int64_t)nc3 * a.ncol + a.pg_col0 + blockIdx.x] = 0.0;
 }
 
 // mu[k][:] = sum over the warps that had released particles by step k, in warp order.
@@ -753,8 +961,8 @@ __global__ void k_stream_reduce_rows(const double* __restrict__ in, int64_t n, d
 static size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 struct StreamLayout {
-  size_t B, P, Q, Qb, Hst, vst, rt_om, ics, fin, ckpt, seg, lam_rel, mu_warp, mu, nu, gp_all, red, total;
-  int64_t np, nwarps, nseg, ncol;
+  size_t B, P, Q, Qb, Hst, vst, rt_om, ics, fin, ckpt, seg, Ys, Hs, vs, lam_rel, mu_warp, mu, nu, gp_all, red, total;
+  int64_t np, nwarps, nseg, ncol, pg_col0, pg_blocks;
   int S;
 };
 
@@ -763,9 +971,13 @@ static StreamLayout stream_layout(int ncomp, const gal_stream_config& c, bool gr
   L.S = c.method == 5 ? Dopri5::S : Dopri8::S;
   L.np = 2 * c.n_release;
   L.nwarps = (L.np + 31) / 32;
+  const bool stored = c.k_ckpt == 0;
   const int K = c.k_ckpt > 0 ? c.k_ckpt : 1;
   L.nseg = (c.n_release + K - 1) / K;
-  L.ncol = L.np + c.n_release + 2 * c.n_release * L.S;
+  const int64_t nq = c.n_release * (c.n_release + 1);  // particle-steps
+  L.pg_col0 = L.np + c.n_release + 2 * c.n_release * L.S;
+  L.pg_blocks = stored ? (nq + 255) / 256 : 0;
+  L.ncol = L.pg_col0 + L.pg_blocks;
   const size_t d = sizeof(double);
   const size_t nr = (size_t)c.n_release;
   size_t off = 0;
@@ -784,8 +996,14 @@ static StreamLayout stream_layout(int ncomp, const gal_stream_config& c, bool gr
     L.Qb = take(d * 3 * L.S * nr);
     L.Hst = take(d * 6 * 2 * L.S * nr);
     L.vst = take(d * 3 * 2 * L.S * nr);
-    L.ckpt = take(d * 6 * L.nseg * L.np);
-    L.seg = take(d * 6 * (size_t)K * L.np);
+    if (stored) {
+      L.Ys = take(d * 3 * L.S * (size_t)nq);
+      L.Hs = take(d * 12 * L.S * (size_t)nq);
+      L.vs = take(d * 3 * L.S * (size_t)nq);
+    } else {
+      L.ckpt = take(d * 6 * L.nseg * L.np);
+      L.seg = take(d * 6 * (size_t)K * L.np);
+    }
     L.lam_rel = take(d * 6 * L.np);
     L.mu_warp = take(d * 3 * L.S * nr * L.nwarps);
     L.mu = take(d * 3 * L.S * nr);
@@ -802,7 +1020,7 @@ static gal_status stream_validate(const gal_potential* pot, const gal_stream_con
   if (c->method != 5 && c->method != 8) return fail(GAL_ERR_INVALID_ARGUMENT, "method must be 5 or 8");
   if (!(c->dt > 0.0)) return fail(GAL_ERR_INVALID_ARGUMENT, "dt must be > 0");
   if (c->n_release < 1) return fail(GAL_ERR_INVALID_ARGUMENT, "n_release must be >= 1");
-  if (c->k_ckpt < 1) return fail(GAL_ERR_INVALID_ARGUMENT, "k_ckpt must be >= 1");
+  if (c->k_ckpt < 0) return fail(GAL_ERR_INVALID_ARGUMENT, "k_ckpt must be >= 0");
   if (!(c->prog_m > 0.0) || !(c->prog_b > 0.0)) return fail(GAL_ERR_INVALID_ARGUMENT, "progenitor m, b must be > 0");
   if (pot->n > kAdjMaxComps) return fail(GAL_ERR_UNSUPPORTED, "stream host potentials have at most 8 components");
   return GAL_OK;
@@ -815,6 +1033,7 @@ static StreamDev stream_args(const gal_potential* pot, const gal_stream_config* 
   a.np = L.np;
   a.nwarps = L.nwarps;
   a.ncol = L.ncol;
+  a.pg_col0 = L.pg_col0;
   a.dt = c->dt;
   a.GMp = pot->G * c->prog_m;
   a.b2 = c->prog_b * c->prog_b;
@@ -833,8 +1052,14 @@ static StreamDev stream_args(const gal_potential* pot, const gal_stream_config* 
     a.Qb = at(L.Qb);
     a.Hst = at(L.Hst);
     a.vst = at(L.vst);
-    a.ckpt = at(L.ckpt);
-    a.seg = at(L.seg);
+    if (c->k_ckpt == 0) {
+      a.Ys = at(L.Ys);
+      a.Hs = at(L.Hs);
+      a.vs = at(L.vs);
+    } else {
+      a.ckpt = at(L.ckpt);
+      a.seg = at(L.seg);
+    }
     a.lam_rel = at(L.lam_rel);
     a.mu_warp = at(L.mu_warp);
     a.mu = at(L.mu);
@@ -854,7 +1079,14 @@ static cudaError_t stream_forward(const StreamDev& a, const Host& host, const De
 
 template <class TB, class Host>
 static cudaError_t stream_backward(const StreamDev& a, const Host& host, const DevComp* comps, cudaStream_t s) {
-  k_stream_particles_adj<TB, Host><<<(unsigned)a.nwarps, 32, 0, s>>>(a, host, comps);
+  if (a.Ys) {
+    const int64_t nq = a.n_rel * (a.n_rel + 1);
+    k_stream_particle_hess<TB><<<(unsigned)((nq + 127) / 128), 128, 0, s>>>(a, comps);
+    k_stream_particles_sweep<TB><<<(unsigned)a.nwarps, 32, 0, s>>>(a);
+    k_stream_particles_pgrad<TB><<<(unsigned)((nq + 255) / 256), 256, 0, s>>>(a, comps);
+  } else {
+    k_stream_particles_adj<TB, Host><<<(unsigned)a.nwarps, 32, 0, s>>>(a, host, comps);
+  }
   const int S3 = 3 * TB::S;
   k_stream_mu_reduce<<<(unsigned)((a.n_rel * S3 + 255) / 256), 256, 0, s>>>(a, S3);
   k_stream_release_adj<<<(unsigned)((a.n_rel + 127) / 128), 128, 0, s>>>(a, comps);

@@ -233,7 +233,11 @@ GAL_API gal_status gal_adjoint(const gal_potential* pot, const gal_solver_config
  * xi_lead(3), eta_lead(3), xi_trail(3), eta_trail(3). */
 typedef struct gal_stream_config {
   int32_t method;    /* 5 = Dopri5, 8 = Dopri8 */
-  int32_t k_ckpt;    /* gradient: particle checkpoint interval in steps (>= 1) */
+  int32_t k_ckpt;    /* gradient: >= 1 keeps particle checkpoints every k_ckpt steps and recomputes
+                      * (memory ~ 2 n_release (n_release / k_ckpt + k_ckpt) 48 bytes); 0 stores every
+                      * particle stage position and Hessian instead, taking all potential evaluations
+                      * off the reverse sweep (memory n_release (n_release + 1) S 144 bytes, S = 13
+                      * for Dopri8) */
   int64_t n_release; /* releases (>= 1); particles = 2 n_release */
   double dt;         /* constant step (> 0) */
   double t_now;      /* present time (the potential is static: only labels times) */

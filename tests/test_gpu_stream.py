@@ -81,13 +81,14 @@ def test_forward_matches_oracle(S, host, method):
     assert _relmax(got.final, ref["final"]) < 1e-9
 
 
+@pytest.mark.parametrize("k_ckpt", [64, 0])
 @pytest.mark.parametrize("host", list(HOSTS))
-def test_gradient_matches_finite_differences(S, host):
+def test_gradient_matches_finite_differences(S, host, k_ckpt):
     comps = HOSTS[host]
     s = _setup(comps)
     ref = O.stream_forward(comps, s)
     target = ref["final"] + s.pert
-    g = S.gradient(_pot(comps), _cfg(S, s), s.noise, target)
+    g = S.gradient(_pot(comps), _cfg(S, s, k_ckpt=k_ckpt), s.noise, target)
     assert _relmax(g.final, ref["final"]) < 1e-9
     assert g.loss == pytest.approx(float(np.sum((ref["final"] - target) ** 2)), rel=1e-7)
     fields = ("m", "l1", "l2")
@@ -127,6 +128,8 @@ def test_gradient_with_respect_to_the_present_progenitor_point(S):
 
 
 def test_checkpoint_interval_does_not_change_results(S):
+    """Checkpointed sweeps agree bitwise for every interval; the stored-stage
+    sweep (k_ckpt = 0, Hessians computed ahead) agrees to rounding."""
     comps = HOSTS["milky_way"]
     s = _setup(comps, n_release=70)
     target = O.stream_forward(comps, s)["final"] + s.pert
@@ -135,6 +138,10 @@ def test_checkpoint_interval_does_not_change_results(S):
         assert np.array_equal(o.grad_params, outs[0].grad_params)
         assert np.array_equal(o.grad_w_now, outs[0].grad_w_now)
         assert np.array_equal(o.final, outs[0].final)
+    st = S.gradient(_pot(comps), _cfg(S, s, k_ckpt=0), s.noise, target)
+    assert np.array_equal(st.final, outs[0].final)
+    np.testing.assert_allclose(st.grad_params, outs[0].grad_params, rtol=1e-10, atol=1e-300)
+    np.testing.assert_allclose(st.grad_w_now, outs[0].grad_w_now, rtol=1e-10, atol=1e-14)
 
 
 def test_single_release_and_repeatability(S):
@@ -158,7 +165,7 @@ def test_invalid_configurations_raise(S):
 
     comps = HOSTS["milky_way"]
     s = _setup(comps, n_release=4)
-    for bad in (dict(method=6), dict(k_ckpt=0)):
+    for bad in (dict(method=6), dict(k_ckpt=-1)):
         cfg = _cfg(S, s, **bad)
         with pytest.raises(GalaxGB300Error):
             S.simulate(_pot(comps), cfg, s.noise)

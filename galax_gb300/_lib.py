@@ -85,6 +85,11 @@ SIGNATURES = {
     "gal_integrate_noalloc": (C.c_int, [C.c_void_p, C.POINTER(SolverConfig), _DP, _DP, _DP, _I64P, _DP, C.c_int64,
                                         _DP, _I32P, _I64P, _I32P, C.c_int64, C.c_void_p]),
     "gal_set_launch": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
+    "gal_dense_coef_per_step": (C.c_int32, [C.c_int32]),
+    "gal_integrate_dense": (C.c_int, [C.c_void_p, C.POINTER(SolverConfig), _DP, _DP, _DP, C.c_int64, C.c_int64, _DP,
+                                      _DP, _I64P, _I32P, C.c_void_p]),
+    "gal_dense_evaluate": (C.c_int, [C.c_void_p, C.c_int32, _DP, _DP, _I64P, C.c_int64, C.c_int64, _I64P, _DP,
+                                     C.c_int64, _DP, C.c_void_p, C.c_void_p]),
     "gal_adjoint_workspace_size": (C.c_int, [C.c_void_p, C.POINTER(SolverConfig), C.c_double, C.c_double,
                                              C.c_int32, C.c_int64, C.POINTER(C.c_size_t)]),
     "gal_adjoint": (C.c_int, [C.c_void_p, C.POINTER(SolverConfig), _DP, C.c_double, C.c_double, _DP, _DP, _DP, _DP,

@@ -6,11 +6,13 @@
 // and a long-range remainder Phi_i (1 - S), with the C2 taper
 // S(q) = (1 - q^2)^3 for q < 1 and 0 beyond. The remainder is smooth on the
 // scale r_c, which is what the MLP learns; the short-range part, non-zero only
-// within r_c of a centre, is summed exactly in FP64 here. A uniform grid of
+// within r_c of a centre, is summed directly here (FP64 offsets and
+// accumulation, FP32 terms: see split.cuh). A uniform grid of
 // cells of side r_c over the centres' bounding box (grown by r_c) lists, for
 // every cell, the spheres whose centre lies within r_c of some point of the
-// cell, with their parameters copied into the list (cx, cy, cz, G m, b^2) so a
-// lookup touches one contiguous run. Points outside the grid have no
+// cell, with their parameters copied into the list (centre relative to the
+// cell's low corner and G m as a float4, b^2 beside it) so a lookup touches one
+// contiguous run. Points outside the grid have no
 // short-range neighbours.
 #include <cuda_runtime.h>
 
@@ -26,7 +28,8 @@ using namespace gal;
 struct gal_split {
   SplitDev dev;
   int64_t* d_start;
-  double* d_items;
+  float4* d_items;
+  float* d_b2;
   int32_t n;
 };
 
@@ -96,37 +99,47 @@ gal_status gal_split_create(const gal_component* comps, int32_t n, double G, dou
   }
   std::vector<int64_t> start((size_t)ncell + 1, 0);
   for (int64_t cidx = 0; cidx < ncell; ++cidx) start[cidx + 1] = start[cidx] + (int64_t)lists[cidx].size();
-  std::vector<double> items((size_t)start[ncell] * 5);
-  for (int64_t cidx = 0; cidx < ncell; ++cidx)
+  std::vector<float4> items((size_t)start[ncell]);
+  std::vector<float> b2s((size_t)start[ncell]);
+  for (int64_t cidx = 0; cidx < ncell; ++cidx) {
+    const int64_t ix = cidx % nx, iy = (cidx / nx) % nx, iz = cidx / ((int64_t)nx * nx);
+    const double corner[3] = {glo + ix * h, glo + iy * h, glo + iz * h};
     for (size_t k = 0; k < lists[cidx].size(); ++k) {
       const gal_component& cc = comps[lists[cidx][k]];
-      double* it = &items[((size_t)start[cidx] + k) * 5];
-      it[0] = cc.origin[0];
-      it[1] = cc.origin[1];
-      it[2] = cc.origin[2];
-      it[3] = G * cc.m;
-      it[4] = cc.l1 * cc.l1;
+      const size_t o = (size_t)start[cidx] + k;
+      items[o] = make_float4((float)(cc.origin[0] - corner[0]), (float)(cc.origin[1] - corner[1]),
+                             (float)(cc.origin[2] - corner[2]), (float)(G * cc.m));
+      b2s[o] = (float)(cc.l1 * cc.l1);
     }
+  }
   gal_split* sp = new gal_split();
   sp->n = n;
   sp->d_start = nullptr;
   sp->d_items = nullptr;
+  sp->d_b2 = nullptr;
+  const size_t ni = std::max<size_t>(items.size(), 1);
   cudaError_t e = cudaMalloc(&sp->d_start, sizeof(int64_t) * start.size());
-  if (e == cudaSuccess) e = cudaMalloc(&sp->d_items, sizeof(double) * std::max<size_t>(items.size(), 5));
+  if (e == cudaSuccess) e = cudaMalloc(&sp->d_items, sizeof(float4) * ni);
+  if (e == cudaSuccess) e = cudaMalloc(&sp->d_b2, sizeof(float) * ni);
   if (e == cudaSuccess)
     e = cudaMemcpy(sp->d_start, start.data(), sizeof(int64_t) * start.size(), cudaMemcpyHostToDevice);
   if (e == cudaSuccess && !items.empty())
-    e = cudaMemcpy(sp->d_items, items.data(), sizeof(double) * items.size(), cudaMemcpyHostToDevice);
+    e = cudaMemcpy(sp->d_items, items.data(), sizeof(float4) * items.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && !b2s.empty())
+    e = cudaMemcpy(sp->d_b2, b2s.data(), sizeof(float) * b2s.size(), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
     cudaFree(sp->d_start);
     cudaFree(sp->d_items);
+    cudaFree(sp->d_b2);
     delete sp;
     return cuda_fail(e, "gal_split_create");
   }
   sp->dev.start = sp->d_start;
   sp->dev.items = sp->d_items;
+  sp->dev.b2 = sp->d_b2;
   sp->dev.nx = nx;
   sp->dev.lo = glo;
+  sp->dev.h = h;
   sp->dev.inv_h = 1.0 / h;
   sp->dev.rc2 = r_cut * r_cut;
   sp->dev.inv_rc2 = 1.0 / (r_cut * r_cut);
@@ -138,6 +151,7 @@ gal_status gal_split_destroy(gal_split* sp) {
   if (!sp) return GAL_OK;
   cudaFree(sp->d_start);
   cudaFree(sp->d_items);
+  cudaFree(sp->d_b2);
   delete sp;
   return GAL_OK;
 }

@@ -287,6 +287,95 @@ def _split_w0(w0):
     return w, None
 
 
+# ---------------------------------------------------------------- dense output
+class PhaseSpaceInterpolation:
+    """Dense orbits on the GPU (galax's PhaseSpaceInterpolation,
+    src/galax/dynamics/_src/orbit/interp.py:42-145): per accepted step the
+    library keeps the step boundaries and its interpolation data
+    (``gal_integrate_dense``); ``evaluate(ts)`` returns every orbit at the
+    times ``ts`` (``gal_dense_evaluate``). Times outside an orbit's [t0, t1]
+    raise, as galax's ``eqx.error_if(..., "Time out of bounds.")`` does."""
+
+    def __init__(self, pot: AbstractPotential, method: int, ts, coef, nsteps, cap: int, batch: tuple):
+        self.pot = pot
+        self.method = int(method)
+        self.ts = ts            # (n, cap + 1)
+        self.coef = coef        # (n, cap, per_step)
+        self.nsteps = nsteps    # (n,)
+        self.cap = int(cap)
+        self.batch = tuple(batch)
+
+    @property
+    def t0(self):
+        return self.ts[:, 0]
+
+    @property
+    def t1(self):
+        torch = _torch()
+        return torch.gather(self.ts, 1, self.nsteps.reshape(-1, 1)).reshape(-1)
+
+    def evaluate(self, t):
+        """(q, p) of every orbit at times t: shapes (*batch, T, 3)."""
+        torch = _torch()
+        tq = _as_cuda(t, torch.float64).reshape(-1)
+        T = tq.numel()
+        n = self.nsteps.numel()
+        orbit = torch.arange(n, dtype=torch.int64, device="cuda").repeat_interleave(T)
+        times = tq.repeat(n).contiguous()
+        m = orbit.numel()
+        out = torch.empty((6, m), dtype=torch.float64, device="cuda")
+        oob = torch.zeros(1, dtype=torch.int64, device="cuda")
+        L = _lib.load()
+        _lib.check(L.gal_dense_evaluate(self.pot.handle(), self.method, self.ts.data_ptr(), self.coef.data_ptr(),
+                                        self.nsteps.data_ptr(), self.cap, n, orbit.data_ptr(), times.data_ptr(), m,
+                                        out.data_ptr(), oob.data_ptr(), torch.cuda.current_stream().cuda_stream),
+                   "gal_dense_evaluate")
+        if int(oob) != 0:
+            raise ValueError("Time out of bounds.")
+        w = out.t().reshape(*self.batch, T, 6)
+        return w[..., :3], w[..., 3:]
+
+    __call__ = evaluate
+
+
+def integrate_dense(pot: AbstractPotential, y0, t0, t1, cfg: _lib.SolverConfig, *, cap: int | None = None,
+                    batch: tuple | None = None, throw: bool = True) -> PhaseSpaceInterpolation:
+    """Integrate orbits y0 (n, 6) from t0 to t1 keeping a dense interpolant. The
+    step capacity per orbit grows (doubling) until every orbit fits or
+    cfg.max_steps is reached."""
+    torch = _torch()
+    y = _as_cuda(y0, torch.float64).reshape(-1, 6)
+    n = y.shape[0]
+    t0v = _as_cuda(t0, torch.float64).reshape(-1).expand(n).contiguous()
+    t1v = _as_cuda(t1, torch.float64).reshape(-1).expand(n).contiguous()
+    y_soa = y.t().contiguous()
+    L = _lib.load()
+    per = int(L.gal_dense_coef_per_step(cfg.method))
+    if cap is None:
+        if not cfg.adaptive and cfg.dt0 > 0:
+            cap = int(float((t1v - t0v).abs().max()) / cfg.dt0) + 2
+        else:
+            cap = 1024
+    cap = max(1, min(int(cap), int(cfg.max_steps)))
+    while True:
+        ts = torch.empty((n, cap + 1), dtype=torch.float64, device="cuda")
+        coef = torch.empty((n, cap, per), dtype=torch.float64, device="cuda")
+        nsteps = torch.empty(n, dtype=torch.int64, device="cuda")
+        status = torch.empty(n, dtype=torch.int32, device="cuda")
+        _lib.check(L.gal_integrate_dense(pot.handle(), C.byref(cfg), y_soa.data_ptr(), t0v.data_ptr(),
+                                         t1v.data_ptr(), n, cap, ts.data_ptr(), coef.data_ptr(), nsteps.data_ptr(),
+                                         status.data_ptr(), torch.cuda.current_stream().cuda_stream),
+                   "gal_integrate_dense")
+        full = bool(((status == 1) & (nsteps == cap)).any())
+        if full and cap < cfg.max_steps:
+            cap = min(2 * cap, int(cfg.max_steps))
+            continue
+        break
+    if throw:
+        _raise_on_status(status, "dense integration")
+    return PhaseSpaceInterpolation(pot, cfg.method, ts, coef, nsteps, cap, batch if batch is not None else (n,))
+
+
 # ---------------------------------------------------------------- front doors
 def evaluate_orbit(pot: AbstractPotential, w0, t, /, *, integrator: Integrator | None = None, dense: bool = False,
                    throw: bool = True) -> Orbit:
@@ -297,8 +386,6 @@ def evaluate_orbit(pot: AbstractPotential, w0, t, /, *, integrator: Integrator |
     ``t``; without a time, ``w0`` is taken to be at ``t[0]``.
     """
     torch = _torch()
-    if dense:
-        raise NotImplementedError("dense=True (interpolated orbits) is not implemented on the GPU path")
     integrator = integrator or Integrator()
     cfg = integrator.config()
     is_np = not isinstance(t, torch.Tensor) and not isinstance(w0, torch.Tensor)
@@ -316,6 +403,15 @@ def evaluate_orbit(pot: AbstractPotential, w0, t, /, *, integrator: Integrator |
         if throw:
             _raise_on_status(st0, "evaluate_orbit (w0.t -> t[0])")
         y = out0[:, 0, :].t()
+    if dense:
+        # galax returns the saves plus an interpolant over [t[0], t[-1]]
+        interp = integrate_dense(pot, y, t_first.reshape(1), t_last.reshape(1), cfg, batch=tuple(batch),
+                                 throw=throw)
+        q, p = interp.evaluate(ts)
+        orb = Orbit(q=q, p=p, t=ts, interpolant=interp)
+        if is_np:
+            orb = Orbit(q=q.cpu().numpy(), p=p.cpu().numpy(), t=ts.cpu().numpy(), interpolant=interp)
+        return orb
     out, status, steps = integrate(pot, y, t_first.reshape(1), t_last.reshape(1), ts, cfg)
     if throw:
         _raise_on_status(status, "evaluate_orbit")

@@ -184,6 +184,29 @@ GAL_API gal_status gal_integrate_noalloc(const gal_potential* pot, const gal_sol
                                          const double* save_ts, int64_t n_saves, double* out, int32_t* status,
                                          int64_t* steps, const int32_t* order, int64_t n, gal_stream_t stream);
 
+/* Dense output (dense=True): integrate n orbits from t0[i] to t1[i] like
+ * gal_integrate (own controller per orbit) and record, for every accepted step,
+ * what evaluates the orbit anywhere inside it afterwards. Replaces diffrax's
+ * DenseInterpolation as wrapped by galax's PhaseSpaceInterpolation
+ * (src/galax/dynamics/_src/orbit/interp.py:42-145).
+ *   ts     : [n][cap+1] step boundaries (original time), ts[i][0] = t0[i]
+ *   coef   : [n][cap][gal_dense_coef_per_step(method)] per step: Dopri5 the
+ *            quartic of the save path in monomial form (5 x 6), Dopri8 the
+ *            step's start state (6; evaluation takes a partial Dopri8 step)
+ *   nsteps : [n] accepted steps recorded; status [n] (may be NULL): an orbit
+ *            that needs more than cap steps stops with GAL_ORBIT_MAX_STEPS. */
+GAL_API int32_t gal_dense_coef_per_step(int32_t method);
+GAL_API gal_status gal_integrate_dense(const gal_potential* pot, const gal_solver_config* cfg, const double* y0,
+                                       const double* t0, const double* t1, int64_t n, int64_t cap, double* ts,
+                                       double* coef, int64_t* nsteps, int32_t* status, gal_stream_t stream);
+/* Evaluate m queries (orbit[q], t[q]) of a dense result into out[6][m]; a query
+ * outside its orbit's [t0, t1] gives NaN and adds 1 to *out_of_bounds (device
+ * counter; galax raises "Time out of bounds", interp.py:60-64). */
+GAL_API gal_status gal_dense_evaluate(const gal_potential* pot, int32_t method, const double* ts, const double* coef,
+                                      const int64_t* nsteps, int64_t cap, int64_t n, const int64_t* orbit,
+                                      const double* t, int64_t m, double* out, unsigned long long* out_of_bounds,
+                                      gal_stream_t stream);
+
 /* Launch shape used by gal_integrate for one (method, adaptive) pair: threads per
  * block (multiple of 32, <= 256; 0 = 128), blocks per SM (0 = occupancy maximum)
  * and register variant of the Milky Way kernel (0 = at most 168 registers per
@@ -312,8 +335,9 @@ GAL_API gal_status gal_mlp_error(const gal_mlp* mlp, int32_t* code);
  * (builtin/plummer.py:122-133, centred at its origin) is written as
  * Phi_i S(d / r_cut) + Phi_i (1 - S) with S(q) = (1 - q^2)^3 for q < 1, 0
  * beyond: the MLP learns the smooth remainder, the short-range part is summed
- * exactly in FP64 from per-cell neighbour lists built here (device memory
- * allocated here, freed by gal_split_destroy). comps must all be GAL_PLUMMER. */
+ * directly (FP64 offsets and accumulation, each term in FP32: ~1e-7 relative)
+ * from per-cell neighbour lists built here (device memory allocated here,
+ * freed by gal_split_destroy). comps must all be GAL_PLUMMER. */
 typedef struct gal_split gal_split; /* opaque */
 GAL_API gal_status gal_split_create(const gal_component* comps, int32_t n, double G, double r_cut, gal_split** out);
 GAL_API gal_status gal_split_destroy(gal_split* split);

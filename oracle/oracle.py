@@ -315,14 +315,20 @@ def stream_fd_grad(c: np.ndarray, setup, target, params, *, rel_h: float = 1e-5,
     return np.array(out)
 
 
-def plummer_short_range(c: np.ndarray, x, r_cut: float, G: float = G_GALACTIC):
+def plummer_short_range(c: np.ndarray, x, r_cut: float, G: float = G_GALACTIC, *, magnitudes: bool = False):
     """Short-range part sum_i Phi_i S(d_i / r_cut), S(q) = (1 - q^2)^3 for q < 1,
     of Plummer components (direct sum over all of them, no cell lists): returns
-    (phi (n,), grad (n, 3)). Restates the surrogate's split of
+    (phi (n,), grad (n, 3)), and with magnitudes=True also, over the spheres
+    within r_cut, the sums of the untapered scales |Phi_i| and
+    |grad Phi_i| + |Phi_i| 6 |d| / r_cut^2 (the scales of each term's rounding:
+    near the taper's edge t = 1 - q^2 cancels, so S itself carries a large
+    relative but tiny absolute error). Restates the surrogate's split of
     Phi_i = -G m_i / sqrt(d^2 + b_i^2) (galax builtin/plummer.py:122-133)."""
     x = _xyz(x)
     phi = np.zeros(len(x))
     g = np.zeros((len(x), 3))
+    mphi = np.zeros(len(x))
+    mg = np.zeros(len(x))
     for comp in c:
         d = x - np.asarray(comp["origin"])
         d2 = np.sum(d * d, axis=1)
@@ -335,5 +341,9 @@ def plummer_short_range(c: np.ndarray, x, r_cut: float, G: float = G_GALACTIC):
         ph = -Gm / np.sqrt(s2)
         phi += ph * S
         # grad(Phi S) = S grad Phi + Phi grad S, grad S = -6 t^2 d / r_cut^2
-        g += (S * Gm / s2**1.5)[:, None] * d + (ph * (-6.0 * t**2 / r_cut**2))[:, None] * d
-    return phi, g
+        gi = (S * Gm / s2**1.5)[:, None] * d + (ph * (-6.0 * t**2 / r_cut**2))[:, None] * d
+        g += gi
+        dn = np.sqrt(d2)
+        mphi += np.where(inside, np.abs(ph), 0.0)
+        mg += np.where(inside, Gm * dn / s2**1.5 + np.abs(ph) * 6.0 * dn / r_cut**2, 0.0)
+    return (phi, g, mphi, mg) if magnitudes else (phi, g)

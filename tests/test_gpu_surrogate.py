@@ -181,7 +181,8 @@ def _subhalos(n=64, seed=11):
 
 def test_short_range_split_matches_direct_taper_sum(env):
     """The cell-list short-range sum equals the direct sum of the tapered spheres
-    everywhere: next to centres, across cell faces and outside the grid."""
+    everywhere (next to centres, across cell faces, outside the grid) to the
+    FP32 accuracy of its terms: 1e-6 of the untapered near-field scale."""
     gx, S = env
     subs = _subhalos()
     near = S.ShortRange(gx.potential.from_component_array(subs), 3.0)
@@ -192,16 +193,19 @@ def test_short_range_split_matches_direct_taper_sum(env):
         rng.normal(size=(50, 3)) * 200.0,                                               # mostly outside the grid
     ])
     phi, g = near.evaluate(x)
-    phi_r, g_r = O.plummer_short_range(subs, x, 3.0)
+    phi_r, g_r, mphi, mg = O.plummer_short_range(subs, x, 3.0, magnitudes=True)
     phi, g = phi.cpu().numpy(), g.cpu().numpy()
     assert np.count_nonzero(phi_r) > 4000
-    np.testing.assert_allclose(phi, phi_r, rtol=1e-12, atol=1e-18)
-    np.testing.assert_allclose(g, g_r, rtol=1e-11, atol=1e-18)
+    assert np.all(np.abs(phi - phi_r) <= 1e-6 * mphi + 1e-15 * mphi.max())
+    assert np.all(np.linalg.norm(g - g_r, axis=1) <= 1e-6 * mg + 1e-15 * mg.max())
+    far = np.linalg.norm(x, axis=1) > 150.0
+    assert np.all(phi[far] == 0) and np.all(g[far] == 0)
 
 
 def test_surrogate_integrator_adds_the_exact_short_range_field(env):
     """Zero MLP plus the split: the orbit is Dopri5 under Milky Way + short-range
-    sum (checked against a NumPy constant-step Dopri5 on the oracle's fields)."""
+    sum (checked against a NumPy constant-step Dopri5 on the oracle's FP64
+    fields; the short-range terms are FP32, so agreement is to ~1e-8)."""
     gx, S = env
     from galax_gb300 import workloads as W
 
@@ -227,6 +231,6 @@ def test_surrogate_integrator_adds_the_exact_short_range_field(env):
         for i in range(1, len(c)):
             F.append(f(y + sum(a[i][j] * F[j] for j in range(i)) * 1.0))
         y = y + sum(b[i] * F[i] for i in range(len(c))) * 1.0
-    np.testing.assert_allclose(got, y, rtol=1e-10, atol=1e-12)
+    np.testing.assert_allclose(got, y, rtol=1e-7, atol=1e-9)
     plain = S.integrate(mw, mlp, y0, 0.0, 60.0, 1.0).cpu().numpy()
     assert np.abs(plain - got).max() > 1e-8  # the short-range field does act

@@ -23,7 +23,9 @@ from .dynamics import (
 from .potential import (
     CompositePotential,
     HernquistPotential,
+    IsochronePotential,
     KeplerPotential,
+    LogarithmicPotential,
     MilkyWayPotential,
     MiyamotoNagaiPotential,
     NFWPotential,
@@ -34,6 +36,6 @@ from .potential import (
 __all__ = [
     "GalaxGB300Error", "dynamics", "potential", "ConstantStepSize", "Dopri5", "Dopri8", "Integrator", "Orbit",
     "OrbitSolver", "PhaseSpaceCoordinate", "PIDController", "evaluate_orbit", "integrate_orbit",
-    "CompositePotential", "HernquistPotential", "KeplerPotential", "MilkyWayPotential", "MiyamotoNagaiPotential",
+    "CompositePotential", "HernquistPotential", "IsochronePotential", "KeplerPotential", "LogarithmicPotential", "MilkyWayPotential", "MiyamotoNagaiPotential",
     "NFWPotential", "PlummerPotential", "TranslatedPotential",
 ]

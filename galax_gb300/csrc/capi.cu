@@ -48,12 +48,13 @@ static DevComp fold(const gal_component& c, double G) {
   DevComp d{};
   d.kind = c.kind;
   d.centered = (c.origin[0] == 0.0 && c.origin[1] == 0.0 && c.origin[2] == 0.0) ? 1 : 0;
-  d.Gm = G * c.m;
+  const bool log_kind = c.kind == LOGARITHMIC;  // m holds v_c: Phi scales with v_c^2, not G m
+  d.Gm = log_kind ? c.m * c.m : G * c.m;
   d.l1 = c.l1;
   d.l2 = c.l2;
-  d.l2sq = (c.kind == PLUMMER) ? c.l1 * c.l1 : c.l2 * c.l2;
+  d.l2sq = (c.kind == PLUMMER || c.kind == ISOCHRONE || log_kind) ? c.l1 * c.l1 : c.l2 * c.l2;
   d.inv_l1 = (c.kind == NFW) ? 1.0 / c.l1 : 0.0;
-  d.inv_m = (c.m != 0.0) ? 1.0 / c.m : 0.0;
+  d.inv_m = (c.m != 0.0) ? (log_kind ? 2.0 / c.m : 1.0 / c.m) : 0.0;
   d.ox = c.origin[0];
   d.oy = c.origin[1];
   d.oz = c.origin[2];
@@ -90,7 +91,7 @@ static gal_status validate_components(const gal_component* comps, int32_t n) {
   if (n > GAL_MAX_COMPONENTS) return fail(GAL_ERR_TOO_LARGE, "too many components (max GAL_MAX_COMPONENTS)");
   for (int i = 0; i < n; ++i) {
     const gal_component& c = comps[i];
-    if (c.kind < GAL_KEPLER || c.kind > GAL_PLUMMER) return fail(GAL_ERR_UNSUPPORTED, "unsupported component kind");
+    if (c.kind < GAL_KEPLER || c.kind > GAL_LOGARITHMIC) return fail(GAL_ERR_UNSUPPORTED, "unsupported component kind");
     if (c.flags != 0) return fail(GAL_ERR_INVALID_ARGUMENT, "component flags must be 0");
     const double v[6] = {c.m, c.l1, c.l2, c.origin[0], c.origin[1], c.origin[2]};
     for (double x : v)
@@ -100,6 +101,8 @@ static gal_status validate_components(const gal_component* comps, int32_t n) {
     if (c.kind == GAL_MIYAMOTO_NAGAI && (c.l1 < 0.0 || !(c.l2 > 0.0)))
       return fail(GAL_ERR_INVALID_ARGUMENT, "Miyamoto-Nagai needs a >= 0 and b > 0");
     if (c.kind == GAL_PLUMMER && c.l1 < 0.0) return fail(GAL_ERR_INVALID_ARGUMENT, "Plummer r_s must be >= 0");
+    if ((c.kind == GAL_ISOCHRONE || c.kind == GAL_LOGARITHMIC) && !(c.l1 > 0.0))
+      return fail(GAL_ERR_INVALID_ARGUMENT, "isochrone b / logarithmic r_s must be > 0");
   }
   return GAL_OK;
 }

@@ -8,6 +8,8 @@
 //   Miyamoto-Nagai  Phi = -G m / sqrt(R^2 + (sqrt(z^2 + b^2) + a)^2)   builtin/miyamotonagai.py:73-78
 //   NFW             Phi = -G m log1p(r / r_s) / r        builtin/nfw/base.py:326-338
 //   Plummer         Phi = -G m / sqrt(r^2 + b^2)         builtin/plummer.py:122-133
+//   Isochrone       Phi = -G m / (b + sqrt(r^2 + b^2))    builtin/isochrone.py:61-110
+//   Logarithmic     Phi = v_c^2 / 2 log(r_s^2 + r^2)      builtin/logarithmic.py:45-53
 // galax differentiates these with jax.grad (src/galax/potential/_src/base.py:170-179);
 // here the derivatives are written out analytically and arranged for the FP64
 // pipe: reciprocal square roots instead of sqrt + divide, one shared radius for
@@ -19,7 +21,8 @@
 
 namespace gal {
 
-enum Kind : int32_t { KEPLER = 0, HERNQUIST = 1, MIYAMOTO_NAGAI = 2, NFW = 3, PLUMMER = 4 };
+enum Kind : int32_t { KEPLER = 0, HERNQUIST = 1, MIYAMOTO_NAGAI = 2, NFW = 3, PLUMMER = 4, ISOCHRONE = 5,
+                      LOGARITHMIC = 6 };
 
 constexpr double TINY = 2.2250738585072014e-308;  // DBL_MIN, galax's safe_sqrt offset
 
@@ -27,13 +30,13 @@ constexpr double TINY = 2.2250738585072014e-308;  // DBL_MIN, galax's safe_sqrt 
 struct DevComp {
   int32_t kind;
   int32_t centered;  // 1 when origin == 0
-  double Gm;         // G * m
-  double l1;         // a (MN) or r_s
+  double Gm;         // G * m (v_c^2 for the logarithmic potential)
+  double l1;         // a (MN) or r_s / b
   double l2;         // b (MN)
-  double l2sq;       // b^2 (MN) or r_s^2 (Plummer)
+  double l2sq;       // b^2 (MN) or l1^2 (Plummer, isochrone, logarithmic)
   double inv_l1;     // 1 / r_s (NFW)
   double ox, oy, oz;
-  double inv_m;      // 1 / m (parameter derivatives)
+  double inv_m;      // d(log Gm)/dm: 1 / m, or 2 / v_c for the logarithmic potential
 };
 static_assert(sizeof(DevComp) == 80, "DevComp layout");
 
@@ -72,6 +75,16 @@ __device__ __forceinline__ void comp_grad(const DevComp& c, double x, double y, 
       f = c.Gm * (ir * ir) * fma(L, ir, -1.0 / (c.l1 + r));
       break;
     }
+    case ISOCHRONE: {
+      const double s2 = r2 + c.l2sq;
+      const double is = rsqrt(s2);
+      const double d = fma(s2, is, c.l1);
+      f = c.Gm * is / (d * d);
+      break;
+    }
+    case LOGARITHMIC:
+      f = c.Gm / (r2 + c.l2sq);
+      break;
     default: {  // PLUMMER
       const double s2 = r2 + c.l2sq;
       const double is = rsqrt(s2);
@@ -99,6 +112,14 @@ __device__ __forceinline__ double comp_phi(const DevComp& c, double x, double y,
       const double r = sqrt(fma(dx, dx, fma(dy, dy, fma(dz, dz, TINY))));
       const double s = r * c.inv_l1;
       return -c.Gm * c.inv_l1 * log1p(s) / s;
+    }
+    case ISOCHRONE: {
+      const double r = sqrt(fma(dx, dx, fma(dy, dy, fma(dz, dz, TINY))));
+      return -c.Gm / (c.l1 + sqrt(fma(r, r, c.l2sq)));
+    }
+    case LOGARITHMIC: {
+      const double r = sqrt(fma(dx, dx, fma(dy, dy, fma(dz, dz, TINY))));
+      return 0.5 * c.Gm * log(fma(r, r, c.l2sq));
     }
     default: {
       const double r = sqrt(fma(dx, dx, fma(dy, dy, fma(dz, dz, TINY))));
@@ -145,6 +166,18 @@ __device__ __forceinline__ void comp_hessian(const DevComp& c, double x, double 
       const double L = log1p(r * c.inv_l1), q = c.l1 + r;
       g = c.Gm * (L / (r2 * r) - 1.0 / (r2 * q));
       gpr = c.Gm * (3.0 / (r2 * r2 * q) - 3.0 * L / (r2 * r2 * r) + 1.0 / (r2 * r * q * q));
+      break;
+    }
+    case ISOCHRONE: {  // g = G m / ((b + s)^2 s), s = sqrt(r^2 + b^2)
+      const double s2 = r2 + c.l2sq, s = sqrt(s2), d = c.l1 + s;
+      g = c.Gm / (d * d * s);
+      gpr = -g * (2.0 / (d * s) + 1.0 / s2);
+      break;
+    }
+    case LOGARITHMIC: {  // g = v^2 / (r_s^2 + r^2)
+      const double q = r2 + c.l2sq;
+      g = c.Gm / q;
+      gpr = -2.0 * g / q;
       break;
     }
     default: {

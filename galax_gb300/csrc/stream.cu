@@ -723,6 +723,14 @@ __device__ void comp_hessian_t(int kind, const T& Gm, const T& l1, const T& l2, 
     const T Lg = log1p(r / l1), q = l1 + r;
     g = Gm * (Lg / (r2 * r) - 1.0 / (r2 * q));
     gpr = Gm * (3.0 / (r2 * r2 * q) - 3.0 * Lg / (r2 * r2 * r) + 1.0 / (r2 * r * q * q));
+  } else if (kind == ISOCHRONE) {
+    const T s2 = r2 + l1 * l1, s = sqrt(s2), d = l1 + s;
+    g = Gm / (d * d * s);
+    gpr = -g * (2.0 / (d * s) + 1.0 / s2);
+  } else if (kind == LOGARITHMIC) {
+    const T q = r2 + l1 * l1;
+    g = Gm / q;
+    gpr = -2.0 * g / q;
   } else {  // PLUMMER
     const T s2 = r2 + l1 * l1, s = sqrt(s2);
     g = Gm / (s2 * s);

@@ -59,6 +59,20 @@ __device__ __forceinline__ void comp_vjp(const DevComp& c, const double* x, cons
       dl1 = -c.Gm * ir * c.inv_l1 * iq * iq * xv;
       break;
     }
+    case ISOCHRONE: {  // g = G m / ((b + s)^2 s); dg/db = -g (2 (1 + b/s) / (b + s) + b / s^2)
+      const double s2 = r2 + c.l2sq, is = rsqrt(s2), s = s2 * is, d = c.l1 + s, id = 1.0 / d;
+      g = c.Gm * is * id * id;
+      gpr = -g * (2.0 * id * is + is * is);
+      dl1 = -g * fma(2.0 * id, fma(c.l1, is, 1.0), c.l1 * is * is) * xv;
+      break;
+    }
+    case LOGARITHMIC: {  // g = v^2 / (r_s^2 + r^2); dg/dr_s = -2 r_s g / q
+      const double iq = 1.0 / (r2 + c.l2sq);
+      g = c.Gm * iq;
+      gpr = -2.0 * g * iq;
+      dl1 = -2.0 * c.l1 * g * iq * xv;
+      break;
+    }
     default: {  // PLUMMER
       const double is = rsqrt(r2 + c.l2sq), is2 = is * is;
       g = c.Gm * is2 * is;

@@ -173,6 +173,53 @@ class AbstractPotential:
         dphidr = (g * xt / r[..., None]).sum(-1)
         return self._out(torch.sqrt(r * dphidr.abs()), is_np)
 
+    def dpotential_dr(self, x, t=0.0):
+        """rhat . grad Phi (src/galax/potential/_src/register_funcs.py:415-427)."""
+        torch = _torch()
+        is_np = not isinstance(x, torch.Tensor)
+        xt = torch.as_tensor(np.asarray(x, np.float64) if is_np else x).to("cuda", torch.float64)
+        g = self.gradient(xt, t)
+        rhat = xt / torch.linalg.vector_norm(xt, dim=-1, keepdim=True)
+        return self._out((g * rhat).sum(-1), is_np)
+
+    def d2potential_dr2(self, x, t=0.0):
+        """rhat . H . rhat (src/galax/potential/_src/register_funcs.py:444-457)."""
+        torch = _torch()
+        is_np = not isinstance(x, torch.Tensor)
+        xt = torch.as_tensor(np.asarray(x, np.float64) if is_np else x).to("cuda", torch.float64)
+        H = self.hessian(xt, t)
+        rhat = xt / torch.linalg.vector_norm(xt, dim=-1, keepdim=True)
+        return self._out(torch.einsum("...i,...ij,...j->...", rhat, H, rhat), is_np)
+
+    def tidal_tensor(self, x, t=0.0):
+        """H - tr(H) I / 3 (src/galax/potential/_src/register_funcs.py:347-378)."""
+        torch = _torch()
+        is_np = not isinstance(x, torch.Tensor)
+        xt = torch.as_tensor(np.asarray(x, np.float64) if is_np else x).to("cuda", torch.float64)
+        H = self.hessian(xt, t)
+        tr = torch.diagonal(H, dim1=-2, dim2=-1).sum(-1)
+        eye = torch.eye(3, dtype=torch.float64, device="cuda")
+        return self._out(H - eye * (tr / 3.0)[..., None, None], is_np)
+
+    def density(self, x, t=0.0):
+        """Mass density from Poisson's equation, tr(H) / (4 pi G): equal to galax's
+        closed-form densities of these components (base.py:208-228)."""
+        torch = _torch()
+        is_np = not isinstance(x, torch.Tensor)
+        xt = torch.as_tensor(np.asarray(x, np.float64) if is_np else x).to("cuda", torch.float64)
+        H = self.hessian(xt, t)
+        tr = torch.diagonal(H, dim1=-2, dim2=-1).sum(-1)
+        return self._out(tr / (4.0 * np.pi * self.G), is_np)
+
+    def spherical_mass_enclosed(self, x, t=0.0):
+        """r^2 |dPhi/dr| / G (src/galax/potential/_src/register_funcs.py:473-489)."""
+        torch = _torch()
+        is_np = not isinstance(x, torch.Tensor)
+        xt = torch.as_tensor(np.asarray(x, np.float64) if is_np else x).to("cuda", torch.float64)
+        r2 = (xt * xt).sum(-1)
+        dr = self.dpotential_dr(xt, t)
+        return self._out(r2 * dr.abs() / self.G, is_np)
+
     def evaluate_orbit(self, w0, t, *, integrator=None, dense: bool = False):
         from .dynamics import evaluate_orbit
 
@@ -256,6 +303,26 @@ class PlummerPotential(AbstractSinglePotential):
 
     def components(self):
         return [(self.kind, self.m_tot, self.r_s, 0.0, self.origin)]
+
+
+class IsochronePotential(AbstractSinglePotential):
+    """Phi = -G m_tot / (r_s + sqrt(r^2 + r_s^2)) (builtin/isochrone.py:61-110)."""
+
+    kind = _lib.GAL_ISOCHRONE
+    _names = ("m_tot", "r_s")
+
+    def components(self):
+        return [(self.kind, self.m_tot, self.r_s, 0.0, self.origin)]
+
+
+class LogarithmicPotential(AbstractSinglePotential):
+    """Phi = v_c^2 / 2 log(r_s^2 + r^2) (builtin/logarithmic.py:45-53); v_c in kpc/Myr."""
+
+    kind = _lib.GAL_LOGARITHMIC
+    _names = ("v_c", "r_s")
+
+    def components(self):
+        return [(self.kind, self.v_c, self.r_s, 0.0, self.origin)]
 
 
 def _flatten(p: AbstractPotential) -> list[AbstractPotential]:
@@ -363,7 +430,8 @@ def from_component_array(arr: np.ndarray, G: float = G_GALACTIC) -> CompositePot
     """Composite built from a ``gal_component`` record array."""
     cls = {_lib.GAL_KEPLER: KeplerPotential, _lib.GAL_HERNQUIST: HernquistPotential,
            _lib.GAL_MIYAMOTO_NAGAI: MiyamotoNagaiPotential, _lib.GAL_NFW: NFWPotential,
-           _lib.GAL_PLUMMER: PlummerPotential}
+           _lib.GAL_PLUMMER: PlummerPotential, _lib.GAL_ISOCHRONE: IsochronePotential,
+           _lib.GAL_LOGARITHMIC: LogarithmicPotential}
     parts = {}
     for i, rec in enumerate(arr):
         k = int(rec["kind"])

@@ -63,12 +63,16 @@ typedef enum gal_kind {
   GAL_HERNQUIST = 1,      /* Phi = -G m / (r + r_s)        .../builtin/hernquist.py:80-82 */
   GAL_MIYAMOTO_NAGAI = 2, /* Phi = -G m / sqrt(R^2 + (sqrt(z^2+b^2)+a)^2)  .../miyamotonagai.py:73-78 */
   GAL_NFW = 3,            /* Phi = -G m log(1 + r/r_s) / r .../builtin/nfw/base.py:326-338 */
-  GAL_PLUMMER = 4         /* Phi = -G m / sqrt(r^2 + b^2)  .../builtin/plummer.py:122-133 */
+  GAL_PLUMMER = 4,        /* Phi = -G m / sqrt(r^2 + b^2)  .../builtin/plummer.py:122-133 */
+  GAL_ISOCHRONE = 5,      /* Phi = -G m / (b + sqrt(r^2 + b^2))  .../builtin/isochrone.py:61-110 */
+  GAL_LOGARITHMIC = 6     /* Phi = v_c^2 / 2 log(r_s^2 + r^2)    .../builtin/logarithmic.py:45-53 */
 } gal_kind;
 
 /* One component of a composite potential (src/galax/potential/_src/base_multi.py:39-55).
- * m  : m_tot (Kepler, Hernquist, Miyamoto-Nagai, Plummer) or m (NFW)
- * l1 : r_s (Hernquist, NFW, Plummer) or a (Miyamoto-Nagai); unused for Kepler
+ * m  : m_tot (Kepler, Hernquist, Miyamoto-Nagai, Plummer, isochrone), m (NFW) or
+ *      v_c in kpc/Myr (logarithmic)
+ * l1 : r_s (Hernquist, NFW, Plummer, isochrone b, logarithmic) or a (Miyamoto-Nagai);
+ *      unused for Kepler
  * l2 : b (Miyamoto-Nagai); unused otherwise
  * origin : constant translation of the component centre
  *          (src/galax/potential/_src/xfm/translate.py:28-87 with a constant shift). */

@@ -13,6 +13,9 @@
 //       Miyamoto-Nagai                            src/galax/potential/_src/builtin/miyamotonagai.py:73-78
 //       NFW        Phi = -G m log1p(r/r_s) / r    src/galax/potential/_src/builtin/nfw/base.py:326-338
 //       Plummer    Phi = -G m / sqrt(r^2 + b^2)   src/galax/potential/_src/builtin/plummer.py:122-133
+//       Isochrone  Phi = -G m / (b + sqrt(r^2 + b^2))  src/galax/potential/_src/builtin/isochrone.py:61-110
+//       Logarithmic Phi = v_c^2 / 2 log(r_s^2 + r^2)  src/galax/potential/_src/builtin/logarithmic.py:45-53
+//                  (the component's m field holds v_c)
 //     with r = sqrt(x^2+y^2+z^2 + DBL_MIN)        src/galax/potential/_src/utils.py:45-77
 //     composite = sum over components             src/galax/potential/_src/base_multi.py:39-55
 //   * gradient = analytic derivative of Phi (the reference uses jax.grad of the
@@ -85,7 +88,7 @@ using std::log1p;
 // ---------------------------------------------------------------------------
 // Potential components. Same memory layout as the product's gal_component.
 // ---------------------------------------------------------------------------
-enum Kind : int32_t { KEPLER = 0, HERNQUIST = 1, MIYAMOTO_NAGAI = 2, NFW = 3, PLUMMER = 4 };
+enum Kind : int32_t { KEPLER = 0, HERNQUIST = 1, MIYAMOTO_NAGAI = 2, NFW = 3, PLUMMER = 4, ISOCHRONE = 5, LOGARITHMIC = 6 };
 
 struct Comp {
   int32_t kind;
@@ -129,6 +132,14 @@ T comp_potential(const Comp& c, double G, const T* xin) {
       T r = sqrt(rsph2(x) + T(TINY));
       return -Gm / sqrt(r * r + T(c.l1) * T(c.l1));
     }
+    case ISOCHRONE: {
+      T r = sqrt(rsph2(x) + T(TINY));
+      return -Gm / (T(c.l1) + sqrt(r * r + T(c.l1) * T(c.l1)));
+    }
+    case LOGARITHMIC: {
+      T r = sqrt(rsph2(x) + T(TINY));
+      return T(0.5) * T(c.m) * T(c.m) * log(T(c.l1) * T(c.l1) + r * r);
+    }
   }
   return T(0);
 }
@@ -162,6 +173,12 @@ void comp_gradient(const Comp& c, double G, const T* xin, T* g) {
       break;
     }
     case PLUMMER: { T s2 = r2 + T(c.l1) * T(c.l1); f = Gm / (s2 * sqrt(s2)); break; }
+    case ISOCHRONE: {
+      T b = T(c.l1), s = sqrt(r2 + b * b), d = b + s;
+      f = Gm / (d * d * s);
+      break;
+    }
+    case LOGARITHMIC: { f = T(c.m) * T(c.m) / (r2 + T(c.l1) * T(c.l1)); break; }
     default: f = T(0);
   }
   g[0] += f * x[0];
@@ -213,6 +230,18 @@ void comp_hessian(const Comp& c, double G, const double* xin, double* H) {
       gpr = -3.0 * Gm / (s2 * s2 * s);
       break;
     }
+    case ISOCHRONE: {  // g = G m / ((b + s)^2 s), g'/r = -g (2 / ((b + s) s) + 1 / s^2)
+      double b = c.l1, s2 = r2 + b * b, s = std::sqrt(s2), d = b + s;
+      g = Gm / (d * d * s);
+      gpr = -g * (2.0 / (d * s) + 1.0 / s2);
+      break;
+    }
+    case LOGARITHMIC: {  // g = v^2 / (r_s^2 + r^2), g'/r = -2 g / (r_s^2 + r^2)
+      double q = r2 + c.l1 * c.l1;
+      g = c.m * c.m / q;
+      gpr = -2.0 * g / q;
+      break;
+    }
   }
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) H[3 * i + j] += gpr * x[i] * x[j];
@@ -228,7 +257,7 @@ void comp_dgrad_dparams_dot(const Comp& c, double G, const double* xin, const do
   double gr[3] = {0, 0, 0};
   comp_gradient<double>(c, G, xin, gr);
   double gv = gr[0] * v[0] + gr[1] * v[1] + gr[2] * v[2];
-  out[0] += gv / c.m;
+  out[0] += c.kind == LOGARITHMIC ? 2.0 * gv / c.m : gv / c.m;  // grad Phi ~ v_c^2 for the logarithmic
   if (c.kind == MIYAMOTO_NAGAI) {
     double a = c.l1, b = c.l2;
     double zb = std::sqrt(x[2] * x[2] + b * b);
@@ -252,6 +281,16 @@ void comp_dgrad_dparams_dot(const Comp& c, double G, const double* xin, const do
     case HERNQUIST: { double d = r + c.l1; out[1] += -2.0 * Gm / (r * d * d * d) * xv; break; }
     case NFW: { double rs = c.l1, q = rs + r; out[1] += -Gm / (r * rs * q * q) * xv; break; }
     case PLUMMER: { double s2 = r2 + c.l1 * c.l1; out[1] += -3.0 * Gm * c.l1 / (s2 * s2 * std::sqrt(s2)) * xv; break; }
+    case ISOCHRONE: {  // d/db [G m / ((b + s)^2 s)] = -g (b / s^2 + 2 (1 + b / s) / (b + s))
+      double b = c.l1, s2 = r2 + b * b, s = std::sqrt(s2), d = b + s, g = Gm / (d * d * s);
+      out[1] += -g * (b / s2 + 2.0 * (1.0 + b / s) / d) * xv;
+      break;
+    }
+    case LOGARITHMIC: {  // d/dr_s [v^2 / (r_s^2 + r^2)] = -2 r_s v^2 / (r_s^2 + r^2)^2
+      double q = r2 + c.l1 * c.l1;
+      out[1] += -2.0 * c.l1 * c.m * c.m / (q * q) * xv;
+      break;
+    }
     default: break;
   }
 }

@@ -18,7 +18,7 @@ import numpy as np
 
 from . import build_oracle
 
-KEPLER, HERNQUIST, MIYAMOTO_NAGAI, NFW, PLUMMER = range(5)
+KEPLER, HERNQUIST, MIYAMOTO_NAGAI, NFW, PLUMMER, ISOCHRONE, LOGARITHMIC = range(7)
 
 G_GALACTIC = 4.498502151469553e-12  # kpc^3 / (Msun Myr^2), astropy CODATA-2018 G
 

@@ -8,7 +8,7 @@ import numpy as np
 from oracle import oracle as O
 
 KIND = {"kepler": O.KEPLER, "hernquist": O.HERNQUIST, "miyamoto_nagai": O.MIYAMOTO_NAGAI, "nfw": O.NFW,
-        "plummer": O.PLUMMER}
+        "plummer": O.PLUMMER, "isochrone": O.ISOCHRONE, "logarithmic": O.LOGARITHMIC}
 
 
 def golden_comps(p: dict) -> np.ndarray:

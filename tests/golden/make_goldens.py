@@ -27,7 +27,19 @@ POTENTIAL_SPECS = [
     ("nfw", "tests/unit/potential/builtin/test_nfw.py", [40], [44], [56, 57, 58]),
     ("plummer", "tests/unit/potential/builtin/test_plummer.py", [38], [42], [53, 54, 55]),
     ("milky_way", "tests/unit/potential/builtin/test_milkywaypotential.py", [43], [48], [61, 62, 63]),
+    ("isochrone", "tests/unit/potential/builtin/test_isochrone.py", [31], [35], [46, 47, 48]),
+    ("logarithmic", "tests/unit/potential/builtin/test_logarithmic.py", [38], [43], [55, 56, 57]),
 ]
+# density and tidal-tensor goldens of the same fixtures: (density line, tidal tensor lines)
+DERIVED_SPECS = {
+    "hernquist": ([40], [61, 62, 63]),
+    "miyamoto_nagai": ([49], [70, 71, 72]),
+    "nfw": ([50], [104, 105, 106]),
+    "plummer": ([47], [68, 69, 70]),
+    "milky_way": ([54], [76, 77, 78]),
+    "isochrone": ([40], [61, 62, 63]),
+    "logarithmic": ([48], [71, 72, 73]),
+}
 # parameters of each fixture: tests/unit/potential/builtin/test_common.py
 # (m_tot = m = 1e12 Msun, r_s = a = b = 1 kpc); MilkyWay uses its defaults.
 POTENTIAL_PARAMS = {
@@ -36,6 +48,9 @@ POTENTIAL_PARAMS = {
     "nfw": {"kind": "nfw", "m": 1e12, "l1": 1.0, "l2": 0.0},
     "plummer": {"kind": "plummer", "m": 1e12, "l1": 1.0, "l2": 0.0},
     "milky_way": {"kind": "milky_way"},
+    "isochrone": {"kind": "isochrone", "m": 1e12, "l1": 1.0, "l2": 0.0},
+    # v_c = 220 km/s (test_common.py:359-360), stored in m in kpc/Myr
+    "logarithmic": {"kind": "logarithmic", "m": 220 * KMS, "l1": 1.0, "l2": 0.0},
 }
 
 
@@ -46,6 +61,8 @@ def numbers(root: Path, rel: str, lines: list[int]) -> list[float]:
         line = text[ln - 1]
         # drop unit strings such as "kpc2 / Myr2" before scanning numbers
         line = re.sub(r'"[^"]*"', "", line)
+        # digit-group separators (33_365_858.46)
+        line = re.sub(r"(?<=\d)_(?=\d)", "", line)
         # drop identifiers (dtype=float64, CartesianPos3D, ...) so only literals remain
         line = re.sub(r"\b[A-Za-z_][A-Za-z_0-9]*", " ", line)
         out += [float(x) for x in NUM.findall(line)]
@@ -69,6 +86,13 @@ def main(root: Path) -> None:
             "hessian": hess,
             "tol": {"atol": 1e-8, "rtol": 1e-5},
         }
+        ldens, ltidal = DERIVED_SPECS[name]
+        dens = numbers(root, rel, ldens)
+        tidal = numbers(root, rel, ltidal)
+        assert len(dens) == 1 and len(tidal) == 9, (name, dens, tidal)
+        g["potentials"][name]["density"] = dens[0]
+        g["potentials"][name]["tidal_tensor"] = tidal
+        g["potentials"][name]["cite_derived"] = f"{rel}:{ldens[0]},{ltidal[0]}-{ltidal[-1]}"
 
     f = "src/galax/dynamics/_src/orbit/solver.py"
     v220 = 220 * KMS

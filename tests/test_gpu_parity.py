@@ -71,6 +71,8 @@ def _kinds():
         (O.MIYAMOTO_NAGAI, 6.8e10, 3.0, 0.28),
         (O.NFW, 5.4e11, 15.62, 0),
         (O.PLUMMER, 1e8, 0.5, 0, (4.0, 1.0, -2.0)),
+        (O.ISOCHRONE, 2e10, 1.5, 0, (-1.0, 0.5, 0.2)),
+        (O.LOGARITHMIC, 0.2, 2.0, 0),
     ])
 
 
@@ -105,6 +107,24 @@ def test_reference_potential_goldens_on_gpu(gx, goldens):
         np.testing.assert_allclose(pot.potential(x)[0], g["potential"], **g["tol"])
         np.testing.assert_allclose(pot.gradient(x)[0], g["gradient"], **g["tol"])
         np.testing.assert_allclose(pot.hessian(x)[0].ravel(), g["hessian"], **g["tol"])
+        np.testing.assert_allclose(pot.density(x)[0], g["density"], rtol=1e-5, atol=1e-8)
+        np.testing.assert_allclose(pot.tidal_tensor(x)[0].ravel(), g["tidal_tensor"], rtol=1e-5, atol=1e-8)
+
+
+def test_radial_derivatives_circular_velocity_and_enclosed_mass(gx):
+    """dPhi/dr, d2Phi/dr2, v_circ and M(<r) (register_funcs.py:384-489) against
+    the oracle's gradient and Hessian."""
+    mw = gx.MilkyWayPotential()
+    x = _mixed_points(2048, 21)
+    g = O.gradient(O.milky_way(), x)
+    H = O.hessian(O.milky_way(), x)
+    r = np.linalg.norm(x, axis=1)
+    rh = x / r[:, None]
+    dr = np.sum(g * rh, axis=1)
+    np.testing.assert_allclose(mw.dpotential_dr(x), dr, rtol=1e-12, atol=1e-18)
+    np.testing.assert_allclose(mw.d2potential_dr2(x), np.einsum("ni,nij,nj->n", rh, H, rh), rtol=1e-10, atol=1e-16)
+    np.testing.assert_allclose(mw.local_circular_velocity(x), np.sqrt(r * np.abs(dr)), rtol=1e-12)
+    np.testing.assert_allclose(mw.spherical_mass_enclosed(x), r**2 * np.abs(dr) / O.G_GALACTIC, rtol=1e-12)
 
 
 def test_milky_way_kernel_matches_general_table(gx):
@@ -313,14 +333,15 @@ def test_launch_shapes_give_identical_results(gx):
 
 
 # ------------------------------------------------------------------ adjoint
-@pytest.mark.parametrize("which", ["milky_way", "table"])
+@pytest.mark.parametrize("which", ["milky_way", "table", "isochrone_logarithmic"])
 def test_adjoint_matches_oracle(gx, which):
     import torch
 
     from galax_gb300.adjoint import orbit_adjoint
 
-    comps = O.milky_way() if which == "milky_way" else np.concatenate(
-        [O.milky_way(), O.comps([(O.PLUMMER, 1e9, 0.8, 0, (6.0, 2.0, 0.5))])])
+    extra = {"milky_way": [], "table": [(O.PLUMMER, 1e9, 0.8, 0, (6.0, 2.0, 0.5))],
+             "isochrone_logarithmic": [(O.ISOCHRONE, 3e10, 1.2, 0, (1.0, -0.5, 0.3)), (O.LOGARITHMIC, 0.05, 4.0, 0)]}
+    comps = np.concatenate([O.milky_way(), O.comps(extra[which])]) if extra[which] else O.milky_way()
     pot = _pot(gx, comps)
     y0 = _ics(96, 31)
     rng = np.random.default_rng(20)

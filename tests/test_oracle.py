@@ -19,7 +19,8 @@ from tests._helpers import golden_cfg, golden_comps, golden_save_ts
 
 
 # ---------------------------------------------------------------- potentials
-@pytest.mark.parametrize("name", ["hernquist", "miyamoto_nagai", "nfw", "plummer", "milky_way"])
+@pytest.mark.parametrize("name", ["hernquist", "miyamoto_nagai", "nfw", "plummer", "milky_way", "isochrone",
+                                  "logarithmic"])
 def test_potential_goldens(goldens, name):
     g = goldens["potentials"][name]
     c = golden_comps(g["params"])
@@ -29,9 +30,30 @@ def test_potential_goldens(goldens, name):
     np.testing.assert_allclose(O.gradient(c, x)[0], g["gradient"], **tol)
     np.testing.assert_allclose(O.hessian(c, x)[0].ravel(), g["hessian"], **tol)
     if name != "milky_way":
-        # single components match every printed digit, not just the reference's tolerance
-        np.testing.assert_allclose(O.potential(c, x)[0], g["potential"], rtol=0, atol=5e-9)
-        np.testing.assert_allclose(O.gradient(c, x)[0], g["gradient"], rtol=0, atol=5e-9)
+        # single components match every printed digit (within one unit of the
+        # last printed decimal: some goldens are truncated, e.g. the isochrone
+        # potential -0.9231515 of -0.92315155), not just the reference's tolerance
+        def half_ulp(v):
+            digits = repr(float(v)).split("e")[0].split(".")[-1]
+            return 10.0 ** -len(digits) + 1e-15
+
+        np.testing.assert_allclose(O.potential(c, x)[0], g["potential"], rtol=0, atol=half_ulp(g["potential"]))
+        for got, want in zip(O.gradient(c, x)[0], g["gradient"]):
+            assert abs(got - want) <= half_ulp(want), (got, want)
+
+
+@pytest.mark.parametrize("name", ["hernquist", "miyamoto_nagai", "nfw", "plummer", "milky_way", "isochrone",
+                                  "logarithmic"])
+def test_density_and_tidal_tensor_goldens(goldens, name):
+    """galax's density and tidal-tensor goldens follow from the oracle's Hessian:
+    rho = tr(H) / (4 pi G) (Poisson) and T = H - tr(H) I / 3
+    (register_funcs.py:347-378)."""
+    g = goldens["potentials"][name]
+    c = golden_comps(g["params"])
+    H = O.hessian(c, np.array([g["x"]]))[0]
+    tr = np.trace(H)
+    np.testing.assert_allclose(tr / (4 * np.pi * O.G_GALACTIC), g["density"], rtol=1e-5, atol=1e-8)
+    np.testing.assert_allclose((H - np.eye(3) * tr / 3).ravel(), g["tidal_tensor"], rtol=1e-5, atol=1e-8)
 
 
 def test_gradient_is_finite_at_origin():
@@ -52,6 +74,8 @@ def _all_kinds():
         (O.MIYAMOTO_NAGAI, 6.8e10, 3.0, 0.28),
         (O.NFW, 5.4e11, 15.62, 0),
         (O.PLUMMER, 1e8, 0.5, 0, (4.0, 1.0, -2.0)),
+        (O.ISOCHRONE, 2e10, 1.5, 0, (-1.0, 0.5, 0.2)),
+        (O.LOGARITHMIC, 0.2, 2.0, 0),
     ])
 
 

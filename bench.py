@@ -41,7 +41,8 @@ WORKLOADS = {
             "adjoint with checkpoints every 256 steps",
     "surrogate": "learned surrogate: MilkyWayPotential + 512 Plummer subhalos (m log-uniform 1e6-1e8 Msun, "
                  "r_s U(0.1,1) kpc, centres at U(5,50) kpc); MLP 3-256-256-256-256-1 SiLU on the subhalo part "
-                 "beyond a C2 taper of radius 4 kpc (the part inside summed exactly in FP64 from cell lists), "
+                 "beyond a C2 taper of radius 12 kpc (the part inside summed directly from cell lists: FP64 offsets "
+                 "and accumulation, FP32 terms), "
                  "BF16 weights, FP32 accumulation, trained on 4M FP64 samples; Dopri5 dt=1 Myr over 1 Gyr",
     "stream": "stream-like batched gradient: Plummer progenitor (1e5 Msun, b=0.02 kpc) at 20 kpc apocentre in "
               "MilkyWayPotential, integrated back 3 Gyr; 3,000 release times (King tidal radius), 2 particles each "
@@ -786,11 +787,11 @@ def main():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--t1", type=float, default=0.0, help="grad workload: end time in Myr (default 2000)")
     ap.add_argument("--train-points", type=int, default=4_194_304, help="surrogate workload: training samples")
-    ap.add_argument("--train-epochs", type=int, default=200, help="surrogate workload: training epochs")
+    ap.add_argument("--train-epochs", type=int, default=400, help="surrogate workload: training epochs")
     ap.add_argument("--plain-orbits", type=int, default=65_536, help="surrogate workload: orbits for the plain path")
     ap.add_argument("--stream-ckpt", type=int, default=0,
                     help="stream workload: particle checkpoint interval (0 = store every stage, no recompute)")
-    ap.add_argument("--split-radius", type=float, default=4.0,
+    ap.add_argument("--split-radius", type=float, default=12.0,
                     help="surrogate workload: short-range split radius in kpc (0 = the MLP learns the whole sum)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":

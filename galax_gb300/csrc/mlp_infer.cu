@@ -2,7 +2,7 @@
 // gradient (the acceleration) at n positions, one fused kernel.
 //
 // One CTA per SM, persistent over tiles of 128 points, warp-specialised (a
-// weight-copy warp, a tensor-core warp, sixteen epilogue warps). Per tile:
+// weight-copy warp, a tensor-core warp, eight epilogue warps). Per tile:
 //   layer 1 (3 -> 256) on CUDA cores -> h1 (bf16) into the shared-memory
 //   operand tile; then six 128x256x256 products on the tensor cores
 //   (tcgen05.mma kind::f16, bf16 x bf16 -> f32 accumulator in TMEM):
@@ -30,8 +30,7 @@ namespace gal {
 namespace mlp {
 
 constexpr int TILE = 128;
-constexpr int EPI_WARPS = 16;                           // four per TMEM lane quadrant: column quarters
-constexpr int EPI_COLS = 256 / (EPI_WARPS / 4);         // hidden units per epilogue thread
+constexpr int EPI_WARPS = 8;                            // two per TMEM lane quadrant: column halves
 constexpr int NTHREADS = 64 + 32 * EPI_WARPS;           // warp 0 copies weights, warp 1 issues products
 constexpr int STAGES = 4;
 constexpr uint32_t KBLOCK_BYTES = 256 * 128;           // 256 rows x 64 bf16
@@ -44,8 +43,8 @@ constexpr uint32_t SMEM_RING = A_BYTES;
 constexpr uint32_t SMEM_SMALL = SMEM_RING + STAGES * KBLOCK_BYTES;  // 192 KB
 constexpr int SMALL_FLOATS = H * 3 + 5 * H + 1;         // W1, b1, b2, b3, b4, w5, b5
 constexpr uint32_t SMEM_PART = SMEM_SMALL + ((SMALL_FLOATS * 4 + 255) / 256) * 256;
-constexpr uint32_t SMEM_READY = SMEM_PART + TILE * 3 * 4 * 4;  // partials of column quarters 1..3
-constexpr uint32_t SMEM_BAR = SMEM_READY + TILE * 3 * 4;
+constexpr uint32_t SMEM_READY = SMEM_PART + TILE * 4 * 4;
+constexpr uint32_t SMEM_BAR = SMEM_READY + TILE * 4;
 constexpr uint32_t SMEM_TOTAL = SMEM_BAR + 256;
 constexpr uint32_t SMEM_ALLOC = SMEM_TOTAL + 1024;      // room to align the base to 1024
 constexpr uint32_t WAIT_LIMIT = 1u << 24;
@@ -100,8 +99,8 @@ __device__ __forceinline__ void store_row32(uint8_t* tile, int row, int c, const
 // Warp-specialised, persistent over 128-point tiles:
 //   warp 0   : streams the 24 weight K-blocks of every tile through a 4-stage ring (bulk copies)
 //   warp 1   : allocates TMEM and issues the six 128x256x256 products per tile (tcgen05.mma)
-//   warps 2-17: epilogues, one thread per (point, quarter of the 256 hidden units); a warp may
-//              only touch its TMEM lane quadrant (warp id % 4), so each quadrant has four warps
+//   warps 2-9: epilogues, one thread per (point, half of the 256 hidden units); a warp may only
+//              touch its TMEM lane quadrant (warp id % 4), so each quadrant has two warps
 // Synchronisation: full/empty (ring), acc_full (products -> epilogue), op_ready (epilogue ->
 // products: operand tile rewritten and accumulator drained). Every wait is bounded.
 __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
@@ -116,8 +115,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
   const float* sb3 = sb2 + H;
   const float* sb4 = sb3 + H;
   const float* sw5 = sb4 + H;
-  float* part = reinterpret_cast<float*>(smem + SMEM_PART);  // [TILE][3][4]
-  volatile int* ready = reinterpret_cast<volatile int*>(smem + SMEM_READY);  // [TILE][3]
+  float* part = reinterpret_cast<float*>(smem + SMEM_PART);  // [TILE][4]
+  volatile int* ready = reinterpret_cast<volatile int*>(smem + SMEM_READY);  // [TILE]
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + SMEM_BAR);
   uint64_t* full = bars;
   uint64_t* empty = bars + STAGES;
@@ -131,7 +130,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
   const int t = threadIdx.x;
   const int warp = t >> 5, lane = t & 31;
   for (int i = t; i < SMALL_FLOATS; i += NTHREADS) sm[i] = a.small[i];
-  for (int i = t; i < TILE * 3; i += NTHREADS) ready[i] = 0;
+  for (int i = t; i < TILE; i += NTHREADS) ready[i] = 0;
   if (t == 0) {
     abort_s = 0;
     for (int s = 0; s < STAGES; ++s) {
@@ -217,8 +216,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
     const int e = warp - 2;
     const int quad = warp & 3;
     const int row = quad * 32 + lane;
-    const int hh = e >> 2;  // column quarter
-    const int c0 = hh * EPI_COLS;
+    const int hh = e >= 4 ? 1 : 0;
+    const int c0 = hh * 128;
     const uint32_t lane_base = (uint32_t)(quad * 32) << 16;
     int64_t q = 0;
     for (int64_t it = 0; it < my_tiles; ++it) {
@@ -232,7 +231,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
         for (int j = 0; j < 3; ++j) u[j] = (float)(a.x[j * a.n + gi] * a.inv_length);
       }
       // layer 1 on CUDA cores: h1 = silu(W1 u + b1) -> operand tile
-      for (int c = c0; c < c0 + EPI_COLS; c += 32) {
+      for (int c = c0; c < c0 + 128; c += 32) {
         float v[32];
 #pragma unroll
         for (int k = 0; k < 32; ++k) {
@@ -255,13 +254,22 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
           break;
         }
         tc::tc_fence_after();
-        // one 32-column chunk per TMEM round trip (four warps per quadrant hide the latency)
-        for (int cc0 = c0; cc0 < c0 + EPI_COLS; cc0 += 32) {
-          uint32_t acc[32], sp[16];
-          tc::tmem_ld32(tmem + lane_base + (uint32_t)cc0, acc);
-          if (g == 3 || g == 4) tc::tmem_ld16(tmem + lane_base + (uint32_t)((g == 3 ? COL_S3 : COL_S2) + cc0 / 2), sp);
+        // two 32-column chunks per TMEM round trip
+        for (int c = c0; c < c0 + 128; c += 64) {
+          uint32_t acc0[32], acc1[32], sp0[16], sp1[16];
+          tc::tmem_ld32(tmem + lane_base + (uint32_t)c, acc0);
+          tc::tmem_ld32(tmem + lane_base + (uint32_t)(c + 32), acc1);
+          if (g == 3 || g == 4) {
+            const uint32_t cs = (g == 3 ? COL_S3 : COL_S2) + c / 2;
+            tc::tmem_ld16(tmem + lane_base + cs, sp0);
+            tc::tmem_ld16(tmem + lane_base + cs + 16, sp1);
+          }
           tc::tmem_wait_ld();
-          {
+#pragma unroll
+          for (int half = 0; half < 2; ++half) {
+            const uint32_t(&acc)[32] = half ? acc1 : acc0;
+            const uint32_t(&sp)[16] = half ? sp1 : sp0;
+            const int cc0 = c + 32 * half;
             float v[32];
             if (g <= 1) {  // z2 / z3: h = silu(z) -> tile, silu'(z) -> TMEM
               const float* bb = g == 0 ? sb2 : sb3;
@@ -317,42 +325,29 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
         }
       }
       if (!ok) break;
-      // combine the four quarters of each row (bounded hand-off through shared memory)
-      if (hh != 0) {
-        float* pp = part + (row * 3 + hh - 1) * 4;
-        pp[0] = gpart[0];
-        pp[1] = gpart[1];
-        pp[2] = gpart[2];
-        pp[3] = ppart;
+      // combine the two halves of each row (bounded hand-off through shared memory)
+      if (hh == 1) {
+        part[row * 4 + 0] = gpart[0];
+        part[row * 4 + 1] = gpart[1];
+        part[row * 4 + 2] = gpart[2];
+        part[row * 4 + 3] = ppart;
         __threadfence_block();
-        ready[row * 3 + hh - 1] = (int)(it + 1);
+        ready[row] = (int)(it + 1);
       } else {
-        bool got = true;
-        for (int qq = 0; qq < 3 && got; ++qq) {
-          uint32_t spins = 0;
-          while (ready[row * 3 + qq] != (int)(it + 1) && spins < WAIT_LIMIT && !*abort_flag) ++spins;
-          got = ready[row * 3 + qq] == (int)(it + 1);
-        }
-        if (!got) {
+        uint32_t spins = 0;
+        while (ready[row] != (int)(it + 1) && spins < WAIT_LIMIT && !*abort_flag) ++spins;
+        if (ready[row] != (int)(it + 1)) {
           if (!*abort_flag) set_abort(abort_flag, a.err, 5);
           break;
         }
         __threadfence_block();
         if (valid) {
-          float gs[3] = {gpart[0], gpart[1], gpart[2]}, ps = ppart;
-          for (int qq = 0; qq < 3; ++qq) {
-            const float* pp = part + (row * 3 + qq) * 4;
-            gs[0] += pp[0];
-            gs[1] += pp[1];
-            gs[2] += pp[2];
-            ps += pp[3];
-          }
 #pragma unroll
           for (int j = 0; j < 3; ++j) {
-            const double gj = a.gscale * (double)gs[j];
+            const double gj = a.gscale * (double)(gpart[j] + part[row * 4 + j]);
             if (a.grad) a.grad[j * a.n + gi] = a.accumulate ? a.grad[j * a.n + gi] + gj : gj;
           }
-          if (a.phi) a.phi[gi] = a.pscale * (double)(ps + sw5[H]);
+          if (a.phi) a.phi[gi] = a.pscale * (double)(ppart + part[row * 4 + 3] + sw5[H]);
         }
       }
     }

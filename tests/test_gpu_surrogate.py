@@ -182,7 +182,11 @@ def _subhalos(n=64, seed=11):
 def test_short_range_split_matches_direct_taper_sum(env):
     """The cell-list short-range sum equals the direct sum of the tapered spheres
     everywhere (next to centres, across cell faces, outside the grid) to the
-    FP32 accuracy of its terms: 1e-6 of the untapered near-field scale."""
+    FP32 accuracy of its terms, measured against the untapered near-field scale:
+    the centres and the point are held in FP32 relative to a cell corner
+    (~1e-7 kpc absolute), which next to the most compact spheres (b = 0.1 kpc)
+    is up to ~6e-6 of the gradient scale (an FP32 emulation of the kernel on
+    these points gives 5.7e-6), and ~5e-7 for the potential."""
     gx, S = env
     subs = _subhalos()
     near = S.ShortRange(gx.potential.from_component_array(subs), 3.0)
@@ -196,8 +200,8 @@ def test_short_range_split_matches_direct_taper_sum(env):
     phi_r, g_r, mphi, mg = O.plummer_short_range(subs, x, 3.0, magnitudes=True)
     phi, g = phi.cpu().numpy(), g.cpu().numpy()
     assert np.count_nonzero(phi_r) > 4000
-    assert np.all(np.abs(phi - phi_r) <= 1e-6 * mphi + 1e-15 * mphi.max())
-    assert np.all(np.linalg.norm(g - g_r, axis=1) <= 1e-6 * mg + 1e-15 * mg.max())
+    assert np.all(np.abs(phi - phi_r) <= 2e-6 * mphi + 1e-15 * mphi.max())
+    assert np.all(np.linalg.norm(g - g_r, axis=1) <= 2e-5 * mg + 1e-15 * mg.max())
     far = np.linalg.norm(x, axis=1) > 150.0
     assert np.all(phi[far] == 0) and np.all(g[far] == 0)
 

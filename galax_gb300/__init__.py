@@ -6,7 +6,7 @@ sm_103a through the C ABI in ``include/galax_gb300.h``. There is no CPU path:
 without the built library or a CUDA device, calls raise.
 """
 
-from . import dynamics, potential
+from . import dynamics, mockstream, potential
 from ._lib import GalaxGB300Error
 from .dynamics import (
     ConstantStepSize,
@@ -20,6 +20,7 @@ from .dynamics import (
     evaluate_orbit,
     integrate_orbit,
 )
+from .mockstream import Fardal2015DF, FardalStreamDF, MockStreamGenerator, StreamSimulator
 from .potential import (
     CompositePotential,
     HernquistPotential,
@@ -34,8 +35,9 @@ from .potential import (
 )
 
 __all__ = [
-    "GalaxGB300Error", "dynamics", "potential", "ConstantStepSize", "Dopri5", "Dopri8", "Integrator", "Orbit",
-    "OrbitSolver", "PhaseSpaceCoordinate", "PIDController", "evaluate_orbit", "integrate_orbit",
-    "CompositePotential", "HernquistPotential", "IsochronePotential", "KeplerPotential", "LogarithmicPotential", "MilkyWayPotential", "MiyamotoNagaiPotential",
-    "NFWPotential", "PlummerPotential", "TranslatedPotential",
+    "GalaxGB300Error", "dynamics", "mockstream", "potential", "ConstantStepSize", "Dopri5", "Dopri8", "Integrator",
+    "Orbit", "OrbitSolver", "PhaseSpaceCoordinate", "PIDController", "evaluate_orbit", "integrate_orbit",
+    "Fardal2015DF", "FardalStreamDF", "MockStreamGenerator", "StreamSimulator",
+    "CompositePotential", "HernquistPotential", "IsochronePotential", "KeplerPotential", "LogarithmicPotential",
+    "MilkyWayPotential", "MiyamotoNagaiPotential", "NFWPotential", "PlummerPotential", "TranslatedPotential",
 ]

@@ -60,7 +60,14 @@ class StreamConfig(C.Structure):
         ("prog_m", C.c_double),
         ("prog_b", C.c_double),
         ("w_now", C.c_double * 6),
+        ("df", C.c_int32),
+        ("reserved", C.c_int32),
+        ("df_params", C.c_double * 8),
     ]
+
+
+STREAM_DF_OFFSETS = 0
+STREAM_DF_FARDAL2015 = 1
 
 
 class GalaxGB300Error(RuntimeError):
@@ -100,6 +107,8 @@ SIGNATURES = {
                                  C.c_void_p]),
     "gal_stream_grad": (C.c_int, [C.c_void_p, C.POINTER(StreamConfig), _DP, _DP, _DP, _DP, _DP, _DP, _VP,
                                   C.c_size_t, C.c_void_p]),
+    "gal_stream_df_sample": (C.c_int, [C.c_void_p, C.c_int32, _DP, _DP, _DP, _DP, C.c_int64, _DP, _DP, _DP,
+                                       C.c_void_p]),
     "gal_mlp_num_params": (C.c_int64, []),
     "gal_mlp_workspace_size": (C.c_int, [C.c_int64, C.POINTER(C.c_size_t)]),
     "gal_mlp_forward_f32": (C.c_int, [_VP, _VP, C.c_int64, _VP, _VP, C.c_int32, _VP, C.c_size_t, C.c_void_p]),

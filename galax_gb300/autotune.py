@@ -1,10 +1,16 @@
 """Launch-shape autotuner for the orbit-integration kernels.
 
-Times one full call of the integration under each candidate launch shape
+Times full calls of the integration under each candidate launch shape
 (threads per block, blocks per SM, register variant of the Milky Way kernel)
 with CUDA events on the launching stream and installs the fastest through
 ``gal_set_launch``. Results never depend on the launch shape (the device work
 queue hands whole orbits to lanes), so tuning only changes speed.
+
+Batches with very uneven orbit lengths end in a tail where the longest orbits
+run almost alone; their speed then depends on which warps happen to share a
+sub-partition with them, and shapes with many resident warps vary by up to 2x
+from run to run. Each candidate is therefore timed ``repeats`` times and judged
+by its slowest run.
 """
 
 from __future__ import annotations
@@ -29,22 +35,25 @@ def set_launch(method: int, adaptive: bool, block: int, per_sm: int, variant: in
 
 
 def tune(run: Callable[[], object], method: int, adaptive: bool,
-         candidates: Iterable[tuple[int, int, int]] = DEFAULT_CANDIDATES, repeats: int = 1) -> dict:
-    """Run ``run()`` under each candidate, keep the fastest; returns the timings."""
+         candidates: Iterable[tuple[int, int, int]] = DEFAULT_CANDIDATES, repeats: int = 2) -> dict:
+    """Run ``run()`` under each candidate ``repeats`` times, keep the one whose
+    slowest run is fastest; returns those timings."""
     import torch
 
     timings = {}
     for cand in candidates:
         set_launch(method, adaptive, *cand)
-        torch.cuda.synchronize()
         stream = torch.cuda.current_stream()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
+        worst = 0.0
         for _ in range(repeats):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
             run()
-        e1.record(stream)
-        torch.cuda.synchronize()
-        timings[cand] = e0.elapsed_time(e1) / repeats
+            e1.record(stream)
+            torch.cuda.synchronize()
+            worst = max(worst, e0.elapsed_time(e1))
+        timings[cand] = worst
     best = min(timings, key=timings.get)
     set_launch(method, adaptive, *best)
     return {"best": {"block_threads": best[0], "blocks_per_sm": best[1], "variant": best[2]},

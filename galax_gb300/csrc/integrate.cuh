@@ -268,12 +268,31 @@ __device__ __forceinline__ double initial_step(const IntegrateArgs& a, const Pot
   return fmin(100.0 * h0, h1);
 }
 
+// Queue position of a thread's first orbit. The queue is ordered longest work
+// first; handing the first positions out in stripes (lane 0 of warp 0 of every
+// block, then lane 0 of warp 1, ..., then lane 1) puts the longest orbits on
+// different SMs and sub-partitions, so the tail they form at the end of a batch
+// does not queue up on a few FP64 pipes. Later positions are dequeued
+// atomically after the gridDim.x * blockDim.x striped ones.
+__device__ __forceinline__ unsigned long long first_position() {
+  const unsigned long long W = blockDim.x >> 5, w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  return (l * W + w) * gridDim.x + blockIdx.x;
+}
+
 // Returns false when the queue is empty.
 template <class TB, class Pot>
-__device__ __forceinline__ bool start_orbit(const IntegrateArgs& a, const Pot& pot, OrbitState& s) {
+__device__ __forceinline__ bool start_orbit(const IntegrateArgs& a, const Pot& pot, OrbitState& s,
+                                            bool& first) {
   const unsigned long long qlen = a.queue_len ? *a.queue_len : (unsigned long long)a.n;
+  const unsigned long long striped = (unsigned long long)gridDim.x * blockDim.x;
   while (true) {
-    const unsigned long long k = atomicAdd(a.queue, 1ULL);
+    unsigned long long k;
+    if (first) {
+      first = false;
+      k = first_position();
+    } else {
+      k = striped + atomicAdd(a.queue, 1ULL);
+    }
     if (k >= qlen) return false;
     const int64_t o = a.order ? (int64_t)a.order[k] : (int64_t)k;
     s.orbit = o;
@@ -460,7 +479,8 @@ template <class TB, class Pot>
 __device__ void integrate_loop(const IntegrateArgs& a, const Pot& pot) {
   OrbitState s;
   s.orbit = -1;
-  if (!start_orbit<TB>(a, pot, s)) return;
+  bool first = true;
+  if (!start_orbit<TB>(a, pot, s, first)) return;
   double F[TB::S][6];
   while (true) {
     // One RK evaluation per iteration: either the main step from (tau, y) or,
@@ -493,7 +513,7 @@ __device__ void integrate_loop(const IntegrateArgs& a, const Pot& pot) {
       else if (s.tau >= s.tau1) done = true;
       else if (s.nsteps >= a.max_steps) { done = true; st = ORBIT_MAX_STEPS; }
       else if (maybe_park(a, s)) {
-        if (!start_orbit<TB>(a, pot, s)) return;
+        if (!start_orbit<TB>(a, pot, s, first)) return;
         continue;
       }
     } else {
@@ -563,14 +583,14 @@ __device__ void integrate_loop(const IntegrateArgs& a, const Pot& pot) {
         else if (s.tau >= s.tau1) done = true;
         else if (s.nsteps >= a.max_steps) { done = true; st = ORBIT_MAX_STEPS; }
         else if (maybe_park(a, s)) {
-          if (!start_orbit<TB>(a, pot, s)) return;
+          if (!start_orbit<TB>(a, pot, s, first)) return;
           continue;
         }
       }
     }
     if (done) {
       finish_orbit(a, s, st);
-      if (!start_orbit<TB>(a, pot, s)) return;
+      if (!start_orbit<TB>(a, pot, s, first)) return;
     }
   }
 }

@@ -26,9 +26,11 @@
 // feel the particles, this is exactly the particle half of the coupled
 // (particle, progenitor) system, with no interpolation of the progenitor track.
 //
-// Kernels. The progenitor runs on one thread (it is one serial orbit); the
-// release map on one thread per release; the particles on one thread each, one
-// warp per block. The particle adjoint walks the global step grid backwards in
+// Kernels. The progenitor runs on one block whose four warps split each stage
+// (it is one serial orbit; see k_stream_progenitor_team); the
+// release map on one thread per release; the particles 32 to a block of four
+// warps that split each stage the same way (k_stream_particles_team). The
+// particle adjoint walks the global step grid backwards in
 // lockstep across the warp (a lane joins once the walk reaches its release
 // step), so that at every step and stage the warp can sum its lanes'
 // cotangents on the progenitor's stage position (mu) with shuffles and write
@@ -42,6 +44,7 @@
 #include <cuda_runtime.h>
 
 #include <climits>
+#include <cmath>
 #include <vector>
 
 #include "handle.h"
@@ -55,6 +58,8 @@ struct StreamDev {
   double dt, GMp, b2;
   double w_now[6];
   int32_t k_ckpt, ncomp;
+  int32_t df;            // release model (GAL_STREAM_DF_*)
+  double dfp[8];         // its parameters
   double* B;             // [n_rel + 1][6] backwards progenitor track, B[0] = w_now
   double* P;             // [n_rel + 1][6] forwards progenitor track
   double* Q;             // [n_rel][S][3] progenitor stage positions (forwards track)
@@ -62,7 +67,7 @@ struct StreamDev {
   double* Hst;           // [2][n_rel][S][6] host Hessians at both tracks' stage points (xx xy xz yy yz zz)
   double* vst;           // [2][n_rel][S][3] velocity cotangents at those stage points
   double* rt_om;         // [2][n_rel] tidal radius, angular frequency
-  const double* noise;   // [12][n_rel]: xi_lead, eta_lead, xi_trail, eta_trail
+  const double* noise;   // [12][n_rel] or [4][n_rel] normal draws of the release model
   double* ics;           // [6][np]
   double* fin;           // [6][np]
   double* ckpt;          // [nseg][6][np] (gradient with k_ckpt >= 1)
@@ -81,42 +86,49 @@ struct StreamDev {
   double* grad_w_now;    // [6] or NULL
 };
 
-__device__ __forceinline__ MWPot bind_shared(const MWPot& p, const DevComp*) { return p; }
-__device__ __forceinline__ TablePot bind_shared(const TablePot& p, const DevComp* s) { return TablePot{s, p.n}; }
 
 __device__ __forceinline__ void stage_comps(const DevComp* comps, int ncomp, DevComp* s_comps) {
   for (int i = threadIdx.x; i < ncomp; i += blockDim.x) s_comps[i] = comps[i];
   __syncthreads();
 }
 
-// Particle field: host potential plus the progenitor's Plummer sphere at q.
-template <class Host>
-__device__ __forceinline__ void pfield(const Host& host, double GMp, double b2, const double* q, const double* Y,
-                                       double* F) {
-  double gx, gy, gz;
-  host.grad(Y[0], Y[1], Y[2], gx, gy, gz);
+// Particle field: host potential plus the progenitor's Plummer sphere at q,
+// summed in the order of the four-warp particle kernel: partial sum w
+// (w = 0..3) holds components w, w + 4, ... and partial 3 also the Plummer
+// sphere; the partials are added in order w = 0..3. Recomputed particle steps
+// therefore reproduce the forward pass bitwise.
+__device__ __forceinline__ void pfield(const DevComp* comps, int ncomp, double GMp, double b2, const double* q,
+                                       const double* Y, double* F) {
+  double g[4][3];
+#pragma unroll
+  for (int w = 0; w < 4; ++w) {
+    g[w][0] = g[w][1] = g[w][2] = 0.0;
+    for (int c = w; c < ncomp; c += 4) comp_grad(comps[c], Y[0], Y[1], Y[2], g[w][0], g[w][1], g[w][2]);
+  }
   const double d0 = Y[0] - q[0], d1 = Y[1] - q[1], d2 = Y[2] - q[2];
   const double r2 = fma(d0, d0, fma(d1, d1, fma(d2, d2, TINY)));
   const double is = rsqrt(r2 + b2);
   const double f = GMp * (is * is) * is;
+  g[3][0] = fma(f, d0, g[3][0]);
+  g[3][1] = fma(f, d1, g[3][1]);
+  g[3][2] = fma(f, d2, g[3][2]);
   F[0] = Y[3];
   F[1] = Y[4];
   F[2] = Y[5];
-  F[3] = -fma(f, d0, gx);
-  F[4] = -fma(f, d1, gy);
-  F[5] = -fma(f, d2, gz);
+#pragma unroll
+  for (int j = 0; j < 3; ++j) F[3 + j] = -(((g[0][j] + g[1][j]) + g[2][j]) + g[3][j]);
 }
 
-template <class TB, class Host>
-__device__ __forceinline__ void particle_step(const Host& host, double GMp, double b2, const double* Qk, double* y,
-                                              double hs) {
+template <class TB>
+__device__ __forceinline__ void particle_step(const DevComp* comps, int ncomp, double GMp, double b2,
+                                              const double* Qk, double* y, double hs) {
   double F[TB::S][6];
-  pfield(host, GMp, b2, Qk, y, F[0]);
+  pfield(comps, ncomp, GMp, b2, Qk, y, F[0]);
   static_for<1, TB::S>([&](auto i) {
     constexpr int I = decltype(i)::value;
     double Y[6];
     stage_state<TB, I>(y, hs, F, Y);
-    pfield(host, GMp, b2, Qk + 3 * I, Y, F[I]);
+    pfield(comps, ncomp, GMp, b2, Qk + 3 * I, Y, F[I]);
   });
   double y1[6];
   rk_combine<TB>(y, hs, F, y1, nullptr);
@@ -140,157 +152,204 @@ __host__ __device__ __forceinline__ int64_t stage_idx(int64_t k, int i, int e, i
   return k * (k + 1) * S * E + ((int64_t)i * E + e) * (2 * (k + 1)) + p;
 }
 
-// particle step that also records its stage positions
-template <class TB, class Host>
-__device__ __forceinline__ void particle_step_store(const Host& host, double GMp, double b2, const double* Qk,
-                                                    double* y, double hs, double* Ys, int64_t k, int64_t p) {
+// ------------------------------------------------------------------ forward
+// The progenitor on one block of four warps, one per SM sub-partition: a GB300
+// FP64 instruction holds its sub-partition's pipe for ~64 cycles however few
+// lanes are active, so a single orbit advances faster when the independent
+// parts of each stage run on different sub-partitions. Per stage: lanes 0-5 of
+// warp 0 form the stage state (one state component each), then the host
+// components' gradients run in parallel (component c on lane 0 of warp c % 4),
+// then warp 0 sums them in component order into the stage slope. Records the
+// same tracks and stage positions as the single-thread kernel.
+template <class TB>
+__device__ __forceinline__ void team_step(const DevComp* comps, int ncomp, double hs, double* Qk, double* sy,
+                                          double (*sF)[6], double* sY, double (*sg)[3], int warp, int lane) {
   constexpr int S = TB::S;
-  double F[S][6];
-#pragma unroll
-  for (int c = 0; c < 3; ++c) Ys[stage_idx(k, 0, c, p, S, 3)] = y[c];
-  pfield(host, GMp, b2, Qk, y, F[0]);
+  const bool comb = warp == 0 && lane < 6;
+  auto slope = [&](int I) {
+    __syncthreads();  // sY complete
+    if (lane == 0)
+      for (int c = warp; c < ncomp; c += 4) {
+        double gx = 0.0, gy = 0.0, gz = 0.0;
+        comp_grad(comps[c], sY[0], sY[1], sY[2], gx, gy, gz);
+        sg[c][0] = gx;
+        sg[c][1] = gy;
+        sg[c][2] = gz;
+      }
+    __syncthreads();  // sg complete
+    if (comb) {
+      double f;
+      if (lane < 3) {
+        f = sY[lane + 3];
+      } else {
+        double g = 0.0;
+        for (int c = 0; c < ncomp; ++c) g += sg[c][lane - 3];
+        f = -g;
+      }
+      sF[I][lane] = f;
+      if (Qk && lane < 3) Qk[3 * I + lane] = sY[lane];
+    }
+  };
+  if (comb) sY[lane] = sy[lane];
+  slope(0);
   static_for<1, S>([&](auto i) {
     constexpr int I = decltype(i)::value;
-    double Y[6];
-    stage_state<TB, I>(y, hs, F, Y);
-#pragma unroll
-    for (int c = 0; c < 3; ++c) Ys[stage_idx(k, I, c, p, S, 3)] = Y[c];
-    pfield(host, GMp, b2, Qk + 3 * I, Y, F[I]);
-  });
-  double y1[6];
-  rk_combine<TB>(y, hs, F, y1, nullptr);
-#pragma unroll
-  for (int j = 0; j < 6; ++j) y[j] = y1[j];
-}
-
-// ------------------------------------------------------------------ forward
-template <class TB, class Host>
-__global__ void __launch_bounds__(32) k_stream_progenitor(StreamDev a, Host host, const DevComp* comps) {
-  __shared__ DevComp s_comps[kAdjMaxComps];
-  stage_comps(comps, a.ncomp, s_comps);
-  const Host h = bind_shared(host, s_comps);
-  if (threadIdx.x != 0) return;
-  double y[6];
-#pragma unroll
-  for (int j = 0; j < 6; ++j) {
-    y[j] = a.w_now[j];
-    a.B[j] = y[j];
-  }
-  for (int64_t k = 0; k < a.n_rel; ++k) {
-    if (a.Qb) {  // the same step as rk_step_plain, keeping the stage positions
-      double* Qk = a.Qb + k * TB::S * 3;
-      double F[TB::S][6];
-      field(h, y, F[0]);
-      Qk[0] = y[0];
-      Qk[1] = y[1];
-      Qk[2] = y[2];
-      static_for<1, TB::S>([&](auto i) {
-        constexpr int I = decltype(i)::value;
-        double Y[6];
-        stage_state<TB, I>(y, -a.dt, F, Y);
-        Qk[3 * I + 0] = Y[0];
-        Qk[3 * I + 1] = Y[1];
-        Qk[3 * I + 2] = Y[2];
-        field(h, Y, F[I]);
+    __syncthreads();  // sF[I-1] written, sY free for reuse
+    if (comb) {
+      double acc = 0.0;
+      bool first = true;
+      static_for<0, I>([&](auto l) {
+        constexpr int L = decltype(l)::value;
+        constexpr double c = TB::A[I][L];
+        if constexpr (c != 0.0) {
+          acc = first ? c * sF[L][lane] : fma(c, sF[L][lane], acc);
+          first = false;
+        }
       });
-      double y1[6];
-      rk_combine<TB>(y, -a.dt, F, y1, nullptr);
-#pragma unroll
-      for (int j = 0; j < 6; ++j) y[j] = y1[j];
-    } else {
-      rk_step_plain<TB>(h, y, -a.dt);
+      sY[lane] = fma(hs, acc, sy[lane]);
     }
-#pragma unroll
-    for (int j = 0; j < 6; ++j) a.B[(k + 1) * 6 + j] = y[j];
-  }
-#pragma unroll
-  for (int j = 0; j < 6; ++j) a.P[j] = y[j];
-  for (int64_t k = 0; k < a.n_rel; ++k) {
-    double* Qk = a.Q + k * TB::S * 3;
-    double F[TB::S][6];
-    field(h, y, F[0]);
-    Qk[0] = y[0];
-    Qk[1] = y[1];
-    Qk[2] = y[2];
-    static_for<1, TB::S>([&](auto i) {
-      constexpr int I = decltype(i)::value;
-      double Y[6];
-      stage_state<TB, I>(y, a.dt, F, Y);
-      Qk[3 * I + 0] = Y[0];
-      Qk[3 * I + 1] = Y[1];
-      Qk[3 * I + 2] = Y[2];
-      field(h, Y, F[I]);
+    slope(I);
+  });
+  __syncthreads();
+  if (comb) {
+    double acc = 0.0;
+    bool first = true;
+    static_for<0, S>([&](auto l) {
+      constexpr int L = decltype(l)::value;
+      constexpr double c = TB::B[L];
+      if constexpr (c != 0.0) {
+        acc = first ? c * sF[L][lane] : fma(c, sF[L][lane], acc);
+        first = false;
+      }
     });
-    double y1[6];
-    rk_combine<TB>(y, a.dt, F, y1, nullptr);
-#pragma unroll
-    for (int j = 0; j < 6; ++j) {
-      y[j] = y1[j];
-      a.P[(k + 1) * 6 + j] = y[j];
-    }
+    sy[lane] = fma(hs, acc, sy[lane]);
+  }
+  __syncthreads();
+}
+
+template <class TB>
+__global__ void __launch_bounds__(128) k_stream_progenitor_team(StreamDev a, const DevComp* comps) {
+  __shared__ DevComp s_comps[kAdjMaxComps];
+  __shared__ double sy[6], sY[6], sF[TB::S][6], sg[kAdjMaxComps][3];
+  stage_comps(comps, a.ncomp, s_comps);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x < 6) {
+    sy[threadIdx.x] = a.w_now[threadIdx.x];
+    a.B[threadIdx.x] = sy[threadIdx.x];
+  }
+  __syncthreads();
+  for (int64_t k = 0; k < a.n_rel; ++k) {
+    team_step<TB>(s_comps, a.ncomp, -a.dt, a.Qb ? a.Qb + k * TB::S * 3 : nullptr, sy, sF, sY, sg, warp, lane);
+    if (threadIdx.x < 6) a.B[(k + 1) * 6 + threadIdx.x] = sy[threadIdx.x];
+  }
+  if (threadIdx.x < 6) a.P[threadIdx.x] = sy[threadIdx.x];
+  for (int64_t k = 0; k < a.n_rel; ++k) {
+    team_step<TB>(s_comps, a.ncomp, a.dt, a.Q + k * TB::S * 3, sy, sF, sY, sg, warp, lane);
+    if (threadIdx.x < 6) a.P[(k + 1) * 6 + threadIdx.x] = sy[threadIdx.x];
   }
 }
 
-__global__ void __launch_bounds__(128) k_stream_release(StreamDev a, const DevComp* comps) {
-  __shared__ DevComp s_comps[kAdjMaxComps];
-  stage_comps(comps, a.ncomp, s_comps);
-  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (r >= a.n_rel) return;
-  const double* w = a.P + 6 * r;
-  const double x[3] = {w[0], w[1], w[2]}, v[3] = {w[3], w[4], w[5]};
-  const double rr = sqrt(fma(x[0], x[0], fma(x[1], x[1], x[2] * x[2])));
-  const double rh[3] = {x[0] / rr, x[1] / rr, x[2] / rr};
-  const double L[3] = {x[1] * v[2] - x[2] * v[1], x[2] * v[0] - x[0] * v[2], x[0] * v[1] - x[1] * v[0]};
-  const double om = sqrt(fma(L[0], L[0], fma(L[1], L[1], L[2] * L[2]))) / (rr * rr);
-  double H[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-  for (int c = 0; c < a.ncomp; ++c) comp_hessian(s_comps[c], x[0], x[1], x[2], H);
-  double prr = 0.0;
-#pragma unroll
-  for (int i = 0; i < 3; ++i)
-#pragma unroll
-    for (int j = 0; j < 3; ++j) prr = fma(rh[i] * H[3 * i + j], rh[j], prr);
-  const double rt = cbrt(a.GMp / (om * om - prr));
-  a.rt_om[r] = rt;
-  a.rt_om[a.n_rel + r] = om;
-  for (int side = 0; side < 2; ++side) {
-    const double s = side ? 1.0 : -1.0;
-    const int64_t p = 2 * r + side;
-#pragma unroll
-    for (int j = 0; j < 3; ++j) {
-      const double xi = a.noise[(6 * side + j) * a.n_rel + r];
-      const double eta = a.noise[(6 * side + 3 + j) * a.n_rel + r];
-      a.ics[j * a.np + p] = x[j] + s * rt * rh[j] + 0.1 * rt * xi;
-      a.ics[(3 + j) * a.np + p] = v[j] + 0.1 * om * rt * eta;
-    }
-  }
-}
 
-template <class TB, class Host>
-__global__ void __launch_bounds__(32) k_stream_particles(StreamDev a, Host host, const DevComp* comps) {
+// Particles on teams of four warps: block b integrates particles 32b .. 32b+31
+// (one per lane). Warps 0-2 own state components (w, w+3) of their lane's
+// particle and form the stage states; every warp evaluates its share of the
+// host components (component c on warp c % 4) and warp 3 also the progenitor's
+// Plummer sphere; warps 0-2 then sum the four partial gradients in warp order.
+// A lane joins when the global step reaches its release step. Writes the final
+// states and either the checkpoints or the stored stage positions.
+template <class TB>
+__global__ void __launch_bounds__(128) k_stream_particles_team(StreamDev a, const DevComp* comps) {
   __shared__ DevComp s_comps[kAdjMaxComps];
+  __shared__ double sY[3][32], sg[4][3][32];
   stage_comps(comps, a.ncomp, s_comps);
-  const Host h = bind_shared(host, s_comps);
-  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (p >= a.np) return;
-  const int64_t n = a.np, r = p >> 1;
+  constexpr int S = TB::S;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t p = (int64_t)blockIdx.x * 32 + lane;
+  const int64_t n = a.np;
+  const bool valid = p < n;
+  const int64_t rp = valid ? (p >> 1) : LLONG_MAX;
+  const int64_t rmin = ((int64_t)blockIdx.x * 32) >> 1;
+  const bool own = warp < 3;
+  const int j0 = warp, j1 = warp + 3;  // state components owned by warps 0-2
   const int K = a.k_ckpt;
-  double y[6];
-#pragma unroll
-  for (int j = 0; j < 6; ++j) y[j] = a.ics[j * n + p];
-  for (int64_t k = r; k < a.n_rel; ++k) {
-    if (a.Ys) {
-      particle_step_store<TB>(h, a.GMp, a.b2, a.Q + k * TB::S * 3, y, a.dt, a.Ys, k, p);
-      continue;
-    }
-    if (a.ckpt && (k == r || k % K == 0)) {
-      const int64_t g = k / K;
-#pragma unroll
-      for (int j = 0; j < 6; ++j) a.ckpt[(g * 6 + j) * n + p] = y[j];
-    }
-    particle_step<TB>(h, a.GMp, a.b2, a.Q + k * TB::S * 3, y, a.dt);
+  double y0 = 0.0, y1 = 0.0;  // this warp's two components of the lane's particle
+  if (own) {  // lanes past the last particle follow a circular-ish orbit at 8 kpc
+    y0 = valid ? a.ics[j0 * n + p] : (j0 == 0 ? 8.0 : 0.0);
+    y1 = valid ? a.ics[j1 * n + p] : (j1 == 4 ? 0.2 : 0.0);
   }
-#pragma unroll
-  for (int j = 0; j < 6; ++j) a.fin[j * n + p] = y[j];
+  for (int64_t k = rmin; k < a.n_rel; ++k) {
+    const bool act = valid && k >= rp;
+    if (own && act && a.ckpt && (k == rp || k % K == 0)) {
+      const int64_t g = k / K;
+      a.ckpt[(g * 6 + j0) * n + p] = y0;
+      a.ckpt[(g * 6 + j1) * n + p] = y1;
+    }
+    const double* Qk = a.Q + k * S * 3;
+    double F0[S] = {}, F1[S] = {};  // this warp's components of the stage slopes
+    static_for<0, S>([&](auto i) {
+      constexpr int I = decltype(i)::value;
+      double Y0 = y0, Y1 = y1;
+      if (own && I > 0) {
+        double c0 = 0.0, c1 = 0.0;
+        bool first = true;
+        static_for<0, I>([&](auto l) {
+          constexpr int L = decltype(l)::value;
+          constexpr double c = TB::A[I][L];
+          if constexpr (c != 0.0) {
+            c0 = first ? c * F0[L] : fma(c, F0[L], c0);
+            c1 = first ? c * F1[L] : fma(c, F1[L], c1);
+            first = false;
+          }
+        });
+        Y0 = fma(a.dt, c0, y0);
+        Y1 = fma(a.dt, c1, y1);
+      }
+      if (own) {
+        sY[j0][lane] = Y0;
+        if (a.Ys && act) a.Ys[stage_idx(k, I, j0, p, S, 3)] = Y0;
+      }
+      __syncthreads();
+      const double x0 = sY[0][lane], x1 = sY[1][lane], x2 = sY[2][lane];
+      double gx = 0.0, gy = 0.0, gz = 0.0;
+      for (int c = warp; c < a.ncomp; c += 4) comp_grad(s_comps[c], x0, x1, x2, gx, gy, gz);
+      if (warp == 3) {  // the progenitor's Plummer sphere at its stage position
+        const double d0 = x0 - Qk[3 * I], d1 = x1 - Qk[3 * I + 1], d2 = x2 - Qk[3 * I + 2];
+        const double r2 = fma(d0, d0, fma(d1, d1, fma(d2, d2, TINY)));
+        const double is = rsqrt(r2 + a.b2);
+        const double f = a.GMp * (is * is) * is;
+        gx = fma(f, d0, gx);
+        gy = fma(f, d1, gy);
+        gz = fma(f, d2, gz);
+      }
+      sg[warp][0][lane] = gx;
+      sg[warp][1][lane] = gy;
+      sg[warp][2][lane] = gz;
+      __syncthreads();
+      if (own) {
+        F0[I] = Y1;  // dq/dt = p
+        F1[I] = -(((sg[0][j0][lane] + sg[1][j0][lane]) + sg[2][j0][lane]) + sg[3][j0][lane]);
+      }
+    });
+    if (own && act) {
+      double c0 = 0.0, c1 = 0.0;
+      bool first = true;
+      static_for<0, S>([&](auto l) {
+        constexpr int L = decltype(l)::value;
+        constexpr double c = TB::B[L];
+        if constexpr (c != 0.0) {
+          c0 = first ? c * F0[L] : fma(c, F0[L], c0);
+          c1 = first ? c * F1[L] : fma(c, F1[L], c1);
+          first = false;
+        }
+      });
+      y0 = fma(a.dt, c0, y0);
+      y1 = fma(a.dt, c1, y1);
+    }
+  }
+  if (own && valid) {
+    a.fin[j0 * n + p] = y0;
+    a.fin[j1 * n + p] = y1;
+  }
 }
 
 // ------------------------------------------------------------------ adjoint
@@ -300,11 +359,10 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
-template <class TB, class Host>
-__global__ void __launch_bounds__(32) k_stream_particles_adj(StreamDev a, Host host, const DevComp* comps) {
+template <class TB>
+__global__ void __launch_bounds__(32) k_stream_particles_adj(StreamDev a, const DevComp* comps) {
   __shared__ DevComp s_comps[kAdjMaxComps];
   stage_comps(comps, a.ncomp, s_comps);
-  const Host h = bind_shared(host, s_comps);
   constexpr int S = TB::S;
   const int lane = threadIdx.x;
   const int64_t w = blockIdx.x;
@@ -338,7 +396,7 @@ __global__ void __launch_bounds__(32) k_stream_particles_adj(StreamDev a, Host h
       for (int64_t k = ks; k < k1; ++k) {
 #pragma unroll
         for (int j = 0; j < 6; ++j) a.seg[((k - k0) * 6 + j) * n + p] = y[j];
-        if (k + 1 < k1) particle_step<TB>(h, a.GMp, a.b2, a.Q + k * S * 3, y, dt);
+        if (k + 1 < k1) particle_step<TB>(s_comps, ncomp, a.GMp, a.b2, a.Q + k * S * 3, y, dt);
       }
     }
     const int64_t kstop = k0 > rmin ? k0 : rmin;
@@ -351,7 +409,7 @@ __global__ void __launch_bounds__(32) k_stream_particles_adj(StreamDev a, Host h
         for (int j = 0; j < 6; ++j) yk[j] = a.seg[((k - k0) * 6 + j) * n + p];
       }
       double F[S][6], Yq[S][3];
-      pfield(h, a.GMp, a.b2, Qk, yk, F[0]);
+      pfield(s_comps, ncomp, a.GMp, a.b2, Qk, yk, F[0]);
       Yq[0][0] = yk[0];
       Yq[0][1] = yk[1];
       Yq[0][2] = yk[2];
@@ -362,7 +420,7 @@ __global__ void __launch_bounds__(32) k_stream_particles_adj(StreamDev a, Host h
         Yq[I][0] = Y[0];
         Yq[I][1] = Y[1];
         Yq[I][2] = Y[2];
-        pfield(h, a.GMp, a.b2, Qk + 3 * I, Y, F[I]);
+        pfield(s_comps, ncomp, a.GMp, a.b2, Qk + 3 * I, Y, F[I]);
       });
       static_for<0, S>([&](auto i) {
         constexpr int I = decltype(i)::value;
@@ -751,6 +809,135 @@ __device__ T contract_rhat(const T* H, const T* rh) {
   return s;
 }
 
+__device__ __forceinline__ double vsqrt(double x) { return ::sqrt(x); }
+template <int N>
+__device__ __forceinline__ Dual<N> vsqrt(const Dual<N>& x) {
+  return sqrt(x);
+}
+
+// Release conditions of release r's two particles (out[0] leading, s = -1;
+// out[1] trailing, s = +1) from the progenitor point (x, v), its tidal radius
+// rt and angular frequency om; T = double, or dual numbers for the adjoint.
+// noise[q * stride + r] is draw q of release r.
+//   DF_OFFSETS:    x + s rt rhat + 0.1 rt xi,  v + 0.1 om rt eta (12 draws)
+//   DF_FARDAL2015: kr = kr_bar + s_kr n0, kvphi = kr (kvphi_bar + s_kvphi n1),
+//                  kz = kz_bar + s_kz n2, kvz = kvz_bar + s_kvz n3;
+//                  x + rt (s kr rhat + kz zhat),  v + om rt (s kvphi phihat + kvz zhat)
+//                  with zhat along x cross v and phihat along v - (v.rhat) rhat
+//                  (legacy/mockstream/df/fardal15.py:62-94, experimental/df.py:148-177;
+//                  both particles share the four draws).
+template <class T>
+__device__ void release_pair(int df, const double* dfp, const double* noise, int64_t stride, int64_t r, const T* x,
+                             const T* v, const T& rt, const T& om, T (*out)[6]) {
+  const T rr = vsqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+  const T rh[3] = {x[0] / rr, x[1] / rr, x[2] / rr};
+  if (df == GAL_STREAM_DF_FARDAL2015) {
+    const double kr = dfp[0] + dfp[4] * noise[r];
+    const double kvphi = kr * (dfp[1] + dfp[5] * noise[stride + r]);
+    const double kz = dfp[2] + dfp[6] * noise[2 * stride + r];
+    const double kvz = dfp[3] + dfp[7] * noise[3 * stride + r];
+    const T L[3] = {x[1] * v[2] - x[2] * v[1], x[2] * v[0] - x[0] * v[2], x[0] * v[1] - x[1] * v[0]};
+    const T Lm = vsqrt(L[0] * L[0] + L[1] * L[1] + L[2] * L[2]);
+    const T vr = v[0] * rh[0] + v[1] * rh[1] + v[2] * rh[2];
+    const T ph[3] = {v[0] - vr * rh[0], v[1] - vr * rh[1], v[2] - vr * rh[2]};
+    const T pm = vsqrt(ph[0] * ph[0] + ph[1] * ph[1] + ph[2] * ph[2]);
+    const T vc = om * rt;
+    for (int side = 0; side < 2; ++side) {
+      const double s = side ? 1.0 : -1.0;
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const T zh = L[j] / Lm;
+        out[side][j] = x[j] + rt * (s * kr * rh[j] + kz * zh);
+        out[side][3 + j] = v[j] + vc * (s * kvphi * (ph[j] / pm) + kvz * zh);
+      }
+    }
+  } else {
+    for (int side = 0; side < 2; ++side) {
+      const double s = side ? 1.0 : -1.0;
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const double xi = noise[(6 * side + j) * stride + r];
+        const double eta = noise[(6 * side + 3 + j) * stride + r];
+        out[side][j] = x[j] + s * rt * rh[j] + 0.1 * rt * xi;
+        out[side][3 + j] = v[j] + 0.1 * om * rt * eta;
+      }
+    }
+  }
+}
+
+// King (1962) tidal radius r_t = cbrt(GM / (Omega^2 - d2Phi/dr2)) and Omega =
+// |x cross v| / |x|^2 at (x, v) (cluster/radius.py:198-214, register_api.py:82-88).
+__device__ __forceinline__ void king_rt_om(const DevComp* comps, int ncomp, double GM, const double* x,
+                                           const double* v, double& rt, double& om) {
+  const double rr = ::sqrt(fma(x[0], x[0], fma(x[1], x[1], x[2] * x[2])));
+  const double rh[3] = {x[0] / rr, x[1] / rr, x[2] / rr};
+  const double L[3] = {x[1] * v[2] - x[2] * v[1], x[2] * v[0] - x[0] * v[2], x[0] * v[1] - x[1] * v[0]};
+  om = ::sqrt(fma(L[0], L[0], fma(L[1], L[1], L[2] * L[2]))) / (rr * rr);
+  double H[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  for (int c = 0; c < ncomp; ++c) comp_hessian(comps[c], x[0], x[1], x[2], H);
+  double prr = 0.0;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) prr = fma(rh[i] * H[3 * i + j], rh[j], prr);
+  rt = cbrt(GM / (om * om - prr));
+}
+
+// Release map, one thread per release: tidal radius, angular frequency and
+// the two particles' release conditions.
+__global__ void __launch_bounds__(128) k_stream_release(StreamDev a, const DevComp* comps) {
+  __shared__ DevComp s_comps[kAdjMaxComps];
+  stage_comps(comps, a.ncomp, s_comps);
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= a.n_rel) return;
+  const double* w = a.P + 6 * r;
+  double rt, om, out[2][6];
+  king_rt_om(s_comps, a.ncomp, a.GMp, w, w + 3, rt, om);
+  a.rt_om[r] = rt;
+  a.rt_om[a.n_rel + r] = om;
+  release_pair<double>(a.df, a.dfp, a.noise, a.n_rel, r, w, w + 3, rt, om, out);
+  for (int side = 0; side < 2; ++side)
+#pragma unroll
+    for (int e = 0; e < 6; ++e) a.ics[e * a.np + 2 * r + side] = out[side][e];
+}
+
+// Release conditions at n independent progenitor points (SoA [6][n] in and
+// out), one thread per point.
+struct DfSampleArgs {
+  const double* w;
+  const double* mass;
+  const double* noise;
+  double* lead;
+  double* trail;
+  double* rt;
+  int64_t n;
+  double G;
+  int df, ncomp;
+  double dfp[8];
+};
+
+__global__ void __launch_bounds__(128) k_stream_df_sample(DfSampleArgs a, const DevComp* comps) {
+  __shared__ DevComp s_comps[kAdjMaxComps];
+  stage_comps(comps, a.ncomp, s_comps);
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= a.n) return;
+  double x[3], v[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    x[j] = a.w[j * a.n + r];
+    v[j] = a.w[(3 + j) * a.n + r];
+  }
+  double rt, om, out[2][6];
+  king_rt_om(s_comps, a.ncomp, a.G * a.mass[r], x, v, rt, om);
+  if (a.rt) a.rt[r] = rt;
+  release_pair<double>(a.df, a.dfp, a.noise, a.n, r, x, v, rt, om, out);
+#pragma unroll
+  for (int e = 0; e < 6; ++e) {
+    a.lead[e * a.n + r] = out[0][e];
+    a.trail[e * a.n + r] = out[1][e];
+  }
+}
+
 // The release map's transpose: (dL/dx_p, dL/dv_p) of both particles ->
 // dL/dP[r] (nu) and dL/d(component parameters) through d2Phi/dr2.
 __global__ void __launch_bounds__(128) k_stream_release_adj(StreamDev a, const DevComp* comps) {
@@ -763,22 +950,29 @@ __global__ void __launch_bounds__(128) k_stream_release_adj(StreamDev a, const D
   const double rt = a.rt_om[r], om = a.rt_om[a.n_rel + r];
   const double rr = ::sqrt(fma(x[0], x[0], fma(x[1], x[1], x[2] * x[2])));
   const double rh[3] = {x[0] / rr, x[1] / rr, x[2] / rr};
-  double g_rt = 0.0, g_om = 0.0, g_rh[3] = {0, 0, 0}, xb[3] = {0, 0, 0}, vb[3] = {0, 0, 0};
-  for (int side = 0; side < 2; ++side) {
-    const double s = side ? 1.0 : -1.0;
-    const int64_t p = 2 * r + side;
-#pragma unroll
+  // release map by forward mode: tangents x (0-2), v (3-5), r_t (6), Omega (7)
+  double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  {
+    Dual<8> X8[3], V8[3], RT(rt), OM(om), out[2][6];
     for (int j = 0; j < 3; ++j) {
-      const double lx = a.lam_rel[j * a.np + p], lv = a.lam_rel[(3 + j) * a.np + p];
-      const double xi = a.noise[(6 * side + j) * a.n_rel + r];
-      const double eta = a.noise[(6 * side + 3 + j) * a.n_rel + r];
-      g_rt += lx * (s * rh[j] + 0.1 * xi) + lv * (0.1 * om * eta);
-      g_om += lv * (0.1 * rt * eta);
-      g_rh[j] += s * rt * lx;
-      xb[j] += lx;
-      vb[j] += lv;
+      X8[j] = Dual<8>(x[j]);
+      X8[j].d[j] = 1.0;
+      V8[j] = Dual<8>(v[j]);
+      V8[j].d[3 + j] = 1.0;
     }
+    RT.d[6] = 1.0;
+    OM.d[7] = 1.0;
+    release_pair<Dual<8>>(a.df, a.dfp, a.noise, a.n_rel, r, X8, V8, RT, OM, out);
+    for (int side = 0; side < 2; ++side)
+      for (int e = 0; e < 6; ++e) {
+        const double lam = a.lam_rel[e * a.np + 2 * r + side];
+#pragma unroll
+        for (int t = 0; t < 8; ++t) acc[t] = fma(lam, out[side][e].d[t], acc[t]);
+      }
   }
+  double xb[3] = {acc[0], acc[1], acc[2]}, vb[3] = {acc[3], acc[4], acc[5]};
+  const double g_rt = acc[6];
+  double g_om = acc[7];
   // d2Phi/dr2 and its gradient in x (three tangents)
   Dual<3> X[3], RH[3], Hd[9];
   for (int j = 0; j < 3; ++j) {
@@ -816,10 +1010,6 @@ __global__ void __launch_bounds__(128) k_stream_release_adj(StreamDev a, const D
     a.gp_all[(int64_t)(3 * c + 2) * a.ncol + a.np + r] = prr_b * pc.d[1];
   }
   a.gp_all[(int64_t)(3 * a.ncomp) * a.ncol + a.np + r] = 0.0;
-  // rhat = x / |x|
-  const double rg = rh[0] * g_rh[0] + rh[1] * g_rh[1] + rh[2] * g_rh[2];
-#pragma unroll
-  for (int j = 0; j < 3; ++j) xb[j] += (g_rh[j] - rg * rh[j]) / rr;
   // Omega = |x x v| / |x|^2
   const double L[3] = {x[1] * v[2] - x[2] * v[1], x[2] * v[0] - x[0] * v[2], x[0] * v[1] - x[1] * v[0]};
   const double Lm = ::sqrt(L[0] * L[0] + L[1] * L[1] + L[2] * L[2]);
@@ -1023,6 +1213,17 @@ static StreamLayout stream_layout(int ncomp, const gal_stream_config& c, bool gr
   return L;
 }
 
+static gal_status df_validate(int32_t df, const double* p) {
+  if (df != GAL_STREAM_DF_OFFSETS && df != GAL_STREAM_DF_FARDAL2015)
+    return fail(GAL_ERR_INVALID_ARGUMENT, "df must be GAL_STREAM_DF_OFFSETS or GAL_STREAM_DF_FARDAL2015");
+  if (df == GAL_STREAM_DF_FARDAL2015) {
+    if (!p) return fail(GAL_ERR_INVALID_ARGUMENT, "NULL df_params");
+    for (int j = 0; j < 8; ++j)
+      if (!std::isfinite(p[j])) return fail(GAL_ERR_INVALID_ARGUMENT, "df_params must be finite");
+  }
+  return GAL_OK;
+}
+
 static gal_status stream_validate(const gal_potential* pot, const gal_stream_config* c) {
   if (!pot || !c) return fail(GAL_ERR_INVALID_ARGUMENT, "NULL potential or stream configuration");
   if (c->method != 5 && c->method != 8) return fail(GAL_ERR_INVALID_ARGUMENT, "method must be 5 or 8");
@@ -1031,7 +1232,7 @@ static gal_status stream_validate(const gal_potential* pot, const gal_stream_con
   if (c->k_ckpt < 0) return fail(GAL_ERR_INVALID_ARGUMENT, "k_ckpt must be >= 0");
   if (!(c->prog_m > 0.0) || !(c->prog_b > 0.0)) return fail(GAL_ERR_INVALID_ARGUMENT, "progenitor m, b must be > 0");
   if (pot->n > kAdjMaxComps) return fail(GAL_ERR_UNSUPPORTED, "stream host potentials have at most 8 components");
-  return GAL_OK;
+  return df_validate(c->df, c->df_params);
 }
 
 static StreamDev stream_args(const gal_potential* pot, const gal_stream_config* c, const StreamLayout& L, char* ws,
@@ -1048,6 +1249,8 @@ static StreamDev stream_args(const gal_potential* pot, const gal_stream_config* 
   for (int j = 0; j < 6; ++j) a.w_now[j] = c->w_now[j];
   a.k_ckpt = c->k_ckpt;
   a.ncomp = pot->n;
+  a.df = c->df;
+  for (int j = 0; j < 8; ++j) a.dfp[j] = c->df_params[j];
   auto at = [&](size_t o) { return reinterpret_cast<double*>(ws + o); };
   a.B = at(L.B);
   a.P = at(L.P);
@@ -1077,23 +1280,23 @@ static StreamDev stream_args(const gal_potential* pot, const gal_stream_config* 
   return a;
 }
 
-template <class TB, class Host>
-static cudaError_t stream_forward(const StreamDev& a, const Host& host, const DevComp* comps, cudaStream_t s) {
-  k_stream_progenitor<TB, Host><<<1, 32, 0, s>>>(a, host, comps);
+template <class TB>
+static cudaError_t stream_forward(const StreamDev& a, const DevComp* comps, cudaStream_t s) {
+  k_stream_progenitor_team<TB><<<1, 128, 0, s>>>(a, comps);
   k_stream_release<<<(unsigned)((a.n_rel + 127) / 128), 128, 0, s>>>(a, comps);
-  k_stream_particles<TB, Host><<<(unsigned)((a.np + 31) / 32), 32, 0, s>>>(a, host, comps);
+  k_stream_particles_team<TB><<<(unsigned)((a.np + 31) / 32), 128, 0, s>>>(a, comps);
   return cudaGetLastError();
 }
 
-template <class TB, class Host>
-static cudaError_t stream_backward(const StreamDev& a, const Host& host, const DevComp* comps, cudaStream_t s) {
+template <class TB>
+static cudaError_t stream_backward(const StreamDev& a, const DevComp* comps, cudaStream_t s) {
   if (a.Ys) {
     const int64_t nq = a.n_rel * (a.n_rel + 1);
     k_stream_particle_hess<TB><<<(unsigned)((nq + 127) / 128), 128, 0, s>>>(a, comps);
     k_stream_particles_sweep<TB><<<(unsigned)a.nwarps, 32, 0, s>>>(a);
     k_stream_particles_pgrad<TB><<<(unsigned)((nq + 255) / 256), 256, 0, s>>>(a, comps);
   } else {
-    k_stream_particles_adj<TB, Host><<<(unsigned)a.nwarps, 32, 0, s>>>(a, host, comps);
+    k_stream_particles_adj<TB><<<(unsigned)a.nwarps, 32, 0, s>>>(a, comps);
   }
   const int S3 = 3 * TB::S;
   k_stream_mu_reduce<<<(unsigned)((a.n_rel * S3 + 255) / 256), 256, 0, s>>>(a, S3);
@@ -1106,13 +1309,9 @@ static cudaError_t stream_backward(const StreamDev& a, const Host& host, const D
 }
 
 template <class Fn>
-static cudaError_t dispatch(const gal_potential* pot, int method, Fn&& fn) {
-  if (method == 8) {
-    if (pot->is_mw) return fn(Dopri8{}, MWPot{pot->mw});
-    return fn(Dopri8{}, TablePot{pot->d_comps, pot->n});
-  }
-  if (pot->is_mw) return fn(Dopri5{}, MWPot{pot->mw});
-  return fn(Dopri5{}, TablePot{pot->d_comps, pot->n});
+static cudaError_t dispatch(int method, Fn&& fn) {
+  if (method == 8) return fn(Dopri8{});
+  return fn(Dopri5{});
 }
 
 }  // namespace gal
@@ -1120,6 +1319,25 @@ static cudaError_t dispatch(const gal_potential* pot, int method, Fn&& fn) {
 using namespace gal;
 
 extern "C" {
+
+gal_status gal_stream_df_sample(const gal_potential* pot, int32_t df, const double* df_params, const double* prog_w,
+                                const double* prog_mass, const double* noise, int64_t n, double* lead, double* trail,
+                                double* r_tidal, gal_stream_t stream) {
+  if (!pot) return fail(GAL_ERR_INVALID_ARGUMENT, "NULL potential");
+  gal_status st = df_validate(df, df_params);
+  if (st != GAL_OK) return st;
+  if (n < 0) return fail(GAL_ERR_INVALID_ARGUMENT, "n must be >= 0");
+  if (pot->n > kAdjMaxComps) return fail(GAL_ERR_UNSUPPORTED, "stream host potentials have at most 8 components");
+  if (n == 0) return GAL_OK;
+  if (!prog_w || !prog_mass || !noise || !lead || !trail)
+    return fail(GAL_ERR_INVALID_ARGUMENT, "NULL progenitor points, masses, noise or output");
+  DfSampleArgs a{prog_w, prog_mass, noise, lead, trail, r_tidal, n, pot->G, df, pot->n, {}};
+  if (df == GAL_STREAM_DF_FARDAL2015)
+    for (int j = 0; j < 8; ++j) a.dfp[j] = df_params[j];
+  k_stream_df_sample<<<(unsigned)((n + 127) / 128), 128, 0, (cudaStream_t)stream>>>(a, pot->d_comps);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? GAL_OK : cuda_fail(e, "k_stream_df_sample");
+}
 
 gal_status gal_stream_workspace_size(const gal_potential* pot, const gal_stream_config* cfg, int32_t with_grad,
                                      size_t* bytes) {
@@ -1143,9 +1361,7 @@ gal_status gal_stream_run(const gal_potential* pot, const gal_stream_config* cfg
   a.fin = final_states;
   if (ics) a.ics = ics;
   cudaStream_t s = (cudaStream_t)stream;
-  cudaError_t e = dispatch(pot, cfg->method, [&](auto tb, auto host) {
-    return stream_forward<decltype(tb)>(a, host, pot->d_comps, s);
-  });
+  cudaError_t e = dispatch(cfg->method, [&](auto tb) { return stream_forward<decltype(tb)>(a, pot->d_comps, s); });
   if (e != cudaSuccess) return cuda_fail(e, "stream kernels");
   if (prog_track) {
     e = cudaMemcpyAsync(prog_track, a.P, sizeof(double) * 6 * (size_t)(cfg->n_release + 1), cudaMemcpyDeviceToDevice,
@@ -1169,10 +1385,10 @@ gal_status gal_stream_grad(const gal_potential* pot, const gal_stream_config* cf
   a.target = target;
   a.grad_w_now = grad_w_now;
   cudaStream_t s = (cudaStream_t)stream;
-  cudaError_t e = dispatch(pot, cfg->method, [&](auto tb, auto host) {
-    cudaError_t e1 = stream_forward<decltype(tb)>(a, host, pot->d_comps, s);
+  cudaError_t e = dispatch(cfg->method, [&](auto tb) {
+    cudaError_t e1 = stream_forward<decltype(tb)>(a, pot->d_comps, s);
     if (e1 != cudaSuccess) return e1;
-    return stream_backward<decltype(tb)>(a, host, pot->d_comps, s);
+    return stream_backward<decltype(tb)>(a, pot->d_comps, s);
   });
   if (e != cudaSuccess) return cuda_fail(e, "stream gradient kernels");
   double* red = reinterpret_cast<double*>(ws + L.red);

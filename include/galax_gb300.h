@@ -271,7 +271,26 @@ typedef struct gal_stream_config {
   double prog_m;     /* progenitor Plummer mass */
   double prog_b;     /* progenitor Plummer scale radius */
   double w_now[6];   /* progenitor phase-space point at t_now (host values) */
+  int32_t df;        /* release model: GAL_STREAM_DF_OFFSETS or GAL_STREAM_DF_FARDAL2015 */
+  int32_t reserved;  /* 0 */
+  double df_params[8]; /* Fardal 2015: kr_bar, kvphi_bar, kz_bar, kvz_bar, sigma_kr, sigma_kvphi,
+                        * sigma_kz, sigma_kvz (galax's defaults 2, 0.3, 0, 0, 0.5, 0.5, 0.5, 0.5);
+                        * unused by GAL_STREAM_DF_OFFSETS */
 } gal_stream_config;
+
+/* Release models. For release r with progenitor point (x, v), King tidal radius
+ * r_t and angular frequency Omega = |x cross v| / |x|^2, particle 2r (leading,
+ * s = -1) and 2r + 1 (trailing, s = +1) start at
+ *   OFFSETS:     x + s r_t rhat + 0.1 r_t xi,  v + 0.1 Omega r_t eta;
+ *                noise [12][n]: xi_lead, eta_lead, xi_trail, eta_trail (3 each);
+ *   FARDAL2015:  x + r_t (s kr rhat + kz zhat),  v + Omega r_t (s kvphi phihat + kvz zhat),
+ *                kr = kr_bar + sigma_kr n0, kvphi = kr (kvphi_bar + sigma_kvphi n1),
+ *                kz = kz_bar + sigma_kz n2, kvz = kvz_bar + sigma_kvz n3, zhat along x cross v,
+ *                phihat along v - (v . rhat) rhat; noise [4][n]: n0..n3, shared by both
+ *                particles (legacy/mockstream/df/fardal15.py:49-94,
+ *                experimental/df.py:136-177). */
+#define GAL_STREAM_DF_OFFSETS 0
+#define GAL_STREAM_DF_FARDAL2015 1
 
 /* Scratch bytes for gal_stream_run (with_grad = 0) or gal_stream_grad (1). */
 GAL_API gal_status gal_stream_workspace_size(const gal_potential* pot, const gal_stream_config* cfg,
@@ -293,6 +312,21 @@ GAL_API gal_status gal_stream_grad(const gal_potential* pot, const gal_stream_co
                                    const double* target, double* final_states, double* grad_params,
                                    double* grad_w_now, double* loss, void* workspace, size_t workspace_bytes,
                                    gal_stream_t stream);
+
+/* Release conditions sampled from a stream DF (the df and df_params fields of
+ * gal_stream_config) at n progenitor points prog_w [6][n] with progenitor
+ * masses prog_mass [n] (device arrays; df_params is a host array of 8 as in
+ * gal_stream_config, NULL for the offsets model): lead and trail [6][n]
+ * (device), and optionally the King (1962)
+ * tidal radius r_tidal [n] (NULL to skip). Replaces FardalStreamDF._sample
+ * (legacy/mockstream/df/fardal15.py:49-94) and Fardal2015DF.sample
+ * (experimental/df.py:136-177) for a batch of release points, with
+ * tidal_radius (dynamics/_src/cluster/radius.py:198-214) inside; the normal
+ * draws come from the caller (noise [4][n] or [12][n], see the release models
+ * above) instead of a jax PRNG key. */
+GAL_API gal_status gal_stream_df_sample(const gal_potential* pot, int32_t df, const double* df_params,
+                                        const double* prog_w, const double* prog_mass, const double* noise, int64_t n,
+                                        double* lead, double* trail, double* r_tidal, gal_stream_t stream);
 
 /* ------------------------------------------------------------------ learned surrogate */
 /* A small MLP, 3 -> 256 -> 256 -> 256 -> 256 -> 1 with SiLU activations, that

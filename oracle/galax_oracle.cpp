@@ -849,9 +849,12 @@ int orc_adjoint_fixed(const Comp* comps, int ncomp, double G, const OrcSolverCfg
 // from there to t_now in the host potential plus a Plummer sphere (mass
 // prog_m, radius prog_b) centred on the progenitor's stage positions, i.e.
 // exactly the particle half of the coupled particle + progenitor system.
-// Particle ICs (p = 2 r + side, side 0 = leading, 1 = trailing):
-//   x = x_prog + s r_t rhat + 0.1 r_t xi_p,  v = v_prog + 0.1 Omega r_t eta_p,
-//   s = -1 (leading) / +1 (trailing), xi, eta = given standard-normal draws.
+// Particle ICs (p = 2 r + side, side 0 = leading, 1 = trailing; s = -1 / +1)
+// by one of two release models (see release_pair):
+//   df 0 (offsets): x = x_prog + s r_t rhat + 0.1 r_t xi_p,
+//                   v = v_prog + 0.1 Omega r_t eta_p, xi, eta given normal draws;
+//   df 1 (Fardal 2015, legacy/mockstream/df/fardal15.py:62-94 and
+//         experimental/df.py:148-177): four draws per release shared by both arms.
 // ---------------------------------------------------------------------------
 namespace orc {
 
@@ -934,13 +937,89 @@ static void particle_step(const Pot& P, const Tableau& TB, double Gmp, double b2
   for (int j = 0; j < 6; ++j) y[j] = y1[j];
 }
 
+static double norm3(const double* a) { return std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]); }
+
+// King (1962) tidal radius and angular frequency at (x, v) for mass GM.
+static void king_rt_om(const Pot& P, double GM, const double* x, const double* v, double& rt, double& om) {
+  const double rr = norm3(x);
+  const double rh[3] = {x[0] / rr, x[1] / rr, x[2] / rr};
+  const double L[3] = {x[1] * v[2] - x[2] * v[1], x[2] * v[0] - x[0] * v[2], x[0] * v[1] - x[1] * v[0]};
+  om = norm3(L) / (rr * rr);
+  double H[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  for (int c = 0; c < P.n; ++c) comp_hessian(P.comps[c], P.G, x, H);
+  double prr = 0;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) prr += rh[i] * H[3 * i + j] * rh[j];
+  rt = std::cbrt(GM / (om * om - prr));
+}
+
+// Release conditions of one release (out: lead[6], trail[6]). nz: the release's
+// draws, 12 (offsets: xi_lead, eta_lead, xi_trail, eta_trail) or 4 (Fardal: kr,
+// kvphi, kz, kvz). dfp: kr_bar, kvphi_bar, kz_bar, kvz_bar, sigma_kr,
+// sigma_kvphi, sigma_kz, sigma_kvz.
+static void release_pair(int df, const double* dfp, const double* nz, const double* x, const double* v, double rt,
+                         double om, double* lead, double* trail) {
+  const double rr = norm3(x);
+  const double rh[3] = {x[0] / rr, x[1] / rr, x[2] / rr};
+  double* out[2] = {lead, trail};
+  if (df == 1) {
+    // Fardal et al. 2015 as galax samples it: k values from the four draws,
+    // then the leading arm inside (-kr) and the trailing arm outside (+kr).
+    const double kr = dfp[0] + nz[0] * dfp[4];
+    const double kvphi = kr * (dfp[1] + nz[1] * dfp[5]);
+    const double kz = dfp[2] + nz[2] * dfp[6];
+    const double kvz = dfp[3] + nz[3] * dfp[7];
+    const double L[3] = {x[1] * v[2] - x[2] * v[1], x[2] * v[0] - x[0] * v[2], x[0] * v[1] - x[1] * v[0]};
+    const double Lm = norm3(L);
+    const double zh[3] = {L[0] / Lm, L[1] / Lm, L[2] / Lm};
+    const double vr = v[0] * rh[0] + v[1] * rh[1] + v[2] * rh[2];
+    double ph[3] = {v[0] - vr * rh[0], v[1] - vr * rh[1], v[2] - vr * rh[2]};
+    const double pm = norm3(ph);
+    for (int j = 0; j < 3; ++j) ph[j] /= pm;
+    const double vc = om * rt;
+    for (int j = 0; j < 3; ++j) {
+      lead[j] = x[j] - rt * (kr * rh[j] - kz * zh[j]);
+      lead[3 + j] = v[j] - vc * (kvphi * ph[j] - kvz * zh[j]);
+      trail[j] = x[j] + rt * (kr * rh[j] + kz * zh[j]);
+      trail[3 + j] = v[j] + vc * (kvphi * ph[j] + kvz * zh[j]);
+    }
+    return;
+  }
+  for (int side = 0; side < 2; ++side) {
+    const double s = side == 0 ? -1.0 : 1.0;
+    const double* xi = nz + 6 * side;
+    const double* eta = xi + 3;
+    for (int j = 0; j < 3; ++j) {
+      out[side][j] = x[j] + s * rt * rh[j] + 0.1 * rt * xi[j];
+      out[side][3 + j] = v[j] + 0.1 * om * rt * eta[j];
+    }
+  }
+}
+
 }  // namespace orc
 
+// Release conditions at n independent progenitor points w (n x 6) with masses
+// mass (n): lead, trail (n x 6), r_tidal (n). noise: n x 12 or n x 4 (df).
+int orc_stream_df_sample(const Comp* comps, int ncomp, double G, int df, const double* dfp, const double* w,
+                         const double* mass, const double* noise, int64_t n, double* lead, double* trail,
+                         double* r_tidal) {
+  Pot P{comps, ncomp, G};
+  const int nq = df == 1 ? 4 : 12;
+  for (int64_t r = 0; r < n; ++r) {
+    double rt, om;
+    orc::king_rt_om(P, G * mass[r], w + 6 * r, w + 6 * r + 3, rt, om);
+    r_tidal[r] = rt;
+    orc::release_pair(df, dfp, noise + nq * r, w + 6 * r, w + 6 * r + 3, rt, om, lead + 6 * r, trail + 6 * r);
+  }
+  return 0;
+}
+
 // prog_track: (n_rel + 1) x 6 forward states; ics, final_: 2 n_rel x 6;
-// noise: n_rel x 12 (xi_lead, eta_lead, xi_trail, eta_trail); rt_om: n_rel x 2 (r_t, Omega).
+// noise: n_rel x 12 (offsets) or n_rel x 4 (Fardal); rt_om: n_rel x 2 (r_t, Omega).
 int orc_stream_forward(const Comp* comps, int ncomp, double G, int method, double prog_m, double prog_b,
-                       const double* w_now, double t_now, double dt, int64_t n_rel, const double* noise,
-                       double* prog_track, double* rt_om, double* ics, double* final_, int nthreads) {
+                       const double* w_now, double t_now, double dt, int64_t n_rel, int df, const double* dfp,
+                       const double* noise, double* prog_track, double* rt_om, double* ics, double* final_,
+                       int nthreads) {
   Pot P{comps, ncomp, G};
   const Tableau& TB = (method == 5) ? DOPRI5 : DOPRI8;
   const int S = TB.s;
@@ -964,32 +1043,14 @@ int orc_stream_forward(const Comp* comps, int ncomp, double G, int method, doubl
   }
   const double GM = G * prog_m, b2 = prog_b * prog_b;
   // release: King tidal radius and the particle ICs
+  const int nq = df == 1 ? 4 : 12;
   for (int64_t r = 0; r < n_rel; ++r) {
     const double* w = prog_track + 6 * r;
-    const double* x = w;
-    const double* v = w + 3;
-    double rr = std::sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
-    double rh[3] = {x[0] / rr, x[1] / rr, x[2] / rr};
-    double L[3] = {x[1] * v[2] - x[2] * v[1], x[2] * v[0] - x[0] * v[2], x[0] * v[1] - x[1] * v[0]};
-    double om = std::sqrt(L[0] * L[0] + L[1] * L[1] + L[2] * L[2]) / (rr * rr);
-    double H[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    for (int c = 0; c < ncomp; ++c) comp_hessian(comps[c], G, x, H);
-    double prr = 0;
-    for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j) prr += rh[i] * H[3 * i + j] * rh[j];
-    double rt = std::cbrt(GM / (om * om - prr));
+    double rt, om;
+    orc::king_rt_om(P, GM, w, w + 3, rt, om);
     rt_om[2 * r] = rt;
     rt_om[2 * r + 1] = om;
-    for (int side = 0; side < 2; ++side) {
-      const double s = side == 0 ? -1.0 : 1.0;
-      const double* xi = noise + 12 * r + 6 * side;
-      const double* eta = xi + 3;
-      double* o = ics + 6 * (2 * r + side);
-      for (int j = 0; j < 3; ++j) {
-        o[j] = x[j] + s * rt * rh[j] + 0.1 * rt * xi[j];
-        o[3 + j] = v[j] + 0.1 * om * rt * eta[j];
-      }
-    }
+    orc::release_pair(df, dfp, noise + nq * r, w, w + 3, rt, om, ics + 6 * (2 * r), ics + 6 * (2 * r + 1));
   }
 #ifdef _OPENMP
   if (nthreads > 0) omp_set_num_threads(nthreads);

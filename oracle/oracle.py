@@ -277,18 +277,52 @@ def stream_forward(c: np.ndarray, setup, *, method: int = 8, G: float = G_GALACT
         dp = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
         cp = np.ctypeslib.ndpointer(COMP_DTYPE, flags="C_CONTIGUOUS")
         L.orc_stream_forward.argtypes = [cp, C.c_int, C.c_double, C.c_int, C.c_double, C.c_double, dp, C.c_double,
-                                         C.c_double, C.c_int64, dp, dp, dp, dp, dp, C.c_int]
+                                         C.c_double, C.c_int64, C.c_int, dp, dp, dp, dp, dp, dp, C.c_int]
         L.orc_stream_forward.restype = C.c_int
         L._stream_bound = True
     n = int(setup.n_release)
+    df, dfp = _df_of(setup)
     track = np.empty((n + 1, 6))
     rt_om = np.empty((n, 2))
     ics = np.empty((2 * n, 6))
     final = np.empty((2 * n, 6))
+    noise = np.ascontiguousarray(setup.noise, np.float64).reshape(n, 4 if df == STREAM_DF_FARDAL2015 else 12)
     L.orc_stream_forward(np.ascontiguousarray(c), len(c), G, method, float(setup.prog_m), float(setup.prog_b),
-                         np.ascontiguousarray(setup.w_now, np.float64), float(setup.t_now), float(setup.dt), n,
-                         np.ascontiguousarray(setup.noise, np.float64), track, rt_om, ics, final, nthreads)
+                         np.ascontiguousarray(setup.w_now, np.float64), float(setup.t_now), float(setup.dt), n, df,
+                         dfp, noise, track, rt_om, ics, final, nthreads)
     return dict(track=track, rt_om=rt_om, ics=ics, final=final)
+
+
+STREAM_DF_OFFSETS, STREAM_DF_FARDAL2015 = 0, 1
+FARDAL2015_DEFAULTS = (2.0, 0.3, 0.0, 0.0, 0.5, 0.5, 0.5, 0.5)
+
+
+def _df_of(setup):
+    df = int(getattr(setup, "df", STREAM_DF_OFFSETS))
+    p = getattr(setup, "df_params", None)
+    p = FARDAL2015_DEFAULTS if p is None else p
+    return df, np.ascontiguousarray(p, np.float64).reshape(8)
+
+
+def stream_df_sample(c: np.ndarray, w, mass, noise, *, df: int = STREAM_DF_FARDAL2015, df_params=None,
+                     G: float = G_GALACTIC):
+    """Release conditions at n progenitor points w (n, 6) with masses (n,):
+    returns (lead (n, 6), trail (n, 6), r_tidal (n,)) (see orc_stream_df_sample)."""
+    L = lib()
+    if not hasattr(L, "_df_bound"):
+        dp = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+        cp = np.ctypeslib.ndpointer(COMP_DTYPE, flags="C_CONTIGUOUS")
+        L.orc_stream_df_sample.argtypes = [cp, C.c_int, C.c_double, C.c_int, dp, dp, dp, dp, C.c_int64, dp, dp, dp]
+        L.orc_stream_df_sample.restype = C.c_int
+        L._df_bound = True
+    w = np.ascontiguousarray(w, np.float64).reshape(-1, 6)
+    n = len(w)
+    mass = np.ascontiguousarray(np.broadcast_to(np.asarray(mass, np.float64), (n,)))
+    noise = np.ascontiguousarray(noise, np.float64).reshape(n, 4 if df == STREAM_DF_FARDAL2015 else 12)
+    p = np.ascontiguousarray(FARDAL2015_DEFAULTS if df_params is None else df_params, np.float64).reshape(8)
+    lead, trail, rt = np.empty((n, 6)), np.empty((n, 6)), np.empty(n)
+    L.orc_stream_df_sample(np.ascontiguousarray(c), len(c), G, int(df), p, w, mass, noise, n, lead, trail, rt)
+    return lead, trail, rt
 
 
 def stream_loss(c: np.ndarray, setup, target, **kw) -> float:

@@ -172,6 +172,24 @@ def main(root: Path) -> None:
         "expect_q": [q[0:3]], "expect_p": [p[0:3]], "digits": 3,
     }
 
+    g["stream"] = {}
+    f = "src/galax/dynamics/_src/cluster/api.py"
+    rt = numbers(root, f, [198])
+    g["stream"]["king_tidal_radius"] = {
+        "cite": f"{f}:190-198 (King 1962, cluster/radius.py:198-214)",
+        "potential": {"kind": "nfw", "m": 1e12, "l1": 20.0, "l2": 0.0},
+        "x": [8.0, 0.0, 0.0], "v": [8.0, 0.0, 0.0], "mass": 1e4,
+        "r_tidal": rt[0],
+    }
+    f = "src/galax/dynamics/_src/experimental/df.py"
+    s = numbers(root, f, [117, 118, 119, 120])
+    g["stream"]["fardal2015_sample"] = {
+        "cite": f"{f}:106-120 (draws from jax.random.key(0), not reproducible here)",
+        "potential": {"kind": "nfw", "m": 1e12, "l1": 15.0, "l2": 0.0},
+        "x": [15.0, 0.0, 0.0], "v": [0.0, 220.0, 0.0], "mass": 1e5,
+        "x_lead": s[0:3], "v_lead": s[3:6], "x_trail": s[6:9], "v_trail": s[9:12],
+    }
+
     out = Path(__file__).with_name("reference_goldens.json")
     out.write_text(json.dumps(g, indent=1) + "\n")
     print(f"wrote {out}")

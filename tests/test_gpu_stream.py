@@ -2,7 +2,8 @@
 (needs a GB300).
 
 Forward: progenitor track, release conditions and final particle states agree
-with the oracle to 1e-9 relative (constant steps on both sides). Gradient: the
+with the oracle to 1e-9 relative (constant steps on both sides), for both
+release models (Gaussian offsets and galax's Fardal 2015 DF). Gradient: the
 discrete adjoint of the whole pipeline (particles, tidal-radius release map,
 progenitor orbit) against central finite differences of the oracle with one
 Richardson extrapolation, 1e-6 relative for the halo mass and scale radius,
@@ -43,7 +44,7 @@ def _setup(comps, n_release=N_REL, **kw):
 
 def _cfg(S, s, method=8, k_ckpt=64):
     return S.config(n_release=s.n_release, dt=s.dt, w_now=s.w_now, prog_m=s.prog_m, prog_b=s.prog_b,
-                    t_now=s.t_now, method=method, k_ckpt=k_ckpt)
+                    t_now=s.t_now, method=method, k_ckpt=k_ckpt, df=s.df)
 
 
 def _pot(comps):
@@ -69,11 +70,12 @@ HOSTS = {
 }
 
 
+@pytest.mark.parametrize("df", [0, 1])
 @pytest.mark.parametrize("host", list(HOSTS))
 @pytest.mark.parametrize("method", [8, 5])
-def test_forward_matches_oracle(S, host, method):
+def test_forward_matches_oracle(S, host, method, df):
     comps = HOSTS[host]
-    s = _setup(comps)
+    s = _setup(comps, df=df)
     got = S.simulate(_pot(comps), _cfg(S, s, method), s.noise)
     ref = O.stream_forward(comps, s, method=method)
     assert _relmax(got.track, ref["track"]) < 1e-9
@@ -81,11 +83,11 @@ def test_forward_matches_oracle(S, host, method):
     assert _relmax(got.final, ref["final"]) < 1e-9
 
 
-@pytest.mark.parametrize("k_ckpt", [64, 0])
+@pytest.mark.parametrize("k_ckpt,df", [(64, 0), (0, 0), (0, 1)])
 @pytest.mark.parametrize("host", list(HOSTS))
-def test_gradient_matches_finite_differences(S, host, k_ckpt):
+def test_gradient_matches_finite_differences(S, host, k_ckpt, df):
     comps = HOSTS[host]
-    s = _setup(comps)
+    s = _setup(comps, df=df)
     ref = O.stream_forward(comps, s)
     target = ref["final"] + s.pert
     g = S.gradient(_pot(comps), _cfg(S, s, k_ckpt=k_ckpt), s.noise, target)
@@ -108,15 +110,16 @@ def test_gradient_matches_finite_differences(S, host, k_ckpt):
             assert g.grad_params[c][2] == 0.0
 
 
-def test_gradient_with_respect_to_the_present_progenitor_point(S):
+@pytest.mark.parametrize("df", [0, 1])
+def test_gradient_with_respect_to_the_present_progenitor_point(S, df):
     comps = HOSTS["milky_way"]
-    s = _setup(comps, n_release=60)
+    s = _setup(comps, n_release=60, df=df)
     ref = O.stream_forward(comps, s)
     target = ref["final"] + s.pert
     g = S.gradient(_pot(comps), _cfg(S, s), s.noise, target)
     for j in range(6):
         def loss(h):
-            s2 = _setup(comps, n_release=60)
+            s2 = _setup(comps, n_release=60, df=df)
             s2.w_now = s.w_now.copy()
             s2.w_now[j] += h
             return O.stream_loss(comps, s2, target)
@@ -169,6 +172,14 @@ def test_invalid_configurations_raise(S):
         cfg = _cfg(S, s, **bad)
         with pytest.raises(GalaxGB300Error):
             S.simulate(_pot(comps), cfg, s.noise)
+    cfg = _cfg(S, s)
+    cfg.df = 7
+    with pytest.raises(GalaxGB300Error):
+        S.simulate(_pot(comps), cfg, s.noise)
+    cfg.df = 1
+    cfg.df_params[0] = float("nan")
+    with pytest.raises(GalaxGB300Error):
+        S.simulate(_pot(comps), cfg, s.noise[:, :4])
     cfg = _cfg(S, s)
     cfg.dt = 0.0
     with pytest.raises(GalaxGB300Error):

@@ -370,3 +370,99 @@ def test_stream_finite_difference_gradient_converges():
     g1 = O.stream_fd_grad(c, s, target, [(1, "m"), (1, "l1")], rel_h=1e-4)
     g2 = O.stream_fd_grad(c, s, target, [(1, "m"), (1, "l1")], rel_h=1e-5)
     np.testing.assert_allclose(g1, g2, rtol=1e-6)
+
+
+def test_king_tidal_radius_golden(goldens):
+    """galax's tidal_radius doctest (King 1962): the oracle's release map gives
+    the same r_t to the printed digits."""
+    g = goldens["stream"]["king_tidal_radius"]
+    c = golden_comps(g["potential"])
+    w = np.array([g["x"] + g["v"]])
+    _, _, rt = O.stream_df_sample(c, w, g["mass"], np.zeros((1, 4)))
+    assert abs(rt[0] - g["r_tidal"]) <= 1e-8
+
+
+def _fardal_reference(c, w, mass, nz, p=O.FARDAL2015_DEFAULTS):
+    """Fardal 2015 written out as in galax (experimental/df.py:148-177,
+    legacy/mockstream/df/fardal15.py:62-94), with numpy."""
+    x, v = w[:, :3], w[:, 3:]
+    r = np.linalg.norm(x, axis=1, keepdims=True)
+    rh = x / r
+    om = np.linalg.norm(np.cross(x, v), axis=1, keepdims=True) / r**2
+    H = O.hessian(c, x)
+    d2 = np.einsum("ni,nij,nj->n", rh, H, rh)[:, None]
+    rt = np.cbrt(O.G_GALACTIC * mass / (om**2 - d2))
+    vc = om * rt
+    L = np.cross(x, v)
+    zh = L / np.linalg.norm(L, axis=1, keepdims=True)
+    ph = v - np.sum(v * rh, axis=1, keepdims=True) * rh
+    ph = ph / np.linalg.norm(ph, axis=1, keepdims=True)
+    kr = p[0] + nz[:, 0:1] * p[4]
+    kvphi = kr * (p[1] + nz[:, 1:2] * p[5])
+    kz = p[2] + nz[:, 2:3] * p[6]
+    kvz = p[3] + nz[:, 3:4] * p[7]
+    lead = np.concatenate([x - rt * (kr * rh - kz * zh), v - vc * (kvphi * ph - kvz * zh)], axis=1)
+    trail = np.concatenate([x + rt * (kr * rh + kz * zh), v + vc * (kvphi * ph + kvz * zh)], axis=1)
+    return lead, trail, rt[:, 0]
+
+
+def test_fardal2015_sample_matches_the_written_out_formula():
+    c = O.milky_way()
+    rng = np.random.default_rng(3)
+    x = rng.uniform(-30, 30, (50, 3))
+    v = rng.normal(0, 0.2, (50, 3))
+    w = np.concatenate([x, v], axis=1)
+    nz = rng.normal(size=(50, 4))
+    mass = rng.uniform(1e4, 1e6, 50)
+    lead, trail, rt = O.stream_df_sample(c, w, mass, nz)
+    el, et, ert = _fardal_reference(c, w, mass[:, None], nz)
+    np.testing.assert_allclose(rt, ert, rtol=1e-12)
+    np.testing.assert_allclose(lead, el, rtol=1e-12, atol=1e-14)
+    np.testing.assert_allclose(trail, et, rtol=1e-12, atol=1e-14)
+    # other DF parameters
+    p = (1.5, 0.2, 0.1, -0.1, 0.3, 0.4, 0.2, 0.1)
+    lead, trail, _ = O.stream_df_sample(c, w, mass, nz, df_params=p)
+    el, et, _ = _fardal_reference(c, w, mass[:, None], nz, p)
+    np.testing.assert_allclose(lead, el, rtol=1e-12, atol=1e-14)
+    np.testing.assert_allclose(trail, et, rtol=1e-12, atol=1e-14)
+
+
+def test_fardal2015_doctest_structure(goldens):
+    """galax's Fardal2015DF.sample doctest draws from a jax key, so its numbers
+    pin the arm geometry, not the draws: the arms are symmetric about the
+    progenitor along rhat and phihat and shifted together along zhat. Taking
+    the draws the printed values imply, the oracle reproduces every printed
+    digit, and the implied draws are ordinary standard-normal values."""
+    g = goldens["stream"]["fardal2015_sample"]
+    c = golden_comps(g["potential"])
+    x, v = np.array(g["x"]), np.array(g["v"])
+    xl, vl, xt, vt = (np.array(g[k]) for k in ("x_lead", "v_lead", "x_trail", "v_trail"))
+    w = np.concatenate([x, v])[None]
+    _, _, rt = O.stream_df_sample(c, w, g["mass"], np.zeros((1, 4)))
+    rt = rt[0]
+    om = np.linalg.norm(np.cross(x, v)) / np.dot(x, x)
+    rh, zh, ph = x / np.linalg.norm(x), np.array([0, 0, 1.0]), np.array([0, 1.0, 0])
+    kr = np.dot((xt - xl) / 2, rh) / rt
+    kz = np.dot((xt + xl) / 2 - x, zh) / rt
+    kvphi = np.dot((vt - vl) / 2, ph) / (om * rt)
+    kvz = np.dot((vt + vl) / 2 - v, zh) / (om * rt)
+    p = O.FARDAL2015_DEFAULTS
+    nz = np.array([[(kr - p[0]) / p[4], (kvphi / kr - p[1]) / p[5], (kz - p[2]) / p[6], (kvz - p[3]) / p[7]]])
+    assert np.all(np.abs(nz) < 4.0), nz
+    lead, trail, _ = O.stream_df_sample(c, w, g["mass"], nz)
+    for got, want in ((lead[0, :3], xl), (lead[0, 3:], vl), (trail[0, :3], xt), (trail[0, 3:], vt)):
+        np.testing.assert_allclose(got, want, rtol=2e-8, atol=1e-12)
+
+
+def test_stream_forward_with_fardal_release():
+    """The stream pipeline with Fardal release conditions: the ICs are the DF
+    sample at the progenitor track's release points."""
+    from galax_gb300 import workloads as W
+
+    c = O.milky_way()
+    s = W.stream_setup(lambda x: O.gradient(c, x), n_release=30, df=1)
+    out = O.stream_forward(c, s)
+    lead, trail, rt = O.stream_df_sample(c, out["track"][:-1], s.prog_m, s.noise)
+    np.testing.assert_array_equal(out["ics"][0::2], lead)
+    np.testing.assert_array_equal(out["ics"][1::2], trail)
+    np.testing.assert_array_equal(out["rt_om"][:, 0], rt)

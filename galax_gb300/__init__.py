@@ -20,7 +20,7 @@ from .dynamics import (
     evaluate_orbit,
     integrate_orbit,
 )
-from .mockstream import Fardal2015DF, FardalStreamDF, MockStreamGenerator, StreamSimulator
+from .mockstream import ChenStreamDF, Fardal2015DF, FardalStreamDF, MockStreamGenerator, StreamSimulator
 from .potential import (
     CompositePotential,
     HernquistPotential,
@@ -37,7 +37,7 @@ from .potential import (
 __all__ = [
     "GalaxGB300Error", "dynamics", "mockstream", "potential", "ConstantStepSize", "Dopri5", "Dopri8", "Integrator",
     "Orbit", "OrbitSolver", "PhaseSpaceCoordinate", "PIDController", "evaluate_orbit", "integrate_orbit",
-    "Fardal2015DF", "FardalStreamDF", "MockStreamGenerator", "StreamSimulator",
+    "ChenStreamDF", "Fardal2015DF", "FardalStreamDF", "MockStreamGenerator", "StreamSimulator",
     "CompositePotential", "HernquistPotential", "IsochronePotential", "KeplerPotential", "LogarithmicPotential",
     "MilkyWayPotential", "MiyamotoNagaiPotential", "NFWPotential", "PlummerPotential", "TranslatedPotential",
 ]

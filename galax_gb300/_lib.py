@@ -68,6 +68,7 @@ class StreamConfig(C.Structure):
 
 STREAM_DF_OFFSETS = 0
 STREAM_DF_FARDAL2015 = 1
+STREAM_DF_CHEN2024 = 2
 
 
 class GalaxGB300Error(RuntimeError):

@@ -810,6 +810,7 @@ __device__ T contract_rhat(const T* H, const T* rh) {
 }
 
 __device__ __forceinline__ double vsqrt(double x) { return ::sqrt(x); }
+constexpr double kChenRho = 0.71414284285428499980;  // sqrt(1 - 0.7^2)
 template <int N>
 __device__ __forceinline__ Dual<N> vsqrt(const Dual<N>& x) {
   return sqrt(x);
@@ -826,11 +827,53 @@ __device__ __forceinline__ Dual<N> vsqrt(const Dual<N>& x) {
 //                  with zhat along x cross v and phihat along v - (v.rhat) rhat
 //                  (legacy/mockstream/df/fardal15.py:62-94, experimental/df.py:148-177;
 //                  both particles share the four draws).
+//   DF_CHEN2024:   posvel = mean + A z from six standard-normal draws z, A the
+//                  lower-triangular factor of galax's covariance (only posvel_0
+//                  and posvel_4 are correlated, coefficient -0.7; posvel_3 has
+//                  no spread), then Dr = posvel_0 rt, Dv = posvel_3
+//                  sqrt(2 GM / Dr), angles phi, theta, alpha, beta = posvel_1,2,4,5
+//                  in degrees; x +/- Dr (ct cp xhat + ct sp yhat) + Dr st zhat,
+//                  v +/- Dv (cb ca xhat + cb sa yhat) + Dv sb zhat (+ trailing,
+//                  - leading; legacy/mockstream/df/chen24.py:21-137).
 template <class T>
 __device__ void release_pair(int df, const double* dfp, const double* noise, int64_t stride, int64_t r, const T* x,
-                             const T* v, const T& rt, const T& om, T (*out)[6]) {
+                             const T* v, const T& rt, const T& om, double GM, T (*out)[6]) {
   const T rr = vsqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
   const T rh[3] = {x[0] / rr, x[1] / rr, x[2] / rr};
+  if (df == GAL_STREAM_DF_CHEN2024) {
+    double z[6];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) z[q] = noise[q * stride + r];
+    const double pv0 = 1.6 + 0.35 * z[0];
+    const double pv1 = -30.0 + 23.0 * z[1];
+    const double pv2 = 12.0 * z[2];
+    const double pv3 = 1.0;
+    const double pv4 = 20.0 + 20.0 * fma(-0.7, z[0], kChenRho * z[4]);
+    const double pv5 = 22.0 * z[5];
+    constexpr double DEG = 0.017453292519943295;
+    double sp, cp, st, ct, sa, ca, sb, cb;
+    sincos(pv1 * DEG, &sp, &cp);
+    sincos(pv2 * DEG, &st, &ct);
+    sincos(pv4 * DEG, &sa, &ca);
+    sincos(pv5 * DEG, &sb, &cb);
+    const T L[3] = {x[1] * v[2] - x[2] * v[1], x[2] * v[0] - x[0] * v[2], x[0] * v[1] - x[1] * v[0]};
+    const T Lm = vsqrt(L[0] * L[0] + L[1] * L[1] + L[2] * L[2]);
+    const T vr = v[0] * rh[0] + v[1] * rh[1] + v[2] * rh[2];
+    const T ph[3] = {v[0] - vr * rh[0], v[1] - vr * rh[1], v[2] - vr * rh[2]};
+    const T pm = vsqrt(ph[0] * ph[0] + ph[1] * ph[1] + ph[2] * ph[2]);
+    const T Dr = pv0 * rt;
+    const T Dv = pv3 * vsqrt((2.0 * GM) / Dr);
+    for (int side = 0; side < 2; ++side) {
+      const double s = side ? 1.0 : -1.0;
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const T zh = L[j] / Lm, yh = ph[j] / pm;
+        out[side][j] = x[j] + s * (Dr * (ct * cp) * rh[j] + Dr * (ct * sp) * yh) + Dr * st * zh;
+        out[side][3 + j] = v[j] + s * (Dv * (cb * ca) * rh[j] + Dv * (cb * sa) * yh) + Dv * sb * zh;
+      }
+    }
+    return;
+  }
   if (df == GAL_STREAM_DF_FARDAL2015) {
     const double kr = dfp[0] + dfp[4] * noise[r];
     const double kvphi = kr * (dfp[1] + dfp[5] * noise[stride + r]);
@@ -895,7 +938,7 @@ __global__ void __launch_bounds__(128) k_stream_release(StreamDev a, const DevCo
   king_rt_om(s_comps, a.ncomp, a.GMp, w, w + 3, rt, om);
   a.rt_om[r] = rt;
   a.rt_om[a.n_rel + r] = om;
-  release_pair<double>(a.df, a.dfp, a.noise, a.n_rel, r, w, w + 3, rt, om, out);
+  release_pair<double>(a.df, a.dfp, a.noise, a.n_rel, r, w, w + 3, rt, om, a.GMp, out);
   for (int side = 0; side < 2; ++side)
 #pragma unroll
     for (int e = 0; e < 6; ++e) a.ics[e * a.np + 2 * r + side] = out[side][e];
@@ -928,9 +971,10 @@ __global__ void __launch_bounds__(128) k_stream_df_sample(DfSampleArgs a, const 
     v[j] = a.w[(3 + j) * a.n + r];
   }
   double rt, om, out[2][6];
-  king_rt_om(s_comps, a.ncomp, a.G * a.mass[r], x, v, rt, om);
+  const double GM = a.G * a.mass[r];
+  king_rt_om(s_comps, a.ncomp, GM, x, v, rt, om);
   if (a.rt) a.rt[r] = rt;
-  release_pair<double>(a.df, a.dfp, a.noise, a.n, r, x, v, rt, om, out);
+  release_pair<double>(a.df, a.dfp, a.noise, a.n, r, x, v, rt, om, GM, out);
 #pragma unroll
   for (int e = 0; e < 6; ++e) {
     a.lead[e * a.n + r] = out[0][e];
@@ -962,7 +1006,7 @@ __global__ void __launch_bounds__(128) k_stream_release_adj(StreamDev a, const D
     }
     RT.d[6] = 1.0;
     OM.d[7] = 1.0;
-    release_pair<Dual<8>>(a.df, a.dfp, a.noise, a.n_rel, r, X8, V8, RT, OM, out);
+    release_pair<Dual<8>>(a.df, a.dfp, a.noise, a.n_rel, r, X8, V8, RT, OM, a.GMp, out);
     for (int side = 0; side < 2; ++side)
       for (int e = 0; e < 6; ++e) {
         const double lam = a.lam_rel[e * a.np + 2 * r + side];
@@ -1214,8 +1258,8 @@ static StreamLayout stream_layout(int ncomp, const gal_stream_config& c, bool gr
 }
 
 static gal_status df_validate(int32_t df, const double* p) {
-  if (df != GAL_STREAM_DF_OFFSETS && df != GAL_STREAM_DF_FARDAL2015)
-    return fail(GAL_ERR_INVALID_ARGUMENT, "df must be GAL_STREAM_DF_OFFSETS or GAL_STREAM_DF_FARDAL2015");
+  if (df != GAL_STREAM_DF_OFFSETS && df != GAL_STREAM_DF_FARDAL2015 && df != GAL_STREAM_DF_CHEN2024)
+    return fail(GAL_ERR_INVALID_ARGUMENT, "df must be GAL_STREAM_DF_OFFSETS, _FARDAL2015 or _CHEN2024");
   if (df == GAL_STREAM_DF_FARDAL2015) {
     if (!p) return fail(GAL_ERR_INVALID_ARGUMENT, "NULL df_params");
     for (int j = 0; j < 8; ++j)

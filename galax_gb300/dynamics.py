@@ -191,7 +191,10 @@ def _as_cuda(x, dtype):
     torch = _torch()
     if isinstance(x, torch.Tensor):
         return x.to(device="cuda", dtype=dtype)
-    return torch.as_tensor(np.asarray(x), dtype=dtype, device="cuda")
+    a = np.asarray(x)
+    if not a.flags.writeable:  # broadcast views: torch wants writable memory
+        a = a.copy()
+    return torch.as_tensor(a, dtype=dtype, device="cuda")
 
 
 def integrate(

@@ -15,16 +15,17 @@ galax's two stream front ends, with the same arguments and results:
   progenitor from ``prog_t0`` to the first release time.
 
 The release points are sampled by ``gal_stream_df_sample``: the King (1962)
-tidal radius and Fardal (2015) offsets, one thread per release. The particle
+tidal radius and the Fardal (2015) or Chen (2024) model, one thread per
+release. The particle
 orbits run through the uneven-span integrator (``gal_integrate`` with
 per-orbit start and end times). The progenitor is one ``evaluate_orbit``
 call.
 
 galax draws the DF's normals from a jax PRNG key. Here ``rng`` is a
-``numpy.random.Generator`` or an integer seed: four draws per release point,
-in the order (kr, kvphi, kz, kvz). ``draws=`` passes them explicitly. For
-streams with the progenitor's own moving potential, and for their gradients,
-see ``galax_gb300.stream``.
+``numpy.random.Generator`` or an integer seed: four draws per release point
+for Fardal (kr, kvphi, kz, kvz), six for Chen. ``draws=`` passes them
+explicitly. For streams with the progenitor's own moving potential, and for
+their gradients, see ``galax_gb300.stream``.
 """
 
 from __future__ import annotations
@@ -44,12 +45,11 @@ def _torch():
     return torch
 
 
-def _draws(rng, n: int, draws=None) -> np.ndarray:
+def _draws(rng, n: int, draws=None, k: int = 4) -> np.ndarray:
     if draws is not None:
-        d = np.asarray(draws, np.float64).reshape(n, 4)
-        return d
+        return np.asarray(draws, np.float64).reshape(n, k)
     g = rng if isinstance(rng, np.random.Generator) else np.random.default_rng(rng)
-    return g.normal(size=(n, 4))
+    return g.normal(size=(n, k))
 
 
 def _np(x) -> np.ndarray:
@@ -138,6 +138,27 @@ class FardalStreamDF:
                 "trail": MockStreamArm(trail[:, :3], trail[:, 3:], ts.copy(), ts.copy())}
 
 
+@dataclass(frozen=True)
+class ChenStreamDF:
+    """galax's Chen et al. (2024) DF, "no progenitor" version
+    (legacy/mockstream/df/chen24.py:21-137): six correlated draws per release
+    point, posvel = mean + A z from six standard normals z (A: the
+    lower-triangular factor of galax's covariance). ``sample`` has the same
+    signature and result as FardalStreamDF.sample."""
+
+    def sample(self, rng, pot: AbstractPotential, prog_orbit, prog_mass, *, draws=None) -> dict:
+        q = _np(prog_orbit.q).reshape(-1, 3)
+        p = _np(prog_orbit.p).reshape(-1, 3)
+        ts = _np(prog_orbit.t).reshape(-1)
+        n = q.shape[0]
+        mprog = prog_mass if callable(prog_mass) else ConstantMassProgenitor(prog_mass)
+        m = np.broadcast_to(np.asarray(mprog(ts), np.float64), (n,))
+        lead, trail, _ = _stream.df_sample(pot, np.concatenate([q, p], axis=1), m, _draws(rng, n, draws, 6),
+                                           df="chen2024")
+        return {"lead": MockStreamArm(lead[:, :3], lead[:, 3:], ts.copy(), ts.copy()),
+                "trail": MockStreamArm(trail[:, :3], trail[:, 3:], ts.copy(), ts.copy())}
+
+
 def _default_integrator() -> Integrator:
     return Integrator()
 
@@ -146,7 +167,7 @@ def _default_integrator() -> Integrator:
 class MockStreamGenerator:
     """galax's MockStreamGenerator (legacy/mockstream/mockstream_generator.py:33-275)."""
 
-    df: FardalStreamDF
+    df: FardalStreamDF | ChenStreamDF
     potential: AbstractPotential
     progenitor_integrator: Integrator = field(default_factory=_default_integrator)
     stream_integrator: Integrator = field(default_factory=_default_integrator)

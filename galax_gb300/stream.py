@@ -6,12 +6,17 @@ src/galax/dynamics/_src/experimental/stream.py:121-446) with the progenitor's
 own Plummer potential moved along its orbit (legacy/mockstream/_moving.py and
 ``MockStreamGenerator``), on a constant-step grid of release times. Release
 conditions use the King (1962) tidal radius
-(dynamics/_src/cluster/radius.py:198-214) and one of two release models for
-particles 2r (leading) and 2r + 1 (trailing) of release r: "offsets",
-``x_prog -/+ r_t rhat + 0.1 r_t xi`` with velocity ``v_prog + 0.1 Omega r_t eta``,
-or "fardal2015", galax's Fardal (2015) DF (legacy/mockstream/df/fardal15.py,
-experimental/df.py). ``df_sample`` evaluates a release model alone at any
-batch of progenitor points.
+(dynamics/_src/cluster/radius.py:198-214) and one of three release models for
+particles 2r (leading) and 2r + 1 (trailing) of release r:
+
+- "offsets": ``x_prog -/+ r_t rhat + 0.1 r_t xi`` with velocity
+  ``v_prog + 0.1 Omega r_t eta``;
+- "fardal2015": galax's Fardal (2015) DF (legacy/mockstream/df/fardal15.py,
+  experimental/df.py);
+- "chen2024": galax's Chen (2024) DF (legacy/mockstream/df/chen24.py).
+
+``df_sample`` evaluates a release model alone at any batch of progenitor
+points.
 
 ``simulate`` runs the forward pipeline (``gal_stream_run``); ``gradient``
 returns dL/d(component parameters) of L = sum_p |y_p(t_now) - target_p|^2
@@ -38,11 +43,12 @@ def _torch():
     return torch
 
 
-DFS = {"offsets": _lib.STREAM_DF_OFFSETS, "fardal2015": _lib.STREAM_DF_FARDAL2015}
+DFS = {"offsets": _lib.STREAM_DF_OFFSETS, "fardal2015": _lib.STREAM_DF_FARDAL2015,
+       "chen2024": _lib.STREAM_DF_CHEN2024}
 # kr_bar, kvphi_bar, kz_bar, kvz_bar, sigma_kr, sigma_kvphi, sigma_kz, sigma_kvz
 # (galax's defaults, legacy/mockstream/df/fardal15.py:26-35, experimental/df.py:57-64)
 FARDAL2015_DEFAULTS = (2.0, 0.3, 0.0, 0.0, 0.5, 0.5, 0.5, 0.5)
-NOISE_COLUMNS = {_lib.STREAM_DF_OFFSETS: 12, _lib.STREAM_DF_FARDAL2015: 4}
+NOISE_COLUMNS = {_lib.STREAM_DF_OFFSETS: 12, _lib.STREAM_DF_FARDAL2015: 4, _lib.STREAM_DF_CHEN2024: 6}
 
 
 def _df_code(df) -> int:
@@ -55,9 +61,9 @@ def _df_code(df) -> int:
 
 def config(*, n_release: int, dt: float, w_now, prog_m: float, prog_b: float, t_now: float = 0.0,
            method: int = 8, k_ckpt: int = 256, df="offsets", df_params=None) -> _lib.StreamConfig:
-    """``gal_stream_config``. ``df``: "offsets" (noise (n_release, 12)) or
+    """``gal_stream_config``. ``df``: "offsets" (noise (n_release, 12)),
     "fardal2015" (noise (n_release, 4); ``df_params`` defaults to galax's
-    Fardal values)."""
+    Fardal values) or "chen2024" (noise (n_release, 6))."""
     w = np.asarray(w_now, np.float64).reshape(6)
     code = _df_code(df)
     p = FARDAL2015_DEFAULTS if df_params is None else tuple(float(v) for v in df_params)
@@ -94,7 +100,8 @@ def _noise_soa(noise, n_release: int, df: int):
 def simulate(pot: AbstractPotential, cfg: _lib.StreamConfig, noise) -> StreamResult:
     """Forward stream: ``noise`` holds standard-normal draws per release,
     (n_release, 12) for the offsets model (xi_lead, eta_lead, xi_trail,
-    eta_trail) or (n_release, 4) for Fardal 2015 (kr, kvphi, kz, kvz). NumPy
+    eta_trail), (n_release, 4) for Fardal 2015 (kr, kvphi, kz, kvz) or
+    (n_release, 6) for Chen 2024 (standard normals behind posvel). NumPy
     in, NumPy out; CUDA tensors stay on the device."""
     torch = _torch()
     is_np = not isinstance(noise, torch.Tensor)
@@ -147,7 +154,7 @@ def gradient(pot: AbstractPotential, cfg: _lib.StreamConfig, noise, target) -> S
 def df_sample(pot: AbstractPotential, prog_w, prog_mass, noise, *, df="fardal2015", df_params=None):
     """Release conditions at n progenitor points ``prog_w`` (n, 6) with masses
     ``prog_mass`` (scalar or (n,)) from standard-normal ``noise`` ((n, 4) for
-    Fardal 2015, (n, 12) for the offsets model): returns (lead (n, 6), trail
+    Fardal 2015, (n, 6) for Chen 2024, (n, 12) for the offsets model): returns (lead (n, 6), trail
     (n, 6), r_tidal (n,)) (``gal_stream_df_sample``; FardalStreamDF._sample,
     legacy/mockstream/df/fardal15.py:49-94). NumPy in, NumPy out; CUDA
     tensors stay on the device."""
@@ -158,7 +165,7 @@ def df_sample(pot: AbstractPotential, prog_w, prog_mass, noise, *, df="fardal201
     n = w.shape[0]
     ws = w.t().contiguous()
     m = _as_cuda(prog_mass, torch.float64).reshape(-1).expand(n).contiguous()
-    nz = _as_cuda(noise, torch.float64).reshape(n, NOISE_COLUMNS[code]).t().contiguous()
+    nz = _as_cuda(noise, torch.float64).reshape(n, NOISE_COLUMNS.get(code, 12)).t().contiguous()
     p = FARDAL2015_DEFAULTS if df_params is None else tuple(float(v) for v in df_params)
     if len(p) != 8:
         raise ValueError("df_params has 8 values")

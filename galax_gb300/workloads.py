@@ -103,9 +103,9 @@ class StreamSetup:
     n_release: int        # release times t_now - (n_release - r) dt, r = 0..n_release-1
     prog_m: float
     prog_b: float
-    noise: np.ndarray     # (n_release, 12) offsets draws or (n_release, 4) Fardal draws, N(0, 1)
+    noise: np.ndarray     # (n_release, 12 | 4 | 6) draws of the offsets / Fardal / Chen model, N(0, 1)
     pert: np.ndarray      # (2 n_release, 6): target offsets (N(0, 0.1 kpc), N(0, 2 km/s))
-    df: int = 0           # release model: 0 offsets, 1 Fardal 2015
+    df: int = 0           # release model: 0 offsets, 1 Fardal 2015, 2 Chen 2024
     df_params: tuple = (2.0, 0.3, 0.0, 0.0, 0.5, 0.5, 0.5, 0.5)
 
 
@@ -117,13 +117,14 @@ def stream_setup(grad, n_release: int = 3000, dt: float = 1.0, seed: int = 4, ap
     tangential, inclined incl_deg to the x-y plane) at t_now = 0, released
     over n_release dt before the present, two particles per release with
     seeded release draws (df 0: Gaussian offsets, 12 per release; df 1:
-    Fardal 2015, 4 per release), and seeded target perturbations for the loss."""
+    Fardal 2015, 4; df 2: Chen 2024, 6), and seeded target perturbations for
+    the loss."""
     rng = np.random.default_rng(seed)
     x = np.array([[apocentre, 0.0, 0.0]])
     vc = float(circular_speed(grad, x)[0])
     inc = np.deg2rad(incl_deg)
     w_now = np.array([apocentre, 0.0, 0.0, 0.0, speed_frac * vc * np.cos(inc), speed_frac * vc * np.sin(inc)])
-    noise = rng.normal(size=(n_release, 4 if df == 1 else 12))
+    noise = rng.normal(size=(n_release, {1: 4, 2: 6}.get(df, 12)))
     pert = np.concatenate([rng.normal(0.0, 0.1, (2 * n_release, 3)), rng.normal(0.0, 2 * KMS, (2 * n_release, 3))],
                           axis=1)
     return StreamSetup(w_now, 0.0, dt, n_release, prog_m, prog_b, noise, pert, int(df))

@@ -271,7 +271,7 @@ typedef struct gal_stream_config {
   double prog_m;     /* progenitor Plummer mass */
   double prog_b;     /* progenitor Plummer scale radius */
   double w_now[6];   /* progenitor phase-space point at t_now (host values) */
-  int32_t df;        /* release model: GAL_STREAM_DF_OFFSETS or GAL_STREAM_DF_FARDAL2015 */
+  int32_t df;        /* release model: GAL_STREAM_DF_OFFSETS, _FARDAL2015 or _CHEN2024 */
   int32_t reserved;  /* 0 */
   double df_params[8]; /* Fardal 2015: kr_bar, kvphi_bar, kz_bar, kvz_bar, sigma_kr, sigma_kvphi,
                         * sigma_kz, sigma_kvz (galax's defaults 2, 0.3, 0, 0, 0.5, 0.5, 0.5, 0.5);
@@ -288,9 +288,17 @@ typedef struct gal_stream_config {
  *                kz = kz_bar + sigma_kz n2, kvz = kvz_bar + sigma_kvz n3, zhat along x cross v,
  *                phihat along v - (v . rhat) rhat; noise [4][n]: n0..n3, shared by both
  *                particles (legacy/mockstream/df/fardal15.py:49-94,
- *                experimental/df.py:136-177). */
+ *                experimental/df.py:136-177);
+ *   CHEN2024:    posvel = mean + A z, z = noise [6][n] standard normals, A the
+ *                lower-triangular factor of galax's covariance (posvel_0 and
+ *                posvel_4 correlated at -0.7, posvel_3 fixed at 1); Dr = posvel_0 r_t,
+ *                Dv = posvel_3 sqrt(2 G M / Dr), angles phi, theta, alpha, beta =
+ *                posvel_1, 2, 4, 5 degrees; x -/+ Dr (cos th cos ph rhat + cos th sin ph
+ *                phihat) + Dr sin th zhat, v -/+ Dv (cos b cos a rhat + cos b sin a phihat)
+ *                + Dv sin b zhat (legacy/mockstream/df/chen24.py:21-137). */
 #define GAL_STREAM_DF_OFFSETS 0
 #define GAL_STREAM_DF_FARDAL2015 1
+#define GAL_STREAM_DF_CHEN2024 2
 
 /* Scratch bytes for gal_stream_run (with_grad = 0) or gal_stream_grad (1). */
 GAL_API gal_status gal_stream_workspace_size(const gal_potential* pot, const gal_stream_config* cfg,
@@ -322,7 +330,7 @@ GAL_API gal_status gal_stream_grad(const gal_potential* pot, const gal_stream_co
  * (legacy/mockstream/df/fardal15.py:49-94) and Fardal2015DF.sample
  * (experimental/df.py:136-177) for a batch of release points, with
  * tidal_radius (dynamics/_src/cluster/radius.py:198-214) inside; the normal
- * draws come from the caller (noise [4][n] or [12][n], see the release models
+ * draws come from the caller (noise [12][n], [4][n] or [6][n], see the release models
  * above) instead of a jax PRNG key. */
 GAL_API gal_status gal_stream_df_sample(const gal_potential* pot, int32_t df, const double* df_params,
                                         const double* prog_w, const double* prog_mass, const double* noise, int64_t n,

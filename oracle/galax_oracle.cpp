@@ -850,7 +850,7 @@ int orc_adjoint_fixed(const Comp* comps, int ncomp, double G, const OrcSolverCfg
 // prog_m, radius prog_b) centred on the progenitor's stage positions, i.e.
 // exactly the particle half of the coupled particle + progenitor system.
 // Particle ICs (p = 2 r + side, side 0 = leading, 1 = trailing; s = -1 / +1)
-// by one of two release models (see release_pair):
+// by one of three release models (see release_pair; df 2 is Chen 2024):
 //   df 0 (offsets): x = x_prog + s r_t rhat + 0.1 r_t xi_p,
 //                   v = v_prog + 0.1 Omega r_t eta_p, xi, eta given normal draws;
 //   df 1 (Fardal 2015, legacy/mockstream/df/fardal15.py:62-94 and
@@ -958,10 +958,42 @@ static void king_rt_om(const Pot& P, double GM, const double* x, const double* v
 // kvphi, kz, kvz). dfp: kr_bar, kvphi_bar, kz_bar, kvz_bar, sigma_kr,
 // sigma_kvphi, sigma_kz, sigma_kvz.
 static void release_pair(int df, const double* dfp, const double* nz, const double* x, const double* v, double rt,
-                         double om, double* lead, double* trail) {
+                         double om, double GM, double* lead, double* trail) {
   const double rr = norm3(x);
   const double rh[3] = {x[0] / rr, x[1] / rr, x[2] / rr};
   double* out[2] = {lead, trail};
+  if (df == 2) {
+    // Chen et al. 2024 as galax samples it (legacy/mockstream/df/chen24.py):
+    // posvel ~ N(mean, cov); here posvel = mean + A z with A the lower
+    // triangular factor of cov and z = nz[0..5] standard normals.
+    const double pv0 = 1.6 + 0.35 * nz[0];
+    const double pv1 = -30.0 + 23.0 * nz[1];
+    const double pv2 = 12.0 * nz[2];
+    const double pv3 = 1.0;
+    const double pv4 = 20.0 + 20.0 * (-0.7 * nz[0] + std::sqrt(1.0 - 0.49) * nz[4]);
+    const double pv5 = 22.0 * nz[5];
+    const double deg = 0.017453292519943295;
+    const double Dr = pv0 * rt;
+    const double Dv = pv3 * std::sqrt(2.0 * GM / Dr);
+    const double cth = std::cos(pv2 * deg), sth = std::sin(pv2 * deg);
+    const double cph = std::cos(pv1 * deg), sph = std::sin(pv1 * deg);
+    const double cal = std::cos(pv4 * deg), sal = std::sin(pv4 * deg);
+    const double cbe = std::cos(pv5 * deg), sbe = std::sin(pv5 * deg);
+    const double L[3] = {x[1] * v[2] - x[2] * v[1], x[2] * v[0] - x[0] * v[2], x[0] * v[1] - x[1] * v[0]};
+    const double Lm = norm3(L);
+    const double vr = v[0] * rh[0] + v[1] * rh[1] + v[2] * rh[2];
+    double yh[3] = {v[0] - vr * rh[0], v[1] - vr * rh[1], v[2] - vr * rh[2]};
+    const double ym = norm3(yh);
+    for (int j = 0; j < 3; ++j) {
+      const double zh = L[j] / Lm;
+      yh[j] /= ym;
+      trail[j] = x[j] + Dr * cth * cph * rh[j] + Dr * cth * sph * yh[j] + Dr * sth * zh;
+      trail[3 + j] = v[j] + Dv * cbe * cal * rh[j] + Dv * cbe * sal * yh[j] + Dv * sbe * zh;
+      lead[j] = x[j] - Dr * cth * cph * rh[j] - Dr * cth * sph * yh[j] + Dr * sth * zh;
+      lead[3 + j] = v[j] - Dv * cbe * cal * rh[j] - Dv * cbe * sal * yh[j] + Dv * sbe * zh;
+    }
+    return;
+  }
   if (df == 1) {
     // Fardal et al. 2015 as galax samples it: k values from the four draws,
     // then the leading arm inside (-kr) and the trailing arm outside (+kr).
@@ -999,23 +1031,24 @@ static void release_pair(int df, const double* dfp, const double* nz, const doub
 }  // namespace orc
 
 // Release conditions at n independent progenitor points w (n x 6) with masses
-// mass (n): lead, trail (n x 6), r_tidal (n). noise: n x 12 or n x 4 (df).
+// mass (n): lead, trail (n x 6), r_tidal (n). noise: n x 12, n x 4 or n x 6 (df 0, 1, 2).
 int orc_stream_df_sample(const Comp* comps, int ncomp, double G, int df, const double* dfp, const double* w,
                          const double* mass, const double* noise, int64_t n, double* lead, double* trail,
                          double* r_tidal) {
   Pot P{comps, ncomp, G};
-  const int nq = df == 1 ? 4 : 12;
+  const int nq = df == 1 ? 4 : (df == 2 ? 6 : 12);
   for (int64_t r = 0; r < n; ++r) {
     double rt, om;
     orc::king_rt_om(P, G * mass[r], w + 6 * r, w + 6 * r + 3, rt, om);
     r_tidal[r] = rt;
-    orc::release_pair(df, dfp, noise + nq * r, w + 6 * r, w + 6 * r + 3, rt, om, lead + 6 * r, trail + 6 * r);
+    orc::release_pair(df, dfp, noise + nq * r, w + 6 * r, w + 6 * r + 3, rt, om, G * mass[r], lead + 6 * r,
+                      trail + 6 * r);
   }
   return 0;
 }
 
 // prog_track: (n_rel + 1) x 6 forward states; ics, final_: 2 n_rel x 6;
-// noise: n_rel x 12 (offsets) or n_rel x 4 (Fardal); rt_om: n_rel x 2 (r_t, Omega).
+// noise: n_rel x 12 (offsets), n_rel x 4 (Fardal) or n_rel x 6 (Chen); rt_om: n_rel x 2 (r_t, Omega).
 int orc_stream_forward(const Comp* comps, int ncomp, double G, int method, double prog_m, double prog_b,
                        const double* w_now, double t_now, double dt, int64_t n_rel, int df, const double* dfp,
                        const double* noise, double* prog_track, double* rt_om, double* ics, double* final_,
@@ -1043,14 +1076,14 @@ int orc_stream_forward(const Comp* comps, int ncomp, double G, int method, doubl
   }
   const double GM = G * prog_m, b2 = prog_b * prog_b;
   // release: King tidal radius and the particle ICs
-  const int nq = df == 1 ? 4 : 12;
+  const int nq = df == 1 ? 4 : (df == 2 ? 6 : 12);
   for (int64_t r = 0; r < n_rel; ++r) {
     const double* w = prog_track + 6 * r;
     double rt, om;
     orc::king_rt_om(P, GM, w, w + 3, rt, om);
     rt_om[2 * r] = rt;
     rt_om[2 * r + 1] = om;
-    orc::release_pair(df, dfp, noise + nq * r, w, w + 3, rt, om, ics + 6 * (2 * r), ics + 6 * (2 * r + 1));
+    orc::release_pair(df, dfp, noise + nq * r, w, w + 3, rt, om, GM, ics + 6 * (2 * r), ics + 6 * (2 * r + 1));
   }
 #ifdef _OPENMP
   if (nthreads > 0) omp_set_num_threads(nthreads);

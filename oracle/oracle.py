@@ -286,14 +286,15 @@ def stream_forward(c: np.ndarray, setup, *, method: int = 8, G: float = G_GALACT
     rt_om = np.empty((n, 2))
     ics = np.empty((2 * n, 6))
     final = np.empty((2 * n, 6))
-    noise = np.ascontiguousarray(setup.noise, np.float64).reshape(n, 4 if df == STREAM_DF_FARDAL2015 else 12)
+    noise = np.ascontiguousarray(setup.noise, np.float64).reshape(n, NOISE_COLUMNS.get(df, 12))
     L.orc_stream_forward(np.ascontiguousarray(c), len(c), G, method, float(setup.prog_m), float(setup.prog_b),
                          np.ascontiguousarray(setup.w_now, np.float64), float(setup.t_now), float(setup.dt), n, df,
                          dfp, noise, track, rt_om, ics, final, nthreads)
     return dict(track=track, rt_om=rt_om, ics=ics, final=final)
 
 
-STREAM_DF_OFFSETS, STREAM_DF_FARDAL2015 = 0, 1
+STREAM_DF_OFFSETS, STREAM_DF_FARDAL2015, STREAM_DF_CHEN2024 = 0, 1, 2
+NOISE_COLUMNS = {STREAM_DF_OFFSETS: 12, STREAM_DF_FARDAL2015: 4, STREAM_DF_CHEN2024: 6}
 FARDAL2015_DEFAULTS = (2.0, 0.3, 0.0, 0.0, 0.5, 0.5, 0.5, 0.5)
 
 
@@ -318,7 +319,7 @@ def stream_df_sample(c: np.ndarray, w, mass, noise, *, df: int = STREAM_DF_FARDA
     w = np.ascontiguousarray(w, np.float64).reshape(-1, 6)
     n = len(w)
     mass = np.ascontiguousarray(np.broadcast_to(np.asarray(mass, np.float64), (n,)))
-    noise = np.ascontiguousarray(noise, np.float64).reshape(n, 4 if df == STREAM_DF_FARDAL2015 else 12)
+    noise = np.ascontiguousarray(noise, np.float64).reshape(n, NOISE_COLUMNS.get(df, 12))
     p = np.ascontiguousarray(FARDAL2015_DEFAULTS if df_params is None else df_params, np.float64).reshape(8)
     lead, trail, rt = np.empty((n, 6)), np.empty((n, 6)), np.empty(n)
     L.orc_stream_df_sample(np.ascontiguousarray(c), len(c), G, int(df), p, w, mass, noise, n, lead, trail, rt)

@@ -47,14 +47,14 @@ def _points(n, seed=3):
     return np.concatenate([x, v], axis=1), rng
 
 
-@pytest.mark.parametrize("df", [1, 0])
+@pytest.mark.parametrize("df", [1, 0, 2])
 def test_df_sample_matches_oracle(M, df):
     from galax_gb300 import stream
 
     c = O.milky_way()
     w, rng = _points(1000)
     mass = rng.uniform(1e4, 1e6, len(w))
-    nz = rng.normal(size=(len(w), 4 if df == 1 else 12))
+    nz = rng.normal(size=(len(w), O.NOISE_COLUMNS[df]))
     p = (1.5, 0.2, 0.1, -0.1, 0.3, 0.4, 0.2, 0.1)
     lead, trail, rt = stream.df_sample(_pot(c), w, mass, nz, df=df, df_params=p)
     el, et, ert = O.stream_df_sample(c, w, mass, nz, df=df, df_params=p)
@@ -92,12 +92,24 @@ def test_fardal2015_doctest_geometry(M, goldens):
         np.testing.assert_allclose(a, b, rtol=2e-8, atol=1e-12)
 
 
-def _oracle_generator(c, ts, w0, mass, draws, rtol=1e-7):
+def test_mock_stream_generator_with_chen_df(M):
+    c = O.milky_way()
+    ts = np.linspace(0.0, 500.0, 51)
+    w0 = np.array([12.0, 0.0, 4.0, 0.0, 0.2, 0.02])
+    draws = np.random.default_rng(5).normal(size=(len(ts), 6))
+    gen = M.MockStreamGenerator(M.ChenStreamDF(), _pot(c))
+    arms, _ = gen.run(None, ts, w0, 2e4, draws=draws)
+    lead, trail, _ = _oracle_generator(c, ts, w0, 2e4, draws, df=O.STREAM_DF_CHEN2024)
+    assert _rel(arms["lead"].q, lead[:, :3]) < 1e-6
+    assert _rel(arms["trail"].p, trail[:, 3:]) < 1e-6
+
+
+def _oracle_generator(c, ts, w0, mass, draws, rtol=1e-7, df=O.STREAM_DF_FARDAL2015):
     cfg = O.solver_cfg(8, True, rtol=rtol, atol=rtol)
     saves, st, _, _ = O.integrate(c, w0[None], ts[0], ts[-1], ts, cfg)
     assert st[0] == 0
     track = saves[0]
-    lead, trail, _ = O.stream_df_sample(c, track, mass, draws)
+    lead, trail, _ = O.stream_df_sample(c, track, mass, draws, df=df)
     t_f = ts[-1] + 1e-3
     ics = np.concatenate([lead, trail])
     t0 = np.concatenate([ts, ts])

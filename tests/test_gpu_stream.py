@@ -3,7 +3,7 @@
 
 Forward: progenitor track, release conditions and final particle states agree
 with the oracle to 1e-9 relative (constant steps on both sides), for both
-release models (Gaussian offsets and galax's Fardal 2015 DF). Gradient: the
+release models (Gaussian offsets, galax's Fardal 2015 and Chen 2024 DFs). Gradient: the
 discrete adjoint of the whole pipeline (particles, tidal-radius release map,
 progenitor orbit) against central finite differences of the oracle with one
 Richardson extrapolation, 1e-6 relative for the halo mass and scale radius,
@@ -70,7 +70,7 @@ HOSTS = {
 }
 
 
-@pytest.mark.parametrize("df", [0, 1])
+@pytest.mark.parametrize("df", [0, 1, 2])
 @pytest.mark.parametrize("host", list(HOSTS))
 @pytest.mark.parametrize("method", [8, 5])
 def test_forward_matches_oracle(S, host, method, df):
@@ -83,7 +83,7 @@ def test_forward_matches_oracle(S, host, method, df):
     assert _relmax(got.final, ref["final"]) < 1e-9
 
 
-@pytest.mark.parametrize("k_ckpt,df", [(64, 0), (0, 0), (0, 1)])
+@pytest.mark.parametrize("k_ckpt,df", [(64, 0), (0, 0), (0, 1), (64, 2)])
 @pytest.mark.parametrize("host", list(HOSTS))
 def test_gradient_matches_finite_differences(S, host, k_ckpt, df):
     comps = HOSTS[host]
@@ -110,7 +110,7 @@ def test_gradient_matches_finite_differences(S, host, k_ckpt, df):
             assert g.grad_params[c][2] == 0.0
 
 
-@pytest.mark.parametrize("df", [0, 1])
+@pytest.mark.parametrize("df", [0, 1, 2])
 def test_gradient_with_respect_to_the_present_progenitor_point(S, df):
     comps = HOSTS["milky_way"]
     s = _setup(comps, n_release=60, df=df)

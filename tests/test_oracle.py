@@ -466,3 +466,51 @@ def test_stream_forward_with_fardal_release():
     np.testing.assert_array_equal(out["ics"][0::2], lead)
     np.testing.assert_array_equal(out["ics"][1::2], trail)
     np.testing.assert_array_equal(out["rt_om"][:, 0], rt)
+
+
+CHEN_MEAN = np.array([1.6, -30, 0, 1, 20, 0])
+CHEN_COV = np.array([[0.1225, 0, 0, 0, -4.9, 0], [0, 529, 0, 0, 0, 0], [0, 0, 144, 0, 0, 0], [0, 0, 0, 0, 0, 0],
+                     [-4.9, 0, 0, 0, 400, 0], [0, 0, 0, 0, 0, 484]])  # legacy/mockstream/df/chen24.py:21-32
+
+
+def _chen_factor():
+    A = np.diag([0.35, 23.0, 12.0, 0.0, 20.0 * np.sqrt(1 - 0.49), 22.0])
+    A[4, 0] = -14.0
+    return A
+
+
+def test_chen_factor_reproduces_galax_covariance():
+    np.testing.assert_allclose(_chen_factor() @ _chen_factor().T, CHEN_COV, rtol=1e-14, atol=1e-12)
+
+
+def test_chen2024_sample_matches_the_written_out_formula():
+    """Chen 2024 written out as in galax (legacy/mockstream/df/chen24.py:58-137),
+    with posvel = mean + A z."""
+    c = O.milky_way()
+    rng = np.random.default_rng(8)
+    n = 60
+    x = rng.uniform(-30, 30, (n, 3))
+    v = rng.normal(0, 0.2, (n, 3))
+    w = np.concatenate([x, v], axis=1)
+    z = rng.normal(size=(n, 6))
+    mass = rng.uniform(1e4, 1e6, n)
+    lead, trail, rt = O.stream_df_sample(c, w, mass, z, df=O.STREAM_DF_CHEN2024)
+    _, _, ert = _fardal_reference(c, w, mass[:, None], np.zeros((n, 4)))
+    np.testing.assert_allclose(rt, ert, rtol=1e-12)
+    pv = CHEN_MEAN + z @ _chen_factor().T
+    xh = x / np.linalg.norm(x, axis=1, keepdims=True)
+    L = np.cross(x, v)
+    zh = L / np.linalg.norm(L, axis=1, keepdims=True)
+    yh = v - np.sum(v * xh, axis=1, keepdims=True) * xh
+    yh = yh / np.linalg.norm(yh, axis=1, keepdims=True)
+    Dr = pv[:, 0] * ert
+    Dv = pv[:, 3] * np.sqrt(2 * O.G_GALACTIC * mass / Dr)
+    ph, th, al, be = (np.deg2rad(pv[:, k]) for k in (1, 2, 4, 5))
+    dx_in = (Dr * np.cos(th) * np.cos(ph))[:, None] * xh + (Dr * np.cos(th) * np.sin(ph))[:, None] * yh
+    dx_z = (Dr * np.sin(th))[:, None] * zh
+    dv_in = (Dv * np.cos(be) * np.cos(al))[:, None] * xh + (Dv * np.cos(be) * np.sin(al))[:, None] * yh
+    dv_z = (Dv * np.sin(be))[:, None] * zh
+    np.testing.assert_allclose(trail, np.concatenate([x + dx_in + dx_z, v + dv_in + dv_z], axis=1), rtol=1e-12,
+                               atol=1e-14)
+    np.testing.assert_allclose(lead, np.concatenate([x - dx_in + dx_z, v - dv_in + dv_z], axis=1), rtol=1e-12,
+                               atol=1e-14)

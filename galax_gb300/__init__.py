@@ -22,15 +22,20 @@ from .dynamics import (
 )
 from .mockstream import ChenStreamDF, Fardal2015DF, FardalStreamDF, MockStreamGenerator, StreamSimulator
 from .potential import (
+    BovyMWPotential2014,
     CompositePotential,
     HernquistPotential,
     IsochronePotential,
     KeplerPotential,
     LogarithmicPotential,
     MilkyWayPotential,
+    MilkyWayPotential2022,
     MiyamotoNagaiPotential,
+    MN3ExponentialPotential,
+    MN3Sech2Potential,
     NFWPotential,
     PlummerPotential,
+    PowerLawCutoffPotential,
     TranslatedPotential,
 )
 
@@ -38,6 +43,7 @@ __all__ = [
     "GalaxGB300Error", "dynamics", "mockstream", "potential", "ConstantStepSize", "Dopri5", "Dopri8", "Integrator",
     "Orbit", "OrbitSolver", "PhaseSpaceCoordinate", "PIDController", "evaluate_orbit", "integrate_orbit",
     "ChenStreamDF", "Fardal2015DF", "FardalStreamDF", "MockStreamGenerator", "StreamSimulator",
-    "CompositePotential", "HernquistPotential", "IsochronePotential", "KeplerPotential", "LogarithmicPotential",
-    "MilkyWayPotential", "MiyamotoNagaiPotential", "NFWPotential", "PlummerPotential", "TranslatedPotential",
+    "BovyMWPotential2014", "CompositePotential", "HernquistPotential", "IsochronePotential", "KeplerPotential", "LogarithmicPotential",
+    "MilkyWayPotential", "MilkyWayPotential2022", "MiyamotoNagaiPotential", "MN3ExponentialPotential",
+    "MN3Sech2Potential", "NFWPotential", "PlummerPotential", "PowerLawCutoffPotential", "TranslatedPotential",
 ]

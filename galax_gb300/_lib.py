@@ -15,7 +15,8 @@ import numpy as np
 
 LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libgalax_gb300.so"
 
-GAL_KEPLER, GAL_HERNQUIST, GAL_MIYAMOTO_NAGAI, GAL_NFW, GAL_PLUMMER, GAL_ISOCHRONE, GAL_LOGARITHMIC = range(7)
+(GAL_KEPLER, GAL_HERNQUIST, GAL_MIYAMOTO_NAGAI, GAL_NFW, GAL_PLUMMER, GAL_ISOCHRONE, GAL_LOGARITHMIC,
+ GAL_POWERLAW_CUTOFF) = range(8)
 ORBIT_STATUS = {0: "successful", 1: "max_steps_reached", 2: "dt_min_reached", 3: "non_finite"}
 
 COMPONENT_DTYPE = np.dtype(

@@ -44,6 +44,19 @@ int device_sm_count() {
   return cache[dev];
 }
 
+// digamma by upward recurrence to x >= 8 and the asymptotic series
+// (Abramowitz & Stegun 6.3.18); host side, for the power law with cutoff.
+static double digamma_host(double x) {
+  double acc = 0.0;
+  while (x < 8.0) {
+    acc -= 1.0 / x;
+    x += 1.0;
+  }
+  const double i2 = 1.0 / (x * x);
+  return acc + std::log(x) - 0.5 / x -
+         i2 * (1.0 / 12 - i2 * (1.0 / 120 - i2 * (1.0 / 252 - i2 * (1.0 / 240 - i2 * (1.0 / 132)))));
+}
+
 static DevComp fold(const gal_component& c, double G) {
   DevComp d{};
   d.kind = c.kind;
@@ -58,6 +71,13 @@ static DevComp fold(const gal_component& c, double G) {
   d.ox = c.origin[0];
   d.oy = c.origin[1];
   d.oz = c.origin[2];
+  if (c.kind == POWERLAW_CUTOFF) {
+    const double a1 = 1.5 - 0.5 * c.l2, a2 = 1.0 - 0.5 * c.l2;
+    d.l2sq = 1.0 / std::tgamma(a1);
+    d.inv_l1 = 1.0 / (c.l1 * c.l1);
+    d.aux0 = digamma_host(a1);
+    d.aux1 = std::tgamma(a2);
+  }
   return d;
 }
 
@@ -91,18 +111,22 @@ static gal_status validate_components(const gal_component* comps, int32_t n) {
   if (n > GAL_MAX_COMPONENTS) return fail(GAL_ERR_TOO_LARGE, "too many components (max GAL_MAX_COMPONENTS)");
   for (int i = 0; i < n; ++i) {
     const gal_component& c = comps[i];
-    if (c.kind < GAL_KEPLER || c.kind > GAL_LOGARITHMIC) return fail(GAL_ERR_UNSUPPORTED, "unsupported component kind");
+    if (c.kind < GAL_KEPLER || c.kind > GAL_POWERLAW_CUTOFF)
+      return fail(GAL_ERR_UNSUPPORTED, "unsupported component kind");
     if (c.flags != 0) return fail(GAL_ERR_INVALID_ARGUMENT, "component flags must be 0");
     const double v[6] = {c.m, c.l1, c.l2, c.origin[0], c.origin[1], c.origin[2]};
     for (double x : v)
       if (!std::isfinite(x)) return fail(GAL_ERR_INVALID_ARGUMENT, "non-finite component parameter");
     if ((c.kind == GAL_HERNQUIST || c.kind == GAL_NFW) && !(c.l1 > 0.0))
       return fail(GAL_ERR_INVALID_ARGUMENT, "r_s must be > 0");
-    if (c.kind == GAL_MIYAMOTO_NAGAI && (c.l1 < 0.0 || !(c.l2 > 0.0)))
-      return fail(GAL_ERR_INVALID_ARGUMENT, "Miyamoto-Nagai needs a >= 0 and b > 0");
+    // a < 0 occurs in the three-disk (MN3) fits; a > -b keeps sqrt(z^2 + b^2) + a > 0
+    if (c.kind == GAL_MIYAMOTO_NAGAI && !(c.l2 > 0.0 && c.l1 > -c.l2))
+      return fail(GAL_ERR_INVALID_ARGUMENT, "Miyamoto-Nagai needs b > 0 and a > -b");
     if (c.kind == GAL_PLUMMER && c.l1 < 0.0) return fail(GAL_ERR_INVALID_ARGUMENT, "Plummer r_s must be >= 0");
     if ((c.kind == GAL_ISOCHRONE || c.kind == GAL_LOGARITHMIC) && !(c.l1 > 0.0))
       return fail(GAL_ERR_INVALID_ARGUMENT, "isochrone b / logarithmic r_s must be > 0");
+    if (c.kind == GAL_POWERLAW_CUTOFF && (!(c.l1 > 0.0) || !(c.l2 >= 0.0 && c.l2 < 2.0)))
+      return fail(GAL_ERR_INVALID_ARGUMENT, "power law with cutoff needs r_c > 0 and 0 <= alpha < 2");
   }
   return GAL_OK;
 }

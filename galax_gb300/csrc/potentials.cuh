@@ -10,6 +10,9 @@
 //   Plummer         Phi = -G m / sqrt(r^2 + b^2)         builtin/plummer.py:122-133
 //   Isochrone       Phi = -G m / (b + sqrt(r^2 + b^2))    builtin/isochrone.py:61-110
 //   Logarithmic     Phi = v_c^2 / 2 log(r_s^2 + r^2)      builtin/logarithmic.py:45-53
+//   Power law with cutoff  Phi = -G m P(a1, s^2) / r - G m Gamma(a2, s^2) / (r_c Gamma(a1)),
+//                   s = r / r_c, a1 = (3 - alpha) / 2, a2 = 1 - alpha / 2
+//                   builtin/powerlawcutoff.py:21-120 (galax: jax gammainc * gamma)
 // galax differentiates these with jax.grad (src/galax/potential/_src/base.py:170-179);
 // here the derivatives are written out analytically and arranged for the FP64
 // pipe: reciprocal square roots instead of sqrt + divide, one shared radius for
@@ -22,23 +25,136 @@
 namespace gal {
 
 enum Kind : int32_t { KEPLER = 0, HERNQUIST = 1, MIYAMOTO_NAGAI = 2, NFW = 3, PLUMMER = 4, ISOCHRONE = 5,
-                      LOGARITHMIC = 6 };
+                      LOGARITHMIC = 6, POWERLAW_CUTOFF = 7 };
 
 constexpr double TINY = 2.2250738585072014e-308;  // DBL_MIN, galax's safe_sqrt offset
 
-// Component with parameters folded for evaluation (80 bytes).
+// Component with parameters folded for evaluation (96 bytes).
 struct DevComp {
   int32_t kind;
   int32_t centered;  // 1 when origin == 0
   double Gm;         // G * m (v_c^2 for the logarithmic potential)
-  double l1;         // a (MN) or r_s / b
-  double l2;         // b (MN)
-  double l2sq;       // b^2 (MN) or l1^2 (Plummer, isochrone, logarithmic)
-  double inv_l1;     // 1 / r_s (NFW)
+  double l1;         // a (MN) or r_s / b / r_c
+  double l2;         // b (MN) or alpha (power law with cutoff)
+  double l2sq;       // b^2 (MN), l1^2 (Plummer, isochrone, logarithmic) or 1 / Gamma(a1) (cutoff)
+  double inv_l1;     // 1 / r_s (NFW) or 1 / r_c^2 (cutoff)
   double ox, oy, oz;
   double inv_m;      // d(log Gm)/dm: 1 / m, or 2 / v_c for the logarithmic potential
+  double aux0;       // digamma(a1) (cutoff)
+  double aux1;       // Gamma(a2) (cutoff)
 };
-static_assert(sizeof(DevComp) == 80, "DevComp layout");
+static_assert(sizeof(DevComp) == 96, "DevComp layout");
+
+// ----------------------------------------------------------- incomplete gamma
+// gamma(a, x) for the power law with cutoff, 0 < a <= 3/2, x > 0: with
+// e = x^a exp(-x), the lower function is e S (power series S = sum_n x^n /
+// (a (a+1) ... (a+n)), Abramowitz & Stegun 6.5.29) for x < a + 1, and the upper
+// one is e h (continued fraction h, A&S 6.5.31, modified Lentz evaluation)
+// otherwise. With want_da the a-derivatives S' and h' are carried along the
+// same recurrences. Both loops stop once the terms (and their derivatives)
+// no longer change the sums, and after 400 terms at most.
+struct IncGamma {
+  bool series;  // true: lower = e sum; false: upper = e sum
+  double lx;    // log x
+  double e;     // x^a exp(-x)
+  double sum, dsum;
+};
+
+__device__ __forceinline__ IncGamma inc_gamma(double a, double x, bool want_da) {
+  IncGamma o;
+  o.lx = log(x);
+  o.e = exp(fma(a, o.lx, -x));
+  o.dsum = 0.0;
+  if (x < a + 1.0) {
+    o.series = true;
+    double t = 1.0 / a, h = -t, S = t, dS = t * h;
+    for (int n = 1; n < 400; ++n) {
+      const double ian = 1.0 / (a + n);
+      t *= x * ian;
+      S += t;
+      if (want_da) {
+        h -= ian;
+        dS = fma(t, h, dS);
+      }
+      if (fabs(t) < 1e-17 * fabs(S) && (!want_da || fabs(t * h) < 1e-17 * fabs(dS))) break;
+    }
+    o.sum = S;
+    o.dsum = dS;
+    return o;
+  }
+  o.series = false;
+  const double FP = 1e-300;
+  double b = x + 1.0 - a, c = 1.0 / FP, d = 1.0 / b, hh = d;
+  double dc = 0.0, dd = d * d, dh = dd;  // d/da: db/da = -1
+  for (int i = 1; i < 400; ++i) {
+    const double an = -i * (i - a);
+    b += 2.0;
+    double dp = fma(an, d, b);
+    if (fabs(dp) < FP) dp = FP;
+    const double cn = b + an / c;
+    double ddel = 0.0;
+    const double dnew = 1.0 / dp;
+    if (want_da) {
+      const double ddp = fma((double)i, d, fma(an, dd, -1.0));
+      const double dcn = -1.0 + (i * c - an * dc) / (c * c);
+      dc = dcn;
+      dd = -ddp * dnew * dnew;
+    }
+    c = fabs(cn) < FP ? FP : cn;
+    d = dnew;
+    const double del = d * c;
+    if (want_da) {
+      ddel = fma(dd, c, d * dc);
+      dh = fma(dh, del, hh * ddel);
+    }
+    hh *= del;
+    if (fabs(del - 1.0) < 1e-17 && (!want_da || fabs(ddel) < 1e-17 * (1.0 + fabs(dh / hh)))) break;
+  }
+  o.sum = hh;
+  o.dsum = dh;
+  return o;
+}
+
+// Power law with cutoff: g(r) with grad Phi = g(r) x, and optionally g'(r)/r and
+// the partials of g with respect to r_c and alpha.
+struct PlcG {
+  double g, gpr, dg_drc, dg_dalpha;
+};
+
+// Not inlined: the series / fraction loops would otherwise add to the register
+// budget of every kernel that evaluates component tables.
+static __device__ __noinline__ PlcG plc_g(const DevComp& c, double r2, double ir, bool want_hess, bool want_params) {
+  const double a1 = fma(-0.5, c.l2, 1.5);
+  const double x = r2 * c.inv_l1;  // (r / r_c)^2
+  const IncGamma ig = inc_gamma(a1, x, want_params);
+  const double eN = ig.e * c.l2sq;  // x^a1 e^-x / Gamma(a1)
+  const double P = ig.series ? eN * ig.sum : 1.0 - eN * ig.sum;
+  const double ir3 = ir * ir * ir;
+  PlcG o;
+  o.g = c.Gm * P * ir3;
+  o.gpr = 0.0;
+  o.dg_drc = 0.0;
+  o.dg_dalpha = 0.0;
+  if (want_hess) o.gpr = fma(2.0 * c.Gm * eN, ir3 * ir * ir, -3.0 * o.g * ir * ir);
+  if (want_params) {
+    // dP/da = e (log x S + S') / Gamma(a) - P psi(a) (lower), or -(e (log x h + h') / Gamma(a) - Q psi(a))
+    const double dPda = ig.series ? fma(eN, fma(ig.lx, ig.sum, ig.dsum), -P * c.aux0)
+                                  : -fma(eN, fma(ig.lx, ig.sum, ig.dsum), -(1.0 - P) * c.aux0);
+    o.dg_drc = -2.0 * c.Gm * eN * ir3 * sqrt(c.inv_l1);
+    o.dg_dalpha = -0.5 * c.Gm * dPda * ir3;
+  }
+  return o;
+}
+
+static __device__ __noinline__ double plc_phi(const DevComp& c, double dx, double dy, double dz) {
+  const double r = sqrt(fma(dx, dx, fma(dy, dy, fma(dz, dz, TINY))));
+  const double x = (r * r) * c.inv_l1;
+  const double a1 = fma(-0.5, c.l2, 1.5), a2 = fma(-0.5, c.l2, 1.0);
+  const IncGamma g1 = inc_gamma(a1, x, false), g2 = inc_gamma(a2, x, false);
+  const double P1 = g1.series ? g1.e * g1.sum * c.l2sq : 1.0 - g1.e * g1.sum * c.l2sq;
+  const double up2 = g2.series ? c.aux1 - g2.e * g2.sum : g2.e * g2.sum;  // Gamma(a2, x)
+  return -c.Gm * (P1 / r + up2 * c.l2sq * sqrt(c.inv_l1));
+}
 
 // ----------------------------------------------------------- single components
 __device__ __forceinline__ void comp_grad(const DevComp& c, double x, double y, double z, double& gx, double& gy,
@@ -85,6 +201,9 @@ __device__ __forceinline__ void comp_grad(const DevComp& c, double x, double y, 
     case LOGARITHMIC:
       f = c.Gm / (r2 + c.l2sq);
       break;
+    case POWERLAW_CUTOFF:
+      f = plc_g(c, r2, ir, false, false).g;
+      break;
     default: {  // PLUMMER
       const double s2 = r2 + c.l2sq;
       const double is = rsqrt(s2);
@@ -120,6 +239,9 @@ __device__ __forceinline__ double comp_phi(const DevComp& c, double x, double y,
     case LOGARITHMIC: {
       const double r = sqrt(fma(dx, dx, fma(dy, dy, fma(dz, dz, TINY))));
       return 0.5 * c.Gm * log(fma(r, r, c.l2sq));
+    }
+    case POWERLAW_CUTOFF: {
+      return plc_phi(c, dx, dy, dz);
     }
     default: {
       const double r = sqrt(fma(dx, dx, fma(dy, dy, fma(dz, dz, TINY))));
@@ -178,6 +300,12 @@ __device__ __forceinline__ void comp_hessian(const DevComp& c, double x, double 
       const double q = r2 + c.l2sq;
       g = c.Gm / q;
       gpr = -2.0 * g / q;
+      break;
+    }
+    case POWERLAW_CUTOFF: {
+      const PlcG t = plc_g(c, r2, 1.0 / r, true, false);
+      g = t.g;
+      gpr = t.gpr;
       break;
     }
     default: {

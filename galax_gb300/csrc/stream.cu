@@ -1421,6 +1421,9 @@ gal_status gal_stream_grad(const gal_potential* pot, const gal_stream_config* cf
   gal_status st = stream_validate(pot, cfg);
   if (st != GAL_OK) return st;
   if (!noise || !target || !grad_params) return fail(GAL_ERR_INVALID_ARGUMENT, "NULL noise, target or gradient");
+  for (int c = 0; c < pot->n; ++c)
+    if (pot->comps[c].kind == GAL_POWERLAW_CUTOFF)  // the release-map adjoint has no third derivatives for it
+      return fail(GAL_ERR_UNSUPPORTED, "stream gradients do not support the power law with cutoff");
   const StreamLayout L = stream_layout(pot->n, *cfg, true);
   if (!workspace || workspace_bytes < L.total) return fail(GAL_ERR_WORKSPACE, "workspace too small");
   char* ws = static_cast<char*>(workspace);

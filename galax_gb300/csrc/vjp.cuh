@@ -39,7 +39,7 @@ __device__ __forceinline__ void comp_vjp(const DevComp& c, const double* x, cons
   const double ir2 = ir * ir;
   const double r = r2 * ir;
   const double xv = fma(d0, v[0], fma(d1, v[1], d2 * v[2]));
-  double g, gpr, dl1 = 0.0;
+  double g, gpr, dl1 = 0.0, dl2 = 0.0;
   switch (c.kind) {
     case KEPLER:
       g = c.Gm * ir2 * ir;
@@ -73,6 +73,14 @@ __device__ __forceinline__ void comp_vjp(const DevComp& c, const double* x, cons
       dl1 = -2.0 * c.l1 * g * iq * xv;
       break;
     }
+    case POWERLAW_CUTOFF: {
+      const PlcG t = plc_g(c, r2, ir, true, true);
+      g = t.g;
+      gpr = t.gpr;
+      dl1 = t.dg_drc * xv;
+      dl2 = t.dg_dalpha * xv;
+      break;
+    }
     default: {  // PLUMMER
       const double is = rsqrt(r2 + c.l2sq), is2 = is * is;
       g = c.Gm * is2 * is;
@@ -86,6 +94,7 @@ __device__ __forceinline__ void comp_vjp(const DevComp& c, const double* x, cons
   Hv[2] += fma(g, v[2], gpr * xv * d2);
   dp[0] += g * xv * c.inv_m;
   dp[1] += dl1;
+  dp[2] += dl2;
 }
 
 template <class TB, class Pot>

@@ -325,6 +325,97 @@ class LogarithmicPotential(AbstractSinglePotential):
         return [(self.kind, self.v_c, self.r_s, 0.0, self.origin)]
 
 
+# Smith et al. (2015) fits of a double-exponential / exponential-sech^2 disk by
+# three Miyamoto-Nagai disks, as tabulated in galax (builtin/mn3.py:27-51).
+# Rows: the three mass fractions, then the three a / h_R; columns: coefficients
+# of (b/h_R)^4 ... (b/h_R)^0. b/h_R itself is a cubic in h_z/h_R without a
+# constant term.
+_MN3_K_POSITIVE_DENSITY = (
+    (0.0036, -0.0330, 0.1117, -0.1335, 0.1749),
+    (-0.0131, 0.1090, -0.3035, 0.2921, -5.7976),
+    (-0.0048, 0.0454, -0.1425, 0.1012, 6.7120),
+    (-0.0158, 0.0993, -0.2070, -0.7089, 0.6445),
+    (-0.0319, 0.1514, -0.1279, -0.9325, 2.6836),
+    (-0.0326, 0.1816, -0.2943, -0.6329, 2.3193),
+)
+_MN3_K_NEGATIVE_DENSITY = (
+    (-0.0090, 0.0640, -0.1653, 0.1164, 1.9487),
+    (0.0173, -0.0903, 0.0877, 0.2029, -1.3077),
+    (-0.0051, 0.0287, -0.0361, -0.0544, 0.2242),
+    (-0.0358, 0.2610, -0.6987, -0.1193, 2.0074),
+    (-0.0830, 0.4992, -0.7967, -1.2966, 4.4441),
+    (-0.0247, 0.1718, -0.4124, -0.5944, 0.7333),
+)
+_MN3_B_EXPONENTIAL = (-0.269, 1.08, 1.092)  # (h_z/h_R)^3, ^2, ^1
+_MN3_B_SECH2 = (-0.033, 0.262, 0.659)
+
+
+class _AbstractMN3Potential(AbstractPotential):
+    """Three Miyamoto-Nagai disks standing in for an exponential disk (galax
+    builtin/mn3.py:54-133): the component table holds the three disks, so the
+    GPU evaluates exactly galax's sum."""
+
+    _b_coeffs: tuple = ()
+
+    def __init__(self, *, m_tot, h_R, h_z, positive_density: bool = False, origin=(0.0, 0.0, 0.0),  # noqa: N803
+                 units: Any = "galactic", constants=None):
+        super().__init__(units=units, constants=constants)
+        self.m_tot = _param("m_tot", m_tot)
+        self.h_R = _param("h_R", h_R)
+        self.h_z = _param("h_z", h_z)
+        self.positive_density = bool(positive_density)
+        self.origin = tuple(float(v) for v in origin)
+
+    def disks(self) -> list[tuple[float, float, float]]:
+        """(m_tot, a, b) of the three Miyamoto-Nagai disks."""
+        q = self.h_z / self.h_R
+        c3, c2, c1 = self._b_coeffs
+        b_over_hR = ((c3 * q + c2) * q + c1) * q
+        powers = (b_over_hR**4, b_over_hR**3, b_over_hR**2, b_over_hR, 1.0)
+        K = _MN3_K_POSITIVE_DENSITY if self.positive_density else _MN3_K_NEGATIVE_DENSITY
+        coef = [sum(k * x for k, x in zip(row, powers)) for row in K]
+        b = b_over_hR * self.h_R
+        return [(coef[i] * self.m_tot, coef[3 + i] * self.h_R, b) for i in range(3)]
+
+    def components(self):
+        return [(_lib.GAL_MIYAMOTO_NAGAI, m, a, b, self.origin) for (m, a, b) in self.disks()]
+
+    def _repr_params(self) -> str:
+        return (f"m_tot={self.m_tot!r}, h_R={self.h_R!r}, h_z={self.h_z!r}, "
+                f"positive_density={self.positive_density!r}")
+
+
+class MN3ExponentialPotential(_AbstractMN3Potential):
+    """Double-exponential disk as three Miyamoto-Nagai disks (galax builtin/mn3.py:136-165)."""
+
+    _b_coeffs = _MN3_B_EXPONENTIAL
+
+
+class MN3Sech2Potential(_AbstractMN3Potential):
+    """Exponential disk with a sech^2 vertical profile as three Miyamoto-Nagai
+    disks (galax builtin/mn3.py:168-197)."""
+
+    _b_coeffs = _MN3_B_SECH2
+
+
+class PowerLawCutoffPotential(AbstractSinglePotential):
+    """Spherical power law with an exponential cutoff, rho ~ (r_c / r)^alpha
+    exp(-(r / r_c)^2) (galax builtin/powerlawcutoff.py:26-120). Supported for
+    0 <= alpha < 2, where galax's potential is finite."""
+
+    kind = _lib.GAL_POWERLAW_CUTOFF
+    _names = ("m_tot", "alpha", "r_c")
+    _record = ("m_tot", "r_c", "alpha")  # order of (m, l1, l2) in the component table
+
+    def __init__(self, **kw):
+        super().__init__(**kw)
+        if not (0.0 <= self.alpha < 2.0):
+            raise ValueError("alpha must satisfy 0 <= alpha < 2 (galax's potential is not finite beyond)")
+
+    def components(self):
+        return [(self.kind, self.m_tot, self.r_c, self.alpha, self.origin)]
+
+
 def _flatten(p: AbstractPotential) -> list[AbstractPotential]:
     if isinstance(p, CompositePotential):
         out = []
@@ -410,6 +501,67 @@ class MilkyWayPotential(CompositePotential):
         )
 
 
+class BovyMWPotential2014(CompositePotential):
+    """galax's BovyMWPotential2014 (src/galax/potential/_src/builtin/milkyway.py:33-98):
+    Miyamoto-Nagai disk, power law with cutoff bulge, NFW halo, in that order."""
+
+    DEFAULTS = {
+        "disk": {"m_tot": 68_193_902_782.346756, "a": 3.0, "b": 0.28},
+        "bulge": {"m_tot": 4501365375.06545, "alpha": 1.8, "r_c": 1.9},
+        "halo": {"m": 4.3683325e11, "r_s": 16.0},
+    }
+
+    def __init__(self, disk=None, bulge=None, halo=None, *, units: Any = "galactic", constants=None):
+        def part(name, cls, given):
+            if isinstance(given, AbstractPotential):
+                return given
+            kw = dict(self.DEFAULTS[name])
+            kw.update(given or {})
+            return cls(**kw, units=units, constants=constants)
+
+        super().__init__(
+            {
+                "disk": part("disk", MiyamotoNagaiPotential, disk),
+                "bulge": part("bulge", PowerLawCutoffPotential, bulge),
+                "halo": part("halo", NFWPotential, halo),
+            },
+            units=units,
+            constants=constants,
+        )
+
+
+class MilkyWayPotential2022(CompositePotential):
+    """galax's MilkyWayPotential2022 (src/galax/potential/_src/builtin/milkyway.py:239-313):
+    an MN3Sech2 disk (positive density), NFW halo, Hernquist bulge and nucleus,
+    in that order (six table components)."""
+
+    DEFAULTS = {
+        "disk": {"m_tot": 4.7717e10, "h_R": 2.6, "h_z": 0.3, "positive_density": True},
+        "halo": {"m": 5.5427e11, "r_s": 15.626},
+        "bulge": {"m_tot": 5e9, "r_s": 1.0},
+        "nucleus": {"m_tot": 1.8142e9, "r_s": 0.0688867},
+    }
+
+    def __init__(self, disk=None, halo=None, bulge=None, nucleus=None, *, units: Any = "galactic", constants=None):
+        def part(name, cls, given):
+            if isinstance(given, AbstractPotential):
+                return given
+            kw = dict(self.DEFAULTS[name])
+            kw.update(given or {})
+            return cls(**kw, units=units, constants=constants)
+
+        super().__init__(
+            {
+                "disk": part("disk", MN3Sech2Potential, disk),
+                "halo": part("halo", NFWPotential, halo),
+                "bulge": part("bulge", HernquistPotential, bulge),
+                "nucleus": part("nucleus", HernquistPotential, nucleus),
+            },
+            units=units,
+            constants=constants,
+        )
+
+
 class TranslatedPotential(CompositePotential):
     """A potential shifted by a constant translation (src/galax/potential/_src/xfm/translate.py:28-87,
     constant translations only)."""
@@ -431,11 +583,11 @@ def from_component_array(arr: np.ndarray, G: float = G_GALACTIC) -> CompositePot
     cls = {_lib.GAL_KEPLER: KeplerPotential, _lib.GAL_HERNQUIST: HernquistPotential,
            _lib.GAL_MIYAMOTO_NAGAI: MiyamotoNagaiPotential, _lib.GAL_NFW: NFWPotential,
            _lib.GAL_PLUMMER: PlummerPotential, _lib.GAL_ISOCHRONE: IsochronePotential,
-           _lib.GAL_LOGARITHMIC: LogarithmicPotential}
+           _lib.GAL_LOGARITHMIC: LogarithmicPotential, _lib.GAL_POWERLAW_CUTOFF: PowerLawCutoffPotential}
     parts = {}
     for i, rec in enumerate(arr):
         k = int(rec["kind"])
-        names = cls[k]._names
+        names = getattr(cls[k], "_record", cls[k]._names)
         vals = [float(rec["m"]), float(rec["l1"]), float(rec["l2"])][: len(names)]
         parts[f"c{i}"] = cls[k](**dict(zip(names, vals)), origin=tuple(rec["origin"]), constants={"G": G})
     return CompositePotential(parts, constants={"G": G})

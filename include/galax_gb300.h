@@ -65,15 +65,20 @@ typedef enum gal_kind {
   GAL_NFW = 3,            /* Phi = -G m log(1 + r/r_s) / r .../builtin/nfw/base.py:326-338 */
   GAL_PLUMMER = 4,        /* Phi = -G m / sqrt(r^2 + b^2)  .../builtin/plummer.py:122-133 */
   GAL_ISOCHRONE = 5,      /* Phi = -G m / (b + sqrt(r^2 + b^2))  .../builtin/isochrone.py:61-110 */
-  GAL_LOGARITHMIC = 6     /* Phi = v_c^2 / 2 log(r_s^2 + r^2)    .../builtin/logarithmic.py:45-53 */
+  GAL_LOGARITHMIC = 6,    /* Phi = v_c^2 / 2 log(r_s^2 + r^2)    .../builtin/logarithmic.py:45-53 */
+  GAL_POWERLAW_CUTOFF = 7 /* rho ~ (r_c/r)^alpha exp(-(r/r_c)^2): Phi = -G m P(a1, s^2) / r
+                           * - G m Gamma(a2, s^2) / (r_c Gamma(a1)), s = r / r_c, a1 = (3 - alpha)/2,
+                           * a2 = 1 - alpha/2, P / Gamma(., .) the regularised lower / upper
+                           * incomplete gamma functions  .../builtin/powerlawcutoff.py:21-120 */
 } gal_kind;
 
 /* One component of a composite potential (src/galax/potential/_src/base_multi.py:39-55).
  * m  : m_tot (Kepler, Hernquist, Miyamoto-Nagai, Plummer, isochrone), m (NFW) or
  *      v_c in kpc/Myr (logarithmic)
- * l1 : r_s (Hernquist, NFW, Plummer, isochrone b, logarithmic) or a (Miyamoto-Nagai);
- *      unused for Kepler
- * l2 : b (Miyamoto-Nagai); unused otherwise
+ * l1 : r_s (Hernquist, NFW, Plummer, isochrone b, logarithmic), a (Miyamoto-Nagai) or
+ *      r_c (power law with cutoff); unused for Kepler
+ * l2 : b (Miyamoto-Nagai) or alpha (power law with cutoff, 0 <= alpha < 2: galax's
+ *      potential is not finite for alpha >= 2); unused otherwise
  * origin : constant translation of the component centre
  *          (src/galax/potential/_src/xfm/translate.py:28-87 with a constant shift). */
 typedef struct gal_component {

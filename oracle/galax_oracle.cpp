@@ -88,7 +88,8 @@ using std::log1p;
 // ---------------------------------------------------------------------------
 // Potential components. Same memory layout as the product's gal_component.
 // ---------------------------------------------------------------------------
-enum Kind : int32_t { KEPLER = 0, HERNQUIST = 1, MIYAMOTO_NAGAI = 2, NFW = 3, PLUMMER = 4, ISOCHRONE = 5, LOGARITHMIC = 6 };
+enum Kind : int32_t { KEPLER = 0, HERNQUIST = 1, MIYAMOTO_NAGAI = 2, NFW = 3, PLUMMER = 4, ISOCHRONE = 5, LOGARITHMIC = 6,
+                      POWERLAW_CUTOFF = 7 };
 
 struct Comp {
   int32_t kind;
@@ -101,6 +102,98 @@ struct Comp {
 static_assert(sizeof(Comp) == 56, "component layout");
 
 static const double TINY = std::numeric_limits<double>::min();  // 2.2250738585072014e-308
+
+// ---------------------------------------------------------------------------
+// Incomplete gamma function for the power-law-with-cutoff sphere (galax
+// builtin/powerlawcutoff.py:21-23, jax.scipy gammainc * gamma). Regularised
+// P(a, x) = gamma(a, x) / Gamma(a) by the power series (Abramowitz & Stegun
+// 6.5.29) for x < a + 1 and by the continued fraction of Q = 1 - P (A&S 6.5.31,
+// modified Lentz evaluation) otherwise; dP/da by differentiating the same
+// series / fraction term by term. psi = digamma by recurrence to x >= 8 and
+// the asymptotic series (A&S 6.3.18).
+// ---------------------------------------------------------------------------
+static double digamma(double x) {
+  double acc = 0.0;
+  while (x < 8.0) {
+    acc -= 1.0 / x;
+    x += 1.0;
+  }
+  const double i2 = 1.0 / (x * x);
+  return acc + std::log(x) - 0.5 / x -
+         i2 * (1.0 / 12 - i2 * (1.0 / 120 - i2 * (1.0 / 252 - i2 * (1.0 / 240 - i2 * (1.0 / 132)))));
+}
+
+struct GammaP {
+  double P, dPda;  // regularised lower incomplete gamma and its a-derivative
+  double upper;    // unregularised upper incomplete gamma Gamma(a, x)
+};
+
+static GammaP gamma_p(double a, double x) {
+  GammaP o{0.0, 0.0, std::tgamma(a)};
+  if (!(x > 0.0)) return o;
+  const double lga = std::lgamma(a), psi = digamma(a);
+  const double lx = std::log(x);
+  const double pre = std::exp(a * lx - x - lga);  // x^a e^-x / Gamma(a)
+  if (x < a + 1.0) {
+    double t = 1.0 / a, h = -1.0 / a, S = t, dS = t * h;
+    for (int n = 1; n < 1000; ++n) {
+      t *= x / (a + n);
+      h -= 1.0 / (a + n);
+      S += t;
+      dS += t * h;
+      if (std::fabs(t) < std::fabs(S) * 1e-17 && std::fabs(t * h) < std::fabs(dS) * 1e-17) break;
+    }
+    o.P = pre * S;
+    o.dPda = o.P * (lx - psi) + pre * dS;
+    o.upper = std::tgamma(a) * (1.0 - o.P);
+    return o;
+  }
+  // Lentz on (value, d/da) pairs
+  const double FP = 1e-300;
+  double b = x + 1.0 - a, db = -1.0;
+  double c = 1.0 / FP, dc = 0.0;
+  double d = 1.0 / b, dd = -db / (b * b);
+  double hh = d, dh = dd;
+  for (int i = 1; i < 1000; ++i) {
+    const double an = -i * (i - a), dan = i;
+    b += 2.0;
+    double dpre = an * d + b, ddpre = dan * d + an * dd + db;
+    if (std::fabs(dpre) < FP) dpre = FP;
+    const double cn = b + an / c, dcn = db + (dan * c - an * dc) / (c * c);
+    c = std::fabs(cn) < FP ? FP : cn;
+    dc = dcn;
+    d = 1.0 / dpre;
+    dd = -ddpre / (dpre * dpre);
+    const double del = d * c, ddel = dd * c + d * dc;
+    dh = dh * del + hh * ddel;
+    hh *= del;
+    // the value can converge before its a-derivative (a fraction that ends,
+    // an = 0, at integer a): both must have settled
+    if (std::fabs(del - 1.0) < 1e-17 && std::fabs(ddel) < 1e-17 * (1.0 + std::fabs(dh / hh))) break;
+  }
+  const double Q = pre * hh;
+  o.P = 1.0 - Q;
+  o.dPda = -(Q * (lx - psi) + pre * dh);
+  o.upper = std::exp(a * lx - x) * hh;
+  return o;
+}
+
+// g(r) of grad Phi = g(r) x for the power law with cutoff: g = G M P(a1, s^2) / r^3,
+// a1 = 3/2 - alpha/2, s = r / r_c, and its partials.
+struct PlcTerms {
+  double g, gpr, dg_drc, dg_dalpha;
+};
+static PlcTerms plc_terms(double Gm, double rc, double alpha, double r2) {
+  const double a1 = 1.5 - 0.5 * alpha, x = r2 / (rc * rc), r = std::sqrt(r2);
+  const GammaP gp = gamma_p(a1, x);
+  const double dens = std::exp(a1 * std::log(x) - x - std::lgamma(a1));  // x^a1 e^-x / Gamma(a1)
+  PlcTerms t;
+  t.g = Gm * gp.P / (r2 * r);
+  t.gpr = 2.0 * Gm * dens / (r2 * r2 * r) - 3.0 * t.g / r2;
+  t.dg_drc = -2.0 * Gm * dens / (r2 * r * rc);
+  t.dg_dalpha = -0.5 * Gm * gp.dPda / (r2 * r);
+  return t;
+}
 
 template <class T>
 inline T rsph2(const T* x) { return x[0] * x[0] + x[1] * x[1] + x[2] * x[2]; }
@@ -139,6 +232,12 @@ T comp_potential(const Comp& c, double G, const T* xin) {
     case LOGARITHMIC: {
       T r = sqrt(rsph2(x) + T(TINY));
       return T(0.5) * T(c.m) * T(c.m) * log(T(c.l1) * T(c.l1) + r * r);
+    }
+    case POWERLAW_CUTOFF: {  // -G M P(a1, s^2) / r - G M Gamma(a2, s^2) / (r_c Gamma(a1)), a2 = 1 - alpha/2
+      const double rv = std::sqrt(val(rsph2(x)) + TINY), rc = c.l1, a1 = 1.5 - 0.5 * c.l2;
+      const double s2 = (rv / rc) * (rv / rc);
+      const GammaP p1 = gamma_p(a1, s2), p2 = gamma_p(1.0 - 0.5 * c.l2, s2);
+      return T(-val(Gm) * p1.P / rv - val(Gm) * p2.upper / (rc * std::tgamma(a1)));
     }
   }
   return T(0);
@@ -179,6 +278,7 @@ void comp_gradient(const Comp& c, double G, const T* xin, T* g) {
       break;
     }
     case LOGARITHMIC: { f = T(c.m) * T(c.m) / (r2 + T(c.l1) * T(c.l1)); break; }
+    case POWERLAW_CUTOFF: { f = T(plc_terms(val(Gm), c.l1, c.l2, val(r2)).g); break; }
     default: f = T(0);
   }
   g[0] += f * x[0];
@@ -242,6 +342,12 @@ void comp_hessian(const Comp& c, double G, const double* xin, double* H) {
       gpr = -2.0 * g / q;
       break;
     }
+    case POWERLAW_CUTOFF: {
+      const PlcTerms t = plc_terms(Gm, c.l1, c.l2, r2);
+      g = t.g;
+      gpr = t.gpr;
+      break;
+    }
   }
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) H[3 * i + j] += gpr * x[i] * x[j];
@@ -289,6 +395,12 @@ void comp_dgrad_dparams_dot(const Comp& c, double G, const double* xin, const do
     case LOGARITHMIC: {  // d/dr_s [v^2 / (r_s^2 + r^2)] = -2 r_s v^2 / (r_s^2 + r^2)^2
       double q = r2 + c.l1 * c.l1;
       out[1] += -2.0 * c.l1 * c.m * c.m / (q * q) * xv;
+      break;
+    }
+    case POWERLAW_CUTOFF: {
+      const PlcTerms t = plc_terms(Gm, c.l1, c.l2, r2);
+      out[1] += t.dg_drc * xv;
+      out[2] += t.dg_dalpha * xv;
       break;
     }
     default: break;
@@ -643,6 +755,14 @@ static SolveOut solve_group(const Pot& P, const OrcSolverCfg& cfg, const double*
 extern "C" {
 
 int orc_abi_version() { return 1; }
+
+// P(a, x), dP/da and Gamma(a, x) (see gamma_p), for tests.
+void orc_gamma_p(double a, double x, double* out) {
+  const GammaP g = gamma_p(a, x);
+  out[0] = g.P;
+  out[1] = g.dPda;
+  out[2] = g.upper;
+}
 
 // Phi, grad Phi, Hessian at n points (x: n x 3 row-major).
 void orc_potential(const Comp* comps, int ncomp, double G, const double* x, int64_t n, double* out) {

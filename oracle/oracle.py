@@ -18,7 +18,7 @@ import numpy as np
 
 from . import build_oracle
 
-KEPLER, HERNQUIST, MIYAMOTO_NAGAI, NFW, PLUMMER, ISOCHRONE, LOGARITHMIC = range(7)
+KEPLER, HERNQUIST, MIYAMOTO_NAGAI, NFW, PLUMMER, ISOCHRONE, LOGARITHMIC, POWERLAW_CUTOFF = range(8)
 
 G_GALACTIC = 4.498502151469553e-12  # kpc^3 / (Msun Myr^2), astropy CODATA-2018 G
 
@@ -121,6 +121,58 @@ def comps(records) -> np.ndarray:
         a[i]["l2"] = l2
         a[i]["origin"] = origin
     return a
+
+
+# Smith et al. (2015) three-Miyamoto-Nagai fits as galax tabulates them
+# (src/galax/potential/_src/builtin/mn3.py:27-51): mass fractions and a / h_R
+# as quartics in b / h_R, which is a cubic in h_z / h_R.
+MN3_K = {
+    True: np.array([[0.0036, -0.0330, 0.1117, -0.1335, 0.1749], [-0.0131, 0.1090, -0.3035, 0.2921, -5.7976],
+                    [-0.0048, 0.0454, -0.1425, 0.1012, 6.7120], [-0.0158, 0.0993, -0.2070, -0.7089, 0.6445],
+                    [-0.0319, 0.1514, -0.1279, -0.9325, 2.6836], [-0.0326, 0.1816, -0.2943, -0.6329, 2.3193]]),
+    False: np.array([[-0.0090, 0.0640, -0.1653, 0.1164, 1.9487], [0.0173, -0.0903, 0.0877, 0.2029, -1.3077],
+                     [-0.0051, 0.0287, -0.0361, -0.0544, 0.2242], [-0.0358, 0.2610, -0.6987, -0.1193, 2.0074],
+                     [-0.0830, 0.4992, -0.7967, -1.2966, 4.4441], [-0.0247, 0.1718, -0.4124, -0.5944, 0.7333]]),
+}
+MN3_B = {"exponential": np.array([-0.269, 1.08, 1.092]), "sech2": np.array([-0.033, 0.262, 0.659])}
+
+
+def mn3(m_tot: float, h_R: float, h_z: float, profile: str = "sech2", positive_density: bool = False):  # noqa: N803
+    """Component records of galax's MN3ExponentialPotential / MN3Sech2Potential
+    (builtin/mn3.py:54-133): three Miyamoto-Nagai disks."""
+    q = h_z / h_R
+    b_hR = MN3_B[profile] @ np.array([q**3, q**2, q])
+    pv = MN3_K[bool(positive_density)] @ np.vander([b_hR], N=5)[0]
+    return [(MIYAMOTO_NAGAI, pv[i] * m_tot, pv[3 + i] * h_R, b_hR * h_R) for i in range(3)]
+
+
+def milky_way_2022() -> np.ndarray:
+    """galax MilkyWayPotential2022 defaults (builtin/milkyway.py:239-313): MN3Sech2
+    disk (positive density), NFW halo, Hernquist bulge and nucleus."""
+    return comps(mn3(4.7717e10, 2.6, 0.3, "sech2", True) + [
+        (NFW, 5.5427e11, 15.626, 0.0),
+        (HERNQUIST, 5e9, 1.0, 0.0),
+        (HERNQUIST, 1.8142e9, 0.0688867, 0.0),
+    ])
+
+
+def gamma_p(a: float, x: float):
+    """(P(a, x), dP/da, Gamma(a, x)) from the oracle's incomplete gamma."""
+    L = lib()
+    out = np.zeros(3)
+    L.orc_gamma_p.argtypes = [C.c_double, C.c_double, np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")]
+    L.orc_gamma_p(float(a), float(x), out)
+    return out
+
+
+def bovy_mw_2014() -> np.ndarray:
+    """galax BovyMWPotential2014 defaults (builtin/milkyway.py:33-98): Miyamoto-Nagai
+    disk, power law with cutoff bulge (alpha 1.8, r_c 1.9 kpc), NFW halo."""
+    return comps([
+        (MIYAMOTO_NAGAI, 68_193_902_782.346756, 3.0, 0.28),
+        (POWERLAW_CUTOFF, 4501365375.06545, 1.9, 1.8),
+        (NFW, 4.3683325e11, 16.0, 0.0),
+    ])
 
 
 def milky_way(**over) -> np.ndarray:

@@ -29,6 +29,11 @@ POTENTIAL_SPECS = [
     ("milky_way", "tests/unit/potential/builtin/test_milkywaypotential.py", [43], [48], [61, 62, 63]),
     ("isochrone", "tests/unit/potential/builtin/test_isochrone.py", [31], [35], [46, 47, 48]),
     ("logarithmic", "tests/unit/potential/builtin/test_logarithmic.py", [38], [43], [55, 56, 57]),
+    ("mn3_exponential", "tests/unit/potential/builtin/test_mn3.py", [49], [54], [67, 68, 69]),
+    ("mn3_sech2", "tests/unit/potential/builtin/test_mn3.py", [124], [129], [142, 143, 144]),
+    ("milky_way_2022", "tests/unit/potential/builtin/test_milkywaypotential2022.py", [43], [49], [64, 65, 66]),
+    ("powerlaw_cutoff", "tests/unit/potential/builtin/test_powerlawcutoff.py", [100], [104], [115, 116, 117]),
+    ("bovy_mw_2014", "tests/unit/potential/builtin/test_bovymwpotential2014.py", [32], [36], [49, 50, 51]),
 ]
 # density and tidal-tensor goldens of the same fixtures: (density line, tidal tensor lines)
 DERIVED_SPECS = {
@@ -39,7 +44,14 @@ DERIVED_SPECS = {
     "milky_way": ([54], [76, 77, 78]),
     "isochrone": ([40], [61, 62, 63]),
     "logarithmic": ([48], [71, 72, 73]),
+    "mn3_exponential": ([61], [82, 83, 84]),
+    "mn3_sech2": ([136], [157, 158, 159]),
+    "milky_way_2022": ([57], [79, 80, 81]),
+    "powerlaw_cutoff": ([109], [130, 131, 132]),
+    "bovy_mw_2014": ([42], [64, 65, 66]),
 }
+# densities printed in Msun / pc^3 instead of galactic units (Msun / kpc^3)
+DENSITY_SCALE = {"bovy_mw_2014": 1e9}
 # parameters of each fixture: tests/unit/potential/builtin/test_common.py
 # (m_tot = m = 1e12 Msun, r_s = a = b = 1 kpc); MilkyWay uses its defaults.
 POTENTIAL_PARAMS = {
@@ -51,6 +63,13 @@ POTENTIAL_PARAMS = {
     "isochrone": {"kind": "isochrone", "m": 1e12, "l1": 1.0, "l2": 0.0},
     # v_c = 220 km/s (test_common.py:359-360), stored in m in kpc/Myr
     "logarithmic": {"kind": "logarithmic", "m": 220 * KMS, "l1": 1.0, "l2": 0.0},
+    # m_tot = 1e12 Msun, h_R = h_z = 1 kpc, positive_density False (test_common.py:26-27, 305-306, 331-332)
+    "mn3_exponential": {"kind": "mn3_exponential", "m": 1e12, "h_R": 1.0, "h_z": 1.0, "positive_density": False},
+    "mn3_sech2": {"kind": "mn3_sech2", "m": 1e12, "h_R": 1.0, "h_z": 1.0, "positive_density": False},
+    "milky_way_2022": {"kind": "milky_way_2022"},
+    # m_tot = 1e12 Msun, alpha = 0.9, r_c = 1 kpc (test_powerlawcutoff.py:21-22, 47-48)
+    "powerlaw_cutoff": {"kind": "powerlaw_cutoff", "m": 1e12, "l1": 1.0, "l2": 0.9},
+    "bovy_mw_2014": {"kind": "bovy_mw_2014"},
 }
 
 
@@ -90,7 +109,7 @@ def main(root: Path) -> None:
         dens = numbers(root, rel, ldens)
         tidal = numbers(root, rel, ltidal)
         assert len(dens) == 1 and len(tidal) == 9, (name, dens, tidal)
-        g["potentials"][name]["density"] = dens[0]
+        g["potentials"][name]["density"] = dens[0] * DENSITY_SCALE.get(name, 1.0)
         g["potentials"][name]["tidal_tensor"] = tidal
         g["potentials"][name]["cite_derived"] = f"{rel}:{ldens[0]},{ltidal[0]}-{ltidal[-1]}"
 

@@ -85,6 +85,14 @@ def test_validation_without_gpu(lib):
     bad[0]["l1"] = 0.0
     assert lib.gal_potential_create(bad.ctypes.data, 1, 1.0, C.byref(h)) == 1
     assert lib.gal_potential_create(bad.ctypes.data, 0, 1.0, C.byref(h)) == 1
+    bad[0]["kind"] = _lib.GAL_MIYAMOTO_NAGAI  # a <= -b would let sqrt(z^2 + b^2) + a vanish
+    bad[0]["l1"], bad[0]["l2"] = -1.0, 1.0
+    assert lib.gal_potential_create(bad.ctypes.data, 1, 1.0, C.byref(h)) == 1
+    bad[0]["kind"] = _lib.GAL_POWERLAW_CUTOFF  # alpha >= 2 or r_c <= 0: galax's potential is not finite
+    bad[0]["l1"], bad[0]["l2"] = 1.0, 2.0
+    assert lib.gal_potential_create(bad.ctypes.data, 1, 1.0, C.byref(h)) == 1
+    bad[0]["l1"], bad[0]["l2"] = 0.0, 1.0
+    assert lib.gal_potential_create(bad.ctypes.data, 1, 1.0, C.byref(h)) == 1
     nbytes = C.c_size_t()
     cfg = _lib.solver_config(8, False, dt0=1.0)
     assert lib.gal_integrate_workspace_size(C.byref(cfg), 10, C.byref(nbytes)) == 0 and nbytes.value >= 8
@@ -139,3 +147,21 @@ def test_flop_constants_match_counted_oracle():
         c = np.concatenate([O.milky_way(), O.comps([(O.PLUMMER, 1e5, 0.02, 0.0, (1.0, 2.0, 3.0))])])
         _, s = O.count_ops(c, method)
         assert sum(s.values()) == flops.STEP_FLOPS_MW_PLUMMER[method]
+
+
+def test_mn3_and_milky_way_2022_component_tables():
+    """The front end expands MN3 disks into the same three Miyamoto-Nagai
+    components as the oracle's restatement of galax's fit (whose potentials
+    match galax's goldens), and MilkyWayPotential2022 into six components."""
+    from galax_gb300 import potential as P
+
+    for cls, profile in ((P.MN3ExponentialPotential, "exponential"), (P.MN3Sech2Potential, "sech2")):
+        for pos in (False, True):
+            got = cls(m_tot=3e10, h_R=2.5, h_z=0.4, positive_density=pos).component_array()
+            want = O.comps(O.mn3(3e10, 2.5, 0.4, profile, pos))
+            for f in ("kind", "m", "l1", "l2"):
+                np.testing.assert_allclose(got[f], want[f], rtol=1e-14)
+    got = P.MilkyWayPotential2022().component_array()
+    want = O.milky_way_2022()
+    for f in ("kind", "m", "l1", "l2"):
+        np.testing.assert_allclose(got[f], want[f], rtol=1e-14)

@@ -73,6 +73,8 @@ def _kinds():
         (O.PLUMMER, 1e8, 0.5, 0, (4.0, 1.0, -2.0)),
         (O.ISOCHRONE, 2e10, 1.5, 0, (-1.0, 0.5, 0.2)),
         (O.LOGARITHMIC, 0.2, 2.0, 0),
+        (O.POWERLAW_CUTOFF, 4.5e9, 1.9, 1.8, (0.5, -0.3, 0.2)),
+        (O.POWERLAW_CUTOFF, 2e9, 0.7, 0.4),
     ])
 
 
@@ -110,6 +112,25 @@ def test_reference_potential_goldens_on_gpu(gx, goldens):
         np.testing.assert_allclose(pot.hessian(x)[0].ravel(), g["hessian"], **g["tol"])
         np.testing.assert_allclose(pot.density(x)[0], g["density"], rtol=1e-5, atol=1e-8)
         np.testing.assert_allclose(pot.tidal_tensor(x)[0].ravel(), g["tidal_tensor"], rtol=1e-5, atol=1e-8)
+
+
+def test_catalogue_classes_on_gpu(gx, goldens):
+    """The front-end classes themselves (not the oracle's component tables)
+    against galax's goldens."""
+    cases = {
+        "mn3_exponential": gx.MN3ExponentialPotential(m_tot=1e12, h_R=1.0, h_z=1.0),
+        "mn3_sech2": gx.MN3Sech2Potential(m_tot=1e12, h_R=1.0, h_z=1.0),
+        "milky_way_2022": gx.MilkyWayPotential2022(),
+        "powerlaw_cutoff": gx.PowerLawCutoffPotential(m_tot=1e12, alpha=0.9, r_c=1.0),
+        "bovy_mw_2014": gx.BovyMWPotential2014(),
+    }
+    for name, pot in cases.items():
+        g = goldens["potentials"][name]
+        x = np.array([g["x"]])
+        np.testing.assert_allclose(pot.potential(x)[0], g["potential"], **g["tol"])
+        np.testing.assert_allclose(pot.gradient(x)[0], g["gradient"], **g["tol"])
+        np.testing.assert_allclose(pot.hessian(x)[0].ravel(), g["hessian"], **g["tol"])
+        np.testing.assert_allclose(pot.density(x)[0], g["density"], rtol=1e-5, atol=1e-8)
 
 
 def test_radial_derivatives_circular_velocity_and_enclosed_mass(gx):
@@ -334,14 +355,15 @@ def test_launch_shapes_give_identical_results(gx):
 
 
 # ------------------------------------------------------------------ adjoint
-@pytest.mark.parametrize("which", ["milky_way", "table", "isochrone_logarithmic"])
+@pytest.mark.parametrize("which", ["milky_way", "table", "isochrone_logarithmic", "powerlaw_cutoff"])
 def test_adjoint_matches_oracle(gx, which):
     import torch
 
     from galax_gb300.adjoint import orbit_adjoint
 
     extra = {"milky_way": [], "table": [(O.PLUMMER, 1e9, 0.8, 0, (6.0, 2.0, 0.5))],
-             "isochrone_logarithmic": [(O.ISOCHRONE, 3e10, 1.2, 0, (1.0, -0.5, 0.3)), (O.LOGARITHMIC, 0.05, 4.0, 0)]}
+             "isochrone_logarithmic": [(O.ISOCHRONE, 3e10, 1.2, 0, (1.0, -0.5, 0.3)), (O.LOGARITHMIC, 0.05, 4.0, 0)],
+             "powerlaw_cutoff": [(O.POWERLAW_CUTOFF, 4.5e9, 1.9, 1.8, (0.3, 0.2, -0.1))]}
     comps = np.concatenate([O.milky_way(), O.comps(extra[which])]) if extra[which] else O.milky_way()
     pot = _pot(gx, comps)
     y0 = _ics(96, 31)

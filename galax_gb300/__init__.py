@@ -27,6 +27,7 @@ from .potential import (
     HernquistPotential,
     IsochronePotential,
     KeplerPotential,
+    LinearParameter,
     LogarithmicPotential,
     MilkyWayPotential,
     MilkyWayPotential2022,
@@ -43,7 +44,7 @@ __all__ = [
     "GalaxGB300Error", "dynamics", "mockstream", "potential", "ConstantStepSize", "Dopri5", "Dopri8", "Integrator",
     "Orbit", "OrbitSolver", "PhaseSpaceCoordinate", "PIDController", "evaluate_orbit", "integrate_orbit",
     "ChenStreamDF", "Fardal2015DF", "FardalStreamDF", "MockStreamGenerator", "StreamSimulator",
-    "BovyMWPotential2014", "CompositePotential", "HernquistPotential", "IsochronePotential", "KeplerPotential", "LogarithmicPotential",
+    "BovyMWPotential2014", "CompositePotential", "HernquistPotential", "IsochronePotential", "KeplerPotential", "LinearParameter", "LogarithmicPotential",
     "MilkyWayPotential", "MilkyWayPotential2022", "MiyamotoNagaiPotential", "MN3ExponentialPotential",
     "MN3Sech2Potential", "NFWPotential", "PlummerPotential", "PowerLawCutoffPotential", "TranslatedPotential",
 ]

@@ -109,6 +109,7 @@ SIGNATURES = {
                                  C.c_void_p]),
     "gal_stream_grad": (C.c_int, [C.c_void_p, C.POINTER(StreamConfig), _DP, _DP, _DP, _DP, _DP, _DP, _VP,
                                   C.c_size_t, C.c_void_p]),
+    "gal_potential_set_linear": (C.c_int, [C.c_void_p, _DP]),
     "gal_stream_df_sample": (C.c_int, [C.c_void_p, C.c_int32, _DP, _DP, _DP, _DP, C.c_int64, _DP, _DP, _DP,
                                        C.c_void_p]),
     "gal_mlp_num_params": (C.c_int64, []),

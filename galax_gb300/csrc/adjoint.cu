@@ -217,6 +217,7 @@ gal_status gal_adjoint(const gal_potential* pot, const gal_solver_config* cfg, c
                        double* grad_params, int32_t k_ckpt, int64_t n, void* workspace, size_t workspace_bytes,
                        gal_stream_t stream) {
   if (!pot) return fail(GAL_ERR_INVALID_ARGUMENT, "potential is NULL");
+  if (time_dependent(pot)) return fail(GAL_ERR_UNSUPPORTED, "time-dependent parameters: evaluation and gal_integrate only");
   gal_status st = validate_cfg(cfg);
   if (st != GAL_OK) return st;
   if (cfg->adaptive) return fail(GAL_ERR_UNSUPPORTED, "the adjoint needs a constant step (adaptive = 0)");

@@ -44,41 +44,8 @@ int device_sm_count() {
   return cache[dev];
 }
 
-// digamma by upward recurrence to x >= 8 and the asymptotic series
-// (Abramowitz & Stegun 6.3.18); host side, for the power law with cutoff.
-static double digamma_host(double x) {
-  double acc = 0.0;
-  while (x < 8.0) {
-    acc -= 1.0 / x;
-    x += 1.0;
-  }
-  const double i2 = 1.0 / (x * x);
-  return acc + std::log(x) - 0.5 / x -
-         i2 * (1.0 / 12 - i2 * (1.0 / 120 - i2 * (1.0 / 252 - i2 * (1.0 / 240 - i2 * (1.0 / 132)))));
-}
-
 static DevComp fold(const gal_component& c, double G) {
-  DevComp d{};
-  d.kind = c.kind;
-  d.centered = (c.origin[0] == 0.0 && c.origin[1] == 0.0 && c.origin[2] == 0.0) ? 1 : 0;
-  const bool log_kind = c.kind == LOGARITHMIC;  // m holds v_c: Phi scales with v_c^2, not G m
-  d.Gm = log_kind ? c.m * c.m : G * c.m;
-  d.l1 = c.l1;
-  d.l2 = c.l2;
-  d.l2sq = (c.kind == PLUMMER || c.kind == ISOCHRONE || log_kind) ? c.l1 * c.l1 : c.l2 * c.l2;
-  d.inv_l1 = (c.kind == NFW) ? 1.0 / c.l1 : 0.0;
-  d.inv_m = (c.m != 0.0) ? (log_kind ? 2.0 / c.m : 1.0 / c.m) : 0.0;
-  d.ox = c.origin[0];
-  d.oy = c.origin[1];
-  d.oz = c.origin[2];
-  if (c.kind == POWERLAW_CUTOFF) {
-    const double a1 = 1.5 - 0.5 * c.l2, a2 = 1.0 - 0.5 * c.l2;
-    d.l2sq = 1.0 / std::tgamma(a1);
-    d.inv_l1 = 1.0 / (c.l1 * c.l1);
-    d.aux0 = digamma_host(a1);
-    d.aux1 = std::tgamma(a2);
-  }
-  return d;
+  return fold_comp(c.kind, c.m, c.l1, c.l2, c.origin[0], c.origin[1], c.origin[2], G);
 }
 
 static bool milky_way_shape(const gal_component* c, int n) {
@@ -144,11 +111,12 @@ __global__ void k_eval_gradient(Pot pot, const double* __restrict__ x, int64_t n
   }
 }
 
-__global__ void k_eval_gradient_table(const DevComp* comps, int ncomp, const double* __restrict__ x, int64_t n,
-                                      double* __restrict__ out, double sign) {
+__global__ void k_eval_gradient_table(const DevComp* comps, const DevLinear* lin, double t, int ncomp,
+                                      const double* __restrict__ x, int64_t n, double* __restrict__ out,
+                                      double sign) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   DevComp* s = reinterpret_cast<DevComp*>(smem_raw);
-  for (int i = threadIdx.x; i < ncomp; i += blockDim.x) s[i] = comps[i];
+  for (int i = threadIdx.x; i < ncomp; i += blockDim.x) s[i] = lin ? comp_at_time(comps[i], lin[i], t) : comps[i];
   __syncthreads();
   const TablePot pot{s, ncomp};
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -160,11 +128,17 @@ __global__ void k_eval_gradient_table(const DevComp* comps, int ncomp, const dou
   }
 }
 
-__global__ void k_eval_phi(const DevComp* comps, int ncomp, const double* __restrict__ x, int64_t n,
-                           double* __restrict__ out) {
+// Components staged into shared memory, refolded at time t when time-dependent.
+__device__ __forceinline__ void stage_at_time(const DevComp* comps, const DevLinear* lin, int ncomp, double t,
+                                              DevComp* s) {
+  for (int i = threadIdx.x; i < ncomp; i += blockDim.x) s[i] = lin ? comp_at_time(comps[i], lin[i], t) : comps[i];
+}
+
+__global__ void k_eval_phi(const DevComp* comps, const DevLinear* lin, double t, int ncomp,
+                           const double* __restrict__ x, int64_t n, double* __restrict__ out) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   DevComp* s = reinterpret_cast<DevComp*>(smem_raw);
-  for (int i = threadIdx.x; i < ncomp; i += blockDim.x) s[i] = comps[i];
+  stage_at_time(comps, lin, ncomp, t, s);
   __syncthreads();
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     double phi = 0.0;
@@ -173,11 +147,11 @@ __global__ void k_eval_phi(const DevComp* comps, int ncomp, const double* __rest
   }
 }
 
-__global__ void k_eval_hessian(const DevComp* comps, int ncomp, const double* __restrict__ x, int64_t n,
-                               double* __restrict__ out) {
+__global__ void k_eval_hessian(const DevComp* comps, const DevLinear* lin, double t, int ncomp,
+                               const double* __restrict__ x, int64_t n, double* __restrict__ out) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   DevComp* s = reinterpret_cast<DevComp*>(smem_raw);
-  for (int i = threadIdx.x; i < ncomp; i += blockDim.x) s[i] = comps[i];
+  stage_at_time(comps, lin, ncomp, t, s);
   __syncthreads();
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     double H[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
@@ -333,8 +307,53 @@ gal_status gal_potential_create(const gal_component* comps, int32_t n, double G,
 gal_status gal_potential_destroy(gal_potential* p) {
   if (!p) return GAL_OK;
   cudaError_t e = cudaFree(p->d_comps);
+  if (p->d_lin) {
+    const cudaError_t e2 = cudaFree(p->d_lin);
+    if (e == cudaSuccess) e = e2;
+  }
   delete p;
   return e == cudaSuccess ? GAL_OK : cuda_fail(e, "cudaFree(component table)");
+}
+
+gal_status gal_potential_set_linear(gal_potential* p, const double* slopes) {
+  if (!p) return fail(GAL_ERR_INVALID_ARGUMENT, "potential is NULL");
+  if (slopes) {
+    for (int i = 0; i < 3 * p->n; ++i)
+      if (!std::isfinite(slopes[i])) return fail(GAL_ERR_INVALID_ARGUMENT, "non-finite slope");
+  }
+  bool any = false;
+  std::vector<DevLinear> h(p->n);
+  for (int i = 0; i < p->n; ++i) {
+    const gal_component& c = p->comps[i];
+    DevLinear& L = h[i];
+    L.kind = c.kind;
+    L.m0 = c.m;
+    L.l10 = c.l1;
+    L.l20 = c.l2;
+    L.G = p->G;
+    L.dm = slopes ? slopes[3 * i] : 0.0;
+    L.dl1 = slopes ? slopes[3 * i + 1] : 0.0;
+    L.dl2 = slopes ? slopes[3 * i + 2] : 0.0;
+    L.active = (L.dm != 0.0 || L.dl1 != 0.0 || L.dl2 != 0.0) ? 1 : 0;
+    any = any || L.active;
+  }
+  if (p->d_lin) {
+    cudaError_t e = cudaFree(p->d_lin);
+    p->d_lin = nullptr;
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFree(linear table)");
+  }
+  if (any) {
+    cudaError_t e = cudaMalloc(&p->d_lin, sizeof(DevLinear) * p->n);
+    if (e != cudaSuccess) {
+      p->d_lin = nullptr;
+      return cuda_fail(e, "cudaMalloc(linear table)");
+    }
+    e = cudaMemcpy(p->d_lin, h.data(), sizeof(DevLinear) * p->n, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(linear table)");
+  }
+  // the specialised Milky Way model has constant parameters
+  p->is_mw = !any && milky_way_shape(p->comps.data(), p->n);
+  return GAL_OK;
 }
 
 gal_status gal_potential_update(gal_potential* p, const gal_component* comps, int32_t n, gal_stream_t stream) {
@@ -353,16 +372,28 @@ gal_status gal_potential_update(gal_potential* p, const gal_component* comps, in
   e = cudaStreamSynchronize((cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
   p->comps.assign(comps, comps + n);
-  p->is_mw = milky_way_shape(comps, n);
-  p->mw = p->is_mw ? mw_params(comps, p->G) : MWParams{};
+  p->is_mw = !p->d_lin && milky_way_shape(comps, n);
+  p->mw = milky_way_shape(comps, n) ? mw_params(comps, p->G) : MWParams{};
+  if (p->d_lin) {  // new values at t = 0, same slopes
+    std::vector<DevLinear> L(n);
+    e = cudaMemcpy(L.data(), p->d_lin, sizeof(DevLinear) * n, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(linear table)");
+    for (int i = 0; i < n; ++i) {
+      L[i].m0 = comps[i].m;
+      L[i].l10 = comps[i].l1;
+      L[i].l20 = comps[i].l2;
+    }
+    e = cudaMemcpy(p->d_lin, L.data(), sizeof(DevLinear) * n, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(linear table)");
+  }
   return GAL_OK;
 }
 
 int32_t gal_potential_num_components(const gal_potential* p) { return p ? p->n : 0; }
 int32_t gal_potential_is_milky_way(const gal_potential* p) { return p && p->is_mw ? 1 : 0; }
 
-static gal_status eval_grad_common(const gal_potential* p, const double* x, int64_t n, double* out, double sign,
-                                   gal_stream_t stream) {
+static gal_status eval_grad_common(const gal_potential* p, const double* x, double t, int64_t n, double* out,
+                                   double sign, gal_stream_t stream) {
   if (!p || (!x && n) || (!out && n) || n < 0) return fail(GAL_ERR_INVALID_ARGUMENT, "bad pointer or size");
   if (n == 0) return GAL_OK;
   const int block = 256;
@@ -374,7 +405,8 @@ static gal_status eval_grad_common(const gal_potential* p, const double* x, int6
     const size_t smem = sizeof(DevComp) * p->n;
     if (smem > 48 * 1024)
       cudaFuncSetAttribute(k_eval_gradient_table, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_eval_gradient_table<<<grid, block, smem, (cudaStream_t)stream>>>(p->d_comps, p->n, x, n, out, sign);
+    k_eval_gradient_table<<<grid, block, smem, (cudaStream_t)stream>>>(p->d_comps, p->d_lin, t, p->n, x, n, out,
+                                                                       sign);
   }
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? GAL_OK : cuda_fail(e, "gradient kernel launch");
@@ -382,19 +414,16 @@ static gal_status eval_grad_common(const gal_potential* p, const double* x, int6
 
 gal_status gal_eval_gradient(const gal_potential* p, const double* x, double t, int64_t n, double* out,
                              gal_stream_t stream) {
-  (void)t;
-  return eval_grad_common(p, x, n, out, 1.0, stream);
+  return eval_grad_common(p, x, t, n, out, 1.0, stream);
 }
 
 gal_status gal_eval_acceleration(const gal_potential* p, const double* x, double t, int64_t n, double* out,
                                  gal_stream_t stream) {
-  (void)t;
-  return eval_grad_common(p, x, n, out, -1.0, stream);
+  return eval_grad_common(p, x, t, n, out, -1.0, stream);
 }
 
 gal_status gal_eval_potential(const gal_potential* p, const double* x, double t, int64_t n, double* phi,
                               gal_stream_t stream) {
-  (void)t;
   if (!p || (!x && n) || (!phi && n) || n < 0) return fail(GAL_ERR_INVALID_ARGUMENT, "bad pointer or size");
   if (n == 0) return GAL_OK;
   const int block = 256;
@@ -402,14 +431,13 @@ gal_status gal_eval_potential(const gal_potential* p, const double* x, double t,
   grid_for(n, block, &grid);
   const size_t smem = sizeof(DevComp) * p->n;
   if (smem > 48 * 1024) cudaFuncSetAttribute(k_eval_phi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  k_eval_phi<<<grid, block, smem, (cudaStream_t)stream>>>(p->d_comps, p->n, x, n, phi);
+  k_eval_phi<<<grid, block, smem, (cudaStream_t)stream>>>(p->d_comps, p->d_lin, t, p->n, x, n, phi);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? GAL_OK : cuda_fail(e, "potential kernel launch");
 }
 
 gal_status gal_eval_hessian(const gal_potential* p, const double* x, double t, int64_t n, double* out,
                             gal_stream_t stream) {
-  (void)t;
   if (!p || (!x && n) || (!out && n) || n < 0) return fail(GAL_ERR_INVALID_ARGUMENT, "bad pointer or size");
   if (n == 0) return GAL_OK;
   const int block = 128;
@@ -418,7 +446,7 @@ gal_status gal_eval_hessian(const gal_potential* p, const double* x, double t, i
   const size_t smem = sizeof(DevComp) * p->n;
   if (smem > 48 * 1024)
     cudaFuncSetAttribute(k_eval_hessian, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  k_eval_hessian<<<grid, block, smem, (cudaStream_t)stream>>>(p->d_comps, p->n, x, n, out);
+  k_eval_hessian<<<grid, block, smem, (cudaStream_t)stream>>>(p->d_comps, p->d_lin, t, p->n, x, n, out);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? GAL_OK : cuda_fail(e, "hessian kernel launch");
 }
@@ -485,6 +513,7 @@ gal_status gal_integrate(const gal_potential* p, const gal_solver_config* cfg, c
   a.steps = steps;
   a.order = order;
   a.n = n;
+  a.lin = p->d_lin;
   cudaStream_t s = (cudaStream_t)stream;
   char* ws = static_cast<char*>(workspace);
   a.queue = reinterpret_cast<unsigned long long*>(ws);

@@ -135,7 +135,7 @@ __global__ void __launch_bounds__(128) k_integrate_dense(IntegrateArgs a, Pot po
     field(P, s.y, s.F0);
     double dt;
     if (a.adaptive) {
-      dt = a.dt0 > 0.0 ? a.dt0 : initial_step<TB>(a, P, s.y, s.F0, s.dir);
+      dt = a.dt0 > 0.0 ? a.dt0 : initial_step<TB>(a, P, s.y, s.F0, s.dir, t0);  // static potentials only
       if (a.dtmax > 0.0) dt = fmin(dt, a.dtmax);
       if (a.dtmin > 0.0) {
         s.at_dtmin = dt <= a.dtmin;
@@ -279,6 +279,7 @@ gal_status gal_integrate_dense(const gal_potential* pot, const gal_solver_config
                                const double* t0, const double* t1, int64_t n, int64_t cap, double* ts, double* coef,
                                int64_t* nsteps, int32_t* status, gal_stream_t stream) {
   if (!pot) return fail(GAL_ERR_INVALID_ARGUMENT, "potential is NULL");
+  if (time_dependent(pot)) return fail(GAL_ERR_UNSUPPORTED, "time-dependent parameters: evaluation and gal_integrate only");
   gal_status st = validate_cfg(cfg);
   if (st != GAL_OK) return st;
   if (n < 0 || cap < 1) return fail(GAL_ERR_INVALID_ARGUMENT, "n >= 0 and cap >= 1 required");
@@ -315,6 +316,7 @@ gal_status gal_dense_evaluate(const gal_potential* pot, int32_t method, const do
                               const int64_t* nsteps, int64_t cap, int64_t n, const int64_t* orbit, const double* t,
                               int64_t m, double* out, unsigned long long* out_of_bounds, gal_stream_t stream) {
   if (!pot || (method != 5 && method != 8)) return fail(GAL_ERR_INVALID_ARGUMENT, "bad potential or method");
+  if (time_dependent(pot)) return fail(GAL_ERR_UNSUPPORTED, "time-dependent parameters: evaluation and gal_integrate only");
   if (m < 0 || n < 0 || cap < 1) return fail(GAL_ERR_INVALID_ARGUMENT, "bad sizes");
   if (m == 0) return GAL_OK;
   if (!ts || !coef || !nsteps || !orbit || !t || !out || !out_of_bounds)

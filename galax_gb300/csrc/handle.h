@@ -15,7 +15,14 @@ struct gal_potential {
   int n;
   bool is_mw;             // evaluated by the specialised Milky Way model
   gal::MWParams mw;
+  gal::DevLinear* d_lin = nullptr;  // linear time dependence per component (NULL: static)
 };
+
+namespace gal {
+// Entry points that evaluate the potential at fixed times only (adjoint, dense
+// output, streams, surrogate) refuse time-dependent potentials with this.
+inline bool time_dependent(const gal_potential* p) { return p && p->d_lin; }
+}  // namespace gal
 
 namespace gal {
 gal_status fail(gal_status st, const std::string& msg);

@@ -69,6 +69,7 @@ struct IntegrateArgs {
   const int32_t* order;
   int64_t n;
   unsigned long long* queue;  // work-queue counter (scratch)
+  const DevLinear* lin;       // time-dependent component parameters (table kernel), or NULL
   // two-phase schedule: phase 0 parks every orbit once it has covered split_frac
   // of its span; phase 1 resumes the parked orbits from `resume` in `order`
   int32_t phase;
@@ -77,11 +78,12 @@ struct IntegrateArgs {
   const unsigned long long* queue_len;   // phase 1: number of entries in order (device)
 };
 
-// Hamiltonian field without the time-direction sign: F = (p, -grad Phi(q)).
+// Hamiltonian field without the time-direction sign: F = (p, -grad Phi(q, t)).
+// Static potential models ignore t, so its arithmetic vanishes from their code.
 template <class Pot>
-__device__ __forceinline__ void field(const Pot& pot, const double* Y, double* F) {
+__device__ __forceinline__ void field(const Pot& pot, const double* Y, double* F, double t = 0.0) {
   double gx, gy, gz;
-  pot.grad(Y[0], Y[1], Y[2], gx, gy, gz);
+  pot_grad_t(pot, t, Y[0], Y[1], Y[2], gx, gy, gz);
   F[0] = Y[3];
   F[1] = Y[4];
   F[2] = Y[5];
@@ -109,14 +111,16 @@ __device__ __forceinline__ void stage_state(const double* y, double hs, const do
   }
 }
 
-// Stages 1..S-1 of one RK step of signed length hs from y (F[0] preset).
+// Stages 1..S-1 of one RK step of signed length hs from (t, y) (F[0] preset).
 template <class TB, class Pot>
-__device__ __forceinline__ void rk_stages(const Pot& pot, const double* y, double hs, double (&F)[TB::S][6]) {
+__device__ __forceinline__ void rk_stages(const Pot& pot, const double* y, double hs, double (&F)[TB::S][6],
+                                          double t = 0.0) {
   static_for<1, TB::S>([&](auto i) {
     constexpr int I = decltype(i)::value;
     double Y[6];
     stage_state<TB, I>(y, hs, F, Y);
-    field(pot, Y, F[I]);
+    constexpr double ci = TB::C[I];
+    field(pot, Y, F[I], fma(ci, hs, t));
   });
 }
 
@@ -243,7 +247,7 @@ __device__ __forceinline__ void finish_orbit(const IntegrateArgs& a, OrbitState&
 
 template <class TB, class Pot>
 __device__ __forceinline__ double initial_step(const IntegrateArgs& a, const Pot& pot, const double* y,
-                                               const double* F0, double dir) {
+                                               const double* F0, double dir, double t) {
   // Hairer, Norsett & Wanner (1993) II.4, as used by diffrax when dt0 is None.
   double sc[6], q[6];
 #pragma unroll
@@ -259,7 +263,7 @@ __device__ __forceinline__ double initial_step(const IntegrateArgs& a, const Pot
   double Y[6], F1[6];
 #pragma unroll
   for (int j = 0; j < 6; ++j) Y[j] = fma(h0 * dir, F0[j], y[j]);
-  field(pot, Y, F1);
+  field(pot, Y, F1, fma(h0, dir, t));
 #pragma unroll
   for (int j = 0; j < 6; ++j) q[j] = (F1[j] - F0[j]) / sc[j];
   const double d2 = rms6(q) / h0;
@@ -321,7 +325,7 @@ __device__ __forceinline__ bool start_orbit(const IntegrateArgs& a, const Pot& p
       s.save_i = r.save_i;
       s.at_dtmin = r.at_dtmin;
       s.status = r.status;
-      field(pot, s.y, s.F0);
+      field(pot, s.y, s.F0, s.dir * s.tau);
       return true;
     }
 #pragma unroll
@@ -339,10 +343,10 @@ __device__ __forceinline__ bool start_orbit(const IntegrateArgs& a, const Pot& p
       finish_orbit(a, s, ORBIT_OK);
       continue;
     }
-    field(pot, s.y, s.F0);
+    field(pot, s.y, s.F0, t0);
     double dt;
     if (a.adaptive) {
-      dt = a.dt0 > 0.0 ? a.dt0 : initial_step<TB>(a, pot, s.y, s.F0, s.dir);
+      dt = a.dt0 > 0.0 ? a.dt0 : initial_step<TB>(a, pot, s.y, s.F0, s.dir, t0);
       if (a.dtmax > 0.0) dt = fmin(dt, a.dtmax);
       if (a.dtmin > 0.0) {
         s.at_dtmin = dt <= a.dtmin;
@@ -493,7 +497,7 @@ __device__ void integrate_loop(const IntegrateArgs& a, const Pot& pot) {
     }
 #pragma unroll
     for (int j = 0; j < 6; ++j) F[0][j] = s.F0[j];
-    rk_stages<TB>(pot, s.y, hs, F);
+    rk_stages<TB>(pot, s.y, hs, F, s.dir * s.tau);
     double y1[6], err[6];
     int32_t st = ORBIT_OK;
     bool done = false;
@@ -506,8 +510,8 @@ __device__ void integrate_loop(const IntegrateArgs& a, const Pot& pot) {
       s.pending = 0;
 #pragma unroll
       for (int j = 0; j < 6; ++j) s.y[j] = s.ynew[j];
-      field(pot, s.y, s.F0);
       s.tau = fmin(s.tau_new, s.tau1);
+      field(pot, s.y, s.F0, s.dir * s.tau);
       s.tnext = s.tnext_new;
       if (s.status != ORBIT_OK) { done = true; st = s.status; }
       else if (s.tau >= s.tau1) done = true;
@@ -571,9 +575,9 @@ __device__ void integrate_loop(const IntegrateArgs& a, const Pot& pot) {
             }
 #pragma unroll
             for (int j = 0; j < 6; ++j) s.y[j] = y1[j];
-            field(pot, s.y, s.F0);
             s.tau = tprev_new;
             s.tnext = tnext_new;
+            field(pot, s.y, s.F0, s.dir * s.tau);
           }
         } else {
           s.tau = tprev_new;

@@ -37,14 +37,17 @@ void mw_launch(int variant, unsigned grid, int block, cudaStream_t stream, const
   }
 }
 
-template <class TB>
+template <class TB, bool TIMED>
 __global__ void __launch_bounds__(kMaxBlock) k_integrate_table(IntegrateArgs a, const DevComp* comps, int ncomp) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   DevComp* s_comps = reinterpret_cast<DevComp*>(smem_raw);
   for (int i = threadIdx.x; i < ncomp; i += blockDim.x) s_comps[i] = comps[i];
   __syncthreads();
-  const TablePot pot{s_comps, ncomp};
-  integrate_loop<TB>(a, pot);
+  if constexpr (TIMED) {
+    integrate_loop<TB>(a, TimedTablePot{s_comps, ncomp, a.lin});
+  } else {
+    integrate_loop<TB>(a, TablePot{s_comps, ncomp});
+  }
 }
 
 template <class TB>
@@ -59,8 +62,10 @@ cudaError_t launch_integrate(const IntegrateArgs& a, bool mw, const MWParams& p,
   if (per_sm <= 0) {
     if (mw)
       err = mw_occupancy<TB>(shape.variant, block, &per_sm);
+    else if (a.lin)
+      err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_integrate_table<TB, true>, block, smem);
     else
-      err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_integrate_table<TB>, block, smem);
+      err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_integrate_table<TB, false>, block, smem);
     if (err != cudaSuccess) return err;
     if (per_sm < 1) per_sm = 1;
   }
@@ -71,11 +76,12 @@ cudaError_t launch_integrate(const IntegrateArgs& a, bool mw, const MWParams& p,
   if (mw) {
     mw_launch<TB>(shape.variant, (unsigned)grid, block, stream, a, p);
   } else {
+    auto kernel = a.lin ? k_integrate_table<TB, true> : k_integrate_table<TB, false>;
     if (smem > 48 * 1024) {
-      err = cudaFuncSetAttribute(k_integrate_table<TB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      err = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (err != cudaSuccess) return err;
     }
-    k_integrate_table<TB><<<(unsigned)grid, block, smem, stream>>>(a, comps, ncomp);
+    kernel<<<(unsigned)grid, block, smem, stream>>>(a, comps, ncomp);
   }
   return cudaGetLastError();
 }

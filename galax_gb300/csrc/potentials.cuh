@@ -324,6 +324,60 @@ __device__ __forceinline__ void comp_hessian(const DevComp& c, double x, double 
   H[8] += g;
 }
 
+// ----------------------------------------------------------- folding
+// digamma by upward recurrence to x >= 8 and the asymptotic series
+// (Abramowitz & Stegun 6.3.18).
+__host__ __device__ inline double digamma_fn(double x) {
+  double acc = 0.0;
+  while (x < 8.0) {
+    acc -= 1.0 / x;
+    x += 1.0;
+  }
+  const double i2 = 1.0 / (x * x);
+  return acc + log(x) - 0.5 / x -
+         i2 * (1.0 / 12 - i2 * (1.0 / 120 - i2 * (1.0 / 252 - i2 * (1.0 / 240 - i2 * (1.0 / 132)))));
+}
+
+// Component parameters folded for evaluation (shared by the host, which folds
+// static tables once, and by kernels that refold time-dependent components).
+__host__ __device__ inline DevComp fold_comp(int32_t kind, double m, double l1, double l2, double ox, double oy,
+                                             double oz, double G) {
+  DevComp d{};
+  d.kind = kind;
+  d.centered = (ox == 0.0 && oy == 0.0 && oz == 0.0) ? 1 : 0;
+  const bool log_kind = kind == LOGARITHMIC;  // m holds v_c: Phi scales with v_c^2, not G m
+  d.Gm = log_kind ? m * m : G * m;
+  d.l1 = l1;
+  d.l2 = l2;
+  d.l2sq = (kind == PLUMMER || kind == ISOCHRONE || log_kind) ? l1 * l1 : l2 * l2;
+  d.inv_l1 = (kind == NFW) ? 1.0 / l1 : 0.0;
+  d.inv_m = (m != 0.0) ? (log_kind ? 2.0 / m : 1.0 / m) : 0.0;
+  d.ox = ox;
+  d.oy = oy;
+  d.oz = oz;
+  if (kind == POWERLAW_CUTOFF) {
+    const double a1 = 1.5 - 0.5 * l2, a2 = 1.0 - 0.5 * l2;
+    d.l2sq = 1.0 / tgamma(a1);
+    d.inv_l1 = 1.0 / (l1 * l1);
+    d.aux0 = digamma_fn(a1);
+    d.aux1 = tgamma(a2);
+  }
+  return d;
+}
+
+// Linear time dependence of one component (galax's LinearParameter,
+// src/galax/potential/_src/params/core.py:25-110): p(t) = p0 + slope t for
+// p in (m, l1, l2), with p0 the value at t = 0.
+struct DevLinear {
+  int32_t kind, active;
+  double m0, l10, l20, dm, dl1, dl2, G;
+};
+
+__device__ __forceinline__ DevComp comp_at_time(const DevComp& c, const DevLinear& L, double t) {
+  if (!L.active) return c;
+  return fold_comp(L.kind, fma(L.dm, t, L.m0), fma(L.dl1, t, L.l10), fma(L.dl2, t, L.l20), c.ox, c.oy, c.oz, L.G);
+}
+
 // ----------------------------------------------------------- potential models
 // General composite: a table of components (in shared memory inside kernels).
 struct TablePot {
@@ -334,6 +388,30 @@ struct TablePot {
     for (int i = 0; i < n; ++i) comp_grad(c[i], x, y, z, gx, gy, gz);
   }
 };
+
+// A table whose components have linear time dependence: refolded at every
+// evaluation time.
+struct TimedTablePot {
+  const DevComp* c;
+  int n;
+  const DevLinear* lin;
+  __device__ __forceinline__ void grad_t(double t, double x, double y, double z, double& gx, double& gy,
+                                         double& gz) const {
+    gx = gy = gz = 0.0;
+    for (int i = 0; i < n; ++i) comp_grad(comp_at_time(c[i], lin[i], t), x, y, z, gx, gy, gz);
+  }
+};
+
+// Gradient of any potential model at time t: static models ignore t.
+template <class Pot>
+__device__ __forceinline__ void pot_grad_t(const Pot& p, double, double x, double y, double z, double& gx,
+                                           double& gy, double& gz) {
+  p.grad(x, y, z, gx, gy, gz);
+}
+__device__ __forceinline__ void pot_grad_t(const TimedTablePot& p, double t, double x, double y, double z,
+                                           double& gx, double& gy, double& gz) {
+  p.grad_t(t, x, y, z, gx, gy, gz);
+}
 
 // galax's MilkyWayPotential structure: Miyamoto-Nagai disk, NFW halo and two
 // Hernquist spheres (bulge, nucleus), all centred on the origin

@@ -126,6 +126,7 @@ gal_status gal_integrate_surrogate(const gal_potential* pot, const gal_mlp* mlp,
                                    double t0, double t1, double* y, int64_t n, int32_t use_graph, void* workspace,
                                    size_t workspace_bytes, gal_stream_t stream) {
   if (!pot || !y || n < 0 || !(dt > 0.0)) return fail(GAL_ERR_INVALID_ARGUMENT, "bad surrogate arguments");
+  if (time_dependent(pot)) return fail(GAL_ERR_UNSUPPORTED, "time-dependent parameters: evaluation and gal_integrate only");
   if (n == 0 || t0 == t1) return GAL_OK;
   size_t need = 0;
   gal_surrogate_workspace_size(n, &need);

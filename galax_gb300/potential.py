@@ -22,6 +22,7 @@ from __future__ import annotations
 import ctypes as C
 import math
 from collections.abc import Mapping
+from dataclasses import dataclass
 from typing import Any
 
 import numpy as np
@@ -38,9 +39,27 @@ def _torch():
     return torch
 
 
+@dataclass(frozen=True)
+class LinearParameter:
+    """galax's LinearParameter (src/galax/potential/_src/params/core.py:25-110),
+    in galactic units: p(t) = slope (t - point_time) + point_value."""
+
+    slope: float
+    point_time: float
+    point_value: float
+
+    def __call__(self, t):
+        return self.slope * (np.asarray(t, np.float64) - self.point_time) + self.point_value
+
+    @property
+    def value_at_zero(self) -> float:
+        return float(self.point_value - self.slope * self.point_time)
+
+
 def _param(name: str, v: Any) -> float:
     if callable(v):
-        raise NotImplementedError(f"{name}: only constant parameters are supported on the GPU path")
+        raise NotImplementedError(f"{name}: only constant and LinearParameter parameters are supported on the "
+                                  "GPU path")
     try:
         f = float(v)
     except Exception as e:  # noqa: BLE001
@@ -81,6 +100,10 @@ class AbstractPotential:
             a[i]["origin"] = origin
         return a
 
+    def slopes(self):
+        """d(m, l1, l2)/dt per component (ncomp, 3), or None for a static potential."""
+        return None
+
     def parameter_names(self) -> list[tuple[str, str, str]]:
         """(component, mass-name, length names) per component, for gradients."""
         return [(f"c{i}", "m", "l1", "l2") for i in range(len(self.components()))]
@@ -96,13 +119,20 @@ class AbstractPotential:
             raise _lib.GalaxGB300Error("no CUDA device: the galax_gb300 path has no CPU fallback")
         dev = torch.cuda.current_device()
         arr = self.component_array()
-        key = arr.tobytes() + np.float64(self.G).tobytes()
+        slopes = self.slopes()
+        key = arr.tobytes() + np.float64(self.G).tobytes() + (b"" if slopes is None else slopes.tobytes())
         if self._handle is not None and self._handle_device == dev and self._handle_key == key:
             return self._handle
         self._release()
         L = _lib.load()
         h = C.c_void_p()
         _lib.check(L.gal_potential_create(arr.ctypes.data, len(arr), self.G, C.byref(h)), "gal_potential_create")
+        if slopes is not None:
+            sl = np.ascontiguousarray(slopes, np.float64)
+            st = L.gal_potential_set_linear(h, sl.ctypes.data)
+            if st != 0:
+                L.gal_potential_destroy(h)
+                _lib.check(st, "gal_potential_set_linear")
         self._handle, self._handle_device, self._handle_key, self._arr = h.value, dev, key, arr
         return self._handle
 
@@ -241,10 +271,15 @@ class AbstractSinglePotential(AbstractPotential):
 
     def __init__(self, *, origin=(0.0, 0.0, 0.0), units: Any = "galactic", constants=None, **params):
         super().__init__(units=units, constants=constants)
+        self._slopes = {}
         for name in self._names:
             if name not in params:
                 raise TypeError(f"{type(self).__name__} needs parameter {name!r}")
-            setattr(self, name, _param(name, params.pop(name)))
+            v = params.pop(name)
+            if isinstance(v, LinearParameter):  # stored as its value at t = 0 plus a slope
+                self._slopes[name] = _param(f"{name}.slope", v.slope)
+                v = v.value_at_zero
+            setattr(self, name, _param(name, v))
         if params:
             raise TypeError(f"unexpected parameters {sorted(params)}")
         self.origin = tuple(float(v) for v in origin)
@@ -253,6 +288,13 @@ class AbstractSinglePotential(AbstractPotential):
 
     def _repr_params(self) -> str:
         return ", ".join(f"{k}={getattr(self, k)!r}" for k in self._names)
+
+    def slopes(self):
+        if not any(self._slopes.values()):
+            return None
+        order = getattr(self, "_record", self._names)
+        row = [self._slopes.get(order[j], 0.0) if j < len(order) else 0.0 for j in range(3)]
+        return np.array([row], np.float64)
 
 
 class KeplerPotential(AbstractSinglePotential):
@@ -466,6 +508,12 @@ class CompositePotential(AbstractPotential):
             out += v.components()
         return out
 
+    def slopes(self):
+        parts = [(v.slopes(), len(v.components())) for v in self._items.values()]
+        if all(sl is None for sl, _ in parts):
+            return None
+        return np.concatenate([np.zeros((k, 3)) if sl is None else sl for sl, k in parts], axis=0)
+
     def _repr_params(self) -> str:
         return ", ".join(f"{k}={v!r}" for k, v in self._items.items())
 
@@ -578,8 +626,10 @@ class TranslatedPotential(CompositePotential):
                 for (k, m, l1, l2, o) in self["original"].components()]
 
 
-def from_component_array(arr: np.ndarray, G: float = G_GALACTIC) -> CompositePotential:
-    """Composite built from a ``gal_component`` record array."""
+def from_component_array(arr: np.ndarray, G: float = G_GALACTIC, slopes=None) -> CompositePotential:
+    """Composite built from a ``gal_component`` record array; ``slopes``
+    (ncomp, 3), if given, makes (m, l1, l2) LinearParameters through their
+    table values at t = 0."""
     cls = {_lib.GAL_KEPLER: KeplerPotential, _lib.GAL_HERNQUIST: HernquistPotential,
            _lib.GAL_MIYAMOTO_NAGAI: MiyamotoNagaiPotential, _lib.GAL_NFW: NFWPotential,
            _lib.GAL_PLUMMER: PlummerPotential, _lib.GAL_ISOCHRONE: IsochronePotential,
@@ -589,5 +639,8 @@ def from_component_array(arr: np.ndarray, G: float = G_GALACTIC) -> CompositePot
         k = int(rec["kind"])
         names = getattr(cls[k], "_record", cls[k]._names)
         vals = [float(rec["m"]), float(rec["l1"]), float(rec["l2"])][: len(names)]
+        if slopes is not None:
+            vals = [LinearParameter(float(slopes[i][j]), 0.0, v) if slopes[i][j] != 0.0 else v
+                    for j, v in enumerate(vals)]
         parts[f"c{i}"] = cls[k](**dict(zip(names, vals)), origin=tuple(rec["origin"]), constants={"G": G})
     return CompositePotential(parts, constants={"G": G})

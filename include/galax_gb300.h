@@ -98,6 +98,17 @@ typedef struct gal_potential gal_potential; /* opaque */
 #define GAL_MAX_COMPONENTS 1024
 GAL_API gal_status gal_potential_create(const gal_component* comps, int32_t n, double G, gal_potential** out);
 GAL_API gal_status gal_potential_destroy(gal_potential* pot);
+/* Linear time dependence of component parameters, galax's LinearParameter
+ * (src/galax/potential/_src/params/core.py:25-110): with slopes [n][3] (host
+ * array, d(m, l1, l2)/dt per component), component i is evaluated with
+ * m + slopes[i][0] t, l1 + slopes[i][1] t, l2 + slopes[i][2] t, where the
+ * component table holds the values at t = 0 (galax's point-slope form
+ * p(t) = slope (t - t_i) + p(t_i) gives p(0) = p(t_i) - slope t_i). The
+ * gal_eval_* functions evaluate at their t; gal_integrate and
+ * gal_integrate_noalloc evaluate every stage at its own time. Adjoint, dense
+ * output, stream and surrogate entry points reject time-dependent potentials
+ * (GAL_ERR_UNSUPPORTED). slopes = NULL makes the potential static again. */
+GAL_API gal_status gal_potential_set_linear(gal_potential* pot, const double* slopes);
 /* Replace the parameters (same count and kinds), e.g. between optimiser steps. */
 GAL_API gal_status gal_potential_update(gal_potential* pot, const gal_component* comps, int32_t n, gal_stream_t stream);
 GAL_API int32_t gal_potential_num_components(const gal_potential* pot);

@@ -407,23 +407,38 @@ void comp_dgrad_dparams_dot(const Comp& c, double G, const double* xin, const do
   }
 }
 
+// Components; slopes (n x 3, or NULL) make (m, l1, l2) linear in time,
+// p(t) = p + slope t, with the table holding the values at t = 0 (galax's
+// LinearParameter, src/galax/potential/_src/params/core.py:25-110, in
+// point-slope form p(t) = slope (t - t_i) + p(t_i)).
 struct Pot {
   const Comp* comps;
   int n;
   double G;
+  const double* slopes = nullptr;
 };
 
+inline Comp comp_at(const Pot& P, int i, double t) {
+  Comp c = P.comps[i];
+  if (P.slopes) {
+    c.m += P.slopes[3 * i] * t;
+    c.l1 += P.slopes[3 * i + 1] * t;
+    c.l2 += P.slopes[3 * i + 2] * t;
+  }
+  return c;
+}
+
 template <class T>
-inline void gradient(const Pot& P, const T* x, T* g) {
+inline void gradient(const Pot& P, const T* x, T* g, double t = 0.0) {
   g[0] = g[1] = g[2] = T(0);
-  for (int i = 0; i < P.n; ++i) comp_gradient<T>(P.comps[i], P.G, x, g);
+  for (int i = 0; i < P.n; ++i) comp_gradient<T>(comp_at(P, i, t), P.G, x, g);
 }
 
 // Hamiltonian field with optional time reversal (sign = -1).
 template <class T>
-inline void field(const Pot& P, double sign, const T* y, T* dy) {
+inline void field(const Pot& P, double sign, const T* y, T* dy, double t = 0.0) {
   T g[3];
-  gradient<T>(P, y, g);
+  gradient<T>(P, y, g, t);
   dy[0] = T(sign) * y[3];
   dy[1] = T(sign) * y[4];
   dy[2] = T(sign) * y[5];
@@ -530,15 +545,16 @@ struct System {
   const Pot* P;
   int m;            // orbits in lockstep
   double sign;      // +1 forward, -1 reversed time
-  void f(const T* y, T* dy) const {
-    for (int o = 0; o < m; ++o) field<T>(*P, sign, y + 6 * o, dy + 6 * o);
+  // tau: the integration variable sign * t
+  void f(double tau, const T* y, T* dy) const {
+    for (int o = 0; o < m; ++o) field<T>(*P, sign, y + 6 * o, dy + 6 * o, sign * tau);
   }
 };
 
 // F holds the stage slopes f(Y_i) (s x n); Y is an n-scratch. The step is
 // y1 = y0 + h sum_i b_i F_i and err = h sum_i e_i F_i (diffrax's ODE form).
 template <class T>
-void rk_step(const System<T>& S, const Tableau& TB, const T* y0, const T* f0, double h,
+void rk_step(const System<T>& S, const Tableau& TB, double tau, const T* y0, const T* f0, double h,
              T* F, T* Y, T* y1, T* err) {
   const int n = 6 * S.m;
   for (int j = 0; j < n; ++j) F[j] = f0[j];
@@ -554,7 +570,7 @@ void rk_step(const System<T>& S, const Tableau& TB, const T* y0, const T* f0, do
         }
       Y[j] = y0[j] + T(h) * acc;
     }
-    S.f(Y, F + (size_t)i * n);
+    S.f(tau + TB.c[i] * h, Y, F + (size_t)i * n);
   }
   for (int j = 0; j < n; ++j) {
     T acc = T(0), e = T(0);
@@ -624,7 +640,7 @@ static SolveOut solve_group(const Pot& P, const OrcSolverCfg& cfg, const double*
     for (; si < ns; ++si) std::memcpy(out + si * n, y.data(), sizeof(double) * n);
     return R;
   }
-  S.f(y.data(), f0.data());
+  S.f(tau0, y.data(), f0.data());
   double tprev = tau0, tnext;
   // controller state
   bool at_dtmin = false;
@@ -645,7 +661,7 @@ static SolveOut solve_group(const Pot& P, const OrcSolverCfg& cfg, const double*
       double h0 = cond ? 1e-6 : 0.01 * (d0 / d1_);
       std::vector<double> yy(n), f1(n);
       for (int j = 0; j < n; ++j) yy[j] = y[j] + h0 * f0[j];
-      S.f(yy.data(), f1.data());
+      S.f(tau0 + h0, yy.data(), f1.data());
       for (int j = 0; j < n; ++j) q[j] = (f1[j] - f0[j]) / sc[j];
       double d2 = rms(q) / h0;
       double maxd = std::max(d1, d2);
@@ -665,7 +681,8 @@ static SolveOut solve_group(const Pot& P, const OrcSolverCfg& cfg, const double*
   long long nsteps = 0;
   while (tprev < tau1 && nsteps < cfg.max_steps) {
     const double h = tnext - tprev;
-    rk_step<double>(S, TB, y.data(), f0.data(), h, F.data(), Y.data(), y1.data(), cfg.adaptive ? err.data() : nullptr);
+    rk_step<double>(S, TB, tprev, y.data(), f0.data(), h, F.data(), Y.data(), y1.data(),
+                    cfg.adaptive ? err.data() : nullptr);
     ++nsteps;
     bool finite = true;
     for (int j = 0; j < n; ++j) finite = finite && std::isfinite(y1[j]);
@@ -723,7 +740,8 @@ static SolveOut solve_group(const Pot& P, const OrcSolverCfg& cfg, const double*
             ysave[j] = (((A * th + B) * th + C) * th + F0) * th + Y0;
           }
         } else {
-          rk_step<double>(S, TB, y.data(), f0.data(), ts_ - tprev, Fs.data(), Y.data(), ysave.data(), nullptr);
+          rk_step<double>(S, TB, tprev, y.data(), f0.data(), ts_ - tprev, Fs.data(), Y.data(), ysave.data(),
+                          nullptr);
         }
         std::memcpy(out + si * n, ysave.data(), sizeof(double) * n);
         ++si;
@@ -732,7 +750,7 @@ static SolveOut solve_group(const Pot& P, const OrcSolverCfg& cfg, const double*
       if (TB.fsal) {
         for (int j = 0; j < n; ++j) f0[j] = F[(size_t)(TB.s - 1) * n + j];
       } else {
-        S.f(y.data(), f0.data());
+        S.f(tnext, y.data(), f0.data());
       }
     } else {
       ++R.rejected;
@@ -765,27 +783,31 @@ void orc_gamma_p(double a, double x, double* out) {
 }
 
 // Phi, grad Phi, Hessian at n points (x: n x 3 row-major).
-void orc_potential(const Comp* comps, int ncomp, double G, const double* x, int64_t n, double* out) {
-  Pot P{comps, ncomp, G};
+// slopes: n_comp x 3 or NULL (static); t: evaluation time.
+void orc_potential(const Comp* comps, int ncomp, double G, const double* x, int64_t n, double* out,
+                   const double* slopes, double t) {
+  Pot P{comps, ncomp, G, slopes};
   for (int64_t i = 0; i < n; ++i) {
     double s = 0;
-    for (int c = 0; c < ncomp; ++c) s += comp_potential<double>(comps[c], G, x + 3 * i);
+    for (int c = 0; c < ncomp; ++c) s += comp_potential<double>(comp_at(P, c, t), G, x + 3 * i);
     out[i] = s;
   }
-  (void)P;
 }
 
-void orc_gradient(const Comp* comps, int ncomp, double G, const double* x, int64_t n, double* out) {
-  Pot P{comps, ncomp, G};
+void orc_gradient(const Comp* comps, int ncomp, double G, const double* x, int64_t n, double* out,
+                  const double* slopes, double t) {
+  Pot P{comps, ncomp, G, slopes};
 #pragma omp parallel for schedule(static)
-  for (int64_t i = 0; i < n; ++i) gradient<double>(P, x + 3 * i, out + 3 * i);
+  for (int64_t i = 0; i < n; ++i) gradient<double>(P, x + 3 * i, out + 3 * i, t);
 }
 
-void orc_hessian(const Comp* comps, int ncomp, double G, const double* x, int64_t n, double* out) {
+void orc_hessian(const Comp* comps, int ncomp, double G, const double* x, int64_t n, double* out,
+                 const double* slopes, double t) {
+  Pot P{comps, ncomp, G, slopes};
   for (int64_t i = 0; i < n; ++i) {
     double* H = out + 9 * i;
     for (int j = 0; j < 9; ++j) H[j] = 0;
-    for (int c = 0; c < ncomp; ++c) comp_hessian(comps[c], G, x + 3 * i, H);
+    for (int c = 0; c < ncomp; ++c) comp_hessian(comp_at(P, c, t), G, x + 3 * i, H);
   }
 }
 
@@ -822,8 +844,9 @@ void orc_dopri5_cmid(double* out) {
 // t0, t1 and save grids: orbit 0's are used); out then holds ns x n x 6.
 int orc_integrate(const Comp* comps, int ncomp, double G, const OrcSolverCfg* cfg, const double* y0,
                   const double* t0, const double* t1, const int64_t* save_offsets, const double* save_ts,
-                  double* out, int32_t* status, int64_t* accepted, int64_t* rejected, int64_t n, int nthreads) {
-  Pot P{comps, ncomp, G};
+                  double* out, int32_t* status, int64_t* accepted, int64_t* rejected, int64_t n, int nthreads,
+                  const double* slopes) {
+  Pot P{comps, ncomp, G, slopes};
   if (cfg->lockstep) {
     int64_t ns = save_offsets[1] - save_offsets[0];
     SolveOut R = solve_group(P, *cfg, y0, t0[0], t1[0], save_ts + save_offsets[0], ns, out, (int)n);
@@ -869,7 +892,7 @@ int orc_adjoint_fixed(const Comp* comps, int ncomp, double G, const OrcSolverCfg
 #pragma omp parallel for schedule(dynamic, 1)
   for (int64_t o = 0; o < n; ++o) {
     System<double> S{&P, 1, 1.0};
-    std::vector<double> ys, hs;
+    std::vector<double> ys, hs, taus;
     double y[6], y1[6], f0[6], F[13 * 6], Y[6];
     for (int j = 0; j < 6; ++j) y[j] = y0[6 * o + j];
     double tprev = t0, tnext = std::min(t0 + dt, t1);
@@ -878,8 +901,9 @@ int orc_adjoint_fixed(const Comp* comps, int ncomp, double G, const OrcSolverCfg
       double h = tnext - tprev;
       ys.insert(ys.end(), y, y + 6);
       hs.push_back(h);
-      S.f(y, f0);
-      rk_step<double>(S, TB, y, f0, h, F, Y, y1, nullptr);
+      taus.push_back(tprev);
+      S.f(tprev, y, f0);
+      rk_step<double>(S, TB, tprev, y, f0, h, F, Y, y1, nullptr);
       for (int j = 0; j < 6; ++j) y[j] = y1[j];
       double nt0 = tnext, nt1 = tnext + dt;
       tprev = std::min(nt0, t1);
@@ -896,9 +920,9 @@ int orc_adjoint_fixed(const Comp* comps, int ncomp, double G, const OrcSolverCfg
     double Fb[13 * 6], Ys[13 * 6];
     for (int64_t st = N - 1; st >= 0; --st) {
       const double* yn = ys.data() + 6 * st;
-      const double h = hs[st];
+      const double h = hs[st], tau = taus[st];
       // recompute the stages
-      S.f(yn, f0);
+      S.f(tau, yn, f0);
       for (int j = 0; j < 6; ++j) { F[j] = f0[j]; Ys[j] = yn[j]; }
       for (int i = 1; i < TB.s; ++i) {
         for (int j = 0; j < 6; ++j) {
@@ -912,7 +936,7 @@ int orc_adjoint_fixed(const Comp* comps, int ncomp, double G, const OrcSolverCfg
             }
           Ys[6 * i + j] = yn[j] + h * acc;
         }
-        S.f(Ys + 6 * i, F + 6 * i);
+        S.f(tau + TB.c[i] * h, Ys + 6 * i, F + 6 * i);
       }
       double lam0[6];
       for (int j = 0; j < 6; ++j) lam0[j] = lam[j];
@@ -1235,14 +1259,14 @@ void orc_count_ops(const Comp* comps, int ncomp, double G, int method, const dou
   for (int j = 0; j < 6; ++j) yy[j] = CD(y[j]);
   const Tableau& TB = (method == 5) ? DOPRI5 : DOPRI8;
   g_ops = OpCount();
-  if (!TB.fsal || true) S.f(yy, f0);  // the step's first evaluation
+  if (!TB.fsal || true) S.f(0.0, yy, f0);  // the step's first evaluation
   std::vector<CD> Fb((size_t)TB.s * 6), Yb(6);
-  rk_step<CD>(S, TB, yy, f0, 1.0, Fb.data(), Yb.data(), y1, e);
+  rk_step<CD>(S, TB, 0.0, yy, f0, 1.0, Fb.data(), Yb.data(), y1, e);
   if (TB.fsal) {
     // FSAL: the last stage is the next step's first evaluation; do not count it twice.
     OpCount before = g_ops;
     g_ops = OpCount();
-    S.f(yy, f0);
+    S.f(0.0, yy, f0);
     OpCount one = g_ops;
     g_ops = before;
     g_ops.add -= one.add; g_ops.mul -= one.mul; g_ops.div -= one.div; g_ops.sqrt -= one.sqrt;

@@ -88,7 +88,7 @@ def lib() -> C.CDLL:
         i64p = np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")
         i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
         for name in ("orc_potential", "orc_gradient", "orc_hessian"):
-            getattr(L, name).argtypes = [cp, C.c_int, C.c_double, dp, C.c_int64, dp]
+            getattr(L, name).argtypes = [cp, C.c_int, C.c_double, dp, C.c_int64, dp, C.c_void_p, C.c_double]
             getattr(L, name).restype = None
         L.orc_dgrad_dparams.argtypes = [cp, C.c_int, C.c_double, dp, dp, C.c_int64, dp]
         L.orc_tableau.argtypes = [C.c_int, dp, dp, dp, dp]
@@ -96,7 +96,7 @@ def lib() -> C.CDLL:
         L.orc_dopri5_cmid.argtypes = [dp]
         L.orc_integrate.argtypes = [
             cp, C.c_int, C.c_double, C.POINTER(SolverCfg), dp, dp, dp, i64p, dp, dp, i32p, i64p, i64p,
-            C.c_int64, C.c_int,
+            C.c_int64, C.c_int, C.c_void_p,
         ]
         L.orc_integrate.restype = C.c_int
         L.orc_count_ops.argtypes = [cp, C.c_int, C.c_double, C.c_int, dp, i64p]
@@ -194,24 +194,37 @@ def _xyz(x):
     return x.reshape(-1, 3)
 
 
-def potential(c: np.ndarray, x, G: float = G_GALACTIC) -> np.ndarray:
+def _slopes_ptr(c: np.ndarray, slopes):
+    """(keep-alive array, pointer) for per-component d(m, l1, l2)/dt, or (None, None)."""
+    if slopes is None:
+        return None, None
+    a = np.ascontiguousarray(slopes, np.float64).reshape(len(c), 3)
+    return a, a.ctypes.data
+
+
+def potential(c: np.ndarray, x, G: float = G_GALACTIC, *, slopes=None, t: float = 0.0) -> np.ndarray:
+    """Phi at x (n, 3) and time t; ``slopes`` (ncomp, 3) makes (m, l1, l2)
+    linear in time with the table holding their values at t = 0."""
     x = _xyz(x)
     out = np.empty(len(x))
-    lib().orc_potential(np.ascontiguousarray(c), len(c), G, x, len(x), out)
+    keep, sp = _slopes_ptr(c, slopes)
+    lib().orc_potential(np.ascontiguousarray(c), len(c), G, x, len(x), out, sp, float(t))
     return out
 
 
-def gradient(c: np.ndarray, x, G: float = G_GALACTIC) -> np.ndarray:
+def gradient(c: np.ndarray, x, G: float = G_GALACTIC, *, slopes=None, t: float = 0.0) -> np.ndarray:
     x = _xyz(x)
     out = np.empty((len(x), 3))
-    lib().orc_gradient(np.ascontiguousarray(c), len(c), G, x, len(x), out)
+    keep, sp = _slopes_ptr(c, slopes)
+    lib().orc_gradient(np.ascontiguousarray(c), len(c), G, x, len(x), out, sp, float(t))
     return out
 
 
-def hessian(c: np.ndarray, x, G: float = G_GALACTIC) -> np.ndarray:
+def hessian(c: np.ndarray, x, G: float = G_GALACTIC, *, slopes=None, t: float = 0.0) -> np.ndarray:
     x = _xyz(x)
     out = np.empty((len(x), 3, 3))
-    lib().orc_hessian(np.ascontiguousarray(c), len(c), G, x, len(x), out)
+    keep, sp = _slopes_ptr(c, slopes)
+    lib().orc_hessian(np.ascontiguousarray(c), len(c), G, x, len(x), out, sp, float(t))
     return out
 
 
@@ -246,10 +259,12 @@ def integrate(
     *,
     G: float = G_GALACTIC,
     nthreads: int = 0,
+    slopes=None,
 ):
     """Integrate orbits. ``save_ts`` is a list of per-orbit 1-D arrays or a
     single 1-D array shared by all orbits. Returns (saves list of (T_i, 6),
-    status, accepted, rejected); in lockstep mode saves is (T, n, 6)."""
+    status, accepted, rejected); in lockstep mode saves is (T, n, 6).
+    ``slopes`` (ncomp, 3): linear time dependence of (m, l1, l2)."""
     y0 = np.ascontiguousarray(np.atleast_2d(np.asarray(y0, np.float64)))
     n = len(y0)
     t0 = np.ascontiguousarray(np.broadcast_to(np.asarray(t0, np.float64), (n,)))
@@ -269,9 +284,10 @@ def integrate(
         out = np.empty((ns, n, 6))
     else:
         out = np.empty((int(offs[-1]), 6))
+    keep, sp = _slopes_ptr(c, slopes)
     lib().orc_integrate(
         np.ascontiguousarray(c), len(c), G, C.byref(cfg), y0, t0, t1, offs, flat, out, status, acc, rej, n,
-        nthreads,
+        nthreads, sp,
     )
     if cfg.lockstep:
         return out, status, acc, rej

@@ -191,6 +191,18 @@ def main(root: Path) -> None:
         "expect_q": [q[0:3]], "expect_p": [p[0:3]], "digits": 3,
     }
 
+    f = "src/galax/potential/_src/params/core.py"
+    rho = numbers(root, f, [72, 73])
+    g["orbits"]["kepler_linear_mass"] = {
+        "cite": f"{f}:52-74 (LinearParameter; compute_orbit's default OrbitSolver, orbit/solver.py:121-141)",
+        "potential": {"kind": "kepler", "m": 1e12, "l1": 0.0, "l2": 0.0},
+        # slope -1e3 Msun/yr = -1e9 Msun/Myr through (t = 0, 1e12 Msun)
+        "slopes": [[-1e9, 0.0, 0.0]],
+        "solver": {"method": 8, "adaptive": True, "rtol": 1e-8, "atol": 1e-8, "max_steps": 65536},
+        "y0": [[5.0, 0.0, 0.0, 0.0, 1000 * KMS, 0.0]], "t0": 0.0, "t1": 1000.0,
+        "save_ts_linspace": [0.0, 1000.0, 10], "expect_rho": rho, "rho_decimals": 3,
+    }
+
     g["stream"] = {}
     f = "src/galax/dynamics/_src/cluster/api.py"
     rt = numbers(root, f, [198])

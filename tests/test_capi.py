@@ -165,3 +165,25 @@ def test_mn3_and_milky_way_2022_component_tables():
     want = O.milky_way_2022()
     for f in ("kind", "m", "l1", "l2"):
         np.testing.assert_allclose(got[f], want[f], rtol=1e-14)
+
+
+def test_linear_parameters_on_the_host():
+    """LinearParameter semantics and the slope table the front end hands to
+    gal_potential_set_linear (no GPU needed)."""
+    import galax_gb300 as gx
+
+    lp = gx.LinearParameter(slope=-1e9, point_time=100.0, point_value=1e12)
+    assert lp(100.0) == 1e12 and lp(0.0) == lp.value_at_zero == 1e12 + 1e11
+    pot = gx.CompositePotential(a=gx.KeplerPotential(m_tot=lp),
+                                b=gx.PowerLawCutoffPotential(m_tot=1e10, alpha=gx.LinearParameter(1e-4, 0.0, 1.0),
+                                                             r_c=2.0),
+                                c=gx.NFWPotential(m=1e11, r_s=10.0))
+    np.testing.assert_array_equal(pot.slopes(), [[-1e9, 0, 0], [0, 0, 1e-4], [0, 0, 0]])
+    assert pot.component_array()["m"][0] == 1.1e12  # the table holds the values at t = 0
+    assert gx.MilkyWayPotential().slopes() is None
+    with pytest.raises(NotImplementedError):
+        gx.KeplerPotential(m_tot=lambda t: 1e12)  # other callables stay unsupported
+
+
+def test_set_linear_validates_on_the_host(lib):
+    assert lib.gal_potential_set_linear(None, None) == 1

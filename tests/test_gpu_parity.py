@@ -401,3 +401,83 @@ def test_two_pass_schedule_is_bitwise_identical(gx, method):
     np.testing.assert_array_equal(res[0][1], res[1][1])
     np.testing.assert_array_equal(res[0][2], res[1][2])
     np.testing.assert_array_equal(res[0][0], res[1][0])
+
+
+# ------------------------------------------------------------------ time-dependent (linear) parameters
+def test_linear_parameter_doctest_on_gpu(gx, goldens):
+    """galax's LinearParameter doctest (params/core.py:52-74) through the front
+    end: KeplerPotential(m_tot=LinearParameter(...)) and compute_orbit's
+    default solver, radii to the printed 3 decimals."""
+    g = goldens["orbits"]["kepler_linear_mass"]
+    lp = gx.LinearParameter(slope=g["slopes"][0][0], point_time=0.0, point_value=g["potential"]["m"])
+    pot = gx.KeplerPotential(m_tot=lp)
+    orb = gx.evaluate_orbit(pot, np.array(g["y0"][0]), golden_save_ts(g), integrator=gx.OrbitSolver())
+    rho = np.hypot(orb.q[:, 0], orb.q[:, 1])
+    np.testing.assert_allclose(rho, g["expect_rho"], rtol=0, atol=0.5 * 10.0 ** -g["rho_decimals"] + 1e-9)
+    assert not pot.is_milky_way_kernel()
+
+
+def _timed_kinds(seed=4):
+    c = _kinds()
+    rng = np.random.default_rng(seed)
+    sl = rng.normal(size=(len(c), 3)) * np.stack([np.abs(c["m"]) * 1e-4, np.full(len(c), 1e-4),
+                                                   np.full(len(c), 1e-4)], axis=1)
+    sl[c["kind"] == O.KEPLER, 1:] = 0.0
+    sl[~np.isin(c["kind"], (O.MIYAMOTO_NAGAI, O.POWERLAW_CUTOFF)), 2] = 0.0  # l2 is no parameter there
+    return c, sl
+
+
+def test_linear_parameters_evaluate_at_time(gx):
+    from galax_gb300.potential import from_component_array
+
+    c, sl = _timed_kinds()
+    pot = from_component_array(c, slopes=sl)
+    np.testing.assert_array_equal(pot.slopes(), sl)
+    x = _mixed_points(2048, 12)
+    for t in (0.0, 37.5, -120.0):
+        np.testing.assert_allclose(pot.potential(x, t), O.potential(c, x, slopes=sl, t=t), rtol=1e-13,
+                                   atol=1e-14 * np.abs(O.potential(c, x, slopes=sl, t=t)).max())
+        g_ref = O.gradient(c, x, slopes=sl, t=t)
+        assert np.max(np.abs(pot.gradient(x, t) - g_ref) / np.linalg.norm(g_ref, axis=1, keepdims=True)) < 1e-13
+        H_ref = O.hessian(c, x, slopes=sl, t=t)
+        assert np.max(np.abs(pot.hessian(x, t) - H_ref) / np.abs(H_ref).max(axis=(1, 2), keepdims=True)) < 1e-12
+
+
+@pytest.mark.parametrize("method", [8, 5])
+def test_linear_parameters_integrate_like_oracle(gx, method):
+    """Adaptive integration with time-dependent parameters, forwards and
+    backwards in time, with saves, against the oracle evaluating every stage at
+    its own time."""
+    from galax_gb300.dynamics import integrate
+
+    c = O.milky_way()
+    sl = np.zeros((len(c), 3))
+    sl[0, 0] = -2e7   # disk mass falling 2e7 Msun / Myr
+    sl[1, 1] = 5e-3   # halo scale radius growing 5 pc / Myr
+    y0 = _ics(256, 17)
+    ts = np.linspace(0.0, 400.0, 21)
+    ocfg = O.solver_cfg(method, True, rtol=1e-9, atol=1e-9)
+    cfg = gx.Integrator(solver=gx.Dopri8() if method == 8 else gx.Dopri5(),
+                        stepsize_controller=gx.PIDController(rtol=1e-9, atol=1e-9)).config()
+    from galax_gb300.potential import from_component_array
+
+    pot = from_component_array(c, slopes=sl)
+    for t0, t1, grid in ((0.0, 400.0, ts), (400.0, 0.0, ts[::-1].copy())):
+        out, st, _ = integrate(pot, y0, t0, t1, grid, cfg)
+        ref, rst, _, _ = O.integrate(c, y0, t0, t1, grid, ocfg, slopes=sl)
+        assert np.all(st.cpu().numpy() == 0) and np.all(rst == 0)
+        got = out.permute(2, 1, 0).cpu().numpy()  # (n, T, 6)
+        assert _rel(got.reshape(-1, 6), np.stack(ref).reshape(-1, 6)) < 1e-8
+    # the slopes matter: the same table held static gives different orbits
+    static = integrate(from_component_array(c), y0, 0.0, 400.0, ts, cfg)[0].cpu().numpy()
+    assert not np.allclose(static, integrate(pot, y0, 0.0, 400.0, ts, cfg)[0].cpu().numpy())
+
+
+def test_time_dependent_potentials_are_refused_where_unsupported(gx):
+    from galax_gb300._lib import GalaxGB300Error
+    from galax_gb300.adjoint import orbit_adjoint
+
+    pot = gx.KeplerPotential(m_tot=gx.LinearParameter(slope=-1e8, point_time=0.0, point_value=1e11))
+    y0 = _ics(4, 1)
+    with pytest.raises(GalaxGB300Error):
+        orbit_adjoint(pot, y0, 0.0, 10.0, dt=1.0, target=y0, method=8, k_ckpt=4)

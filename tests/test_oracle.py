@@ -533,3 +533,35 @@ def test_incomplete_gamma_matches_scipy():
             h = 1e-6
             fd = (sp.gammainc(a + h, x) - sp.gammainc(a - h, x)) / (2 * h)
             assert abs(dP - fd) <= 1e-6 * abs(fd) + 1e-9, (a, x, dP, fd)  # FD resolves ~1e-10
+
+
+def test_linear_parameter_doctest(goldens):
+    """galax's LinearParameter doctest (params/core.py:52-74): a Kepler mass
+    falling linearly to zero over 1 Gyr; the orbit's cylindrical radius at ten
+    save times to the printed 3 decimals."""
+    g = goldens["orbits"]["kepler_linear_mass"]
+    c = golden_comps(g["potential"])
+    saves, status, _, _ = O.integrate(c, np.array(g["y0"]), g["t0"], g["t1"], golden_save_ts(g),
+                                      golden_cfg(g["solver"]), slopes=np.array(g["slopes"]))
+    assert status[0] == 0
+    rho = np.hypot(saves[0][:, 0], saves[0][:, 1])
+    np.testing.assert_allclose(rho, g["expect_rho"], rtol=0, atol=0.5 * 10.0 ** -g["rho_decimals"] + 1e-9)
+
+
+def test_linear_parameters_evaluate_at_time():
+    """With slopes, every component is evaluated with p(t) = p(0) + slope t."""
+    c = _all_kinds()
+    rng = np.random.default_rng(4)
+    sl = rng.normal(size=(len(c), 3)) * np.stack([np.abs(c["m"]) * 1e-4, np.full(len(c), 1e-4),
+                                                   np.full(len(c), 1e-4)], axis=1)
+    sl[c["kind"] == O.KEPLER, 1:] = 0.0
+    sl[c["kind"] == O.POWERLAW_CUTOFF, 2] = 0.0
+    x = _mixed_points(16)
+    t = 37.5
+    moved = c.copy()
+    moved["m"] += sl[:, 0] * t
+    moved["l1"] += sl[:, 1] * t
+    moved["l2"] += sl[:, 2] * t
+    np.testing.assert_array_equal(O.gradient(c, x, slopes=sl, t=t), O.gradient(moved, x))
+    np.testing.assert_array_equal(O.potential(c, x, slopes=sl, t=t), O.potential(moved, x))
+    np.testing.assert_array_equal(O.hessian(c, x, slopes=sl, t=t), O.hessian(moved, x))

@@ -12,11 +12,13 @@ from .dynamics import (
     ConstantStepSize,
     Dopri5,
     Dopri8,
+    HamiltonianField,
     Integrator,
     Orbit,
     OrbitSolver,
     PhaseSpaceCoordinate,
     PIDController,
+    compute_orbit,
     evaluate_orbit,
     integrate_orbit,
 )
@@ -42,7 +44,7 @@ from .potential import (
 
 __all__ = [
     "GalaxGB300Error", "dynamics", "mockstream", "potential", "ConstantStepSize", "Dopri5", "Dopri8", "Integrator",
-    "Orbit", "OrbitSolver", "PhaseSpaceCoordinate", "PIDController", "evaluate_orbit", "integrate_orbit",
+    "Orbit", "OrbitSolver", "PhaseSpaceCoordinate", "PIDController", "compute_orbit", "evaluate_orbit", "HamiltonianField", "integrate_orbit",
     "ChenStreamDF", "Fardal2015DF", "FardalStreamDF", "MockStreamGenerator", "StreamSimulator",
     "BovyMWPotential2014", "CompositePotential", "HernquistPotential", "IsochronePotential", "KeplerPotential", "LinearParameter", "LogarithmicPotential",
     "MilkyWayPotential", "MilkyWayPotential2022", "MiyamotoNagaiPotential", "MN3ExponentialPotential",

@@ -428,6 +428,31 @@ def evaluate_orbit(pot: AbstractPotential, w0, t, /, *, integrator: Integrator |
     return orb
 
 
+@dataclass(frozen=True)
+class HamiltonianField:
+    """galax's HamiltonianField over a potential (orbit/field_hamiltonian.py:21-249):
+    (dq/dt, dp/dt) = (p, -grad Phi(q, t))."""
+
+    potential: AbstractPotential
+
+    def __call__(self, t, w):
+        """The field at time t for phase-space points w (..., 6), on the GPU."""
+        torch = _torch()
+        ww = _as_cuda(w, torch.float64).reshape(-1, 6)
+        acc = self.potential.acceleration(ww[:, :3].cpu().numpy(), t)
+        out = np.concatenate([ww[:, 3:].cpu().numpy(), np.asarray(acc).reshape(-1, 3)], axis=1)
+        return out.reshape(np.shape(w))
+
+
+def compute_orbit(field, w0, ts, /, *, solver: Integrator | None = None, dense: bool = False) -> Orbit:
+    """galax's ``compute_orbit`` (orbit/compute.py:28-66): ``evaluate_orbit``'s
+    two phases (``w0.t`` to ``ts[0]``, then saves at ``ts``) with the
+    ``OrbitSolver`` defaults (Dopri8, PID rtol = atol = 1e-8, 2**16 steps).
+    ``field`` is a potential or a HamiltonianField."""
+    pot = field.potential if isinstance(field, HamiltonianField) else field
+    return evaluate_orbit(pot, w0, ts, integrator=solver if solver is not None else OrbitSolver(), dense=dense)
+
+
 def integrate_orbit(pot: AbstractPotential, w0, t0, t1, saveat: Sequence | None = None, *,
                     integrator: Integrator | None = None, throw: bool = True):
     """Per-orbit start/end times and save grids (galax experimental/integrate.py:301-575).

@@ -255,6 +255,13 @@ class AbstractPotential:
 
         return evaluate_orbit(self, w0, t, integrator=integrator, dense=dense)
 
+    def compute_orbit(self, w0, t, *, solver=None, dense: bool = False):
+        """galax's ``AbstractPotential.compute_orbit`` (potential/_src/base.py):
+        ``dynamics.compute_orbit`` on this potential."""
+        from .dynamics import compute_orbit
+
+        return compute_orbit(self, w0, t, solver=solver, dense=dense)
+
     def __or__(self, other: "AbstractPotential") -> "CompositePotential":
         return CompositePotential(_flatten(self) + _flatten(other))
 

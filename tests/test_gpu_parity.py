@@ -411,10 +411,16 @@ def test_linear_parameter_doctest_on_gpu(gx, goldens):
     g = goldens["orbits"]["kepler_linear_mass"]
     lp = gx.LinearParameter(slope=g["slopes"][0][0], point_time=0.0, point_value=g["potential"]["m"])
     pot = gx.KeplerPotential(m_tot=lp)
-    orb = gx.evaluate_orbit(pot, np.array(g["y0"][0]), golden_save_ts(g), integrator=gx.OrbitSolver())
-    rho = np.hypot(orb.q[:, 0], orb.q[:, 1])
-    np.testing.assert_allclose(rho, g["expect_rho"], rtol=0, atol=0.5 * 10.0 ** -g["rho_decimals"] + 1e-9)
+    y0 = np.array(g["y0"][0])
+    w0 = gx.PhaseSpaceCoordinate(q=y0[:3], p=y0[3:], t=g["t0"])
+    for orb in (gx.compute_orbit(pot, w0, golden_save_ts(g)),  # the doctest's own call
+                gx.evaluate_orbit(pot, y0, golden_save_ts(g), integrator=gx.OrbitSolver())):
+        rho = np.hypot(orb.q[:, 0], orb.q[:, 1])
+        np.testing.assert_allclose(rho, g["expect_rho"], rtol=0, atol=0.5 * 10.0 ** -g["rho_decimals"] + 1e-9)
     assert not pot.is_milky_way_kernel()
+    # the Hamiltonian field at t = 500 Myr sees half the mass
+    f = gx.HamiltonianField(pot)(500.0, np.array([[5.0, 0, 0, 0, 0.2, 0]]))
+    np.testing.assert_allclose(f[0, 3], -O.G_GALACTIC * 5e11 / 25.0, rtol=1e-14)
 
 
 def _timed_kinds(seed=4):

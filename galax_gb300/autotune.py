@@ -7,8 +7,11 @@ with CUDA events on the launching stream and installs the fastest through
 queue hands whole orbits to lanes), so tuning only changes speed.
 
 Batches with very uneven orbit lengths end in a tail where the longest orbits
-run almost alone; their speed then depends on which warps happen to share a
-sub-partition with them, and shapes with many resident warps vary by up to 2x
+run almost alone; their speed then depends on which warps share a
+sub-partition with them. A GB300 FP64 warp instruction holds its
+sub-partition's FP64 pipe for ~64 cycles whatever the number of active lanes,
+so one resident warp per sub-partition lets the longest orbits advance at their
+own latency from the start. Shapes with many resident warps vary by up to 2x
 from run to run. Each candidate is therefore timed ``repeats`` times and judged
 by its slowest run.
 """
@@ -20,11 +23,15 @@ from typing import Callable, Iterable
 from . import _lib
 
 DEFAULT_CANDIDATES = (
-    # (block_threads, blocks_per_sm, variant)
-    (128, 0, 0),
-    (128, 0, 1),
-    (64, 0, 0),
+    # (block_threads, blocks_per_sm, variant); blocks_per_sm 0 = as many as fit.
+    # One warp per SM sub-partition (128 x 1, 64 x 2) keeps a long orbit's FP64
+    # instructions from queueing behind a second warp's: uneven batches end with
+    # their longest orbits running alone, and their serial latency sets the time.
+    (128, 1, 2),
+    (64, 2, 2),
+    (128, 1, 0),
     (128, 0, 2),
+    (128, 0, 0),
 )
 
 

@@ -18,7 +18,10 @@ namespace gal {
 thread_local std::string g_last_error;
 // [method 5/8][adaptive]: Dopri5 fits 3 blocks of 128 per SM without spills
 // (variant 0); Dopri8 needs the uncapped variant 2 to avoid spilling.
-static LaunchShape g_shape[2][2] = {{{0, 0, 0}, {0, 0, 0}}, {{0, 0, 2}, {0, 0, 2}}};
+// [method == 8][adaptive]. Adaptive batches default to one warp per SM
+// sub-partition (128 threads, one block per SM): their longest orbits then run
+// at their own latency instead of sharing an FP64 pipe.
+static LaunchShape g_shape[2][2] = {{{0, 0, 0}, {128, 1, 2}}, {{0, 0, 2}, {128, 1, 2}}};
 
 gal_status fail(gal_status st, const std::string& msg) {
   g_last_error = msg;

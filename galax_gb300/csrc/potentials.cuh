@@ -22,12 +22,45 @@
 
 #include <cstdint>
 
+#include "log_table.h"
+
 namespace gal {
 
 enum Kind : int32_t { KEPLER = 0, HERNQUIST = 1, MIYAMOTO_NAGAI = 2, NFW = 3, PLUMMER = 4, ISOCHRONE = 5,
                       LOGARITHMIC = 6, POWERLAW_CUTOFF = 7 };
 
 constexpr double TINY = 2.2250738585072014e-308;  // DBL_MIN, galax's safe_sqrt offset
+
+// log(1 + u) for u >= 0 (the NFW halo's log(1 + r / r_s)) by Tang's
+// table-driven method (P. T. P. Tang, "Table-driven implementation of the
+// logarithm function in IEEE floating-point arithmetic", ACM TOMS 16(4), 1990):
+// 1 + u = 2^k F_j (1 + r) with F_j = 1 + j/128 the nearest table point, so
+// |r| <= 1/256; log(F_j) is tabulated as hi + lo and log(1 + r) is its Taylor
+// polynomial to r^7 (truncation below 2e-18 relative). The rounding error of
+// 1 + u is folded into r. About 20 FP64 operations, where a lone FP64 chain
+// pays ~64 cycles for each; within ~1 unit in the last place.
+__device__ __forceinline__ double log1p_pos(double u) {
+  const double x = 1.0 + u;
+  const double c = (u <= 1.0) ? u - (x - 1.0) : 1.0 - (x - u);  // x + c = 1 + u exactly
+  const long long bits = __double_as_longlong(x);
+  const int k = (int)(bits >> 52) - 1023;
+  const long long mant = bits & 0x000FFFFFFFFFFFFFLL;
+  const double m = __longlong_as_double(mant | 0x3FF0000000000000LL);  // x = 2^k m, 1 <= m < 2
+  const int j = (int)((mant + (1LL << 44)) >> 45);                      // nearest j / 128, 0..128
+  const double F = 1.0 + (double)j * 0.0078125;                         // exact
+  const double scale = __longlong_as_double((long long)(1023 - k) << 52);  // 2^-k
+  const double r = fma(c, scale, m - F) * __ldg(&kLogTable[j][0]);       // m - F is exact
+  double q = fma(0.14285714285714285, r, -0.16666666666666666);
+  q = fma(q, r, 0.2);
+  q = fma(q, r, -0.25);
+  q = fma(q, r, 0.3333333333333333);
+  q = fma(q, r, -0.5);
+  const double p = fma(r * r, q, r);
+  const double dk = (double)k;
+  const double hi = fma(dk, 0.6931471805599453, __ldg(&kLogTable[j][1]));   // ln 2 = hi + lo
+  const double lo = fma(dk, 2.3190468138462996e-17, __ldg(&kLogTable[j][2]));
+  return hi + (lo + p);
+}
 
 // Component with parameters folded for evaluation (96 bytes).
 struct DevComp {
@@ -187,7 +220,7 @@ __device__ __forceinline__ void comp_grad(const DevComp& c, double x, double y, 
     }
     case NFW: {
       const double r = r2 * ir;
-      const double L = log1p(r * c.inv_l1);
+      const double L = log1p_pos(r * c.inv_l1);
       f = c.Gm * (ir * ir) * fma(L, ir, -1.0 / (c.l1 + r));
       break;
     }
@@ -230,7 +263,7 @@ __device__ __forceinline__ double comp_phi(const DevComp& c, double x, double y,
     case NFW: {
       const double r = sqrt(fma(dx, dx, fma(dy, dy, fma(dz, dz, TINY))));
       const double s = r * c.inv_l1;
-      return -c.Gm * c.inv_l1 * log1p(s) / s;
+      return -c.Gm * c.inv_l1 * log1p_pos(s) / s;
     }
     case ISOCHRONE: {
       const double r = sqrt(fma(dx, dx, fma(dy, dy, fma(dz, dz, TINY))));
@@ -285,7 +318,7 @@ __device__ __forceinline__ void comp_hessian(const DevComp& c, double x, double 
       break;
     }
     case NFW: {
-      const double L = log1p(r * c.inv_l1), q = c.l1 + r;
+      const double L = log1p_pos(r * c.inv_l1), q = c.l1 + r;
       g = c.Gm * (L / (r2 * r) - 1.0 / (r2 * q));
       gpr = c.Gm * (3.0 / (r2 * r2 * q) - 3.0 * L / (r2 * r2 * r) + 1.0 / (r2 * r * q * q));
       break;
@@ -444,7 +477,7 @@ struct MWPot {
     const double inv_dh = iP * q;
     const double inv_db2 = iP * dh * dn2;
     const double inv_dn2 = iP * dh * db2;
-    const double L = log1p(r * p.irs_h);
+    const double L = log1p_pos(r * p.irs_h);
     const double f = p.Gm_h * (ir * ir) * fma(L, ir, -inv_dh) + ir * fma(p.Gm_b, inv_db2, p.Gm_n * inv_dn2);
     gx = (u + f) * x;
     gy = (u + f) * y;

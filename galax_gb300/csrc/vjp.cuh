@@ -53,7 +53,7 @@ __device__ __forceinline__ void comp_vjp(const DevComp& c, const double* x, cons
       break;
     }
     case NFW: {
-      const double L = log1p(r * c.inv_l1), q = c.l1 + r, iq = 1.0 / q;
+      const double L = log1p_pos(r * c.inv_l1), q = c.l1 + r, iq = 1.0 / q;
       g = c.Gm * ir2 * fma(L, ir, -iq);
       gpr = c.Gm * ir2 * ir * (3.0 * ir * iq - 3.0 * L * ir2 + iq * iq);
       dl1 = -c.Gm * ir * c.inv_l1 * iq * iq * xv;

@@ -233,7 +233,9 @@ GAL_API gal_status gal_dense_evaluate(const gal_potential* pot, int32_t method, 
  * thread, 3 blocks of 128 per SM; 1 = at most 128 registers, 4 blocks of 128;
  * 2 = up to 255 registers, blocks up to 256 threads; variants 0 and 1 need
  * block_threads <= 128). Process-wide setting, used by the autotuner; results
- * never depend on it. */
+ * never depend on it. Defaults: adaptive runs use 128 threads, one block per SM,
+ * variant 2 (one warp per SM sub-partition); constant-step runs use 128
+ * threads at maximum occupancy (variant 0 for Dopri5, 2 for Dopri8). */
 GAL_API gal_status gal_set_launch(int32_t method, int32_t adaptive, int32_t block_threads, int32_t blocks_per_sm,
                                   int32_t variant);
 

@@ -94,6 +94,7 @@ SIGNATURES = {
     "gal_integrate_noalloc": (C.c_int, [C.c_void_p, C.POINTER(SolverConfig), _DP, _DP, _DP, _I64P, _DP, C.c_int64,
                                         _DP, _I32P, _I64P, _I32P, C.c_int64, C.c_void_p]),
     "gal_set_launch": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
+    "gal_set_team": (C.c_int, [C.c_int32]),
     "gal_dense_coef_per_step": (C.c_int32, [C.c_int32]),
     "gal_integrate_dense": (C.c_int, [C.c_void_p, C.POINTER(SolverConfig), _DP, _DP, _DP, C.c_int64, C.c_int64, _DP,
                                       _DP, _I64P, _I32P, C.c_void_p]),
@@ -132,6 +133,7 @@ SIGNATURES = {
                                           C.c_int32, _VP, C.c_size_t, C.c_void_p]),
     "gal_tableau": (C.c_int32, [C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "gal_fp64_peak_probe": (C.c_int, [C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_void_p]),
+    "gal_fp64_latency_probe": (C.c_int, [C.c_int32, C.c_int32, C.POINTER(C.c_double)]),
     "gal_status_string": (C.c_char_p, [C.c_int32]),
     "gal_last_error": (C.c_char_p, []),
     "gal_abi_version": (C.c_int32, []),

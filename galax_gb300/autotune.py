@@ -41,27 +41,53 @@ def set_launch(method: int, adaptive: bool, block: int, per_sm: int, variant: in
                "gal_set_launch")
 
 
-def tune(run: Callable[[], object], method: int, adaptive: bool,
-         candidates: Iterable[tuple[int, int, int]] = DEFAULT_CANDIDATES, repeats: int = 2) -> dict:
-    """Run ``run()`` under each candidate ``repeats`` times, keep the one whose
-    slowest run is fastest; returns those timings."""
+# SMs given to four-warp teams for the longest orbits (second pass of a
+# two-pass Dopri5 Milky Way batch, gal_set_team)
+DEFAULT_TEAMS = (16, 32, 48)
+
+
+def set_team(blocks: int) -> None:
+    L = _lib.load()
+    _lib.check(L.gal_set_team(int(blocks)), "gal_set_team")
+
+
+def _worst_ms(run: Callable[[], object], repeats: int) -> float:
     import torch
 
+    stream = torch.cuda.current_stream()
+    worst = 0.0
+    for _ in range(repeats):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        run()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        worst = max(worst, e0.elapsed_time(e1))
+    return worst
+
+
+def tune(run: Callable[[], object], method: int, adaptive: bool,
+         candidates: Iterable[tuple[int, int, int]] = DEFAULT_CANDIDATES, repeats: int = 2,
+         teams: Iterable[int] = DEFAULT_TEAMS) -> dict:
+    """Run ``run()`` under each launch-shape candidate ``repeats`` times and keep
+    the one whose slowest run is fastest; then, for adaptive Dopri5, the same
+    over the number of SMs given to four-warp teams. Returns the timings."""
     timings = {}
     for cand in candidates:
         set_launch(method, adaptive, *cand)
-        stream = torch.cuda.current_stream()
-        worst = 0.0
-        for _ in range(repeats):
-            torch.cuda.synchronize()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            run()
-            e1.record(stream)
-            torch.cuda.synchronize()
-            worst = max(worst, e0.elapsed_time(e1))
-        timings[cand] = worst
+        timings[cand] = _worst_ms(run, repeats)
     best = min(timings, key=timings.get)
     set_launch(method, adaptive, *best)
-    return {"best": {"block_threads": best[0], "blocks_per_sm": best[1], "variant": best[2]},
-            "ms": {f"{b}x{s}v{v}": round(t, 3) for (b, s, v), t in timings.items()}}
+    out = {"best": {"block_threads": best[0], "blocks_per_sm": best[1], "variant": best[2]},
+           "ms": {f"{b}x{s}v{v}": round(t, 3) for (b, s, v), t in timings.items()}}
+    if method == 5 and adaptive and teams:
+        tt = {}
+        for blocks in teams:
+            set_team(blocks)
+            tt[blocks] = _worst_ms(run, repeats)
+        tbest = min(tt, key=tt.get)
+        set_team(tbest)
+        out["best"]["team_blocks"] = tbest
+        out["team_ms"] = {str(k): round(v, 3) for k, v in tt.items()}
+    return out

@@ -23,6 +23,12 @@ LIB = LIBDIR / "libgalax_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
          "-Xcompiler", "-fvisibility=hidden"]
+# The integrators' translation units: their kernels must agree bit for bit
+# although their code is arranged differently (the one-thread and four-warp
+# team kernels, the save path and dense output). Without implicit multiply-add
+# contraction every operation is the one written (explicit fma() stays fused),
+# so the same source arithmetic rounds identically in every kernel.
+PER_FILE = {name: ["-fmad=false"] for name in ("integrate_dopri5.cu", "integrate_dopri8.cu", "dense.cu")}
 
 
 def nvcc() -> str:
@@ -54,7 +60,7 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
 
     def compile_one(src: Path) -> Path:
         obj = BUILD / (src.stem + ".o")
-        cmd = [cc, *ARCH, *FLAGS, *extra, "-c", str(src), "-o", str(obj)]
+        cmd = [cc, *ARCH, *FLAGS, *PER_FILE.get(src.name, []), *extra, "-c", str(src), "-o", str(obj)]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {src.name}:\n{r.stderr}")

@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -21,6 +22,25 @@ thread_local std::string g_last_error;
 // [method == 8][adaptive]. Adaptive batches default to one warp per SM
 // sub-partition (128 threads, one block per SM): their longest orbits then run
 // at their own latency instead of sharing an FP64 pipe.
+static int g_team_blocks = 32;  // SMs given to four-warp teams for the longest orbits (gal_set_team)
+
+// One library-owned stream per device for the team kernel, created on first use.
+static cudaError_t team_stream(cudaStream_t* out) {
+  static std::mutex mu;
+  static cudaStream_t streams[64] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(mu);
+  if (!streams[dev]) {
+    e = cudaStreamCreateWithFlags(&streams[dev], cudaStreamNonBlocking);
+    if (e != cudaSuccess) return e;
+  }
+  *out = streams[dev];
+  return cudaSuccess;
+}
+
 static LaunchShape g_shape[2][2] = {{{0, 0, 0}, {128, 1, 2}}, {{0, 0, 2}, {128, 1, 2}}};
 
 gal_status fail(gal_status st, const std::string& msg) {
@@ -174,6 +194,29 @@ __global__ void k_fp64_probe(int64_t iters, double seed, double* sink) {
   }
   const double s = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
   if (s == 12345.678) sink[threadIdx.x] = s;  // keep the chain alive
+}
+
+// Lone-chain latency: one thread of one warp runs `iters` dependent
+// operations of one kind; cycles measured with clock64 on the device.
+__global__ void k_fp64_latency(int which, int iters, double seed, long long* cycles, double* sink) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double x = seed;
+  const long long t0 = clock64();
+  for (int i = 0; i < iters; ++i) {
+    switch (which) {
+      case 0: x = fma(x, 0.999999, 1e-7); break;
+      case 1: x = log1p(x) + 0.5; break;
+      case 2: x = log1p_pos(x) + 0.5; break;
+      case 3: x = rsqrt(x) + 0.5; break;
+      case 4: x = sqrt(x) + 0.5; break;
+      case 5: x = 1.0 / x + 0.5; break;
+      case 6: x = exp(-x) + 0.5; break;
+      default: x = log(x) + 2.0; break;
+    }
+  }
+  const long long t1 = clock64();
+  *cycles = t1 - t0;
+  *sink = x;
 }
 
 gal_status validate_cfg(const gal_solver_config* c) {
@@ -460,6 +503,12 @@ gal_status gal_integrate_workspace_size(const gal_solver_config* cfg, int64_t n,
   return GAL_OK;
 }
 
+gal_status gal_set_team(int32_t blocks) {
+  if (blocks < 0 || blocks > 1024) return fail(GAL_ERR_INVALID_ARGUMENT, "team blocks must be in [0, 1024]");
+  g_team_blocks = blocks;
+  return GAL_OK;
+}
+
 gal_status gal_set_launch(int32_t method, int32_t adaptive, int32_t block_threads, int32_t blocks_per_sm,
                           int32_t variant) {
   if ((method != 5 && method != 8) || block_threads < 0 || block_threads > 256 || (block_threads % 32) ||
@@ -560,6 +609,32 @@ gal_status gal_integrate(const gal_potential* p, const gal_solver_config* cfg, c
   a.phase = 1;
   a.order = order2;
   a.queue_len = qlen;
+  const int sms = device_sm_count();
+  const int blocks = g_team_blocks < sms - 1 ? g_team_blocks : sms - 1;
+  if (blocks > 0 && p->is_mw && cfg->method == 5) {
+    // The longest orbits go to four-warp teams on `blocks` SMs of their own
+    // (second stream), the rest to the one-thread kernel on the other SMs, one
+    // block per SM; results are the same either way.
+    const long long tcap = (long long)kTeamLanes * blocks;
+    cudaStream_t ts = nullptr;
+    e = team_stream(&ts);
+    cudaEvent_t fork = nullptr, join = nullptr;
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&join, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventRecord(fork, s);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(ts, fork, 0);
+    if (e == cudaSuccess) e = launch_integrate_team(a, p->mw, reinterpret_cast<unsigned long long*>(ws + 528), tcap,
+                                                    blocks, kExclusiveSmem, ts);
+    if (e == cudaSuccess) e = cudaEventRecord(join, ts);
+    if (e == cudaSuccess) {
+      a.queue_base = tcap;
+      e = launch_integrate_dopri5_exclusive(a, p->mw, shape.variant, sms - blocks, kExclusiveSmem, s);
+    }
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, join, 0);
+    if (fork) cudaEventDestroy(fork);
+    if (join) cudaEventDestroy(join);
+    return e == cudaSuccess ? GAL_OK : cuda_fail(e, "integrate kernel launch (second pass, teams)");
+  }
   e = launch();
   return e == cudaSuccess ? GAL_OK : cuda_fail(e, "integrate kernel launch (second pass)");
 }
@@ -581,6 +656,24 @@ int32_t gal_tableau(int32_t method, double* c, double* a, double* b, double* e) 
     return TB::S;
   };
   return method == 5 ? copy(Dopri5{}) : copy(Dopri8{});
+}
+
+gal_status gal_fp64_latency_probe(int32_t which, int32_t iters, double* cycles_per_op) {
+  if (which < 0 || which > 7 || iters < 1 || !cycles_per_op) return fail(GAL_ERR_INVALID_ARGUMENT, "bad probe arguments");
+  long long* d = nullptr;
+  cudaError_t e = cudaMalloc(&d, 2 * sizeof(long long));
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(latency probe)");
+  double* sink = reinterpret_cast<double*>(d + 1);
+  long long c = 0;
+  for (int rep = 0; rep < 2 && e == cudaSuccess; ++rep) {  // the first run warms the instruction cache
+    k_fp64_latency<<<1, 32>>>(which, iters, 1.3, d, sink);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpy(&c, d, sizeof(c), cudaMemcpyDeviceToHost);
+  }
+  cudaFree(d);
+  if (e != cudaSuccess) return cuda_fail(e, "latency probe");
+  *cycles_per_op = (double)c / iters;
+  return GAL_OK;
 }
 
 gal_status gal_fp64_peak_probe(int64_t iters, double* ms, double* flops, gal_stream_t stream) {

@@ -36,6 +36,8 @@ namespace gal {
 
 enum { ORBIT_OK = 0, ORBIT_MAX_STEPS = 1, ORBIT_DT_MIN = 2, ORBIT_NONFINITE = 3 };
 
+constexpr int kTeamLanes = 32;  // orbits per four-warp team block (integrate_team.cuh)
+
 // Everything needed to continue an orbit exactly where a first pass parked it
 // (state, step times, controller memory, counters, save cursor). 128 bytes.
 struct OrbitResume {
@@ -70,6 +72,7 @@ struct IntegrateArgs {
   int64_t n;
   unsigned long long* queue;  // work-queue counter (scratch)
   const DevLinear* lin;       // time-dependent component parameters (table kernel), or NULL
+  long long queue_base;       // first queue position of this launch (earlier ones belong to a team kernel)
   // two-phase schedule: phase 0 parks every orbit once it has covered split_frac
   // of its span; phase 1 resumes the parked orbits from `resume` in `order`
   int32_t phase;
@@ -289,13 +292,14 @@ __device__ __forceinline__ bool start_orbit(const IntegrateArgs& a, const Pot& p
                                             bool& first) {
   const unsigned long long qlen = a.queue_len ? *a.queue_len : (unsigned long long)a.n;
   const unsigned long long striped = (unsigned long long)gridDim.x * blockDim.x;
+  const unsigned long long base = (unsigned long long)a.queue_base;
   while (true) {
     unsigned long long k;
     if (first) {
       first = false;
-      k = first_position();
+      k = base + first_position();
     } else {
-      k = striped + atomicAdd(a.queue, 1ULL);
+      k = base + striped + atomicAdd(a.queue, 1ULL);
     }
     if (k >= qlen) return false;
     const int64_t o = a.order ? (int64_t)a.order[k] : (int64_t)k;

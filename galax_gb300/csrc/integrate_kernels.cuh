@@ -37,6 +37,30 @@ void mw_launch(int variant, unsigned grid, int block, cudaStream_t stream, const
   }
 }
 
+// The Milky Way kernel on `grid` blocks with `smem` bytes of dynamic shared
+// memory that it does not use: a request above half an SM's capacity keeps
+// every other block that makes such a request off its SM.
+template <class TB>
+cudaError_t mw_launch_exclusive(int variant, unsigned grid, int block, size_t smem, cudaStream_t stream,
+                                const IntegrateArgs& a, const MWParams& p) {
+  cudaError_t e;
+  switch (variant) {
+    case 1:
+      e = cudaFuncSetAttribute(k_integrate_mw<TB, 128, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e == cudaSuccess) k_integrate_mw<TB, 128, 4><<<grid, block, smem, stream>>>(a, p);
+      break;
+    case 2:
+      e = cudaFuncSetAttribute(k_integrate_mw<TB, 256, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e == cudaSuccess) k_integrate_mw<TB, 256, 1><<<grid, block, smem, stream>>>(a, p);
+      break;
+    default:
+      e = cudaFuncSetAttribute(k_integrate_mw<TB, 128, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e == cudaSuccess) k_integrate_mw<TB, 128, 3><<<grid, block, smem, stream>>>(a, p);
+      break;
+  }
+  return e == cudaSuccess ? cudaGetLastError() : e;
+}
+
 template <class TB, bool TIMED>
 __global__ void __launch_bounds__(kMaxBlock) k_integrate_table(IntegrateArgs a, const DevComp* comps, int ncomp) {
   extern __shared__ __align__(16) unsigned char smem_raw[];

@@ -18,6 +18,18 @@ cudaError_t launch_integrate_dopri5(const IntegrateArgs& a, bool mw, const MWPar
 cudaError_t launch_integrate_dopri8(const IntegrateArgs& a, bool mw, const MWParams& p, const DevComp* comps,
                                     int ncomp, LaunchShape shape, cudaStream_t stream);
 
+// Four-warp teams (32 orbits per block) for queue positions [0, tcap) of a
+// second-pass Milky Way Dopri5 batch; *tqueue must be zero. smem: dynamic
+// shared memory requested (unused) to hold each team block's SM alone.
+cudaError_t launch_integrate_team(const IntegrateArgs& a, const MWParams& p, unsigned long long* tqueue,
+                                  long long tcap, int blocks, size_t smem, cudaStream_t stream);
+// The one-thread Milky Way Dopri5 kernel, 128 threads per block, `grid` blocks,
+// each requesting `smem` bytes (unused) so that blocks of this launch and of the
+// team launch never share an SM.
+cudaError_t launch_integrate_dopri5_exclusive(const IntegrateArgs& a, const MWParams& p, int variant, int grid,
+                                              size_t smem, cudaStream_t stream);
+constexpr size_t kExclusiveSmem = 120 * 1024;
+
 int device_sm_count();
 
 }  // namespace gal

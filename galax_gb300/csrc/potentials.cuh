@@ -456,32 +456,58 @@ struct MWParams {
   double Gm_n, rs_n;        // nucleus
 };
 
+// The Milky Way gradient in four pieces, shared by MWPot::grad and the
+// four-warp team kernel (which evaluates the pieces on different warps), so
+// that both produce bitwise-identical results.
+struct MWDisk {
+  double u, us, izb;  // Gm_d / D^3, u s, 1 / sqrt(z^2 + b^2)
+};
+__device__ __forceinline__ MWDisk mw_disk(const MWParams& p, double x, double y, double z) {
+  const double zb2 = fma(z, z, p.b2_d);
+  const double izb = rsqrt(zb2);
+  const double s = fma(zb2, izb, p.a_d);
+  const double R2 = fma(x, x, y * y);
+  const double iD = rsqrt(fma(s, s, R2));
+  const double u = p.Gm_d * (iD * iD) * iD;
+  return MWDisk{u, u * s, izb};
+}
+// centred spheres: 1/r and r
+__device__ __forceinline__ double mw_ir(double x, double y, double z, double& r) {
+  const double R2 = fma(x, x, y * y);
+  const double r2 = fma(z, z, R2 + TINY);
+  const double ir = rsqrt(r2);
+  r = r2 * ir;
+  return ir;
+}
+struct MWRecip {
+  double inv_dh, inv_db2, inv_dn2;
+};
+// one reciprocal for 1/(r + rs_h), 1/(r + rs_b)^2, 1/(r + rs_n)^2
+__device__ __forceinline__ MWRecip mw_recip(const MWParams& p, double r) {
+  const double dh = p.rs_h + r, db = r + p.rs_b, dn = r + p.rs_n;
+  const double db2 = db * db, dn2 = dn * dn;
+  const double q = db2 * dn2;
+  const double iP = 1.0 / (dh * q);
+  return MWRecip{iP * q, iP * dh * dn2, iP * dh * db2};
+}
+__device__ __forceinline__ double mw_halo_log(const MWParams& p, double r) { return log1p_pos(r * p.irs_h); }
+// radial factor of the three spheres
+__device__ __forceinline__ double mw_f(const MWParams& p, double ir, double L, const MWRecip& c) {
+  return p.Gm_h * (ir * ir) * fma(L, ir, -c.inv_dh) + ir * fma(p.Gm_b, c.inv_db2, p.Gm_n * c.inv_dn2);
+}
+
 struct MWPot {
   MWParams p;
   __device__ __forceinline__ void grad(double x, double y, double z, double& gx, double& gy, double& gz) const {
-    // disk
-    const double zb2 = fma(z, z, p.b2_d);
-    const double izb = rsqrt(zb2);
-    const double s = fma(zb2, izb, p.a_d);
-    const double R2 = fma(x, x, y * y);
-    const double iD = rsqrt(fma(s, s, R2));
-    const double u = p.Gm_d * (iD * iD) * iD;
-    // centred spheres share r
-    const double r2 = fma(z, z, R2 + TINY);
-    const double ir = rsqrt(r2);
-    const double r = r2 * ir;
-    const double dh = p.rs_h + r, db = r + p.rs_b, dn = r + p.rs_n;
-    const double db2 = db * db, dn2 = dn * dn;
-    const double q = db2 * dn2;
-    const double iP = 1.0 / (dh * q);  // one reciprocal for 1/dh, 1/db^2, 1/dn^2
-    const double inv_dh = iP * q;
-    const double inv_db2 = iP * dh * dn2;
-    const double inv_dn2 = iP * dh * db2;
-    const double L = log1p_pos(r * p.irs_h);
-    const double f = p.Gm_h * (ir * ir) * fma(L, ir, -inv_dh) + ir * fma(p.Gm_b, inv_db2, p.Gm_n * inv_dn2);
-    gx = (u + f) * x;
-    gy = (u + f) * y;
-    gz = fma(u * s, izb, f) * z;
+    const MWDisk d = mw_disk(p, x, y, z);
+    double r;
+    const double ir = mw_ir(x, y, z, r);
+    const MWRecip c = mw_recip(p, r);
+    const double L = mw_halo_log(p, r);
+    const double f = mw_f(p, ir, L, c);
+    gx = (d.u + f) * x;
+    gy = (d.u + f) * y;
+    gz = fma(d.us, d.izb, f) * z;
   }
 };
 

@@ -238,6 +238,14 @@ GAL_API gal_status gal_dense_evaluate(const gal_potential* pot, int32_t method, 
  * threads at maximum occupancy (variant 0 for Dopri5, 2 for Dopri8). */
 GAL_API gal_status gal_set_launch(int32_t method, int32_t adaptive, int32_t block_threads, int32_t blocks_per_sm,
                                   int32_t variant);
+/* Second pass of a two-pass Dopri5 batch in the Milky Way model: `blocks` > 0
+ * (default 32, at most the SM count - 1) hands the 32 x blocks longest orbits to
+ * four-warp team blocks, each on an SM of its own, on a library-owned stream
+ * beside the one-thread-per-orbit kernel, which runs one block per remaining
+ * SM; 0 keeps every orbit on the one-thread kernel with the launch shape of
+ * gal_set_launch. Results are bitwise identical either way; the teams cut the
+ * serial latency of the longest orbits. Process-wide. */
+GAL_API gal_status gal_set_team(int32_t blocks);
 
 /* ------------------------------------------------------------------ adjoint */
 /* Scratch bytes gal_adjoint needs for n orbits with checkpoints every k_ckpt steps. */
@@ -429,6 +437,11 @@ GAL_API int32_t gal_tableau(int32_t method, double* c, double* a, double* b, dou
  * a full-device grid and writes the elapsed device time (ms) to *ms. Used to
  * measure the chip's FP64 peak for roofline reporting. */
 GAL_API gal_status gal_fp64_peak_probe(int64_t iters, double* ms, double* flops, gal_stream_t stream);
+/* Lone-chain latency probe (synchronous, default stream): one thread runs
+ * `iters` dependent operations and *cycles_per_op receives SM cycles per
+ * operation. which: 0 FMA, 1 log1p, 2 the library's table-driven log1p,
+ * 3 rsqrt, 4 sqrt, 5 division, 6 exp, 7 log (each but FMA plus one add). */
+GAL_API gal_status gal_fp64_latency_probe(int32_t which, int32_t iters, double* cycles_per_op);
 GAL_API const char* gal_status_string(int32_t status);
 GAL_API const char* gal_last_error(void);
 GAL_API int32_t gal_abi_version(void);

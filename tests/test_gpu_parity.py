@@ -487,3 +487,44 @@ def test_time_dependent_potentials_are_refused_where_unsupported(gx):
     y0 = _ics(4, 1)
     with pytest.raises(GalaxGB300Error):
         orbit_adjoint(pot, y0, 0.0, 10.0, dt=1.0, target=y0, method=8, k_ckpt=4)
+
+
+# ------------------------------------------------------------------ four-warp teams for the longest orbits
+def _set_team(blocks):
+    from galax_gb300 import _lib
+
+    _lib.check(_lib.load().gal_set_team(int(blocks)), "gal_set_team")
+
+
+@pytest.mark.parametrize("case", ["csr_forward", "shared_grid_backward", "few_orbits", "max_steps"])
+def test_team_kernel_is_bitwise_identical(gx, case):
+    """The second pass with the longest orbits on four-warp teams gives the
+    same saves, statuses and step counts, bit for bit, as the one-thread
+    kernel alone."""
+    from galax_gb300 import workloads as W
+    from galax_gb300.dynamics import integrate
+
+    mw = gx.MilkyWayPotential()
+    n = {"csr_forward": 12000, "shared_grid_backward": 6000, "few_orbits": 300, "max_steps": 3000}[case]
+    b = W.uneven_ics(lambda x: O.gradient(O.milky_way(), x), n, seed=8, tmax=1500.0, smax=40)
+    max_steps = 2000 if case == "max_steps" else 2**16
+    cfg = gx.Integrator(solver=gx.Dopri5(), stepsize_controller=gx.PIDController(rtol=1e-8, atol=1e-10),
+                        max_steps=max_steps).config()
+    res = []
+    try:
+        for team in (0, 8, 100):
+            _set_team(team)
+            if case == "shared_grid_backward":
+                ts = np.linspace(0.0, -400.0, 17)
+                out, st, steps = integrate(mw, b.y0, 0.0, -400.0, ts, cfg)
+            else:
+                out, st, steps = integrate(mw, b.y0, b.t0, b.t1, b.save_ts, cfg, save_offsets=b.save_offsets)
+            res.append((out.cpu().numpy(), st.cpu().numpy(), steps.cpu().numpy()))
+    finally:
+        _set_team(32)
+    for other in res[1:]:
+        np.testing.assert_array_equal(res[0][1], other[1])
+        np.testing.assert_array_equal(res[0][2], other[2])
+        np.testing.assert_array_equal(res[0][0], other[0])
+    if case == "max_steps":
+        assert (res[1][1] == 1).any()  # some orbits ran out of steps, on the team path too

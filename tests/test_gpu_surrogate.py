@@ -118,7 +118,9 @@ def test_tensor_core_inference_matches_fp32(env, n):
 
 def test_zero_network_surrogate_equals_plain_integrator(env):
     """With an MLP whose output is identically zero the surrogate integrator must
-    reproduce the plain constant-step Dopri5 kernel on the analytic part."""
+    reproduce the plain constant-step Dopri5 kernel on the analytic part, to
+    rounding: the plain integrator compiles without implicit multiply-add
+    contraction, the surrogate's stage kernels with it."""
     gx, S = env
     from galax_gb300 import workloads as W
     from galax_gb300.dynamics import integrate
@@ -135,7 +137,7 @@ def test_zero_network_surrogate_equals_plain_integrator(env):
         cfg = gx.Integrator(solver=gx.Dopri5(), stepsize_controller=gx.ConstantStepSize(), dt0=1.0).config()
         out, st, steps = integrate(mw, y0, 0.0, 100.0, np.array([100.0]), cfg)
         ref = out[:, 0, :].t().cpu().numpy()
-        np.testing.assert_allclose(yT, ref, rtol=1e-13, atol=1e-15)
+        np.testing.assert_allclose(yT, ref, rtol=1e-12, atol=1e-15)
 
 
 def test_surrogate_integrator_with_table_potential(env):

@@ -628,7 +628,8 @@ gal_status gal_integrate(const gal_potential* p, const gal_solver_config* cfg, c
     if (e == cudaSuccess) e = cudaEventRecord(join, ts);
     if (e == cudaSuccess) {
       a.queue_base = tcap;
-      e = launch_integrate_dopri5_exclusive(a, p->mw, shape.variant, sms - blocks, kExclusiveSmem, s);
+      // one warp per sub-partition: two (256 threads) made the step 1.4x longer
+      e = launch_integrate_dopri5_exclusive(a, p->mw, shape.variant, 128, sms - blocks, kExclusiveSmem, s);
     }
     if (e == cudaSuccess) e = cudaStreamWaitEvent(s, join, 0);
     if (fork) cudaEventDestroy(fork);

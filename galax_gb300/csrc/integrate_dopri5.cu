@@ -17,8 +17,9 @@ cudaError_t launch_integrate_team(const IntegrateArgs& a, const MWParams& p, uns
   return cudaGetLastError();
 }
 
-cudaError_t launch_integrate_dopri5_exclusive(const IntegrateArgs& a, const MWParams& p, int variant, int grid,
-                                              size_t smem, cudaStream_t stream) {
-  return mw_launch_exclusive<Dopri5>(variant, (unsigned)grid, 128, smem, stream, a, p);
+cudaError_t launch_integrate_dopri5_exclusive(const IntegrateArgs& a, const MWParams& p, int variant, int block,
+                                              int grid, size_t smem, cudaStream_t stream) {
+  if (variant != 2 && block > 128) block = 128;  // variants 0 and 1 are built for at most 128 threads
+  return mw_launch_exclusive<Dopri5>(variant, (unsigned)grid, block, smem, stream, a, p);
 }
 }  // namespace gal

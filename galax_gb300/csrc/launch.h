@@ -23,11 +23,11 @@ cudaError_t launch_integrate_dopri8(const IntegrateArgs& a, bool mw, const MWPar
 // shared memory requested (unused) to hold each team block's SM alone.
 cudaError_t launch_integrate_team(const IntegrateArgs& a, const MWParams& p, unsigned long long* tqueue,
                                   long long tcap, int blocks, size_t smem, cudaStream_t stream);
-// The one-thread Milky Way Dopri5 kernel, 128 threads per block, `grid` blocks,
-// each requesting `smem` bytes (unused) so that blocks of this launch and of the
-// team launch never share an SM.
-cudaError_t launch_integrate_dopri5_exclusive(const IntegrateArgs& a, const MWParams& p, int variant, int grid,
-                                              size_t smem, cudaStream_t stream);
+// The one-thread Milky Way Dopri5 kernel, `block` threads per block, `grid`
+// blocks, each requesting `smem` bytes (unused) so that blocks of this launch
+// and of the team launch never share an SM.
+cudaError_t launch_integrate_dopri5_exclusive(const IntegrateArgs& a, const MWParams& p, int variant, int block,
+                                              int grid, size_t smem, cudaStream_t stream);
 constexpr size_t kExclusiveSmem = 120 * 1024;
 
 int device_sm_count();

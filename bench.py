@@ -330,14 +330,16 @@ def run_ours(args) -> dict | None:
     d2h = h_out.numel() * 8 + h_status.numel() * 4
 
     def e2e_step():
+        # inputs copied in; saves and statuses written by the kernels straight
+        # into the pinned host buffers (device-visible host memory), so their
+        # transfer overlaps the integration
         dy0 = h_y0.to(dev, non_blocking=True)
         dt0 = h_t0.to(dev, non_blocking=True)
         dt1 = h_t1.to(dev, non_blocking=True)
         doffs = h_offs.to(dev, non_blocking=True)
         dts = h_ts.to(dev, non_blocking=True)
-        o, s, _ = integrate(mw, dy0, dt0, dt1, dts, cfg, save_offsets=doffs, order=order, soa=True, workspace=ws)
-        h_out.copy_(o, non_blocking=True)
-        h_status.copy_(s, non_blocking=True)
+        integrate(mw, dy0, dt0, dt1, dts, cfg, save_offsets=doffs, order=order, soa=True, workspace=ws,
+                  out=h_out, status=h_status)
 
     e2e_step()
     torch.cuda.synchronize()
@@ -375,7 +377,8 @@ def run_ours(args) -> dict | None:
                    "parallelism": f"orbit shards x{world}, no collective",
                    "schedule": "two passes, longest remaining work first", "launch_autotune": tuning},
         "e2e": {"value": e2e_value, "unit": "orbit-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "ms_per_step": e2e_ms, "path": "pinned host -> gal_integrate -> pinned host"},
+                "ms_per_step": e2e_ms, "path": "pinned host -> gal_integrate -> pinned host (saves written by the "
+                                                "kernels into device-visible pinned memory)"},
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak["tflops"], "unit": "TFLOP/s",
                      "frac": achieved / peak["tflops"], "traffic": traffic,
                      "flops_per_accepted_step": f_step,

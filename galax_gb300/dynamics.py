@@ -197,6 +197,19 @@ def _as_cuda(x, dtype):
     return torch.as_tensor(a, dtype=dtype, device="cuda")
 
 
+def _result_buffer(buf, shape, dtype, name):
+    """A caller-given output (CUDA or pinned host, contiguous, right shape and
+    dtype) or a new CUDA tensor."""
+    torch = _torch()
+    if buf is None:
+        return torch.empty(shape, dtype=dtype, device="cuda")
+    if not isinstance(buf, torch.Tensor) or buf.dtype != dtype or tuple(buf.shape) != tuple(shape):
+        raise ValueError(f"{name} must be a {dtype} tensor of shape {tuple(shape)}")
+    if not buf.is_contiguous() or not (buf.is_cuda or buf.is_pinned()):
+        raise ValueError(f"{name} must be contiguous, on the GPU or in pinned host memory")
+    return buf
+
+
 def integrate(
     pot: AbstractPotential,
     y0,
@@ -210,6 +223,8 @@ def integrate(
     soa: bool = False,
     stream=None,
     workspace: Workspace | None = None,
+    out=None,
+    status=None,
 ):
     """Integrate n orbits on the current CUDA device.
 
@@ -217,6 +232,11 @@ def integrate(
     save_ts: (T,) shared by all orbits, or the flat CSR values with
     ``save_offsets`` (n+1,). Returns (out, status, steps) with out of shape
     (6, T, n) for a shared grid or (6, total) for CSR saves. Asynchronous.
+
+    ``out`` (float64) and ``status`` (int32), if given, receive the results in
+    place: contiguous CUDA tensors of those shapes, or pinned host tensors,
+    which the kernels then write directly (device-visible host memory under
+    unified addressing), overlapping the transfer with the integration.
     """
     torch = _torch()
     y = _as_cuda(y0, torch.float64)
@@ -235,12 +255,13 @@ def integrate(
         # the kernel indexes saves through these offsets: reject inconsistent ones before launch
         if int(offs[0]) != 0 or int(offs[-1]) != total or bool((offs[1:] < offs[:-1]).any()):
             raise ValueError("save_offsets must start at 0, be non-decreasing and end at len(save_ts)")
-        out = torch.empty((6, total), dtype=torch.float64, device="cuda")
+        shape = (6, total)
         offs_ptr, n_saves = offs.data_ptr(), total
     else:
-        out = torch.empty((6, ts.numel(), n), dtype=torch.float64, device="cuda")
+        shape = (6, ts.numel(), n)
         offs_ptr, n_saves = None, ts.numel()
-    status = torch.empty(n, dtype=torch.int32, device="cuda")
+    out = _result_buffer(out, shape, torch.float64, "out")
+    status = _result_buffer(status, (n,), torch.int32, "status")
     steps = torch.empty(n, dtype=torch.int64, device="cuda")
     ordp = None
     if order is not None:

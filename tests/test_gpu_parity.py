@@ -528,3 +528,28 @@ def test_team_kernel_is_bitwise_identical(gx, case):
         np.testing.assert_array_equal(res[0][0], other[0])
     if case == "max_steps":
         assert (res[1][1] == 1).any()  # some orbits ran out of steps, on the team path too
+
+
+def test_results_written_straight_into_pinned_host_memory(gx):
+    """``out``/``status`` may be pinned host tensors: the kernels write them
+    directly (device-visible host memory), with the same bits as device outputs."""
+    import torch
+
+    from galax_gb300 import workloads as W
+    from galax_gb300.dynamics import integrate
+
+    mw = gx.MilkyWayPotential()
+    b = W.uneven_ics(lambda x: O.gradient(O.milky_way(), x), 3000, seed=12, tmax=800.0, smax=30)
+    cfg = gx.Integrator(solver=gx.Dopri5(), stepsize_controller=gx.PIDController(rtol=1e-8, atol=1e-10)).config()
+    out_d, st_d, steps_d = integrate(mw, b.y0, b.t0, b.t1, b.save_ts, cfg, save_offsets=b.save_offsets)
+    h_out = torch.empty(tuple(out_d.shape), dtype=torch.float64).pin_memory()
+    h_st = torch.empty(tuple(st_d.shape), dtype=torch.int32).pin_memory()
+    o, s, steps = integrate(mw, b.y0, b.t0, b.t1, b.save_ts, cfg, save_offsets=b.save_offsets, out=h_out,
+                            status=h_st)
+    torch.cuda.synchronize()
+    assert o is h_out and s is h_st
+    np.testing.assert_array_equal(h_out.numpy(), out_d.cpu().numpy())
+    np.testing.assert_array_equal(h_st.numpy(), st_d.cpu().numpy())
+    with pytest.raises(ValueError):
+        integrate(mw, b.y0, b.t0, b.t1, b.save_ts, cfg, save_offsets=b.save_offsets,
+                  out=torch.empty(3, dtype=torch.float64))

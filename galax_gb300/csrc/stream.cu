@@ -227,6 +227,112 @@ __device__ __forceinline__ void team_step(const DevComp* comps, int ncomp, doubl
   __syncthreads();
 }
 
+// team_step for a Milky Way host: the gradient split as in the integrators'
+// four-warp teams (warp 0: radius and shared reciprocal, warp 1: NFW log,
+// warp 3: disk; mw_* pieces), combined on lanes 0-2 of warp 0. The NFW log,
+// the longest chain, no longer shares a warp with the rest of its component.
+template <class TB>
+__device__ __forceinline__ void team_step_mw(const MWParams& p, double hs, double* Qk, double* sy,
+                                             double (*sF)[6], double* sY, double* sw, int warp, int lane) {
+  constexpr int S = TB::S;
+  const bool comb = warp == 0 && lane < 6;
+  // sw: [0] ir, [1] inv_dh, [2] inv_db2, [3] inv_dn2, [4] L, [5] u, [6] us, [7] izb
+  auto slope = [&](int I) {
+    __syncthreads();  // sY complete
+    if (lane == 0) {
+      const double x = sY[0], y = sY[1], z = sY[2];
+      if (warp == 0) {
+        double r;
+        const double ir = mw_ir(x, y, z, r);
+        const MWRecip c = mw_recip(p, r);
+        sw[0] = ir;
+        sw[1] = c.inv_dh;
+        sw[2] = c.inv_db2;
+        sw[3] = c.inv_dn2;
+      } else if (warp == 1) {
+        double r;
+        mw_ir(x, y, z, r);
+        sw[4] = mw_halo_log(p, r);
+      } else if (warp == 3) {
+        const MWDisk d = mw_disk(p, x, y, z);
+        sw[5] = d.u;
+        sw[6] = d.us;
+        sw[7] = d.izb;
+      }
+    }
+    __syncthreads();  // pieces complete
+    if (comb) {
+      double f;
+      if (lane < 3) {
+        f = sY[lane + 3];
+      } else {
+        const MWRecip c{sw[1], sw[2], sw[3]};
+        const double fr = mw_f(p, sw[0], sw[4], c);
+        const int j = lane - 3;
+        const double g = (j == 2) ? fma(sw[6], sw[7], fr) * sY[2] : (sw[5] + fr) * sY[j];
+        f = -g;
+      }
+      sF[I][lane] = f;
+      if (Qk && lane < 3) Qk[3 * I + lane] = sY[lane];
+    }
+  };
+  if (comb) sY[lane] = sy[lane];
+  slope(0);
+  static_for<1, S>([&](auto i) {
+    constexpr int I = decltype(i)::value;
+    __syncthreads();  // sF[I-1] written, sY free for reuse
+    if (comb) {
+      double acc = 0.0;
+      bool first = true;
+      static_for<0, I>([&](auto l) {
+        constexpr int L = decltype(l)::value;
+        constexpr double c = TB::A[I][L];
+        if constexpr (c != 0.0) {
+          acc = first ? c * sF[L][lane] : fma(c, sF[L][lane], acc);
+          first = false;
+        }
+      });
+      sY[lane] = fma(hs, acc, sy[lane]);
+    }
+    slope(I);
+  });
+  __syncthreads();
+  if (comb) {
+    double acc = 0.0;
+    bool first = true;
+    static_for<0, S>([&](auto l) {
+      constexpr int L = decltype(l)::value;
+      constexpr double c = TB::B[L];
+      if constexpr (c != 0.0) {
+        acc = first ? c * sF[L][lane] : fma(c, sF[L][lane], acc);
+        first = false;
+      }
+    });
+    sy[lane] = fma(hs, acc, sy[lane]);
+  }
+  __syncthreads();
+}
+
+template <class TB>
+__global__ void __launch_bounds__(128) k_stream_progenitor_mw(StreamDev a, MWParams p) {
+  __shared__ double sy[6], sY[6], sF[TB::S][6], sw[8];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x < 6) {
+    sy[threadIdx.x] = a.w_now[threadIdx.x];
+    a.B[threadIdx.x] = sy[threadIdx.x];
+  }
+  __syncthreads();
+  for (int64_t k = 0; k < a.n_rel; ++k) {
+    team_step_mw<TB>(p, -a.dt, a.Qb ? a.Qb + k * TB::S * 3 : nullptr, sy, sF, sY, sw, warp, lane);
+    if (threadIdx.x < 6) a.B[(k + 1) * 6 + threadIdx.x] = sy[threadIdx.x];
+  }
+  if (threadIdx.x < 6) a.P[threadIdx.x] = sy[threadIdx.x];
+  for (int64_t k = 0; k < a.n_rel; ++k) {
+    team_step_mw<TB>(p, a.dt, a.Q + k * TB::S * 3, sy, sF, sY, sw, warp, lane);
+    if (threadIdx.x < 6) a.P[(k + 1) * 6 + threadIdx.x] = sy[threadIdx.x];
+  }
+}
+
 template <class TB>
 __global__ void __launch_bounds__(128) k_stream_progenitor_team(StreamDev a, const DevComp* comps) {
   __shared__ DevComp s_comps[kAdjMaxComps];
@@ -1326,8 +1432,12 @@ static StreamDev stream_args(const gal_potential* pot, const gal_stream_config* 
 }
 
 template <class TB>
-static cudaError_t stream_forward(const StreamDev& a, const DevComp* comps, cudaStream_t s) {
-  k_stream_progenitor_team<TB><<<1, 128, 0, s>>>(a, comps);
+static cudaError_t stream_forward(const StreamDev& a, const gal_potential* pot, cudaStream_t s) {
+  const DevComp* comps = pot->d_comps;
+  if (pot->is_mw)
+    k_stream_progenitor_mw<TB><<<1, 128, 0, s>>>(a, pot->mw);
+  else
+    k_stream_progenitor_team<TB><<<1, 128, 0, s>>>(a, comps);
   k_stream_release<<<(unsigned)((a.n_rel + 127) / 128), 128, 0, s>>>(a, comps);
   k_stream_particles_team<TB><<<(unsigned)((a.np + 31) / 32), 128, 0, s>>>(a, comps);
   return cudaGetLastError();
@@ -1407,7 +1517,7 @@ gal_status gal_stream_run(const gal_potential* pot, const gal_stream_config* cfg
   a.fin = final_states;
   if (ics) a.ics = ics;
   cudaStream_t s = (cudaStream_t)stream;
-  cudaError_t e = dispatch(cfg->method, [&](auto tb) { return stream_forward<decltype(tb)>(a, pot->d_comps, s); });
+  cudaError_t e = dispatch(cfg->method, [&](auto tb) { return stream_forward<decltype(tb)>(a, pot, s); });
   if (e != cudaSuccess) return cuda_fail(e, "stream kernels");
   if (prog_track) {
     e = cudaMemcpyAsync(prog_track, a.P, sizeof(double) * 6 * (size_t)(cfg->n_release + 1), cudaMemcpyDeviceToDevice,
@@ -1435,7 +1545,7 @@ gal_status gal_stream_grad(const gal_potential* pot, const gal_stream_config* cf
   a.grad_w_now = grad_w_now;
   cudaStream_t s = (cudaStream_t)stream;
   cudaError_t e = dispatch(cfg->method, [&](auto tb) {
-    cudaError_t e1 = stream_forward<decltype(tb)>(a, pot->d_comps, s);
+    cudaError_t e1 = stream_forward<decltype(tb)>(a, pot, s);
     if (e1 != cudaSuccess) return e1;
     return stream_backward<decltype(tb)>(a, pot->d_comps, s);
   });

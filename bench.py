@@ -295,6 +295,7 @@ def run_ours(args) -> dict | None:
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
+    team_blocks = (tuning or {}).get("best", {}).get("team_blocks", 32)  # the library's default is 32
     clocks.start()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
@@ -389,8 +390,9 @@ def run_ours(args) -> dict | None:
                              "peak_gbs": measured_peaks().get("hbm_gbs"),
                              "note": "save writes only; of measured"}},
         "clocks": clk,
-        # per step: two integrate launches (both passes) and three ordering kernels
-        "gpu_launches": launches * (5 if cfg.schedule else 1),
+        # per step: the first pass, three ordering kernels and the second pass
+        # (one launch, or two when the longest orbits go to four-warp teams)
+        "gpu_launches": launches * ((6 if team_blocks > 0 else 5) if cfg.schedule else 1),
     }
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(b, target_s=args.cpu_seconds)

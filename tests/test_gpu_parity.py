@@ -496,7 +496,8 @@ def _set_team(blocks):
     _lib.check(_lib.load().gal_set_team(int(blocks)), "gal_set_team")
 
 
-@pytest.mark.parametrize("case", ["csr_forward", "shared_grid_backward", "few_orbits", "max_steps"])
+@pytest.mark.parametrize("case", ["csr_forward", "shared_grid_backward", "few_orbits", "max_steps",
+                                  "constant_step_scheduled"])
 def test_team_kernel_is_bitwise_identical(gx, case):
     """The second pass with the longest orbits on four-warp teams gives the
     same saves, statuses and step counts, bit for bit, as the one-thread
@@ -505,11 +506,16 @@ def test_team_kernel_is_bitwise_identical(gx, case):
     from galax_gb300.dynamics import integrate
 
     mw = gx.MilkyWayPotential()
-    n = {"csr_forward": 12000, "shared_grid_backward": 6000, "few_orbits": 300, "max_steps": 3000}[case]
+    n = {"csr_forward": 12000, "shared_grid_backward": 6000, "few_orbits": 300, "max_steps": 3000,
+         "constant_step_scheduled": 4000}[case]
     b = W.uneven_ics(lambda x: O.gradient(O.milky_way(), x), n, seed=8, tmax=1500.0, smax=40)
     max_steps = 2000 if case == "max_steps" else 2**16
-    cfg = gx.Integrator(solver=gx.Dopri5(), stepsize_controller=gx.PIDController(rtol=1e-8, atol=1e-10),
-                        max_steps=max_steps).config()
+    if case == "constant_step_scheduled":
+        cfg = gx.Integrator(solver=gx.Dopri5(), stepsize_controller=gx.ConstantStepSize(), dt0=0.7,
+                            schedule=True).config()
+    else:
+        cfg = gx.Integrator(solver=gx.Dopri5(), stepsize_controller=gx.PIDController(rtol=1e-8, atol=1e-10),
+                            max_steps=max_steps).config()
     res = []
     try:
         for team in (0, 8, 100):
@@ -553,3 +559,30 @@ def test_results_written_straight_into_pinned_host_memory(gx):
     with pytest.raises(ValueError):
         integrate(mw, b.y0, b.t0, b.t1, b.save_ts, cfg, save_offsets=b.save_offsets,
                   out=torch.empty(3, dtype=torch.float64))
+
+
+def test_team_path_replays_from_a_cuda_graph(gx):
+    """gal_integrate with the team fork/join (library stream, events) captured
+    into a CUDA graph replays to the eager result."""
+    import torch
+
+    from galax_gb300 import workloads as W
+    from galax_gb300.dynamics import Workspace, integrate
+
+    mw = gx.MilkyWayPotential()
+    y0 = torch.as_tensor(W.disk_like_ics(lambda x: O.gradient(O.milky_way(), x), 2000, seed=21),
+                         device="cuda").t().contiguous()
+    t0 = torch.zeros(2000, dtype=torch.float64, device="cuda")
+    t1 = torch.full((2000,), 300.0, dtype=torch.float64, device="cuda")
+    ts = torch.linspace(0.0, 300.0, 11, dtype=torch.float64, device="cuda")
+    cfg = gx.Integrator(solver=gx.Dopri5(), stepsize_controller=gx.PIDController(rtol=1e-8, atol=1e-10),
+                        schedule=True).config()
+    ws = Workspace()
+    eager, st_e, _ = integrate(mw, y0, t0, t1, ts, cfg, soa=True, workspace=ws)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        out_g, st_g, _ = integrate(mw, y0, t0, t1, ts, cfg, soa=True, workspace=ws)
+    g.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(out_g, eager) and torch.equal(st_g, st_e)

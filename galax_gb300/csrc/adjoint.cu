@@ -19,6 +19,7 @@
 // fixed-order reduction, so results are bitwise reproducible.
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <vector>
 
 #include "handle.h"
@@ -155,22 +156,32 @@ __global__ void k_reduce_rows(const double* __restrict__ in, int64_t n, double* 
   if (threadIdx.x == 0) out[blockIdx.x] = red[0];
 }
 
-// Constant-step time grid exactly as the forward kernels build it.
-static std::vector<double> time_grid(double t0, double t1, double dt) {
-  std::vector<double> ts;
+// Constant-step time grid exactly as the forward kernels build it
+// (ts[k+1] - ts[k] == dir * h_k exactly: negation is exact). False when t0 or
+// t1 is not finite, when the grid would need more than max_steps steps, or
+// when a step of dt no longer moves the time (dt below its spacing); the
+// host grid holds at most 2^28 steps whatever max_steps says.
+constexpr int64_t kMaxGridSteps = int64_t(1) << 28;  // 2 GiB of step times on the host
+
+static bool time_grid(double t0, double t1, double dt, int64_t max_steps, std::vector<double>& ts) {
+  ts.clear();
+  if (max_steps > kMaxGridSteps) max_steps = kMaxGridSteps;
+  if (!std::isfinite(t0) || !std::isfinite(t1) || !(dt > 0.0)) return false;
+  if (std::fabs(t1 - t0) / dt > (double)max_steps + 1.0) return false;
   const double dir = (t0 < t1) ? 1.0 : -1.0;
   const double tau1 = dir * t1;
   double tprev = dir * t0, tnext = tprev + dt;
   if (tnext > tau1) tnext = tau1;
   ts.push_back(dir * tprev);
   while (tprev < tau1) {
+    if (!(tnext > tprev) || (int64_t)ts.size() > max_steps) return false;
     ts.push_back(dir * tnext);
     double nt1 = tnext + dt;
     tprev = tnext < tau1 ? tnext : tau1;
     if (nt1 > tau1 - 1e-10) nt1 = tau1;
     tnext = nt1;
   }
-  return ts;  // ts[k+1] - ts[k] == dir * h_k exactly (negation is exact)
+  return true;
 }
 
 static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
@@ -180,9 +191,8 @@ struct AdjLayout {
   int64_t nsteps, nseg;
 };
 
-static AdjLayout adj_layout(int ncomp, double t0, double t1, double dt, int k, int64_t n) {
+static AdjLayout adj_layout(int ncomp, const std::vector<double>& ts, int k, int64_t n) {
   AdjLayout L{};
-  const std::vector<double> ts = time_grid(t0, t1, dt);
   L.nsteps = (int64_t)ts.size() - 1;
   L.nseg = (L.nsteps + k - 1) / k;
   size_t off = 0;
@@ -208,7 +218,10 @@ gal_status gal_adjoint_workspace_size(const gal_potential* pot, const gal_solver
                                       int32_t k_ckpt, int64_t n, size_t* bytes) {
   if (!pot || !cfg || !bytes || k_ckpt < 1 || n < 0) return fail(GAL_ERR_INVALID_ARGUMENT, "bad adjoint arguments");
   if (cfg->adaptive || !(cfg->dt0 > 0.0)) return fail(GAL_ERR_UNSUPPORTED, "the adjoint needs a constant step");
-  *bytes = adj_layout(pot->n, t0, t1, cfg->dt0, k_ckpt, n).total;
+  std::vector<double> ts;
+  if (!time_grid(t0, t1, cfg->dt0, cfg->max_steps, ts))
+    return fail(GAL_ERR_INVALID_ARGUMENT, "t0 and t1 must be finite and at most max_steps steps of dt0 apart");
+  *bytes = adj_layout(pot->n, ts, k_ckpt, n).total;
   return GAL_OK;
 }
 
@@ -227,10 +240,12 @@ gal_status gal_adjoint(const gal_potential* pot, const gal_solver_config* cfg, c
   if (!y0 || !yT || !grad_y0 || !grad_params || (!lambda && !target))
     return fail(GAL_ERR_INVALID_ARGUMENT, "NULL array");
   if (!(t0 != t1)) return fail(GAL_ERR_INVALID_ARGUMENT, "t0 == t1");
-  const AdjLayout L = adj_layout(pot->n, t0, t1, cfg->dt0, k_ckpt, n);
+  std::vector<double> ts;
+  if (!time_grid(t0, t1, cfg->dt0, cfg->max_steps, ts))
+    return fail(GAL_ERR_INVALID_ARGUMENT, "t0 and t1 must be finite and at most max_steps steps of dt0 apart");
+  const AdjLayout L = adj_layout(pot->n, ts, k_ckpt, n);
   if (!workspace || workspace_bytes < L.total) return fail(GAL_ERR_WORKSPACE, "workspace too small");
   char* ws = static_cast<char*>(workspace);
-  const std::vector<double> ts = time_grid(t0, t1, cfg->dt0);
   cudaStream_t s = (cudaStream_t)stream;
   cudaError_t e = cudaMemcpyAsync(ws + L.ts, ts.data(), sizeof(double) * ts.size(), cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return cuda_fail(e, "copying the time grid");

@@ -131,6 +131,10 @@ __global__ void __launch_bounds__(128) k_integrate_dense(IntegrateArgs a, Pot po
   if (t0 == t1) {  // nothing to integrate: the interpolant is the initial state
 #pragma unroll
     for (int j = 0; j < 6; ++j) co[j] = s.y[j];
+  } else if (!isfinite(t0) || !isfinite(t1)) {  // an infinite span never ends: report it at once
+#pragma unroll
+    for (int j = 0; j < 6; ++j) co[j] = __longlong_as_double(0x7ff8000000000000LL);
+    st = ORBIT_NONFINITE;
   } else {
     field(P, s.y, s.F0);
     double dt;

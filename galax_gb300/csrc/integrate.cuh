@@ -347,6 +347,10 @@ __device__ __forceinline__ bool start_orbit(const IntegrateArgs& a, const Pot& p
       finish_orbit(a, s, ORBIT_OK);
       continue;
     }
+    if (!isfinite(t0) || !isfinite(t1)) {  // an infinite span never ends: report it at once
+      finish_orbit(a, s, ORBIT_NONFINITE);
+      continue;
+    }
     field(pot, s.y, s.F0, t0);
     double dt;
     if (a.adaptive) {

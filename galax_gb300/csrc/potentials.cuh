@@ -362,7 +362,10 @@ __device__ __forceinline__ void comp_hessian(const DevComp& c, double x, double 
 // (Abramowitz & Stegun 6.3.18).
 __host__ __device__ inline double digamma_fn(double x) {
   double acc = 0.0;
-  while (x < 8.0) {
+  // at most 8 shifts: the power law with cutoff needs x = (3 - alpha)/2 in
+  // (0.5, 1.5]; outside that the result is not used, and the bound keeps a
+  // huge negative x (x + 1 == x) from looping
+  for (int i = 0; i < 8 && x < 8.0; ++i) {
     acc -= 1.0 / x;
     x += 1.0;
   }

@@ -127,6 +127,7 @@ gal_status gal_integrate_surrogate(const gal_potential* pot, const gal_mlp* mlp,
                                    size_t workspace_bytes, gal_stream_t stream) {
   if (!pot || !y || n < 0 || !(dt > 0.0)) return fail(GAL_ERR_INVALID_ARGUMENT, "bad surrogate arguments");
   if (time_dependent(pot)) return fail(GAL_ERR_UNSUPPORTED, "time-dependent parameters: evaluation and gal_integrate only");
+  if (!std::isfinite(t0) || !std::isfinite(t1)) return fail(GAL_ERR_INVALID_ARGUMENT, "t0 and t1 must be finite");
   if (n == 0 || t0 == t1) return GAL_OK;
   size_t need = 0;
   gal_surrogate_workspace_size(n, &need);
@@ -190,6 +191,10 @@ gal_status gal_integrate_surrogate(const gal_potential* pot, const gal_mlp* mlp,
   cudaGraphExec_t exec = nullptr;
   double graph_hs = 0.0;
   while (tprev < tau1) {
+    if (!(tnext > tprev)) {  // dt below the spacing of the times: the grid would never reach t1
+      if (exec) cudaGraphExecDestroy(exec);
+      return finish(fail(GAL_ERR_INVALID_ARGUMENT, "dt does not advance the time"));
+    }
     const double hs = dir * (tnext - tprev);
     if (use_graph && hs == dir * dt) {
       if (!exec || graph_hs != hs) {

@@ -114,7 +114,7 @@ static const double TINY = std::numeric_limits<double>::min();  // 2.22507385850
 // ---------------------------------------------------------------------------
 static double digamma(double x) {
   double acc = 0.0;
-  while (x < 8.0) {
+  for (int i = 0; i < 8 && x < 8.0; ++i) {  // x in (0.5, 1.5] here; bounded for any input
     acc -= 1.0 / x;
     x += 1.0;
   }
@@ -638,6 +638,12 @@ static SolveOut solve_group(const Pot& P, const OrcSolverCfg& cfg, const double*
   auto tau_s = [&](int64_t i) { return dir * ts[i]; };
   if (t0 == t1) {
     for (; si < ns; ++si) std::memcpy(out + si * n, y.data(), sizeof(double) * n);
+    return R;
+  }
+  if (!std::isfinite(t0) || !std::isfinite(t1)) {  // an infinite span never ends: report it at once
+    for (; si < ns; ++si)
+      for (int j = 0; j < n; ++j) out[si * n + j] = std::numeric_limits<double>::quiet_NaN();
+    R.status = ORC_NONFINITE;
     return R;
   }
   S.f(tau0, y.data(), f0.data());

@@ -274,6 +274,15 @@ def test_max_steps_status():
     assert np.all(np.isnan(s[0][-1]))
 
 
+@pytest.mark.parametrize("t0, t1", [(0.0, np.inf), (0.0, -np.inf), (np.nan, 10.0)])
+def test_non_finite_span_status(t0, t1):
+    c = O.milky_way()
+    y0 = np.array([[8.0, 0.0, 0.0, 0.0, 0.2, 0.0]])
+    s, st, acc, rej = O.integrate(c, y0, t0, t1, np.array([0.0, 5.0]), O.solver_cfg(5, True, rtol=1e-8, atol=1e-10))
+    assert st[0] == 3 and acc[0] + rej[0] == 0
+    assert np.all(np.isnan(s[0]))
+
+
 # ---------------------------------------------------------------- adjoint
 def test_adjoint_matches_central_differences():
     c = O.milky_way()

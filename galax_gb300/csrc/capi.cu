@@ -3,6 +3,7 @@
 // orbit-integration entry point and small utilities.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -17,12 +18,9 @@
 namespace gal {
 
 thread_local std::string g_last_error;
-// [method 5/8][adaptive]: Dopri5 fits 3 blocks of 128 per SM without spills
-// (variant 0); Dopri8 needs the uncapped variant 2 to avoid spilling.
-// [method == 8][adaptive]. Adaptive batches default to one warp per SM
-// sub-partition (128 threads, one block per SM): their longest orbits then run
-// at their own latency instead of sharing an FP64 pipe.
-static int g_team_blocks = 32;  // SMs given to four-warp teams for the longest orbits (gal_set_team)
+// SMs given to four-warp teams for the longest orbits (gal_set_team); atomic
+// because calls on other threads may read it while it is set
+static std::atomic<int> g_team_blocks{32};
 
 // One library-owned stream per device for the team kernel, created on first use.
 static cudaError_t team_stream(cudaStream_t* out) {
@@ -41,7 +39,19 @@ static cudaError_t team_stream(cudaStream_t* out) {
   return cudaSuccess;
 }
 
+// Launch shape per [method == 8][adaptive], set by gal_set_launch. Dopri5 fits
+// 3 blocks of 128 per SM without spills (variant 0); Dopri8 needs the uncapped
+// variant 2 to avoid spilling. Adaptive batches default to one warp per SM
+// sub-partition (128 threads, one block per SM): their longest orbits then run
+// at their own latency instead of sharing an FP64 pipe. Read and written under
+// g_shape_mu so that a shape is never seen half-set.
 static LaunchShape g_shape[2][2] = {{{0, 0, 0}, {128, 1, 2}}, {{0, 0, 2}, {128, 1, 2}}};
+static std::mutex g_shape_mu;
+
+static LaunchShape launch_shape(int method, int adaptive) {
+  std::lock_guard<std::mutex> lock(g_shape_mu);
+  return g_shape[method == 8][adaptive ? 1 : 0];
+}
 
 gal_status fail(gal_status st, const std::string& msg) {
   g_last_error = msg;
@@ -55,16 +65,17 @@ gal_status cuda_fail(cudaError_t e, const char* where) {
 // SM count of the current device, looked up once per device (so that launches
 // made while a stream is being captured query nothing)
 int device_sm_count() {
-  static int cache[64] = {0};
+  static std::atomic<int> cache[64] = {};
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= 64) dev = 0;
-  if (cache[dev] <= 0) {
-    int sms = 0;
+  int sms = cache[dev].load(std::memory_order_relaxed);
+  if (sms <= 0) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cache[dev] = sms > 0 ? sms : 1;
+    if (sms <= 0) sms = 1;
+    cache[dev].store(sms, std::memory_order_relaxed);
   }
-  return cache[dev];
+  return sms;
 }
 
 static DevComp fold(const gal_component& c, double G) {
@@ -505,7 +516,7 @@ gal_status gal_integrate_workspace_size(const gal_solver_config* cfg, int64_t n,
 
 gal_status gal_set_team(int32_t blocks) {
   if (blocks < 0 || blocks > 1024) return fail(GAL_ERR_INVALID_ARGUMENT, "team blocks must be in [0, 1024]");
-  g_team_blocks = blocks;
+  g_team_blocks.store(blocks, std::memory_order_relaxed);
   return GAL_OK;
 }
 
@@ -514,6 +525,7 @@ gal_status gal_set_launch(int32_t method, int32_t adaptive, int32_t block_thread
   if ((method != 5 && method != 8) || block_threads < 0 || block_threads > 256 || (block_threads % 32) ||
       blocks_per_sm < 0 || variant < 0 || variant > 2 || (variant != 2 && block_threads > 128))
     return fail(GAL_ERR_INVALID_ARGUMENT, "bad launch shape");
+  std::lock_guard<std::mutex> lock(g_shape_mu);
   g_shape[method == 8][adaptive ? 1 : 0] = LaunchShape{block_threads, blocks_per_sm, variant};
   return GAL_OK;
 }
@@ -573,7 +585,7 @@ gal_status gal_integrate(const gal_potential* p, const gal_solver_config* cfg, c
   a.split_frac = 0.0;
   a.resume = nullptr;
   a.queue_len = nullptr;
-  const LaunchShape shape = g_shape[cfg->method == 8][cfg->adaptive ? 1 : 0];
+  const LaunchShape shape = launch_shape(cfg->method, cfg->adaptive);
   auto launch = [&]() {
     return cfg->method == 8 ? launch_integrate_dopri8(a, p->is_mw, p->mw, p->d_comps, p->n, shape, s)
                             : launch_integrate_dopri5(a, p->is_mw, p->mw, p->d_comps, p->n, shape, s);
@@ -610,7 +622,8 @@ gal_status gal_integrate(const gal_potential* p, const gal_solver_config* cfg, c
   a.order = order2;
   a.queue_len = qlen;
   const int sms = device_sm_count();
-  const int blocks = g_team_blocks < sms - 1 ? g_team_blocks : sms - 1;
+  const int team_blocks = g_team_blocks.load(std::memory_order_relaxed);
+  const int blocks = team_blocks < sms - 1 ? team_blocks : sms - 1;
   if (blocks > 0 && p->is_mw && cfg->method == 5) {
     // The longest orbits go to four-warp teams on `blocks` SMs of their own
     // (second stream), the rest to the one-thread kernel on the other SMs, one

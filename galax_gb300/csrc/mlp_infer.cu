@@ -19,6 +19,7 @@
 // releases its TMEM and returns.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstring>
 #include <vector>
 
@@ -447,11 +448,16 @@ gal_status gal_mlp_eval(const gal_mlp* m, const double* x, int64_t n, double* gr
                         double grad_sign, double* phi, gal_stream_t stream) {
   if (!m || (!x && n) || n < 0) return fail(GAL_ERR_INVALID_ARGUMENT, "bad gal_mlp_eval arguments");
   if (n == 0) return GAL_OK;
-  static bool attr = false;
-  if (!attr) {
+  // the shared-memory opt-in is per device: set once on each (not again while a stream is captured)
+  static std::atomic<bool> attr[64] = {};
+  int dev = 0;
+  cudaError_t e0 = cudaGetDevice(&dev);
+  if (e0 != cudaSuccess) return cuda_fail(e0, "cudaGetDevice");
+  if (dev < 0 || dev >= 64) return fail(GAL_ERR_UNSUPPORTED, "device index above 63");
+  if (!attr[dev].load(std::memory_order_acquire)) {
     cudaError_t e = cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_ALLOC);
     if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(k_mlp_infer)");
-    attr = true;
+    attr[dev].store(true, std::memory_order_release);
   }
   InferArgs a{};
   a.x = x;

@@ -216,70 +216,75 @@ extern "C" {
 
 gal_status gal_adjoint_workspace_size(const gal_potential* pot, const gal_solver_config* cfg, double t0, double t1,
                                       int32_t k_ckpt, int64_t n, size_t* bytes) {
-  if (!pot || !cfg || !bytes || k_ckpt < 1 || n < 0) return fail(GAL_ERR_INVALID_ARGUMENT, "bad adjoint arguments");
-  if (cfg->adaptive || !(cfg->dt0 > 0.0)) return fail(GAL_ERR_UNSUPPORTED, "the adjoint needs a constant step");
-  std::vector<double> ts;
-  if (!time_grid(t0, t1, cfg->dt0, cfg->max_steps, ts))
-    return fail(GAL_ERR_INVALID_ARGUMENT, "t0 and t1 must be finite and at most max_steps steps of dt0 apart");
-  *bytes = adj_layout(pot->n, ts, k_ckpt, n).total;
-  return GAL_OK;
+  return no_throw([&]() -> gal_status {
+    if (!pot || !cfg || !bytes || k_ckpt < 1 || n < 0) return fail(GAL_ERR_INVALID_ARGUMENT, "bad adjoint arguments");
+    if (cfg->adaptive || !(cfg->dt0 > 0.0)) return fail(GAL_ERR_UNSUPPORTED, "the adjoint needs a constant step");
+    std::vector<double> ts;
+    if (!time_grid(t0, t1, cfg->dt0, cfg->max_steps, ts))
+      return fail(GAL_ERR_INVALID_ARGUMENT, "t0 and t1 must be finite and at most max_steps steps of dt0 apart");
+    *bytes = adj_layout(pot->n, ts, k_ckpt, n).total;
+    return GAL_OK;
+  });
 }
 
 gal_status gal_adjoint(const gal_potential* pot, const gal_solver_config* cfg, const double* y0, double t0,
                        double t1, const double* lambda, const double* target, double* yT, double* grad_y0,
                        double* grad_params, int32_t k_ckpt, int64_t n, void* workspace, size_t workspace_bytes,
                        gal_stream_t stream) {
-  if (!pot) return fail(GAL_ERR_INVALID_ARGUMENT, "potential is NULL");
-  if (time_dependent(pot)) return fail(GAL_ERR_UNSUPPORTED, "time-dependent parameters: evaluation and gal_integrate only");
-  gal_status st = validate_cfg(cfg);
-  if (st != GAL_OK) return st;
-  if (cfg->adaptive) return fail(GAL_ERR_UNSUPPORTED, "the adjoint needs a constant step (adaptive = 0)");
-  if (pot->n > kAdjMaxComps) return fail(GAL_ERR_UNSUPPORTED, "the adjoint supports at most 8 components");
-  if (k_ckpt < 1 || n < 0) return fail(GAL_ERR_INVALID_ARGUMENT, "k_ckpt >= 1 and n >= 0 required");
-  if (n == 0) return GAL_OK;
-  if (!y0 || !yT || !grad_y0 || !grad_params || (!lambda && !target))
-    return fail(GAL_ERR_INVALID_ARGUMENT, "NULL array");
-  if (!(t0 != t1)) return fail(GAL_ERR_INVALID_ARGUMENT, "t0 == t1");
-  std::vector<double> ts;
-  if (!time_grid(t0, t1, cfg->dt0, cfg->max_steps, ts))
-    return fail(GAL_ERR_INVALID_ARGUMENT, "t0 and t1 must be finite and at most max_steps steps of dt0 apart");
-  const AdjLayout L = adj_layout(pot->n, ts, k_ckpt, n);
-  if (!workspace || workspace_bytes < L.total) return fail(GAL_ERR_WORKSPACE, "workspace too small");
-  char* ws = static_cast<char*>(workspace);
-  cudaStream_t s = (cudaStream_t)stream;
-  cudaError_t e = cudaMemcpyAsync(ws + L.ts, ts.data(), sizeof(double) * ts.size(), cudaMemcpyHostToDevice, s);
-  if (e != cudaSuccess) return cuda_fail(e, "copying the time grid");
-  AdjointArgs a{};
-  a.y0 = y0;
-  a.lambda = lambda;
-  a.target = target;
-  a.yT = yT;
-  a.grad_y0 = grad_y0;
-  a.ts = reinterpret_cast<const double*>(ws + L.ts);
-  a.ckpt = reinterpret_cast<double*>(ws + L.ckpt);
-  a.seg = reinterpret_cast<double*>(ws + L.seg);
-  a.gp_orbit = reinterpret_cast<double*>(ws + L.gp);
-  a.nsteps = L.nsteps;
-  a.k_ckpt = k_ckpt;
-  a.n = n;
-  const int block = 64;
-  const unsigned grid = (unsigned)((n + block - 1) / block);
-  if (cfg->method == 8) {
-    if (pot->is_mw)
-      k_adjoint<Dopri8, MWPot><<<grid, block, 0, s>>>(a, MWPot{pot->mw}, pot->d_comps, pot->n);
-    else
-      k_adjoint<Dopri8, TablePot><<<grid, block, 0, s>>>(a, TablePot{pot->d_comps, pot->n}, pot->d_comps, pot->n);
-  } else {
-    if (pot->is_mw)
-      k_adjoint<Dopri5, MWPot><<<grid, block, 0, s>>>(a, MWPot{pot->mw}, pot->d_comps, pot->n);
-    else
-      k_adjoint<Dopri5, TablePot><<<grid, block, 0, s>>>(a, TablePot{pot->d_comps, pot->n}, pot->d_comps, pot->n);
-  }
-  e = cudaGetLastError();
-  if (e != cudaSuccess) return cuda_fail(e, "adjoint kernel launch");
-  k_reduce_rows<<<(unsigned)(pot->n * 3), 256, 0, s>>>(a.gp_orbit, n, grad_params);
-  e = cudaGetLastError();
-  return e == cudaSuccess ? GAL_OK : cuda_fail(e, "adjoint reduction launch");
+  return no_throw([&]() -> gal_status {
+    if (!pot) return fail(GAL_ERR_INVALID_ARGUMENT, "potential is NULL");
+    if (time_dependent(pot))
+      return fail(GAL_ERR_UNSUPPORTED, "time-dependent parameters: evaluation and gal_integrate only");
+    gal_status st = validate_cfg(cfg);
+    if (st != GAL_OK) return st;
+    if (cfg->adaptive) return fail(GAL_ERR_UNSUPPORTED, "the adjoint needs a constant step (adaptive = 0)");
+    if (pot->n > kAdjMaxComps) return fail(GAL_ERR_UNSUPPORTED, "the adjoint supports at most 8 components");
+    if (k_ckpt < 1 || n < 0) return fail(GAL_ERR_INVALID_ARGUMENT, "k_ckpt >= 1 and n >= 0 required");
+    if (n == 0) return GAL_OK;
+    if (!y0 || !yT || !grad_y0 || !grad_params || (!lambda && !target))
+      return fail(GAL_ERR_INVALID_ARGUMENT, "NULL array");
+    if (!(t0 != t1)) return fail(GAL_ERR_INVALID_ARGUMENT, "t0 == t1");
+    std::vector<double> ts;
+    if (!time_grid(t0, t1, cfg->dt0, cfg->max_steps, ts))
+      return fail(GAL_ERR_INVALID_ARGUMENT, "t0 and t1 must be finite and at most max_steps steps of dt0 apart");
+    const AdjLayout L = adj_layout(pot->n, ts, k_ckpt, n);
+    if (!workspace || workspace_bytes < L.total) return fail(GAL_ERR_WORKSPACE, "workspace too small");
+    char* ws = static_cast<char*>(workspace);
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e = cudaMemcpyAsync(ws + L.ts, ts.data(), sizeof(double) * ts.size(), cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return cuda_fail(e, "copying the time grid");
+    AdjointArgs a{};
+    a.y0 = y0;
+    a.lambda = lambda;
+    a.target = target;
+    a.yT = yT;
+    a.grad_y0 = grad_y0;
+    a.ts = reinterpret_cast<const double*>(ws + L.ts);
+    a.ckpt = reinterpret_cast<double*>(ws + L.ckpt);
+    a.seg = reinterpret_cast<double*>(ws + L.seg);
+    a.gp_orbit = reinterpret_cast<double*>(ws + L.gp);
+    a.nsteps = L.nsteps;
+    a.k_ckpt = k_ckpt;
+    a.n = n;
+    const int block = 64;
+    const unsigned grid = (unsigned)((n + block - 1) / block);
+    if (cfg->method == 8) {
+      if (pot->is_mw)
+        k_adjoint<Dopri8, MWPot><<<grid, block, 0, s>>>(a, MWPot{pot->mw}, pot->d_comps, pot->n);
+      else
+        k_adjoint<Dopri8, TablePot><<<grid, block, 0, s>>>(a, TablePot{pot->d_comps, pot->n}, pot->d_comps, pot->n);
+    } else {
+      if (pot->is_mw)
+        k_adjoint<Dopri5, MWPot><<<grid, block, 0, s>>>(a, MWPot{pot->mw}, pot->d_comps, pot->n);
+      else
+        k_adjoint<Dopri5, TablePot><<<grid, block, 0, s>>>(a, TablePot{pot->d_comps, pot->n}, pot->d_comps, pot->n);
+    }
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "adjoint kernel launch");
+    k_reduce_rows<<<(unsigned)(pot->n * 3), 256, 0, s>>>(a.gp_orbit, n, grad_params);
+    e = cudaGetLastError();
+    return e == cudaSuccess ? GAL_OK : cuda_fail(e, "adjoint reduction launch");
+  });
 }
 
 }  // extern "C"

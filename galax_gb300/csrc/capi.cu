@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -328,37 +329,37 @@ const char* gal_status_string(int32_t st) {
     case GAL_ERR_CUDA: return "CUDA error";
     case GAL_ERR_WORKSPACE: return "workspace too small";
     case GAL_ERR_TOO_LARGE: return "size beyond the supported maximum";
+    case GAL_ERR_HOST_ALLOC: return "host allocation failed";
     default: return "unknown status";
   }
 }
 
 gal_status gal_potential_create(const gal_component* comps, int32_t n, double G, gal_potential** out) {
-  if (!out) return fail(GAL_ERR_INVALID_ARGUMENT, "out is NULL");
-  *out = nullptr;
-  gal_status st = validate_components(comps, n);
-  if (st != GAL_OK) return st;
-  if (!(G > 0.0) || !std::isfinite(G)) return fail(GAL_ERR_INVALID_ARGUMENT, "G must be finite and > 0");
-  gal_potential* p = new gal_potential();
-  p->comps.assign(comps, comps + n);
-  p->G = G;
-  p->n = n;
-  p->is_mw = milky_way_shape(comps, n);
-  p->mw = p->is_mw ? mw_params(comps, G) : MWParams{};
-  std::vector<DevComp> h(n);
-  for (int i = 0; i < n; ++i) h[i] = fold(comps[i], G);
-  cudaError_t e = cudaMalloc(&p->d_comps, sizeof(DevComp) * n);
-  if (e != cudaSuccess) {
-    delete p;
-    return cuda_fail(e, "cudaMalloc(component table)");
-  }
-  e = cudaMemcpy(p->d_comps, h.data(), sizeof(DevComp) * n, cudaMemcpyHostToDevice);
-  if (e != cudaSuccess) {
-    cudaFree(p->d_comps);
-    delete p;
-    return cuda_fail(e, "cudaMemcpy(component table)");
-  }
-  *out = p;
-  return GAL_OK;
+  return no_throw([&]() -> gal_status {
+    if (!out) return fail(GAL_ERR_INVALID_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    gal_status st = validate_components(comps, n);
+    if (st != GAL_OK) return st;
+    if (!(G > 0.0) || !std::isfinite(G)) return fail(GAL_ERR_INVALID_ARGUMENT, "G must be finite and > 0");
+    std::unique_ptr<gal_potential> holder(new gal_potential());
+    gal_potential* p = holder.get();
+    p->comps.assign(comps, comps + n);
+    p->G = G;
+    p->n = n;
+    p->is_mw = milky_way_shape(comps, n);
+    p->mw = p->is_mw ? mw_params(comps, G) : MWParams{};
+    std::vector<DevComp> h(n);
+    for (int i = 0; i < n; ++i) h[i] = fold(comps[i], G);
+    cudaError_t e = cudaMalloc(&p->d_comps, sizeof(DevComp) * n);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(component table)");
+    e = cudaMemcpy(p->d_comps, h.data(), sizeof(DevComp) * n, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      cudaFree(p->d_comps);
+      return cuda_fail(e, "cudaMemcpy(component table)");
+    }
+    *out = holder.release();
+    return GAL_OK;
+  });
 }
 
 gal_status gal_potential_destroy(gal_potential* p) {
@@ -373,77 +374,81 @@ gal_status gal_potential_destroy(gal_potential* p) {
 }
 
 gal_status gal_potential_set_linear(gal_potential* p, const double* slopes) {
-  if (!p) return fail(GAL_ERR_INVALID_ARGUMENT, "potential is NULL");
-  if (slopes) {
-    for (int i = 0; i < 3 * p->n; ++i)
-      if (!std::isfinite(slopes[i])) return fail(GAL_ERR_INVALID_ARGUMENT, "non-finite slope");
-  }
-  bool any = false;
-  std::vector<DevLinear> h(p->n);
-  for (int i = 0; i < p->n; ++i) {
-    const gal_component& c = p->comps[i];
-    DevLinear& L = h[i];
-    L.kind = c.kind;
-    L.m0 = c.m;
-    L.l10 = c.l1;
-    L.l20 = c.l2;
-    L.G = p->G;
-    L.dm = slopes ? slopes[3 * i] : 0.0;
-    L.dl1 = slopes ? slopes[3 * i + 1] : 0.0;
-    L.dl2 = slopes ? slopes[3 * i + 2] : 0.0;
-    L.active = (L.dm != 0.0 || L.dl1 != 0.0 || L.dl2 != 0.0) ? 1 : 0;
-    any = any || L.active;
-  }
-  if (p->d_lin) {
-    cudaError_t e = cudaFree(p->d_lin);
-    p->d_lin = nullptr;
-    if (e != cudaSuccess) return cuda_fail(e, "cudaFree(linear table)");
-  }
-  if (any) {
-    cudaError_t e = cudaMalloc(&p->d_lin, sizeof(DevLinear) * p->n);
-    if (e != cudaSuccess) {
-      p->d_lin = nullptr;
-      return cuda_fail(e, "cudaMalloc(linear table)");
+  return no_throw([&]() -> gal_status {
+    if (!p) return fail(GAL_ERR_INVALID_ARGUMENT, "potential is NULL");
+    if (slopes) {
+      for (int i = 0; i < 3 * p->n; ++i)
+        if (!std::isfinite(slopes[i])) return fail(GAL_ERR_INVALID_ARGUMENT, "non-finite slope");
     }
-    e = cudaMemcpy(p->d_lin, h.data(), sizeof(DevLinear) * p->n, cudaMemcpyHostToDevice);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(linear table)");
-  }
-  // the specialised Milky Way model has constant parameters
-  p->is_mw = !any && milky_way_shape(p->comps.data(), p->n);
-  return GAL_OK;
+    bool any = false;
+    std::vector<DevLinear> h(p->n);
+    for (int i = 0; i < p->n; ++i) {
+      const gal_component& c = p->comps[i];
+      DevLinear& L = h[i];
+      L.kind = c.kind;
+      L.m0 = c.m;
+      L.l10 = c.l1;
+      L.l20 = c.l2;
+      L.G = p->G;
+      L.dm = slopes ? slopes[3 * i] : 0.0;
+      L.dl1 = slopes ? slopes[3 * i + 1] : 0.0;
+      L.dl2 = slopes ? slopes[3 * i + 2] : 0.0;
+      L.active = (L.dm != 0.0 || L.dl1 != 0.0 || L.dl2 != 0.0) ? 1 : 0;
+      any = any || L.active;
+    }
+    if (p->d_lin) {
+      cudaError_t e = cudaFree(p->d_lin);
+      p->d_lin = nullptr;
+      if (e != cudaSuccess) return cuda_fail(e, "cudaFree(linear table)");
+    }
+    if (any) {
+      cudaError_t e = cudaMalloc(&p->d_lin, sizeof(DevLinear) * p->n);
+      if (e != cudaSuccess) {
+        p->d_lin = nullptr;
+        return cuda_fail(e, "cudaMalloc(linear table)");
+      }
+      e = cudaMemcpy(p->d_lin, h.data(), sizeof(DevLinear) * p->n, cudaMemcpyHostToDevice);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(linear table)");
+    }
+    // the specialised Milky Way model has constant parameters
+    p->is_mw = !any && milky_way_shape(p->comps.data(), p->n);
+    return GAL_OK;
+  });
 }
 
 gal_status gal_potential_update(gal_potential* p, const gal_component* comps, int32_t n, gal_stream_t stream) {
-  if (!p) return fail(GAL_ERR_INVALID_ARGUMENT, "potential is NULL");
-  if (n != p->n) return fail(GAL_ERR_INVALID_ARGUMENT, "component count differs from the handle's");
-  gal_status st = validate_components(comps, n);
-  if (st != GAL_OK) return st;
-  for (int i = 0; i < n; ++i)
-    if (comps[i].kind != p->comps[i].kind) return fail(GAL_ERR_INVALID_ARGUMENT, "component kinds differ");
-  std::vector<DevComp> h(n);
-  for (int i = 0; i < n; ++i) h[i] = fold(comps[i], p->G);
-  // pageable source: the call returns once the bytes are staged, so h may go out of scope
-  cudaError_t e = cudaMemcpyAsync(p->d_comps, h.data(), sizeof(DevComp) * n, cudaMemcpyHostToDevice,
-                                  (cudaStream_t)stream);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(component table)");
-  e = cudaStreamSynchronize((cudaStream_t)stream);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
-  p->comps.assign(comps, comps + n);
-  p->is_mw = !p->d_lin && milky_way_shape(comps, n);
-  p->mw = milky_way_shape(comps, n) ? mw_params(comps, p->G) : MWParams{};
-  if (p->d_lin) {  // new values at t = 0, same slopes
-    std::vector<DevLinear> L(n);
-    e = cudaMemcpy(L.data(), p->d_lin, sizeof(DevLinear) * n, cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(linear table)");
-    for (int i = 0; i < n; ++i) {
-      L[i].m0 = comps[i].m;
-      L[i].l10 = comps[i].l1;
-      L[i].l20 = comps[i].l2;
+  return no_throw([&]() -> gal_status {
+    if (!p) return fail(GAL_ERR_INVALID_ARGUMENT, "potential is NULL");
+    if (n != p->n) return fail(GAL_ERR_INVALID_ARGUMENT, "component count differs from the handle's");
+    gal_status st = validate_components(comps, n);
+    if (st != GAL_OK) return st;
+    for (int i = 0; i < n; ++i)
+      if (comps[i].kind != p->comps[i].kind) return fail(GAL_ERR_INVALID_ARGUMENT, "component kinds differ");
+    std::vector<DevComp> h(n);
+    for (int i = 0; i < n; ++i) h[i] = fold(comps[i], p->G);
+    // pageable source: the call returns once the bytes are staged, so h may go out of scope
+    cudaError_t e = cudaMemcpyAsync(p->d_comps, h.data(), sizeof(DevComp) * n, cudaMemcpyHostToDevice,
+                                    (cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(component table)");
+    e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
+    p->comps.assign(comps, comps + n);
+    p->is_mw = !p->d_lin && milky_way_shape(comps, n);
+    p->mw = milky_way_shape(comps, n) ? mw_params(comps, p->G) : MWParams{};
+    if (p->d_lin) {  // new values at t = 0, same slopes
+      std::vector<DevLinear> L(n);
+      e = cudaMemcpy(L.data(), p->d_lin, sizeof(DevLinear) * n, cudaMemcpyDeviceToHost);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(linear table)");
+      for (int i = 0; i < n; ++i) {
+        L[i].m0 = comps[i].m;
+        L[i].l10 = comps[i].l1;
+        L[i].l20 = comps[i].l2;
+      }
+      e = cudaMemcpy(p->d_lin, L.data(), sizeof(DevLinear) * n, cudaMemcpyHostToDevice);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(linear table)");
     }
-    e = cudaMemcpy(p->d_lin, L.data(), sizeof(DevLinear) * n, cudaMemcpyHostToDevice);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(linear table)");
-  }
-  return GAL_OK;
+    return GAL_OK;
+  });
 }
 
 int32_t gal_potential_num_components(const gal_potential* p) { return p ? p->n : 0; }

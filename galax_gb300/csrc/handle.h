@@ -2,6 +2,7 @@
 // shared by the library's translation units.
 #pragma once
 
+#include <new>
 #include <string>
 #include <vector>
 
@@ -29,4 +30,22 @@ gal_status fail(gal_status st, const std::string& msg);
 gal_status cuda_fail(cudaError_t e, const char* where);
 gal_status validate_cfg(const gal_solver_config* c);
 int device_sm_count();
+
+// Runs the body of an entry point that allocates host memory, so that no C++
+// exception crosses the C ABI: a failed allocation becomes GAL_ERR_HOST_ALLOC.
+template <class Body>
+gal_status no_throw(Body&& body) noexcept {
+  gal_status st = GAL_ERR_HOST_ALLOC;
+  try {
+    return body();
+  } catch (const std::bad_alloc&) {
+  } catch (...) {
+    st = GAL_ERR_INVALID_ARGUMENT;
+  }
+  try {
+    fail(st, st == GAL_ERR_HOST_ALLOC ? "host allocation failed" : "unexpected C++ exception");
+  } catch (...) {
+  }
+  return st;
+}
 }  // namespace gal

@@ -386,53 +386,56 @@ uint16_t to_bf16(float f) {
 extern "C" {
 
 gal_status gal_mlp_create(const float* params_host, double length_scale, double phi_scale, gal_mlp** out) {
-  if (!params_host || !out || !(length_scale > 0) || !(phi_scale != 0))
-    return fail(GAL_ERR_INVALID_ARGUMENT, "bad gal_mlp_create arguments");
-  *out = nullptr;
-  const float* P = params_host;
-  std::vector<float> small(SMALL_FLOATS);
-  std::memcpy(small.data(), P + OFF_W1, sizeof(float) * 3 * H);
-  std::memcpy(small.data() + 3 * H, P + OFF_B1, sizeof(float) * H);
-  std::memcpy(small.data() + 4 * H, P + OFF_B2, sizeof(float) * H);
-  std::memcpy(small.data() + 5 * H, P + OFF_B3, sizeof(float) * H);
-  std::memcpy(small.data() + 6 * H, P + OFF_B4, sizeof(float) * H);
-  std::memcpy(small.data() + 7 * H, P + OFF_W5, sizeof(float) * H);
-  small[8 * H] = P[OFF_B5];
-  // B operands, K-major: product "A x B^T" with B[n][k]. Forward z = h W^T uses
-  // B = W (n = output unit, k = input unit); backward u = d W uses B = W^T.
-  std::vector<uint8_t> img((size_t)KBLOCKS_PER_TILE * KBLOCK_BYTES, 0);
-  const int64_t offs[3] = {OFF_W2, OFF_W3, OFF_W4};
-  const int order[6][2] = {{0, 0}, {1, 0}, {2, 0}, {2, 1}, {1, 1}, {0, 1}};  // (matrix, transposed)
-  for (int g = 0; g < GEMMS; ++g) {
-    const float* W = P + offs[order[g][0]];
-    const bool tr = order[g][1] != 0;
-    for (int n = 0; n < H; ++n)
-      for (int k = 0; k < H; ++k) {
-        const float v = tr ? W[(size_t)k * H + n] : W[(size_t)n * H + k];
-        const uint32_t kb = k >> 6;
-        const uint32_t off = tc::sw128_offset(256, n, k & 63);  // within the K-block
-        const uint16_t b = to_bf16(v);
-        std::memcpy(&img[((size_t)g * KBLOCKS_PER_GEMM + kb) * KBLOCK_BYTES + off], &b, 2);
-      }
-  }
-  gal_mlp* m = new gal_mlp();
-  m->length_scale = length_scale;
-  m->phi_scale = phi_scale;
-  cudaError_t e = cudaMalloc(&m->d_small, sizeof(float) * small.size());
-  if (e == cudaSuccess) e = cudaMalloc(&m->d_wimg, img.size());
-  if (e == cudaSuccess) e = cudaMalloc(&m->d_err, sizeof(int));
-  if (e == cudaSuccess) e = cudaMemcpy(m->d_small, small.data(), sizeof(float) * small.size(), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemcpy(m->d_wimg, img.data(), img.size(), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemset(m->d_err, 0, sizeof(int));
-  if (e != cudaSuccess) {
-    cudaFree(m->d_small);
-    cudaFree(m->d_wimg);
-    cudaFree(m->d_err);
-    delete m;
-    return cuda_fail(e, "gal_mlp_create");
-  }
-  *out = m;
-  return GAL_OK;
+  return no_throw([&]() -> gal_status {
+    if (!params_host || !out || !(length_scale > 0) || !(phi_scale != 0))
+      return fail(GAL_ERR_INVALID_ARGUMENT, "bad gal_mlp_create arguments");
+    *out = nullptr;
+    const float* P = params_host;
+    std::vector<float> small(SMALL_FLOATS);
+    std::memcpy(small.data(), P + OFF_W1, sizeof(float) * 3 * H);
+    std::memcpy(small.data() + 3 * H, P + OFF_B1, sizeof(float) * H);
+    std::memcpy(small.data() + 4 * H, P + OFF_B2, sizeof(float) * H);
+    std::memcpy(small.data() + 5 * H, P + OFF_B3, sizeof(float) * H);
+    std::memcpy(small.data() + 6 * H, P + OFF_B4, sizeof(float) * H);
+    std::memcpy(small.data() + 7 * H, P + OFF_W5, sizeof(float) * H);
+    small[8 * H] = P[OFF_B5];
+    // B operands, K-major: product "A x B^T" with B[n][k]. Forward z = h W^T uses
+    // B = W (n = output unit, k = input unit); backward u = d W uses B = W^T.
+    std::vector<uint8_t> img((size_t)KBLOCKS_PER_TILE * KBLOCK_BYTES, 0);
+    const int64_t offs[3] = {OFF_W2, OFF_W3, OFF_W4};
+    const int order[6][2] = {{0, 0}, {1, 0}, {2, 0}, {2, 1}, {1, 1}, {0, 1}};  // (matrix, transposed)
+    for (int g = 0; g < GEMMS; ++g) {
+      const float* W = P + offs[order[g][0]];
+      const bool tr = order[g][1] != 0;
+      for (int n = 0; n < H; ++n)
+        for (int k = 0; k < H; ++k) {
+          const float v = tr ? W[(size_t)k * H + n] : W[(size_t)n * H + k];
+          const uint32_t kb = k >> 6;
+          const uint32_t off = tc::sw128_offset(256, n, k & 63);  // within the K-block
+          const uint16_t b = to_bf16(v);
+          std::memcpy(&img[((size_t)g * KBLOCKS_PER_GEMM + kb) * KBLOCK_BYTES + off], &b, 2);
+        }
+    }
+    gal_mlp* m = new gal_mlp();
+    m->length_scale = length_scale;
+    m->phi_scale = phi_scale;
+    cudaError_t e = cudaMalloc(&m->d_small, sizeof(float) * small.size());
+    if (e == cudaSuccess) e = cudaMalloc(&m->d_wimg, img.size());
+    if (e == cudaSuccess) e = cudaMalloc(&m->d_err, sizeof(int));
+    if (e == cudaSuccess)
+      e = cudaMemcpy(m->d_small, small.data(), sizeof(float) * small.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(m->d_wimg, img.data(), img.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(m->d_err, 0, sizeof(int));
+    if (e != cudaSuccess) {
+      cudaFree(m->d_small);
+      cudaFree(m->d_wimg);
+      cudaFree(m->d_err);
+      delete m;
+      return cuda_fail(e, "gal_mlp_create");
+    }
+    *out = m;
+    return GAL_OK;
+  });
 }
 
 gal_status gal_mlp_destroy(gal_mlp* m) {

@@ -45,7 +45,8 @@ typedef enum gal_status {
   GAL_ERR_UNSUPPORTED = 2,
   GAL_ERR_CUDA = 3,
   GAL_ERR_WORKSPACE = 4,
-  GAL_ERR_TOO_LARGE = 5
+  GAL_ERR_TOO_LARGE = 5,
+  GAL_ERR_HOST_ALLOC = 6 /* a host-side allocation failed; no C++ exception leaves the library */
 } gal_status;
 
 /* Per-orbit outcome; mirrors diffrax.RESULTS as raised by galax's solvers

@@ -49,6 +49,7 @@ def test_abi_version_and_status_strings(lib):
     assert lib.gal_abi_version() == 1
     assert lib.gal_status_string(0) == b"ok"
     assert lib.gal_status_string(4) == b"workspace too small"
+    assert lib.gal_status_string(6) == b"host allocation failed"
 
 
 @pytest.mark.parametrize("method", [5, 8])

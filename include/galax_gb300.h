@@ -365,8 +365,8 @@ GAL_API gal_status gal_stream_df_sample(const gal_potential* pot, int32_t df, co
 
 /* ------------------------------------------------------------------ learned surrogate */
 /* A small MLP, 3 -> 256 -> 256 -> 256 -> 256 -> 1 with SiLU activations, that
- * stands in for an expensive composite (the north-star's MilkyWayPotential plus
- * hundreds of Plummer subhalos; no counterpart class in galax). Input
+ * stands in for an expensive composite (a MilkyWayPotential plus hundreds of
+ * Plummer subhalos; no counterpart class in galax). Input
  * u = x / length_scale, potential = phi_scale * out(u), gradient =
  * (phi_scale / length_scale) grad_u out. Parameters are one float32 vector of
  * gal_mlp_num_params() values: W1[256][3], b1, W2[256][256], b2, W3, b3, W4,

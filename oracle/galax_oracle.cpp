@@ -2,9 +2,9 @@
 //
 // TEST INFRASTRUCTURE ONLY. This file restates, in plain C++17, the arithmetic
 // that GalacticDynamics/galax (and its pinned ODE engine diffrax 0.7.0)
-// performs on the `evaluate_orbit` / `AbstractPotential.gradient` path. It is
-// the checker the CUDA library is compared against and the CPU baseline the
-// benchmark times; nothing in the shipped package links or calls it.
+// performs on the `evaluate_orbit` / `AbstractPotential.gradient` path. The
+// tests compare the CUDA library against it and the benchmark times it as the
+// CPU baseline; nothing in the shipped package links or calls it.
 //
 // What is restated, and from where:
 //   * closed-form potentials

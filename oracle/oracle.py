@@ -3,7 +3,8 @@
 The oracle restates galax's potentials, Hamiltonian field and the diffrax
 Runge-Kutta / PID-controller arithmetic in C++ (``galax_oracle.cpp``). Only the
 test suite, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
-``bench.py`` use it, as the checker; the ``galax_gb300`` package never does.
+``bench.py`` use it, to check and to time the CUDA library against; the
+``galax_gb300`` package never does.
 
 Component records use the same 56-byte layout as the CUDA library's
 ``gal_component`` (kind, flags, mass, l1, l2, origin[3]).

@@ -1,6 +1,6 @@
 """The CPU oracle against the reference's golden vectors and known-answer tests.
 
-These pin the oracle before it is trusted as the checker of the CUDA library:
+These pin the oracle before the CUDA library's tests trust it as their reference:
 every potential / gradient / Hessian golden of the reference's unit tests, the
 Dopri8 single-step doctest, the PID-controlled doctests, and self-consistency
 (order conditions of both tableaux, finite differences of the Hessians, the
@@ -376,7 +376,7 @@ def test_stream_particles_follow_the_coupled_system():
 
 def test_stream_finite_difference_gradient_converges():
     """The oracle's central differences (one Richardson step) agree across step
-    sizes for the halo parameters, so they can judge the GPU adjoint at 1e-6."""
+    sizes for the halo parameters, so they can check the GPU adjoint at 1e-6."""
     c, s = _stream_setup(100)
     target = O.stream_forward(c, s)["final"] + s.pert
     g1 = O.stream_fd_grad(c, s, target, [(1, "m"), (1, "l1")], rel_h=1e-4)

@@ -882,14 +882,20 @@ int orc_integrate(const Comp* comps, int ncomp, double G, const OrcSolverCfg* cf
 // Discrete adjoint of the constant-step RK map (diffrax ConstantStepSize time
 // grid: t_{n+1} = t_n + dt, last step clipped onto t1) for the terminal loss
 // L = sum_i |y_i(t1) - target_i|^2. Outputs the final states yT (n x 6), dL/dy0
-// (n x 6) and dL/d(m, l1, l2) per component summed over orbits (ncomp x 3).
+// (n x 6) and, per component summed over orbits, dL/d(m, l1, l2) (ncomp x 3).
+// With slopes (LinearParameter: p(t) = p + slope t, galax
+// potential/_src/params/core.py:25-110) every stage evaluates the parameters
+// at its own time, gparams holds the derivatives with respect to the values at
+// t = 0, and gslopes (ncomp x 3) those with respect to the slopes: the
+// stage-time derivative dL/dp(t_s), times 1 and times t_s.
 int orc_adjoint_fixed(const Comp* comps, int ncomp, double G, const OrcSolverCfg* cfg, const double* y0,
                       double t0, double t1, const double* target, double* yT, double* gy,
-                      double* gparams, int64_t n, int nthreads) {
-  Pot P{comps, ncomp, G};
+                      double* gparams, int64_t n, int nthreads, const double* slopes, double* gslopes) {
+  Pot P{comps, ncomp, G, slopes};
   const Tableau& TB = (cfg->method == 5) ? DOPRI5 : DOPRI8;
   const double dt = cfg->dt0;
-  std::vector<double> gp_all((size_t)n * ncomp * 3, 0.0);
+  const int np = slopes ? 6 : 3;  // per component: values, then slopes
+  std::vector<double> gp_all((size_t)n * ncomp * np, 0.0);
 #ifdef _OPENMP
   if (nthreads > 0) omp_set_num_threads(nthreads);
 #else
@@ -921,7 +927,7 @@ int orc_adjoint_fixed(const Comp* comps, int ncomp, double G, const OrcSolverCfg
       yT[6 * o + j] = y[j];
       lam[j] = 2.0 * (y[j] - target[6 * o + j]);
     }
-    double* gpo = gp_all.data() + (size_t)o * ncomp * 3;
+    double* gpo = gp_all.data() + (size_t)o * ncomp * np;
     const int64_t N = (int64_t)hs.size();
     double Fb[13 * 6], Ys[13 * 6];
     for (int64_t st = N - 1; st >= 0; --st) {
@@ -951,16 +957,19 @@ int orc_adjoint_fixed(const Comp* comps, int ncomp, double G, const OrcSolverCfg
       for (int i = TB.s - 1; i >= 0; --i) {
         const double* Yi = Ys + 6 * i;
         const double* fb = Fb + 6 * i;
+        const double ti = tau + TB.c[i] * h;  // the stage's time (forward direction)
         // J^T fb with f = (p, -grad Phi(q)): (-H fb_p, fb_q)
         double H[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-        for (int c = 0; c < ncomp; ++c) comp_hessian(comps[c], G, Yi, H);
+        for (int c = 0; c < ncomp; ++c) comp_hessian(comp_at(P, c, ti), G, Yi, H);
         double Yb[6];
         for (int r = 0; r < 3; ++r) Yb[r] = -(H[3 * r] * fb[3] + H[3 * r + 1] * fb[4] + H[3 * r + 2] * fb[5]);
         Yb[3] = fb[0]; Yb[4] = fb[1]; Yb[5] = fb[2];
         for (int c = 0; c < ncomp; ++c) {
           double d[3] = {0, 0, 0};
-          comp_dgrad_dparams_dot(comps[c], G, Yi, fb + 3, d);
-          for (int k = 0; k < 3; ++k) gpo[3 * c + k] -= d[k];
+          comp_dgrad_dparams_dot(comp_at(P, c, ti), G, Yi, fb + 3, d);
+          for (int k = 0; k < 3; ++k) gpo[np * c + k] -= d[k];
+          if (slopes)
+            for (int k = 0; k < 3; ++k) gpo[np * c + 3 + k] -= ti * d[k];
         }
         for (int j = 0; j < 6; ++j) lam0[j] += Yb[j];
         for (int l = 0; l < i; ++l)
@@ -972,8 +981,16 @@ int orc_adjoint_fixed(const Comp* comps, int ncomp, double G, const OrcSolverCfg
     for (int j = 0; j < 6; ++j) gy[6 * o + j] = lam[j];
   }
   for (int c = 0; c < ncomp * 3; ++c) gparams[c] = 0;
-  for (int64_t o = 0; o < n; ++o)
-    for (int c = 0; c < ncomp * 3; ++c) gparams[c] += gp_all[(size_t)o * ncomp * 3 + c];
+  if (slopes && gslopes)
+    for (int c = 0; c < ncomp * 3; ++c) gslopes[c] = 0;
+  for (int64_t o = 0; o < n; ++o) {
+    const double* g = gp_all.data() + (size_t)o * ncomp * np;
+    for (int c = 0; c < ncomp; ++c)
+      for (int k = 0; k < 3; ++k) {
+        gparams[3 * c + k] += g[np * c + k];
+        if (slopes && gslopes) gslopes[3 * c + k] += g[np * c + 3 + k];
+      }
+  }
   return 0;
 }
 

@@ -103,7 +103,7 @@ def lib() -> C.CDLL:
         L.orc_count_ops.argtypes = [cp, C.c_int, C.c_double, C.c_int, dp, i64p]
         L.orc_adjoint_fixed.argtypes = [
             cp, C.c_int, C.c_double, C.POINTER(SolverCfg), dp, C.c_double, C.c_double, dp, dp, dp, dp,
-            C.c_int64, C.c_int,
+            C.c_int64, C.c_int, C.c_void_p, C.c_void_p,
         ]
         L.orc_adjoint_fixed.restype = C.c_int
         _lib = L
@@ -305,23 +305,28 @@ def adjoint_fixed(
     *,
     G: float = G_GALACTIC,
     nthreads: int = 0,
+    slopes=None,
 ):
     """Discrete adjoint of constant steps ``cfg.dt0`` from t0 to t1 for the loss
     L = sum_i |y_i(t1) - target_i|^2. Returns (yT (n,6), dL/dy0 (n,6),
-    dL/dparams (ncomp,3), L)."""
+    dL/dparams, L). dL/dparams is (ncomp, 3), d/d(m, l1, l2); with ``slopes``
+    (ncomp, 3) of LinearParameter time dependence it is (ncomp, 6): d/d(m, l1,
+    l2) at t = 0, then d/d(slopes)."""
     y0 = np.ascontiguousarray(np.atleast_2d(np.asarray(y0, np.float64)))
     target = np.ascontiguousarray(np.asarray(target, np.float64).reshape(y0.shape))
     n = len(y0)
     yT = np.empty_like(y0)
     gy = np.empty_like(y0)
     gp = np.zeros((len(c), 3))
-    loss = np.zeros(1)
+    gs = np.zeros((len(c), 3))
+    keep, sp = _slopes_ptr(c, slopes)
     lib().orc_adjoint_fixed(
         np.ascontiguousarray(c), len(c), G, C.byref(cfg), y0, float(t0), float(t1), target, yT, gy,
-        gp.reshape(-1), n, nthreads,
+        gp.reshape(-1), n, nthreads, sp, gs.ctypes.data if sp else None,
     )
+    del keep
     L = float(np.sum((yT - target) ** 2))
-    return yT, gy, gp, L
+    return yT, gy, (np.concatenate([gp, gs], axis=1) if sp else gp), L
 
 
 def count_ops(c: np.ndarray, method: int, y=(8.0, 1.0, 0.5, 0.0, 0.2, 0.01), G: float = G_GALACTIC):

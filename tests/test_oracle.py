@@ -318,6 +318,51 @@ def test_adjoint_matches_central_differences():
             assert abs(gp[ci, j] - fd) <= 1e-5 * max(abs(fd), 1e-12 / p0), (ci, field, gp[ci, j], fd)
 
 
+def test_adjoint_with_linear_parameters_matches_central_differences():
+    """LinearParameter time dependence in the adjoint: d/d(value at t = 0) and
+    d/d(slope) against central differences of the oracle's own integration, and
+    zero slopes give the static adjoint bitwise."""
+    c = O.milky_way()
+    slopes = np.zeros((len(c), 3))
+    slopes[0, 0] = -2e8    # disk mass (Msun / Myr)
+    slopes[0, 1] = 1e-3    # disk a (kpc / Myr)
+    slopes[1, 0] = 5e8     # halo mass
+    slopes[1, 1] = -4e-3   # halo r_s
+    y0 = np.array([[8.0, 0.5, 0.3, 0.02, 0.21, 0.01], [12.0, -3.0, 1.0, 0.1, 0.15, -0.02]])
+    cfg = O.solver_cfg(8, False, dt0=1.0)
+    t1 = 60.0
+    yT, *_ = O.integrate(c, y0, 0.0, t1, np.array([t1]), cfg, slopes=slopes)
+    target = np.stack([s[0] for s in yT]) + np.random.default_rng(8).normal(0, 0.1, (2, 6))
+    _, gy, gp, L = O.adjoint_fixed(c, y0, 0.0, t1, target, cfg, slopes=slopes)
+    assert gp.shape == (len(c), 6)
+
+    def loss(cc, ss):
+        s, *_ = O.integrate(cc, y0, 0.0, t1, np.array([t1]), cfg, slopes=ss)
+        return float(sum(((s[i][0] - target[i]) ** 2).sum() for i in range(len(s))))
+
+    assert abs(loss(c, slopes) - L) < 1e-12 * max(1, L)
+    for ci, field, j in [(0, "m", 0), (0, "l1", 1), (0, "l2", 2), (1, "m", 0), (1, "l1", 1), (2, "m", 0)]:
+        p0 = float(c[ci][field])
+        h = 1e-6 * p0
+        cp, cm = c.copy(), c.copy()
+        cp[ci][field] = p0 + h
+        cm[ci][field] = p0 - h
+        fd = (loss(cp, slopes) - loss(cm, slopes)) / (2 * h)
+        assert abs(gp[ci, j] - fd) <= 1e-5 * max(abs(fd), 1e-12 / p0), ("value", ci, field, gp[ci, j], fd)
+        # the slope's scale: the value's, spread over the span
+        hs = 1e-6 * p0 / t1
+        sp, sm = slopes.copy(), slopes.copy()
+        sp[ci, j] += hs
+        sm[ci, j] -= hs
+        fd = (loss(c, sp) - loss(c, sm)) / (2 * hs)
+        assert abs(gp[ci, 3 + j] - fd) <= 1e-5 * max(abs(fd), 1e-12 * t1 / p0), ("slope", ci, field, gp[ci, 3 + j], fd)
+    # static potential: the same values bitwise, slope derivatives = sum of t * d/dp(t)
+    _, gy0, gp0, _ = O.adjoint_fixed(c, y0, 0.0, t1, target, cfg)
+    _, gyz, gpz, _ = O.adjoint_fixed(c, y0, 0.0, t1, target, cfg, slopes=np.zeros_like(slopes))
+    assert np.array_equal(gp0, gpz[:, :3]) and np.array_equal(gy0, gyz)
+    assert np.all(np.isfinite(gpz[:, 3:]))
+
+
 # ---------------------------------------------------------------- stream
 def _stream_setup(n_release):
     from galax_gb300 import workloads as W

@@ -22,7 +22,7 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _lib
-from .dynamics import Workspace, _as_cuda
+from .dynamics import Workspace, _as_cuda, on_stream
 from .potential import AbstractPotential, from_component_array
 
 
@@ -45,6 +45,9 @@ _WS = Workspace()
 
 def _run(pot, y0_soa, t0, t1, dt, method, k_ckpt, lam_soa=None, target_soa=None, stream=None):
     torch = _torch()
+    if stream is not None and stream != torch.cuda.current_stream().cuda_stream:
+        with on_stream(stream):
+            return _run(pot, y0_soa, t0, t1, dt, method, k_ckpt, lam_soa, target_soa)
     n = y0_soa.shape[1]
     cfg = _lib.solver_config(method, False, dt0=dt)
     L = _lib.load()
@@ -57,7 +60,7 @@ def _run(pot, y0_soa, t0, t1, dt, method, k_ckpt, lam_soa=None, target_soa=None,
     gy = torch.empty((6, n), dtype=torch.float64, device="cuda")
     ncomp = len(pot.components())
     gp = torch.empty((ncomp, 3), dtype=torch.float64, device="cuda")
-    st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+    st = torch.cuda.current_stream().cuda_stream
     _lib.check(
         L.gal_adjoint(
             h, C.byref(cfg), y0_soa.data_ptr(), float(t0), float(t1),

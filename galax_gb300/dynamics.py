@@ -172,16 +172,41 @@ def kms(v):
 
 # ---------------------------------------------------------------- low level
 class Workspace:
-    """Device scratch reused across calls (grown on demand)."""
+    """Device scratch reused across calls, grown on demand.
+
+    One buffer per (device, current stream): calls queued on different streams
+    never share scratch, and torch's caching allocator only hands a replaced
+    buffer's memory to later work on the stream it was allocated on. The work
+    using it must run on torch's current stream (``on_stream`` below makes an
+    explicit stream current). The 16 most recently used streams keep theirs."""
+
+    MAX_STREAMS = 16
 
     def __init__(self):
-        self._buf = None
+        self._bufs: dict = {}
 
     def get(self, nbytes: int):
         torch = _torch()
-        if self._buf is None or self._buf.numel() < nbytes or self._buf.device.index != torch.cuda.current_device():
-            self._buf = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device="cuda")
-        return self._buf
+        key = (torch.cuda.current_device(), torch.cuda.current_stream().cuda_stream)
+        buf = self._bufs.pop(key, None)
+        if buf is None or buf.numel() < nbytes:
+            buf = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device="cuda")
+        self._bufs[key] = buf  # most recently used last
+        while len(self._bufs) > self.MAX_STREAMS:
+            self._bufs.pop(next(iter(self._bufs)))
+        return buf
+
+
+def on_stream(stream):
+    """Context in which torch's current stream is ``stream`` (a cudaStream_t
+    handle as int, or None for no change), so that every temporary a call
+    allocates is ordered with the kernels it launches there."""
+    import contextlib
+
+    torch = _torch()
+    if stream is None or stream == torch.cuda.current_stream().cuda_stream:
+        return contextlib.nullcontext()
+    return torch.cuda.stream(torch.cuda.ExternalStream(stream))
 
 
 _WS = Workspace()
@@ -237,8 +262,15 @@ def integrate(
     place: contiguous CUDA tensors of those shapes, or pinned host tensors,
     which the kernels then write directly (device-visible host memory under
     unified addressing), overlapping the transfer with the integration.
+
+    ``stream`` (a cudaStream_t handle) runs the call on that stream instead of
+    torch's current one; its temporaries are then allocated there too.
     """
     torch = _torch()
+    if stream is not None and stream != torch.cuda.current_stream().cuda_stream:
+        with on_stream(stream):
+            return integrate(pot, y0, t0, t1, save_ts, cfg, save_offsets=save_offsets, order=order, soa=soa,
+                             workspace=workspace, out=out, status=status)
     y = _as_cuda(y0, torch.float64)
     if not soa:
         y = y.reshape(-1, 6).t()
@@ -273,7 +305,7 @@ def integrate(
     nbytes = C.c_size_t()
     _lib.check(L.gal_integrate_workspace_size(C.byref(cfg), n, C.byref(nbytes)), "gal_integrate_workspace_size")
     ws = (workspace or _WS).get(nbytes.value)
-    st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+    st = torch.cuda.current_stream().cuda_stream
     _lib.check(
         L.gal_integrate(
             pot.handle(), C.byref(cfg), y.data_ptr(), t0v.data_ptr(), t1v.data_ptr(), offs_ptr, ts.data_ptr(),

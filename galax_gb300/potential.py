@@ -57,6 +57,8 @@ class LinearParameter:
 
 
 def _param(name: str, v: Any) -> float:
+    if isinstance(v, LinearParameter):
+        raise NotImplementedError(f"{name}: a LinearParameter is not supported for this parameter on the GPU path")
     if callable(v):
         raise NotImplementedError(f"{name}: only constant and LinearParameter parameters are supported on the "
                                   "GPU path")
@@ -409,25 +411,41 @@ class _AbstractMN3Potential(AbstractPotential):
     def __init__(self, *, m_tot, h_R, h_z, positive_density: bool = False, origin=(0.0, 0.0, 0.0),  # noqa: N803
                  units: Any = "galactic", constants=None):
         super().__init__(units=units, constants=constants)
+        # each disk's mass is a fixed multiple of m_tot, so a LinearParameter
+        # m_tot is exact as per-disk slopes; the scale lengths enter the disks
+        # non-linearly and must be constant
+        self._m_tot_slope = 0.0
+        if isinstance(m_tot, LinearParameter):
+            self._m_tot_slope = _param("m_tot.slope", m_tot.slope)
+            m_tot = m_tot.value_at_zero
         self.m_tot = _param("m_tot", m_tot)
         self.h_R = _param("h_R", h_R)
         self.h_z = _param("h_z", h_z)
         self.positive_density = bool(positive_density)
         self.origin = tuple(float(v) for v in origin)
 
-    def disks(self) -> list[tuple[float, float, float]]:
-        """(m_tot, a, b) of the three Miyamoto-Nagai disks."""
+    def _coefficients(self) -> tuple[list[float], float]:
+        """The six mass / scale-length factors of the three disks, and b."""
         q = self.h_z / self.h_R
         c3, c2, c1 = self._b_coeffs
         b_over_hR = ((c3 * q + c2) * q + c1) * q
         powers = (b_over_hR**4, b_over_hR**3, b_over_hR**2, b_over_hR, 1.0)
         K = _MN3_K_POSITIVE_DENSITY if self.positive_density else _MN3_K_NEGATIVE_DENSITY
-        coef = [sum(k * x for k, x in zip(row, powers)) for row in K]
-        b = b_over_hR * self.h_R
+        return [sum(k * x for k, x in zip(row, powers)) for row in K], b_over_hR * self.h_R
+
+    def disks(self) -> list[tuple[float, float, float]]:
+        """(m_tot, a, b) of the three Miyamoto-Nagai disks (at t = 0)."""
+        coef, b = self._coefficients()
         return [(coef[i] * self.m_tot, coef[3 + i] * self.h_R, b) for i in range(3)]
 
     def components(self):
         return [(_lib.GAL_MIYAMOTO_NAGAI, m, a, b, self.origin) for (m, a, b) in self.disks()]
+
+    def slopes(self):
+        if not self._m_tot_slope:
+            return None
+        coef, _ = self._coefficients()
+        return np.array([[coef[i] * self._m_tot_slope, 0.0, 0.0] for i in range(3)], np.float64)
 
     def _repr_params(self) -> str:
         return (f"m_tot={self.m_tot!r}, h_R={self.h_R!r}, h_z={self.h_z!r}, "

@@ -184,6 +184,15 @@ def test_linear_parameters_on_the_host():
     assert gx.MilkyWayPotential().slopes() is None
     with pytest.raises(NotImplementedError):
         gx.KeplerPotential(m_tot=lambda t: 1e12)  # other callables stay unsupported
+    # MN3: a linear m_tot is exact as per-disk slopes; the scale lengths must be constant
+    mn3 = gx.MN3Sech2Potential(m_tot=gx.LinearParameter(2e8, 0.0, 5e10), h_R=3.0, h_z=0.3)
+    ref = gx.MN3Sech2Potential(m_tot=5e10, h_R=3.0, h_z=0.3)
+    np.testing.assert_array_equal(mn3.component_array(), ref.component_array())
+    masses = ref.component_array()["m"]
+    np.testing.assert_allclose(mn3.slopes()[:, 0], masses / 5e10 * 2e8, rtol=1e-15)
+    assert not mn3.slopes()[:, 1:].any() and ref.slopes() is None
+    with pytest.raises(NotImplementedError, match="h_R"):
+        gx.MN3ExponentialPotential(m_tot=5e10, h_R=gx.LinearParameter(1e-3, 0.0, 3.0), h_z=0.3)
 
 
 def test_set_linear_validates_on_the_host(lib):

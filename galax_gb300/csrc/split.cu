@@ -61,8 +61,10 @@ gal_status gal_split_create(const gal_component* comps, int32_t n, double G, dou
     double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
     for (int i = 0; i < n; ++i) {
       if (comps[i].kind != GAL_PLUMMER) return fail(GAL_ERR_UNSUPPORTED, "the split takes Plummer components only");
-      if (!(comps[i].l1 > 0.0)) return fail(GAL_ERR_INVALID_ARGUMENT, "Plummer b must be > 0");
+      if (!(comps[i].l1 > 0.0) || !std::isfinite(comps[i].l1) || !std::isfinite(comps[i].m))
+        return fail(GAL_ERR_INVALID_ARGUMENT, "Plummer m must be finite and b finite and > 0");
       for (int d = 0; d < 3; ++d) {
+        if (!std::isfinite(comps[i].origin[d])) return fail(GAL_ERR_INVALID_ARGUMENT, "non-finite Plummer centre");
         lo[d] = std::min(lo[d], comps[i].origin[d]);
         hi[d] = std::max(hi[d], comps[i].origin[d]);
       }
@@ -73,8 +75,9 @@ gal_status gal_split_create(const gal_component* comps, int32_t n, double G, dou
       glo = std::min(glo, lo[d] - r_cut);
       ghi = std::max(ghi, hi[d] + r_cut);
     }
-    const int nx = std::max(1, (int)std::ceil((ghi - glo) / h));
-    if ((int64_t)nx * nx * nx > (int64_t)1 << 26) return fail(GAL_ERR_TOO_LARGE, "split grid above 2^26 cells");
+    const double cells = std::ceil((ghi - glo) / h);  // per axis; checked before the integer conversion
+    if (!(cells <= 406.0)) return fail(GAL_ERR_TOO_LARGE, "split grid above 2^26 cells");
+    const int nx = std::max(1, (int)cells);
     const int64_t ncell = (int64_t)nx * nx * nx;
     std::vector<std::vector<int>> lists((size_t)ncell);
     for (int i = 0; i < n; ++i) {

@@ -546,7 +546,7 @@ def run_surrogate(args, n, rank, world, dist) -> dict | None:
     """Learned-surrogate workload: orbit-steps/s of the surrogate path (analytic Milky
     Way in FP64 + MLP subhalo term on the tensor cores) against the plain FP64
     direct sum over all 516 components, and the surrogate's median relative
-    position error after 1 Gyr (judged by the plain path)."""
+    position error after 1 Gyr (measured against the plain path)."""
     import torch
 
     import galax_gb300 as gx
@@ -632,7 +632,7 @@ def run_surrogate(args, n, rank, world, dist) -> dict | None:
         "speedup_vs_plain": value / plain_value,
         "median_rel_pos_err_1gyr": {"surrogate": float(e_sur.median()), "analytic_mw_only": float(e_mw.median()),
                                     "surrogate_p90": float(torch.quantile(e_sur, 0.9)),
-                                    "judged_on_orbits": ns},
+                                    "measured_on_orbits": ns},
         "roofline": {"bound": "tensor", "kernel": "k_mlp_infer", "achieved": achieved_tf,
                      "peak": peaks.get("bf16_tflops"), "unit": "TFLOP/s",
                      "frac": achieved_tf / peaks["bf16_tflops"] if peaks.get("bf16_tflops") else None,

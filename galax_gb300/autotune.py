@@ -12,7 +12,7 @@ sub-partition with them. A GB300 FP64 warp instruction holds its
 sub-partition's FP64 pipe for ~64 cycles whatever the number of active lanes,
 so one resident warp per sub-partition lets the longest orbits advance at their
 own latency from the start. Shapes with many resident warps vary by up to 2x
-from run to run. Each candidate is therefore timed ``repeats`` times and judged
+from run to run. Each candidate is therefore timed ``repeats`` times and ranked
 by its slowest run.
 """
 

@@ -166,6 +166,28 @@ def test_gradient_at_origin_is_zero(gx):
     assert np.all(g == 0)
 
 
+def test_batch_equals_rows_and_orbit_shapes(gx):
+    """galax's AbstractPotential_Test (tests/unit/potential/test_base.py:120-131,
+    177-201): a batch [[1,2,3],[4,5,6],[7,8,9]] evaluates to its rows evaluated
+    one at a time (galax: atol 1e-15; here bitwise), and evaluate_orbit of one
+    point with 100 saves over 1 Myr returns (100, 3) positions at those times."""
+    xs = np.array([[1.0, 2.0, 3.0], [4.0, 5.0, 6.0], [7.0, 8.0, 9.0]])
+    pots = [gx.MilkyWayPotential(), gx.HernquistPotential(m_tot=1e12, r_s=1.0),
+            gx.MiyamotoNagaiPotential(m_tot=1e12, a=1.0, b=1.0), gx.NFWPotential(m=1e12, r_s=1.0),
+            gx.PlummerPotential(m_tot=1e12, r_s=1.0)]
+    for pot in pots:
+        for fn in ("potential", "gradient", "hessian"):
+            batch = getattr(pot, fn)(xs)
+            for i in range(len(xs)):
+                one = getattr(pot, fn)(xs[i])
+                assert one.shape == batch[i].shape
+                np.testing.assert_array_equal(one, batch[i])
+    t = np.linspace(0.0, 1.0, 100)
+    orb = gx.MilkyWayPotential().evaluate_orbit(np.array([8.0, 0.0, 0.0, 0.0, 0.2, 0.0]), t)
+    assert orb.q.shape == (100, 3) and orb.p.shape == (100, 3)
+    np.testing.assert_array_equal(orb.t, t)
+
+
 # ------------------------------------------------------------------ fixed step
 def _ics(n, seed):
     from galax_gb300 import workloads as W

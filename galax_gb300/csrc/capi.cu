@@ -641,15 +641,29 @@ gal_status gal_integrate(const gal_potential* p, const gal_solver_config* cfg, c
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&join, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventRecord(fork, s);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(ts, fork, 0);
-    if (e == cudaSuccess) e = launch_integrate_team(a, p->mw, reinterpret_cast<unsigned long long*>(ws + 528), tcap,
-                                                    blocks, kExclusiveSmem, ts);
-    if (e == cudaSuccess) e = cudaEventRecord(join, ts);
+    bool team_launched = false, joinable = false;
+    if (e == cudaSuccess) {
+      e = launch_integrate_team(a, p->mw, reinterpret_cast<unsigned long long*>(ws + 528), tcap, blocks,
+                                kExclusiveSmem, ts);
+      team_launched = e == cudaSuccess;
+    }
+    if (e == cudaSuccess) {
+      e = cudaEventRecord(join, ts);
+      joinable = e == cudaSuccess;
+    }
     if (e == cudaSuccess) {
       a.queue_base = tcap;
       // one warp per sub-partition: two (256 threads) made the step 1.4x longer
       e = launch_integrate_dopri5_exclusive(a, p->mw, shape.variant, 128, sms - blocks, kExclusiveSmem, s);
     }
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, join, 0);
+    // Whatever failed after the team kernel was queued, the caller's stream
+    // still waits for it, so the caller never frees buffers it is using.
+    if (joinable) {
+      const cudaError_t ej = cudaStreamWaitEvent(s, join, 0);
+      if (e == cudaSuccess) e = ej;
+    } else if (team_launched) {
+      cudaStreamSynchronize(ts);
+    }
     if (fork) cudaEventDestroy(fork);
     if (join) cudaEventDestroy(join);
     return e == cudaSuccess ? GAL_OK : cuda_fail(e, "integrate kernel launch (second pass, teams)");

@@ -140,12 +140,18 @@ gal_status gal_integrate_surrogate(const gal_potential* pot, const gal_mlp* mlp,
   cudaStream_t s = caller;
   cudaEvent_t ev_in = nullptr, ev_out = nullptr;
   if (use_graph) {
+    s = nullptr;
     cudaError_t e0 = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
     if (e0 == cudaSuccess) e0 = cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming);
     if (e0 == cudaSuccess) e0 = cudaEventCreateWithFlags(&ev_out, cudaEventDisableTiming);
     if (e0 == cudaSuccess) e0 = cudaEventRecord(ev_in, caller);
     if (e0 == cudaSuccess) e0 = cudaStreamWaitEvent(s, ev_in, 0);
-    if (e0 != cudaSuccess) return cuda_fail(e0, "setting up the capture stream");
+    if (e0 != cudaSuccess) {  // nothing was queued on s: release what was created
+      if (ev_in) cudaEventDestroy(ev_in);
+      if (ev_out) cudaEventDestroy(ev_out);
+      if (s) cudaStreamDestroy(s);
+      return cuda_fail(e0, "setting up the capture stream");
+    }
   }
   auto finish = [&](gal_status st) -> gal_status {
     if (use_graph) {

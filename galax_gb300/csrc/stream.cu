@@ -1379,6 +1379,8 @@ static gal_status stream_validate(const gal_potential* pot, const gal_stream_con
   if (c->method != 5 && c->method != 8) return fail(GAL_ERR_INVALID_ARGUMENT, "method must be 5 or 8");
   if (!(c->dt > 0.0)) return fail(GAL_ERR_INVALID_ARGUMENT, "dt must be > 0");
   if (c->n_release < 1) return fail(GAL_ERR_INVALID_ARGUMENT, "n_release must be >= 1");
+  // the particle-step grids (n_release (n_release + 1) entries) must fit one launch
+  if (c->n_release > (int64_t(1) << 18)) return fail(GAL_ERR_TOO_LARGE, "n_release must be <= 2^18");
   if (c->k_ckpt < 0) return fail(GAL_ERR_INVALID_ARGUMENT, "k_ckpt must be >= 0");
   if (!(c->prog_m > 0.0) || !(c->prog_b > 0.0)) return fail(GAL_ERR_INVALID_ARGUMENT, "progenitor m, b must be > 0");
   if (pot->n > kAdjMaxComps) return fail(GAL_ERR_UNSUPPORTED, "stream host potentials have at most 8 components");

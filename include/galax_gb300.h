@@ -292,7 +292,7 @@ typedef struct gal_stream_config {
                       * particle stage position and Hessian instead, taking all potential evaluations
                       * off the reverse sweep (memory n_release (n_release + 1) S 144 bytes, S = 13
                       * for Dopri8) */
-  int64_t n_release; /* releases (>= 1); particles = 2 n_release */
+  int64_t n_release; /* releases (1 .. 2^18; GAL_ERR_TOO_LARGE above); particles = 2 n_release */
   double dt;         /* constant step (> 0) */
   double t_now;      /* present time (the potential is static: only labels times) */
   double prog_m;     /* progenitor Plummer mass */

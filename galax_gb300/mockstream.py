@@ -35,7 +35,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import stream as _stream
-from .dynamics import Dopri8, Integrator, PIDController, evaluate_orbit, integrate_orbit
+from .dynamics import Dopri8, Integrator, PIDController, evaluate_orbit, integrate_dense, integrate_orbit
 from .potential import AbstractPotential
 
 
@@ -240,13 +240,19 @@ class StreamSimulator:
 
     def run(self, pot: AbstractPotential, prog: StreamICs, /, *, t1, dense: bool = False, solver_kwargs=None):
         """Each arm integrated from its release time to ``t1``: returns
-        ((q_lead, v_lead), (q_trail, v_trail))."""
-        if dense:
-            raise NotImplementedError("StreamSimulator.run(dense=True): use dynamics.integrate_dense")
+        ((q_lead, v_lead), (q_trail, v_trail)).
+
+        With ``dense=True`` it returns instead one dense interpolant over every
+        particle (galax returns one dense diffrax solution per particle,
+        experimental/stream.py:393-399, 436-441): a ``PhaseSpaceInterpolation``
+        with batch (2, n), leading arm first, each particle valid from its
+        release time to ``t1``."""
         n = prog.release_times.size
         ics = np.concatenate([np.concatenate(prog.qp_lead, axis=1), np.concatenate(prog.qp_trail, axis=1)], axis=0)
         t0 = np.concatenate([prog.release_times, prog.release_times])
-        fin, _, _ = integrate_orbit(pot, ics, t0, np.full(2 * n, float(t1)), None,
-                                    integrator=_experimental_integrator(solver_kwargs))
+        integ = _experimental_integrator(solver_kwargs)
+        if dense:
+            return integrate_dense(pot, ics, t0, np.full(2 * n, float(t1)), integ.config(), batch=(2, n))
+        fin, _, _ = integrate_orbit(pot, ics, t0, np.full(2 * n, float(t1)), None, integrator=integ)
         fin = _np(fin)
         return (fin[:n, :3], fin[:n, 3:]), (fin[n:, :3], fin[n:, 3:])

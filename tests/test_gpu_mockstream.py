@@ -180,3 +180,9 @@ def test_stream_simulator_matches_oracle(M):
     assert _rel(qt, fin[n:, :3]) < 1e-6
     # the particle released at t0 is already there: it comes back unchanged
     np.testing.assert_allclose(ql[0], ics.qp_lead[0][0], rtol=1e-14)
+    # dense=True: one interpolant over both arms, valid from each release time to t1
+    interp = sim.run(pot, ics, t1=0.0, dense=True)
+    q, p = (x.cpu().numpy() for x in interp.evaluate(np.array([0.0])))
+    assert q.shape == (2, n, 1, 3) and p.shape == (2, n, 1, 3)
+    assert _rel(q[0, :, 0], ql) < 1e-12 and _rel(q[1, :, 0], qt) < 1e-12
+    assert _rel(p[0, :, 0], vl) < 1e-12 and _rel(p[1, :, 0], vt) < 1e-12

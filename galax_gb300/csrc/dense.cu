@@ -22,6 +22,9 @@ namespace gal {
 
 __device__ __forceinline__ MWPot bind_table(const MWPot& p, const DevComp*) { return p; }
 __device__ __forceinline__ TablePot bind_table(const TablePot& p, const DevComp* s) { return TablePot{s, p.n}; }
+__device__ __forceinline__ TimedTablePot bind_table(const TimedTablePot& p, const DevComp* s) {
+  return TimedTablePot{s, p.n, p.lin};
+}
 
 // Solver fields of gal_integrate's argument block (the same mapping as gal_integrate).
 static IntegrateArgs make_integrate_args(const gal_solver_config* cfg) {
@@ -136,10 +139,10 @@ __global__ void __launch_bounds__(128) k_integrate_dense(IntegrateArgs a, Pot po
     for (int j = 0; j < 6; ++j) co[j] = __longlong_as_double(0x7ff8000000000000LL);
     st = ORBIT_NONFINITE;
   } else {
-    field(P, s.y, s.F0);
+    field(P, s.y, s.F0, t0);
     double dt;
     if (a.adaptive) {
-      dt = a.dt0 > 0.0 ? a.dt0 : initial_step<TB>(a, P, s.y, s.F0, s.dir, t0);  // static potentials only
+      dt = a.dt0 > 0.0 ? a.dt0 : initial_step<TB>(a, P, s.y, s.F0, s.dir, t0);
       if (a.dtmax > 0.0) dt = fmin(dt, a.dtmax);
       if (a.dtmin > 0.0) {
         s.at_dtmin = dt <= a.dtmin;
@@ -154,7 +157,7 @@ __global__ void __launch_bounds__(128) k_integrate_dense(IntegrateArgs a, Pot po
       const double hs = s.dir * (s.tnext - s.tau);
 #pragma unroll
       for (int j = 0; j < 6; ++j) F[0][j] = s.F0[j];
-      rk_stages<TB>(P, s.y, hs, F);
+      rk_stages<TB>(P, s.y, hs, F, s.dir * s.tau);
       double y1[6], err[6];
       rk_combine<TB>(s.y, hs, F, y1, a.adaptive ? err : nullptr);
       ++s.nsteps;
@@ -191,7 +194,7 @@ __global__ void __launch_bounds__(128) k_integrate_dense(IntegrateArgs a, Pot po
 #pragma unroll
           for (int j = 0; j < 6; ++j) s.F0[j] = F[TB::S - 1][j];
         } else {
-          field(P, s.y, s.F0);
+          field(P, s.y, s.F0, s.dir * tprev_new);
         }
       }
       s.tau = tprev_new;
@@ -261,8 +264,8 @@ __global__ void __launch_bounds__(128) k_dense_eval(Pot pot, const DevComp* comp
 #pragma unroll
         for (int j = 0; j < 6; ++j) y[j] = c[j];
         const double hs = dir * (tau - ta);
-        field(P, y, F[0]);
-        rk_stages<TB>(P, y, hs, F);
+        field(P, y, F[0], tso[lo]);  // tso[lo]: the step's start time
+        rk_stages<TB>(P, y, hs, F, tso[lo]);
         rk_combine<TB>(y, hs, F, v, nullptr);
       }
     }
@@ -283,7 +286,6 @@ gal_status gal_integrate_dense(const gal_potential* pot, const gal_solver_config
                                const double* t0, const double* t1, int64_t n, int64_t cap, double* ts, double* coef,
                                int64_t* nsteps, int32_t* status, gal_stream_t stream) {
   if (!pot) return fail(GAL_ERR_INVALID_ARGUMENT, "potential is NULL");
-  if (time_dependent(pot)) return fail(GAL_ERR_UNSUPPORTED, "time-dependent parameters: evaluation and gal_integrate only");
   gal_status st = validate_cfg(cfg);
   if (st != GAL_OK) return st;
   if (n < 0 || cap < 1) return fail(GAL_ERR_INVALID_ARGUMENT, "n >= 0 and cap >= 1 required");
@@ -299,19 +301,21 @@ gal_status gal_integrate_dense(const gal_potential* pot, const gal_solver_config
   const size_t smem = pot->is_mw ? 0 : sizeof(DevComp) * (size_t)pot->n;
   cudaStream_t s = (cudaStream_t)stream;
   if (smem > 48 * 1024) return fail(GAL_ERR_UNSUPPORTED, "dense output supports tables up to 48 KB");
-  if (cfg->method == 8) {
+  auto run = [&](auto tb) {
+    using TB = decltype(tb);
     if (pot->is_mw)
-      k_integrate_dense<Dopri8, MWPot><<<grid, 128, 0, s>>>(a, MWPot{pot->mw}, pot->d_comps, 0, cap, ts, coef, nsteps);
+      k_integrate_dense<TB, MWPot><<<grid, 128, 0, s>>>(a, MWPot{pot->mw}, pot->d_comps, 0, cap, ts, coef, nsteps);
+    else if (pot->d_lin)  // LinearParameter components, refolded at every stage time
+      k_integrate_dense<TB, TimedTablePot><<<grid, 128, smem, s>>>(
+          a, TimedTablePot{pot->d_comps, pot->n, pot->d_lin}, pot->d_comps, pot->n, cap, ts, coef, nsteps);
     else
-      k_integrate_dense<Dopri8, TablePot><<<grid, 128, smem, s>>>(a, TablePot{pot->d_comps, pot->n}, pot->d_comps,
-                                                                  pot->n, cap, ts, coef, nsteps);
-  } else {
-    if (pot->is_mw)
-      k_integrate_dense<Dopri5, MWPot><<<grid, 128, 0, s>>>(a, MWPot{pot->mw}, pot->d_comps, 0, cap, ts, coef, nsteps);
-    else
-      k_integrate_dense<Dopri5, TablePot><<<grid, 128, smem, s>>>(a, TablePot{pot->d_comps, pot->n}, pot->d_comps,
-                                                                  pot->n, cap, ts, coef, nsteps);
-  }
+      k_integrate_dense<TB, TablePot><<<grid, 128, smem, s>>>(a, TablePot{pot->d_comps, pot->n}, pot->d_comps,
+                                                              pot->n, cap, ts, coef, nsteps);
+  };
+  if (cfg->method == 8)
+    run(Dopri8{});
+  else
+    run(Dopri5{});
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? GAL_OK : cuda_fail(e, "dense integration launch");
 }
@@ -320,7 +324,6 @@ gal_status gal_dense_evaluate(const gal_potential* pot, int32_t method, const do
                               const int64_t* nsteps, int64_t cap, int64_t n, const int64_t* orbit, const double* t,
                               int64_t m, double* out, unsigned long long* out_of_bounds, gal_stream_t stream) {
   if (!pot || (method != 5 && method != 8)) return fail(GAL_ERR_INVALID_ARGUMENT, "bad potential or method");
-  if (time_dependent(pot)) return fail(GAL_ERR_UNSUPPORTED, "time-dependent parameters: evaluation and gal_integrate only");
   if (m < 0 || n < 0 || cap < 1) return fail(GAL_ERR_INVALID_ARGUMENT, "bad sizes");
   if (m == 0) return GAL_OK;
   if (!ts || !coef || !nsteps || !orbit || !t || !out || !out_of_bounds)
@@ -331,23 +334,24 @@ gal_status gal_dense_evaluate(const gal_potential* pot, int32_t method, const do
   const size_t smem = pot->is_mw ? 0 : sizeof(DevComp) * (size_t)pot->n;
   if (smem > 48 * 1024) return fail(GAL_ERR_UNSUPPORTED, "dense output supports tables up to 48 KB");
   cudaStream_t s = (cudaStream_t)stream;
-  if (method == 8) {
+  auto run = [&](auto tb) {
+    using TB = decltype(tb);
+    const unsigned g = (unsigned)grid;
     if (pot->is_mw)
-      k_dense_eval<Dopri8, MWPot><<<(unsigned)grid, 128, 0, s>>>(MWPot{pot->mw}, pot->d_comps, 0, ts, coef, nsteps,
-                                                                 cap, n, orbit, t, m, out, out_of_bounds);
+      k_dense_eval<TB, MWPot><<<g, 128, 0, s>>>(MWPot{pot->mw}, pot->d_comps, 0, ts, coef, nsteps, cap, n, orbit, t,
+                                                m, out, out_of_bounds);
+    else if (pot->d_lin && TB::S == Dopri8::S)  // Dopri8 re-evaluates the field: at the step's own times
+      k_dense_eval<TB, TimedTablePot><<<g, 128, smem, s>>>(TimedTablePot{pot->d_comps, pot->n, pot->d_lin},
+                                                           pot->d_comps, pot->n, ts, coef, nsteps, cap, n, orbit, t,
+                                                           m, out, out_of_bounds);
     else
-      k_dense_eval<Dopri8, TablePot><<<(unsigned)grid, 128, smem, s>>>(TablePot{pot->d_comps, pot->n}, pot->d_comps,
-                                                                       pot->n, ts, coef, nsteps, cap, n, orbit, t, m,
-                                                                       out, out_of_bounds);
-  } else {
-    if (pot->is_mw)
-      k_dense_eval<Dopri5, MWPot><<<(unsigned)grid, 128, 0, s>>>(MWPot{pot->mw}, pot->d_comps, 0, ts, coef, nsteps,
-                                                                 cap, n, orbit, t, m, out, out_of_bounds);
-    else
-      k_dense_eval<Dopri5, TablePot><<<(unsigned)grid, 128, smem, s>>>(TablePot{pot->d_comps, pot->n}, pot->d_comps,
-                                                                       pot->n, ts, coef, nsteps, cap, n, orbit, t, m,
-                                                                       out, out_of_bounds);
-  }
+      k_dense_eval<TB, TablePot><<<g, 128, smem, s>>>(TablePot{pot->d_comps, pot->n}, pot->d_comps, pot->n, ts,
+                                                      coef, nsteps, cap, n, orbit, t, m, out, out_of_bounds);
+  };
+  if (method == 8)
+    run(Dopri8{});
+  else
+    run(Dopri5{});
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? GAL_OK : cuda_fail(e, "dense evaluation launch");
 }

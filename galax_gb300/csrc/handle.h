@@ -20,8 +20,8 @@ struct gal_potential {
 };
 
 namespace gal {
-// Entry points that evaluate the potential at fixed times only (adjoint, dense
-// output, streams, surrogate) refuse time-dependent potentials with this.
+// Entry points that evaluate the potential at fixed times only (adjoint,
+// streams, surrogate) refuse time-dependent potentials with this.
 inline bool time_dependent(const gal_potential* p) { return p && p->d_lin; }
 }  // namespace gal
 

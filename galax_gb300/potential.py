@@ -13,8 +13,8 @@ register_funcs.py:327-340, 384-400).
 Inputs are arrays in galax's "galactic" unit system (kpc, Myr, Msun; velocities
 in kpc/Myr) with positions on the last axis, as galax accepts bare arrays. NumPy
 inputs give NumPy outputs; CUDA torch tensors stay on the device. Parameters
-must be constants (galax's ConstantParameter): time-dependent or callable
-parameters are rejected, as are unit systems other than "galactic".
+are constants (galax's ConstantParameter) or galax's LinearParameter; other
+callable parameters are rejected, as are unit systems other than "galactic".
 """
 
 from __future__ import annotations

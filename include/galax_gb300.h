@@ -105,9 +105,10 @@ GAL_API gal_status gal_potential_destroy(gal_potential* pot);
  * m + slopes[i][0] t, l1 + slopes[i][1] t, l2 + slopes[i][2] t, where the
  * component table holds the values at t = 0 (galax's point-slope form
  * p(t) = slope (t - t_i) + p(t_i) gives p(0) = p(t_i) - slope t_i). The
- * gal_eval_* functions evaluate at their t; gal_integrate and
- * gal_integrate_noalloc evaluate every stage at its own time. Adjoint, dense
- * output, stream and surrogate entry points reject time-dependent potentials
+ * gal_eval_* functions evaluate at their t; gal_integrate,
+ * gal_integrate_noalloc and the dense-output pair (gal_integrate_dense,
+ * gal_dense_evaluate) evaluate every stage at its own time. Adjoint, stream
+ * and surrogate entry points reject time-dependent potentials
  * (GAL_ERR_UNSUPPORTED). slopes = NULL makes the potential static again. */
 GAL_API gal_status gal_potential_set_linear(gal_potential* pot, const double* slopes);
 /* Replace the parameters (same count and kinds), e.g. between optimiser steps. */

@@ -119,3 +119,40 @@ def test_table_potential_dense(gx):
     out, *_ = integrate(pot, y0, 0.0, 80.0, ts, cfg)
     q, p = integrate_dense(pot, y0, 0.0, 80.0, cfg).evaluate(ts)
     assert np.array_equal(np.concatenate([q.cpu().numpy(), p.cpu().numpy()], -1), out.permute(2, 1, 0).cpu().numpy())
+
+
+@pytest.mark.parametrize("method,adaptive", [(8, False), (5, True), (8, True)])
+def test_linear_parameters_dense_matches_saves(gx, method, adaptive):
+    """LinearParameter potentials in dense output: every stage, and every
+    Dopri8 re-evaluation, at its own time, so the interpolant at the save times
+    reproduces the save path (constant-step Dopri8 bitwise, otherwise to
+    rounding), and the time dependence is visible against the static values."""
+    from galax_gb300.dynamics import integrate, integrate_dense
+
+    def pot(lin):
+        L = gx.LinearParameter
+        return gx.CompositePotential(
+            disk=gx.MiyamotoNagaiPotential(m_tot=L(5e7, 0.0, 6.8e10) if lin else 6.8e10, a=3.0, b=0.28),
+            halo=gx.NFWPotential(m=L(2e8, 0.0, 5.4e11) if lin else 5.4e11,
+                                 r_s=L(-2e-3, 0.0, 15.62) if lin else 15.62))
+
+    solver = gx.Dopri8() if method == 8 else gx.Dopri5()
+    if adaptive:
+        integ = gx.Integrator(solver=solver, stepsize_controller=gx.PIDController(rtol=1e-8, atol=1e-10))
+    else:
+        integ = gx.Integrator(solver=solver, stepsize_controller=gx.ConstantStepSize(), dt0=1.0)
+    cfg = integ.config()
+    y0 = _ics(64, 7)
+    ts = np.linspace(0.0, 400.0, 29)
+    out, st, _ = integrate(pot(True), y0, 0.0, 400.0, ts, cfg)
+    interp = integrate_dense(pot(True), y0, 0.0, 400.0, cfg)
+    q, p = interp.evaluate(ts)
+    w = np.concatenate([q.cpu().numpy(), p.cpu().numpy()], axis=-1)
+    ref = out.permute(2, 1, 0).cpu().numpy()
+    assert np.all(st.cpu().numpy() == 0)
+    if method == 8 and not adaptive:
+        assert np.array_equal(w, ref)
+    else:
+        assert _rel(w, ref) < 1e-12
+    static, _, _ = integrate(pot(False), y0, 0.0, 400.0, ts, cfg)
+    assert _rel(ref, static.permute(2, 1, 0).cpu().numpy()) > 1e-6

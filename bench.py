@@ -639,7 +639,8 @@ def run_surrogate(args, n, rank, world, dist) -> dict | None:
                      "traffic": None, "ms_per_1M_points": mlp_ms,
                      "note": "MLP forward + input gradient on 1,048,576 points, algorithmic flops; peak = measured "
                              "burst BF16 (cuBLAS) from MEASURED_PEAKS.json"},
-        "clocks": clk, "gpu_launches": args.steps * (1 + 2 * 6 * nsteps),
+        # per run: the first slope (stage kernel + MLP), then per step six stage kernels and six MLP launches
+        "clocks": clk, "gpu_launches": args.steps * (2 + 2 * 6 * nsteps),
     }
 
 
@@ -750,7 +751,11 @@ def run_stream(args, n_rel, rank, world, dist) -> dict | None:
                              "the checkpointed adjoint's count, kept as the unit of work for both storage modes; "
                              "6,000 particles fill 188 warps, and the progenitor is one serial orbit, so the "
                              "pipeline is bound by FP64 latency along its longest chains, not by the FP64 pipe"},
-        "clocks": clk, "gpu_launches": 9 * args.steps,
+        # per gradient: progenitor, release map and particles forward; the particle adjoint (Hessians,
+        # sweep and parameter terms when every stage is stored, one kernel when checkpointed); the
+        # progenitor-cotangent reduction, release-map adjoint, progenitor Hessians, sweep and
+        # parameter terms; the final reduction
+        "clocks": clk, "gpu_launches": (3 + (3 if args.stream_ckpt == 0 else 1) + 5 + 1) * args.steps,
     }
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = stream_cpu_baseline(s)

@@ -50,6 +50,12 @@ def test_abi_version_and_status_strings(lib):
     assert lib.gal_status_string(0) == b"ok"
     assert lib.gal_status_string(4) == b"workspace too small"
     assert lib.gal_status_string(6) == b"host allocation failed"
+    # every status the header declares has its own message
+    codes = [int(v) for v in re.findall(r"GAL_(?:OK|ERR_[A-Z_]+) = (\d+)", HEADER.read_text())]
+    assert sorted(codes) == list(range(len(codes)))
+    msgs = [lib.gal_status_string(c) for c in codes]
+    assert len(set(msgs)) == len(codes) and b"unknown status" not in msgs
+    assert lib.gal_status_string(len(codes)) == b"unknown status"
 
 
 @pytest.mark.parametrize("method", [5, 8])

@@ -203,3 +203,42 @@ def test_linear_parameters_on_the_host():
 
 def test_set_linear_validates_on_the_host(lib):
     assert lib.gal_potential_set_linear(None, None) == 1
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """Every field of the header's structs sits at the offset the ctypes and
+    NumPy layouts use (the header compiled as C99 by the host compiler)."""
+    import shutil
+    import subprocess
+
+    from galax_gb300 import _lib
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no host C compiler")
+    layouts = {
+        "gal_component": {n: (_lib.COMPONENT_DTYPE.fields[n][1]) for n in _lib.COMPONENT_DTYPE.names},
+        "gal_solver_config": {n: getattr(_lib.SolverConfig, n).offset for n, _ in _lib.SolverConfig._fields_},
+        "gal_stream_config": {n: getattr(_lib.StreamConfig, n).offset for n, _ in _lib.StreamConfig._fields_},
+    }
+    sizes = {"gal_component": _lib.COMPONENT_DTYPE.itemsize, "gal_solver_config": C.sizeof(_lib.SolverConfig),
+             "gal_stream_config": C.sizeof(_lib.StreamConfig)}
+    lines = ['#include "galax_gb300.h"', "#include <stdio.h>", "#include <stddef.h>", "int main(void) {"]
+    for st, fields in layouts.items():
+        lines.append(f'  printf("{st} size %zu\\n", sizeof({st}));')
+        for f in fields:
+            lines.append(f'  printf("{st} {f} %zu\\n", offsetof({st}, {f}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c99", "-I", str(HEADER.parent), "-o", str(exe), str(src)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    got = {}
+    for ln in filter(None, out):
+        st, f, v = ln.split()
+        got[(st, f)] = int(v)
+    for st, fields in layouts.items():
+        assert got[(st, "size")] == sizes[st], st
+        for f, off in fields.items():
+            assert got[(st, f)] == off, (st, f)

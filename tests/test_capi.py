@@ -242,3 +242,17 @@ def test_struct_layouts_match_the_header(tmp_path):
         assert got[(st, "size")] == sizes[st], st
         for f, off in fields.items():
             assert got[(st, f)] == off, (st, f)
+
+
+def test_ctypes_signatures_match_the_header_arity():
+    """Each ctypes binding passes as many arguments as the header's prototype
+    declares (a missing or extra argument would shift every later one)."""
+    from galax_gb300 import _lib
+
+    text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
+    protos = re.findall(r"GAL_API\s+[\w\s\*]+?\b(gal_\w+)\((.*?)\);", text, flags=re.S)
+    assert len(protos) == len(declared_symbols())
+    for name, params in protos:
+        params = params.strip()
+        n = 0 if params in ("", "void") else params.count(",") + 1
+        assert len(_lib.SIGNATURES[name][1]) == n, (name, n, len(_lib.SIGNATURES[name][1]))

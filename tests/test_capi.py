@@ -256,3 +256,24 @@ def test_ctypes_signatures_match_the_header_arity():
         params = params.strip()
         n = 0 if params in ("", "void") else params.count(",") + 1
         assert len(_lib.SIGNATURES[name][1]) == n, (name, n, len(_lib.SIGNATURES[name][1]))
+
+
+def test_ctypes_argument_types_match_the_header():
+    """Scalars are bound with the header's width and kind (an int32 passed
+    where an int64 is declared leaves the upper half of the register
+    undefined); pointers and streams are bound as pointers."""
+    from galax_gb300 import _lib
+
+    scalar = {"int32_t": C.c_int32, "int64_t": C.c_int64, "double": C.c_double, "float": C.c_float,
+              "size_t": C.c_size_t}
+    text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
+    for name, params in re.findall(r"GAL_API\s+[\w\s\*]+?\b(gal_\w+)\((.*?)\);", text, flags=re.S):
+        decl = [p.strip() for p in params.split(",") if p.strip() and p.strip() != "void"]
+        for i, (p, t) in enumerate(zip(decl, _lib.SIGNATURES[name][1])):
+            ctype = " ".join(p.split()[:-1])
+            if "*" in p or ctype == "gal_stream_t":
+                is_ptr = t is C.c_void_p or t is C.c_char_p or issubclass(t, C._Pointer) or hasattr(t, "_dtype_")
+                assert is_ptr, (name, i, p, t)
+            else:
+                assert C.sizeof(t) == C.sizeof(scalar[ctype]) and (t._type_ in "fd") == (ctype in ("float", "double")), \
+                    (name, i, p, t)

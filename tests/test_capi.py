@@ -277,3 +277,13 @@ def test_ctypes_argument_types_match_the_header():
             else:
                 assert C.sizeof(t) == C.sizeof(scalar[ctype]) and (t._type_ in "fd") == (ctype in ("float", "double")), \
                     (name, i, p, t)
+
+
+def test_ctypes_return_types_match_the_header():
+    from galax_gb300 import _lib
+
+    want = {"gal_status": C.c_int32, "int32_t": C.c_int32, "int64_t": C.c_int64, "const char*": C.c_char_p}
+    text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
+    for ret, name in re.findall(r"GAL_API\s+([\w\s\*]+?)\b(gal_\w+)\(", text):
+        r, w = _lib.SIGNATURES[name][0], want[" ".join(ret.split())]
+        assert r is w or (w is not C.c_char_p and C.sizeof(r) == C.sizeof(w) and r._type_ in "ilq"), (name, r)

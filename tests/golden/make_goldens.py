@@ -203,6 +203,15 @@ def main(root: Path) -> None:
         "save_ts_linspace": [0.0, 1000.0, 10], "expect_rho": rho, "rho_decimals": 3,
     }
 
+    f = "src/galax/dynamics/_src/orbit/field_hamiltonian.py"
+    fv = numbers(root, f, [118, 119])
+    g["fields"] = {"hamiltonian_kepler": {
+        "cite": f"{f}:103-119 (HamiltonianField(KeplerPotential(1e11)) at t = 0)",
+        "potential": {"kind": "kepler", "m": 1e11, "l1": 0.0, "l2": 0.0},
+        "x": [8.0, 0.0, 0.0], "v": [0.0, 0.22499668, 0.0],
+        "dq_dt": fv[0:3], "dp_dt": fv[3:6], "decimals": 8,
+    }}
+
     g["stream"] = {}
     f = "src/galax/dynamics/_src/cluster/api.py"
     rt = numbers(root, f, [198])

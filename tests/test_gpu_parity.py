@@ -166,6 +166,17 @@ def test_gradient_at_origin_is_zero(gx):
     assert np.all(g == 0)
 
 
+def test_hamiltonian_field_doctest_on_gpu(gx, goldens):
+    """The front end's HamiltonianField on galax's doctest point (Kepler 1e11 at
+    8 kpc, 220 km/s): the printed field to every digit."""
+    g = goldens["fields"]["hamiltonian_kepler"]
+    field = gx.HamiltonianField(gx.KeplerPotential(m_tot=g["potential"]["m"]))
+    w = np.concatenate([g["x"], g["v"]])
+    f = np.asarray(field(0.0, w)).reshape(6)
+    half = 0.5 * 10.0 ** -g["decimals"]
+    np.testing.assert_allclose(f, np.concatenate([g["dq_dt"], g["dp_dt"]]), rtol=0, atol=half)
+
+
 def test_batch_equals_rows_and_orbit_shapes(gx):
     """galax's AbstractPotential_Test (tests/unit/potential/test_base.py:120-131,
     177-201): a batch [[1,2,3],[4,5,6],[7,8,9]] evaluates to its rows evaluated

@@ -58,6 +58,17 @@ def test_density_and_tidal_tensor_goldens(goldens, name):
     np.testing.assert_allclose((H - np.eye(3) * tr / 3).ravel(), g["tidal_tensor"], rtol=1e-5, atol=1e-8)
 
 
+def test_hamiltonian_field_doctest(goldens):
+    """galax's HamiltonianField doctest: (dq/dt, dp/dt) = (p, -grad Phi) of a
+    Kepler potential at 8 kpc, to every printed digit."""
+    g = goldens["fields"]["hamiltonian_kepler"]
+    c = golden_comps(g["potential"])
+    acc = -O.gradient(c, np.array([g["x"]]))[0]
+    half = 0.5 * 10.0 ** -g["decimals"]
+    np.testing.assert_allclose(g["v"], g["dq_dt"], rtol=0, atol=half)
+    np.testing.assert_allclose(acc, g["dp_dt"], rtol=0, atol=half)
+
+
 def test_gradient_is_finite_at_origin():
     c = O.milky_way()
     g = O.gradient(c, np.zeros((1, 3)))

@@ -130,86 +130,6 @@ def fp64_peak() -> dict:
     return {"tflops": best / 1e12, "how": "dependent-chain DFMA probe, 8 chains/thread, full-device grid, best of 3"}
 
 
-def run_study(args) -> dict:
-    """Measurements behind the uneven workload's design (not a bench line):
-    ``latency``: SM cycles per dependent FP64 operation on a lone chain;
-    ``tail``: one step of the uneven workload, then the K longest orbits alone
-    and the batch without them; ``shapes``: one step under several launch
-    shapes; ``teams``: one step by the number of SMs given to four-warp teams. CUDA events on the current stream, best (tail) or all (shapes) of
-    repeated runs."""
-    import ctypes as C
-
-    import torch
-
-    import galax_gb300 as gx
-    from galax_gb300 import _lib, autotune
-    from galax_gb300.dynamics import Workspace, integrate
-
-    torch.cuda.set_device(0)
-    if args.study == "latency":
-        L = _lib.load()
-        names = ("fma", "log1p (CUDA)", "log1p (table-driven)", "rsqrt", "sqrt", "division", "exp", "log")
-        out = {}
-        for w, nm in enumerate(names):
-            c = C.c_double()
-            _lib.check(L.gal_fp64_latency_probe(w, 20000, C.byref(c)), "gal_fp64_latency_probe")
-            out[nm] = round(c.value, 1)
-        return {"study": "latency", "unit": "SM cycles per dependent operation (lone thread)", "cycles": out}
-    mw, b = make_uneven(args.orbits or DEFAULT_ORBITS["uneven"], seed=1)
-    cfg = gx.Integrator(solver=gx.Dopri5(), stepsize_controller=gx.PIDController(rtol=1e-8, atol=1e-10),
-                        max_steps=2**16).config()
-    ws = Workspace()
-
-    def subset(idx):
-        idx = np.asarray(idx)
-        ns = b.save_offsets[idx + 1] - b.save_offsets[idx]
-        offs = np.zeros(len(idx) + 1, np.int64)
-        offs[1:] = np.cumsum(ns)
-        pick = np.concatenate([np.arange(b.save_offsets[i], b.save_offsets[i + 1]) for i in idx])
-        return [torch.as_tensor(v, device="cuda") for v in
-                (b.y0[idx].T.copy(), b.t0[idx], b.t1[idx], offs, b.save_ts[pick])]
-
-    def timed(data, reps):
-        y0, t0, t1, offs, sts = data
-        ts, steps = [], None
-        for _ in range(reps):
-            torch.cuda.synchronize()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record()
-            _, _, steps = integrate(mw, y0, t0, t1, sts, cfg, save_offsets=offs, soa=True, workspace=ws)
-            e1.record()
-            torch.cuda.synchronize()
-            ts.append(round(e0.elapsed_time(e1), 1))
-        return ts, steps
-
-    full = subset(np.arange(len(b.t1)))
-    if args.study == "teams":
-        L = _lib.load()
-        out = {}
-        for blocks in (0, 4, 8, 16, 32, 64):
-            _lib.check(L.gal_set_team(blocks), "gal_set_team")
-            out[str(blocks)], _ = timed(full, 3)
-        _lib.check(L.gal_set_team(32), "gal_set_team")
-        return {"study": "teams", "unit": "ms per step (3 runs) by SMs given to four-warp teams", "ms": out}
-    if args.study == "shapes":
-        out = {}
-        for shape in ((128, 0, 2), (128, 1, 2), (64, 2, 2), (128, 1, 0), (256, 1, 2), (128, 2, 2)):
-            autotune.set_launch(5, True, *shape)
-            out["%dx%dv%d" % shape], _ = timed(full, 3)
-        return {"study": "shapes", "unit": "ms per step (3 runs)", "ms": out}
-    ms, steps = timed(full, 2)
-    steps = steps.cpu().numpy()
-    order = np.argsort(-steps)
-    out = {"study": "tail", "unit": "ms (best of 2)", "full": min(ms), "accepted_steps": int(steps.sum()),
-           "longest": steps[order[:5]].tolist(),
-           "quantiles": {str(q): float(np.quantile(steps, q)) for q in (0.5, 0.9, 0.99, 0.999)}}
-    for k in (1, 152, 2432):
-        out[f"longest_{k}_alone"] = min(timed(subset(np.sort(order[:k])), 2)[0])
-    for k in (2432, 9728):
-        out[f"without_longest_{k}"] = min(timed(subset(np.sort(order[k:])), 2)[0])
-    return out
-
-
 def measured_peaks() -> dict:
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -883,14 +803,9 @@ def main():
                     help="stream workload: particle checkpoint interval (0 = store every stage, no recompute)")
     ap.add_argument("--split-radius", type=float, default=12.0,
                     help="surrogate workload: short-range split radius in kpc (0 = the MLP learns the whole sum)")
-    ap.add_argument("--study", choices=("latency", "tail", "shapes", "teams"), default=None,
-                    help="print a design measurement instead of a bench line")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("note: fewer than 3 warm-up steps", file=sys.stderr)
-    if args.study:
-        print(json.dumps(run_study(args)), flush=True)
-        return
     line = run_reference(args) if args.impl == "reference" else run_ours(args)
     if line is not None:
         print(json.dumps(line), flush=True)

@@ -133,7 +133,6 @@ SIGNATURES = {
                                           C.c_int32, _VP, C.c_size_t, C.c_void_p]),
     "gal_tableau": (C.c_int32, [C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "gal_fp64_peak_probe": (C.c_int, [C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_void_p]),
-    "gal_fp64_latency_probe": (C.c_int, [C.c_int32, C.c_int32, C.POINTER(C.c_double)]),
     "gal_status_string": (C.c_char_p, [C.c_int32]),
     "gal_last_error": (C.c_char_p, []),
     "gal_abi_version": (C.c_int32, []),

@@ -40,6 +40,40 @@ static cudaError_t team_stream(cudaStream_t* out) {
   return cudaSuccess;
 }
 
+// The fork/join event pair that orders the team stream after, and the caller's
+// stream before, one team launch. Created once per thread and device and then
+// reused: an event is re-recorded by every call, and cudaStreamWaitEvent takes
+// the record current at the time of the wait, so a pair must not be shared
+// between threads that launch concurrently.
+struct TeamEvents {
+  cudaEvent_t ev[64][2] = {};
+  ~TeamEvents() {
+    for (auto& p : ev)
+      for (cudaEvent_t e : p)
+        if (e) cudaEventDestroy(e);
+  }
+};
+
+static cudaError_t team_events(cudaEvent_t* fork, cudaEvent_t* join) {
+  thread_local TeamEvents cache;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  for (int k = 0; k < 2; ++k) {
+    if (!cache.ev[dev][k]) {
+      e = cudaEventCreateWithFlags(&cache.ev[dev][k], cudaEventDisableTiming);
+      if (e != cudaSuccess) {
+        cache.ev[dev][k] = nullptr;
+        return e;
+      }
+    }
+  }
+  *fork = cache.ev[dev][0];
+  *join = cache.ev[dev][1];
+  return cudaSuccess;
+}
+
 // Launch shape per [method == 8][adaptive], set by gal_set_launch. Dopri5 fits
 // 3 blocks of 128 per SM without spills (variant 0); Dopri8 needs the uncapped
 // variant 2 to avoid spilling. Adaptive batches default to one warp per SM
@@ -206,29 +240,6 @@ __global__ void k_fp64_probe(int64_t iters, double seed, double* sink) {
   }
   const double s = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
   if (s == 12345.678) sink[threadIdx.x] = s;  // keep the chain alive
-}
-
-// Lone-chain latency: one thread of one warp runs `iters` dependent
-// operations of one kind; cycles measured with clock64 on the device.
-__global__ void k_fp64_latency(int which, int iters, double seed, long long* cycles, double* sink) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  double x = seed;
-  const long long t0 = clock64();
-  for (int i = 0; i < iters; ++i) {
-    switch (which) {
-      case 0: x = fma(x, 0.999999, 1e-7); break;
-      case 1: x = log1p(x) + 0.5; break;
-      case 2: x = log1p_pos(x) + 0.5; break;
-      case 3: x = rsqrt(x) + 0.5; break;
-      case 4: x = sqrt(x) + 0.5; break;
-      case 5: x = 1.0 / x + 0.5; break;
-      case 6: x = exp(-x) + 0.5; break;
-      default: x = log(x) + 2.0; break;
-    }
-  }
-  const long long t1 = clock64();
-  *cycles = t1 - t0;
-  *sink = x;
 }
 
 gal_status validate_cfg(const gal_solver_config* c) {
@@ -637,8 +648,7 @@ gal_status gal_integrate(const gal_potential* p, const gal_solver_config* cfg, c
     cudaStream_t ts = nullptr;
     e = team_stream(&ts);
     cudaEvent_t fork = nullptr, join = nullptr;
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&join, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = team_events(&fork, &join);
     if (e == cudaSuccess) e = cudaEventRecord(fork, s);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(ts, fork, 0);
     bool team_launched = false, joinable = false;
@@ -662,10 +672,12 @@ gal_status gal_integrate(const gal_potential* p, const gal_solver_config* cfg, c
       const cudaError_t ej = cudaStreamWaitEvent(s, join, 0);
       if (e == cudaSuccess) e = ej;
     } else if (team_launched) {
-      cudaStreamSynchronize(ts);
+      // Under stream capture nothing has run yet and a synchronize would
+      // invalidate the caller's capture; the caller discards it on this error.
+      cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+      if (cudaStreamIsCapturing(s, &cap) != cudaSuccess || cap == cudaStreamCaptureStatusNone)
+        cudaStreamSynchronize(ts);
     }
-    if (fork) cudaEventDestroy(fork);
-    if (join) cudaEventDestroy(join);
     return e == cudaSuccess ? GAL_OK : cuda_fail(e, "integrate kernel launch (second pass, teams)");
   }
   e = launch();
@@ -689,24 +701,6 @@ int32_t gal_tableau(int32_t method, double* c, double* a, double* b, double* e) 
     return TB::S;
   };
   return method == 5 ? copy(Dopri5{}) : copy(Dopri8{});
-}
-
-gal_status gal_fp64_latency_probe(int32_t which, int32_t iters, double* cycles_per_op) {
-  if (which < 0 || which > 7 || iters < 1 || !cycles_per_op) return fail(GAL_ERR_INVALID_ARGUMENT, "bad probe arguments");
-  long long* d = nullptr;
-  cudaError_t e = cudaMalloc(&d, 2 * sizeof(long long));
-  if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(latency probe)");
-  double* sink = reinterpret_cast<double*>(d + 1);
-  long long c = 0;
-  for (int rep = 0; rep < 2 && e == cudaSuccess; ++rep) {  // the first run warms the instruction cache
-    k_fp64_latency<<<1, 32>>>(which, iters, 1.3, d, sink);
-    e = cudaGetLastError();
-    if (e == cudaSuccess) e = cudaMemcpy(&c, d, sizeof(c), cudaMemcpyDeviceToHost);
-  }
-  cudaFree(d);
-  if (e != cudaSuccess) return cuda_fail(e, "latency probe");
-  *cycles_per_op = (double)c / iters;
-  return GAL_OK;
 }
 
 gal_status gal_fp64_peak_probe(int64_t iters, double* ms, double* flops, gal_stream_t stream) {

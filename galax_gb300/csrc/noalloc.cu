@@ -3,14 +3,18 @@
 //
 // gal_integrate takes its scratch (the work-queue counter and, for the two-pass
 // schedule, one resume record per orbit) from a caller-provided workspace. Some
-// callers cannot provide one: code that runs while a CUDA graph is being
-// captured, host plugins that are handed only their input and output buffers
-// (an XLA custom call without a scratch allocator, for instance), and services
-// that forbid device allocation after start-up. For them this entry point
-// takes the scratch from a fixed array that lives in the library's own device
-// memory (allocated by the CUDA runtime when the library's module loads, and
-// held by every GPU that loads the library until the process exits), and then
-// runs the same integration path as gal_integrate.
+// callers cannot provide one: host plug-ins that are handed only their input
+// and output buffers (an XLA custom call registered without a scratch
+// allocator, for instance), services that forbid device allocation after
+// start-up, and hosts with a fixed device-memory budget. For them this entry
+// point takes the scratch from a fixed array that lives in the library's own
+// device memory (allocated by the CUDA runtime when the library's module loads,
+// and held by every GPU that loads the library until the process exits), and
+// then runs the same integration path as gal_integrate.
+//
+// The array's device address is looked up once per device and cached. A
+// cudaDeviceReset unloads the module, so the cached address is then stale; the
+// header tells callers not to use this entry point on a device after a reset.
 #include <cuda_runtime.h>
 
 #include <mutex>

@@ -117,8 +117,9 @@ GAL_API int32_t gal_potential_num_components(const gal_potential* pot);
 /* 1 when the composite is evaluated by the specialised MilkyWayPotential kernel. */
 GAL_API int32_t gal_potential_is_milky_way(const gal_potential* pot);
 
-/* Batched evaluation at n positions x[3][n] (time t is accepted for API parity:
- * all supported parameters are constant in time).
+/* Batched evaluation at n positions x[3][n] at time t. t matters only for a
+ * potential with LinearParameter slopes (gal_potential_set_linear), whose
+ * parameters are evaluated at t; static potentials ignore it.
  *   gal_eval_potential    : phi[n]       replaces AbstractPotential._potential   (base.py:113-136)
  *   gal_eval_gradient     : out[3][n]    replaces AbstractPotential._gradient    (base.py:170-179)
  *   gal_eval_acceleration : out[3][n]    replaces api.acceleration = -gradient   (register_funcs.py:327-340)
@@ -181,22 +182,26 @@ GAL_API gal_status gal_integrate(const gal_potential* pot, const gal_solver_conf
                          double* out, int32_t* status, int64_t* steps, const int32_t* order, int64_t n,
                          void* workspace, size_t workspace_bytes, gal_stream_t stream);
 
-/* gal_integrate without a workspace (no counterpart in the reference: galax runs
- * under XLA, which manages all device memory).
+/* gal_integrate without a workspace. It has no counterpart in the reference:
+ * galax runs under XLA, which manages all device memory.
  *
- * For callers that cannot allocate device memory: code running while a CUDA
- * graph is captured, plugins that are handed only their input and output
- * buffers, services that forbid allocation after start-up. The scratch that
+ * For callers that cannot allocate device memory: plug-ins that are handed
+ * only their input and output buffers (an XLA custom call registered without a
+ * scratch allocator, say), services that forbid device allocation after
+ * start-up, and hosts with a fixed device-memory budget. The scratch that
  * gal_integrate takes from its workspace comes instead from a fixed array of
  * GAL_NOALLOC_SCRATCH_BYTES (4 MiB) in the library's own device memory, which
  * every GPU that loads the library holds until the process exits. Inputs and
  * outputs are the caller's, exactly as for gal_integrate, and the results are
- * the same. This function allocates and frees nothing.
+ * bitwise the same. This function allocates and frees nothing.
  *  - Limit: a call whose gal_integrate_workspace_size exceeds the array is
  *    rejected with GAL_ERR_TOO_LARGE (with schedule = 1 that is about 30,000
  *    orbits per call; with schedule = 0 only 8 bytes are needed, so any n).
- *  - The first call on each device looks up the array's device address with
- *    that device current; make that first call before any stream capture.
+ *  - Set-up: the first call on each device looks up the array's device address
+ *    (cudaGetSymbolAddress) with that device current and keeps it for later
+ *    calls; make that first call before any stream capture. cudaDeviceReset
+ *    unloads the library's module and with it the array: do not call this
+ *    function on a device after resetting it.
  *  - All calls share the one array and it keeps the previous call's contents
  *    (each call clears what must start at zero). Calls that overlap on the GPU,
  *    from different streams or threads, race on it: serialise them. */
@@ -439,11 +444,6 @@ GAL_API int32_t gal_tableau(int32_t method, double* c, double* a, double* b, dou
  * a full-device grid and writes the elapsed device time (ms) to *ms. Used to
  * measure the chip's FP64 peak for roofline reporting. */
 GAL_API gal_status gal_fp64_peak_probe(int64_t iters, double* ms, double* flops, gal_stream_t stream);
-/* Lone-chain latency probe (synchronous, default stream): one thread runs
- * `iters` dependent operations and *cycles_per_op receives SM cycles per
- * operation. which: 0 FMA, 1 log1p, 2 the library's table-driven log1p,
- * 3 rsqrt, 4 sqrt, 5 division, 6 exp, 7 log (each but FMA plus one add). */
-GAL_API gal_status gal_fp64_latency_probe(int32_t which, int32_t iters, double* cycles_per_op);
 GAL_API const char* gal_status_string(int32_t status);
 GAL_API const char* gal_last_error(void);
 GAL_API int32_t gal_abi_version(void);

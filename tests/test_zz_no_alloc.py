@@ -1,7 +1,8 @@
 """gal_integrate_noalloc: the integration entry point for callers that cannot
-allocate device memory (graph capture, plugins handed only their buffers,
-allocation-free services). It must give exactly what gal_integrate gives with a
-caller workspace, call after call, although every call reuses the same built-in
+allocate device memory (plug-ins handed only their input and output buffers,
+services that forbid allocation after start-up, hosts with a fixed device-memory
+budget). It must give bitwise what gal_integrate gives with a caller
+workspace, call after call, although every call reuses the same built-in
 scratch array, and must refuse calls whose scratch would not fit.
 
 Collected last on purpose (``zz``), so that a run that stops at the first
@@ -90,7 +91,9 @@ def test_noalloc_matches_workspace_path_on_consecutive_calls(env, schedule):
         assert np.all(ref[1] == 0)
         np.testing.assert_array_equal(got[1], ref[1])
         np.testing.assert_array_equal(got[2], ref[2])
-        np.testing.assert_allclose(got[0], ref[0], rtol=1e-12, atol=0)
+        # same kernels, same scratch layout: any difference, even one rounding,
+        # would mean the shared array leaked state from the previous call
+        np.testing.assert_array_equal(got[0], ref[0])
 
 
 def test_noalloc_rejects_calls_beyond_its_scratch(env):

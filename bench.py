@@ -188,14 +188,19 @@ def run_ours(args) -> dict | None:
     offs = torch.as_tensor(b.save_offsets, device=dev)
     sts = torch.as_tensor(b.save_ts, device=dev)
     total_saves = int(b.save_offsets[-1])
-    # longest-first order: cost estimate = duration x local orbital frequency
-    r = torch.linalg.vector_norm(y0[:3], dim=0)
-    a = torch.linalg.vector_norm(torch.as_tensor(mw.gradient(y0[:3].t())), dim=1)
-    order = torch.argsort(t1 * torch.sqrt(a / r), descending=True).to(torch.int32).contiguous()
     ws = Workspace()
     stream = torch.cuda.current_stream()
 
+    def longest_first(y0_, t0_, t1_):
+        # hand-out order for the first pass: cost estimate = duration x local
+        # orbital frequency sqrt(|grad Phi| / r), longest first (part of every
+        # timed step: one gradient kernel and a device sort)
+        r = torch.linalg.vector_norm(y0_[:3], dim=0)
+        a = torch.linalg.vector_norm(mw.gradient(y0_[:3].t()), dim=1)
+        return torch.argsort((t1_ - t0_).abs() * torch.sqrt(a / r), descending=True).to(torch.int32)
+
     def step():
+        order = longest_first(y0, t0, t1)
         return integrate(mw, y0, t0, t1, sts, cfg, save_offsets=offs, order=order, soa=True, workspace=ws)
 
     out, status, steps = step()  # first call: lazy set-up outside any measurement
@@ -259,8 +264,9 @@ def run_ours(args) -> dict | None:
         dt1 = h_t1.to(dev, non_blocking=True)
         doffs = h_offs.to(dev, non_blocking=True)
         dts = h_ts.to(dev, non_blocking=True)
-        integrate(mw, dy0, dt0, dt1, dts, cfg, save_offsets=doffs, order=order, soa=True, workspace=ws,
-                  out=h_out, status=h_status)
+        order = longest_first(dy0, dt0, dt1)
+        return integrate(mw, dy0, dt0, dt1, dts, cfg, save_offsets=doffs, order=order, soa=True, workspace=ws,
+                         out=h_out, status=h_status)[2]
 
     e2e_step()
     torch.cuda.synchronize()
@@ -269,7 +275,7 @@ def run_ours(args) -> dict | None:
     t_start = time.perf_counter()
     e2e_steps = max(1, min(args.steps, 3))
     for _ in range(e2e_steps):
-        e2e_step()
+        e2e_acc = e2e_step()
     torch.cuda.synchronize()
     e2e_ms = (time.perf_counter() - t_start) * 1e3 / e2e_steps
     if dist:
@@ -310,15 +316,73 @@ def run_ours(args) -> dict | None:
                              "peak_gbs": measured_peaks().get("hbm_gbs"),
                              "note": "save writes only; of measured"}},
         "clocks": clk,
-        # per step: the first pass, three ordering kernels and the second pass
-        # (one launch, or two when the longest orbits go to four-warp teams)
-        "gpu_launches": launches * ((6 if team_blocks > 0 else 5) if cfg.schedule else 1),
+        # per step: the gradient kernel of the hand-out order, the first pass,
+        # three ordering kernels and the second pass (one launch, or two when
+        # the longest orbits go to four-warp teams)
+        "gpu_launches": launches * (1 + ((6 if team_blocks > 0 else 5) if cfg.schedule else 1)),
     }
     if world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(b, target_s=args.cpu_seconds)
+        line["cpu_baseline"], sample = cpu_baseline(b, target_s=args.cpu_seconds)
+        line["parity"] = parity_at_full_size(b, sample, h_out.numpy(), h_status.numpy(), e2e_acc.cpu().numpy())
+    if world == 1 and args.extras:
+        line["extra"] = run_extras(args)
     if dist:
         dist.destroy_process_group()
     return line
+
+
+def parity_at_full_size(b, sample, out_gpu, status_gpu, acc_gpu, rtol: float = 1e-8) -> dict:
+    """The CPU-baseline leg's oracle orbits against the GPU saves of the same
+    orbits from the end-to-end run of the full batch: per orbit, the largest
+    relative position and velocity error over its saves (|dq|/|q|, |dv|/|v|),
+    and whether the accepted-step counts are equal."""
+    idx, saves_o, st_o, acc_o = sample
+    offs = b.save_offsets
+    lens = offs[idx + 1] - offs[idx]
+    pos = np.repeat(offs[idx] - np.concatenate([[0], np.cumsum(lens)[:-1]]), lens) + np.arange(int(lens.sum()))
+    g = out_gpu[:, pos].T  # (saves, 6), the oracle's order
+    err = np.zeros(len(g))
+    for sl in (slice(0, 3), slice(3, 6)):
+        d = np.linalg.norm(g[:, sl] - saves_o[:, sl], axis=1)
+        err = np.maximum(err, d / np.maximum(np.linalg.norm(saves_o[:, sl], axis=1), 1e-300))
+    starts = np.concatenate([[0], np.cumsum(lens)[:-1]])
+    per_orbit = np.maximum.reduceat(err, starts) if len(err) else np.zeros(0)
+    same = acc_gpu[idx] == acc_o
+    worst = int(np.argmax(per_orbit))
+    return {
+        "orbits_compared": int(len(idx)), "saves_compared": int(len(g)),
+        "max_rel": float(per_orbit.max()), "median_rel": float(np.median(per_orbit)),
+        "p999_rel": float(np.quantile(per_orbit, 0.999)),
+        "within_10x_rtol": float(np.mean(per_orbit <= 10 * rtol)),
+        "identical_step_sequences": float(np.mean(same)),
+        "max_rel_where_step_counts_equal": float(per_orbit[same].max()) if same.any() else None,
+        "status_equal": bool(np.array_equal(status_gpu[idx], st_o)),
+        "worst_orbit": {"accepted_steps": int(acc_o[worst]), "rel": float(per_orbit[worst])},
+        "longest_orbit_compared": {"accepted_steps": int(acc_o.max()),
+                                   "rel": float(per_orbit[int(np.argmax(acc_o))])},
+        "orbits_over_40k_steps": int(np.sum(acc_o > 40_000)),
+        "note": "oracle = C++ FP64 restatement (per-orbit PID controllers); GPU saves from the end-to-end run; "
+                "identical_step_sequences = equal accepted-step counts; tolerance 10 x rtol = 1e-7",
+    }
+
+
+def run_extras(args) -> dict:
+    """The other two parts of the metric on the same GPU, after the headline:
+    gradients/s of the differentiation workload at full size, and the learned
+    surrogate against the plain FP64 direct sum."""
+    import argparse as _ap
+
+    out = {}
+    g = run_grad(_ap.Namespace(**{**vars(args), "steps": 2, "warmup": 3, "t1": 0.0}), DEFAULT_ORBITS["grad"], 0, 1,
+                 None)
+    out["grad"] = {k: g[k] for k in ("metric", "value", "unit", "ms_per_step", "steps", "warmup", "config", "e2e",
+                                     "roofline", "gpu_launches")}
+    sg = run_surrogate(_ap.Namespace(**{**vars(args), "steps": 2, "warmup": 3}), DEFAULT_ORBITS["surrogate"], 0, 1,
+                       None)
+    out["surrogate"] = {k: sg[k] for k in ("metric", "value", "unit", "ms_per_step", "steps", "warmup", "config",
+                                           "plain_fp64_direct_sum", "speedup_vs_plain", "median_rel_pos_err_1gyr",
+                                           "roofline", "gpu_launches")}
+    return out
 
 
 def _timed(fn, steps, stream):
@@ -728,20 +792,22 @@ def cpu_baseline(b, target_s: float = 15.0) -> dict:
     def run(idx):
         grids = [b.save_ts[b.save_offsets[i]:b.save_offsets[i + 1]] for i in idx]
         t = time.perf_counter()
-        _, st, acc, _ = O.integrate(comps, b.y0[idx], b.t0[idx], b.t1[idx], grids, cfg, nthreads=cores)
-        return time.perf_counter() - t, int(acc.sum())
+        saves, st, acc, _ = O.integrate(comps, b.y0[idx], b.t0[idx], b.t1[idx], grids, cfg, nthreads=cores,
+                                        flat=True)
+        return time.perf_counter() - t, int(acc.sum()), (idx, saves, st, acc)
 
     m = max(64, 4 * cores)
-    dt, acc = run(idx_all[:m])
+    dt, acc, res = run(idx_all[:m])
     while dt < 1.0 and m < len(idx_all):
         m = min(len(idx_all), m * 4)
-        dt, acc = run(idx_all[:m])
+        dt, acc, res = run(idx_all[:m])
     m2 = int(min(len(idx_all), max(m, m * target_s / max(dt, 1e-3))))
     if m2 > m:
-        dt, acc = run(idx_all[:m2])
+        dt, acc, res = run(idx_all[:m2])
         m = m2
-    return {"value": acc / dt, "unit": "orbit-steps/s", "cores": cores, "kind": "port",
-            "sample": f"{m} randomly chosen orbits of the same workload ({acc} accepted steps, {dt:.1f} s wall)"}
+    return ({"value": acc / dt, "unit": "orbit-steps/s", "cores": cores, "kind": "port",
+             "sample": f"{m} randomly chosen orbits of the same workload ({acc} accepted steps, {dt:.1f} s wall)"},
+            res)
 
 
 def run_reference(args) -> dict | None:
@@ -795,6 +861,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--extras", action=argparse.BooleanOptionalAction, default=True,
+                    help="uneven workload at one GPU: also measure the gradient and surrogate workloads")
     ap.add_argument("--t1", type=float, default=0.0, help="grad workload: end time in Myr (default 2000)")
     ap.add_argument("--train-points", type=int, default=4_194_304, help="surrogate workload: training samples")
     ap.add_argument("--train-epochs", type=int, default=400, help="surrogate workload: training epochs")

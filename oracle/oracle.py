@@ -261,11 +261,14 @@ def integrate(
     G: float = G_GALACTIC,
     nthreads: int = 0,
     slopes=None,
+    flat: bool = False,
 ):
     """Integrate orbits. ``save_ts`` is a list of per-orbit 1-D arrays or a
     single 1-D array shared by all orbits. Returns (saves list of (T_i, 6),
     status, accepted, rejected); in lockstep mode saves is (T, n, 6).
-    ``slopes`` (ncomp, 3): linear time dependence of (m, l1, l2)."""
+    ``slopes`` (ncomp, 3): linear time dependence of (m, l1, l2).
+    ``flat``: return the saves as one (sum T_i, 6) array in orbit order instead
+    of a list."""
     y0 = np.ascontiguousarray(np.atleast_2d(np.asarray(y0, np.float64)))
     n = len(y0)
     t0 = np.ascontiguousarray(np.broadcast_to(np.asarray(t0, np.float64), (n,)))
@@ -276,7 +279,7 @@ def integrate(
         save_list = [np.asarray(s, np.float64).ravel() for s in save_ts]
     offs = np.zeros(n + 1, np.int64)
     offs[1:] = np.cumsum([len(s) for s in save_list])
-    flat = np.ascontiguousarray(np.concatenate(save_list) if n else np.zeros(0))
+    ts_flat = np.ascontiguousarray(np.concatenate(save_list) if n else np.zeros(0))
     status = np.zeros(n, np.int32)
     acc = np.zeros(n, np.int64)
     rej = np.zeros(n, np.int64)
@@ -287,10 +290,10 @@ def integrate(
         out = np.empty((int(offs[-1]), 6))
     keep, sp = _slopes_ptr(c, slopes)
     lib().orc_integrate(
-        np.ascontiguousarray(c), len(c), G, C.byref(cfg), y0, t0, t1, offs, flat, out, status, acc, rej, n,
+        np.ascontiguousarray(c), len(c), G, C.byref(cfg), y0, t0, t1, offs, ts_flat, out, status, acc, rej, n,
         nthreads, sp,
     )
-    if cfg.lockstep:
+    if cfg.lockstep or flat:
         return out, status, acc, rej
     return [out[offs[i]:offs[i + 1]] for i in range(n)], status, acc, rej
 

@@ -415,6 +415,71 @@ def test_adjoint_matches_oracle(gx, which):
     assert abs(res.loss - L_o) <= 1e-10 * L_o
 
 
+@pytest.mark.parametrize("method", [8, 5])
+def test_adjoint_matches_oracle_at_the_differentiation_shape(gx, method):
+    """The differentiation workload's shape: dt = 0.5 Myr, checkpoints every 256
+    steps, 1,200 steps (four full segments and a partial fifth), Milky Way, the
+    workload's initial conditions; both tableaux."""
+    import torch
+
+    from galax_gb300 import workloads as W
+    from galax_gb300.adjoint import orbit_adjoint
+
+    comps = O.milky_way()
+    n, dt, t1 = 128, 0.5, 600.0
+    y0 = W.disk_like_ics(lambda x: O.gradient(comps, x), n, seed=2)
+    cfg = O.solver_cfg(method, False, dt0=dt)
+    yT_ref, *_ = O.integrate(comps, y0, 0.0, t1, np.array([t1]), cfg)
+    rng = np.random.default_rng(20)
+    target = np.stack(yT_ref).reshape(-1, 6) + np.concatenate(
+        [rng.normal(0, 0.1, (n, 3)), rng.normal(0, 2 * 0.001022712165045695, (n, 3))], axis=1)
+    yT_o, gy_o, gp_o, L_o = O.adjoint_fixed(comps, y0, 0.0, t1, target, cfg)
+    res = orbit_adjoint(gx.MilkyWayPotential(), y0, 0.0, t1, dt=dt, target=target, method=method, k_ckpt=256)
+    torch.cuda.synchronize()
+    assert _rel(res.yT, yT_o) < 1e-9
+    np.testing.assert_allclose(res.grad_y0, gy_o, rtol=1e-7, atol=1e-10 * np.abs(gy_o).max())
+    mask = gp_o != 0
+    np.testing.assert_allclose(res.grad_params[mask], gp_o[mask], rtol=1e-7)
+    assert abs(res.loss - L_o) <= 1e-9 * L_o
+    # the checkpoint interval changes only where the forward states come from
+    res16 = orbit_adjoint(gx.MilkyWayPotential(), y0, 0.0, t1, dt=dt, target=target, method=method, k_ckpt=16)
+    np.testing.assert_array_equal(res16.grad_y0, res.grad_y0)
+    np.testing.assert_array_equal(res16.grad_params, res.grad_params)
+
+
+def test_orbit_map_backward_matches_oracle_adjoint(gx):
+    """The torch.autograd.Function: loss.backward() through OrbitMap gives the
+    oracle's discrete-adjoint gradients with respect to the initial conditions
+    and the (m, l1, l2) of every component."""
+    import torch
+
+    from galax_gb300 import workloads as W
+    from galax_gb300.adjoint import OrbitMap, params_of
+
+    comps = O.milky_way()
+    n, dt, t1 = 64, 0.5, 300.0
+    y0h = W.disk_like_ics(lambda x: O.gradient(comps, x), n, seed=5)
+    cfg = O.solver_cfg(8, False, dt0=dt)
+    yT_ref, *_ = O.integrate(comps, y0h, 0.0, t1, np.array([t1]), cfg)
+    rng = np.random.default_rng(6)
+    target = np.stack(yT_ref).reshape(-1, 6) + rng.normal(0, 0.05, (n, 6))
+    _, gy_o, gp_o, L_o = O.adjoint_fixed(comps, y0h, 0.0, t1, target, cfg)
+
+    mw = gx.MilkyWayPotential()
+    y0 = torch.tensor(y0h, dtype=torch.float64, device="cuda", requires_grad=True)
+    params = params_of(mw).requires_grad_()
+    yT = OrbitMap.apply(mw, y0, params, 0.0, t1, dt, 8, 64)
+    loss = ((yT - torch.as_tensor(target, device="cuda")) ** 2).sum()
+    loss.backward()
+    torch.cuda.synchronize()
+    assert abs(float(loss) - L_o) <= 1e-9 * L_o
+    np.testing.assert_allclose(y0.grad.cpu().numpy(), gy_o, rtol=1e-8, atol=1e-12 * np.abs(gy_o).max())
+    gp = params.grad.cpu().numpy()
+    mask = gp_o != 0
+    np.testing.assert_allclose(gp[mask], gp_o[mask], rtol=1e-8)
+    np.testing.assert_array_equal(gp[~mask], 0.0)
+
+
 @pytest.mark.parametrize("method", [5, 8])
 def test_two_pass_schedule_is_bitwise_identical(gx, method):
     """Longest-remaining-first rescheduling parks and resumes orbits from their

@@ -95,6 +95,7 @@ SIGNATURES = {
                                         _DP, _I32P, _I64P, _I32P, C.c_int64, C.c_void_p]),
     "gal_set_launch": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
     "gal_set_team": (C.c_int, [C.c_int32]),
+    "gal_set_table_lanes": (C.c_int, [C.c_int32]),
     "gal_dense_coef_per_step": (C.c_int32, [C.c_int32]),
     "gal_integrate_dense": (C.c_int, [C.c_void_p, C.POINTER(SolverConfig), _DP, _DP, _DP, C.c_int64, C.c_int64, _DP,
                                       _DP, _I64P, _I32P, C.c_void_p]),
@@ -115,6 +116,7 @@ SIGNATURES = {
                                        C.c_void_p]),
     "gal_mlp_num_params": (C.c_int64, []),
     "gal_mlp_workspace_size": (C.c_int, [C.c_int64, C.POINTER(C.c_size_t)]),
+    "gal_mlp_workspace_error": (C.c_int, [_VP, C.c_int64, C.POINTER(C.c_int32), C.c_void_p]),
     "gal_mlp_forward_f32": (C.c_int, [_VP, _VP, C.c_int64, _VP, _VP, C.c_int32, _VP, C.c_size_t, C.c_void_p]),
     "gal_mlp_loss_grads": (C.c_int, [_VP, _VP, _VP, _VP, _VP, C.c_int64, C.c_float, C.c_float, C.c_int32, _VP,
                                      _VP, _VP, C.c_size_t, C.c_void_p]),

@@ -80,12 +80,18 @@ static cudaError_t team_events(cudaEvent_t* fork, cudaEvent_t* join) {
 // sub-partition (128 threads, one block per SM): their longest orbits then run
 // at their own latency instead of sharing an FP64 pipe. Read and written under
 // g_shape_mu so that a shape is never seen half-set.
-static LaunchShape g_shape[2][2] = {{{0, 0, 0}, {128, 1, 2}}, {{0, 0, 2}, {128, 1, 2}}};
+static LaunchShape g_shape[2][2] = {{{0, 0, 0, 0}, {128, 1, 2, 0}}, {{0, 0, 2, 0}, {128, 1, 2, 0}}};
 static std::mutex g_shape_mu;
+
+// Component tables: 0 = choose one thread or one warp per orbit automatically,
+// 1 / 32 = always that (gal_set_table_lanes).
+static std::atomic<int> g_table_lanes{0};
 
 static LaunchShape launch_shape(int method, int adaptive) {
   std::lock_guard<std::mutex> lock(g_shape_mu);
-  return g_shape[method == 8][adaptive ? 1 : 0];
+  LaunchShape s = g_shape[method == 8][adaptive ? 1 : 0];
+  s.table_lanes = g_table_lanes.load(std::memory_order_relaxed);
+  return s;
 }
 
 gal_status fail(gal_status st, const std::string& msg) {
@@ -536,13 +542,19 @@ gal_status gal_set_team(int32_t blocks) {
   return GAL_OK;
 }
 
+gal_status gal_set_table_lanes(int32_t lanes) {
+  if (lanes != 0 && lanes != 1 && lanes != 32) return fail(GAL_ERR_INVALID_ARGUMENT, "lanes must be 0, 1 or 32");
+  g_table_lanes.store(lanes, std::memory_order_relaxed);
+  return GAL_OK;
+}
+
 gal_status gal_set_launch(int32_t method, int32_t adaptive, int32_t block_threads, int32_t blocks_per_sm,
                           int32_t variant) {
   if ((method != 5 && method != 8) || block_threads < 0 || block_threads > 256 || (block_threads % 32) ||
       blocks_per_sm < 0 || variant < 0 || variant > 2 || (variant != 2 && block_threads > 128))
     return fail(GAL_ERR_INVALID_ARGUMENT, "bad launch shape");
   std::lock_guard<std::mutex> lock(g_shape_mu);
-  g_shape[method == 8][adaptive ? 1 : 0] = LaunchShape{block_threads, blocks_per_sm, variant};
+  g_shape[method == 8][adaptive ? 1 : 0] = LaunchShape{block_threads, blocks_per_sm, variant, 0};
   return GAL_OK;
 }
 

@@ -281,25 +281,41 @@ __device__ __forceinline__ double initial_step(const IntegrateArgs& a, const Pot
 // different SMs and sub-partitions, so the tail they form at the end of a batch
 // does not queue up on a few FP64 pipes. Later positions are dequeued
 // atomically after the gridDim.x * blockDim.x striped ones.
+//
+// With LANES = 32 a whole warp owns one orbit (warp-per-orbit mode, for
+// composites with many components): the positions are handed out per warp,
+// and lane 0 takes the next one from the queue for the warp.
+template <int LANES>
 __device__ __forceinline__ unsigned long long first_position() {
   const unsigned long long W = blockDim.x >> 5, w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if constexpr (LANES == 32) return w * gridDim.x + blockIdx.x;
   return (l * W + w) * gridDim.x + blockIdx.x;
 }
 
+template <int LANES>
+__device__ __forceinline__ unsigned long long next_position(unsigned long long* queue) {
+  if constexpr (LANES == 32) {
+    unsigned long long k = 0;
+    if ((threadIdx.x & 31) == 0) k = atomicAdd(queue, 1ULL);
+    return __shfl_sync(0xffffffffu, k, 0);
+  }
+  return atomicAdd(queue, 1ULL);
+}
+
 // Returns false when the queue is empty.
-template <class TB, class Pot>
+template <class TB, class Pot, int LANES = 1>
 __device__ __forceinline__ bool start_orbit(const IntegrateArgs& a, const Pot& pot, OrbitState& s,
                                             bool& first) {
   const unsigned long long qlen = a.queue_len ? *a.queue_len : (unsigned long long)a.n;
-  const unsigned long long striped = (unsigned long long)gridDim.x * blockDim.x;
+  const unsigned long long striped = (unsigned long long)gridDim.x * (blockDim.x / LANES);
   const unsigned long long base = (unsigned long long)a.queue_base;
   while (true) {
     unsigned long long k;
     if (first) {
       first = false;
-      k = base + first_position();
+      k = base + first_position<LANES>();
     } else {
-      k = base + striped + atomicAdd(a.queue, 1ULL);
+      k = base + striped + next_position<LANES>(a.queue);
     }
     if (k >= qlen) return false;
     const int64_t o = a.order ? (int64_t)a.order[k] : (int64_t)k;
@@ -487,12 +503,16 @@ __device__ __forceinline__ double clip_to_end(double tprev, double tnext, double
   return tnext;
 }
 
-template <class TB, class Pot>
+// LANES = 1: one thread per orbit. LANES = 32: one warp per orbit; Pot must
+// then give every lane of the warp the bitwise-same gradient (WarpTablePot), so
+// the 32 lanes run the orbit's steps in lockstep on identical values and their
+// identical stores of saves, status and steps coincide.
+template <class TB, class Pot, int LANES = 1>
 __device__ void integrate_loop(const IntegrateArgs& a, const Pot& pot) {
   OrbitState s;
   s.orbit = -1;
   bool first = true;
-  if (!start_orbit<TB>(a, pot, s, first)) return;
+  if (!start_orbit<TB, Pot, LANES>(a, pot, s, first)) return;
   double F[TB::S][6];
   while (true) {
     // One RK evaluation per iteration: either the main step from (tau, y) or,
@@ -525,7 +545,7 @@ __device__ void integrate_loop(const IntegrateArgs& a, const Pot& pot) {
       else if (s.tau >= s.tau1) done = true;
       else if (s.nsteps >= a.max_steps) { done = true; st = ORBIT_MAX_STEPS; }
       else if (maybe_park(a, s)) {
-        if (!start_orbit<TB>(a, pot, s, first)) return;
+        if (!start_orbit<TB, Pot, LANES>(a, pot, s, first)) return;
         continue;
       }
     } else {
@@ -595,14 +615,14 @@ __device__ void integrate_loop(const IntegrateArgs& a, const Pot& pot) {
         else if (s.tau >= s.tau1) done = true;
         else if (s.nsteps >= a.max_steps) { done = true; st = ORBIT_MAX_STEPS; }
         else if (maybe_park(a, s)) {
-          if (!start_orbit<TB>(a, pot, s, first)) return;
+          if (!start_orbit<TB, Pot, LANES>(a, pot, s, first)) return;
           continue;
         }
       }
     }
     if (done) {
       finish_orbit(a, s, st);
-      if (!start_orbit<TB>(a, pot, s, first)) return;
+      if (!start_orbit<TB, Pot, LANES>(a, pot, s, first)) return;
     }
   }
 }

@@ -74,9 +74,56 @@ __global__ void __launch_bounds__(kMaxBlock) k_integrate_table(IntegrateArgs a, 
   }
 }
 
+// One warp per orbit (composites with many components): the lanes split the
+// components and every lane ends each gradient with the same sum.
+template <class TB, bool TIMED>
+__global__ void __launch_bounds__(kMaxBlock) k_integrate_table_warp(IntegrateArgs a, const DevComp* comps, int ncomp) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  DevComp* s_comps = reinterpret_cast<DevComp*>(smem_raw);
+  for (int i = threadIdx.x; i < ncomp; i += blockDim.x) s_comps[i] = comps[i];
+  __syncthreads();
+  integrate_loop<TB, WarpTablePot<TIMED>, 32>(a, WarpTablePot<TIMED>{s_comps, ncomp, a.lin});
+}
+
+// Whether a component table runs one warp per orbit: always or never when
+// asked (table_lanes 32 / 1); automatically when the table has many components
+// and the batch is too small to give every SM sub-partition a warp of 32
+// orbits, so that one thread per orbit would leave FP64 pipes idle.
+inline bool use_warp_per_orbit(const LaunchShape& shape, int64_t n, int ncomp) {
+  if (shape.table_lanes == 32) return true;
+  if (shape.table_lanes == 1 || ncomp < kWarpMinComponents) return false;
+  return (n + 31) / 32 < 4LL * device_sm_count();
+}
+
+// Four orbits per block of 128 threads and as many blocks per SM as fit (the
+// launch shapes tuned for one thread per orbit do not apply).
+template <class TB>
+cudaError_t launch_integrate_warp(const IntegrateArgs& a, const DevComp* comps, int ncomp, cudaStream_t stream) {
+  const int block = 128;
+  const size_t smem = sizeof(DevComp) * (size_t)ncomp;
+  auto kernel = a.lin ? k_integrate_table_warp<TB, true> : k_integrate_table_warp<TB, false>;
+  cudaError_t err;
+  if (smem > 48 * 1024) {
+    err = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err != cudaSuccess) return err;
+  }
+  int per_sm = 0;
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem);
+  if (err != cudaSuccess) return err;
+  if (per_sm < 1) per_sm = 1;
+  const int warps = block / 32;
+  int64_t grid = (int64_t)per_sm * device_sm_count();
+  const int64_t need = (a.n + warps - 1) / warps;
+  if (grid > need) grid = need;
+  if (grid < 1) grid = 1;
+  kernel<<<(unsigned)grid, block, smem, stream>>>(a, comps, ncomp);
+  return cudaGetLastError();
+}
+
 template <class TB>
 cudaError_t launch_integrate(const IntegrateArgs& a, bool mw, const MWParams& p, const DevComp* comps, int ncomp,
                              LaunchShape shape, cudaStream_t stream) {
+  if (!mw && use_warp_per_orbit(shape, a.n, ncomp)) return launch_integrate_warp<TB>(a, comps, ncomp, stream);
   const int block = shape.block_threads > 0 ? shape.block_threads : 128;
   if (block > kMaxBlock || block % 32 != 0) return cudaErrorInvalidValue;
   const size_t smem = mw ? 0 : sizeof(DevComp) * (size_t)ncomp;

@@ -11,7 +11,11 @@ struct LaunchShape {
   int block_threads;  // 0 = default
   int blocks_per_sm;  // 0 = occupancy maximum
   int variant;        // Milky Way kernel: 0 = up to 255 registers, 1 = at most 128 (more warps)
+  int table_lanes;    // component tables: 0 = automatic, 1 = one thread per orbit, 32 = one warp per orbit
 };
+
+// Component tables with at least this many components may run one warp per orbit.
+constexpr int kWarpMinComponents = 32;
 
 cudaError_t launch_integrate_dopri5(const IntegrateArgs& a, bool mw, const MWParams& p, const DevComp* comps,
                                     int ncomp, LaunchShape shape, cudaStream_t stream);

@@ -1,4 +1,4 @@
-// Training of the potential-surrogate MLP on the GPU (FP32 CUDA cores).
+// Training of the potential-surrogate MLP on the GPU.
 //
 // One call, gal_mlp_train_step, runs for a batch of B points: the forward pass,
 // the input-gradient (backward) pass, the loss on potential and gradient
@@ -9,12 +9,22 @@
 // the trained network is the one that will be run (gradients pass the rounding
 // straight through). gal_mlp_loss_grads returns the loss and gradient without
 // updating (checked against a NumPy restatement).
+//
+// Every product with 256 output columns and K >= 64 (the 256 x 256 layers of
+// the forward and backward passes, and the weight gradients with K = batch)
+// runs on the tensor cores (tc_gemm.cuh): operands the quantised passes round
+// to bf16 enter as one bf16 part, all others as two (hi + lo), so the
+// gradients keep FP32-level accuracy. The products with 3 or 1 columns or K = 3
+// (first and last layers) stay on a tiled FP32 kernel; elementwise work runs in
+// small grid-stride kernels.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <string>
 
 #include "handle.h"
 #include "mlp.cuh"
+#include "tc_gemm.cuh"
 
 namespace gal {
 namespace mlp {
@@ -201,6 +211,7 @@ __global__ void k_adam(float* p, const float* g, float* m, float* v, int64_t n, 
 
 struct Ws {
   float *Z[5], *Hh[5], *D[5], *U[4], *Zb[5], *Db, *Ub, *Hb, *out, *G, *Pb, *Eb;
+  int* err;  // set by a tensor-core product that gave up waiting (gal_mlp_workspace_error)
 };
 
 static size_t ws_bytes(int64_t B) {
@@ -229,12 +240,69 @@ static Ws carve(void* ws, int64_t B) {
   w.G = take(sizeof(float) * B * 3);
   w.Pb = take(sizeof(float) * B);
   w.Eb = take(sizeof(float) * B * 3);
+  w.err = reinterpret_cast<int*>(take(256));
   return w;
 }
 
+// Tensor-core product C = op(A) op(B) (+ beta C) (+ bias) with op as in
+// gemm() below; split_a / split_b as in tc_gemm.cuh. Returns false when the
+// kernel cannot be configured (then the caller uses the FP32 kernel).
+static bool tc_gemm(cudaStream_t s, bool TA, bool TB, int M, int N, int K, const float* A, int lda, const float* B,
+                    int ldb, float* C, int ldc, float beta, const float* bias, int split_a, int split_b, int* err) {
+  static std::atomic<int> configured[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return false;
+  if (!configured[dev].load()) {
+    if (cudaFuncSetAttribute(tcg::k_tc_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tcg::SMEM_ALLOC) !=
+        cudaSuccess)
+      return false;
+    configured[dev].store(1);
+  }
+  tcg::Args a{};
+  a.M = M;
+  a.N = N;
+  a.K = K;
+  a.A = A;
+  a.sam = TA ? 1 : lda;
+  a.sak = TA ? lda : 1;
+  a.B = B;
+  a.sbn = TB ? ldb : 1;
+  a.sbk = TB ? 1 : ldb;
+  a.C = C;
+  a.ldc = ldc;
+  a.beta = beta;
+  a.bias = bias;
+  a.split_a = split_a;
+  a.split_b = split_b;
+  a.err = err;
+  dim3 grid((N + tcg::BN - 1) / tcg::BN, (M + tcg::BM - 1) / tcg::BM, 1);
+  a.kchunk = ((K + tcg::BK - 1) / tcg::BK) * tcg::BK;
+  // few output tiles and a long K (the weight gradients, K = batch): split K
+  // over enough CTAs to fill the GPU, each adding its partial tile with atomics
+  const int tiles = (int)(grid.x * grid.y);
+  const int sms = device_sm_count();
+  if (!bias && (beta == 0.0f || beta == 1.0f) && (beta == 1.0f || ldc == N) && tiles < sms && K >= 4 * tcg::BK) {
+    int splits = sms / tiles;
+    if (splits > K / (4 * tcg::BK)) splits = K / (4 * tcg::BK);
+    if (splits > 1) {
+      a.kchunk = ((K + splits - 1) / splits + tcg::BK - 1) / tcg::BK * tcg::BK;
+      grid.z = (K + a.kchunk - 1) / a.kchunk;
+      if (beta == 0.0f) cudaMemsetAsync(C, 0, sizeof(float) * (size_t)M * N, s);
+    }
+  }
+  tcg::k_tc_gemm<<<grid, tcg::NTHREADS, tcg::SMEM_ALLOC, s>>>(a);
+  return true;
+}
+
+// Products run on the tensor cores when they have 256 output columns and
+// K >= 64, else on the FP32 kernel. qa / qb: the operand is rounded to bf16
+// (one bf16 part on the tensor cores); otherwise it enters unrounded (two parts).
 template <bool TA, bool TB>
-static void gemm(cudaStream_t s, int M, int N, int K, const float* A, int lda, const float* B, int ldb, float* C,
-                 int ldc, float beta = 0.0f, const float* bias = nullptr, int qa = 0, int qb = 0) {
+static void gemm(cudaStream_t s, int* err, int M, int N, int K, const float* A, int lda, const float* B, int ldb,
+                 float* C, int ldc, float beta = 0.0f, const float* bias = nullptr, int qa = 0, int qb = 0) {
+  if (N == H && K >= tcg::BK &&
+      tc_gemm(s, TA, TB, M, N, K, A, lda, B, ldb, C, ldc, beta, bias, qa ? 0 : 1, qb ? 0 : 1, err))
+    return;
   dim3 grid((N + 63) / 64, (M + 63) / 64);
   // few output tiles and a long K (the weight gradients, K = batch): split K over
   // enough blocks to fill the GPU and accumulate with atomics
@@ -263,24 +331,24 @@ static unsigned ew_grid(int64_t n) {
 static void forward_backward(cudaStream_t s, const float* P, const float* x, int64_t B, const Ws& w, int q) {
   const int64_t n = B * H;
   const int Bi = (int)B;
-  gemm<false, true>(s, Bi, H, 3, x, 3, P + OFF_W1, 3, w.Z[1], H, 0.0f, P + OFF_B1);
+  gemm<false, true>(s, w.err, Bi, H, 3, x, 3, P + OFF_W1, 3, w.Z[1], H, 0.0f, P + OFF_B1);
   k_silu<<<ew_grid(n), 256, 0, s>>>(w.Z[1], w.Hh[1], n, q);
-  gemm<false, true>(s, Bi, H, H, w.Hh[1], H, P + OFF_W2, H, w.Z[2], H, 0.0f, P + OFF_B2, 0, q);
+  gemm<false, true>(s, w.err, Bi, H, H, w.Hh[1], H, P + OFF_W2, H, w.Z[2], H, 0.0f, P + OFF_B2, q, q);
   k_silu<<<ew_grid(n), 256, 0, s>>>(w.Z[2], w.Hh[2], n, q);
-  gemm<false, true>(s, Bi, H, H, w.Hh[2], H, P + OFF_W3, H, w.Z[3], H, 0.0f, P + OFF_B3, 0, q);
+  gemm<false, true>(s, w.err, Bi, H, H, w.Hh[2], H, P + OFF_W3, H, w.Z[3], H, 0.0f, P + OFF_B3, q, q);
   k_silu<<<ew_grid(n), 256, 0, s>>>(w.Z[3], w.Hh[3], n, q);
-  gemm<false, true>(s, Bi, H, H, w.Hh[3], H, P + OFF_W4, H, w.Z[4], H, 0.0f, P + OFF_B4, 0, q);
+  gemm<false, true>(s, w.err, Bi, H, H, w.Hh[3], H, P + OFF_W4, H, w.Z[4], H, 0.0f, P + OFF_B4, q, q);
   k_silu<<<ew_grid(n), 256, 0, s>>>(w.Z[4], w.Hh[4], n, 0);
-  gemm<false, false>(s, Bi, 1, H, w.Hh[4], H, P + OFF_W5, 1, w.out, 1, 0.0f, P + OFF_B5);
+  gemm<false, false>(s, w.err, Bi, 1, H, w.Hh[4], H, P + OFF_W5, 1, w.out, 1, 0.0f, P + OFF_B5);
   // input gradient
   k_d4<<<ew_grid(n), 256, 0, s>>>(w.Z[4], P + OFF_W5, w.D[4], n, q);
-  gemm<false, false>(s, Bi, H, H, w.D[4], H, P + OFF_W4, H, w.U[3], H, 0.0f, nullptr, 0, q);
+  gemm<false, false>(s, w.err, Bi, H, H, w.D[4], H, P + OFF_W4, H, w.U[3], H, 0.0f, nullptr, q, q);
   k_dmul<<<ew_grid(n), 256, 0, s>>>(w.Z[3], w.U[3], w.D[3], n, q, q);
-  gemm<false, false>(s, Bi, H, H, w.D[3], H, P + OFF_W3, H, w.U[2], H, 0.0f, nullptr, 0, q);
+  gemm<false, false>(s, w.err, Bi, H, H, w.D[3], H, P + OFF_W3, H, w.U[2], H, 0.0f, nullptr, q, q);
   k_dmul<<<ew_grid(n), 256, 0, s>>>(w.Z[2], w.U[2], w.D[2], n, q, q);
-  gemm<false, false>(s, Bi, H, H, w.D[2], H, P + OFF_W2, H, w.U[1], H, 0.0f, nullptr, 0, q);
+  gemm<false, false>(s, w.err, Bi, H, H, w.D[2], H, P + OFF_W2, H, w.U[1], H, 0.0f, nullptr, q, q);
   k_dmul<<<ew_grid(n), 256, 0, s>>>(w.Z[1], w.U[1], w.D[1], n, 0, 0);
-  gemm<false, false>(s, Bi, 3, H, w.D[1], H, P + OFF_W1, 3, w.G, 3);
+  gemm<false, false>(s, w.err, Bi, 3, H, w.D[1], H, P + OFF_W1, 3, w.G, 3);
 }
 
 static void loss_grads(cudaStream_t s, const float* P, const float* x, const float* phi_t, const float* g_t,
@@ -292,35 +360,35 @@ static void loss_grads(cudaStream_t s, const float* P, const float* x, const flo
   cudaMemsetAsync(loss, 0, sizeof(float), s);
   k_loss<<<ew_grid(B), 256, 0, s>>>(w.out, w.G, phi_t, g_t, wt, B, alpha, beta, w.Pb, w.Eb, loss);
   // ---- through the input-gradient graph, layer 1 up to 4
-  gemm<true, false>(s, H, 3, Bi, w.D[1], H, w.Eb, 3, grad + OFF_W1, 3);                       // gW1 = D1^T Eb
-  gemm<false, true>(s, Bi, H, 3, w.Eb, 3, P + OFF_W1, 3, w.Db, H);                           // Db1 = Eb W1^T
+  gemm<true, false>(s, w.err, H, 3, Bi, w.D[1], H, w.Eb, 3, grad + OFF_W1, 3);                       // gW1 = D1^T Eb
+  gemm<false, true>(s, w.err, Bi, H, 3, w.Eb, 3, P + OFF_W1, 3, w.Db, H);                           // Db1 = Eb W1^T
   k_dd<<<ew_grid(n), 256, 0, s>>>(w.Z[1], w.U[1], w.Db, w.Ub, w.Zb[1], n, 0);
-  gemm<true, false>(s, H, H, Bi, w.D[2], H, w.Ub, H, grad + OFF_W2, H);                      // gW2 = D2^T Ub1
-  gemm<false, true>(s, Bi, H, H, w.Ub, H, P + OFF_W2, H, w.Db, H, 0.0f, nullptr, 0, q);      // Db2 = Ub1 W2^T
+  gemm<true, false>(s, w.err, H, H, Bi, w.D[2], H, w.Ub, H, grad + OFF_W2, H, 0.0f, nullptr, q, 0);                      // gW2 = D2^T Ub1
+  gemm<false, true>(s, w.err, Bi, H, H, w.Ub, H, P + OFF_W2, H, w.Db, H, 0.0f, nullptr, 0, q);      // Db2 = Ub1 W2^T
   k_dd<<<ew_grid(n), 256, 0, s>>>(w.Z[2], w.U[2], w.Db, w.Ub, w.Zb[2], n, q);
-  gemm<true, false>(s, H, H, Bi, w.D[3], H, w.Ub, H, grad + OFF_W3, H);                      // gW3 = D3^T Ub2
-  gemm<false, true>(s, Bi, H, H, w.Ub, H, P + OFF_W3, H, w.Db, H, 0.0f, nullptr, 0, q);      // Db3 = Ub2 W3^T
+  gemm<true, false>(s, w.err, H, H, Bi, w.D[3], H, w.Ub, H, grad + OFF_W3, H, 0.0f, nullptr, q, 0);                      // gW3 = D3^T Ub2
+  gemm<false, true>(s, w.err, Bi, H, H, w.Ub, H, P + OFF_W3, H, w.Db, H, 0.0f, nullptr, 0, q);      // Db3 = Ub2 W3^T
   k_dd<<<ew_grid(n), 256, 0, s>>>(w.Z[3], w.U[3], w.Db, w.Ub, w.Zb[3], n, q);
-  gemm<true, false>(s, H, H, Bi, w.D[4], H, w.Ub, H, grad + OFF_W4, H);                      // gW4 = D4^T Ub3
-  gemm<false, true>(s, Bi, H, H, w.Ub, H, P + OFF_W4, H, w.Db, H, 0.0f, nullptr, 0, q);      // Db4 = Ub3 W4^T
+  gemm<true, false>(s, w.err, H, H, Bi, w.D[4], H, w.Ub, H, grad + OFF_W4, H, 0.0f, nullptr, q, 0);                      // gW4 = D4^T Ub3
+  gemm<false, true>(s, w.err, Bi, H, H, w.Ub, H, P + OFF_W4, H, w.Db, H, 0.0f, nullptr, 0, q);      // Db4 = Ub3 W4^T
   k_colsum<<<H, 256, 0, s>>>(w.Z[4], w.Db, nullptr, B, H, grad + OFF_W5, 2, 0);              // gw5 = sum silu'(Z4) Db4
   k_zb4<<<ew_grid(n), 256, 0, s>>>(w.Z[4], w.Db, w.Pb, P + OFF_W5, w.Zb[4], n);
   // ---- potential term and the forward graph, layer 4 down to 1
   k_colsum<<<H, 256, 0, s>>>(w.Hh[4], nullptr, w.Pb, B, H, grad + OFF_W5, 1, 1);             // gw5 += H4^T Pb
   k_colsum<<<1, 256, 0, s>>>(w.Pb, nullptr, nullptr, B, 1, grad + OFF_B5, 0, 0);             // gb5
-  gemm<true, false>(s, H, H, Bi, w.Zb[4], H, w.Hh[3], H, grad + OFF_W4, H, 1.0f);            // gW4 += Zb4^T H3
+  gemm<true, false>(s, w.err, H, H, Bi, w.Zb[4], H, w.Hh[3], H, grad + OFF_W4, H, 1.0f, nullptr, 0, q);            // gW4 += Zb4^T H3
   k_colsum<<<H, 256, 0, s>>>(w.Zb[4], nullptr, nullptr, B, H, grad + OFF_B4, 0, 0);
-  gemm<false, false>(s, Bi, H, H, w.Zb[4], H, P + OFF_W4, H, w.Hb, H, 0.0f, nullptr, 0, q);  // Hb3 = Zb4 W4
+  gemm<false, false>(s, w.err, Bi, H, H, w.Zb[4], H, P + OFF_W4, H, w.Hb, H, 0.0f, nullptr, 0, q);  // Hb3 = Zb4 W4
   k_zb_acc<<<ew_grid(n), 256, 0, s>>>(w.Z[3], w.Hb, w.Zb[3], n);
-  gemm<true, false>(s, H, H, Bi, w.Zb[3], H, w.Hh[2], H, grad + OFF_W3, H, 1.0f);
+  gemm<true, false>(s, w.err, H, H, Bi, w.Zb[3], H, w.Hh[2], H, grad + OFF_W3, H, 1.0f, nullptr, 0, q);
   k_colsum<<<H, 256, 0, s>>>(w.Zb[3], nullptr, nullptr, B, H, grad + OFF_B3, 0, 0);
-  gemm<false, false>(s, Bi, H, H, w.Zb[3], H, P + OFF_W3, H, w.Hb, H, 0.0f, nullptr, 0, q);
+  gemm<false, false>(s, w.err, Bi, H, H, w.Zb[3], H, P + OFF_W3, H, w.Hb, H, 0.0f, nullptr, 0, q);
   k_zb_acc<<<ew_grid(n), 256, 0, s>>>(w.Z[2], w.Hb, w.Zb[2], n);
-  gemm<true, false>(s, H, H, Bi, w.Zb[2], H, w.Hh[1], H, grad + OFF_W2, H, 1.0f);
+  gemm<true, false>(s, w.err, H, H, Bi, w.Zb[2], H, w.Hh[1], H, grad + OFF_W2, H, 1.0f, nullptr, 0, q);
   k_colsum<<<H, 256, 0, s>>>(w.Zb[2], nullptr, nullptr, B, H, grad + OFF_B2, 0, 0);
-  gemm<false, false>(s, Bi, H, H, w.Zb[2], H, P + OFF_W2, H, w.Hb, H, 0.0f, nullptr, 0, q);
+  gemm<false, false>(s, w.err, Bi, H, H, w.Zb[2], H, P + OFF_W2, H, w.Hb, H, 0.0f, nullptr, 0, q);
   k_zb_acc<<<ew_grid(n), 256, 0, s>>>(w.Z[1], w.Hb, w.Zb[1], n);
-  gemm<true, false>(s, H, 3, Bi, w.Zb[1], H, x, 3, grad + OFF_W1, 3, 1.0f);                  // gW1 += Zb1^T X
+  gemm<true, false>(s, w.err, H, 3, Bi, w.Zb[1], H, x, 3, grad + OFF_W1, 3, 1.0f);                  // gW1 += Zb1^T X
   k_colsum<<<H, 256, 0, s>>>(w.Zb[1], nullptr, nullptr, B, H, grad + OFF_B1, 0, 0);
 }
 
@@ -333,6 +401,18 @@ using namespace gal::mlp;
 extern "C" {
 
 int64_t gal_mlp_num_params(void) { return NPARAM; }
+
+gal_status gal_mlp_workspace_error(void* workspace, int64_t batch, int32_t* code, gal_stream_t stream) {
+  if (!workspace || !code || batch < 1) return fail(GAL_ERR_INVALID_ARGUMENT, "bad arguments");
+  int* flag = carve(workspace, batch).err;
+  int v = 0;
+  cudaError_t e = cudaMemcpyAsync(&v, flag, sizeof(int), cudaMemcpyDeviceToHost, (cudaStream_t)stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(flag, 0, sizeof(int), (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "reading the training error flag");
+  *code = v;
+  return GAL_OK;
+}
 
 gal_status gal_mlp_workspace_size(int64_t batch, size_t* bytes) {
   if (!bytes || batch < 1) return fail(GAL_ERR_INVALID_ARGUMENT, "batch >= 1 required");

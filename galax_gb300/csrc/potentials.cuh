@@ -438,6 +438,39 @@ struct TimedTablePot {
   }
 };
 
+// A table evaluated by a whole warp for one orbit (integrate_loop with
+// LANES = 32, for composites with many components): lane l sums components
+// l, l + 32, ..., then a butterfly of xor-shuffles gives every lane the total.
+// At each level a lane adds its partner's partial sum to its own while the
+// partner adds the same two numbers in the other order; IEEE addition is
+// commutative, so both get the same bits, and after five levels all 32 lanes
+// hold bitwise-identical sums. Every lane of the warp must call it.
+template <bool TIMED>
+struct WarpTablePot {
+  const DevComp* c;
+  int n;
+  const DevLinear* lin;  // TIMED: time-dependent parameters
+  __device__ __forceinline__ void grad_t(double t, double x, double y, double z, double& gx, double& gy,
+                                         double& gz) const {
+    double ax = 0.0, ay = 0.0, az = 0.0;
+    for (int i = threadIdx.x & 31; i < n; i += 32) {
+      if constexpr (TIMED)
+        comp_grad(comp_at_time(c[i], lin[i], t), x, y, z, ax, ay, az);
+      else
+        comp_grad(c[i], x, y, z, ax, ay, az);
+    }
+#pragma unroll
+    for (int m = 16; m >= 1; m >>= 1) {
+      ax += __shfl_xor_sync(0xffffffffu, ax, m);
+      ay += __shfl_xor_sync(0xffffffffu, ay, m);
+      az += __shfl_xor_sync(0xffffffffu, az, m);
+    }
+    gx = ax;
+    gy = ay;
+    gz = az;
+  }
+};
+
 // Gradient of any potential model at time t: static models ignore t.
 template <class Pot>
 __device__ __forceinline__ void pot_grad_t(const Pot& p, double, double x, double y, double z, double& gx,
@@ -445,6 +478,11 @@ __device__ __forceinline__ void pot_grad_t(const Pot& p, double, double x, doubl
   p.grad(x, y, z, gx, gy, gz);
 }
 __device__ __forceinline__ void pot_grad_t(const TimedTablePot& p, double t, double x, double y, double z,
+                                           double& gx, double& gy, double& gz) {
+  p.grad_t(t, x, y, z, gx, gy, gz);
+}
+template <bool TIMED>
+__device__ __forceinline__ void pot_grad_t(const WarpTablePot<TIMED>& p, double t, double x, double y, double z,
                                            double& gx, double& gy, double& gz) {
   p.grad_t(t, x, y, z, gx, gy, gz);
 }

@@ -1,0 +1,213 @@
+// Tensor-core GEMM for the surrogate's training products (tcgen05.mma,
+// kind::f16: bf16 operands, f32 accumulation in TMEM):
+//
+//   C[m][n] = sum_k A(m, k) B(n, k) (+ beta C[m][n]) (+ bias[n])
+//
+// with A(m, k) = A[m sam + k sak] and B(n, k) = B[n sbn + k sbk] read from FP32
+// arrays of any layout (row- or column-major), so the transposed products of
+// backpropagation need no transposes in memory. Every operand block is rounded
+// to bf16 on its way into shared memory; an operand may instead be split into
+// two bf16 parts, v = hi + lo with hi = bf16(v), lo = bf16(v - hi), and the
+// product formed as hi*hi + hi*lo + lo*hi (the bf16x3 scheme of Henry, Tang &
+// Heinecke, "Leveraging the bfloat16 artificial intelligence datatype for
+// higher-precision computations", ARITH 2019), which carries ~16 significant
+// bits per operand: the FP32 reference gradients of the loss need that, the
+// quantised forward pass does not.
+//
+// One CTA of 128 threads computes a 128 x 256 tile of C; K runs in blocks of 64
+// through two shared-memory stages (96 KB each: A hi/lo 128 x 64, B hi/lo
+// 256 x 64, K-major, 128-byte swizzle, the layout of the inference kernel's
+// operands). All threads load and convert; thread 0 issues the products and
+// commits them to the stage's mbarrier, which frees the stage for the block
+// after next. The accumulator (256 TMEM columns) drains through shared memory
+// so that C is read and written row-contiguously. With gridDim.z > 1 each z
+// takes a K range and adds its partial tile into C with atomics.
+//
+// Every mbarrier wait is bounded; on timeout the kernel records an error code,
+// waits (bounded) for its products, releases TMEM and returns.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "tc.cuh"
+
+namespace gal {
+namespace tcg {
+
+constexpr int BM = 128, BN = 256, BK = 64;
+constexpr int NTHREADS = 128;
+constexpr uint32_t A_BLK = BM * 128;  // 16 KB: 128 rows x 64 bf16
+constexpr uint32_t B_BLK = BN * 128;  // 32 KB
+constexpr uint32_t STAGE_BYTES = 2 * A_BLK + 2 * B_BLK;  // hi and lo of both
+constexpr uint32_t SMEM_BAR = 2 * STAGE_BYTES;            // 192 KB
+constexpr uint32_t SMEM_ALLOC = SMEM_BAR + 64 + 1024;     // barriers, TMEM address, alignment slack
+constexpr int OUT_STRIDE = BN + 1;                        // floats per staged output row (no bank conflicts)
+constexpr uint32_t WAIT_LIMIT = 1u << 24;
+static_assert(SMEM_ALLOC <= 227 * 1024, "shared memory budget");
+static_assert((uint32_t)BM * OUT_STRIDE * 4 <= SMEM_BAR, "output staging fits in the operand stages");
+
+struct Args {
+  int M, N, K;
+  const float* A;
+  int64_t sam, sak;
+  const float* B;
+  int64_t sbn, sbk;
+  float* C;
+  int64_t ldc;
+  float beta;
+  const float* bias;
+  int split_a, split_b;
+  int kchunk;  // K per blockIdx.z, a multiple of BK
+  int* err;
+};
+
+__device__ __forceinline__ uint16_t bf16_bits(float f) {
+  uint32_t r;
+  asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(0.0f), "f"(f));
+  return (uint16_t)(r & 0xffffu);
+}
+
+// Load rows [r0, r0+R) x k [k0, k0+64) of an operand into the hi (and lo)
+// images of one stage. Consecutive threads take consecutive 8-element chunks
+// along the contiguous dimension of the source, so global reads coalesce.
+template <int R>
+__device__ __forceinline__ void load_block(uint8_t* hi, uint8_t* lo, const float* src, int64_t s_row, int64_t s_k,
+                                           int r0, int rlim, int k0, int klim, int split) {
+  const bool kmajor = s_k == 1;
+  for (int i = threadIdx.x; i < R * 8; i += NTHREADS) {
+    const int row = kmajor ? (i >> 3) : (i % R);
+    const int c = kmajor ? (i & 7) : (i / R);
+    const int gr = r0 + row, k = k0 + 8 * c;
+    float v[8];
+    if (kmajor && gr < rlim && k + 8 <= klim && ((reinterpret_cast<uintptr_t>(src + gr * s_row + k) & 15) == 0)) {
+      const float4 a = *reinterpret_cast<const float4*>(src + gr * s_row + k);
+      const float4 b = *reinterpret_cast<const float4*>(src + gr * s_row + k + 4);
+      v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+    } else {
+#pragma unroll
+      for (int j = 0; j < 8; ++j) v[j] = (gr < rlim && k + j < klim) ? src[gr * s_row + (int64_t)(k + j) * s_k] : 0.0f;
+    }
+    uint32_t h[4], l[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const uint16_t h0 = bf16_bits(v[2 * j]), h1 = bf16_bits(v[2 * j + 1]);
+      h[j] = (uint32_t)h0 | ((uint32_t)h1 << 16);
+      if (split) {
+        const uint16_t l0 = bf16_bits(v[2 * j] - __uint_as_float((uint32_t)h0 << 16));
+        const uint16_t l1 = bf16_bits(v[2 * j + 1] - __uint_as_float((uint32_t)h1 << 16));
+        l[j] = (uint32_t)l0 | ((uint32_t)l1 << 16);
+      }
+    }
+    const uint32_t off = tc::sw128_offset(R, row, 8 * c);
+    *reinterpret_cast<uint4*>(hi + off) = make_uint4(h[0], h[1], h[2], h[3]);
+    if (split) *reinterpret_cast<uint4*>(lo + off) = make_uint4(l[0], l[1], l[2], l[3]);
+  }
+}
+
+__global__ void __launch_bounds__(NTHREADS, 1) k_tc_gemm(Args a) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = smem_raw + ((1024 - (tc::smem_u32(smem_raw) & 1023)) & 1023);
+  uint64_t* done = reinterpret_cast<uint64_t*>(smem + SMEM_BAR);  // [2] stage free again
+  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(done + 2);
+  __shared__ int fail_s;
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  const int kbeg = blockIdx.z * a.kchunk;
+  const int kend = min(a.K, kbeg + a.kchunk);
+  const int nk = kend > kbeg ? (kend - kbeg + BK - 1) / BK : 0;
+  if (t == 0) {
+    fail_s = 0;
+    tc::mbar_init(&done[0], 1);
+    tc::mbar_init(&done[1], 1);
+    tc::fence_barrier_init();
+  }
+  if (warp == 0) {
+    tc::tmem_alloc(tmem_holder, BN);
+    tc::tmem_relinquish();
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t tmem = *tmem_holder;
+  constexpr uint32_t idesc = tc::idesc_bf16(BM, BN);
+  int committed = 0;  // k blocks whose products were issued (the same count in every thread)
+  for (int kb = 0; kb < nk; ++kb) {
+    const int s = kb & 1;
+    uint8_t* st = smem + s * STAGE_BYTES;
+    if (kb >= 2 && !tc::mbar_wait(&done[s], (uint32_t)((kb / 2 - 1) & 1), WAIT_LIMIT)) fail_s = 1;
+    __syncthreads();
+    if (fail_s) break;
+    const int k0 = kbeg + kb * BK;
+    load_block<BM>(st, st + A_BLK, a.A, a.sam, a.sak, m0, a.M, k0, kend, a.split_a);
+    load_block<BN>(st + 2 * A_BLK, st + 2 * A_BLK + B_BLK, a.B, a.sbn, a.sbk, n0, a.N, k0, kend, a.split_b);
+    tc::fence_proxy_async_smem();
+    __syncthreads();
+    if (t == 0) {
+      tc::tc_fence_after();
+      const uint32_t ah = tc::smem_u32(st), al = ah + A_BLK, bh = ah + 2 * A_BLK, bl = bh + B_BLK;
+#pragma unroll
+      for (int ks = 0; ks < 4; ++ks) {
+        tc::mma_bf16(tmem, tc::desc_sw128(ah + ks * 32), tc::desc_sw128(bh + ks * 32), idesc, (kb | ks) != 0);
+        if (a.split_b) tc::mma_bf16(tmem, tc::desc_sw128(ah + ks * 32), tc::desc_sw128(bl + ks * 32), idesc, 1);
+        if (a.split_a) tc::mma_bf16(tmem, tc::desc_sw128(al + ks * 32), tc::desc_sw128(bh + ks * 32), idesc, 1);
+      }
+      tc::mma_commit(&done[s]);
+    }
+    committed = kb + 1;
+  }
+  // the last commit arrives once every product issued by this CTA has completed
+  if (committed > 0) {
+    const int last = committed - 1;
+    if (!tc::mbar_wait(&done[last & 1], (uint32_t)((last / 2) & 1), WAIT_LIMIT)) fail_s = 1;
+  }
+  tc::tc_fence_after();
+  __syncthreads();
+  const bool ok = !fail_s;  // the same in every thread after the barrier
+  if (!ok) {
+    if (t == 0 && a.err) atomicExch(a.err, 1);
+  } else {
+    // TMEM -> shared memory (row m = TMEM lane m), then coalesced rows into C
+    float* out = reinterpret_cast<float*>(smem);
+    const int row = warp * 32 + lane;
+    const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+    for (int c = 0; c < BN; c += 32) {
+      uint32_t r[32];
+      if (committed > 0) {
+        tc::tmem_ld32(tmem + lane_base + (uint32_t)c, r);
+        tc::tmem_wait_ld();
+      } else {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) r[j] = 0u;
+      }
+#pragma unroll
+      for (int j = 0; j < 32; ++j) out[row * OUT_STRIDE + c + j] = __uint_as_float(r[j]);
+    }
+    __syncthreads();
+    const bool atomic = gridDim.z > 1;
+    for (int rr = warp; rr < BM; rr += NTHREADS / 32) {
+      const int m = m0 + rr;
+      if (m >= a.M) break;
+      for (int c = lane; c < BN; c += 32) {
+        const int n = n0 + c;
+        if (n >= a.N) break;
+        float v = out[rr * OUT_STRIDE + c];
+        float* dst = a.C + (int64_t)m * a.ldc + n;
+        if (atomic) {
+          atomicAdd(dst, v);
+          continue;
+        }
+        if (a.beta != 0.0f) v = fmaf(a.beta, *dst, v);
+        if (a.bias) v += a.bias[n];
+        *dst = v;
+      }
+    }
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, BN);
+}
+
+}  // namespace tcg
+}  // namespace gal

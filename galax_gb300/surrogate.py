@@ -142,10 +142,11 @@ class MLPSurrogate:
         L = _lib.load()
         nb = C.c_size_t()
         _lib.check(L.gal_mlp_workspace_size(B, C.byref(nb)), "gal_mlp_workspace_size")
-        ws = torch.empty(nb.value, dtype=torch.uint8, device="cuda")
+        ws = torch.zeros(nb.value, dtype=torch.uint8, device="cuda")
         st = torch.cuda.current_stream().cuda_stream
         _lib.check(L.gal_mlp_forward_f32(P.data_ptr(), U.data_ptr(), B, phi.data_ptr(), g.data_ptr(), int(quantize),
                                          ws.data_ptr(), ws.numel(), st), "gal_mlp_forward_f32")
+        _check_ws(L, ws, B, st)
         return phi, g
 
 
@@ -163,13 +164,21 @@ def loss_grads(params, u, phi_t, g_t, alpha: float, beta: float, *, quantize: bo
     L = _lib.load()
     nb = C.c_size_t()
     _lib.check(L.gal_mlp_workspace_size(B, C.byref(nb)), "gal_mlp_workspace_size")
-    ws = torch.empty(nb.value, dtype=torch.uint8, device="cuda")
+    ws = torch.zeros(nb.value, dtype=torch.uint8, device="cuda")
     st = torch.cuda.current_stream().cuda_stream
     _lib.check(L.gal_mlp_loss_grads(P.data_ptr(), U.data_ptr(), pt.data_ptr(), gt.data_ptr(),
                                     wt.data_ptr() if wt is not None else None, B, alpha, beta, int(quantize),
                                     grad.data_ptr(), loss.data_ptr(), ws.data_ptr(), ws.numel(), st),
                "gal_mlp_loss_grads")
+    _check_ws(L, ws, B, st)
     return float(loss), grad.cpu().numpy()
+
+
+def _check_ws(L, ws, batch: int, stream) -> None:
+    code = C.c_int32()
+    _lib.check(L.gal_mlp_workspace_error(ws.data_ptr(), batch, C.byref(code), stream), "gal_mlp_workspace_error")
+    if code.value:
+        raise _lib.GalaxGB300Error(f"MLP training kernels: a tensor-core product gave up waiting (code {code.value})")
 
 
 def train(x, phi, grad, *, length_scale: float, epochs: int = 30, batch: int = 8192, lr: float = 2e-3,
@@ -210,7 +219,7 @@ def train(x, phi, grad, *, length_scale: float, epochs: int = 30, batch: int = 8
     L = _lib.load()
     nb = C.c_size_t()
     _lib.check(L.gal_mlp_workspace_size(batch, C.byref(nb)), "gal_mlp_workspace_size")
-    ws = torch.empty(nb.value, dtype=torch.uint8, device="cuda")
+    ws = torch.zeros(nb.value, dtype=torch.uint8, device="cuda")  # zeroed: it holds the error flag
     st = torch.cuda.current_stream().cuda_stream
     gen = torch.Generator(device="cuda").manual_seed(seed)
     steps_per_epoch = n // batch
@@ -236,7 +245,10 @@ def train(x, phi, grad, *, length_scale: float, epochs: int = 30, batch: int = 8
         rep.loss.append(float(ep_loss) / steps_per_epoch)
         if log_every and (ep + 1) % log_every == 0:
             print(f"epoch {ep + 1}: loss {rep.loss[-1]:.4e}", flush=True)
-    torch.cuda.synchronize()
+    code = C.c_int32()
+    _lib.check(L.gal_mlp_workspace_error(ws.data_ptr(), batch, C.byref(code), st), "gal_mlp_workspace_error")
+    if code.value:
+        raise _lib.GalaxGB300Error(f"MLP training: a tensor-core product gave up waiting (code {code.value})")
     rep.seconds = time.perf_counter() - t0
     return MLPSurrogate(P.cpu().numpy(), length_scale, phi_scale), rep
 

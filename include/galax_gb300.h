@@ -253,6 +253,16 @@ GAL_API gal_status gal_set_launch(int32_t method, int32_t adaptive, int32_t bloc
  * gal_set_launch. Results are bitwise identical either way; the teams cut the
  * serial latency of the longest orbits. Process-wide. */
 GAL_API gal_status gal_set_team(int32_t blocks);
+/* Orbits per thread or warp for component tables (composites other than the
+ * specialised Milky Way kernel) in gal_integrate: 1 runs one thread per orbit;
+ * 32 runs one warp per orbit, its lanes splitting the components and reducing
+ * the gradient with warp shuffles; 0 (default) takes a warp per orbit when the
+ * table has at least 32 components and the batch is too small to give every
+ * SM sub-partition a warp of 32 orbits (fewer than 128 orbits per SM).
+ * The two differ only in the order of the component sum (rounding).
+ * Process-wide. galax evaluates a composite by summing its components
+ * (src/galax/potential/_src/base_multi.py:48-55). */
+GAL_API gal_status gal_set_table_lanes(int32_t lanes);
 
 /* ------------------------------------------------------------------ adjoint */
 /* Scratch bytes gal_adjoint needs for n orbits with checkpoints every k_ckpt steps. */
@@ -379,8 +389,16 @@ GAL_API gal_status gal_stream_df_sample(const gal_potential* pot, int32_t df, co
  * b4, w5[256], b5 (W rows are output units). */
 typedef struct gal_mlp gal_mlp; /* opaque, device-resident inference weights */
 GAL_API int64_t gal_mlp_num_params(void);
-/* Training-side scratch for a batch of `batch` points. */
+/* Training-side scratch for a batch of `batch` points. The 256 x 256 products
+ * of the calls below run on the tensor cores (bf16 operands, FP32
+ * accumulation); operands that the quantised passes do not round to bf16
+ * enter as two bf16 parts (hi + lo), which keeps FP32-level accuracy. Zero a
+ * new workspace before its first use: it holds a sticky error flag. */
 GAL_API gal_status gal_mlp_workspace_size(int64_t batch, size_t* bytes);
+/* The error flag of a training workspace (0 = none; non-zero = a tensor-core
+ * product gave up waiting, so results since the last check are not valid);
+ * synchronises `stream`, then clears the flag. */
+GAL_API gal_status gal_mlp_workspace_error(void* workspace, int64_t batch, int32_t* code, gal_stream_t stream);
 /* FP32 forward and input gradient of `batch` points u[batch][3] (network units):
  * phi[batch] = out(u), grad[batch][3] = grad_u out. quantize = 1 rounds weights
  * and the activations entering the 256x256 products to bfloat16, as inference does. */

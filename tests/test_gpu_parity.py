@@ -235,6 +235,73 @@ def test_fixed_step_general_table_matches_oracle(gx):
     assert _rel(orb.w.reshape(-1, 6), np.stack(ref).reshape(-1, 6)) < 1e-9
 
 
+def _table_lanes(lanes):
+    from galax_gb300 import _lib
+
+    _lib.check(_lib.load().gal_set_table_lanes(lanes), "gal_set_table_lanes")
+
+
+@pytest.mark.parametrize("method,adaptive", [(8, False), (5, True), (8, True)])
+def test_warp_per_orbit_composite_matches_oracle(gx, method, adaptive):
+    """One warp per orbit for a composite with many components (the Milky Way
+    plus 512 Plummer subhalos): chosen automatically for a small batch, forced
+    on and off; against the oracle, and the two modes against each other (they
+    differ only in the order of the component sum)."""
+    from galax_gb300.dynamics import integrate
+
+    comps = _subhalos()
+    pot = _pot(gx, comps)
+    y0 = _ics(300, 23)
+    ts = np.linspace(0.0, 200.0, 21)
+    ctrl = gx.PIDController(rtol=1e-8, atol=1e-10) if adaptive else gx.ConstantStepSize()
+    cfg = gx.Integrator(solver=gx.Dopri8() if method == 8 else gx.Dopri5(), stepsize_controller=ctrl,
+                        dt0=None if adaptive else 0.5, max_steps=2**16).config()
+    ocfg = (O.solver_cfg(method, True, rtol=1e-8, atol=1e-10, max_steps=2**16) if adaptive
+            else O.solver_cfg(method, False, dt0=0.5))
+    ref, rst, acc, _ = O.integrate(comps, y0, 0.0, 200.0, ts, ocfg)
+    want = np.stack(ref).reshape(-1, 6)
+    got = {}
+    try:
+        for lanes in (0, 32, 1):
+            _table_lanes(lanes)
+            out, st, steps = integrate(pot, y0, 0.0, 200.0, ts, cfg)
+            assert np.all(st.cpu().numpy() == 0)
+            got[lanes] = (out.permute(2, 1, 0).cpu().numpy().reshape(-1, 6), steps.cpu().numpy())
+    finally:
+        _table_lanes(0)
+    np.testing.assert_array_equal(got[0][0], got[32][0])  # 300 orbits: the automatic choice is a warp each
+    for lanes in (32, 1):
+        rel = _rel_each(got[lanes][0], want)
+        if adaptive:
+            assert rel.max() <= 10 * 1e-8 and np.median(rel) < 1e-11
+            assert np.mean(got[lanes][1] == acc) > 0.95
+        else:
+            assert rel.max() < 1e-9
+    assert _rel(got[32][0], got[1][0]) < (1e-7 if adaptive else 1e-11)
+
+
+def test_warp_per_orbit_time_dependent_composite(gx):
+    """The warp-per-orbit kernel with LinearParameter slopes, against the oracle."""
+    from galax_gb300.dynamics import integrate
+    from galax_gb300.potential import from_component_array
+
+    comps = _subhalos(n=60, seed=8)
+    sl = np.zeros((len(comps), 3))
+    sl[0, 0] = -2e7
+    sl[4:, 0] = -1e3 * comps["m"][4:] / 1e6  # subhalos losing mass
+    y0 = _ics(128, 29)
+    ts = np.linspace(0.0, 300.0, 16)
+    cfg = gx.Integrator(solver=gx.Dopri8(), stepsize_controller=gx.ConstantStepSize(), dt0=1.0).config()
+    try:
+        _table_lanes(32)
+        out, st, _ = integrate(from_component_array(comps, slopes=sl), y0, 0.0, 300.0, ts, cfg)
+    finally:
+        _table_lanes(0)
+    ref, rst, _, _ = O.integrate(comps, y0, 0.0, 300.0, ts, O.solver_cfg(8, False, dt0=1.0), slopes=sl)
+    assert np.all(st.cpu().numpy() == 0)
+    assert _rel(out.permute(2, 1, 0).cpu().numpy().reshape(-1, 6), np.stack(ref).reshape(-1, 6)) < 1e-9
+
+
 # ------------------------------------------------------------------ adaptive
 @pytest.mark.parametrize("method,rtol,atol", [(8, 1e-7, 1e-7), (5, 1e-8, 1e-10)])
 def test_adaptive_matches_oracle(gx, method, rtol, atol):

@@ -349,6 +349,7 @@ def parity_at_full_size(b, sample, out_gpu, status_gpu, acc_gpu, rtol: float = 1
     per_orbit = np.maximum.reduceat(err, starts) if len(err) else np.zeros(0)
     same = acc_gpu[idx] == acc_o
     worst = int(np.argmax(per_orbit))
+    sensitivity = _sensitivity(b, idx, per_orbit, saves_o, starts, lens, 10 * rtol)
     return {
         "orbits_compared": int(len(idx)), "saves_compared": int(len(g)),
         "max_rel": float(per_orbit.max()), "median_rel": float(np.median(per_orbit)),
@@ -361,8 +362,52 @@ def parity_at_full_size(b, sample, out_gpu, status_gpu, acc_gpu, rtol: float = 1
         "longest_orbit_compared": {"accepted_steps": int(acc_o.max()),
                                    "rel": float(per_orbit[int(np.argmax(acc_o))])},
         "orbits_over_40k_steps": int(np.sum(acc_o > 40_000)),
+        "sensitivity_control": sensitivity,
         "note": "oracle = C++ FP64 restatement (per-orbit PID controllers); GPU saves from the end-to-end run; "
                 "identical_step_sequences = equal accepted-step counts; tolerance 10 x rtol = 1e-7",
+    }
+
+
+def _sensitivity(b, idx, per_orbit, saves_o, starts, lens, tol, n_control: int = 2000) -> dict:
+    """Whether the orbits beyond tolerance are ones whose saves the oracle itself
+    cannot pin: each is integrated again on the oracle from its initial state
+    with every coordinate moved by one unit in the last place (a relative
+    2**-52), and compared with the oracle's unperturbed run. An orbit whose
+    saves move by more than the tolerance under that perturbation amplifies
+    rounding (chaotic, or close encounters with the nucleus), so no FP64
+    implementation with a different rounding sequence can match it to the
+    tolerance. A random sample of the orbits within tolerance is the control."""
+    from oracle import oracle as O
+
+    cfg = O.solver_cfg(5, True, rtol=1e-8, atol=1e-10, max_steps=2**16)
+    bad = np.nonzero(per_orbit > tol)[0]
+    good = np.nonzero(per_orbit <= tol)[0]
+    rng = np.random.default_rng(7)
+    ctrl = rng.choice(good, min(n_control, len(good)), replace=False) if len(good) else good
+
+    def moved(sel):
+        if len(sel) == 0:
+            return np.zeros(0)
+        o = idx[sel]
+        y0 = b.y0[o] * (1.0 + 2.0**-52)
+        grids = [b.save_ts[b.save_offsets[i]:b.save_offsets[i + 1]] for i in o]
+        sv, *_ = O.integrate(O.milky_way(), y0, b.t0[o], b.t1[o], grids, cfg, nthreads=os.cpu_count() or 1,
+                             flat=True)
+        ref = np.concatenate([saves_o[starts[j]:starts[j] + lens[j]] for j in sel])
+        err = np.zeros(len(ref))
+        for sl in (slice(0, 3), slice(3, 6)):
+            d = np.linalg.norm(sv[:, sl] - ref[:, sl], axis=1)
+            err = np.maximum(err, d / np.maximum(np.linalg.norm(ref[:, sl], axis=1), 1e-300))
+        st = np.concatenate([[0], np.cumsum(lens[sel])[:-1]])
+        return np.maximum.reduceat(err, st)
+
+    mb, mc = moved(bad), moved(ctrl)
+    return {
+        "orbits_beyond_tolerance": int(len(bad)),
+        "of_which_oracle_moves_beyond_tolerance_under_1ulp": float(np.mean(mb > tol)) if len(mb) else None,
+        "median_oracle_1ulp_divergence_of_those": float(np.median(mb)) if len(mb) else None,
+        "control_orbits": int(len(ctrl)),
+        "control_oracle_moves_beyond_tolerance_under_1ulp": float(np.mean(mc > tol)) if len(mc) else None,
     }
 
 

@@ -84,6 +84,7 @@ SIGNATURES = {
     "gal_potential_update": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]),
     "gal_potential_num_components": (C.c_int32, [C.c_void_p]),
     "gal_potential_is_milky_way": (C.c_int32, [C.c_void_p]),
+    "gal_potential_is_time_dependent": (C.c_int32, [C.c_void_p]),
     "gal_eval_potential": (C.c_int, [C.c_void_p, _DP, C.c_double, C.c_int64, _DP, C.c_void_p]),
     "gal_eval_gradient": (C.c_int, [C.c_void_p, _DP, C.c_double, C.c_int64, _DP, C.c_void_p]),
     "gal_eval_acceleration": (C.c_int, [C.c_void_p, _DP, C.c_double, C.c_int64, _DP, C.c_void_p]),

@@ -10,8 +10,10 @@ Two entry points:
   optimisers.
 
 Parameters are the component table's (m, l1, l2) per component, in the order
-of ``pot.components()``. galax differentiates through diffrax instead
-(ForwardMode by default, src/galax/dynamics/_src/orbit/solver.py:133).
+of ``pot.components()``; for a potential with LinearParameter slopes they are
+(m, l1, l2) at t = 0 followed by the three slopes, six per component, and
+every stage is evaluated at its own time. galax differentiates through diffrax
+instead (ForwardMode by default, src/galax/dynamics/_src/orbit/solver.py:133).
 """
 
 from __future__ import annotations
@@ -23,7 +25,7 @@ import numpy as np
 
 from . import _lib
 from .dynamics import Workspace, _as_cuda, on_stream
-from .potential import AbstractPotential, from_component_array
+from .potential import AbstractPotential, CompositePotential, from_component_array
 
 
 def _torch():
@@ -36,7 +38,7 @@ def _torch():
 class AdjointResult:
     yT: object          # (n, 6)
     grad_y0: object     # (n, 6)
-    grad_params: object  # (ncomp, 3): d/d(m, l1, l2)
+    grad_params: object  # (ncomp, 3): d/d(m, l1, l2); (ncomp, 6) with d/d(slopes) for time-dependent potentials
     loss: float | None
 
 
@@ -59,7 +61,7 @@ def _run(pot, y0_soa, t0, t1, dt, method, k_ckpt, lam_soa=None, target_soa=None,
     yT = torch.empty((6, n), dtype=torch.float64, device="cuda")
     gy = torch.empty((6, n), dtype=torch.float64, device="cuda")
     ncomp = len(pot.components())
-    gp = torch.empty((ncomp, 3), dtype=torch.float64, device="cuda")
+    gp = torch.empty((ncomp, 6 if L.gal_potential_is_time_dependent(h) else 3), dtype=torch.float64, device="cuda")
     st = torch.cuda.current_stream().cuda_stream
     _lib.check(
         L.gal_adjoint(
@@ -100,7 +102,9 @@ def orbit_adjoint(pot: AbstractPotential, y0, t0: float, t1: float, *, dt: float
 
 
 class OrbitMap:
-    """y(t1) = Phi(y0; params) as a differentiable torch op (constant step)."""
+    """y(t1) = Phi(y0; params) as a differentiable torch op (constant step).
+    ``params`` is ``params_of(pot)``: (ncomp, 3), or (ncomp, 6) with the
+    LinearParameter slopes of a time-dependent potential."""
 
     @staticmethod
     def apply(pot: AbstractPotential, y0, params, t0: float, t1: float, dt: float, method: int = 8,
@@ -133,16 +137,37 @@ class OrbitMap:
 
 
 def _with_params(pot: AbstractPotential, params) -> AbstractPotential:
-    """A potential with the same component kinds and origins but parameters ``params`` (ncomp, 3)."""
+    """A potential with the same component kinds and origins but parameters
+    ``params``: (ncomp, 3) values, or (ncomp, 6) values at t = 0 and slopes."""
     arr = pot.component_array().copy()
     p = params.detach().cpu().numpy() if hasattr(params, "detach") else np.asarray(params)
-    p = p.reshape(len(arr), 3)
+    p = p.reshape(len(arr), -1)
     arr["m"], arr["l1"], arr["l2"] = p[:, 0], p[:, 1], p[:, 2]
-    return from_component_array(arr, G=pot.G)
+    if p.shape[1] != 6:
+        return from_component_array(arr, G=pot.G)
+    return _WithSlopes(from_component_array(arr, G=pot.G, slopes=p[:, 3:6]), p[:, 3:6])
+
+
+class _WithSlopes(CompositePotential):
+    """A component table with explicit LinearParameter slopes, kept even when
+    they are all zero, so that the adjoint differentiates with respect to them."""
+
+    def __init__(self, table: AbstractPotential, slopes):
+        super().__init__({"table": table}, constants=table.constants)
+        self._sl = np.ascontiguousarray(slopes, np.float64).reshape(-1, 3)
+
+    def slopes(self):
+        return self._sl
 
 
 def params_of(pot: AbstractPotential):
-    """The (ncomp, 3) parameter tensor (m, l1, l2) of ``pot`` on the GPU."""
+    """The parameter tensor of ``pot`` on the GPU: (ncomp, 3) = (m, l1, l2), or
+    (ncomp, 6) = (m, l1, l2) at t = 0 and their slopes when ``pot`` has
+    LinearParameter time dependence."""
     torch = _torch()
     arr = pot.component_array()
-    return torch.tensor(np.stack([arr["m"], arr["l1"], arr["l2"]], axis=1), dtype=torch.float64, device="cuda")
+    vals = np.stack([arr["m"], arr["l1"], arr["l2"]], axis=1)
+    sl = pot.slopes()
+    if sl is not None:
+        vals = np.concatenate([vals, np.asarray(sl, np.float64).reshape(len(arr), 3)], axis=1)
+    return torch.tensor(vals, dtype=torch.float64, device="cuda")

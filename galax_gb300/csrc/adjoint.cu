@@ -17,6 +17,12 @@
 // states from its checkpoint into scratch and sweeping the stages in reverse.
 // Per-orbit parameter gradients go to scratch and are summed over orbits by a
 // fixed-order reduction, so results are bitwise reproducible.
+//
+// Time-dependent potentials (galax's LinearParameter,
+// src/galax/potential/_src/params/core.py:25-110): every stage runs at its own
+// time t_i, with each component's (m, l1, l2) = values at t = 0 + slopes t_i.
+// Their parameter cotangent at t_i, dL/dp(t_i), adds to dL/dp(0) and, times
+// t_i, to dL/d(slope).
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -37,16 +43,22 @@ struct AdjointArgs {
   const double* ts;      // [N+1] time grid (same for every orbit); ts[k+1] - ts[k] is the signed step
   double* ckpt;          // [nseg][6][n]
   double* seg;           // [K][6][n]
-  double* gp_orbit;      // [ncomp*3][n]
+  double* gp_orbit;      // [ncomp*NP][n]: NP = 3 (m, l1, l2), or 6 with the slopes
+  const DevLinear* lin;  // time-dependent parameters, or NULL
   int64_t nsteps;
   int32_t k_ckpt;
   int64_t n;
 };
 
-template <class TB, class Pot>
+template <class TB, class Pot, bool TIMED = false>
 __global__ void __launch_bounds__(128) k_adjoint(AdjointArgs a, Pot pot, const DevComp* comps, int ncomp) {
+  constexpr int NP = TIMED ? 6 : 3;
   __shared__ DevComp s_comps[kAdjMaxComps];
-  for (int i = threadIdx.x; i < ncomp; i += blockDim.x) s_comps[i] = comps[i];
+  __shared__ DevLinear s_lin[TIMED ? kAdjMaxComps : 1];
+  for (int i = threadIdx.x; i < ncomp; i += blockDim.x) {
+    s_comps[i] = comps[i];
+    if constexpr (TIMED) s_lin[i] = a.lin[i];
+  }
   __syncthreads();
   const int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (o >= a.n) return;
@@ -62,7 +74,7 @@ __global__ void __launch_bounds__(128) k_adjoint(AdjointArgs a, Pot pot, const D
 #pragma unroll
       for (int j = 0; j < 6; ++j) a.ckpt[(c * 6 + j) * n + o] = y[j];
     }
-    rk_step_plain<TB>(pot, y, a.ts[k + 1] - a.ts[k]);
+    rk_step_plain<TB>(pot, y, a.ts[k + 1] - a.ts[k], a.ts[k]);
   }
   double lam[6];
 #pragma unroll
@@ -70,9 +82,9 @@ __global__ void __launch_bounds__(128) k_adjoint(AdjointArgs a, Pot pot, const D
     a.yT[j * n + o] = y[j];
     lam[j] = a.lambda ? a.lambda[j * n + o] : 2.0 * (y[j] - a.target[j * n + o]);
   }
-  double gp[kAdjMaxComps * 3];
+  double gp[kAdjMaxComps * NP];
 #pragma unroll
-  for (int i = 0; i < kAdjMaxComps * 3; ++i) gp[i] = 0.0;
+  for (int i = 0; i < kAdjMaxComps * NP; ++i) gp[i] = 0.0;
   const int64_t nseg = (a.nsteps + K - 1) / K;
   for (int64_t sgi = nseg - 1; sgi >= 0; --sgi) {
     const int64_t k0 = sgi * K;
@@ -82,16 +94,17 @@ __global__ void __launch_bounds__(128) k_adjoint(AdjointArgs a, Pot pot, const D
     for (int64_t k = k0; k < k1; ++k) {
 #pragma unroll
       for (int j = 0; j < 6; ++j) a.seg[((k - k0) * 6 + j) * n + o] = y[j];
-      if (k + 1 < k1) rk_step_plain<TB>(pot, y, a.ts[k + 1] - a.ts[k]);
+      if (k + 1 < k1) rk_step_plain<TB>(pot, y, a.ts[k + 1] - a.ts[k], a.ts[k]);
     }
     for (int64_t k = k1 - 1; k >= k0; --k) {
       const double hs = a.ts[k + 1] - a.ts[k];  // signed step (the grid carries the direction)
+      const double tk = a.ts[k];
       double yk[6];
 #pragma unroll
       for (int j = 0; j < 6; ++j) yk[j] = a.seg[((k - k0) * 6 + j) * n + o];
       // recompute the stages, keeping each stage position
       double F[TB::S][6], Yq[TB::S][3];
-      field(pot, yk, F[0]);
+      field(pot, yk, F[0], tk);
       Yq[0][0] = yk[0];
       Yq[0][1] = yk[1];
       Yq[0][2] = yk[2];
@@ -102,7 +115,8 @@ __global__ void __launch_bounds__(128) k_adjoint(AdjointArgs a, Pot pot, const D
         Yq[I][0] = Y[0];
         Yq[I][1] = Y[1];
         Yq[I][2] = Y[2];
-        field(pot, Y, F[I]);
+        constexpr double ci = TB::C[I];
+        field(pot, Y, F[I], fma(ci, hs, tk));
       });
       // reverse sweep (F is reused as Fbar)
       static_for<0, TB::S>([&](auto i) {
@@ -115,12 +129,19 @@ __global__ void __launch_bounds__(128) k_adjoint(AdjointArgs a, Pot pot, const D
         constexpr int I = TB::S - 1 - decltype(r)::value;
         double Hv[3] = {0.0, 0.0, 0.0};
         const double v[3] = {F[I][3], F[I][4], F[I][5]};
+        constexpr double ci = TB::C[I];
+        const double ti = fma(ci, hs, tk);  // the stage's time, as in the forward pass
         for (int c = 0; c < ncomp; ++c) {
           double dp[3] = {0.0, 0.0, 0.0};
-          comp_vjp(s_comps[c], Yq[I], v, Hv, dp);
-          gp[3 * c + 0] -= dp[0];
-          gp[3 * c + 1] -= dp[1];
-          gp[3 * c + 2] -= dp[2];
+          if constexpr (TIMED)
+            comp_vjp(comp_at_time(s_comps[c], s_lin[c], ti), Yq[I], v, Hv, dp);
+          else
+            comp_vjp(s_comps[c], Yq[I], v, Hv, dp);
+#pragma unroll
+          for (int j = 0; j < 3; ++j) {
+            gp[NP * c + j] -= dp[j];
+            if constexpr (TIMED) gp[NP * c + 3 + j] -= dp[j] * ti;
+          }
         }
         const double Yb[6] = {-Hv[0], -Hv[1], -Hv[2], F[I][0], F[I][1], F[I][2]};
 #pragma unroll
@@ -138,7 +159,7 @@ __global__ void __launch_bounds__(128) k_adjoint(AdjointArgs a, Pot pot, const D
   }
 #pragma unroll
   for (int j = 0; j < 6; ++j) a.grad_y0[j * n + o] = lam[j];
-  for (int i = 0; i < ncomp * 3; ++i) a.gp_orbit[(int64_t)i * n + o] = gp[i];
+  for (int i = 0; i < ncomp * NP; ++i) a.gp_orbit[(int64_t)i * n + o] = gp[i];
 }
 
 // grad_params[p] = sum over orbits of gp_orbit[p][:], in a fixed order.
@@ -191,7 +212,7 @@ struct AdjLayout {
   int64_t nsteps, nseg;
 };
 
-static AdjLayout adj_layout(int ncomp, const std::vector<double>& ts, int k, int64_t n) {
+static AdjLayout adj_layout(int ncomp, int np, const std::vector<double>& ts, int k, int64_t n) {
   AdjLayout L{};
   L.nsteps = (int64_t)ts.size() - 1;
   L.nseg = (L.nsteps + k - 1) / k;
@@ -203,7 +224,7 @@ static AdjLayout adj_layout(int ncomp, const std::vector<double>& ts, int k, int
   L.seg = off;
   off += align256(sizeof(double) * 6 * (size_t)k * n);
   L.gp = off;
-  off += align256(sizeof(double) * 3 * (size_t)ncomp * n);
+  off += align256(sizeof(double) * np * (size_t)ncomp * n);
   L.total = off;
   return L;
 }
@@ -222,7 +243,7 @@ gal_status gal_adjoint_workspace_size(const gal_potential* pot, const gal_solver
     std::vector<double> ts;
     if (!time_grid(t0, t1, cfg->dt0, cfg->max_steps, ts))
       return fail(GAL_ERR_INVALID_ARGUMENT, "t0 and t1 must be finite and at most max_steps steps of dt0 apart");
-    *bytes = adj_layout(pot->n, ts, k_ckpt, n).total;
+    *bytes = adj_layout(pot->n, time_dependent(pot) ? 6 : 3, ts, k_ckpt, n).total;
     return GAL_OK;
   });
 }
@@ -233,8 +254,7 @@ gal_status gal_adjoint(const gal_potential* pot, const gal_solver_config* cfg, c
                        gal_stream_t stream) {
   return no_throw([&]() -> gal_status {
     if (!pot) return fail(GAL_ERR_INVALID_ARGUMENT, "potential is NULL");
-    if (time_dependent(pot))
-      return fail(GAL_ERR_UNSUPPORTED, "time-dependent parameters: evaluation and gal_integrate only");
+    const bool timed = time_dependent(pot);
     gal_status st = validate_cfg(cfg);
     if (st != GAL_OK) return st;
     if (cfg->adaptive) return fail(GAL_ERR_UNSUPPORTED, "the adjoint needs a constant step (adaptive = 0)");
@@ -247,7 +267,8 @@ gal_status gal_adjoint(const gal_potential* pot, const gal_solver_config* cfg, c
     std::vector<double> ts;
     if (!time_grid(t0, t1, cfg->dt0, cfg->max_steps, ts))
       return fail(GAL_ERR_INVALID_ARGUMENT, "t0 and t1 must be finite and at most max_steps steps of dt0 apart");
-    const AdjLayout L = adj_layout(pot->n, ts, k_ckpt, n);
+    const int np = timed ? 6 : 3;
+    const AdjLayout L = adj_layout(pot->n, np, ts, k_ckpt, n);
     if (!workspace || workspace_bytes < L.total) return fail(GAL_ERR_WORKSPACE, "workspace too small");
     char* ws = static_cast<char*>(workspace);
     cudaStream_t s = (cudaStream_t)stream;
@@ -266,9 +287,16 @@ gal_status gal_adjoint(const gal_potential* pot, const gal_solver_config* cfg, c
     a.nsteps = L.nsteps;
     a.k_ckpt = k_ckpt;
     a.n = n;
+    a.lin = pot->d_lin;
     const int block = 64;
     const unsigned grid = (unsigned)((n + block - 1) / block);
-    if (cfg->method == 8) {
+    if (timed) {
+      const TimedTablePot tp{pot->d_comps, pot->n, pot->d_lin};
+      if (cfg->method == 8)
+        k_adjoint<Dopri8, TimedTablePot, true><<<grid, block, 0, s>>>(a, tp, pot->d_comps, pot->n);
+      else
+        k_adjoint<Dopri5, TimedTablePot, true><<<grid, block, 0, s>>>(a, tp, pot->d_comps, pot->n);
+    } else if (cfg->method == 8) {
       if (pot->is_mw)
         k_adjoint<Dopri8, MWPot><<<grid, block, 0, s>>>(a, MWPot{pot->mw}, pot->d_comps, pot->n);
       else
@@ -281,7 +309,7 @@ gal_status gal_adjoint(const gal_potential* pot, const gal_solver_config* cfg, c
     }
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "adjoint kernel launch");
-    k_reduce_rows<<<(unsigned)(pot->n * 3), 256, 0, s>>>(a.gp_orbit, n, grad_params);
+    k_reduce_rows<<<(unsigned)(pot->n * np), 256, 0, s>>>(a.gp_orbit, n, grad_params);
     e = cudaGetLastError();
     return e == cudaSuccess ? GAL_OK : cuda_fail(e, "adjoint reduction launch");
   });

@@ -418,7 +418,8 @@ gal_status gal_potential_set_linear(gal_potential* p, const double* slopes) {
       p->d_lin = nullptr;
       if (e != cudaSuccess) return cuda_fail(e, "cudaFree(linear table)");
     }
-    if (any) {
+    (void)any;
+    if (slopes) {  // time-dependent even when every slope is zero: the adjoint then gives d/d(slope)
       cudaError_t e = cudaMalloc(&p->d_lin, sizeof(DevLinear) * p->n);
       if (e != cudaSuccess) {
         p->d_lin = nullptr;
@@ -428,7 +429,7 @@ gal_status gal_potential_set_linear(gal_potential* p, const double* slopes) {
       if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(linear table)");
     }
     // the specialised Milky Way model has constant parameters
-    p->is_mw = !any && milky_way_shape(p->comps.data(), p->n);
+    p->is_mw = !p->d_lin && milky_way_shape(p->comps.data(), p->n);
     return GAL_OK;
   });
 }
@@ -470,6 +471,8 @@ gal_status gal_potential_update(gal_potential* p, const gal_component* comps, in
 
 int32_t gal_potential_num_components(const gal_potential* p) { return p ? p->n : 0; }
 int32_t gal_potential_is_milky_way(const gal_potential* p) { return p && p->is_mw ? 1 : 0; }
+
+int32_t gal_potential_is_time_dependent(const gal_potential* p) { return time_dependent(p) ? 1 : 0; }
 
 static gal_status eval_grad_common(const gal_potential* p, const double* x, double t, int64_t n, double* out,
                                    double sign, gal_stream_t stream) {

@@ -1384,7 +1384,7 @@ static gal_status stream_validate(const gal_potential* pot, const gal_stream_con
   if (c->k_ckpt < 0) return fail(GAL_ERR_INVALID_ARGUMENT, "k_ckpt must be >= 0");
   if (!(c->prog_m > 0.0) || !(c->prog_b > 0.0)) return fail(GAL_ERR_INVALID_ARGUMENT, "progenitor m, b must be > 0");
   if (pot->n > kAdjMaxComps) return fail(GAL_ERR_UNSUPPORTED, "stream host potentials have at most 8 components");
-  if (time_dependent(pot)) return fail(GAL_ERR_UNSUPPORTED, "time-dependent parameters: evaluation and gal_integrate only");
+  if (time_dependent(pot)) return fail(GAL_ERR_UNSUPPORTED, "time-dependent parameters: evaluation, integration and the orbit adjoint only");
   return df_validate(c->df, c->df_params);
 }
 
@@ -1481,7 +1481,7 @@ gal_status gal_stream_df_sample(const gal_potential* pot, int32_t df, const doub
                                 const double* prog_mass, const double* noise, int64_t n, double* lead, double* trail,
                                 double* r_tidal, gal_stream_t stream) {
   if (!pot) return fail(GAL_ERR_INVALID_ARGUMENT, "NULL potential");
-  if (time_dependent(pot)) return fail(GAL_ERR_UNSUPPORTED, "time-dependent parameters: evaluation and gal_integrate only");
+  if (time_dependent(pot)) return fail(GAL_ERR_UNSUPPORTED, "time-dependent parameters: evaluation, integration and the orbit adjoint only");
   gal_status st = df_validate(df, df_params);
   if (st != GAL_OK) return st;
   if (n < 0) return fail(GAL_ERR_INVALID_ARGUMENT, "n must be >= 0");

@@ -126,7 +126,7 @@ gal_status gal_integrate_surrogate(const gal_potential* pot, const gal_mlp* mlp,
                                    double t0, double t1, double* y, int64_t n, int32_t use_graph, void* workspace,
                                    size_t workspace_bytes, gal_stream_t stream) {
   if (!pot || !y || n < 0 || !(dt > 0.0)) return fail(GAL_ERR_INVALID_ARGUMENT, "bad surrogate arguments");
-  if (time_dependent(pot)) return fail(GAL_ERR_UNSUPPORTED, "time-dependent parameters: evaluation and gal_integrate only");
+  if (time_dependent(pot)) return fail(GAL_ERR_UNSUPPORTED, "time-dependent parameters: evaluation, integration and the orbit adjoint only");
   if (!std::isfinite(t0) || !std::isfinite(t1)) return fail(GAL_ERR_INVALID_ARGUMENT, "t0 and t1 must be finite");
   if (n == 0 || t0 == t1) return GAL_OK;
   size_t need = 0;

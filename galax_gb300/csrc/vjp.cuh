@@ -97,11 +97,12 @@ __device__ __forceinline__ void comp_vjp(const DevComp& c, const double* x, cons
   dp[2] += dl2;
 }
 
+// One constant step of signed length hs from time t (static models ignore t).
 template <class TB, class Pot>
-__device__ __forceinline__ void rk_step_plain(const Pot& pot, double* y, double hs) {
+__device__ __forceinline__ void rk_step_plain(const Pot& pot, double* y, double hs, double t = 0.0) {
   double F[TB::S][6], y1[6];
-  field(pot, y, F[0]);
-  rk_stages<TB>(pot, y, hs, F);
+  field(pot, y, F[0], t);
+  rk_stages<TB>(pot, y, hs, F, t);
   rk_combine<TB>(y, hs, F, y1, nullptr);
 #pragma unroll
   for (int j = 0; j < 6; ++j) y[j] = y1[j];

@@ -106,16 +106,20 @@ GAL_API gal_status gal_potential_destroy(gal_potential* pot);
  * component table holds the values at t = 0 (galax's point-slope form
  * p(t) = slope (t - t_i) + p(t_i) gives p(0) = p(t_i) - slope t_i). The
  * gal_eval_* functions evaluate at their t; gal_integrate,
- * gal_integrate_noalloc and the dense-output pair (gal_integrate_dense,
- * gal_dense_evaluate) evaluate every stage at its own time. Adjoint, stream
+ * gal_integrate_noalloc, the dense-output pair (gal_integrate_dense,
+ * gal_dense_evaluate) and gal_adjoint evaluate every stage at its own time;
+ * gal_adjoint also returns the derivatives with respect to the slopes. Stream
  * and surrogate entry points reject time-dependent potentials
- * (GAL_ERR_UNSUPPORTED). slopes = NULL makes the potential static again. */
+ * (GAL_ERR_UNSUPPORTED). slopes = NULL makes the potential static again; any
+ * other array, all zeros included, makes it time-dependent. */
 GAL_API gal_status gal_potential_set_linear(gal_potential* pot, const double* slopes);
 /* Replace the parameters (same count and kinds), e.g. between optimiser steps. */
 GAL_API gal_status gal_potential_update(gal_potential* pot, const gal_component* comps, int32_t n, gal_stream_t stream);
 GAL_API int32_t gal_potential_num_components(const gal_potential* pot);
 /* 1 when the composite is evaluated by the specialised MilkyWayPotential kernel. */
 GAL_API int32_t gal_potential_is_milky_way(const gal_potential* pot);
+/* 1 when gal_potential_set_linear gave the composite time-dependent parameters. */
+GAL_API int32_t gal_potential_is_time_dependent(const gal_potential* pot);
 
 /* Batched evaluation at n positions x[3][n] at time t. t matters only for a
  * potential with LinearParameter slopes (gal_potential_set_linear), whose
@@ -272,7 +276,11 @@ GAL_API gal_status gal_adjoint_workspace_size(const gal_potential* pot, const ga
 /* Discrete adjoint of the constant-step map y(t0) -> y(t1) (cfg->adaptive must be
  * 0; step cfg->dt0) for terminal cotangents: given lambda = dL/dy(t1) [6][n],
  * returns the final states yT [6][n], dL/dy0 [6][n] and dL/d(m, l1, l2) for
- * every component, summed over orbits, [ncomp][3]. The forward pass stores the
+ * every component, summed over orbits, [ncomp][3]; for a time-dependent
+ * potential (gal_potential_is_time_dependent) grad_params is [ncomp][6]:
+ * d/d(m, l1, l2) of the values at t = 0, then d/d(their slopes), each stage
+ * evaluated at its own time (galax's LinearParameter,
+ * src/galax/potential/_src/params/core.py:25-110). The forward pass stores the
  * state every k_ckpt steps; the reverse pass recomputes each segment from its
  * checkpoint. Replaces reverse-mode differentiation through diffeqsolve with
  * RecursiveCheckpointAdjoint (src/galax/dynamics/_src/orbit/solver.py:99-108)

@@ -645,13 +645,90 @@ def test_linear_parameters_integrate_like_oracle(gx, method):
 
 
 def test_time_dependent_potentials_are_refused_where_unsupported(gx):
+    from galax_gb300 import surrogate as S
     from galax_gb300._lib import GalaxGB300Error
-    from galax_gb300.adjoint import orbit_adjoint
 
     pot = gx.KeplerPotential(m_tot=gx.LinearParameter(slope=-1e8, point_time=0.0, point_value=1e11))
     y0 = _ics(4, 1)
     with pytest.raises(GalaxGB300Error):
-        orbit_adjoint(pot, y0, 0.0, 10.0, dt=1.0, target=y0, method=8, k_ckpt=4)
+        S.integrate(pot, None, y0, 0.0, 10.0, 1.0)
+
+
+def _linear_mw():
+    c = O.milky_way()
+    slopes = np.zeros((len(c), 3))
+    slopes[0, 0] = -2e8    # disk mass (Msun / Myr)
+    slopes[0, 1] = 1e-3    # disk a (kpc / Myr)
+    slopes[1, 0] = 5e8     # halo mass
+    slopes[1, 1] = -4e-3   # halo r_s
+    return c, slopes
+
+
+@pytest.mark.parametrize("method", [8, 5])
+def test_adjoint_with_linear_parameters_matches_oracle(gx, method):
+    """The GPU adjoint through LinearParameter time dependence (every stage at
+    its own time) against the oracle's, which central differences pin:
+    d/d(values at t = 0) and d/d(slopes) of every component."""
+    import torch
+
+    from galax_gb300.adjoint import orbit_adjoint
+    from galax_gb300.potential import from_component_array
+
+    c, slopes = _linear_mw()
+    n, dt, t1 = 64, 0.5, 300.0
+    y0 = _ics(n, 41)
+    cfg = O.solver_cfg(method, False, dt0=dt)
+    yT_ref, *_ = O.integrate(c, y0, 0.0, t1, np.array([t1]), cfg, slopes=slopes)
+    target = np.stack(yT_ref).reshape(-1, 6) + np.random.default_rng(42).normal(0, 0.05, (n, 6))
+    yT_o, gy_o, gp_o, L_o = O.adjoint_fixed(c, y0, 0.0, t1, target, cfg, slopes=slopes)
+    assert gp_o.shape == (len(c), 6)
+    res = orbit_adjoint(from_component_array(c, slopes=slopes), y0, 0.0, t1, dt=dt, target=target,
+                        method=method, k_ckpt=64)
+    torch.cuda.synchronize()
+    assert res.grad_params.shape == (len(c), 6)
+    assert _rel(res.yT, yT_o) < 1e-9
+    np.testing.assert_allclose(res.grad_y0, gy_o, rtol=1e-7, atol=1e-10 * np.abs(gy_o).max())
+    mask = gp_o != 0
+    np.testing.assert_allclose(res.grad_params[mask], gp_o[mask], rtol=1e-7)
+    assert abs(res.loss - L_o) <= 1e-9 * L_o
+
+
+@pytest.mark.parametrize("zero_slopes", [False, True])
+def test_orbit_map_through_linear_parameters(gx, zero_slopes):
+    """OrbitMap with (ncomp, 6) parameters: values at t = 0 and slopes; with
+    every slope zero the potential stays time-dependent, so the slope
+    derivatives are still returned (and equal the oracle's at zero slope)."""
+    import torch
+
+    from galax_gb300.adjoint import OrbitMap, params_of
+    from galax_gb300.potential import from_component_array
+
+    c, slopes = _linear_mw()
+    if zero_slopes:
+        slopes = np.zeros_like(slopes)
+    n, dt, t1 = 32, 1.0, 200.0
+    y0h = _ics(n, 43)
+    cfg = O.solver_cfg(8, False, dt0=dt)
+    yT_ref, *_ = O.integrate(c, y0h, 0.0, t1, np.array([t1]), cfg, slopes=slopes)
+    target = np.stack(yT_ref).reshape(-1, 6) + np.random.default_rng(44).normal(0, 0.05, (n, 6))
+    _, gy_o, gp_o, L_o = O.adjoint_fixed(c, y0h, 0.0, t1, target, cfg, slopes=slopes)
+    base = from_component_array(c)
+    params = torch.tensor(np.concatenate([np.stack([c["m"], c["l1"], c["l2"]], 1), slopes], 1),
+                          dtype=torch.float64, device="cuda", requires_grad=True)
+    if not zero_slopes:
+        np.testing.assert_array_equal(params_of(from_component_array(c, slopes=slopes)).cpu().numpy(),
+                                      params.detach().cpu().numpy())
+    y0 = torch.tensor(y0h, dtype=torch.float64, device="cuda", requires_grad=True)
+    yT = OrbitMap.apply(base, y0, params, 0.0, t1, dt, 8, 50)
+    loss = ((yT - torch.as_tensor(target, device="cuda")) ** 2).sum()
+    loss.backward()
+    torch.cuda.synchronize()
+    assert abs(float(loss) - L_o) <= 1e-9 * L_o
+    np.testing.assert_allclose(y0.grad.cpu().numpy(), gy_o, rtol=1e-8, atol=1e-12 * np.abs(gy_o).max())
+    gp = params.grad.cpu().numpy()
+    mask = gp_o != 0
+    np.testing.assert_allclose(gp[mask], gp_o[mask], rtol=1e-8)
+    assert np.count_nonzero(gp[:, 3:]) > 0  # slope derivatives, also at zero slope
 
 
 # ------------------------------------------------------------------ four-warp teams for the longest orbits

@@ -411,13 +411,62 @@ def _sensitivity(b, idx, per_orbit, saves_o, starts, lens, tol, n_control: int =
     }
 
 
+def run_uneven_dopri8(steps: int = 2, warmup: int = 1) -> dict:
+    """The headline batch (262,144 uneven orbits, PID rtol 1e-8 atol 1e-10) with
+    Dopri8, galax's default method, with the longest orbits on four-warp teams
+    (the library's default) and, once, without them."""
+    import torch
+
+    import galax_gb300 as gx
+    from galax_gb300 import _lib
+    from galax_gb300.dynamics import Workspace, integrate
+    from galax_gb300.flops import STEP_FLOPS_MW
+
+    mw, b = make_uneven(DEFAULT_ORBITS["uneven"], seed=1)
+    cfg = gx.Integrator(solver=gx.Dopri8(), stepsize_controller=gx.PIDController(rtol=1e-8, atol=1e-10),
+                        max_steps=2**16).config()
+    dev = "cuda"
+    y0 = torch.as_tensor(b.y0, device=dev).t().contiguous()
+    t0, t1 = torch.as_tensor(b.t0, device=dev), torch.as_tensor(b.t1, device=dev)
+    offs, sts = torch.as_tensor(b.save_offsets, device=dev), torch.as_tensor(b.save_ts, device=dev)
+    ws = Workspace()
+    stream = torch.cuda.current_stream()
+
+    def step():
+        r = torch.linalg.vector_norm(y0[:3], dim=0)
+        a = torch.linalg.vector_norm(mw.gradient(y0[:3].t()), dim=1)
+        order = torch.argsort((t1 - t0).abs() * torch.sqrt(a / r), descending=True).to(torch.int32)
+        return integrate(mw, y0, t0, t1, sts, cfg, save_offsets=offs, order=order, soa=True, workspace=ws)
+
+    L = _lib.load()
+    res = {}
+    for team in (32, 0):
+        _lib.check(L.gal_set_team(team), "gal_set_team")
+        for _ in range(warmup):
+            _, st, acc = step()
+        ms = _timed(step, steps if team else 1, stream)
+        res[team] = (ms, int(acc.sum()), int((st != 0).sum()))
+    _lib.check(L.gal_set_team(32), "gal_set_team")
+    ms, accepted, bad = res[32]
+    peak = fp64_peak()
+    achieved = accepted * STEP_FLOPS_MW[8] / (ms * 1e-3) / 1e12
+    return {"metric": "orbit-steps/s", "value": accepted / (ms * 1e-3), "unit": "orbit-steps/s",
+            "ms_per_step": ms, "steps": steps, "warmup": warmup,
+            "config": {"workload": WORKLOADS["uneven"].replace("Dopri5", "Dopri8"), "accepted_steps": accepted,
+                       "orbits_not_finished": bad},
+            "without_teams": {"ms_per_step": res[0][0], "value": res[0][1] / (res[0][0] * 1e-3)},
+            "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak["tflops"], "unit": "TFLOP/s",
+                         "frac": achieved / peak["tflops"], "flops_per_accepted_step": STEP_FLOPS_MW[8]}}
+
+
 def run_extras(args) -> dict:
     """The other two parts of the metric on the same GPU, after the headline:
     gradients/s of the differentiation workload at full size, and the learned
-    surrogate against the plain FP64 direct sum."""
+    surrogate against the plain FP64 direct sum; and the headline batch with
+    Dopri8."""
     import argparse as _ap
 
-    out = {}
+    out = {"uneven_dopri8": run_uneven_dopri8()}
     g = run_grad(_ap.Namespace(**{**vars(args), "steps": 2, "warmup": 3, "t1": 0.0}), DEFAULT_ORBITS["grad"], 0, 1,
                  None)
     out["grad"] = {k: g[k] for k in ("metric", "value", "unit", "ms_per_step", "steps", "warmup", "config", "e2e",

@@ -655,7 +655,7 @@ gal_status gal_integrate(const gal_potential* p, const gal_solver_config* cfg, c
   const int sms = device_sm_count();
   const int team_blocks = g_team_blocks.load(std::memory_order_relaxed);
   const int blocks = team_blocks < sms - 1 ? team_blocks : sms - 1;
-  if (blocks > 0 && p->is_mw && cfg->method == 5) {
+  if (blocks > 0 && p->is_mw) {
     // The longest orbits go to four-warp teams on `blocks` SMs of their own
     // (second stream), the rest to the one-thread kernel on the other SMs, one
     // block per SM; results are the same either way.
@@ -668,8 +668,9 @@ gal_status gal_integrate(const gal_potential* p, const gal_solver_config* cfg, c
     if (e == cudaSuccess) e = cudaStreamWaitEvent(ts, fork, 0);
     bool team_launched = false, joinable = false;
     if (e == cudaSuccess) {
-      e = launch_integrate_team(a, p->mw, reinterpret_cast<unsigned long long*>(ws + 528), tcap, blocks,
-                                kExclusiveSmem, ts);
+      unsigned long long* tq = reinterpret_cast<unsigned long long*>(ws + 528);
+      e = cfg->method == 8 ? launch_integrate_team8(a, p->mw, tq, tcap, blocks, kExclusiveSmem, ts)
+                           : launch_integrate_team(a, p->mw, tq, tcap, blocks, kExclusiveSmem, ts);
       team_launched = e == cudaSuccess;
     }
     if (e == cudaSuccess) {
@@ -679,7 +680,9 @@ gal_status gal_integrate(const gal_potential* p, const gal_solver_config* cfg, c
     if (e == cudaSuccess) {
       a.queue_base = tcap;
       // one warp per sub-partition: two (256 threads) made the step 1.4x longer
-      e = launch_integrate_dopri5_exclusive(a, p->mw, shape.variant, 128, sms - blocks, kExclusiveSmem, s);
+      e = cfg->method == 8
+              ? launch_integrate_dopri8_exclusive(a, p->mw, shape.variant, 128, sms - blocks, kExclusiveSmem, s)
+              : launch_integrate_dopri5_exclusive(a, p->mw, shape.variant, 128, sms - blocks, kExclusiveSmem, s);
     }
     // Whatever failed after the team kernel was queued, the caller's stream
     // still waits for it, so the caller never frees buffers it is using.

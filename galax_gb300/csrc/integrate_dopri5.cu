@@ -11,9 +11,10 @@ cudaError_t launch_integrate_dopri5(const IntegrateArgs& a, bool mw, const MWPar
 
 cudaError_t launch_integrate_team(const IntegrateArgs& a, const MWParams& p, unsigned long long* tqueue,
                                   long long tcap, int blocks, size_t smem, cudaStream_t stream) {
-  cudaError_t e = cudaFuncSetAttribute(k_integrate_mw_team, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e =
+      cudaFuncSetAttribute(k_integrate_mw_team<Dopri5>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  k_integrate_mw_team<<<(unsigned)blocks, 128, smem, stream>>>(a, p, tqueue, tcap);
+  k_integrate_mw_team<Dopri5><<<(unsigned)blocks, 128, smem, stream>>>(a, p, tqueue, tcap);
   return cudaGetLastError();
 }
 

@@ -1,5 +1,5 @@
-// Four-warp teams for the longest orbits of an adaptive Dopri5 batch in the
-// Milky Way model.
+// Four-warp teams for the longest orbits of an adaptive Dopri5 or Dopri8
+// batch in the Milky Way model.
 //
 // The orbits that run longest set the duration of an uneven batch, and a lone
 // orbit is latency-bound: a GB300 FP64 warp instruction holds its
@@ -14,6 +14,13 @@
 // computed redundantly by all four warps from the same shared-memory values.
 // Every operation matches the one-thread-per-orbit kernel (k_integrate_mw with
 // MWPot::grad, integrate_loop), so results are bitwise identical.
+//
+// Dopri5 is FSAL: a step's last stage is the next step's first slope. Dopri8
+// is not, and follows integrate_loop's non-FSAL branch: after an accepted step
+// the slope at the new state is one more team round, and saves inside an
+// accepted step are written by sub-steps of the partial length from the
+// step's start (the orbit stays "pending" until its last save of the step),
+// each one RK evaluation of its own.
 //
 // Used for the second pass of the two-pass schedule only: every orbit resumes
 // from its parked state.
@@ -134,9 +141,9 @@ __device__ __forceinline__ void team_write_save(const IntegrateArgs& a, const Or
 
 // tqueue: the team's position counter; positions [0, min(tcap, *a.queue_len))
 // of a.order are the team's.
+template <class TB>
 __global__ void __launch_bounds__(128, 1) k_integrate_mw_team(IntegrateArgs a, MWParams p,
                                                               unsigned long long* tqueue, long long tcap) {
-  using TB = Dopri5;
   constexpr int S = TB::S;
   __shared__ TeamShared sh;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -148,7 +155,9 @@ __global__ void __launch_bounds__(128, 1) k_integrate_mw_team(IntegrateArgs a, M
   s.orbit = -1;
   bool need_orbit = true, queue_open = true;
   double yo0 = 0.0, yo1 = 0.0;  // owned state components j0, j1 (s.y holds all six for the controller)
-  double F0[2] = {0.0, 0.0};    // owned components of the FSAL slope
+  double yn0 = 0.0, yn1 = 0.0;  // Dopri8: owned components of the accepted end state while saves are pending
+  double F0[2] = {0.0, 0.0};    // owned components of the slope at (tau, y)
+  bool need_f0 = false;         // Dopri8: the slope at a newly committed state is still to be evaluated
   int round = 0;
   while (true) {
     // ---- lanes without an orbit take the next queue position (warp 0 dequeues)
@@ -196,18 +205,23 @@ __global__ void __launch_bounds__(128, 1) k_integrate_mw_team(IntegrateArgs a, M
     }
     const bool active = s.orbit >= 0;
     if (!__syncthreads_or(active)) break;
-    // ---- slope at the resumed states (one team round, only when a lane needs it)
-    if (__syncthreads_or(fresh)) {
+    // ---- slope at resumed (and, for Dopri8, newly committed) states: one team
+    // round, only when a lane needs it
+    const bool want_f0 = fresh || (need_f0 && active);
+    if (__syncthreads_or(want_f0)) {
       const int b = round++ & 1;
-      if (owner) sh.pos[b][warp][lane] = fresh ? yo0 : 8.0;
+      if (owner) sh.pos[b][warp][lane] = want_f0 ? yo0 : 8.0;
       const double g = team_grad(sh, b, warp, lane, p);
-      if (owner && fresh) {
+      if (owner && want_f0) {
         F0[0] = yo1;
         F0[1] = -g;
       }
     }
-    // ---- one step (integrate_loop, FSAL branch)
-    const double hs = s.dir * (s.tnext - s.tau);
+    need_f0 = false;
+    // ---- one RK evaluation (integrate_loop): a step from (tau, y), or for
+    // Dopri8 with saves pending the sub-step from (tau, y) to the next save
+    const bool sub = !TB::FSAL && s.pending && active;
+    const double hs = sub ? s.dir * (save_tau(a, s, s.save_i) - s.tau) : s.dir * (s.tnext - s.tau);
     double Fp[S], Fv[S];  // owned components of the stage slopes: position j0, velocity j1
     Fp[0] = F0[0];
     Fv[0] = F0[1];
@@ -231,7 +245,7 @@ __global__ void __launch_bounds__(128, 1) k_integrate_mw_team(IntegrateArgs a, M
       y1o1 = weighted_comp<TB, W_SOLUTION, true>(yo1, hs, Fv);
       sh.y1[j0][lane] = y1o0;
       sh.y1[j1][lane] = y1o1;
-      if (a.adaptive) {
+      if (a.adaptive && !sub) {
         sh.err[j0][lane] = weighted_comp<TB, W_ERROR, false>(0.0, hs, Fp);
         sh.err[j1][lane] = weighted_comp<TB, W_ERROR, false>(0.0, hs, Fv);
       }
@@ -245,6 +259,46 @@ __global__ void __launch_bounds__(128, 1) k_integrate_mw_team(IntegrateArgs a, M
     }
     __syncthreads();  // the exchange arrays are reused next step
     if (!active) continue;
+    if constexpr (!TB::FSAL) {
+      if (sub) {  // the partial step's end is a save of the accepted step
+        if (owner) {
+          team_write_save(a, s, s.save_i, j0, y1o0);
+          team_write_save(a, s, s.save_i, j1, y1o1);
+        }
+        ++s.save_i;
+        if (s.save_i < s.save_end && save_tau(a, s, s.save_i) <= s.tau_new) continue;
+        // all saves of the accepted step written: commit it
+        s.pending = 0;
+#pragma unroll
+        for (int j = 0; j < 6; ++j) s.y[j] = s.ynew[j];
+        yo0 = yn0;
+        yo1 = yn1;
+        s.tau = fmin(s.tau_new, s.tau1);
+        need_f0 = true;
+        s.tnext = s.tnext_new;
+        bool done = false;
+        int32_t st = ORBIT_OK;
+        if (s.status != ORBIT_OK) {
+          done = true;
+          st = s.status;
+        } else if (s.tau >= s.tau1) {
+          done = true;
+        } else if (s.nsteps >= a.max_steps) {
+          done = true;
+          st = ORBIT_MAX_STEPS;
+        }
+        if (done) {
+          if (warp == 0) {
+            finish_orbit(a, s, st);
+          } else {
+            s.orbit = -1;
+          }
+          need_orbit = true;
+          need_f0 = false;
+        }
+        continue;
+      }
+    }
     ++s.nsteps;
     const double h = s.tnext - s.tau;
     double next_t0, next_t1;
@@ -269,25 +323,46 @@ __global__ void __launch_bounds__(128, 1) k_integrate_mw_team(IntegrateArgs a, M
       const double tnext_new = clip_to_end(tprev_new, next_t1, s.tau1, keep);
       if (keep) {
         ++s.naccepted;
-        if (s.save_i < s.save_end && save_tau(a, s, s.save_i) <= next_t0) {
-          const double ih = 1.0 / h;
-          do {
-            const double th = (save_tau(a, s, s.save_i) - s.tau) * ih;
-            if (owner) {
-              team_write_save(a, s, s.save_i, j0, dense_comp(yo0, hs, Fp, th));
-              team_write_save(a, s, s.save_i, j1, dense_comp(yo1, hs, Fv, th));
-            }
-            ++s.save_i;
-          } while (s.save_i < s.save_end && save_tau(a, s, s.save_i) <= next_t0);
-        }
+        if constexpr (TB::FSAL) {
+          if (s.save_i < s.save_end && save_tau(a, s, s.save_i) <= next_t0) {
+            const double ih = 1.0 / h;
+            do {
+              const double th = (save_tau(a, s, s.save_i) - s.tau) * ih;
+              if (owner) {
+                team_write_save(a, s, s.save_i, j0, dense_comp(yo0, hs, Fp, th));
+                team_write_save(a, s, s.save_i, j1, dense_comp(yo1, hs, Fv, th));
+              }
+              ++s.save_i;
+            } while (s.save_i < s.save_end && save_tau(a, s, s.save_i) <= next_t0);
+          }
 #pragma unroll
-        for (int j = 0; j < 6; ++j) s.y[j] = y1[j];
-        yo0 = y1o0;
-        yo1 = y1o1;
-        F0[0] = Fp[S - 1];
-        F0[1] = Fv[S - 1];
-        s.tau = tprev_new;
-        s.tnext = tnext_new;
+          for (int j = 0; j < 6; ++j) s.y[j] = y1[j];
+          yo0 = y1o0;
+          yo1 = y1o1;
+          F0[0] = Fp[S - 1];
+          F0[1] = Fv[S - 1];
+          s.tau = tprev_new;
+          s.tnext = tnext_new;
+        } else {
+          if (s.save_i < s.save_end && save_tau(a, s, s.save_i) <= next_t0) {
+            // saves inside this step: keep (tau, y) for the sub-steps
+            s.pending = 1;
+#pragma unroll
+            for (int j = 0; j < 6; ++j) s.ynew[j] = y1[j];
+            yn0 = y1o0;
+            yn1 = y1o1;
+            s.tau_new = next_t0;
+            s.tnext_new = tnext_new;
+            continue;
+          }
+#pragma unroll
+          for (int j = 0; j < 6; ++j) s.y[j] = y1[j];
+          yo0 = y1o0;
+          yo1 = y1o1;
+          s.tau = tprev_new;
+          s.tnext = tnext_new;
+          need_f0 = true;
+        }
       } else {
         s.tau = tprev_new;
         s.tnext = tnext_new;
@@ -309,6 +384,7 @@ __global__ void __launch_bounds__(128, 1) k_integrate_mw_team(IntegrateArgs a, M
         s.orbit = -1;
       }
       need_orbit = true;
+      need_f0 = false;
     }
   }
 }

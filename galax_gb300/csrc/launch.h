@@ -32,6 +32,11 @@ cudaError_t launch_integrate_team(const IntegrateArgs& a, const MWParams& p, uns
 // and of the team launch never share an SM.
 cudaError_t launch_integrate_dopri5_exclusive(const IntegrateArgs& a, const MWParams& p, int variant, int block,
                                               int grid, size_t smem, cudaStream_t stream);
+// The same two launches for a Dopri8 batch.
+cudaError_t launch_integrate_team8(const IntegrateArgs& a, const MWParams& p, unsigned long long* tqueue,
+                                   long long tcap, int blocks, size_t smem, cudaStream_t stream);
+cudaError_t launch_integrate_dopri8_exclusive(const IntegrateArgs& a, const MWParams& p, int variant, int block,
+                                              int grid, size_t smem, cudaStream_t stream);
 constexpr size_t kExclusiveSmem = 120 * 1024;
 
 int device_sm_count();

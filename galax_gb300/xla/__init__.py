@@ -147,7 +147,8 @@ def _ws_adjoint(pot, cfg, t0, t1, k_ckpt, n) -> int:
 
 def adjoint(pot, y0, lam, t0: float, t1: float, dt: float, method: int = 8, k_ckpt: int = 256):
     """Discrete adjoint of the constant-step map y0 -> y(t1) for the cotangent
-    lam = dL/dy(t1) (n, 6): returns (y(t1), dL/dy0, dL/d(m, l1, l2) per component)."""
+    lam = dL/dy(t1) (n, 6): returns (y(t1), dL/dy0, dL/d(m, l1, l2) per component,
+    followed by d/d(slopes) for a time-dependent potential)."""
     jax = _jax()
     jnp = jax.numpy
     register()
@@ -156,10 +157,11 @@ def adjoint(pot, y0, lam, t0: float, t1: float, dt: float, method: int = 8, k_ck
     n = y0.shape[0]
     cfg = _lib.solver_config(method, False, dt0=dt)
     ncomp = len(pot.components())
+    per = 6 if _lib.load().gal_potential_is_time_dependent(pot.handle()) else 3
     call = jax.ffi.ffi_call(
         "gal_adjoint",
         (jax.ShapeDtypeStruct((6, n), jnp.float64), jax.ShapeDtypeStruct((6, n), jnp.float64),
-         jax.ShapeDtypeStruct((ncomp, 3), jnp.float64),
+         jax.ShapeDtypeStruct((ncomp, per), jnp.float64),
          jax.ShapeDtypeStruct((_ws_adjoint(pot, cfg, t0, t1, k_ckpt, n),), jnp.uint8)))
     yT, gy, gp, _ = call(y0.T, lam.T, pot=np.int64(pot.handle()), method=np.int32(method), dt=np.float64(dt),
                          t0=np.float64(t0), t1=np.float64(t1), k_ckpt=np.int32(k_ckpt))

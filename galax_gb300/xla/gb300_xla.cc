@@ -108,7 +108,8 @@ ffi::Error Gradient(cudaStream_t stream, ffi::Buffer<ffi::F64> x, ffi::ResultBuf
 }
 
 // y0 [6][n], lambda = dL/dy(t1) [6][n] -> yT [6][n], dL/dy0 [6][n],
-// dL/d(m, l1, l2) [ncomp][3], workspace [bytes]; constant step dt.
+// dL/d(m, l1, l2) [ncomp][3] (with the slopes, [ncomp][6], for a
+// time-dependent potential), workspace [bytes]; constant step dt.
 ffi::Error Adjoint(cudaStream_t stream, ffi::Buffer<ffi::F64> y0, ffi::Buffer<ffi::F64> lambda,
                    ffi::ResultBuffer<ffi::F64> yT, ffi::ResultBuffer<ffi::F64> grad_y0,
                    ffi::ResultBuffer<ffi::F64> grad_params, ffi::ResultBuffer<ffi::U8> workspace, int64_t pot,
@@ -117,8 +118,9 @@ ffi::Error Adjoint(cudaStream_t stream, ffi::Buffer<ffi::F64> y0, ffi::Buffer<ff
   if ((int64_t)y0.element_count() != 6 * n || lambda.element_count() != y0.element_count() ||
       yT->element_count() != y0.element_count() || grad_y0->element_count() != y0.element_count())
     return ffi::Error::InvalidArgument("GalAdjoint: y0, lambda, yT and grad_y0 must be [6][n]");
-  if ((int64_t)grad_params->element_count() != 3 * (int64_t)gal_potential_num_components(as_potential(pot)))
-    return ffi::Error::InvalidArgument("GalAdjoint: grad_params must be [ncomp][3]");
+  const int64_t per = gal_potential_is_time_dependent(as_potential(pot)) ? 6 : 3;
+  if ((int64_t)grad_params->element_count() != per * (int64_t)gal_potential_num_components(as_potential(pot)))
+    return ffi::Error::InvalidArgument("GalAdjoint: grad_params must be [ncomp][3] ([ncomp][6] when time-dependent)");
   const gal_solver_config cfg =
       solver_config(method, 0, INT64_MAX, dt, 0.0, 0.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.9, 0.2, 10.0, 1, 0);
   const gal_status st = gal_adjoint(as_potential(pot), &cfg, y0.typed_data(), t0, t1, lambda.typed_data(), nullptr,

@@ -249,7 +249,7 @@ GAL_API gal_status gal_dense_evaluate(const gal_potential* pot, int32_t method, 
  * threads at maximum occupancy (variant 0 for Dopri5, 2 for Dopri8). */
 GAL_API gal_status gal_set_launch(int32_t method, int32_t adaptive, int32_t block_threads, int32_t blocks_per_sm,
                                   int32_t variant);
-/* Second pass of a two-pass Dopri5 batch in the Milky Way model: `blocks` > 0
+/* Second pass of a two-pass Dopri5 or Dopri8 batch in the Milky Way model: `blocks` > 0
  * (default 32, at most the SM count - 1) hands the 32 x blocks longest orbits to
  * four-warp team blocks, each on an SM of its own, on a library-owned stream
  * beside the one-thread-per-orbit kernel, which runs one block per remaining

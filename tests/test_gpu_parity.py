@@ -738,25 +738,30 @@ def _set_team(blocks):
     _lib.check(_lib.load().gal_set_team(int(blocks)), "gal_set_team")
 
 
+@pytest.mark.parametrize("method", [5, 8])
 @pytest.mark.parametrize("case", ["csr_forward", "shared_grid_backward", "few_orbits", "max_steps",
                                   "constant_step_scheduled"])
-def test_team_kernel_is_bitwise_identical(gx, case):
+def test_team_kernel_is_bitwise_identical(gx, case, method):
     """The second pass with the longest orbits on four-warp teams gives the
     same saves, statuses and step counts, bit for bit, as the one-thread
-    kernel alone."""
+    kernel alone; Dopri5 (FSAL, quartic saves) and Dopri8 (a slope round after
+    every accepted step, saves by partial sub-steps)."""
     from galax_gb300 import workloads as W
     from galax_gb300.dynamics import integrate
 
     mw = gx.MilkyWayPotential()
     n = {"csr_forward": 12000, "shared_grid_backward": 6000, "few_orbits": 300, "max_steps": 3000,
          "constant_step_scheduled": 4000}[case]
+    if method == 8:
+        n //= 2
     b = W.uneven_ics(lambda x: O.gradient(O.milky_way(), x), n, seed=8, tmax=1500.0, smax=40)
     max_steps = 2000 if case == "max_steps" else 2**16
+    solver = gx.Dopri5() if method == 5 else gx.Dopri8()
     if case == "constant_step_scheduled":
-        cfg = gx.Integrator(solver=gx.Dopri5(), stepsize_controller=gx.ConstantStepSize(), dt0=0.7,
+        cfg = gx.Integrator(solver=solver, stepsize_controller=gx.ConstantStepSize(), dt0=0.7,
                             schedule=True).config()
     else:
-        cfg = gx.Integrator(solver=gx.Dopri5(), stepsize_controller=gx.PIDController(rtol=1e-8, atol=1e-10),
+        cfg = gx.Integrator(solver=solver, stepsize_controller=gx.PIDController(rtol=1e-8, atol=1e-10),
                             max_steps=max_steps).config()
     res = []
     try:

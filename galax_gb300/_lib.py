@@ -124,6 +124,10 @@ SIGNATURES = {
     "gal_mlp_train_step": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, C.c_int64, C.c_float, C.c_float,
                                      C.c_float, C.c_float, C.c_float, C.c_float, C.c_int32, C.c_int32, _VP, _VP,
                                      C.c_size_t, C.c_void_p]),
+    "gal_mlp_train_workspace_size": (C.c_int, [C.c_int64, C.POINTER(C.c_size_t)]),
+    "gal_mlp_train": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP, _VP, C.c_int64, C.c_int64, C.c_int32, C.c_float,
+                                C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, C.c_uint64,
+                                C.c_int32, _VP, _VP, C.c_size_t, C.c_void_p]),
     "gal_mlp_create": (C.c_int, [_VP, C.c_double, C.c_double, C.POINTER(C.c_void_p)]),
     "gal_mlp_destroy": (C.c_int, [_VP]),
     "gal_mlp_eval": (C.c_int, [_VP, _DP, C.c_int64, _DP, C.c_int32, C.c_double, _DP, C.c_void_p]),

@@ -392,6 +392,118 @@ static void loss_grads(cudaStream_t s, const float* P, const float* x, const flo
   k_colsum<<<H, 256, 0, s>>>(w.Zb[1], nullptr, nullptr, B, H, grad + OFF_B1, 0, 0);
 }
 
+// ---------------------------------------------------------------- device-driven training
+// gal_mlp_train runs whole epochs without the host in the loop: every step
+// gathers its batch on the device through a pseudo-random permutation of the
+// samples, reads the step number from device memory for the learning-rate
+// schedule and Adam's bias corrections, and advances it; so one step has no
+// host-side arguments, is captured once as a CUDA graph and replayed.
+
+// MurmurHash3's 32-bit finaliser (Appleby, public domain): a bijective mixer.
+__device__ __forceinline__ uint32_t fmix32(uint32_t h) {
+  h ^= h >> 16;
+  h *= 0x85ebca6bu;
+  h ^= h >> 13;
+  h *= 0xc2b2ae35u;
+  h ^= h >> 16;
+  return h;
+}
+
+// A keyed permutation of [0, n): a four-round balanced Feistel network on
+// 2 hb bits (round function fmix32 of the right half and a round key), with
+// cycle-walking past n (Black & Rogaway, "Ciphers with arbitrary finite
+// domains", 2002). The domain 2^(2 hb) is below 4 n, so a walk of more than a
+// few steps is rare; after 64 the index maps to itself (a repeated sample,
+// harmless to stochastic gradient descent).
+__device__ __forceinline__ int64_t permute(int64_t i, int64_t n, int hb, uint32_t key) {
+  const uint64_t mask = (1ull << hb) - 1ull;
+  uint64_t x = (uint64_t)i;
+  for (int walk = 0; walk < 64; ++walk) {
+    uint64_t L = (x >> hb) & mask, R = x & mask;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const uint64_t F = fmix32((uint32_t)R ^ (key + 0x9e3779b9u * (uint32_t)(r + 1))) & mask;
+      const uint64_t t = L ^ F;
+      L = R;
+      R = t;
+    }
+    x = (L << hb) | R;
+    if ((int64_t)x < n) return (int64_t)x;
+  }
+  return i;
+}
+
+struct TrainRun {
+  const float *u, *phi_t, *g_t, *wt;  // the whole training set
+  int64_t n, batch, steps_per_epoch, total;
+  int hb;
+  uint64_t seed;
+  float *ub, *pb, *gb, *wb;  // this step's batch
+  long long* step;           // device step counter (0-based)
+  const float* loss;         // this step's loss (written by k_loss)
+  float* loss_per_epoch;
+};
+
+__global__ void k_gather(TrainRun r) {
+  const long long s = *r.step;
+  const int64_t e = s / r.steps_per_epoch, b = s % r.steps_per_epoch;
+  const uint32_t key = fmix32((uint32_t)r.seed ^ fmix32((uint32_t)e + 0x632be5abu + (uint32_t)(r.seed >> 32)));
+  GRID_STRIDE(j, r.batch) {
+    const int64_t i = permute(b * r.batch + j, r.n, r.hb, key);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      r.ub[j * 3 + c] = r.u[i * 3 + c];
+      r.gb[j * 3 + c] = r.g_t[i * 3 + c];
+    }
+    r.pb[j] = r.phi_t[i];
+    if (r.wt) r.wb[j] = r.wt[i];
+  }
+}
+
+// Adam with the step's cosine learning rate and bias corrections (step t = s + 1).
+__global__ void k_adam_run(float* p, const float* g, float* m, float* v, int64_t np, const long long* step,
+                           int64_t total, float lr, float lr_final, float b1, float b2, float eps) {
+  const float t = (float)(*step + 1);
+  const float lr_t = lr_final + 0.5f * (lr - lr_final) * (1.0f + cosf(3.14159265358979f * t / (float)total));
+  const float c1 = 1.0f - powf(b1, t), c2 = 1.0f - powf(b2, t);
+  GRID_STRIDE(i, np) {
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.0f - b1) * gi;
+    const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    p[i] -= lr_t * (mi / c1) / (sqrtf(vi / c2) + eps);
+  }
+}
+
+__global__ void k_step_end(TrainRun r) {
+  const long long s = *r.step;
+  if (r.loss_per_epoch) r.loss_per_epoch[s / r.steps_per_epoch] += *r.loss / (float)r.steps_per_epoch;
+  *r.step = s + 1;
+}
+
+struct RunLayout {
+  size_t ub, pb, gb, wb, grad, state, total;
+};
+
+static RunLayout run_layout(int64_t B) {
+  RunLayout L{};
+  size_t off = (ws_bytes(B) + 255) & ~(size_t)255;  // gal_mlp_loss_grads's workspace comes first
+  auto take = [&](size_t bytes) {
+    const size_t o = off;
+    off += (bytes + 255) & ~(size_t)255;
+    return o;
+  };
+  L.ub = take(sizeof(float) * 3 * B);
+  L.pb = take(sizeof(float) * B);
+  L.gb = take(sizeof(float) * 3 * B);
+  L.wb = take(sizeof(float) * B);
+  L.grad = take(sizeof(float) * NPARAM);
+  L.state = take(256);  // step counter, loss
+  L.total = off;
+  return L;
+}
+
 }  // namespace mlp
 }  // namespace gal
 
@@ -464,6 +576,97 @@ gal_status gal_mlp_train_step(float* params, float* grad, float* adam_m, float* 
                                                             eps, c1, c2);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? GAL_OK : cuda_fail(e, "MLP Adam update");
+}
+
+gal_status gal_mlp_train_workspace_size(int64_t batch, size_t* bytes) {
+  if (!bytes || batch < 1) return fail(GAL_ERR_INVALID_ARGUMENT, "batch >= 1 required");
+  if (batch > (int64_t)1 << 24) return fail(GAL_ERR_TOO_LARGE, "batch above 2^24 points");
+  *bytes = run_layout(batch).total;
+  return GAL_OK;
+}
+
+gal_status gal_mlp_train(float* params, float* adam_m, float* adam_v, const float* u, const float* phi_t,
+                         const float* g_t, const float* weights, int64_t n, int64_t batch, int32_t epochs, float alpha,
+                         float beta, float lr, float lr_final, float beta1, float beta2, float eps, uint64_t seed,
+                         int32_t quantize, float* loss_per_epoch, void* workspace, size_t workspace_bytes,
+                         gal_stream_t stream) {
+  if (!params || !adam_m || !adam_v || !u || !phi_t || !g_t || batch < 1 || epochs < 0 || n < batch)
+    return fail(GAL_ERR_INVALID_ARGUMENT, "bad gal_mlp_train arguments (n >= batch >= 1, epochs >= 0)");
+  if (batch > (int64_t)1 << 24 || n > ((int64_t)1 << 40)) return fail(GAL_ERR_TOO_LARGE, "batch or n too large");
+  const RunLayout RL = run_layout(batch);
+  if (!workspace || workspace_bytes < RL.total) return fail(GAL_ERR_WORKSPACE, "workspace too small");
+  if (epochs == 0) return GAL_OK;
+  char* ws = static_cast<char*>(workspace);
+  TrainRun r{};
+  r.u = u;
+  r.phi_t = phi_t;
+  r.g_t = g_t;
+  r.wt = weights;
+  r.n = n;
+  r.batch = batch;
+  r.steps_per_epoch = n / batch;
+  r.total = r.steps_per_epoch * epochs;
+  int bits = 1;
+  while (bits < 62 && ((int64_t)1 << bits) < n) ++bits;
+  r.hb = (bits + 1) / 2;
+  r.seed = seed;
+  r.ub = reinterpret_cast<float*>(ws + RL.ub);
+  r.pb = reinterpret_cast<float*>(ws + RL.pb);
+  r.gb = reinterpret_cast<float*>(ws + RL.gb);
+  r.wb = reinterpret_cast<float*>(ws + RL.wb);
+  r.step = reinterpret_cast<long long*>(ws + RL.state);
+  float* loss = reinterpret_cast<float*>(ws + RL.state + 8);
+  r.loss = loss;
+  r.loss_per_epoch = loss_per_epoch;
+  float* grad = reinterpret_cast<float*>(ws + RL.grad);
+  const Ws w = carve(workspace, batch);
+  const int q = quantize ? 1 : 0;
+  cudaStream_t caller = (cudaStream_t)stream;
+  // one step is captured on a private stream (the legacy default stream cannot
+  // be captured), ordered after and before the caller's stream
+  cudaStream_t s = nullptr;
+  cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_out, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventRecord(ev_in, caller);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(s, ev_in, 0);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ws + RL.state, 0, 256, s);
+  if (e == cudaSuccess && loss_per_epoch) e = cudaMemsetAsync(loss_per_epoch, 0, sizeof(float) * epochs, s);
+  auto one_step = [&]() {
+    k_gather<<<ew_grid(batch), 256, 0, s>>>(r);
+    loss_grads(s, params, r.ub, r.pb, r.gb, weights ? r.wb : nullptr, batch, alpha, beta, grad, loss, w, q);
+    k_adam_run<<<ew_grid(NPARAM), 256, 0, s>>>(params, grad, adam_m, adam_v, NPARAM, r.step, r.total, lr, lr_final,
+                                               beta1, beta2, eps);
+    k_step_end<<<1, 1, 0, s>>>(r);
+  };
+  if (e == cudaSuccess) {
+    // the first step runs uncaptured: it configures the tensor-core kernel
+    one_step();
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess && r.total > 1) {
+    e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+      one_step();
+      const cudaError_t e2 = cudaStreamEndCapture(s, &g);
+      e = e2 != cudaSuccess ? e2 : cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, g, 0);
+    for (int64_t k = 1; k < r.total && e == cudaSuccess; ++k) e = cudaGraphLaunch(exec, s);
+  }
+  if (ev_out && s) {
+    cudaEventRecord(ev_out, s);
+    cudaStreamWaitEvent(caller, ev_out, 0);
+  }
+  if (exec) cudaGraphExecDestroy(exec);
+  if (g) cudaGraphDestroy(g);
+  if (ev_in) cudaEventDestroy(ev_in);
+  if (ev_out) cudaEventDestroy(ev_out);
+  if (s) cudaStreamDestroy(s);  // returns at once; queued work still completes
+  return e == cudaSuccess ? GAL_OK : cuda_fail(e, "gal_mlp_train");
 }
 
 }  // extern "C"

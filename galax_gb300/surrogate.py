@@ -200,6 +200,7 @@ def train(x, phi, grad, *, length_scale: float, epochs: int = 30, batch: int = 8
     ph = _as_cuda(phi, torch.float64).reshape(-1)
     gr = _as_cuda(grad, torch.float64).reshape(-1, 3)
     n = xs.shape[0]
+    batch = min(batch, n)
     phi_scale = float(ph.std()) or 1.0
     u = (xs / length_scale).to(torch.float32)
     pt = (ph / phi_scale).to(torch.float32)
@@ -212,43 +213,32 @@ def train(x, phi, grad, *, length_scale: float, epochs: int = 30, batch: int = 8
         wts = (w / w.mean()).to(torch.float32)
         beta = 1.0 / float((wts.double() * g2).mean())
     P = torch.as_tensor(init_params(seed), device="cuda")
-    G = torch.zeros_like(P)
     M = torch.zeros_like(P)
     V = torch.zeros_like(P)
-    loss = torch.zeros(1, dtype=torch.float32, device="cuda")
     L = _lib.load()
     nb = C.c_size_t()
-    _lib.check(L.gal_mlp_workspace_size(batch, C.byref(nb)), "gal_mlp_workspace_size")
+    _lib.check(L.gal_mlp_train_workspace_size(batch, C.byref(nb)), "gal_mlp_train_workspace_size")
     ws = torch.zeros(nb.value, dtype=torch.uint8, device="cuda")  # zeroed: it holds the error flag
     st = torch.cuda.current_stream().cuda_stream
-    gen = torch.Generator(device="cuda").manual_seed(seed)
-    steps_per_epoch = n // batch
-    total = steps_per_epoch * epochs
-    rep = TrainReport(steps=total, epochs=epochs)
+    u, pt, gt = u.contiguous(), pt.contiguous(), gt.contiguous()
+    wts = wts.contiguous() if wts is not None else None
+    hist = torch.zeros(max(epochs, 1), dtype=torch.float32, device="cuda")
+    rep = TrainReport(steps=(n // batch) * epochs, epochs=epochs)
     t0 = time.perf_counter()
-    step = 0
-    for ep in range(epochs):
-        perm = torch.randperm(n, device="cuda", generator=gen)
-        ep_loss = torch.zeros(1, dtype=torch.float32, device="cuda")
-        for b in range(steps_per_epoch):
-            idx = perm[b * batch:(b + 1) * batch]
-            ub, pb, gb = u[idx].contiguous(), pt[idx].contiguous(), gt[idx].contiguous()
-            wb = wts[idx].contiguous() if wts is not None else None
-            step += 1
-            lr_t = lr_final + 0.5 * (lr - lr_final) * (1 + math.cos(math.pi * step / total))
-            _lib.check(L.gal_mlp_train_step(P.data_ptr(), G.data_ptr(), M.data_ptr(), V.data_ptr(), ub.data_ptr(),
-                                            pb.data_ptr(), gb.data_ptr(), wb.data_ptr() if wb is not None else None,
-                                            batch, alpha, beta, lr_t, 0.9, 0.999, 1e-8, step, int(quantize),
-                                            loss.data_ptr(), ws.data_ptr(), ws.numel(), st),
-                       "gal_mlp_train_step")
-            ep_loss += loss
-        rep.loss.append(float(ep_loss) / steps_per_epoch)
-        if log_every and (ep + 1) % log_every == 0:
-            print(f"epoch {ep + 1}: loss {rep.loss[-1]:.4e}", flush=True)
+    # whole epochs on the device: batches gathered through a keyed permutation,
+    # one CUDA graph per step (gal_mlp_train)
+    _lib.check(L.gal_mlp_train(P.data_ptr(), M.data_ptr(), V.data_ptr(), u.data_ptr(), pt.data_ptr(), gt.data_ptr(),
+                               wts.data_ptr() if wts is not None else None, n, batch, epochs, alpha, beta, lr,
+                               lr_final, 0.9, 0.999, 1e-8, seed, int(quantize), hist.data_ptr(), ws.data_ptr(),
+                               ws.numel(), st), "gal_mlp_train")
     code = C.c_int32()
     _lib.check(L.gal_mlp_workspace_error(ws.data_ptr(), batch, C.byref(code), st), "gal_mlp_workspace_error")
     if code.value:
         raise _lib.GalaxGB300Error(f"MLP training: a tensor-core product gave up waiting (code {code.value})")
+    rep.loss = hist[:epochs].cpu().tolist()
+    if log_every:
+        for ep in range(log_every - 1, epochs, log_every):
+            print(f"epoch {ep + 1}: loss {rep.loss[ep]:.4e}", flush=True)
     rep.seconds = time.perf_counter() - t0
     return MLPSurrogate(P.cpu().numpy(), length_scale, phi_scale), rep
 

@@ -425,6 +425,23 @@ GAL_API gal_status gal_mlp_train_step(float* params, float* grad, float* adam_m,
                                       float alpha, float beta, float lr, float beta1, float beta2, float eps,
                                       int32_t step, int32_t quantize, float* loss, void* workspace,
                                       size_t workspace_bytes, gal_stream_t stream);
+/* Train for `epochs` passes over n samples (u[n][3], phi_t[n], g_t[n][3],
+ * weights[n] or NULL) in batches of `batch` (n / batch steps per epoch; the
+ * remaining samples of a pass are left out), entirely on the device: each step
+ * gathers its batch through a keyed pseudo-random permutation of the samples
+ * (a new key every epoch, from `seed`), runs gal_mlp_loss_grads's kernels and
+ * an Adam step with the cosine schedule lr_t = lr_final + (lr - lr_final)
+ * (1 + cos(pi t / T)) / 2 (t = 1..T, T = all steps), and adds its loss / steps
+ * per epoch to loss_per_epoch[epoch] (may be NULL). One step is captured as a
+ * CUDA graph and replayed, so the host issues one launch per step. The
+ * workspace (gal_mlp_train_workspace_size) starts with the error flag of
+ * gal_mlp_workspace_error for `batch`; zero it before first use. */
+GAL_API gal_status gal_mlp_train_workspace_size(int64_t batch, size_t* bytes);
+GAL_API gal_status gal_mlp_train(float* params, float* adam_m, float* adam_v, const float* u, const float* phi_t,
+                                 const float* g_t, const float* weights, int64_t n, int64_t batch, int32_t epochs,
+                                 float alpha, float beta, float lr, float lr_final, float beta1, float beta2,
+                                 float eps, uint64_t seed, int32_t quantize, float* loss_per_epoch, void* workspace,
+                                 size_t workspace_bytes, gal_stream_t stream);
 /* Build inference weights (bfloat16 operand images) from a host parameter vector. */
 GAL_API gal_status gal_mlp_create(const float* params_host, double length_scale, double phi_scale, gal_mlp** out);
 GAL_API gal_status gal_mlp_destroy(gal_mlp* mlp);

@@ -264,7 +264,8 @@ def test_ctypes_argument_types_match_the_header():
     undefined); pointers and streams are bound as pointers."""
     from galax_gb300 import _lib
 
-    scalar = {"int32_t": C.c_int32, "int64_t": C.c_int64, "double": C.c_double, "float": C.c_float,
+    scalar = {"int32_t": C.c_int32, "int64_t": C.c_int64, "uint64_t": C.c_uint64, "double": C.c_double,
+              "float": C.c_float,
               "size_t": C.c_size_t}
     text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
     for name, params in re.findall(r"GAL_API\s+[\w\s\*]+?\b(gal_\w+)\((.*?)\);", text, flags=re.S):

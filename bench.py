@@ -127,7 +127,15 @@ def fp64_peak() -> dict:
         _lib.check(L.gal_fp64_peak_probe(20000, C.byref(ms), C.byref(fl), torch.cuda.current_stream().cuda_stream),
                    "gal_fp64_peak_probe")
         best = max(best, fl.value / (ms.value * 1e-3))
-    return {"tflops": best / 1e12, "how": "dependent-chain DFMA probe, 8 chains/thread, full-device grid, best of 3"}
+    import torch
+
+    props = torch.cuda.get_device_properties(torch.cuda.current_device())
+    mhz = measured_peaks().get("sm_max_mhz") or 2070.0
+    # issue ceiling: one FP64 FMA (2 flops) per SM sub-partition every other clock
+    ceiling = props.multi_processor_count * 4 * mhz * 1e6 / 1e12
+    return {"tflops": best / 1e12, "issue_ceiling_tflops": ceiling,
+            "how": "dependent-chain DFMA probe, 8 chains/thread, full-device grid, best of 3; issue ceiling = "
+                   "SMs x 4 flop/clk x max SM clock"}
 
 
 def measured_peaks() -> dict:
@@ -307,6 +315,8 @@ def run_ours(args) -> dict | None:
                 "ms_per_step": e2e_ms, "path": "pinned host -> gal_integrate -> pinned host (saves written by the "
                                                 "kernels into device-visible pinned memory)"},
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak["tflops"], "unit": "TFLOP/s",
+                     "issue_ceiling": peak["issue_ceiling_tflops"],
+                     "frac_of_issue_ceiling": achieved / peak["issue_ceiling_tflops"],
                      "frac": achieved / peak["tflops"], "traffic": traffic,
                      "flops_per_accepted_step": f_step,
                      "note": "FP64 pipe bound; achieved counts accepted steps only (rejected attempts, saves and "
@@ -456,6 +466,8 @@ def run_uneven_dopri8(steps: int = 2, warmup: int = 1) -> dict:
                        "orbits_not_finished": bad},
             "without_teams": {"ms_per_step": res[0][0], "value": res[0][1] / (res[0][0] * 1e-3)},
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak["tflops"], "unit": "TFLOP/s",
+                     "issue_ceiling": peak["issue_ceiling_tflops"],
+                     "frac_of_issue_ceiling": achieved / peak["issue_ceiling_tflops"],
                          "frac": achieved / peak["tflops"], "flops_per_accepted_step": STEP_FLOPS_MW[8]}}
 
 
@@ -576,6 +588,8 @@ def run_grad(args, n, rank, world, dist) -> dict | None:
         "e2e": {"value": n * world / (e2e_ms * 1e-3), "unit": "grads/s", "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": 2 * 6 * n * 8, "d2h_bytes_per_step": 6 * n * 8 + 12 * 8},
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak["tflops"], "unit": "TFLOP/s",
+                     "issue_ceiling": peak["issue_ceiling_tflops"],
+                     "frac_of_issue_ceiling": achieved / peak["issue_ceiling_tflops"],
                      "frac": achieved / peak["tflops"], "traffic": None,
                      "note": "algorithmic flops = 4 x Dopri8 forward step flops per step; peak measured live"},
         "clocks": clk, "gpu_launches": 2 * args.steps,
@@ -615,6 +629,8 @@ def run_plain(args, n, rank, world, dist) -> dict | None:
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": WORKLOADS["plain"], "orbits_per_gpu": n},
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak["tflops"], "unit": "TFLOP/s",
+                     "issue_ceiling": peak["issue_ceiling_tflops"],
+                     "frac_of_issue_ceiling": achieved / peak["issue_ceiling_tflops"],
                          "frac": achieved / peak["tflops"],
                          "note": "1,024 orbits occupy 8 of 152 SMs: latency-bound by construction"},
             "gpu_launches": args.steps}
@@ -824,6 +840,8 @@ def run_stream(args, n_rel, rank, world, dist) -> dict | None:
         "e2e": {"value": world / (e2e_ms * 1e-3), "unit": "gradients/s", "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": int(s.noise.size * 8 + target.numel() * 8), "d2h_bytes_per_step": 12 * 8},
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak["tflops"], "unit": "TFLOP/s",
+                     "issue_ceiling": peak["issue_ceiling_tflops"],
+                     "frac_of_issue_ceiling": achieved / peak["issue_ceiling_tflops"],
                      "frac": achieved / peak["tflops"], "traffic": None,
                      "note": "algorithmic flops = 4 x forward (particle steps x 2,562 + progenitor 2 x n_rel x 2,276), "
                              "the checkpointed adjoint's count, kept as the unit of work for both storage modes; "

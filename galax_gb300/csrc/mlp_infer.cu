@@ -3,17 +3,22 @@
 //
 // One CTA per SM, persistent over tiles of 128 points, warp-specialised (a
 // weight-copy warp, a tensor-core warp, eight epilogue warps). Per tile:
-//   layer 1 (3 -> 256) on CUDA cores -> h1 (bf16) into the shared-memory
+//   layer 1 (3 -> 256) on CUDA cores -> h1 (bf16) into a shared-memory
 //   operand tile; then six 128x256x256 products on the tensor cores
 //   (tcgen05.mma kind::f16, bf16 x bf16 -> f32 accumulator in TMEM):
 //     z2 = h1 W2^T, z3 = h2 W3^T, z4 = h3 W4^T           (forward)
 //     u3 = d4 W4,   u2 = d3 W3,   u1 = d2 W2              (input gradient)
 //   with d4 = silu'(z4) w5, d3 = silu'(z3) u3, d2 = silu'(z2) u2 (bf16), and
 //   grad_u out = (silu'(z1) u1) W1 on CUDA cores. silu'(z2), silu'(z3) wait in
-//   TMEM as packed bf16 pairs; every operand tile is rewritten in place.
-// Weights stream through a four-stage ring of 32 KB K-blocks (bulk copies from
-// pre-swizzled global images) run by their own warp ahead of the products. The numerics are those
-// of the training kernels' quantised forward/backward (mlp_train.cu).
+//   TMEM as packed bf16 pairs.
+// Every product runs as two N halves of 128 columns, committed separately, so
+// the epilogue of one half overlaps the tensor cores' work on the other, and
+// two operand tiles alternate so that an epilogue writes the next product's
+// operand while the current one is still read. The next product starts on K
+// 0..127 once the epilogue of half 0 has written those columns. Weights stream
+// through a ring of 16 KB N-halves of K-blocks (bulk copies from pre-swizzled
+// global images) run by their own warp ahead of the products. The numerics
+// are those of the training kernels' quantised forward/backward (mlp_train.cu).
 //
 // Every mbarrier wait is bounded: on timeout the kernel records an error code,
 // releases its TMEM and returns.
@@ -31,17 +36,19 @@ namespace gal {
 namespace mlp {
 
 constexpr int TILE = 128;
-constexpr int EPI_WARPS = 8;                            // two per TMEM lane quadrant: column halves
+constexpr int EPI_WARPS = 8;                            // two per TMEM lane quadrant
 constexpr int NTHREADS = 64 + 32 * EPI_WARPS;           // warp 0 copies weights, warp 1 issues products
-constexpr int STAGES = 4;
-constexpr uint32_t KBLOCK_BYTES = 256 * 128;           // 256 rows x 64 bf16
+constexpr int STAGES = 5;
+constexpr uint32_t HALF_BYTES = 128 * 128;              // one N half of a weight K-block: 128 rows x 64 bf16
+constexpr uint32_t KBLOCK_BYTES = 2 * HALF_BYTES;       // a K-block of the global image: 256 rows x 64 bf16
 constexpr int KBLOCKS_PER_GEMM = 4;
 constexpr int GEMMS = 6;
-constexpr int KBLOCKS_PER_TILE = GEMMS * KBLOCKS_PER_GEMM;  // 24
-constexpr uint32_t A_BYTES = TILE * 256 * 2;            // 64 KB
-constexpr uint32_t SMEM_A = 0;
-constexpr uint32_t SMEM_RING = A_BYTES;
-constexpr uint32_t SMEM_SMALL = SMEM_RING + STAGES * KBLOCK_BYTES;  // 192 KB
+constexpr int KBLOCKS_PER_TILE = GEMMS * KBLOCKS_PER_GEMM;  // 24 in the global image
+constexpr int HALVES_PER_TILE = 2 * KBLOCKS_PER_TILE;       // 48 ring entries per tile
+constexpr uint32_t A_BYTES = TILE * 256 * 2;            // 64 KB: one operand tile
+constexpr uint32_t SMEM_A = 0;                          // two operand tiles, ping-pong
+constexpr uint32_t SMEM_RING = 2 * A_BYTES;
+constexpr uint32_t SMEM_SMALL = SMEM_RING + STAGES * HALF_BYTES;
 constexpr int SMALL_FLOATS = H * 3 + 5 * H + 1;         // W1, b1, b2, b3, b4, w5, b5
 constexpr uint32_t SMEM_PART = SMEM_SMALL + ((SMALL_FLOATS * 4 + 255) / 256) * 256;
 constexpr uint32_t SMEM_READY = SMEM_PART + TILE * 4 * 4;
@@ -52,6 +59,7 @@ constexpr uint32_t WAIT_LIMIT = 1u << 24;
 constexpr uint32_t TMEM_COLS = 512;
 constexpr uint32_t COL_S2 = 256, COL_S3 = 384;          // packed silu'(z2), silu'(z3)
 static_assert(SMEM_ALLOC <= 227 * 1024, "shared memory budget");
+static_assert(2 * STAGES + 5 <= 32, "barriers fit their 256 bytes");
 
 struct InferArgs {
   const double* x;       // [3][n]
@@ -84,7 +92,7 @@ __device__ __forceinline__ void set_abort(volatile int* abort_flag, int* err, in
 // sigmoid from one SFU operation: 1 / (1 + e^-z) = (1 + tanh(z / 2)) / 2
 __device__ __forceinline__ float sig(float z) { return fmaf(0.5f, tc::tanh_approx(0.5f * z), 0.5f); }
 
-// write 32 consecutive hidden units [c, c+32) of row `row` into the operand tile
+// write 32 consecutive hidden units [c, c+32) of row `row` into an operand tile
 __device__ __forceinline__ void store_row32(uint8_t* tile, int row, int c, const float (&v)[32]) {
 #pragma unroll
   for (int q = 0; q < 4; ++q) {  // four 16-byte chunks of 8 values
@@ -98,16 +106,21 @@ __device__ __forceinline__ void store_row32(uint8_t* tile, int row, int c, const
 }
 
 // Warp-specialised, persistent over 128-point tiles:
-//   warp 0   : streams the 24 weight K-blocks of every tile through a 4-stage ring (bulk copies)
-//   warp 1   : allocates TMEM and issues the six 128x256x256 products per tile (tcgen05.mma)
-//   warps 2-9: epilogues, one thread per (point, half of the 256 hidden units); a warp may only
-//              touch its TMEM lane quadrant (warp id % 4), so each quadrant has two warps
-// Synchronisation: full/empty (ring), acc_full (products -> epilogue), op_ready (epilogue ->
-// products: operand tile rewritten and accumulator drained). Every wait is bounded.
+//   warp 0   : streams the weights of every tile through a ring of 16 KB N-halves of K-blocks
+//              (bulk copies), in the order the products consume them
+//   warp 1   : allocates TMEM and issues the six 128x256x256 products per tile (tcgen05.mma),
+//              each as two N halves of 128 columns
+//   warps 2-9: epilogues, one thread per (point, quarter of each half's columns); a warp may
+//              only touch its TMEM lane quadrant (warp id % 4), so each quadrant has two warps
+// Each product splits into its two N halves, committed separately (acc_full[h]), so the
+// epilogue of half 0 runs while half 1 is on the tensor cores; the epilogue writes the next
+// product's operand into the other of two operand tiles, half by half (op_ready[h]), and the
+// next product starts on the K range of half 0 while the epilogue of half 1 still runs.
+// Every wait is bounded.
 __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = smem_raw + ((1024 - (tc::smem_u32(smem_raw) & 1023)) & 1023);
-  uint8_t* tileA = smem + SMEM_A;
+  uint8_t* tiles = smem + SMEM_A;  // [2][A_BYTES]
   uint8_t* ring = smem + SMEM_RING;
   float* sm = reinterpret_cast<float*>(smem + SMEM_SMALL);
   const float* sW1 = sm;
@@ -121,9 +134,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + SMEM_BAR);
   uint64_t* full = bars;
   uint64_t* empty = bars + STAGES;
-  uint64_t* acc_full = bars + 2 * STAGES;
-  uint64_t* op_ready = acc_full + 1;
-  uint64_t* drain = op_ready + 1;
+  uint64_t* acc_full = bars + 2 * STAGES;  // [2]
+  uint64_t* op_ready = acc_full + 2;       // [2]
+  uint64_t* drain = op_ready + 2;
   uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(drain + 1);
   __shared__ int abort_s;
   volatile int* abort_flag = &abort_s;
@@ -138,8 +151,10 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
       tc::mbar_init(&full[s], 1);
       tc::mbar_init(&empty[s], 1);
     }
-    tc::mbar_init(acc_full, 1);
-    tc::mbar_init(op_ready, EPI_WARPS);
+    for (int h = 0; h < 2; ++h) {
+      tc::mbar_init(&acc_full[h], 1);
+      tc::mbar_init(&op_ready[h], EPI_WARPS);
+    }
     tc::mbar_init(drain, 1);
     tc::fence_barrier_init();
   }
@@ -157,7 +172,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
   if (warp == 0) {
     // ------------------------------------------------------------ weight producer
     if (lane == 0) {
-      const int64_t total = my_tiles * KBLOCKS_PER_TILE;
+      const int64_t total = my_tiles * HALVES_PER_TILE;
       int64_t j = 0;
       for (; j < total; ++j) {
         const int s = (int)(j % STAGES);
@@ -166,9 +181,13 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
           if (!*abort_flag) set_abort(abort_flag, a.err, 3);
           break;
         }
-        tc::mbar_expect_tx(&full[s], KBLOCK_BYTES);
-        tc::bulk_g2s(ring + (size_t)s * KBLOCK_BYTES, a.wimg + (size_t)(j % KBLOCKS_PER_TILE) * KBLOCK_BYTES,
-                     KBLOCK_BYTES, &full[s]);
+        // entry e of a tile: product g = e / 8, half h = (e / 4) % 2, K-block kb = e % 4
+        const int e = (int)(j % HALVES_PER_TILE);
+        const int g = e >> 3, h = (e >> 2) & 1, kb = e & 3;
+        tc::mbar_expect_tx(&full[s], HALF_BYTES);
+        tc::bulk_g2s(ring + (size_t)s * HALF_BYTES,
+                     a.wimg + (size_t)(g * KBLOCKS_PER_GEMM + kb) * KBLOCK_BYTES + (size_t)h * HALF_BYTES, HALF_BYTES,
+                     &full[s]);
       }
       // every copy issued must have landed before the CTA can exit (bounded)
       for (int64_t q = (j > STAGES ? j - STAGES : 0); q < j; ++q)
@@ -177,34 +196,38 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
   } else if (warp == 1) {
     // ------------------------------------------------------------ tensor-core products
     if (lane == 0) {
-      constexpr uint32_t idesc = tc::idesc_bf16(TILE, 256);
-      const uint32_t a_base = tc::smem_u32(tileA);
-      int64_t j = 0, q = 0;
+      constexpr uint32_t idesc = tc::idesc_bf16(TILE, 128);
+      int64_t j = 0, q = 0;  // ring entries consumed; products started (op_ready phases)
       bool ok = true;
+      auto run_blocks = [&](uint32_t a_base, int h, int kb0, int kb1) -> bool {
+        for (int kb = kb0; kb < kb1; ++kb, ++j) {
+          const int s = (int)(j % STAGES);
+          if (!wait_bar(&full[s], (uint32_t)((j / STAGES) & 1), abort_flag)) return false;
+          tc::tc_fence_after();
+          const uint32_t b_base = tc::smem_u32(ring + (size_t)s * HALF_BYTES);
+#pragma unroll
+          for (int ks = 0; ks < 4; ++ks) {
+            const uint64_t ad = tc::desc_sw128(a_base + kb * (TILE * 128) + ks * 32);
+            const uint64_t bd = tc::desc_sw128(b_base + ks * 32);
+            tc::mma_bf16(tmem + (uint32_t)(h * 128), ad, bd, idesc, (kb | ks) != 0);
+          }
+          tc::mma_commit(&empty[s]);  // stage free once these products complete
+        }
+        return true;
+      };
       for (int64_t it = 0; it < my_tiles && ok; ++it) {
         for (int g = 0; g < GEMMS && ok; ++g, ++q) {
-          if (!wait_bar(op_ready, (uint32_t)(q & 1), abort_flag)) {
-            ok = false;
-            break;
-          }
+          const uint32_t a_base = tc::smem_u32(tiles + (size_t)(g & 1) * A_BYTES);
+          // half 0 over K 0..127 as soon as the first half of the operand is written
+          if (!wait_bar(&op_ready[0], (uint32_t)(q & 1), abort_flag)) { ok = false; break; }
           tc::tc_fence_after();
-          for (int kb = 0; kb < KBLOCKS_PER_GEMM; ++kb, ++j) {
-            const int s = (int)(j % STAGES);
-            if (!wait_bar(&full[s], (uint32_t)((j / STAGES) & 1), abort_flag)) {
-              ok = false;
-              break;
-            }
-            tc::tc_fence_after();
-            const uint32_t b_base = tc::smem_u32(ring + (size_t)s * KBLOCK_BYTES);
-#pragma unroll
-            for (int ks = 0; ks < 4; ++ks) {
-              const uint64_t ad = tc::desc_sw128(a_base + kb * (TILE * 128) + ks * 32);
-              const uint64_t bd = tc::desc_sw128(b_base + ks * 32);
-              tc::mma_bf16(tmem, ad, bd, idesc, (kb | ks) != 0);
-            }
-            tc::mma_commit(&empty[s]);  // stage free once these products complete
-          }
-          if (ok) tc::mma_commit(acc_full);
+          if (!run_blocks(a_base, 0, 0, 2)) { ok = false; break; }
+          if (!wait_bar(&op_ready[1], (uint32_t)(q & 1), abort_flag)) { ok = false; break; }
+          tc::tc_fence_after();
+          if (!run_blocks(a_base, 0, 2, 4)) { ok = false; break; }
+          tc::mma_commit(&acc_full[0]);
+          if (!run_blocks(a_base, 1, 0, 4)) { ok = false; break; }
+          tc::mma_commit(&acc_full[1]);
         }
       }
       if (!ok && !*abort_flag) set_abort(abort_flag, a.err, 4);
@@ -217,10 +240,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
     const int e = warp - 2;
     const int quad = warp & 3;
     const int row = quad * 32 + lane;
-    const int hh = e >= 4 ? 1 : 0;
-    const int c0 = hh * 128;
+    const int qq = e >= 4 ? 1 : 0;  // which 64-column quarter of each half
     const uint32_t lane_base = (uint32_t)(quad * 32) << 16;
-    int64_t q = 0;
+    int64_t q = 0;  // acc_full phases
     for (int64_t it = 0; it < my_tiles; ++it) {
       if (*abort_flag) break;
       const int64_t tile = blockIdx.x + it * gridDim.x;
@@ -231,32 +253,38 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
 #pragma unroll
         for (int j = 0; j < 3; ++j) u[j] = (float)(a.x[j * a.n + gi] * a.inv_length);
       }
-      // layer 1 on CUDA cores: h1 = silu(W1 u + b1) -> operand tile
-      for (int c = c0; c < c0 + 128; c += 32) {
-        float v[32];
+      // layer 1 on CUDA cores: h1 = silu(W1 u + b1) -> operand tile 0, half by half
+      for (int h = 0; h < 2; ++h) {
+        const int cbase = h * 128 + qq * 64;
+        for (int c = cbase; c < cbase + 64; c += 32) {
+          float v[32];
 #pragma unroll
-        for (int k = 0; k < 32; ++k) {
-          const int cc = c + k;
-          const float z = fmaf(sW1[3 * cc], u[0], fmaf(sW1[3 * cc + 1], u[1], fmaf(sW1[3 * cc + 2], u[2], sb1[cc])));
-          v[k] = z * sig(z);
+          for (int k = 0; k < 32; ++k) {
+            const int cc = c + k;
+            const float z =
+                fmaf(sW1[3 * cc], u[0], fmaf(sW1[3 * cc + 1], u[1], fmaf(sW1[3 * cc + 2], u[2], sb1[cc])));
+            v[k] = z * sig(z);
+          }
+          store_row32(tiles, row, c, v);
         }
-        store_row32(tileA, row, c, v);
+        tc::fence_proxy_async_smem();
+        tc::tc_fence_before();
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(&op_ready[h]);
       }
-      tc::fence_proxy_async_smem();
-      __syncwarp();
-      if (lane == 0) tc::mbar_arrive(op_ready);
       float gpart[3] = {0.f, 0.f, 0.f};
       float ppart = 0.f;
       bool ok = true;
-      for (int g = 0; g < GEMMS; ++g, ++q) {
-        if (!wait_bar(acc_full, (uint32_t)(q & 1), abort_flag)) {
-          if (!*abort_flag) set_abort(abort_flag, a.err, 2);
-          ok = false;
-          break;
-        }
-        tc::tc_fence_after();
-        // two 32-column chunks per TMEM round trip
-        for (int c = c0; c < c0 + 128; c += 64) {
+      for (int g = 0; g < GEMMS && ok; ++g) {
+        uint8_t* tile_out = tiles + (size_t)((g + 1) & 1) * A_BYTES;
+        for (int h = 0; h < 2; ++h, ++q) {
+          if (!wait_bar(&acc_full[h], (uint32_t)((q >> 1) & 1), abort_flag)) {
+            if (!*abort_flag) set_abort(abort_flag, a.err, 2);
+            ok = false;
+            break;
+          }
+          tc::tc_fence_after();
+          const int c = h * 128 + qq * 64;  // this thread's 64 columns of half h
           uint32_t acc0[32], acc1[32], sp0[16], sp1[16];
           tc::tmem_ld32(tmem + lane_base + (uint32_t)c, acc0);
           tc::tmem_ld32(tmem + lane_base + (uint32_t)(c + 32), acc1);
@@ -272,7 +300,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
             const uint32_t(&sp)[16] = half ? sp1 : sp0;
             const int cc0 = c + 32 * half;
             float v[32];
-            if (g <= 1) {  // z2 / z3: h = silu(z) -> tile, silu'(z) -> TMEM
+            if (g <= 1) {  // z2 / z3: h = silu(z) -> operand tile, silu'(z) -> TMEM
               const float* bb = g == 0 ? sb2 : sb3;
               uint32_t spk[16];
 #pragma unroll
@@ -285,8 +313,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
                 spk[k / 2] = tc::pack_bf16x2(s0 * fmaf(z0, 1.f - s0, 1.f), s1 * fmaf(z1, 1.f - s1, 1.f));
               }
               tc::tmem_st16(tmem + lane_base + (uint32_t)((g == 0 ? COL_S2 : COL_S3) + cc0 / 2), spk);
-              store_row32(tileA, row, cc0, v);
-            } else if (g == 2) {  // z4: d4 = silu'(z4) w5 -> tile; out = w5 . silu(z4)
+              store_row32(tile_out, row, cc0, v);
+            } else if (g == 2) {  // z4: d4 = silu'(z4) w5 -> operand tile; out = w5 . silu(z4)
 #pragma unroll
               for (int k = 0; k < 32; ++k) {
                 const float z = __uint_as_float(acc[k]) + sb4[cc0 + k];
@@ -294,14 +322,14 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
                 ppart = fmaf(z * sg, sw5[cc0 + k], ppart);
                 v[k] = sg * fmaf(z, 1.f - sg, 1.f) * sw5[cc0 + k];
               }
-              store_row32(tileA, row, cc0, v);
-            } else if (g <= 4) {  // u3 / u2: d = silu'(z) u -> tile
+              store_row32(tile_out, row, cc0, v);
+            } else if (g <= 4) {  // u3 / u2: d = silu'(z) u -> operand tile
 #pragma unroll
               for (int k = 0; k < 32; k += 2) {
                 v[k] = tc::bf16_lo(sp[k / 2]) * __uint_as_float(acc[k]);
                 v[k + 1] = tc::bf16_hi(sp[k / 2]) * __uint_as_float(acc[k + 1]);
               }
-              store_row32(tileA, row, cc0, v);
+              store_row32(tile_out, row, cc0, v);
             } else {  // u1: grad_u out = sum_c silu'(z1_c) u1_c W1[c]
 #pragma unroll
               for (int k = 0; k < 32; ++k) {
@@ -316,18 +344,18 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
               }
             }
           }
-        }
-        if (g <= 1) tc::tmem_wait_st();
-        if (g < GEMMS - 1) {
-          tc::fence_proxy_async_smem();
-          tc::tc_fence_before();
-          __syncwarp();
-          if (lane == 0) tc::mbar_arrive(op_ready);
+          if (g <= 1) tc::tmem_wait_st();
+          if (g < GEMMS - 1) {  // this half of the next operand written, this half of the accumulator drained
+            tc::fence_proxy_async_smem();
+            tc::tc_fence_before();
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(&op_ready[h]);
+          }
         }
       }
       if (!ok) break;
-      // combine the two halves of each row (bounded hand-off through shared memory)
-      if (hh == 1) {
+      // combine the two column quarters of each row (bounded hand-off through shared memory)
+      if (qq == 1) {
         part[row * 4 + 0] = gpart[0];
         part[row * 4 + 1] = gpart[1];
         part[row * 4 + 2] = gpart[2];

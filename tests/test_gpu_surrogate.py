@@ -116,6 +116,28 @@ def test_tensor_core_inference_matches_fp32(env, n):
     torch.cuda.synchronize()
 
 
+@pytest.mark.parametrize("n", [300, 40000])
+def test_tensor_core_inference_matches_numpy_bf16(env, n):
+    """The tensor-core kernel against the NumPy restatement of the quantised
+    network (oracle/mlp_oracle.py: bf16 weights and activations entering the
+    256x256 products, FP32 accumulation), directly. Beyond bf16 rounding the
+    kernel's sigmoid comes from one tanh.approx (~2^-11 relative) and its
+    silu' is stored as bf16, so agreement is to a few bf16 units."""
+    gx, S = env
+    p = _params(S)
+    length, pscale = 50.0, 3e-3
+    mlp = S.MLPSurrogate(p, length, pscale)
+    rng = np.random.default_rng(15)
+    x = rng.normal(size=(n, 3)) * 30.0
+    g, phi = mlp.evaluate(x, potential=True)
+    out_r, g_r = M.forward_bf16(_as_oracle(S, p), x / length)
+    g_r = g_r * (pscale / length)
+    phi_r = out_r * pscale
+    rel = np.linalg.norm(g - g_r, axis=1) / np.linalg.norm(g_r, axis=1)
+    assert np.median(rel) < 5e-3 and np.percentile(rel, 99) < 3e-2
+    assert np.median(np.abs(phi - phi_r)) < 2e-3 * np.abs(phi_r).mean()
+
+
 def test_zero_network_surrogate_equals_plain_integrator(env):
     """With an MLP whose output is identically zero the surrogate integrator must
     reproduce the plain constant-step Dopri5 kernel on the analytic part, to

@@ -170,6 +170,48 @@ __global__ void k_colsum(const float* X, const float* Y, const float* v, int64_t
   if (threadIdx.x == 0) out[c] = accumulate ? out[c] + red[0] : red[0];
 }
 
+// Column sums over the B rows of a [B][H] array in two deterministic passes:
+// k_colpart sums f(b, c) over 64-row chunks (thread c reads column c, so a
+// warp reads 32 consecutive columns of a row), k_colfinal adds the chunks in
+// order. f: mode 0 X[b,c]; 1 X[b,c] v[b]; 2 silu'(X[b,c]) Y[b,c];
+// 3 X[b,c] V[b][j] for j = 0..2, out[c][3] (the first layer's weight gradient).
+constexpr int kColRows = 64;
+
+__global__ void __launch_bounds__(256) k_colpart(const float* X, const float* Y, const float* v, const float* V,
+                                                 int64_t rows, int mode, float* part) {
+  const int c = threadIdx.x;
+  const int64_t r0 = (int64_t)blockIdx.x * kColRows;
+  const int64_t r1 = r0 + kColRows < rows ? r0 + kColRows : rows;
+  float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f;
+  for (int64_t b = r0; b < r1; ++b) {
+    const float x = X[b * H + c];
+    if (mode == 0) s0 += x;
+    else if (mode == 1) s0 += x * v[b];
+    else if (mode == 2) s0 += dsilu(x) * Y[b * H + c];
+    else {
+      s0 = fmaf(x, V[b * 3 + 0], s0);
+      s1 = fmaf(x, V[b * 3 + 1], s1);
+      s2 = fmaf(x, V[b * 3 + 2], s2);
+    }
+  }
+  float* p = part + ((int64_t)blockIdx.x * H + c) * 3;
+  p[0] = s0;
+  p[1] = s1;
+  p[2] = s2;
+}
+
+__global__ void __launch_bounds__(256) k_colfinal(const float* part, int64_t chunks, int mode, float* out,
+                                                  int accumulate) {
+  const int c = threadIdx.x;
+  const int nj = mode == 3 ? 3 : 1;
+  for (int j = 0; j < nj; ++j) {
+    float s = 0.0f;
+    for (int64_t k = 0; k < chunks; ++k) s += part[(k * H + c) * 3 + j];
+    float* o = out + (int64_t)c * nj + j;
+    *o = accumulate ? *o + s : s;
+  }
+}
+
 // residuals, their loss weights and the loss value
 // (optional per-point weights wt[b] multiply both terms of point b)
 __global__ void k_loss(const float* out, const float* G, const float* phi_t, const float* g_t, const float* wt,
@@ -211,12 +253,16 @@ __global__ void k_adam(float* p, const float* g, float* m, float* v, int64_t n, 
 
 struct Ws {
   float *Z[5], *Hh[5], *D[5], *U[4], *Zb[5], *Db, *Ub, *Hb, *out, *G, *Pb, *Eb;
+  float* colpart;  // [chunks][H][3] partial column sums
   int* err;  // set by a tensor-core product that gave up waiting (gal_mlp_workspace_error)
 };
 
+static int64_t col_chunks(int64_t B) { return (B + kColRows - 1) / kColRows; }
+
 static size_t ws_bytes(int64_t B) {
   const size_t big = sizeof(float) * (size_t)B * H;
-  return big * (4 + 4 + 4 + 3 + 4 + 3) + sizeof(float) * (size_t)B * (1 + 3 + 1 + 3) + 64 * 256;
+  return big * (4 + 4 + 4 + 3 + 4 + 3) + sizeof(float) * (size_t)B * (1 + 3 + 1 + 3) +
+         sizeof(float) * (size_t)col_chunks(B) * H * 3 + 64 * 256;
 }
 
 static Ws carve(void* ws, int64_t B) {
@@ -241,6 +287,7 @@ static Ws carve(void* ws, int64_t B) {
   w.Pb = take(sizeof(float) * B);
   w.Eb = take(sizeof(float) * B * 3);
   w.err = reinterpret_cast<int*>(take(256));
+  w.colpart = take(sizeof(float) * (size_t)col_chunks(B) * H * 3);
   return w;
 }
 
@@ -322,6 +369,13 @@ static void gemm(cudaStream_t s, int* err, int M, int N, int K, const float* A, 
   k_gemm<TA, TB><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc, 1.0f, beta, bias, qa, qb);
 }
 
+static void colsum(cudaStream_t s, const Ws& w, const float* X, const float* Y, const float* v, const float* V,
+                   int64_t B, int mode, float* out, int accumulate) {
+  const int64_t chunks = col_chunks(B);
+  k_colpart<<<(unsigned)chunks, H, 0, s>>>(X, Y, v, V, B, mode, w.colpart);
+  k_colfinal<<<1, H, 0, s>>>(w.colpart, chunks, mode, out, accumulate);
+}
+
 static unsigned ew_grid(int64_t n) {
   int64_t g = (n + 255) / 256;
   return (unsigned)(g > 4096 ? 4096 : (g < 1 ? 1 : g));
@@ -360,7 +414,7 @@ static void loss_grads(cudaStream_t s, const float* P, const float* x, const flo
   cudaMemsetAsync(loss, 0, sizeof(float), s);
   k_loss<<<ew_grid(B), 256, 0, s>>>(w.out, w.G, phi_t, g_t, wt, B, alpha, beta, w.Pb, w.Eb, loss);
   // ---- through the input-gradient graph, layer 1 up to 4
-  gemm<true, false>(s, w.err, H, 3, Bi, w.D[1], H, w.Eb, 3, grad + OFF_W1, 3);                       // gW1 = D1^T Eb
+  colsum(s, w, w.D[1], nullptr, nullptr, w.Eb, B, 3, grad + OFF_W1, 0);                             // gW1 = D1^T Eb
   gemm<false, true>(s, w.err, Bi, H, 3, w.Eb, 3, P + OFF_W1, 3, w.Db, H);                           // Db1 = Eb W1^T
   k_dd<<<ew_grid(n), 256, 0, s>>>(w.Z[1], w.U[1], w.Db, w.Ub, w.Zb[1], n, 0);
   gemm<true, false>(s, w.err, H, H, Bi, w.D[2], H, w.Ub, H, grad + OFF_W2, H, 0.0f, nullptr, q, 0);                      // gW2 = D2^T Ub1
@@ -371,25 +425,25 @@ static void loss_grads(cudaStream_t s, const float* P, const float* x, const flo
   k_dd<<<ew_grid(n), 256, 0, s>>>(w.Z[3], w.U[3], w.Db, w.Ub, w.Zb[3], n, q);
   gemm<true, false>(s, w.err, H, H, Bi, w.D[4], H, w.Ub, H, grad + OFF_W4, H, 0.0f, nullptr, q, 0);                      // gW4 = D4^T Ub3
   gemm<false, true>(s, w.err, Bi, H, H, w.Ub, H, P + OFF_W4, H, w.Db, H, 0.0f, nullptr, 0, q);      // Db4 = Ub3 W4^T
-  k_colsum<<<H, 256, 0, s>>>(w.Z[4], w.Db, nullptr, B, H, grad + OFF_W5, 2, 0);              // gw5 = sum silu'(Z4) Db4
+  colsum(s, w, w.Z[4], w.Db, nullptr, nullptr, B, 2, grad + OFF_W5, 0);                   // gw5 = sum silu'(Z4) Db4
   k_zb4<<<ew_grid(n), 256, 0, s>>>(w.Z[4], w.Db, w.Pb, P + OFF_W5, w.Zb[4], n);
   // ---- potential term and the forward graph, layer 4 down to 1
-  k_colsum<<<H, 256, 0, s>>>(w.Hh[4], nullptr, w.Pb, B, H, grad + OFF_W5, 1, 1);             // gw5 += H4^T Pb
+  colsum(s, w, w.Hh[4], nullptr, w.Pb, nullptr, B, 1, grad + OFF_W5, 1);                  // gw5 += H4^T Pb
   k_colsum<<<1, 256, 0, s>>>(w.Pb, nullptr, nullptr, B, 1, grad + OFF_B5, 0, 0);             // gb5
   gemm<true, false>(s, w.err, H, H, Bi, w.Zb[4], H, w.Hh[3], H, grad + OFF_W4, H, 1.0f, nullptr, 0, q);            // gW4 += Zb4^T H3
-  k_colsum<<<H, 256, 0, s>>>(w.Zb[4], nullptr, nullptr, B, H, grad + OFF_B4, 0, 0);
+  colsum(s, w, w.Zb[4], nullptr, nullptr, nullptr, B, 0, grad + OFF_B4, 0);
   gemm<false, false>(s, w.err, Bi, H, H, w.Zb[4], H, P + OFF_W4, H, w.Hb, H, 0.0f, nullptr, 0, q);  // Hb3 = Zb4 W4
   k_zb_acc<<<ew_grid(n), 256, 0, s>>>(w.Z[3], w.Hb, w.Zb[3], n);
   gemm<true, false>(s, w.err, H, H, Bi, w.Zb[3], H, w.Hh[2], H, grad + OFF_W3, H, 1.0f, nullptr, 0, q);
-  k_colsum<<<H, 256, 0, s>>>(w.Zb[3], nullptr, nullptr, B, H, grad + OFF_B3, 0, 0);
+  colsum(s, w, w.Zb[3], nullptr, nullptr, nullptr, B, 0, grad + OFF_B3, 0);
   gemm<false, false>(s, w.err, Bi, H, H, w.Zb[3], H, P + OFF_W3, H, w.Hb, H, 0.0f, nullptr, 0, q);
   k_zb_acc<<<ew_grid(n), 256, 0, s>>>(w.Z[2], w.Hb, w.Zb[2], n);
   gemm<true, false>(s, w.err, H, H, Bi, w.Zb[2], H, w.Hh[1], H, grad + OFF_W2, H, 1.0f, nullptr, 0, q);
-  k_colsum<<<H, 256, 0, s>>>(w.Zb[2], nullptr, nullptr, B, H, grad + OFF_B2, 0, 0);
+  colsum(s, w, w.Zb[2], nullptr, nullptr, nullptr, B, 0, grad + OFF_B2, 0);
   gemm<false, false>(s, w.err, Bi, H, H, w.Zb[2], H, P + OFF_W2, H, w.Hb, H, 0.0f, nullptr, 0, q);
   k_zb_acc<<<ew_grid(n), 256, 0, s>>>(w.Z[1], w.Hb, w.Zb[1], n);
-  gemm<true, false>(s, w.err, H, 3, Bi, w.Zb[1], H, x, 3, grad + OFF_W1, 3, 1.0f);                  // gW1 += Zb1^T X
-  k_colsum<<<H, 256, 0, s>>>(w.Zb[1], nullptr, nullptr, B, H, grad + OFF_B1, 0, 0);
+  colsum(s, w, w.Zb[1], nullptr, nullptr, x, B, 3, grad + OFF_W1, 1);                                // gW1 += Zb1^T X
+  colsum(s, w, w.Zb[1], nullptr, nullptr, nullptr, B, 0, grad + OFF_B1, 0);
 }
 
 // ---------------------------------------------------------------- device-driven training

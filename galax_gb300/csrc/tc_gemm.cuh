@@ -71,38 +71,57 @@ __device__ __forceinline__ uint16_t bf16_bits(float f) {
 
 // Load rows [r0, r0+R) x k [k0, k0+64) of an operand into the hi (and lo)
 // images of one stage. Consecutive threads take consecutive 8-element chunks
-// along the contiguous dimension of the source, so global reads coalesce.
+// along the contiguous dimension of the source, so global reads coalesce; a
+// thread issues the loads of 8 chunks before it converts and stores any, so
+// that their latencies overlap.
 template <int R>
 __device__ __forceinline__ void load_block(uint8_t* hi, uint8_t* lo, const float* src, int64_t s_row, int64_t s_k,
                                            int r0, int rlim, int k0, int klim, int split) {
+  constexpr int PER = R * 8 / NTHREADS;  // chunks per thread: 8 (A) or 16 (B)
+  constexpr int BATCH = 8;
+  static_assert(PER % BATCH == 0, "whole batches");
   const bool kmajor = s_k == 1;
-  for (int i = threadIdx.x; i < R * 8; i += NTHREADS) {
-    const int row = kmajor ? (i >> 3) : (i % R);
-    const int c = kmajor ? (i & 7) : (i / R);
-    const int gr = r0 + row, k = k0 + 8 * c;
-    float v[8];
-    if (kmajor && gr < rlim && k + 8 <= klim && ((reinterpret_cast<uintptr_t>(src + gr * s_row + k) & 15) == 0)) {
-      const float4 a = *reinterpret_cast<const float4*>(src + gr * s_row + k);
-      const float4 b = *reinterpret_cast<const float4*>(src + gr * s_row + k + 4);
-      v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
-    } else {
+#pragma unroll 1
+  for (int b0 = 0; b0 < PER; b0 += BATCH) {
+    float v[BATCH][8];
+    int rows[BATCH], cs[BATCH];
 #pragma unroll
-      for (int j = 0; j < 8; ++j) v[j] = (gr < rlim && k + j < klim) ? src[gr * s_row + (int64_t)(k + j) * s_k] : 0.0f;
-    }
-    uint32_t h[4], l[4];
+    for (int u = 0; u < BATCH; ++u) {
+      const int i = threadIdx.x + (b0 + u) * NTHREADS;
+      const int row = kmajor ? (i >> 3) : (i % R);
+      const int c = kmajor ? (i & 7) : (i / R);
+      rows[u] = row;
+      cs[u] = c;
+      const int gr = r0 + row, k = k0 + 8 * c;
+      if (kmajor && gr < rlim && k + 8 <= klim &&
+          ((reinterpret_cast<uintptr_t>(src + gr * s_row + k) & 15) == 0)) {
+        const float4 a = __ldg(reinterpret_cast<const float4*>(src + gr * s_row + k));
+        const float4 b = __ldg(reinterpret_cast<const float4*>(src + gr * s_row + k + 4));
+        v[u][0] = a.x; v[u][1] = a.y; v[u][2] = a.z; v[u][3] = a.w;
+        v[u][4] = b.x; v[u][5] = b.y; v[u][6] = b.z; v[u][7] = b.w;
+      } else {
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const uint16_t h0 = bf16_bits(v[2 * j]), h1 = bf16_bits(v[2 * j + 1]);
-      h[j] = (uint32_t)h0 | ((uint32_t)h1 << 16);
-      if (split) {
-        const uint16_t l0 = bf16_bits(v[2 * j] - __uint_as_float((uint32_t)h0 << 16));
-        const uint16_t l1 = bf16_bits(v[2 * j + 1] - __uint_as_float((uint32_t)h1 << 16));
-        l[j] = (uint32_t)l0 | ((uint32_t)l1 << 16);
+        for (int j = 0; j < 8; ++j)
+          v[u][j] = (gr < rlim && k + j < klim) ? __ldg(src + gr * s_row + (int64_t)(k + j) * s_k) : 0.0f;
       }
     }
-    const uint32_t off = tc::sw128_offset(R, row, 8 * c);
-    *reinterpret_cast<uint4*>(hi + off) = make_uint4(h[0], h[1], h[2], h[3]);
-    if (split) *reinterpret_cast<uint4*>(lo + off) = make_uint4(l[0], l[1], l[2], l[3]);
+#pragma unroll
+    for (int u = 0; u < BATCH; ++u) {
+      uint32_t h[4], l[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const uint16_t h0 = bf16_bits(v[u][2 * j]), h1 = bf16_bits(v[u][2 * j + 1]);
+        h[j] = (uint32_t)h0 | ((uint32_t)h1 << 16);
+        if (split) {
+          const uint16_t l0 = bf16_bits(v[u][2 * j] - __uint_as_float((uint32_t)h0 << 16));
+          const uint16_t l1 = bf16_bits(v[u][2 * j + 1] - __uint_as_float((uint32_t)h1 << 16));
+          l[j] = (uint32_t)l0 | ((uint32_t)l1 << 16);
+        }
+      }
+      const uint32_t off = tc::sw128_offset(R, rows[u], 8 * cs[u]);
+      *reinterpret_cast<uint4*>(hi + off) = make_uint4(h[0], h[1], h[2], h[3]);
+      if (split) *reinterpret_cast<uint4*>(lo + off) = make_uint4(l[0], l[1], l[2], l[3]);
+    }
   }
 }
 

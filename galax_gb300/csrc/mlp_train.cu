@@ -200,15 +200,28 @@ __global__ void __launch_bounds__(256) k_colpart(const float* X, const float* Y,
   p[2] = s2;
 }
 
+// 32 columns per block; the 8 warps sum interleaved chunks, then one warp adds
+// the 8 partial sums in a fixed order.
 __global__ void __launch_bounds__(256) k_colfinal(const float* part, int64_t chunks, int mode, float* out,
                                                   int accumulate) {
-  const int c = threadIdx.x;
+  __shared__ float red[8][32][3];
+  const int cl = threadIdx.x & 31, g = threadIdx.x >> 5;
+  const int c = blockIdx.x * 32 + cl;
   const int nj = mode == 3 ? 3 : 1;
   for (int j = 0; j < nj; ++j) {
     float s = 0.0f;
-    for (int64_t k = 0; k < chunks; ++k) s += part[(k * H + c) * 3 + j];
-    float* o = out + (int64_t)c * nj + j;
-    *o = accumulate ? *o + s : s;
+    for (int64_t k = g; k < chunks; k += 8) s += part[(k * H + c) * 3 + j];
+    red[g][cl][j] = s;
+  }
+  __syncthreads();
+  if (g == 0) {
+    for (int j = 0; j < nj; ++j) {
+      float s = 0.0f;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) s += red[q][cl][j];
+      float* o = out + (int64_t)c * nj + j;
+      *o = accumulate ? *o + s : s;
+    }
   }
 }
 
@@ -373,7 +386,7 @@ static void colsum(cudaStream_t s, const Ws& w, const float* X, const float* Y, 
                    int64_t B, int mode, float* out, int accumulate) {
   const int64_t chunks = col_chunks(B);
   k_colpart<<<(unsigned)chunks, H, 0, s>>>(X, Y, v, V, B, mode, w.colpart);
-  k_colfinal<<<1, H, 0, s>>>(w.colpart, chunks, mode, out, accumulate);
+  k_colfinal<<<H / 32, 256, 0, s>>>(w.colpart, chunks, mode, out, accumulate);
 }
 
 static unsigned ew_grid(int64_t n) {

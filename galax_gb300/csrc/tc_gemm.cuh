@@ -14,14 +14,15 @@
 // bits per operand: the FP32 reference gradients of the loss need that, the
 // quantised forward pass does not.
 //
-// One CTA of 128 threads computes a 128 x 256 tile of C; K runs in blocks of 64
-// through two shared-memory stages (96 KB each: A hi/lo 128 x 64, B hi/lo
-// 256 x 64, K-major, 128-byte swizzle, the layout of the inference kernel's
-// operands). All threads load and convert; thread 0 issues the products and
-// commits them to the stage's mbarrier, which frees the stage for the block
-// after next. The accumulator (256 TMEM columns) drains through shared memory
-// so that C is read and written row-contiguously. With gridDim.z > 1 each z
-// takes a K range and adds its partial tile into C with atomics.
+// One CTA of 256 threads computes a 128 x 128 tile of C (so the 8192 x 256
+// products of a training batch spread over 128 CTAs); K runs in blocks of 64
+// through two shared-memory stages (64 KB each: A and B hi/lo, 128 x 64,
+// K-major, 128-byte swizzle, the layout of the inference kernel's operands).
+// All threads load and convert; thread 0 issues the products and commits them
+// to the stage's mbarrier, which frees the stage for the block after next. The
+// accumulator (128 TMEM columns) drains through shared memory so that C is
+// read and written row-contiguously. With gridDim.z > 1 each z takes a K
+// range and adds its partial tile into C with atomics.
 //
 // Every mbarrier wait is bounded; on timeout the kernel records an error code,
 // waits (bounded) for its products, releases TMEM and returns.
@@ -36,12 +37,12 @@
 namespace gal {
 namespace tcg {
 
-constexpr int BM = 128, BN = 256, BK = 64;
-constexpr int NTHREADS = 128;
+constexpr int BM = 128, BN = 128, BK = 64;
+constexpr int NTHREADS = 256;
 constexpr uint32_t A_BLK = BM * 128;  // 16 KB: 128 rows x 64 bf16
-constexpr uint32_t B_BLK = BN * 128;  // 32 KB
+constexpr uint32_t B_BLK = BN * 128;  // 16 KB
 constexpr uint32_t STAGE_BYTES = 2 * A_BLK + 2 * B_BLK;  // hi and lo of both
-constexpr uint32_t SMEM_BAR = 2 * STAGE_BYTES;            // 192 KB
+constexpr uint32_t SMEM_BAR = 2 * STAGE_BYTES;            // 128 KB
 constexpr uint32_t SMEM_ALLOC = SMEM_BAR + 64 + 1024;     // barriers, TMEM address, alignment slack
 constexpr int OUT_STRIDE = BN + 1;                        // floats per staged output row (no bank conflicts)
 constexpr uint32_t WAIT_LIMIT = 1u << 24;
@@ -72,13 +73,13 @@ __device__ __forceinline__ uint16_t bf16_bits(float f) {
 // Load rows [r0, r0+R) x k [k0, k0+64) of an operand into the hi (and lo)
 // images of one stage. Consecutive threads take consecutive 8-element chunks
 // along the contiguous dimension of the source, so global reads coalesce; a
-// thread issues the loads of 8 chunks before it converts and stores any, so
-// that their latencies overlap.
+// thread issues the loads of all its chunks before it converts and stores
+// any, so that their latencies overlap.
 template <int R>
 __device__ __forceinline__ void load_block(uint8_t* hi, uint8_t* lo, const float* src, int64_t s_row, int64_t s_k,
                                            int r0, int rlim, int k0, int klim, int split) {
-  constexpr int PER = R * 8 / NTHREADS;  // chunks per thread: 8 (A) or 16 (B)
-  constexpr int BATCH = 8;
+  constexpr int PER = R * 8 / NTHREADS;  // chunks per thread
+  constexpr int BATCH = PER < 8 ? PER : 8;
   static_assert(PER % BATCH == 0, "whole batches");
   const bool kmajor = s_k == 1;
 #pragma unroll 1
@@ -187,11 +188,14 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_tc_gemm(Args a) {
   if (!ok) {
     if (t == 0 && a.err) atomicExch(a.err, 1);
   } else {
-    // TMEM -> shared memory (row m = TMEM lane m), then coalesced rows into C
+    // TMEM -> shared memory (row m = TMEM lane m; warp w reads lane quadrant
+    // w % 4, column half w / 4), then coalesced rows into C
     float* out = reinterpret_cast<float*>(smem);
-    const int row = warp * 32 + lane;
-    const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
-    for (int c = 0; c < BN; c += 32) {
+    const int quad = warp & 3;
+    const int row = quad * 32 + lane;
+    const uint32_t lane_base = (uint32_t)(quad * 32) << 16;
+    const int c0 = (warp >> 2) * (BN / 2);
+    for (int c = c0; c < c0 + BN / 2; c += 32) {
       uint32_t r[32];
       if (committed > 0) {
         tc::tmem_ld32(tmem + lane_base + (uint32_t)c, r);

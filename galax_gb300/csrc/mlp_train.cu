@@ -171,11 +171,11 @@ __global__ void k_colsum(const float* X, const float* Y, const float* v, int64_t
 }
 
 // Column sums over the B rows of a [B][H] array in two deterministic passes:
-// k_colpart sums f(b, c) over 64-row chunks (thread c reads column c, so a
+// k_colpart sums f(b, c) over 16-row chunks (thread c reads column c, so a
 // warp reads 32 consecutive columns of a row), k_colfinal adds the chunks in
 // order. f: mode 0 X[b,c]; 1 X[b,c] v[b]; 2 silu'(X[b,c]) Y[b,c];
 // 3 X[b,c] V[b][j] for j = 0..2, out[c][3] (the first layer's weight gradient).
-constexpr int kColRows = 64;
+constexpr int kColRows = 16;
 
 __global__ void __launch_bounds__(256) k_colpart(const float* X, const float* Y, const float* v, const float* V,
                                                  int64_t rows, int mode, float* part) {
@@ -222,6 +222,28 @@ __global__ void __launch_bounds__(256) k_colfinal(const float* part, int64_t chu
       float* o = out + (int64_t)c * nj + j;
       *o = accumulate ? *o + s : s;
     }
+  }
+}
+
+// out[b][j] = sum_c X[b][c] W[c * ncol + j] (+ bias[j]) for ncol = 1 or 3: the
+// products with one or three output columns (the last layer's output and the
+// first layer's input gradient). One warp per row, lanes over columns
+// (coalesced), a fixed-order shuffle reduction.
+__global__ void __launch_bounds__(256) k_rowdot(const float* X, const float* W, const float* bias, int64_t rows,
+                                                int ncol, float* out) {
+  const int lane = threadIdx.x & 31;
+  const int64_t b = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (b >= rows) return;
+  float x[H / 32];
+#pragma unroll
+  for (int i = 0; i < H / 32; ++i) x[i] = X[b * H + lane + 32 * i];
+  for (int j = 0; j < ncol; ++j) {
+    float acc = 0.0f;
+#pragma unroll
+    for (int i = 0; i < H / 32; ++i) acc = fmaf(x[i], W[(lane + 32 * i) * ncol + j], acc);
+#pragma unroll
+    for (int m = 16; m >= 1; m >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, m);
+    if (lane == 0) out[b * ncol + j] = bias ? acc + bias[j] : acc;
   }
 }
 
@@ -406,7 +428,7 @@ static void forward_backward(cudaStream_t s, const float* P, const float* x, int
   k_silu<<<ew_grid(n), 256, 0, s>>>(w.Z[3], w.Hh[3], n, q);
   gemm<false, true>(s, w.err, Bi, H, H, w.Hh[3], H, P + OFF_W4, H, w.Z[4], H, 0.0f, P + OFF_B4, q, q);
   k_silu<<<ew_grid(n), 256, 0, s>>>(w.Z[4], w.Hh[4], n, 0);
-  gemm<false, false>(s, w.err, Bi, 1, H, w.Hh[4], H, P + OFF_W5, 1, w.out, 1, 0.0f, P + OFF_B5);
+  k_rowdot<<<(unsigned)((B + 7) / 8), 256, 0, s>>>(w.Hh[4], P + OFF_W5, P + OFF_B5, B, 1, w.out);
   // input gradient
   k_d4<<<ew_grid(n), 256, 0, s>>>(w.Z[4], P + OFF_W5, w.D[4], n, q);
   gemm<false, false>(s, w.err, Bi, H, H, w.D[4], H, P + OFF_W4, H, w.U[3], H, 0.0f, nullptr, q, q);
@@ -415,7 +437,7 @@ static void forward_backward(cudaStream_t s, const float* P, const float* x, int
   k_dmul<<<ew_grid(n), 256, 0, s>>>(w.Z[2], w.U[2], w.D[2], n, q, q);
   gemm<false, false>(s, w.err, Bi, H, H, w.D[2], H, P + OFF_W2, H, w.U[1], H, 0.0f, nullptr, q, q);
   k_dmul<<<ew_grid(n), 256, 0, s>>>(w.Z[1], w.U[1], w.D[1], n, 0, 0);
-  gemm<false, false>(s, w.err, Bi, 3, H, w.D[1], H, P + OFF_W1, 3, w.G, 3);
+  k_rowdot<<<(unsigned)((B + 7) / 8), 256, 0, s>>>(w.D[1], P + OFF_W1, nullptr, B, 3, w.G);
 }
 
 static void loss_grads(cudaStream_t s, const float* P, const float* x, const float* phi_t, const float* g_t,

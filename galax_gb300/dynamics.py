@@ -222,6 +222,15 @@ def _as_cuda(x, dtype):
     return torch.as_tensor(a, dtype=dtype, device="cuda")
 
 
+def _in_place_or_cuda(x, dtype):
+    """A contiguous pinned host tensor of the right dtype as it is (the kernels
+    read it through unified addressing), anything else as a contiguous CUDA tensor."""
+    torch = _torch()
+    if isinstance(x, torch.Tensor) and not x.is_cuda and x.dtype == dtype and x.is_contiguous() and x.is_pinned():
+        return x
+    return _as_cuda(x, dtype).contiguous()
+
+
 def _result_buffer(buf, shape, dtype, name):
     """A caller-given output (CUDA or pinned host, contiguous, right shape and
     dtype) or a new CUDA tensor."""
@@ -262,6 +271,10 @@ def integrate(
     place: contiguous CUDA tensors of those shapes, or pinned host tensors,
     which the kernels then write directly (device-visible host memory under
     unified addressing), overlapping the transfer with the integration.
+    Likewise ``save_ts`` (float64) and ``save_offsets`` (int64) may be
+    contiguous pinned host tensors, which the kernels read in place: the save
+    grid, usually the largest input, then crosses to the GPU while the orbits
+    run instead of in a copy before them.
 
     ``stream`` (a cudaStream_t handle) runs the call on that stream instead of
     torch's current one; its temporaries are then allocated there too.
@@ -278,9 +291,9 @@ def integrate(
     n = y.shape[1]
     t0v = _as_cuda(t0, torch.float64).reshape(-1).expand(n).contiguous()
     t1v = _as_cuda(t1, torch.float64).reshape(-1).expand(n).contiguous()
-    ts = _as_cuda(save_ts, torch.float64).reshape(-1).contiguous()
+    ts = _in_place_or_cuda(save_ts, torch.float64).reshape(-1)
     if save_offsets is not None:
-        offs = _as_cuda(save_offsets, torch.int64).reshape(-1).contiguous()
+        offs = _in_place_or_cuda(save_offsets, torch.int64).reshape(-1)
         if offs.numel() != n + 1:
             raise ValueError("save_offsets must have n + 1 entries")
         total = int(ts.numel())

@@ -804,6 +804,13 @@ def test_results_written_straight_into_pinned_host_memory(gx):
     assert o is h_out and s is h_st
     np.testing.assert_array_equal(h_out.numpy(), out_d.cpu().numpy())
     np.testing.assert_array_equal(h_st.numpy(), st_d.cpu().numpy())
+    # the save grid read in place from pinned host memory, too
+    h_ts = torch.as_tensor(b.save_ts).pin_memory()
+    h_offs = torch.as_tensor(b.save_offsets).pin_memory()
+    o2, s2, steps2 = integrate(mw, b.y0, b.t0, b.t1, h_ts, cfg, save_offsets=h_offs, out=h_out, status=h_st)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(h_out.numpy(), out_d.cpu().numpy())
+    np.testing.assert_array_equal(steps2.cpu().numpy(), steps_d.cpu().numpy())
     with pytest.raises(ValueError):
         integrate(mw, b.y0, b.t0, b.t1, b.save_ts, cfg, save_offsets=b.save_offsets,
                   out=torch.empty(3, dtype=torch.float64))

@@ -289,15 +289,17 @@ __global__ void k_adam(float* p, const float* g, float* m, float* v, int64_t n, 
 struct Ws {
   float *Z[5], *Hh[5], *D[5], *U[4], *Zb[5], *Db, *Ub, *Hb, *out, *G, *Pb, *Eb;
   float* colpart;  // [chunks][H][3] partial column sums
+  float* splitk;   // [kMaxSplits][H][H] partial tiles of the tensor-core weight gradients
   int* err;  // set by a tensor-core product that gave up waiting (gal_mlp_workspace_error)
 };
 
 static int64_t col_chunks(int64_t B) { return (B + kColRows - 1) / kColRows; }
+constexpr int kMaxSplits = 32;
 
 static size_t ws_bytes(int64_t B) {
   const size_t big = sizeof(float) * (size_t)B * H;
   return big * (4 + 4 + 4 + 3 + 4 + 3) + sizeof(float) * (size_t)B * (1 + 3 + 1 + 3) +
-         sizeof(float) * (size_t)col_chunks(B) * H * 3 + 64 * 256;
+         sizeof(float) * (size_t)col_chunks(B) * H * 3 + sizeof(float) * (size_t)kMaxSplits * H * H + 64 * 256;
 }
 
 static Ws carve(void* ws, int64_t B) {
@@ -323,6 +325,7 @@ static Ws carve(void* ws, int64_t B) {
   w.Eb = take(sizeof(float) * B * 3);
   w.err = reinterpret_cast<int*>(take(256));
   w.colpart = take(sizeof(float) * (size_t)col_chunks(B) * H * 3);
+  w.splitk = take(sizeof(float) * (size_t)kMaxSplits * H * H);
   return w;
 }
 
@@ -330,7 +333,8 @@ static Ws carve(void* ws, int64_t B) {
 // gemm() below; split_a / split_b as in tc_gemm.cuh. Returns false when the
 // kernel cannot be configured (then the caller uses the FP32 kernel).
 static bool tc_gemm(cudaStream_t s, bool TA, bool TB, int M, int N, int K, const float* A, int lda, const float* B,
-                    int ldb, float* C, int ldc, float beta, const float* bias, int split_a, int split_b, int* err) {
+                    int ldb, float* C, int ldc, float beta, const float* bias, int split_a, int split_b, int* err,
+                    float* part) {
   static std::atomic<int> configured[64] = {};
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return false;
@@ -360,19 +364,25 @@ static bool tc_gemm(cudaStream_t s, bool TA, bool TB, int M, int N, int K, const
   dim3 grid((N + tcg::BN - 1) / tcg::BN, (M + tcg::BM - 1) / tcg::BM, 1);
   a.kchunk = ((K + tcg::BK - 1) / tcg::BK) * tcg::BK;
   // few output tiles and a long K (the weight gradients, K = batch): split K
-  // over enough CTAs to fill the GPU, each adding its partial tile with atomics
+  // over enough CTAs to fill the GPU; each stores its partial tile, and the
+  // slices are added in a fixed order (deterministic, unlike atomics)
   const int tiles = (int)(grid.x * grid.y);
   const int sms = device_sm_count();
-  if (!bias && (beta == 0.0f || beta == 1.0f) && (beta == 1.0f || ldc == N) && tiles < sms && K >= 4 * tcg::BK) {
+  if (!bias && part && (int64_t)M * N <= (int64_t)H * H && tiles < sms && K >= 4 * tcg::BK) {
     int splits = sms / tiles;
     if (splits > K / (4 * tcg::BK)) splits = K / (4 * tcg::BK);
+    if (splits > kMaxSplits) splits = kMaxSplits;
     if (splits > 1) {
       a.kchunk = ((K + splits - 1) / splits + tcg::BK - 1) / tcg::BK * tcg::BK;
       grid.z = (K + a.kchunk - 1) / a.kchunk;
-      if (beta == 0.0f) cudaMemsetAsync(C, 0, sizeof(float) * (size_t)M * N, s);
+      a.part = part;
     }
   }
   tcg::k_tc_gemm<<<grid, tcg::NTHREADS, tcg::SMEM_ALLOC, s>>>(a);
+  if (grid.z > 1) {
+    const int64_t mn = (int64_t)M * N;
+    tcg::k_splitk_sum<<<(unsigned)((mn + 255) / 256), 256, 0, s>>>(part, (int)grid.z, M, N, C, ldc, beta);
+  }
   return true;
 }
 
@@ -380,10 +390,10 @@ static bool tc_gemm(cudaStream_t s, bool TA, bool TB, int M, int N, int K, const
 // K >= 64, else on the FP32 kernel. qa / qb: the operand is rounded to bf16
 // (one bf16 part on the tensor cores); otherwise it enters unrounded (two parts).
 template <bool TA, bool TB>
-static void gemm(cudaStream_t s, int* err, int M, int N, int K, const float* A, int lda, const float* B, int ldb,
+static void gemm(cudaStream_t s, const Ws& w, int M, int N, int K, const float* A, int lda, const float* B, int ldb,
                  float* C, int ldc, float beta = 0.0f, const float* bias = nullptr, int qa = 0, int qb = 0) {
   if (N == H && K >= tcg::BK &&
-      tc_gemm(s, TA, TB, M, N, K, A, lda, B, ldb, C, ldc, beta, bias, qa ? 0 : 1, qb ? 0 : 1, err))
+      tc_gemm(s, TA, TB, M, N, K, A, lda, B, ldb, C, ldc, beta, bias, qa ? 0 : 1, qb ? 0 : 1, w.err, w.splitk))
     return;
   dim3 grid((N + 63) / 64, (M + 63) / 64);
   // few output tiles and a long K (the weight gradients, K = batch): split K over
@@ -420,22 +430,22 @@ static unsigned ew_grid(int64_t n) {
 static void forward_backward(cudaStream_t s, const float* P, const float* x, int64_t B, const Ws& w, int q) {
   const int64_t n = B * H;
   const int Bi = (int)B;
-  gemm<false, true>(s, w.err, Bi, H, 3, x, 3, P + OFF_W1, 3, w.Z[1], H, 0.0f, P + OFF_B1);
+  gemm<false, true>(s, w, Bi, H, 3, x, 3, P + OFF_W1, 3, w.Z[1], H, 0.0f, P + OFF_B1);
   k_silu<<<ew_grid(n), 256, 0, s>>>(w.Z[1], w.Hh[1], n, q);
-  gemm<false, true>(s, w.err, Bi, H, H, w.Hh[1], H, P + OFF_W2, H, w.Z[2], H, 0.0f, P + OFF_B2, q, q);
+  gemm<false, true>(s, w, Bi, H, H, w.Hh[1], H, P + OFF_W2, H, w.Z[2], H, 0.0f, P + OFF_B2, q, q);
   k_silu<<<ew_grid(n), 256, 0, s>>>(w.Z[2], w.Hh[2], n, q);
-  gemm<false, true>(s, w.err, Bi, H, H, w.Hh[2], H, P + OFF_W3, H, w.Z[3], H, 0.0f, P + OFF_B3, q, q);
+  gemm<false, true>(s, w, Bi, H, H, w.Hh[2], H, P + OFF_W3, H, w.Z[3], H, 0.0f, P + OFF_B3, q, q);
   k_silu<<<ew_grid(n), 256, 0, s>>>(w.Z[3], w.Hh[3], n, q);
-  gemm<false, true>(s, w.err, Bi, H, H, w.Hh[3], H, P + OFF_W4, H, w.Z[4], H, 0.0f, P + OFF_B4, q, q);
+  gemm<false, true>(s, w, Bi, H, H, w.Hh[3], H, P + OFF_W4, H, w.Z[4], H, 0.0f, P + OFF_B4, q, q);
   k_silu<<<ew_grid(n), 256, 0, s>>>(w.Z[4], w.Hh[4], n, 0);
   k_rowdot<<<(unsigned)((B + 7) / 8), 256, 0, s>>>(w.Hh[4], P + OFF_W5, P + OFF_B5, B, 1, w.out);
   // input gradient
   k_d4<<<ew_grid(n), 256, 0, s>>>(w.Z[4], P + OFF_W5, w.D[4], n, q);
-  gemm<false, false>(s, w.err, Bi, H, H, w.D[4], H, P + OFF_W4, H, w.U[3], H, 0.0f, nullptr, q, q);
+  gemm<false, false>(s, w, Bi, H, H, w.D[4], H, P + OFF_W4, H, w.U[3], H, 0.0f, nullptr, q, q);
   k_dmul<<<ew_grid(n), 256, 0, s>>>(w.Z[3], w.U[3], w.D[3], n, q, q);
-  gemm<false, false>(s, w.err, Bi, H, H, w.D[3], H, P + OFF_W3, H, w.U[2], H, 0.0f, nullptr, q, q);
+  gemm<false, false>(s, w, Bi, H, H, w.D[3], H, P + OFF_W3, H, w.U[2], H, 0.0f, nullptr, q, q);
   k_dmul<<<ew_grid(n), 256, 0, s>>>(w.Z[2], w.U[2], w.D[2], n, q, q);
-  gemm<false, false>(s, w.err, Bi, H, H, w.D[2], H, P + OFF_W2, H, w.U[1], H, 0.0f, nullptr, q, q);
+  gemm<false, false>(s, w, Bi, H, H, w.D[2], H, P + OFF_W2, H, w.U[1], H, 0.0f, nullptr, q, q);
   k_dmul<<<ew_grid(n), 256, 0, s>>>(w.Z[1], w.U[1], w.D[1], n, 0, 0);
   k_rowdot<<<(unsigned)((B + 7) / 8), 256, 0, s>>>(w.D[1], P + OFF_W1, nullptr, B, 3, w.G);
 }
@@ -450,32 +460,32 @@ static void loss_grads(cudaStream_t s, const float* P, const float* x, const flo
   k_loss<<<ew_grid(B), 256, 0, s>>>(w.out, w.G, phi_t, g_t, wt, B, alpha, beta, w.Pb, w.Eb, loss);
   // ---- through the input-gradient graph, layer 1 up to 4
   colsum(s, w, w.D[1], nullptr, nullptr, w.Eb, B, 3, grad + OFF_W1, 0);                             // gW1 = D1^T Eb
-  gemm<false, true>(s, w.err, Bi, H, 3, w.Eb, 3, P + OFF_W1, 3, w.Db, H);                           // Db1 = Eb W1^T
+  gemm<false, true>(s, w, Bi, H, 3, w.Eb, 3, P + OFF_W1, 3, w.Db, H);                           // Db1 = Eb W1^T
   k_dd<<<ew_grid(n), 256, 0, s>>>(w.Z[1], w.U[1], w.Db, w.Ub, w.Zb[1], n, 0);
-  gemm<true, false>(s, w.err, H, H, Bi, w.D[2], H, w.Ub, H, grad + OFF_W2, H, 0.0f, nullptr, q, 0);                      // gW2 = D2^T Ub1
-  gemm<false, true>(s, w.err, Bi, H, H, w.Ub, H, P + OFF_W2, H, w.Db, H, 0.0f, nullptr, 0, q);      // Db2 = Ub1 W2^T
+  gemm<true, false>(s, w, H, H, Bi, w.D[2], H, w.Ub, H, grad + OFF_W2, H, 0.0f, nullptr, q, 0);                      // gW2 = D2^T Ub1
+  gemm<false, true>(s, w, Bi, H, H, w.Ub, H, P + OFF_W2, H, w.Db, H, 0.0f, nullptr, 0, q);      // Db2 = Ub1 W2^T
   k_dd<<<ew_grid(n), 256, 0, s>>>(w.Z[2], w.U[2], w.Db, w.Ub, w.Zb[2], n, q);
-  gemm<true, false>(s, w.err, H, H, Bi, w.D[3], H, w.Ub, H, grad + OFF_W3, H, 0.0f, nullptr, q, 0);                      // gW3 = D3^T Ub2
-  gemm<false, true>(s, w.err, Bi, H, H, w.Ub, H, P + OFF_W3, H, w.Db, H, 0.0f, nullptr, 0, q);      // Db3 = Ub2 W3^T
+  gemm<true, false>(s, w, H, H, Bi, w.D[3], H, w.Ub, H, grad + OFF_W3, H, 0.0f, nullptr, q, 0);                      // gW3 = D3^T Ub2
+  gemm<false, true>(s, w, Bi, H, H, w.Ub, H, P + OFF_W3, H, w.Db, H, 0.0f, nullptr, 0, q);      // Db3 = Ub2 W3^T
   k_dd<<<ew_grid(n), 256, 0, s>>>(w.Z[3], w.U[3], w.Db, w.Ub, w.Zb[3], n, q);
-  gemm<true, false>(s, w.err, H, H, Bi, w.D[4], H, w.Ub, H, grad + OFF_W4, H, 0.0f, nullptr, q, 0);                      // gW4 = D4^T Ub3
-  gemm<false, true>(s, w.err, Bi, H, H, w.Ub, H, P + OFF_W4, H, w.Db, H, 0.0f, nullptr, 0, q);      // Db4 = Ub3 W4^T
+  gemm<true, false>(s, w, H, H, Bi, w.D[4], H, w.Ub, H, grad + OFF_W4, H, 0.0f, nullptr, q, 0);                      // gW4 = D4^T Ub3
+  gemm<false, true>(s, w, Bi, H, H, w.Ub, H, P + OFF_W4, H, w.Db, H, 0.0f, nullptr, 0, q);      // Db4 = Ub3 W4^T
   colsum(s, w, w.Z[4], w.Db, nullptr, nullptr, B, 2, grad + OFF_W5, 0);                   // gw5 = sum silu'(Z4) Db4
   k_zb4<<<ew_grid(n), 256, 0, s>>>(w.Z[4], w.Db, w.Pb, P + OFF_W5, w.Zb[4], n);
   // ---- potential term and the forward graph, layer 4 down to 1
   colsum(s, w, w.Hh[4], nullptr, w.Pb, nullptr, B, 1, grad + OFF_W5, 1);                  // gw5 += H4^T Pb
   k_colsum<<<1, 256, 0, s>>>(w.Pb, nullptr, nullptr, B, 1, grad + OFF_B5, 0, 0);             // gb5
-  gemm<true, false>(s, w.err, H, H, Bi, w.Zb[4], H, w.Hh[3], H, grad + OFF_W4, H, 1.0f, nullptr, 0, q);            // gW4 += Zb4^T H3
+  gemm<true, false>(s, w, H, H, Bi, w.Zb[4], H, w.Hh[3], H, grad + OFF_W4, H, 1.0f, nullptr, 0, q);            // gW4 += Zb4^T H3
   colsum(s, w, w.Zb[4], nullptr, nullptr, nullptr, B, 0, grad + OFF_B4, 0);
-  gemm<false, false>(s, w.err, Bi, H, H, w.Zb[4], H, P + OFF_W4, H, w.Hb, H, 0.0f, nullptr, 0, q);  // Hb3 = Zb4 W4
+  gemm<false, false>(s, w, Bi, H, H, w.Zb[4], H, P + OFF_W4, H, w.Hb, H, 0.0f, nullptr, 0, q);  // Hb3 = Zb4 W4
   k_zb_acc<<<ew_grid(n), 256, 0, s>>>(w.Z[3], w.Hb, w.Zb[3], n);
-  gemm<true, false>(s, w.err, H, H, Bi, w.Zb[3], H, w.Hh[2], H, grad + OFF_W3, H, 1.0f, nullptr, 0, q);
+  gemm<true, false>(s, w, H, H, Bi, w.Zb[3], H, w.Hh[2], H, grad + OFF_W3, H, 1.0f, nullptr, 0, q);
   colsum(s, w, w.Zb[3], nullptr, nullptr, nullptr, B, 0, grad + OFF_B3, 0);
-  gemm<false, false>(s, w.err, Bi, H, H, w.Zb[3], H, P + OFF_W3, H, w.Hb, H, 0.0f, nullptr, 0, q);
+  gemm<false, false>(s, w, Bi, H, H, w.Zb[3], H, P + OFF_W3, H, w.Hb, H, 0.0f, nullptr, 0, q);
   k_zb_acc<<<ew_grid(n), 256, 0, s>>>(w.Z[2], w.Hb, w.Zb[2], n);
-  gemm<true, false>(s, w.err, H, H, Bi, w.Zb[2], H, w.Hh[1], H, grad + OFF_W2, H, 1.0f, nullptr, 0, q);
+  gemm<true, false>(s, w, H, H, Bi, w.Zb[2], H, w.Hh[1], H, grad + OFF_W2, H, 1.0f, nullptr, 0, q);
   colsum(s, w, w.Zb[2], nullptr, nullptr, nullptr, B, 0, grad + OFF_B2, 0);
-  gemm<false, false>(s, w.err, Bi, H, H, w.Zb[2], H, P + OFF_W2, H, w.Hb, H, 0.0f, nullptr, 0, q);
+  gemm<false, false>(s, w, Bi, H, H, w.Zb[2], H, P + OFF_W2, H, w.Hb, H, 0.0f, nullptr, 0, q);
   k_zb_acc<<<ew_grid(n), 256, 0, s>>>(w.Z[1], w.Hb, w.Zb[1], n);
   colsum(s, w, w.Zb[1], nullptr, nullptr, x, B, 3, grad + OFF_W1, 1);                                // gW1 += Zb1^T X
   colsum(s, w, w.Zb[1], nullptr, nullptr, nullptr, B, 0, grad + OFF_B1, 0);

@@ -22,7 +22,9 @@
 // to the stage's mbarrier, which frees the stage for the block after next. The
 // accumulator (128 TMEM columns) drains through shared memory so that C is
 // read and written row-contiguously. With gridDim.z > 1 each z takes a K
-// range and adds its partial tile into C with atomics.
+// range and stores its partial tile into its own slice of `part` ([z][M][N]),
+// which k_splitk_sum then adds into C in z order, so results do not depend on
+// the order in which CTAs finish.
 //
 // Every mbarrier wait is bounded; on timeout the kernel records an error code,
 // waits (bounded) for its products, releases TMEM and returns.
@@ -61,6 +63,7 @@ struct Args {
   const float* bias;
   int split_a, split_b;
   int kchunk;  // K per blockIdx.z, a multiple of BK
+  float* part;  // gridDim.z > 1: partial tiles [z][M][N]
   int* err;
 };
 
@@ -208,7 +211,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_tc_gemm(Args a) {
       for (int j = 0; j < 32; ++j) out[row * OUT_STRIDE + c + j] = __uint_as_float(r[j]);
     }
     __syncthreads();
-    const bool atomic = gridDim.z > 1;
+    const bool partial = gridDim.z > 1;
     for (int rr = warp; rr < BM; rr += NTHREADS / 32) {
       const int m = m0 + rr;
       if (m >= a.M) break;
@@ -216,11 +219,11 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_tc_gemm(Args a) {
         const int n = n0 + c;
         if (n >= a.N) break;
         float v = out[rr * OUT_STRIDE + c];
-        float* dst = a.C + (int64_t)m * a.ldc + n;
-        if (atomic) {
-          atomicAdd(dst, v);
+        if (partial) {
+          a.part[((int64_t)blockIdx.z * a.M + m) * a.N + n] = v;
           continue;
         }
+        float* dst = a.C + (int64_t)m * a.ldc + n;
         if (a.beta != 0.0f) v = fmaf(a.beta, *dst, v);
         if (a.bias) v += a.bias[n];
         *dst = v;
@@ -230,6 +233,17 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_tc_gemm(Args a) {
   tc::tc_fence_before();
   __syncthreads();
   if (warp == 0) tc::tmem_dealloc(tmem, BN);
+}
+
+// C[m][n] = beta C[m][n] + sum_z part[z][m][n], the slices added in z order.
+__global__ void k_splitk_sum(const float* part, int splits, int M, int N, float* C, int64_t ldc, float beta) {
+  const int64_t mn = (int64_t)M * N;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < mn; i += (int64_t)gridDim.x * blockDim.x) {
+    float s = 0.0f;
+    for (int z = 0; z < splits; ++z) s += part[z * mn + i];
+    float* dst = C + (i / N) * ldc + (i % N);
+    *dst = beta != 0.0f ? fmaf(beta, *dst, s) : s;
+  }
 }
 
 }  // namespace tcg

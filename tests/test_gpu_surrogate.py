@@ -302,3 +302,20 @@ def test_trained_surrogate_beats_the_analytic_part_alone(env):
     e_sur = float(err(S.integrate(mw, mlp, y0, 0.0, t1, 1.0, near=near)).median())
     assert e_mw > 1e-2  # the subhalos matter
     assert e_sur < e_mw / 10, (e_sur, e_mw)
+
+
+def test_training_is_deterministic(env):
+    """Two trainings from the same seed give the same network bit for bit: the
+    batches come from a keyed permutation, and the split-K weight gradients add
+    their partial tiles in a fixed order."""
+    gx, S = env
+    rng = np.random.default_rng(16)
+    plum = O.comps([(O.PLUMMER, 5e9, 2.0, 0, (3.0, -1.0, 0.5))])
+    r = np.exp(rng.uniform(np.log(0.5), np.log(40), 16384))
+    v = rng.normal(size=(16384, 3))
+    x = v / np.linalg.norm(v, axis=1, keepdims=True) * r[:, None]
+    phi, g = O.potential(plum, x), O.gradient(plum, x)
+    a, ra = S.train(x, phi, g, length_scale=20.0, epochs=3, batch=8192, lr=2e-3)
+    b, rb = S.train(x, phi, g, length_scale=20.0, epochs=3, batch=8192, lr=2e-3)
+    np.testing.assert_array_equal(a.params, b.params)
+    assert ra.loss == rb.loss

@@ -73,59 +73,68 @@ __device__ __forceinline__ uint16_t bf16_bits(float f) {
   return (uint16_t)(r & 0xffffu);
 }
 
-// Load rows [r0, r0+R) x k [k0, k0+64) of an operand into the hi (and lo)
-// images of one stage. Consecutive threads take consecutive 8-element chunks
-// along the contiguous dimension of the source, so global reads coalesce; a
-// thread issues the loads of all its chunks before it converts and stores
-// any, so that their latencies overlap.
+// One thread's share of an operand block, rows [r0, r0+R) x k [k0, k0+64):
+// PER chunks of 8 consecutive k. Consecutive threads take consecutive chunks
+// along the contiguous dimension of the source, so global reads coalesce.
+// fetch() issues all of a thread's loads; put() converts them to bf16 (hi,
+// and lo when split) and stores them into the 128-byte-swizzled stage. The
+// main loop fetches block kb + 1 before the barrier and product issue of
+// block kb, so the load latency overlaps them.
 template <int R>
-__device__ __forceinline__ void load_block(uint8_t* hi, uint8_t* lo, const float* src, int64_t s_row, int64_t s_k,
-                                           int r0, int rlim, int k0, int klim, int split) {
-  constexpr int PER = R * 8 / NTHREADS;  // chunks per thread
-  constexpr int BATCH = PER < 8 ? PER : 8;
-  static_assert(PER % BATCH == 0, "whole batches");
+struct Frag {
+  static constexpr int PER = R * 8 / NTHREADS;
+  float v[PER][8];
+};
+
+template <int R>
+__device__ __forceinline__ void chunk_of(int u, bool kmajor, int& row, int& c) {
+  const int i = threadIdx.x + u * NTHREADS;
+  row = kmajor ? (i >> 3) : (i % R);
+  c = kmajor ? (i & 7) : (i / R);
+}
+
+template <int R>
+__device__ __forceinline__ void fetch(Frag<R>& f, const float* src, int64_t s_row, int64_t s_k, int r0, int rlim,
+                                      int k0, int klim) {
   const bool kmajor = s_k == 1;
-#pragma unroll 1
-  for (int b0 = 0; b0 < PER; b0 += BATCH) {
-    float v[BATCH][8];
-    int rows[BATCH], cs[BATCH];
 #pragma unroll
-    for (int u = 0; u < BATCH; ++u) {
-      const int i = threadIdx.x + (b0 + u) * NTHREADS;
-      const int row = kmajor ? (i >> 3) : (i % R);
-      const int c = kmajor ? (i & 7) : (i / R);
-      rows[u] = row;
-      cs[u] = c;
-      const int gr = r0 + row, k = k0 + 8 * c;
-      if (kmajor && gr < rlim && k + 8 <= klim &&
-          ((reinterpret_cast<uintptr_t>(src + gr * s_row + k) & 15) == 0)) {
-        const float4 a = __ldg(reinterpret_cast<const float4*>(src + gr * s_row + k));
-        const float4 b = __ldg(reinterpret_cast<const float4*>(src + gr * s_row + k + 4));
-        v[u][0] = a.x; v[u][1] = a.y; v[u][2] = a.z; v[u][3] = a.w;
-        v[u][4] = b.x; v[u][5] = b.y; v[u][6] = b.z; v[u][7] = b.w;
-      } else {
+  for (int u = 0; u < Frag<R>::PER; ++u) {
+    int row, c;
+    chunk_of<R>(u, kmajor, row, c);
+    const int gr = r0 + row, k = k0 + 8 * c;
+    if (kmajor && gr < rlim && k + 8 <= klim && ((reinterpret_cast<uintptr_t>(src + gr * s_row + k) & 15) == 0)) {
+      const float4 a = __ldg(reinterpret_cast<const float4*>(src + gr * s_row + k));
+      const float4 b = __ldg(reinterpret_cast<const float4*>(src + gr * s_row + k + 4));
+      f.v[u][0] = a.x; f.v[u][1] = a.y; f.v[u][2] = a.z; f.v[u][3] = a.w;
+      f.v[u][4] = b.x; f.v[u][5] = b.y; f.v[u][6] = b.z; f.v[u][7] = b.w;
+    } else {
 #pragma unroll
-        for (int j = 0; j < 8; ++j)
-          v[u][j] = (gr < rlim && k + j < klim) ? __ldg(src + gr * s_row + (int64_t)(k + j) * s_k) : 0.0f;
+      for (int j = 0; j < 8; ++j)
+        f.v[u][j] = (gr < rlim && k + j < klim) ? __ldg(src + gr * s_row + (int64_t)(k + j) * s_k) : 0.0f;
+    }
+  }
+}
+
+template <int R>
+__device__ __forceinline__ void put(const Frag<R>& f, uint8_t* hi, uint8_t* lo, bool kmajor, int split) {
+#pragma unroll
+  for (int u = 0; u < Frag<R>::PER; ++u) {
+    int row, c;
+    chunk_of<R>(u, kmajor, row, c);
+    uint32_t h[4], l[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const uint16_t h0 = bf16_bits(f.v[u][2 * j]), h1 = bf16_bits(f.v[u][2 * j + 1]);
+      h[j] = (uint32_t)h0 | ((uint32_t)h1 << 16);
+      if (split) {
+        const uint16_t l0 = bf16_bits(f.v[u][2 * j] - __uint_as_float((uint32_t)h0 << 16));
+        const uint16_t l1 = bf16_bits(f.v[u][2 * j + 1] - __uint_as_float((uint32_t)h1 << 16));
+        l[j] = (uint32_t)l0 | ((uint32_t)l1 << 16);
       }
     }
-#pragma unroll
-    for (int u = 0; u < BATCH; ++u) {
-      uint32_t h[4], l[4];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const uint16_t h0 = bf16_bits(v[u][2 * j]), h1 = bf16_bits(v[u][2 * j + 1]);
-        h[j] = (uint32_t)h0 | ((uint32_t)h1 << 16);
-        if (split) {
-          const uint16_t l0 = bf16_bits(v[u][2 * j] - __uint_as_float((uint32_t)h0 << 16));
-          const uint16_t l1 = bf16_bits(v[u][2 * j + 1] - __uint_as_float((uint32_t)h1 << 16));
-          l[j] = (uint32_t)l0 | ((uint32_t)l1 << 16);
-        }
-      }
-      const uint32_t off = tc::sw128_offset(R, rows[u], 8 * cs[u]);
-      *reinterpret_cast<uint4*>(hi + off) = make_uint4(h[0], h[1], h[2], h[3]);
-      if (split) *reinterpret_cast<uint4*>(lo + off) = make_uint4(l[0], l[1], l[2], l[3]);
-    }
+    const uint32_t off = tc::sw128_offset(R, row, 8 * c);
+    *reinterpret_cast<uint4*>(hi + off) = make_uint4(h[0], h[1], h[2], h[3]);
+    if (split) *reinterpret_cast<uint4*>(lo + off) = make_uint4(l[0], l[1], l[2], l[3]);
   }
 }
 
@@ -156,15 +165,25 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_tc_gemm(Args a) {
   const uint32_t tmem = *tmem_holder;
   constexpr uint32_t idesc = tc::idesc_bf16(BM, BN);
   int committed = 0;  // k blocks whose products were issued (the same count in every thread)
+  Frag<BM> fa;
+  Frag<BN> fb;
+  if (nk > 0) {
+    fetch<BM>(fa, a.A, a.sam, a.sak, m0, a.M, kbeg, kend);
+    fetch<BN>(fb, a.B, a.sbn, a.sbk, n0, a.N, kbeg, kend);
+  }
   for (int kb = 0; kb < nk; ++kb) {
     const int s = kb & 1;
     uint8_t* st = smem + s * STAGE_BYTES;
     if (kb >= 2 && !tc::mbar_wait(&done[s], (uint32_t)((kb / 2 - 1) & 1), WAIT_LIMIT)) fail_s = 1;
     __syncthreads();
     if (fail_s) break;
-    const int k0 = kbeg + kb * BK;
-    load_block<BM>(st, st + A_BLK, a.A, a.sam, a.sak, m0, a.M, k0, kend, a.split_a);
-    load_block<BN>(st + 2 * A_BLK, st + 2 * A_BLK + B_BLK, a.B, a.sbn, a.sbk, n0, a.N, k0, kend, a.split_b);
+    put<BM>(fa, st, st + A_BLK, a.sak == 1, a.split_a);
+    put<BN>(fb, st + 2 * A_BLK, st + 2 * A_BLK + B_BLK, a.sbk == 1, a.split_b);
+    if (kb + 1 < nk) {  // the next block's loads in flight across the barrier and the product issue
+      const int k1 = kbeg + (kb + 1) * BK;
+      fetch<BM>(fa, a.A, a.sam, a.sak, m0, a.M, k1, kend);
+      fetch<BN>(fb, a.B, a.sbn, a.sbk, n0, a.N, k1, kend);
+    }
     tc::fence_proxy_async_smem();
     __syncthreads();
     if (t == 0) {

@@ -287,7 +287,7 @@ __global__ void k_adam(float* p, const float* g, float* m, float* v, int64_t n, 
 }
 
 struct Ws {
-  float *Z[5], *Hh[5], *D[5], *U[4], *Zb[5], *Db, *Ub, *Hb, *out, *G, *Pb, *Eb;
+  float *Z[5], *Hh[5], *D[5], *U[4], *Zb[5], *Db, *Ub, *Ub2, *Hb, *out, *G, *Pb, *Eb;  // Ub, Ub2 alternate
   float* colpart;  // [chunks][H][3] partial column sums
   float* splitk;   // [kMaxSplits][H][H] partial tiles of the tensor-core weight gradients
   int* err;  // set by a tensor-core product that gave up waiting (gal_mlp_workspace_error)
@@ -298,7 +298,7 @@ constexpr int kMaxSplits = 32;
 
 static size_t ws_bytes(int64_t B) {
   const size_t big = sizeof(float) * (size_t)B * H;
-  return big * (4 + 4 + 4 + 3 + 4 + 3) + sizeof(float) * (size_t)B * (1 + 3 + 1 + 3) +
+  return big * (4 + 4 + 4 + 3 + 4 + 4) + sizeof(float) * (size_t)B * (1 + 3 + 1 + 3) +
          sizeof(float) * (size_t)col_chunks(B) * H * 3 + sizeof(float) * (size_t)kMaxSplits * H * H + 64 * 256;
 }
 
@@ -318,6 +318,7 @@ static Ws carve(void* ws, int64_t B) {
   for (int k = 1; k <= 4; ++k) w.Zb[k] = take(big);
   w.Db = take(big);
   w.Ub = take(big);
+  w.Ub2 = take(big);
   w.Hb = take(big);
   w.out = take(sizeof(float) * B);
   w.G = take(sizeof(float) * B * 3);
@@ -332,9 +333,20 @@ static Ws carve(void* ws, int64_t B) {
 // Tensor-core product C = op(A) op(B) (+ beta C) (+ bias) with op as in
 // gemm() below; split_a / split_b as in tc_gemm.cuh. Returns false when the
 // kernel cannot be configured (then the caller uses the FP32 kernel).
+// The elementwise step fused into a product's store (tcg::EPI_*); the FP32
+// fallback runs the same step as a kernel of its own.
+struct Epi {
+  int mode = tcg::EPI_NONE;
+  const float* e1 = nullptr;
+  const float* e2 = nullptr;
+  float* o1 = nullptr;
+  float* o2 = nullptr;
+  int q1 = 0, q2 = 0;
+};
+
 static bool tc_gemm(cudaStream_t s, bool TA, bool TB, int M, int N, int K, const float* A, int lda, const float* B,
                     int ldb, float* C, int ldc, float beta, const float* bias, int split_a, int split_b, int* err,
-                    float* part) {
+                    float* part, const Epi& epi) {
   static std::atomic<int> configured[64] = {};
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return false;
@@ -361,6 +373,13 @@ static bool tc_gemm(cudaStream_t s, bool TA, bool TB, int M, int N, int K, const
   a.split_a = split_a;
   a.split_b = split_b;
   a.err = err;
+  a.epi = epi.mode;
+  a.e1 = epi.e1;
+  a.e2 = epi.e2;
+  a.o1 = epi.o1;
+  a.o2 = epi.o2;
+  a.q1 = epi.q1;
+  a.q2 = epi.q2;
   dim3 grid((N + tcg::BN - 1) / tcg::BN, (M + tcg::BM - 1) / tcg::BM, 1);
   a.kchunk = ((K + tcg::BK - 1) / tcg::BK) * tcg::BK;
   // few output tiles and a long K (the weight gradients, K = batch): split K
@@ -368,7 +387,8 @@ static bool tc_gemm(cudaStream_t s, bool TA, bool TB, int M, int N, int K, const
   // slices are added in a fixed order (deterministic, unlike atomics)
   const int tiles = (int)(grid.x * grid.y);
   const int sms = device_sm_count();
-  if (!bias && part && (int64_t)M * N <= (int64_t)H * H && tiles < sms && K >= 4 * tcg::BK) {
+  if (!bias && part && epi.mode == tcg::EPI_NONE && (int64_t)M * N <= (int64_t)H * H && tiles < sms &&
+      K >= 4 * tcg::BK) {
     int splits = sms / tiles;
     if (splits > K / (4 * tcg::BK)) splits = K / (4 * tcg::BK);
     if (splits > kMaxSplits) splits = kMaxSplits;
@@ -389,12 +409,20 @@ static bool tc_gemm(cudaStream_t s, bool TA, bool TB, int M, int N, int K, const
 // Products run on the tensor cores when they have 256 output columns and
 // K >= 64, else on the FP32 kernel. qa / qb: the operand is rounded to bf16
 // (one bf16 part on the tensor cores); otherwise it enters unrounded (two parts).
+static void epi_fallback(cudaStream_t s, const Epi& e, const float* C, int64_t n);
+
 template <bool TA, bool TB>
 static void gemm(cudaStream_t s, const Ws& w, int M, int N, int K, const float* A, int lda, const float* B, int ldb,
-                 float* C, int ldc, float beta = 0.0f, const float* bias = nullptr, int qa = 0, int qb = 0) {
+                 float* C, int ldc, float beta = 0.0f, const float* bias = nullptr, int qa = 0, int qb = 0,
+                 const Epi& epi = Epi()) {
   if (N == H && K >= tcg::BK &&
-      tc_gemm(s, TA, TB, M, N, K, A, lda, B, ldb, C, ldc, beta, bias, qa ? 0 : 1, qb ? 0 : 1, w.err, w.splitk))
+      tc_gemm(s, TA, TB, M, N, K, A, lda, B, ldb, C, ldc, beta, bias, qa ? 0 : 1, qb ? 0 : 1, w.err, w.splitk, epi))
     return;
+  if (epi.mode != tcg::EPI_NONE) {  // FP32 product, then the elementwise step on its own
+    gemm<TA, TB>(s, w, M, N, K, A, lda, B, ldb, C, ldc, beta, bias, qa, qb);
+    epi_fallback(s, epi, C, (int64_t)M * N);
+    return;
+  }
   dim3 grid((N + 63) / 64, (M + 63) / 64);
   // few output tiles and a long K (the weight gradients, K = batch): split K over
   // enough blocks to fill the GPU and accumulate with atomics
@@ -426,27 +454,71 @@ static unsigned ew_grid(int64_t n) {
   return (unsigned)(g > 4096 ? 4096 : (g < 1 ? 1 : g));
 }
 
+static void epi_fallback(cudaStream_t s, const Epi& e, const float* C, int64_t n) {
+  switch (e.mode) {
+    case tcg::EPI_SILU: k_silu<<<ew_grid(n), 256, 0, s>>>(C, e.o1, n, e.q1); break;
+    case tcg::EPI_DMUL: k_dmul<<<ew_grid(n), 256, 0, s>>>(e.e1, C, e.o1, n, e.q1, e.q2); break;
+    case tcg::EPI_DD: k_dd<<<ew_grid(n), 256, 0, s>>>(e.e1, e.e2, C, e.o1, e.o2, n, e.q1); break;
+    case tcg::EPI_ZBACC: k_zb_acc<<<ew_grid(n), 256, 0, s>>>(e.e1, C, e.o1, n); break;
+    default: break;
+  }
+}
+
+static Epi epi_silu(float* h, int q) {
+  Epi e;
+  e.mode = tcg::EPI_SILU;
+  e.o1 = h;
+  e.q1 = q;
+  return e;
+}
+static Epi epi_dmul(const float* z, float* d, int qs, int qd) {
+  Epi e;
+  e.mode = tcg::EPI_DMUL;
+  e.e1 = z;
+  e.o1 = d;
+  e.q1 = qs;
+  e.q2 = qd;
+  return e;
+}
+static Epi epi_dd(const float* z, const float* u, float* ub, float* zb, int qs) {
+  Epi e;
+  e.mode = tcg::EPI_DD;
+  e.e1 = z;
+  e.e2 = u;
+  e.o1 = ub;
+  e.o2 = zb;
+  e.q1 = qs;
+  return e;
+}
+static Epi epi_zbacc(const float* z, float* zb) {
+  Epi e;
+  e.mode = tcg::EPI_ZBACC;
+  e.e1 = z;
+  e.o1 = zb;
+  return e;
+}
+
 // forward and input-gradient pass; leaves Z, H, D, U, out, G in the workspace
 static void forward_backward(cudaStream_t s, const float* P, const float* x, int64_t B, const Ws& w, int q) {
   const int64_t n = B * H;
   const int Bi = (int)B;
   gemm<false, true>(s, w, Bi, H, 3, x, 3, P + OFF_W1, 3, w.Z[1], H, 0.0f, P + OFF_B1);
   k_silu<<<ew_grid(n), 256, 0, s>>>(w.Z[1], w.Hh[1], n, q);
-  gemm<false, true>(s, w, Bi, H, H, w.Hh[1], H, P + OFF_W2, H, w.Z[2], H, 0.0f, P + OFF_B2, q, q);
-  k_silu<<<ew_grid(n), 256, 0, s>>>(w.Z[2], w.Hh[2], n, q);
-  gemm<false, true>(s, w, Bi, H, H, w.Hh[2], H, P + OFF_W3, H, w.Z[3], H, 0.0f, P + OFF_B3, q, q);
-  k_silu<<<ew_grid(n), 256, 0, s>>>(w.Z[3], w.Hh[3], n, q);
-  gemm<false, true>(s, w, Bi, H, H, w.Hh[3], H, P + OFF_W4, H, w.Z[4], H, 0.0f, P + OFF_B4, q, q);
-  k_silu<<<ew_grid(n), 256, 0, s>>>(w.Z[4], w.Hh[4], n, 0);
+  gemm<false, true>(s, w, Bi, H, H, w.Hh[1], H, P + OFF_W2, H, w.Z[2], H, 0.0f, P + OFF_B2, q, q,
+                    epi_silu(w.Hh[2], q));
+  gemm<false, true>(s, w, Bi, H, H, w.Hh[2], H, P + OFF_W3, H, w.Z[3], H, 0.0f, P + OFF_B3, q, q,
+                    epi_silu(w.Hh[3], q));
+  gemm<false, true>(s, w, Bi, H, H, w.Hh[3], H, P + OFF_W4, H, w.Z[4], H, 0.0f, P + OFF_B4, q, q,
+                    epi_silu(w.Hh[4], 0));
   k_rowdot<<<(unsigned)((B + 7) / 8), 256, 0, s>>>(w.Hh[4], P + OFF_W5, P + OFF_B5, B, 1, w.out);
   // input gradient
   k_d4<<<ew_grid(n), 256, 0, s>>>(w.Z[4], P + OFF_W5, w.D[4], n, q);
-  gemm<false, false>(s, w, Bi, H, H, w.D[4], H, P + OFF_W4, H, w.U[3], H, 0.0f, nullptr, q, q);
-  k_dmul<<<ew_grid(n), 256, 0, s>>>(w.Z[3], w.U[3], w.D[3], n, q, q);
-  gemm<false, false>(s, w, Bi, H, H, w.D[3], H, P + OFF_W3, H, w.U[2], H, 0.0f, nullptr, q, q);
-  k_dmul<<<ew_grid(n), 256, 0, s>>>(w.Z[2], w.U[2], w.D[2], n, q, q);
-  gemm<false, false>(s, w, Bi, H, H, w.D[2], H, P + OFF_W2, H, w.U[1], H, 0.0f, nullptr, q, q);
-  k_dmul<<<ew_grid(n), 256, 0, s>>>(w.Z[1], w.U[1], w.D[1], n, 0, 0);
+  gemm<false, false>(s, w, Bi, H, H, w.D[4], H, P + OFF_W4, H, w.U[3], H, 0.0f, nullptr, q, q,
+                     epi_dmul(w.Z[3], w.D[3], q, q));
+  gemm<false, false>(s, w, Bi, H, H, w.D[3], H, P + OFF_W3, H, w.U[2], H, 0.0f, nullptr, q, q,
+                     epi_dmul(w.Z[2], w.D[2], q, q));
+  gemm<false, false>(s, w, Bi, H, H, w.D[2], H, P + OFF_W2, H, w.U[1], H, 0.0f, nullptr, q, q,
+                     epi_dmul(w.Z[1], w.D[1], 0, 0));
   k_rowdot<<<(unsigned)((B + 7) / 8), 256, 0, s>>>(w.D[1], P + OFF_W1, nullptr, B, 3, w.G);
 }
 
@@ -463,11 +535,12 @@ static void loss_grads(cudaStream_t s, const float* P, const float* x, const flo
   gemm<false, true>(s, w, Bi, H, 3, w.Eb, 3, P + OFF_W1, 3, w.Db, H);                           // Db1 = Eb W1^T
   k_dd<<<ew_grid(n), 256, 0, s>>>(w.Z[1], w.U[1], w.Db, w.Ub, w.Zb[1], n, 0);
   gemm<true, false>(s, w, H, H, Bi, w.D[2], H, w.Ub, H, grad + OFF_W2, H, 0.0f, nullptr, q, 0);                      // gW2 = D2^T Ub1
-  gemm<false, true>(s, w, Bi, H, H, w.Ub, H, P + OFF_W2, H, w.Db, H, 0.0f, nullptr, 0, q);      // Db2 = Ub1 W2^T
-  k_dd<<<ew_grid(n), 256, 0, s>>>(w.Z[2], w.U[2], w.Db, w.Ub, w.Zb[2], n, q);
-  gemm<true, false>(s, w, H, H, Bi, w.D[3], H, w.Ub, H, grad + OFF_W3, H, 0.0f, nullptr, q, 0);                      // gW3 = D3^T Ub2
-  gemm<false, true>(s, w, Bi, H, H, w.Ub, H, P + OFF_W3, H, w.Db, H, 0.0f, nullptr, 0, q);      // Db3 = Ub2 W3^T
-  k_dd<<<ew_grid(n), 256, 0, s>>>(w.Z[3], w.U[3], w.Db, w.Ub, w.Zb[3], n, q);
+  // the fused step writes the next Ub into the other buffer: this product still reads Ub
+  gemm<false, true>(s, w, Bi, H, H, w.Ub, H, P + OFF_W2, H, w.Db, H, 0.0f, nullptr, 0, q,
+                    epi_dd(w.Z[2], w.U[2], w.Ub2, w.Zb[2], q));                               // Db2 = Ub1 W2^T
+  gemm<true, false>(s, w, H, H, Bi, w.D[3], H, w.Ub2, H, grad + OFF_W3, H, 0.0f, nullptr, q, 0);                     // gW3 = D3^T Ub2
+  gemm<false, true>(s, w, Bi, H, H, w.Ub2, H, P + OFF_W3, H, w.Db, H, 0.0f, nullptr, 0, q,
+                    epi_dd(w.Z[3], w.U[3], w.Ub, w.Zb[3], q));                                // Db3 = Ub2 W3^T
   gemm<true, false>(s, w, H, H, Bi, w.D[4], H, w.Ub, H, grad + OFF_W4, H, 0.0f, nullptr, q, 0);                      // gW4 = D4^T Ub3
   gemm<false, true>(s, w, Bi, H, H, w.Ub, H, P + OFF_W4, H, w.Db, H, 0.0f, nullptr, 0, q);      // Db4 = Ub3 W4^T
   colsum(s, w, w.Z[4], w.Db, nullptr, nullptr, B, 2, grad + OFF_W5, 0);                   // gw5 = sum silu'(Z4) Db4
@@ -477,16 +550,16 @@ static void loss_grads(cudaStream_t s, const float* P, const float* x, const flo
   k_colsum<<<1, 256, 0, s>>>(w.Pb, nullptr, nullptr, B, 1, grad + OFF_B5, 0, 0);             // gb5
   gemm<true, false>(s, w, H, H, Bi, w.Zb[4], H, w.Hh[3], H, grad + OFF_W4, H, 1.0f, nullptr, 0, q);            // gW4 += Zb4^T H3
   colsum(s, w, w.Zb[4], nullptr, nullptr, nullptr, B, 0, grad + OFF_B4, 0);
-  gemm<false, false>(s, w, Bi, H, H, w.Zb[4], H, P + OFF_W4, H, w.Hb, H, 0.0f, nullptr, 0, q);  // Hb3 = Zb4 W4
-  k_zb_acc<<<ew_grid(n), 256, 0, s>>>(w.Z[3], w.Hb, w.Zb[3], n);
+  gemm<false, false>(s, w, Bi, H, H, w.Zb[4], H, P + OFF_W4, H, w.Hb, H, 0.0f, nullptr, 0, q,
+                     epi_zbacc(w.Z[3], w.Zb[3]));                                              // Hb3 = Zb4 W4
   gemm<true, false>(s, w, H, H, Bi, w.Zb[3], H, w.Hh[2], H, grad + OFF_W3, H, 1.0f, nullptr, 0, q);
   colsum(s, w, w.Zb[3], nullptr, nullptr, nullptr, B, 0, grad + OFF_B3, 0);
-  gemm<false, false>(s, w, Bi, H, H, w.Zb[3], H, P + OFF_W3, H, w.Hb, H, 0.0f, nullptr, 0, q);
-  k_zb_acc<<<ew_grid(n), 256, 0, s>>>(w.Z[2], w.Hb, w.Zb[2], n);
+  gemm<false, false>(s, w, Bi, H, H, w.Zb[3], H, P + OFF_W3, H, w.Hb, H, 0.0f, nullptr, 0, q,
+                     epi_zbacc(w.Z[2], w.Zb[2]));
   gemm<true, false>(s, w, H, H, Bi, w.Zb[2], H, w.Hh[1], H, grad + OFF_W2, H, 1.0f, nullptr, 0, q);
   colsum(s, w, w.Zb[2], nullptr, nullptr, nullptr, B, 0, grad + OFF_B2, 0);
-  gemm<false, false>(s, w, Bi, H, H, w.Zb[2], H, P + OFF_W2, H, w.Hb, H, 0.0f, nullptr, 0, q);
-  k_zb_acc<<<ew_grid(n), 256, 0, s>>>(w.Z[1], w.Hb, w.Zb[1], n);
+  gemm<false, false>(s, w, Bi, H, H, w.Zb[2], H, P + OFF_W2, H, w.Hb, H, 0.0f, nullptr, 0, q,
+                     epi_zbacc(w.Z[1], w.Zb[1]));
   colsum(s, w, w.Zb[1], nullptr, nullptr, x, B, 3, grad + OFF_W1, 1);                                // gW1 += Zb1^T X
   colsum(s, w, w.Zb[1], nullptr, nullptr, nullptr, B, 0, grad + OFF_B1, 0);
 }

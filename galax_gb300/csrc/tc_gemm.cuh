@@ -34,6 +34,7 @@
 
 #include <cstdint>
 
+#include "mlp.cuh"
 #include "tc.cuh"
 
 namespace gal {
@@ -65,7 +66,19 @@ struct Args {
   int kchunk;  // K per blockIdx.z, a multiple of BK
   float* part;  // gridDim.z > 1: partial tiles [z][M][N]
   int* err;
+  // Elementwise work of the next training step fused into the store of C
+  // (same layout as C, v = the stored value of C[m][n]):
+  //   EPI_SILU : o1 = silu(v)                                  (q1: rounded to bf16)
+  //   EPI_DMUL : o1 = silu'(e1) v                              (q1: silu' rounded, q2: o1 rounded)
+  //   EPI_DD   : o1 = silu'(e1) v (q1: silu' rounded), o2 = silu''(e1) e2 v; C not stored
+  //   EPI_ZBACC: o1 += silu'(e1) v; C not stored
+  int epi;
+  const float *e1, *e2;
+  float *o1, *o2;
+  int q1, q2;
 };
+
+enum { EPI_NONE = 0, EPI_SILU = 1, EPI_DMUL = 2, EPI_DD = 3, EPI_ZBACC = 4 };
 
 __device__ __forceinline__ uint16_t bf16_bits(float f) {
   uint32_t r;
@@ -242,10 +255,31 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_tc_gemm(Args a) {
           a.part[((int64_t)blockIdx.z * a.M + m) * a.N + n] = v;
           continue;
         }
-        float* dst = a.C + (int64_t)m * a.ldc + n;
+        const int64_t idx = (int64_t)m * a.ldc + n;
+        float* dst = a.C + idx;
         if (a.beta != 0.0f) v = fmaf(a.beta, *dst, v);
         if (a.bias) v += a.bias[n];
-        *dst = v;
+        if (a.epi == EPI_NONE) {
+          *dst = v;
+        } else if (a.epi == EPI_SILU) {
+          *dst = v;
+          const float h = mlp::silu(v);
+          a.o1[idx] = a.q1 ? mlp::bf16r(h) : h;
+        } else if (a.epi == EPI_DMUL) {
+          *dst = v;
+          float sd = mlp::dsilu(a.e1[idx]);
+          if (a.q1) sd = mlp::bf16r(sd);
+          const float d = sd * v;
+          a.o1[idx] = a.q2 ? mlp::bf16r(d) : d;
+        } else if (a.epi == EPI_DD) {
+          const float z = a.e1[idx];
+          float sd = mlp::dsilu(z);
+          if (a.q1) sd = mlp::bf16r(sd);
+          a.o1[idx] = sd * v;
+          a.o2[idx] = mlp::d2silu(z) * a.e2[idx] * v;
+        } else {  // EPI_ZBACC
+          a.o1[idx] += mlp::dsilu(a.e1[idx]) * v;
+        }
       }
     }
   }

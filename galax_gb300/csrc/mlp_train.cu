@@ -171,11 +171,11 @@ __global__ void k_colsum(const float* X, const float* Y, const float* v, int64_t
 }
 
 // Column sums over the B rows of a [B][H] array in two deterministic passes:
-// k_colpart sums f(b, c) over 16-row chunks (thread c reads column c, so a
+// k_colpart sums f(b, c) over 32-row chunks (thread c reads column c, so a
 // warp reads 32 consecutive columns of a row), k_colfinal adds the chunks in
 // order. f: mode 0 X[b,c]; 1 X[b,c] v[b]; 2 silu'(X[b,c]) Y[b,c];
 // 3 X[b,c] V[b][j] for j = 0..2, out[c][3] (the first layer's weight gradient).
-constexpr int kColRows = 16;
+constexpr int kColRows = 32;
 
 __global__ void __launch_bounds__(256) k_colpart(const float* X, const float* Y, const float* v, const float* V,
                                                  int64_t rows, int mode, float* part) {
@@ -183,6 +183,7 @@ __global__ void __launch_bounds__(256) k_colpart(const float* X, const float* Y,
   const int64_t r0 = (int64_t)blockIdx.x * kColRows;
   const int64_t r1 = r0 + kColRows < rows ? r0 + kColRows : rows;
   float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f;
+#pragma unroll 4
   for (int64_t b = r0; b < r1; ++b) {
     const float x = X[b * H + c];
     if (mode == 0) s0 += x;
@@ -210,6 +211,7 @@ __global__ void __launch_bounds__(256) k_colfinal(const float* part, int64_t chu
   const int nj = mode == 3 ? 3 : 1;
   for (int j = 0; j < nj; ++j) {
     float s = 0.0f;
+#pragma unroll 8
     for (int64_t k = g; k < chunks; k += 8) s += part[(k * H + c) * 3 + j];
     red[g][cl][j] = s;
   }

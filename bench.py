@@ -37,6 +37,8 @@ WORKLOADS = {
               "radii log-uniform 0.5-100 kpc, durations log-uniform 0.1-5 Gyr, 10-1000 saves/orbit, "
               "one persistent launch",
     "plain": "plain small: MilkyWayPotential, Dopri8 fixed dt=1 Myr over 1 Gyr, 100 uniform saves",
+    "subhalos": "plain FP64 direct sum: MilkyWayPotential + 512 Plummer subhalos (the learned surrogate's tables), "
+                "Dopri5 fixed dt=1 Myr over 1 Gyr, disk-like orbits at 4-20 kpc, final state saved",
     "grad": "differentiation: MilkyWayPotential, Dopri8 fixed dt=0.5 Myr over 2 Gyr, squared-distance loss, "
             "adjoint with checkpoints every 256 steps",
     "surrogate": "learned surrogate: MilkyWayPotential + 512 Plummer subhalos (m log-uniform 1e6-1e8 Msun, "
@@ -52,8 +54,8 @@ WORKLOADS = {
     "mlp": "surrogate MLP inference alone: forward + input gradient of 3-256-256-256-256-1 SiLU at n points "
            "(random weights), fused tensor-core kernel",
 }
-DEFAULT_ORBITS = {"uneven": 262_144, "plain": 1024, "grad": 65_536, "surrogate": 1_048_576, "mlp": 1_048_576,
-                  "stream": 3000}
+DEFAULT_ORBITS = {"uneven": 262_144, "plain": 1024, "subhalos": 65_536, "grad": 65_536, "surrogate": 1_048_576,
+                  "mlp": 1_048_576, "stream": 3000}
 
 
 def dist_env():
@@ -180,6 +182,8 @@ def run_ours(args) -> dict | None:
         return run_grad(args, n, rank, world, dist)
     if args.workload == "plain":
         return run_plain(args, n, rank, world, dist)
+    if args.workload == "subhalos":
+        return run_subhalos(args, n, rank, world, dist)
     if args.workload == "surrogate":
         return run_surrogate(args, n, rank, world, dist)
     if args.workload == "mlp":
@@ -636,6 +640,66 @@ def run_plain(args, n, rank, world, dist) -> dict | None:
             "gpu_launches": args.steps}
 
 
+def subhalo_tables():
+    """The Milky Way, the 512 Plummer subhalos, and both as one 516-component table."""
+    import galax_gb300 as gx
+    from galax_gb300 import workloads as W
+    from galax_gb300.potential import from_component_array
+
+    mw = gx.MilkyWayPotential()
+    m, b, c = W.subhalo_table(3, 512)
+    sub_arr = np.zeros(512, mw.component_array().dtype)
+    sub_arr["kind"] = 4
+    sub_arr["m"], sub_arr["l1"], sub_arr["origin"] = m, b, c
+    return mw, from_component_array(sub_arr), from_component_array(np.concatenate([mw.component_array(), sub_arr]))
+
+
+def run_subhalos(args, n, rank, world, dist) -> dict | None:
+    """The plain FP64 direct sum over the 516-component table (the learned
+    surrogate's denominator) on its own, with its FP64 roofline."""
+    import torch
+
+    import galax_gb300 as gx
+    from galax_gb300 import workloads as W
+    from galax_gb300.dynamics import integrate
+    from galax_gb300.flops import STEP_FLOPS_MW_SUBHALOS
+
+    mw, _, full = subhalo_tables()
+    y0 = torch.as_tensor(W.disk_like_ics(lambda x: mw.gradient(x), n, seed=31 + rank), device="cuda")
+    dt, t1 = 1.0, args.t1 if args.t1 > 0 else 1000.0
+    cfg = gx.Integrator(solver=gx.Dopri5(), stepsize_controller=gx.ConstantStepSize(), dt0=dt).config()
+    ys = y0.t().contiguous()
+    ts = torch.tensor([t1], dtype=torch.float64)
+    stream = torch.cuda.current_stream()
+
+    def step():
+        return integrate(full, ys, 0.0, t1, ts, cfg, soa=True)
+
+    for _ in range(args.warmup):
+        step()
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", 0)))
+    clocks.start()
+    ms = _max_over_ranks(_timed(step, args.steps, stream), dist)
+    clk = clocks.stop()
+    _, st, _ = step()
+    if rank != 0:
+        return None
+    nsteps = int(round(t1 / dt))
+    value = n * world * nsteps / (ms * 1e-3)
+    peak = fp64_peak()
+    achieved = n * nsteps * STEP_FLOPS_MW_SUBHALOS[5] / (ms * 1e-3) / 1e12
+    return {"metric": "orbit-steps/s", "value": value, "unit": "orbit-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOADS["subhalos"].replace("1 Gyr", f"{t1:g} Myr"), "orbits_per_gpu": n,
+                       "steps_per_orbit": nsteps, "orbits_not_finished": int((st != 0).sum())},
+            "roofline": {"bound": "fp64", "kernel": "k_integrate_table", "achieved": achieved,
+                         "peak": peak["tflops"], "unit": "TFLOP/s", "issue_ceiling": peak["issue_ceiling_tflops"],
+                         "frac_of_issue_ceiling": achieved / peak["issue_ceiling_tflops"],
+                         "frac": achieved / peak["tflops"], "flops_per_step": STEP_FLOPS_MW_SUBHALOS[5]},
+            "clocks": clk, "gpu_launches": args.steps}
+
+
 def run_surrogate(args, n, rank, world, dist) -> dict | None:
     """Learned-surrogate workload: orbit-steps/s of the surrogate path (analytic Milky
     Way in FP64 + MLP subhalo term on the tensor cores) against the plain FP64
@@ -647,15 +711,9 @@ def run_surrogate(args, n, rank, world, dist) -> dict | None:
     from galax_gb300 import surrogate as S
     from galax_gb300 import workloads as W
     from galax_gb300.dynamics import integrate
-    from galax_gb300.potential import from_component_array
+    from galax_gb300.flops import STEP_FLOPS_MW_SUBHALOS
 
-    mw = gx.MilkyWayPotential()
-    m, b, c = W.subhalo_table(3, 512)
-    sub_arr = np.zeros(512, mw.component_array().dtype)
-    sub_arr["kind"] = 4
-    sub_arr["m"], sub_arr["l1"], sub_arr["origin"] = m, b, c
-    sub = from_component_array(sub_arr)
-    full = from_component_array(np.concatenate([mw.component_array(), sub_arr]))
+    mw, sub, full = subhalo_tables()
     # training set: positions log-uniform in radius, FP64 targets from the direct sum;
     # with a split radius the MLP learns only the long-range remainder and the
     # short-range part is summed exactly along the orbits
@@ -722,7 +780,10 @@ def run_surrogate(args, n, rank, world, dist) -> dict | None:
                    "train_points": npts, "train_epochs": args.train_epochs, "train_seconds": round(train_s, 2),
                    "split_radius_kpc": args.split_radius,
                    "train_loss_first_last": [rep.loss[0], rep.loss[-1]]},
-        "plain_fp64_direct_sum": {"value": plain_value, "unit": "orbit-steps/s", "orbits": ns, "ms": plain_ms},
+        "plain_fp64_direct_sum": {"value": plain_value, "unit": "orbit-steps/s", "orbits": ns, "ms": plain_ms,
+                                  "fp64_tflops": plain_value * STEP_FLOPS_MW_SUBHALOS[5] / 1e12,
+                                  "frac_of_fp64_probe": plain_value * STEP_FLOPS_MW_SUBHALOS[5] / 1e12
+                                  / fp64_peak()["tflops"]},
         "speedup_vs_plain": value / plain_value,
         "median_rel_pos_err_1gyr": {"surrogate": float(e_sur.median()), "analytic_mw_only": float(e_mw.median()),
                                     "surrogate_p90": float(torch.quantile(e_sur, 0.9)),

@@ -171,34 +171,82 @@ __global__ void k_colsum(const float* X, const float* Y, const float* v, int64_t
 }
 
 // Column sums over the B rows of a [B][H] array in two deterministic passes:
-// k_colpart sums f(b, c) over 32-row chunks (thread c reads column c, so a
-// warp reads 32 consecutive columns of a row), k_colfinal adds the chunks in
+// k_colpart sums f(b, c) over 64-row chunks, k_colfinal adds the chunks in
 // order. f: mode 0 X[b,c]; 1 X[b,c] v[b]; 2 silu'(X[b,c]) Y[b,c];
 // 3 X[b,c] V[b][j] for j = 0..2, out[c][3] (the first layer's weight gradient).
-constexpr int kColRows = 32;
+// In k_colpart warp w sums rows w*8 .. w*8+7 of the chunk, lane l columns
+// 4l..4l+3 and 128+4l..128+4l+3 (two float4 per row: a warp reads whole
+// rows); the eight loads of each operand are issued together, and the eight
+// warps' sums are added in warp order through shared memory.
+constexpr int kColRows = 64;
 
+template <int mode>
 __global__ void __launch_bounds__(256) k_colpart(const float* X, const float* Y, const float* v, const float* V,
-                                                 int64_t rows, int mode, float* part) {
-  const int c = threadIdx.x;
-  const int64_t r0 = (int64_t)blockIdx.x * kColRows;
-  const int64_t r1 = r0 + kColRows < rows ? r0 + kColRows : rows;
-  float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f;
-#pragma unroll 4
-  for (int64_t b = r0; b < r1; ++b) {
-    const float x = X[b * H + c];
-    if (mode == 0) s0 += x;
-    else if (mode == 1) s0 += x * v[b];
-    else if (mode == 2) s0 += dsilu(x) * Y[b * H + c];
-    else {
-      s0 = fmaf(x, V[b * 3 + 0], s0);
-      s1 = fmaf(x, V[b * 3 + 1], s1);
-      s2 = fmaf(x, V[b * 3 + 2], s2);
+                                                 int64_t rows, float* part) {
+  __shared__ float red[3][8][H];
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  const int64_t b0 = (int64_t)blockIdx.x * kColRows + wp * 8;
+  float s[3][8];
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+#pragma unroll
+    for (int e = 0; e < 8; ++e) s[j][e] = 0.0f;
+  // all of the thread's loads first, then the sums
+  const float4 z4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  float4 xa[8], xb[8], ya[8], yb[8];
+  float sc[8][3];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int64_t b = b0 + i;
+    const bool in = b < rows;
+    const float4* xr = reinterpret_cast<const float4*>(X + b * H);
+    xa[i] = in ? xr[lane] : z4;
+    xb[i] = in ? xr[32 + lane] : z4;
+    if constexpr (mode == 2) {
+      const float4* yr = reinterpret_cast<const float4*>(Y + b * H);
+      ya[i] = in ? yr[lane] : z4;
+      yb[i] = in ? yr[32 + lane] : z4;
+    }
+    if constexpr (mode == 1) sc[i][0] = in ? v[b] : 0.0f;
+    if constexpr (mode == 3)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) sc[i][j] = in ? V[b * 3 + j] : 0.0f;
+  }
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const float x[8] = {xa[i].x, xa[i].y, xa[i].z, xa[i].w, xb[i].x, xb[i].y, xb[i].z, xb[i].w};
+    if constexpr (mode == 0) {
+#pragma unroll
+      for (int e = 0; e < 8; ++e) s[0][e] += x[e];
+    } else if constexpr (mode == 1) {
+#pragma unroll
+      for (int e = 0; e < 8; ++e) s[0][e] += x[e] * sc[i][0];
+    } else if constexpr (mode == 2) {
+      const float y[8] = {ya[i].x, ya[i].y, ya[i].z, ya[i].w, yb[i].x, yb[i].y, yb[i].z, yb[i].w};
+#pragma unroll
+      for (int e = 0; e < 8; ++e) s[0][e] += dsilu(x[e]) * y[e];
+    } else {
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+#pragma unroll
+        for (int e = 0; e < 8; ++e) s[j][e] = fmaf(x[e], sc[i][j], s[j][e]);
     }
   }
+  constexpr int nj = mode == 3 ? 3 : 1;
+#pragma unroll
+  for (int j = 0; j < nj; ++j)
+#pragma unroll
+    for (int e = 0; e < 8; ++e) red[j][wp][(e < 4 ? 0 : 128) + 4 * lane + (e & 3)] = s[j][e];
+  __syncthreads();
+  const int c = threadIdx.x;
   float* p = part + ((int64_t)blockIdx.x * H + c) * 3;
-  p[0] = s0;
-  p[1] = s1;
-  p[2] = s2;
+  for (int j = 0; j < 3; ++j) {
+    float t = 0.0f;
+    if (j < nj)
+#pragma unroll
+      for (int q = 0; q < 8; ++q) t += red[j][q][c];
+    p[j] = t;
+  }
 }
 
 // 32 columns per block; the 8 warps sum interleaved chunks, then one warp adds
@@ -211,7 +259,7 @@ __global__ void __launch_bounds__(256) k_colfinal(const float* part, int64_t chu
   const int nj = mode == 3 ? 3 : 1;
   for (int j = 0; j < nj; ++j) {
     float s = 0.0f;
-#pragma unroll 8
+#pragma unroll 16
     for (int64_t k = g; k < chunks; k += 8) s += part[(k * H + c) * 3 + j];
     red[g][cl][j] = s;
   }
@@ -306,7 +354,9 @@ static size_t ws_bytes(int64_t B) {
 
 static Ws carve(void* ws, int64_t B) {
   Ws w{};
-  char* p = static_cast<char*>(ws);
+  // 256-byte aligned whatever the caller's pointer (the size has the slack):
+  // the column sums read rows as float4
+  char* p = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(ws) + 255) & ~(uintptr_t)255);
   const size_t big = sizeof(float) * (size_t)B * H;
   auto take = [&](size_t bytes) {
     float* r = reinterpret_cast<float*>(p);
@@ -353,9 +403,12 @@ static bool tc_gemm(cudaStream_t s, bool TA, bool TB, int M, int N, int K, const
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return false;
   if (!configured[dev].load()) {
-    if (cudaFuncSetAttribute(tcg::k_tc_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tcg::SMEM_ALLOC) !=
-        cudaSuccess)
-      return false;
+    const void* fns[] = {(const void*)tcg::k_tc_gemm<tcg::EPI_NONE>, (const void*)tcg::k_tc_gemm<tcg::EPI_SILU>,
+                         (const void*)tcg::k_tc_gemm<tcg::EPI_DMUL>, (const void*)tcg::k_tc_gemm<tcg::EPI_DD>,
+                         (const void*)tcg::k_tc_gemm<tcg::EPI_ZBACC>};
+    for (const void* f : fns)
+      if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tcg::SMEM_ALLOC) != cudaSuccess)
+        return false;
     configured[dev].store(1);
   }
   tcg::Args a{};
@@ -400,7 +453,13 @@ static bool tc_gemm(cudaStream_t s, bool TA, bool TB, int M, int N, int K, const
       a.part = part;
     }
   }
-  tcg::k_tc_gemm<<<grid, tcg::NTHREADS, tcg::SMEM_ALLOC, s>>>(a);
+  switch (epi.mode) {
+    case tcg::EPI_SILU: tcg::k_tc_gemm<tcg::EPI_SILU><<<grid, tcg::NTHREADS, tcg::SMEM_ALLOC, s>>>(a); break;
+    case tcg::EPI_DMUL: tcg::k_tc_gemm<tcg::EPI_DMUL><<<grid, tcg::NTHREADS, tcg::SMEM_ALLOC, s>>>(a); break;
+    case tcg::EPI_DD: tcg::k_tc_gemm<tcg::EPI_DD><<<grid, tcg::NTHREADS, tcg::SMEM_ALLOC, s>>>(a); break;
+    case tcg::EPI_ZBACC: tcg::k_tc_gemm<tcg::EPI_ZBACC><<<grid, tcg::NTHREADS, tcg::SMEM_ALLOC, s>>>(a); break;
+    default: tcg::k_tc_gemm<tcg::EPI_NONE><<<grid, tcg::NTHREADS, tcg::SMEM_ALLOC, s>>>(a); break;
+  }
   if (grid.z > 1) {
     const int64_t mn = (int64_t)M * N;
     tcg::k_splitk_sum<<<(unsigned)((mn + 255) / 256), 256, 0, s>>>(part, (int)grid.z, M, N, C, ldc, beta);
@@ -447,7 +506,13 @@ static void gemm(cudaStream_t s, const Ws& w, int M, int N, int K, const float* 
 static void colsum(cudaStream_t s, const Ws& w, const float* X, const float* Y, const float* v, const float* V,
                    int64_t B, int mode, float* out, int accumulate) {
   const int64_t chunks = col_chunks(B);
-  k_colpart<<<(unsigned)chunks, H, 0, s>>>(X, Y, v, V, B, mode, w.colpart);
+  const unsigned g = (unsigned)chunks;
+  switch (mode) {
+    case 0: k_colpart<0><<<g, H, 0, s>>>(X, Y, v, V, B, w.colpart); break;
+    case 1: k_colpart<1><<<g, H, 0, s>>>(X, Y, v, V, B, w.colpart); break;
+    case 2: k_colpart<2><<<g, H, 0, s>>>(X, Y, v, V, B, w.colpart); break;
+    default: k_colpart<3><<<g, H, 0, s>>>(X, Y, v, V, B, w.colpart); break;
+  }
   k_colfinal<<<H / 32, 256, 0, s>>>(w.colpart, chunks, mode, out, accumulate);
 }
 

@@ -47,7 +47,7 @@ constexpr uint32_t B_BLK = BN * 128;  // 16 KB
 constexpr uint32_t STAGE_BYTES = 2 * A_BLK + 2 * B_BLK;  // hi and lo of both
 constexpr uint32_t SMEM_BAR = 2 * STAGE_BYTES;            // 128 KB
 constexpr uint32_t SMEM_ALLOC = SMEM_BAR + 64 + 1024;     // barriers, TMEM address, alignment slack
-constexpr int OUT_STRIDE = BN + 1;                        // floats per staged output row (no bank conflicts)
+constexpr int OUT_STRIDE = BN + 4;  // floats per staged output row: rows 16-byte aligned, float4 access conflict-free
 constexpr uint32_t WAIT_LIMIT = 1u << 24;
 static_assert(SMEM_ALLOC <= 227 * 1024, "shared memory budget");
 static_assert((uint32_t)BM * OUT_STRIDE * 4 <= SMEM_BAR, "output staging fits in the operand stages");
@@ -151,6 +151,159 @@ __device__ __forceinline__ void put(const Frag<R>& f, uint8_t* hi, uint8_t* lo, 
   }
 }
 
+__device__ __forceinline__ void prefetch_l2(const float* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
+// The operands of the fused step do not depend on the product: ask L2 for the
+// tile's lines while the tensor cores work, so that the store phase finds them
+// there.
+template <int EPI>
+__device__ __forceinline__ void prefetch_epilogue(const Args& a, int m0, int n0) {
+  if constexpr (EPI == EPI_DMUL || EPI == EPI_DD || EPI == EPI_ZBACC) {
+    for (int i = threadIdx.x; i < BM * (BN / 32); i += NTHREADS) {
+      const int m = m0 + (i >> 2), n = n0 + (i & 3) * 32;
+      if (m >= a.M || n >= a.N) continue;
+      const int64_t idx = (int64_t)m * a.ldc + n;
+      prefetch_l2(a.e1 + idx);
+      if constexpr (EPI == EPI_DD) prefetch_l2(a.e2 + idx);
+      if constexpr (EPI == EPI_ZBACC) prefetch_l2(a.o1 + idx);
+    }
+  }
+}
+
+// v: four consecutive outputs C[m][n..n+3] (beta and bias applied); x1, x2,
+// xo: the fused step's operands at the same places. Stores what EPI asks.
+template <int EPI>
+__device__ __forceinline__ void finish4(const Args& a, int64_t idx, const float (&v)[4], const float (&x1)[4],
+                                        const float (&x2)[4], const float (&xo)[4]) {
+  float r1[4], r2[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    if constexpr (EPI == EPI_SILU) {
+      const float h = mlp::silu(v[k]);
+      r1[k] = a.q1 ? mlp::bf16r(h) : h;
+    } else if constexpr (EPI == EPI_DMUL) {
+      float sd = mlp::dsilu(x1[k]);
+      if (a.q1) sd = mlp::bf16r(sd);
+      const float d = sd * v[k];
+      r1[k] = a.q2 ? mlp::bf16r(d) : d;
+    } else if constexpr (EPI == EPI_DD) {
+      float sd = mlp::dsilu(x1[k]);
+      if (a.q1) sd = mlp::bf16r(sd);
+      r1[k] = sd * v[k];
+      r2[k] = mlp::d2silu(x1[k]) * x2[k] * v[k];
+    } else if constexpr (EPI == EPI_ZBACC) {
+      r1[k] = xo[k] + mlp::dsilu(x1[k]) * v[k];
+    }
+  }
+  if constexpr (EPI == EPI_NONE || EPI == EPI_SILU || EPI == EPI_DMUL)
+    *reinterpret_cast<float4*>(a.C + idx) = make_float4(v[0], v[1], v[2], v[3]);
+  if constexpr (EPI != EPI_NONE) *reinterpret_cast<float4*>(a.o1 + idx) = make_float4(r1[0], r1[1], r1[2], r1[3]);
+  if constexpr (EPI == EPI_DD) *reinterpret_cast<float4*>(a.o2 + idx) = make_float4(r2[0], r2[1], r2[2], r2[3]);
+}
+
+__device__ __forceinline__ void ld4(const float* p, float (&x)[4]) {
+  const float4 v = *reinterpret_cast<const float4*>(p);
+  x[0] = v.x; x[1] = v.y; x[2] = v.z; x[3] = v.w;
+}
+
+// Store phase: the staged tile `out` (rows of OUT_STRIDE floats) into C and
+// the fused step's outputs. vec: every array 16-byte aligned, ldc and N
+// multiples of 4; then warp w takes rows w, w + 8, ... and lane l columns
+// 4l..4l+3 as float4, in groups of four rows whose loads (the fused step's
+// operands, C when beta != 0) are all issued before the group's first store
+// (the stores may alias them as far as the compiler knows, so interleaved
+// loads would each wait a full memory latency). Otherwise one element at a
+// time.
+template <int EPI>
+__device__ __forceinline__ void store_tile(const Args& a, const float* out, int m0, int n0, bool vec) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  constexpr int WARPS = NTHREADS / 32, RG = 4;
+  const bool partial = gridDim.z > 1;
+  const bool ld_c = !partial && a.beta != 0.0f;
+  constexpr bool ld_e1 = EPI == EPI_DMUL || EPI == EPI_DD || EPI == EPI_ZBACC;
+  if (vec) {
+    const int c = 4 * lane, n = n0 + c;
+    if (n >= a.N) return;
+    float bias[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    if (!partial && a.bias) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) bias[k] = a.bias[n + k];
+    }
+    for (int g = 0; g < BM / WARPS; g += RG) {
+      float xc[RG][4], x1[RG][4], x2[RG][4], xo[RG][4];
+#pragma unroll
+      for (int i = 0; i < RG; ++i) {
+        const int m = m0 + warp + (g + i) * WARPS;
+        const int64_t idx = (int64_t)m * a.ldc + n;
+        const bool in = m < a.M;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) xc[i][k] = x1[i][k] = x2[i][k] = xo[i][k] = 0.0f;
+        if (in && ld_c) ld4(a.C + idx, xc[i]);
+        if constexpr (ld_e1) if (in) ld4(a.e1 + idx, x1[i]);
+        if constexpr (EPI == EPI_DD) if (in) ld4(a.e2 + idx, x2[i]);
+        if constexpr (EPI == EPI_ZBACC) if (in) ld4(a.o1 + idx, xo[i]);
+      }
+#pragma unroll
+      for (int i = 0; i < RG; ++i) {
+        const int rr = warp + (g + i) * WARPS, m = m0 + rr;
+        if (m >= a.M) continue;
+        const float4 t = *reinterpret_cast<const float4*>(out + rr * OUT_STRIDE + c);
+        float v[4] = {t.x, t.y, t.z, t.w};
+        if (partial) {
+          *reinterpret_cast<float4*>(a.part + ((int64_t)blockIdx.z * a.M + m) * a.N + n) = t;
+          continue;
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          if (ld_c) v[k] = fmaf(a.beta, xc[i][k], v[k]);
+          v[k] += bias[k];
+        }
+        finish4<EPI>(a, (int64_t)m * a.ldc + n, v, x1[i], x2[i], xo[i]);
+      }
+    }
+    return;
+  }
+  for (int rr = warp; rr < BM; rr += WARPS) {
+    const int m = m0 + rr;
+    if (m >= a.M) break;
+    for (int c = lane; c < BN; c += 32) {
+      const int n = n0 + c;
+      if (n >= a.N) break;
+      float v = out[rr * OUT_STRIDE + c];
+      if (partial) {
+        a.part[((int64_t)blockIdx.z * a.M + m) * a.N + n] = v;
+        continue;
+      }
+      const int64_t idx = (int64_t)m * a.ldc + n;
+      if (ld_c) v = fmaf(a.beta, a.C[idx], v);
+      if (a.bias) v += a.bias[n];
+      if constexpr (EPI == EPI_NONE) {
+        a.C[idx] = v;
+      } else if constexpr (EPI == EPI_SILU) {
+        a.C[idx] = v;
+        const float h = mlp::silu(v);
+        a.o1[idx] = a.q1 ? mlp::bf16r(h) : h;
+      } else if constexpr (EPI == EPI_DMUL) {
+        a.C[idx] = v;
+        float sd = mlp::dsilu(a.e1[idx]);
+        if (a.q1) sd = mlp::bf16r(sd);
+        const float d = sd * v;
+        a.o1[idx] = a.q2 ? mlp::bf16r(d) : d;
+      } else if constexpr (EPI == EPI_DD) {
+        const float z = a.e1[idx];
+        float sd = mlp::dsilu(z);
+        if (a.q1) sd = mlp::bf16r(sd);
+        const float ee = a.e2[idx];
+        a.o1[idx] = sd * v;
+        a.o2[idx] = mlp::d2silu(z) * ee * v;
+      } else {  // EPI_ZBACC
+        a.o1[idx] += mlp::dsilu(a.e1[idx]) * v;
+      }
+    }
+  }
+}
+
+template <int EPI>
 __global__ void __launch_bounds__(NTHREADS, 1) k_tc_gemm(Args a) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = smem_raw + ((1024 - (tc::smem_u32(smem_raw) & 1023)) & 1023);
@@ -178,6 +331,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_tc_gemm(Args a) {
   const uint32_t tmem = *tmem_holder;
   constexpr uint32_t idesc = tc::idesc_bf16(BM, BN);
   int committed = 0;  // k blocks whose products were issued (the same count in every thread)
+  prefetch_epilogue<EPI>(a, m0, n0);
   Frag<BM> fa;
   Frag<BN> fb;
   if (nk > 0) {
@@ -224,7 +378,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_tc_gemm(Args a) {
     if (t == 0 && a.err) atomicExch(a.err, 1);
   } else {
     // TMEM -> shared memory (row m = TMEM lane m; warp w reads lane quadrant
-    // w % 4, column half w / 4), then coalesced rows into C
+    // w % 4, column half w / 4), then rows into C
     float* out = reinterpret_cast<float*>(smem);
     const int quad = warp & 3;
     const int row = quad * 32 + lane;
@@ -240,48 +394,16 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_tc_gemm(Args a) {
         for (int j = 0; j < 32; ++j) r[j] = 0u;
       }
 #pragma unroll
-      for (int j = 0; j < 32; ++j) out[row * OUT_STRIDE + c + j] = __uint_as_float(r[j]);
+      for (int j = 0; j < 32; j += 4)
+        *reinterpret_cast<float4*>(out + row * OUT_STRIDE + c + j) =
+            make_float4(__uint_as_float(r[j]), __uint_as_float(r[j + 1]), __uint_as_float(r[j + 2]),
+                        __uint_as_float(r[j + 3]));
     }
     __syncthreads();
-    const bool partial = gridDim.z > 1;
-    for (int rr = warp; rr < BM; rr += NTHREADS / 32) {
-      const int m = m0 + rr;
-      if (m >= a.M) break;
-      for (int c = lane; c < BN; c += 32) {
-        const int n = n0 + c;
-        if (n >= a.N) break;
-        float v = out[rr * OUT_STRIDE + c];
-        if (partial) {
-          a.part[((int64_t)blockIdx.z * a.M + m) * a.N + n] = v;
-          continue;
-        }
-        const int64_t idx = (int64_t)m * a.ldc + n;
-        float* dst = a.C + idx;
-        if (a.beta != 0.0f) v = fmaf(a.beta, *dst, v);
-        if (a.bias) v += a.bias[n];
-        if (a.epi == EPI_NONE) {
-          *dst = v;
-        } else if (a.epi == EPI_SILU) {
-          *dst = v;
-          const float h = mlp::silu(v);
-          a.o1[idx] = a.q1 ? mlp::bf16r(h) : h;
-        } else if (a.epi == EPI_DMUL) {
-          *dst = v;
-          float sd = mlp::dsilu(a.e1[idx]);
-          if (a.q1) sd = mlp::bf16r(sd);
-          const float d = sd * v;
-          a.o1[idx] = a.q2 ? mlp::bf16r(d) : d;
-        } else if (a.epi == EPI_DD) {
-          const float z = a.e1[idx];
-          float sd = mlp::dsilu(z);
-          if (a.q1) sd = mlp::bf16r(sd);
-          a.o1[idx] = sd * v;
-          a.o2[idx] = mlp::d2silu(z) * a.e2[idx] * v;
-        } else {  // EPI_ZBACC
-          a.o1[idx] += mlp::dsilu(a.e1[idx]) * v;
-        }
-      }
-    }
+    auto al16 = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; };
+    const bool vec = (a.N & 3) == 0 && (a.ldc & 3) == 0 && al16(a.C) && al16(a.part) && al16(a.e1) &&
+                     al16(a.e2) && al16(a.o1) && al16(a.o2);
+    store_tile<EPI>(a, out, m0, n0, vec);
   }
   tc::tc_fence_before();
   __syncthreads();

@@ -154,6 +154,13 @@ def test_flop_constants_match_counted_oracle():
         c = np.concatenate([O.milky_way(), O.comps([(O.PLUMMER, 1e5, 0.02, 0.0, (1.0, 2.0, 3.0))])])
         _, s = O.count_ops(c, method)
         assert sum(s.values()) == flops.STEP_FLOPS_MW_PLUMMER[method]
+    from galax_gb300 import workloads as W
+
+    m, b, c = W.subhalo_table(3, 512)
+    sub = O.comps([(O.PLUMMER, float(m[i]), float(b[i]), 0.0, tuple(c[i])) for i in range(512)])
+    for method in (5, 8):
+        _, s = O.count_ops(np.concatenate([O.milky_way(), sub]), method)
+        assert sum(s.values()) == flops.STEP_FLOPS_MW_SUBHALOS[method]
 
 
 def test_mn3_and_milky_way_2022_component_tables():

@@ -191,7 +191,8 @@ def run_ours(args) -> dict | None:
     if args.workload == "stream":
         return run_stream(args, n, rank, world, dist)
     mw, b = make_uneven(n, seed=1 + rank)  # weak scaling: every rank its own shard
-    cfg = gx.Integrator(solver=gx.Dopri5(), stepsize_controller=gx.PIDController(rtol=1e-8, atol=1e-10),
+    solver = gx.Dopri8() if args.method == 8 else gx.Dopri5()
+    cfg = gx.Integrator(solver=solver, stepsize_controller=gx.PIDController(rtol=1e-8, atol=1e-10),
                         max_steps=2**16).config()
     dev = "cuda"
     y0 = torch.as_tensor(b.y0, device=dev).t().contiguous()
@@ -300,7 +301,7 @@ def run_ours(args) -> dict | None:
             dist.destroy_process_group()
         return None
     peak = fp64_peak()
-    f_step = flops_per_step(5)
+    f_step = flops_per_step(args.method)
     achieved = accepted * f_step / (ms * 1e-3) / 1e12
     traffic = traffic_from_profiles()
     save_bytes = total_saves * 6 * 8
@@ -308,7 +309,8 @@ def run_ours(args) -> dict | None:
         "metric": "orbit-steps/s", "value": value, "unit": "orbit-steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded numpy, galactic units)",
-        "config": {"workload": WORKLOADS["uneven"], "orbits_per_gpu": n, "accepted_steps_per_gpu": accepted,
+        "config": {"workload": WORKLOADS["uneven"].replace("Dopri5", f"Dopri{args.method}"), "orbits_per_gpu": n,
+                   "accepted_steps_per_gpu": accepted,
                    "orbits_not_finished": n_bad, "saves_per_gpu": total_saves,
                    "save_bytes_per_step": save_bytes,
                    "l2": "inputs larger than L2: 1.0 GB save-time grid read and 6.3 GB of saves written per step",
@@ -335,10 +337,11 @@ def run_ours(args) -> dict | None:
         # the longest orbits go to four-warp teams)
         "gpu_launches": launches * (1 + ((6 if team_blocks > 0 else 5) if cfg.schedule else 1)),
     }
-    if world == 1 and not args.no_cpu_baseline:
+    # the CPU baseline, full-size parity and the other workloads go with the headline (Dopri5) line
+    if world == 1 and not args.no_cpu_baseline and args.method == 5:
         line["cpu_baseline"], sample = cpu_baseline(b, target_s=args.cpu_seconds)
         line["parity"] = parity_at_full_size(b, sample, h_out.numpy(), h_status.numpy(), e2e_acc.cpu().numpy())
-    if world == 1 and args.extras:
+    if world == 1 and args.extras and args.method == 5:
         line["extra"] = run_extras(args)
     if dist:
         dist.destroy_process_group()
@@ -1030,6 +1033,8 @@ def main():
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--workload", choices=tuple(WORKLOADS), default="uneven")
     ap.add_argument("--orbits", type=int, default=0)
+    ap.add_argument("--method", type=int, choices=(5, 8), default=5,
+                    help="uneven workload: Dopri5 (the headline) or Dopri8 (galax's default method)")
     ap.add_argument("--ref-orbits", type=int, default=8192)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")

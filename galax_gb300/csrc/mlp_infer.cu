@@ -49,7 +49,7 @@ constexpr uint32_t A_BYTES = TILE * 256 * 2;            // 64 KB: one operand ti
 constexpr uint32_t SMEM_A = 0;                          // two operand tiles, ping-pong
 constexpr uint32_t SMEM_RING = 2 * A_BYTES;
 constexpr uint32_t SMEM_SMALL = SMEM_RING + STAGES * HALF_BYTES;
-constexpr int SMALL_FLOATS = H * 3 + 5 * H + 1;         // W1, b1, b2, b3, b4, w5, b5
+constexpr int SMALL_FLOATS = H * 4 + 4 * H + 1;         // (W1 row, b1) per unit, b2, b3, b4, w5, b5
 constexpr uint32_t SMEM_PART = SMEM_SMALL + ((SMALL_FLOATS * 4 + 255) / 256) * 256;
 constexpr uint32_t SMEM_READY = SMEM_PART + TILE * 4 * 4;
 constexpr uint32_t SMEM_BAR = SMEM_READY + TILE * 4;
@@ -70,7 +70,7 @@ struct InferArgs {
   double* grad;          // [3][n] or NULL
   int32_t accumulate;    // grad += (1) or = (0)
   double* phi;           // [n] or NULL
-  const float* small;    // W1, b1, b2, b3, b4, w5, b5 (SMALL_FLOATS)
+  const float* small;    // {W1[c][0..2], b1[c]} for each unit c, then b2, b3, b4, w5, b5 (SMALL_FLOATS)
   const uint8_t* wimg;   // 24 pre-swizzled 32 KB K-blocks
   int* err;
 };
@@ -123,9 +123,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
   uint8_t* tiles = smem + SMEM_A;  // [2][A_BYTES]
   uint8_t* ring = smem + SMEM_RING;
   float* sm = reinterpret_cast<float*>(smem + SMEM_SMALL);
-  const float* sW1 = sm;
-  const float* sb1 = sm + 3 * H;
-  const float* sb2 = sb1 + H;
+  const float4* sL1 = reinterpret_cast<const float4*>(sm);  // {W1 row, b1} per unit: one 16-byte load
+  const float* sb2 = sm + 4 * H;
   const float* sb3 = sb2 + H;
   const float* sb4 = sb3 + H;
   const float* sw5 = sb4 + H;
@@ -261,8 +260,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
 #pragma unroll
           for (int k = 0; k < 32; ++k) {
             const int cc = c + k;
-            const float z =
-                fmaf(sW1[3 * cc], u[0], fmaf(sW1[3 * cc + 1], u[1], fmaf(sW1[3 * cc + 2], u[2], sb1[cc])));
+            const float4 l1 = sL1[cc];
+            const float z = fmaf(l1.x, u[0], fmaf(l1.y, u[1], fmaf(l1.z, u[2], l1.w)));
             v[k] = z * sig(z);
           }
           store_row32(tiles, row, c, v);
@@ -310,7 +309,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
                 const float s0 = sig(z0), s1 = sig(z1);
                 v[k] = z0 * s0;
                 v[k + 1] = z1 * s1;
-                spk[k / 2] = tc::pack_bf16x2(s0 * fmaf(z0, 1.f - s0, 1.f), s1 * fmaf(z1, 1.f - s1, 1.f));
+                // silu'(z) = s (1 + z (1 - s)) = s + silu(z) (1 - s)
+                spk[k / 2] = tc::pack_bf16x2(fmaf(v[k], 1.f - s0, s0), fmaf(v[k + 1], 1.f - s1, s1));
               }
               tc::tmem_st16(tmem + lane_base + (uint32_t)((g == 0 ? COL_S2 : COL_S3) + cc0 / 2), spk);
               store_row32(tile_out, row, cc0, v);
@@ -319,8 +319,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
               for (int k = 0; k < 32; ++k) {
                 const float z = __uint_as_float(acc[k]) + sb4[cc0 + k];
                 const float sg = sig(z);
-                ppart = fmaf(z * sg, sw5[cc0 + k], ppart);
-                v[k] = sg * fmaf(z, 1.f - sg, 1.f) * sw5[cc0 + k];
+                const float hz = z * sg;
+                ppart = fmaf(hz, sw5[cc0 + k], ppart);
+                v[k] = fmaf(hz, 1.f - sg, sg) * sw5[cc0 + k];
               }
               store_row32(tile_out, row, cc0, v);
             } else if (g <= 4) {  // u3 / u2: d = silu'(z) u -> operand tile
@@ -334,13 +335,13 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
 #pragma unroll
               for (int k = 0; k < 32; ++k) {
                 const int cc = cc0 + k;
-                const float z =
-                    fmaf(sW1[3 * cc], u[0], fmaf(sW1[3 * cc + 1], u[1], fmaf(sW1[3 * cc + 2], u[2], sb1[cc])));
+                const float4 l1 = sL1[cc];
+                const float z = fmaf(l1.x, u[0], fmaf(l1.y, u[1], fmaf(l1.z, u[2], l1.w)));
                 const float sg = sig(z);
                 const float d1 = sg * fmaf(z, 1.f - sg, 1.f) * __uint_as_float(acc[k]);
-                gpart[0] = fmaf(d1, sW1[3 * cc], gpart[0]);
-                gpart[1] = fmaf(d1, sW1[3 * cc + 1], gpart[1]);
-                gpart[2] = fmaf(d1, sW1[3 * cc + 2], gpart[2]);
+                gpart[0] = fmaf(d1, l1.x, gpart[0]);
+                gpart[1] = fmaf(d1, l1.y, gpart[1]);
+                gpart[2] = fmaf(d1, l1.z, gpart[2]);
               }
             }
           }
@@ -396,7 +397,7 @@ using namespace gal;
 using namespace gal::mlp;
 
 struct gal_mlp {
-  float* d_small;      // W1, b1, b2, b3, b4, w5, b5
+  float* d_small;      // {W1 row, b1} per unit, b2, b3, b4, w5, b5
   uint8_t* d_wimg;     // 24 x 32 KB pre-swizzled bf16 K-blocks
   int* d_err;
   double length_scale, phi_scale;
@@ -420,8 +421,10 @@ gal_status gal_mlp_create(const float* params_host, double length_scale, double 
     *out = nullptr;
     const float* P = params_host;
     std::vector<float> small(SMALL_FLOATS);
-    std::memcpy(small.data(), P + OFF_W1, sizeof(float) * 3 * H);
-    std::memcpy(small.data() + 3 * H, P + OFF_B1, sizeof(float) * H);
+    for (int c = 0; c < H; ++c) {
+      for (int j = 0; j < 3; ++j) small[4 * c + j] = P[OFF_W1 + 3 * c + j];
+      small[4 * c + 3] = P[OFF_B1 + c];
+    }
     std::memcpy(small.data() + 4 * H, P + OFF_B2, sizeof(float) * H);
     std::memcpy(small.data() + 5 * H, P + OFF_B3, sizeof(float) * H);
     std::memcpy(small.data() + 6 * H, P + OFF_B4, sizeof(float) * H);

@@ -151,27 +151,53 @@ __global__ void k_zb_acc(const float* Z, const float* Hb, float* Zb, int64_t n) 
   GRID_STRIDE(i, n) { Zb[i] += dsilu(Z[i]) * Hb[i]; }
 }
 
-// out[c] (+)= sum_b f(b, c) over rows; mode 0: X[b,c]; 1: X[b,c]*v[b]; 2: silu'(X[b,c]) * Y[b,c]
-__global__ void k_colsum(const float* X, const float* Y, const float* v, int64_t rows, int cols, float* out, int mode,
-                         int accumulate) {
-  const int c = blockIdx.x;
-  float s = 0.0f;
-  for (int64_t b = threadIdx.x; b < rows; b += blockDim.x) {
-    const float x = X[b * cols + c];
-    s += mode == 0 ? x : (mode == 1 ? x * v[b] : dsilu(x) * Y[b * cols + c]);
+// The first layer's 3-wide products with the elementwise step that follows:
+//   MODE 0: Z1 = X W1^T + b1 and H1 = silu(Z1) (bf16-rounded when q) -> o1 = Z1, o2 = H1
+//   MODE 1: Db1 = X W1^T (X = the gradient residual weights), then
+//           o1 = Ub = silu'(Z1) Db1, o2 = Zb1 = silu''(Z1) U1 Db1 (Db1 itself is not stored)
+// Thread c owns column c (row c of W1 in registers); a block takes kL1Rows rows,
+// all of whose loads are issued before the first store.
+// The sum is fma(w0, x0, fma(w1, x1, fma(w2, x2, b1))), the inference
+// kernel's order, so both compute the same first layer.
+constexpr int kL1Rows = 8;
+
+template <int MODE>
+__global__ void __launch_bounds__(256) k_layer1(const float* __restrict__ X, const float* __restrict__ W1,
+                                                const float* __restrict__ b1, const float* __restrict__ Z,
+                                                const float* __restrict__ U, float* __restrict__ o1,
+                                                float* __restrict__ o2, int64_t rows, int q) {
+  const int c = threadIdx.x;
+  const float w0 = W1[3 * c], w1 = W1[3 * c + 1], w2 = W1[3 * c + 2];
+  const float bc = MODE == 0 ? b1[c] : 0.0f;
+  const int64_t b0 = (int64_t)blockIdx.x * kL1Rows;
+  float v[kL1Rows], z[kL1Rows], u[kL1Rows];
+#pragma unroll
+  for (int i = 0; i < kL1Rows; ++i) {
+    const int64_t b = b0 + i < rows ? b0 + i : rows - 1;  // rows past the end repeat the last (not stored)
+    v[i] = fmaf(w0, X[3 * b], fmaf(w1, X[3 * b + 1], fmaf(w2, X[3 * b + 2], bc)));
+    if constexpr (MODE == 1) {
+      z[i] = Z[b * H + c];
+      u[i] = U[b * H + c];
+    }
   }
-  __shared__ float red[256];
-  red[threadIdx.x] = s;
-  __syncthreads();
-  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-    if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-    __syncthreads();
+#pragma unroll
+  for (int i = 0; i < kL1Rows; ++i) {
+    const int64_t b = b0 + i;
+    if (b >= rows) break;
+    const int64_t idx = b * H + c;
+    if constexpr (MODE == 0) {
+      const float h = silu(v[i]);
+      o1[idx] = v[i];
+      o2[idx] = q ? bf16r(h) : h;
+    } else {
+      o1[idx] = dsilu(z[i]) * v[i];
+      o2[idx] = d2silu(z[i]) * u[i] * v[i];
+    }
   }
-  if (threadIdx.x == 0) out[c] = accumulate ? out[c] + red[0] : red[0];
 }
 
 // Column sums over the B rows of a [B][H] array in two deterministic passes:
-// k_colpart sums f(b, c) over 64-row chunks, k_colfinal adds the chunks in
+// k_colpart sums f(b, c) over 64-row chunks, k_colfinal_all adds the chunks in
 // order. f: mode 0 X[b,c]; 1 X[b,c] v[b]; 2 silu'(X[b,c]) Y[b,c];
 // 3 X[b,c] V[b][j] for j = 0..2, out[c][3] (the first layer's weight gradient).
 // In k_colpart warp w sums rows w*8 .. w*8+7 of the chunk, lane l columns
@@ -249,29 +275,65 @@ __global__ void __launch_bounds__(256) k_colpart(const float* X, const float* Y,
   }
 }
 
-// 32 columns per block; the 8 warps sum interleaved chunks, then one warp adds
-// the 8 partial sums in a fixed order.
-__global__ void __launch_bounds__(256) k_colfinal(const float* part, int64_t chunks, int mode, float* out,
-                                                  int accumulate) {
+// The column sums of one training step, finished in one launch. Job j adds
+// the chunks of part[j][0] (and then those of part[j][1], when set) for each
+// of its H * nj outputs and stores the total (first + second) to out[j];
+// a job with nj = 0 is the sum of n0 scalars part[j][0][0..n0) (the output
+// bias gradient from the loss kernel's per-block sums).
+constexpr int kColJobs = 7;
+struct ColJobs {
+  const float* part[kColJobs][2];
+  float* out[kColJobs];
+  int nj[kColJobs];
+  int64_t chunks;
+  int n0;
+};
+
+// grid (H / 32, jobs): 32 columns per block; the 8 warps sum interleaved
+// chunks, then one warp adds the 8 partial sums in a fixed order.
+__global__ void __launch_bounds__(256) k_colfinal_all(ColJobs J) {
   __shared__ float red[8][32][3];
+  const int job = blockIdx.y;
   const int cl = threadIdx.x & 31, g = threadIdx.x >> 5;
   const int c = blockIdx.x * 32 + cl;
-  const int nj = mode == 3 ? 3 : 1;
-  for (int j = 0; j < nj; ++j) {
-    float s = 0.0f;
-#pragma unroll 16
-    for (int64_t k = g; k < chunks; k += 8) s += part[(k * H + c) * 3 + j];
-    red[g][cl][j] = s;
-  }
-  __syncthreads();
-  if (g == 0) {
-    for (int j = 0; j < nj; ++j) {
-      float s = 0.0f;
-#pragma unroll
-      for (int q = 0; q < 8; ++q) s += red[q][cl][j];
-      float* o = out + (int64_t)c * nj + j;
-      *o = accumulate ? *o + s : s;
+  const int nj = J.nj[job];
+  if (nj == 0) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      float t = 0.0f;
+      for (int i = 0; i < J.n0; ++i) t += J.part[job][0][i];
+      *J.out[job] = t;
     }
+    return;
+  }
+  float tot[3] = {0.0f, 0.0f, 0.0f};
+  for (int src = 0; src < 2; ++src) {
+    const float* part = J.part[job][src];
+    if (!part) break;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      if (j >= nj) break;
+      float s = 0.0f;
+#pragma unroll 16
+      for (int64_t k = g; k < J.chunks; k += 8) s += part[(k * H + c) * 3 + j];
+      red[g][cl][j] = s;
+    }
+    __syncthreads();
+    if (g == 0) {
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        if (j >= nj) break;
+        float s = 0.0f;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) s += red[q][cl][j];
+        tot[j] = src == 0 ? s : tot[j] + s;
+      }
+    }
+    __syncthreads();
+  }
+  if (g == 0) {
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      if (j < nj) J.out[job][(int64_t)c * nj + j] = tot[j];
   }
 }
 
@@ -299,13 +361,16 @@ __global__ void __launch_bounds__(256) k_rowdot(const float* X, const float* W, 
 
 // residuals, their loss weights and the loss value
 // (optional per-point weights wt[b] multiply both terms of point b)
+// pbsum[block] = the block's sum of Pb (added in a fixed order: the output
+// bias gradient)
 __global__ void k_loss(const float* out, const float* G, const float* phi_t, const float* g_t, const float* wt,
-                       int64_t B, float alpha, float beta, float* Pb, float* Eb, float* loss) {
-  float s = 0.0f;
+                       int64_t B, float alpha, float beta, float* Pb, float* Eb, float* loss, float* pbsum) {
+  float s = 0.0f, ps = 0.0f;
   GRID_STRIDE(b, B) {
     const float w = wt ? wt[b] : 1.0f;
     const float r = out[b] - phi_t[b];
     Pb[b] = 2.0f * alpha * w * r / (float)B;
+    ps += Pb[b];
     s += alpha * w * r * r;
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
@@ -314,14 +379,21 @@ __global__ void k_loss(const float* out, const float* G, const float* phi_t, con
       s += beta * w * e * e;
     }
   }
-  __shared__ float red[256];
-  red[threadIdx.x] = s;
+  __shared__ float red[2][256];
+  red[0][threadIdx.x] = s;
+  red[1][threadIdx.x] = ps;
   __syncthreads();
   for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-    if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    if ((int)threadIdx.x < w) {
+      red[0][threadIdx.x] += red[0][threadIdx.x + w];
+      red[1][threadIdx.x] += red[1][threadIdx.x + w];
+    }
     __syncthreads();
   }
-  if (threadIdx.x == 0) atomicAdd(loss, red[0] / (float)B);
+  if (threadIdx.x == 0) {
+    atomicAdd(loss, red[0][0] / (float)B);
+    pbsum[blockIdx.x] = red[1][0];
+  }
 }
 
 __global__ void k_adam(float* p, const float* g, float* m, float* v, int64_t n, float lr, float b1, float b2,
@@ -337,19 +409,23 @@ __global__ void k_adam(float* p, const float* g, float* m, float* v, int64_t n, 
 }
 
 struct Ws {
-  float *Z[5], *Hh[5], *D[5], *U[4], *Zb[5], *Db, *Ub, *Ub2, *Hb, *out, *G, *Pb, *Eb;  // Ub, Ub2 alternate
-  float* colpart;  // [chunks][H][3] partial column sums
+  float *Z[5], *Hh[5], *D[5], *U[4], *Zb[5], *Db, *Ub, *Ub2, *Ub3, *Hb, *out, *G, *Pb, *Eb;  // Ub1, Ub2, Ub3
+  float* colpart;  // [kColSlots][chunks][H][3] partial column sums, one slot per column sum of a step
+  float* pbsum;    // [kLossBlocks] per-block sums of Pb
   float* splitk;   // [kMaxSplits][H][H] partial tiles of the tensor-core weight gradients
   int* err;  // set by a tensor-core product that gave up waiting (gal_mlp_workspace_error)
 };
 
 static int64_t col_chunks(int64_t B) { return (B + kColRows - 1) / kColRows; }
 constexpr int kMaxSplits = 32;
+constexpr int kColSlots = 8;      // column sums per training step
+constexpr int kLossBlocks = 4096;  // k_loss's largest grid (ew_grid)
 
 static size_t ws_bytes(int64_t B) {
   const size_t big = sizeof(float) * (size_t)B * H;
-  return big * (4 + 4 + 4 + 3 + 4 + 4) + sizeof(float) * (size_t)B * (1 + 3 + 1 + 3) +
-         sizeof(float) * (size_t)col_chunks(B) * H * 3 + sizeof(float) * (size_t)kMaxSplits * H * H + 64 * 256;
+  return big * (4 + 4 + 4 + 3 + 4 + 5) + sizeof(float) * (size_t)B * (1 + 3 + 1 + 3) +
+         sizeof(float) * (size_t)kColSlots * col_chunks(B) * H * 3 + sizeof(float) * kLossBlocks +
+         sizeof(float) * (size_t)kMaxSplits * H * H + 64 * 256;
 }
 
 static Ws carve(void* ws, int64_t B) {
@@ -371,13 +447,15 @@ static Ws carve(void* ws, int64_t B) {
   w.Db = take(big);
   w.Ub = take(big);
   w.Ub2 = take(big);
+  w.Ub3 = take(big);
   w.Hb = take(big);
   w.out = take(sizeof(float) * B);
   w.G = take(sizeof(float) * B * 3);
   w.Pb = take(sizeof(float) * B);
   w.Eb = take(sizeof(float) * B * 3);
   w.err = reinterpret_cast<int*>(take(256));
-  w.colpart = take(sizeof(float) * (size_t)col_chunks(B) * H * 3);
+  w.colpart = take(sizeof(float) * (size_t)kColSlots * col_chunks(B) * H * 3);
+  w.pbsum = take(sizeof(float) * kLossBlocks);
   w.splitk = take(sizeof(float) * (size_t)kMaxSplits * H * H);
   return w;
 }
@@ -393,24 +471,78 @@ struct Epi {
   const float* e2 = nullptr;
   float* o1 = nullptr;
   float* o2 = nullptr;
+  const float* cvec = nullptr;
+  const float* rvec = nullptr;
   int q1 = 0, q2 = 0;
 };
 
-static bool tc_gemm(cudaStream_t s, bool TA, bool TB, int M, int N, int K, const float* A, int lda, const float* B,
-                    int ldb, float* C, int ldc, float beta, const float* bias, int split_a, int split_b, int* err,
-                    float* part, const Epi& epi) {
+// the tensor-core product kernels' shared-memory opt-in, once per device
+static bool tc_configure() {
   static std::atomic<int> configured[64] = {};
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return false;
   if (!configured[dev].load()) {
     const void* fns[] = {(const void*)tcg::k_tc_gemm<tcg::EPI_NONE>, (const void*)tcg::k_tc_gemm<tcg::EPI_SILU>,
                          (const void*)tcg::k_tc_gemm<tcg::EPI_DMUL>, (const void*)tcg::k_tc_gemm<tcg::EPI_DD>,
-                         (const void*)tcg::k_tc_gemm<tcg::EPI_ZBACC>};
+                         (const void*)tcg::k_tc_gemm<tcg::EPI_ZBACC>, (const void*)tcg::k_tc_gemm<tcg::EPI_SILU_D4>,
+                         (const void*)tcg::k_tc_gemm<tcg::EPI_ZB4>};
     for (const void* f : fns)
       if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tcg::SMEM_ALLOC) != cudaSuccess)
         return false;
     configured[dev].store(1);
   }
+  return true;
+}
+
+// C[H][H] = A1^T B1 + A2^T B2 with A_i, B_i of [K][H] (row-major): both terms
+// of a weight gradient in one split-K launch (slices 0..z-1 the first term,
+// z..2z-1 the second, one wave of CTAs) and one ordered sum of the slices.
+static bool tc_wgrad2(cudaStream_t s, int K, const float* A1, const float* B1, int split_a1, int split_b1,
+                      const float* A2, const float* B2, int split_a2, int split_b2, float* C, int* err,
+                      float* part) {
+  if (K < tcg::BK || !tc_configure()) return false;
+  const int tiles = (H / tcg::BN) * (H / tcg::BM);
+  int per = device_sm_count() / (2 * tiles);
+  if (per > K / (4 * tcg::BK)) per = K / (4 * tcg::BK);
+  if (per > kMaxSplits / 2) per = kMaxSplits / 2;
+  if (per < 1) per = 1;
+  tcg::Args a{};
+  a.M = H;
+  a.N = H;
+  a.K = K;
+  a.A = A1;
+  a.sam = 1;
+  a.sak = H;
+  a.B = B1;
+  a.sbn = 1;
+  a.sbk = H;
+  a.split_a = split_a1;
+  a.split_b = split_b1;
+  a.A2 = A2;
+  a.sam2 = 1;
+  a.sak2 = H;
+  a.B2 = B2;
+  a.sbn2 = 1;
+  a.sbk2 = H;
+  a.split_a2 = split_a2;
+  a.split_b2 = split_b2;
+  a.C = C;
+  a.ldc = H;
+  a.err = err;
+  a.part = part;
+  a.kchunk = ((K + per - 1) / per + tcg::BK - 1) / tcg::BK * tcg::BK;
+  const int z = (K + a.kchunk - 1) / a.kchunk;
+  a.z2 = z;
+  const dim3 grid(H / tcg::BN, H / tcg::BM, 2 * z);
+  tcg::k_tc_gemm<tcg::EPI_NONE><<<grid, tcg::NTHREADS, tcg::SMEM_ALLOC, s>>>(a);
+  tcg::k_splitk_sum<<<(unsigned)((H * H + 255) / 256), 256, 0, s>>>(part, 2 * z, H, H, C, H, 0.0f);
+  return true;
+}
+
+static bool tc_gemm(cudaStream_t s, bool TA, bool TB, int M, int N, int K, const float* A, int lda, const float* B,
+                    int ldb, float* C, int ldc, float beta, const float* bias, int split_a, int split_b, int* err,
+                    float* part, const Epi& epi) {
+  if (!tc_configure()) return false;
   tcg::Args a{};
   a.M = M;
   a.N = N;
@@ -433,6 +565,8 @@ static bool tc_gemm(cudaStream_t s, bool TA, bool TB, int M, int N, int K, const
   a.e2 = epi.e2;
   a.o1 = epi.o1;
   a.o2 = epi.o2;
+  a.cvec = epi.cvec;
+  a.rvec = epi.rvec;
   a.q1 = epi.q1;
   a.q2 = epi.q2;
   dim3 grid((N + tcg::BN - 1) / tcg::BN, (M + tcg::BM - 1) / tcg::BM, 1);
@@ -458,6 +592,8 @@ static bool tc_gemm(cudaStream_t s, bool TA, bool TB, int M, int N, int K, const
     case tcg::EPI_DMUL: tcg::k_tc_gemm<tcg::EPI_DMUL><<<grid, tcg::NTHREADS, tcg::SMEM_ALLOC, s>>>(a); break;
     case tcg::EPI_DD: tcg::k_tc_gemm<tcg::EPI_DD><<<grid, tcg::NTHREADS, tcg::SMEM_ALLOC, s>>>(a); break;
     case tcg::EPI_ZBACC: tcg::k_tc_gemm<tcg::EPI_ZBACC><<<grid, tcg::NTHREADS, tcg::SMEM_ALLOC, s>>>(a); break;
+    case tcg::EPI_SILU_D4: tcg::k_tc_gemm<tcg::EPI_SILU_D4><<<grid, tcg::NTHREADS, tcg::SMEM_ALLOC, s>>>(a); break;
+    case tcg::EPI_ZB4: tcg::k_tc_gemm<tcg::EPI_ZB4><<<grid, tcg::NTHREADS, tcg::SMEM_ALLOC, s>>>(a); break;
     default: tcg::k_tc_gemm<tcg::EPI_NONE><<<grid, tcg::NTHREADS, tcg::SMEM_ALLOC, s>>>(a); break;
   }
   if (grid.z > 1) {
@@ -503,17 +639,30 @@ static void gemm(cudaStream_t s, const Ws& w, int M, int N, int K, const float* 
   k_gemm<TA, TB><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc, 1.0f, beta, bias, qa, qb);
 }
 
-static void colsum(cudaStream_t s, const Ws& w, const float* X, const float* Y, const float* v, const float* V,
-                   int64_t B, int mode, float* out, int accumulate) {
-  const int64_t chunks = col_chunks(B);
-  const unsigned g = (unsigned)chunks;
+// gW = A1^T B1 + A2^T B2 over the batch (the two terms of a weight gradient);
+// qa / qb as in gemm()
+static void wgrad2(cudaStream_t s, const Ws& w, int B, const float* A1, const float* B1, int qa1, int qb1,
+                   const float* A2, const float* B2, int qa2, int qb2, float* C) {
+  if (tc_wgrad2(s, B, A1, B1, qa1 ? 0 : 1, qb1 ? 0 : 1, A2, B2, qa2 ? 0 : 1, qb2 ? 0 : 1, C, w.err, w.splitk)) return;
+  gemm<true, false>(s, w, H, H, B, A1, H, B1, H, C, H, 0.0f, nullptr, qa1, qb1);
+  gemm<true, false>(s, w, H, H, B, A2, H, B2, H, C, H, 1.0f, nullptr, qa2, qb2);
+}
+
+static float* col_slot(const Ws& w, int64_t B, int slot) {
+  return w.colpart + (size_t)slot * col_chunks(B) * H * 3;
+}
+
+// the chunk sums of one column sum into its slot (finished by k_colfinal_all)
+static void colpart(cudaStream_t s, const Ws& w, const float* X, const float* Y, const float* v, const float* V,
+                    int64_t B, int mode, int slot) {
+  const unsigned g = (unsigned)col_chunks(B);
+  float* part = col_slot(w, B, slot);
   switch (mode) {
-    case 0: k_colpart<0><<<g, H, 0, s>>>(X, Y, v, V, B, w.colpart); break;
-    case 1: k_colpart<1><<<g, H, 0, s>>>(X, Y, v, V, B, w.colpart); break;
-    case 2: k_colpart<2><<<g, H, 0, s>>>(X, Y, v, V, B, w.colpart); break;
-    default: k_colpart<3><<<g, H, 0, s>>>(X, Y, v, V, B, w.colpart); break;
+    case 0: k_colpart<0><<<g, H, 0, s>>>(X, Y, v, V, B, part); break;
+    case 1: k_colpart<1><<<g, H, 0, s>>>(X, Y, v, V, B, part); break;
+    case 2: k_colpart<2><<<g, H, 0, s>>>(X, Y, v, V, B, part); break;
+    default: k_colpart<3><<<g, H, 0, s>>>(X, Y, v, V, B, part); break;
   }
-  k_colfinal<<<H / 32, 256, 0, s>>>(w.colpart, chunks, mode, out, accumulate);
 }
 
 static unsigned ew_grid(int64_t n) {
@@ -527,6 +676,11 @@ static void epi_fallback(cudaStream_t s, const Epi& e, const float* C, int64_t n
     case tcg::EPI_DMUL: k_dmul<<<ew_grid(n), 256, 0, s>>>(e.e1, C, e.o1, n, e.q1, e.q2); break;
     case tcg::EPI_DD: k_dd<<<ew_grid(n), 256, 0, s>>>(e.e1, e.e2, C, e.o1, e.o2, n, e.q1); break;
     case tcg::EPI_ZBACC: k_zb_acc<<<ew_grid(n), 256, 0, s>>>(e.e1, C, e.o1, n); break;
+    case tcg::EPI_SILU_D4:
+      k_silu<<<ew_grid(n), 256, 0, s>>>(C, e.o1, n, e.q1);
+      k_d4<<<ew_grid(n), 256, 0, s>>>(C, e.cvec, e.o2, n, e.q2);
+      break;
+    case tcg::EPI_ZB4: k_zb4<<<ew_grid(n), 256, 0, s>>>(e.e1, C, e.rvec, e.cvec, e.o1, n); break;
     default: break;
   }
 }
@@ -564,22 +718,41 @@ static Epi epi_zbacc(const float* z, float* zb) {
   e.o1 = zb;
   return e;
 }
+// H4 = silu(Z4) (qh: rounded) and D4 = silu'(Z4) w5 (qd: rounded)
+static Epi epi_silu_d4(float* h, int qh, const float* w5, float* d, int qd) {
+  Epi e;
+  e.mode = tcg::EPI_SILU_D4;
+  e.o1 = h;
+  e.o2 = d;
+  e.cvec = w5;
+  e.q1 = qh;
+  e.q2 = qd;
+  return e;
+}
+// Zb4 = silu''(Z4) w5 Db4 + silu'(Z4) Pb w5 (C = Db4)
+static Epi epi_zb4(const float* z, const float* w5, const float* pb, float* zb) {
+  Epi e;
+  e.mode = tcg::EPI_ZB4;
+  e.e1 = z;
+  e.cvec = w5;
+  e.rvec = pb;
+  e.o1 = zb;
+  return e;
+}
 
 // forward and input-gradient pass; leaves Z, H, D, U, out, G in the workspace
 static void forward_backward(cudaStream_t s, const float* P, const float* x, int64_t B, const Ws& w, int q) {
-  const int64_t n = B * H;
   const int Bi = (int)B;
-  gemm<false, true>(s, w, Bi, H, 3, x, 3, P + OFF_W1, 3, w.Z[1], H, 0.0f, P + OFF_B1);
-  k_silu<<<ew_grid(n), 256, 0, s>>>(w.Z[1], w.Hh[1], n, q);
+  const unsigned l1_blocks = (unsigned)((B + kL1Rows - 1) / kL1Rows);
+  k_layer1<0><<<l1_blocks, H, 0, s>>>(x, P + OFF_W1, P + OFF_B1, nullptr, nullptr, w.Z[1], w.Hh[1], B, q);
   gemm<false, true>(s, w, Bi, H, H, w.Hh[1], H, P + OFF_W2, H, w.Z[2], H, 0.0f, P + OFF_B2, q, q,
                     epi_silu(w.Hh[2], q));
   gemm<false, true>(s, w, Bi, H, H, w.Hh[2], H, P + OFF_W3, H, w.Z[3], H, 0.0f, P + OFF_B3, q, q,
                     epi_silu(w.Hh[3], q));
   gemm<false, true>(s, w, Bi, H, H, w.Hh[3], H, P + OFF_W4, H, w.Z[4], H, 0.0f, P + OFF_B4, q, q,
-                    epi_silu(w.Hh[4], 0));
+                    epi_silu_d4(w.Hh[4], 0, P + OFF_W5, w.D[4], q));  // and D4 = silu'(Z4) w5
   k_rowdot<<<(unsigned)((B + 7) / 8), 256, 0, s>>>(w.Hh[4], P + OFF_W5, P + OFF_B5, B, 1, w.out);
   // input gradient
-  k_d4<<<ew_grid(n), 256, 0, s>>>(w.Z[4], P + OFF_W5, w.D[4], n, q);
   gemm<false, false>(s, w, Bi, H, H, w.D[4], H, P + OFF_W4, H, w.U[3], H, 0.0f, nullptr, q, q,
                      epi_dmul(w.Z[3], w.D[3], q, q));
   gemm<false, false>(s, w, Bi, H, H, w.D[3], H, P + OFF_W3, H, w.U[2], H, 0.0f, nullptr, q, q,
@@ -592,43 +765,55 @@ static void forward_backward(cudaStream_t s, const float* P, const float* x, int
 static void loss_grads(cudaStream_t s, const float* P, const float* x, const float* phi_t, const float* g_t,
                        const float* wt, int64_t B, float alpha, float beta, float* grad, float* loss, const Ws& w,
                        int q) {
-  const int64_t n = B * H;
   const int Bi = (int)B;
   forward_backward(s, P, x, B, w, q);
   cudaMemsetAsync(loss, 0, sizeof(float), s);
-  k_loss<<<ew_grid(B), 256, 0, s>>>(w.out, w.G, phi_t, g_t, wt, B, alpha, beta, w.Pb, w.Eb, loss);
+  const unsigned loss_blocks = ew_grid(B);
+  k_loss<<<loss_blocks, 256, 0, s>>>(w.out, w.G, phi_t, g_t, wt, B, alpha, beta, w.Pb, w.Eb, loss, w.pbsum);
+  // Column sums go to slots of their own; one launch at the end finishes them all:
+  //   0 + 6: gW1 = D1^T Eb + Zb1^T X   1 + 2: gw5 = sum silu'(Z4) Db4 + H4^T Pb
+  //   3, 4, 5, 7: gb4, gb3, gb2, gb1   gb5 = sum Pb from k_loss's block sums
   // ---- through the input-gradient graph, layer 1 up to 4
-  colsum(s, w, w.D[1], nullptr, nullptr, w.Eb, B, 3, grad + OFF_W1, 0);                             // gW1 = D1^T Eb
-  gemm<false, true>(s, w, Bi, H, 3, w.Eb, 3, P + OFF_W1, 3, w.Db, H);                           // Db1 = Eb W1^T
-  k_dd<<<ew_grid(n), 256, 0, s>>>(w.Z[1], w.U[1], w.Db, w.Ub, w.Zb[1], n, 0);
-  gemm<true, false>(s, w, H, H, Bi, w.D[2], H, w.Ub, H, grad + OFF_W2, H, 0.0f, nullptr, q, 0);                      // gW2 = D2^T Ub1
-  // the fused step writes the next Ub into the other buffer: this product still reads Ub
+  colpart(s, w, w.D[1], nullptr, nullptr, w.Eb, B, 3, 0);                                     // gW1 = D1^T Eb
+  k_layer1<1><<<(unsigned)((B + kL1Rows - 1) / kL1Rows), H, 0, s>>>(w.Eb, P + OFF_W1, nullptr, w.Z[1], w.U[1], w.Ub,
+                                                                   w.Zb[1], B, 0);           // Db1 = Eb W1^T
+  // Ub1, Ub2, Ub3 in buffers of their own: each stays until the weight gradient
+  // that pairs it with a forward-graph term (gWk = Dk^T Ub(k-1) + Zbk^T H(k-1))
   gemm<false, true>(s, w, Bi, H, H, w.Ub, H, P + OFF_W2, H, w.Db, H, 0.0f, nullptr, 0, q,
                     epi_dd(w.Z[2], w.U[2], w.Ub2, w.Zb[2], q));                               // Db2 = Ub1 W2^T
-  gemm<true, false>(s, w, H, H, Bi, w.D[3], H, w.Ub2, H, grad + OFF_W3, H, 0.0f, nullptr, q, 0);                     // gW3 = D3^T Ub2
   gemm<false, true>(s, w, Bi, H, H, w.Ub2, H, P + OFF_W3, H, w.Db, H, 0.0f, nullptr, 0, q,
-                    epi_dd(w.Z[3], w.U[3], w.Ub, w.Zb[3], q));                                // Db3 = Ub2 W3^T
-  gemm<true, false>(s, w, H, H, Bi, w.D[4], H, w.Ub, H, grad + OFF_W4, H, 0.0f, nullptr, q, 0);                      // gW4 = D4^T Ub3
-  gemm<false, true>(s, w, Bi, H, H, w.Ub, H, P + OFF_W4, H, w.Db, H, 0.0f, nullptr, 0, q);      // Db4 = Ub3 W4^T
-  colsum(s, w, w.Z[4], w.Db, nullptr, nullptr, B, 2, grad + OFF_W5, 0);                   // gw5 = sum silu'(Z4) Db4
-  k_zb4<<<ew_grid(n), 256, 0, s>>>(w.Z[4], w.Db, w.Pb, P + OFF_W5, w.Zb[4], n);
+                    epi_dd(w.Z[3], w.U[3], w.Ub3, w.Zb[3], q));                               // Db3 = Ub2 W3^T
+  gemm<false, true>(s, w, Bi, H, H, w.Ub3, H, P + OFF_W4, H, w.Db, H, 0.0f, nullptr, 0, q,
+                    epi_zb4(w.Z[4], P + OFF_W5, w.Pb, w.Zb[4]));                              // Db4 = Ub3 W4^T, Zb4
+  colpart(s, w, w.Z[4], w.Db, nullptr, nullptr, B, 2, 1);                                 // gw5 = sum silu'(Z4) Db4
   // ---- potential term and the forward graph, layer 4 down to 1
-  colsum(s, w, w.Hh[4], nullptr, w.Pb, nullptr, B, 1, grad + OFF_W5, 1);                  // gw5 += H4^T Pb
-  k_colsum<<<1, 256, 0, s>>>(w.Pb, nullptr, nullptr, B, 1, grad + OFF_B5, 0, 0);             // gb5
-  gemm<true, false>(s, w, H, H, Bi, w.Zb[4], H, w.Hh[3], H, grad + OFF_W4, H, 1.0f, nullptr, 0, q);            // gW4 += Zb4^T H3
-  colsum(s, w, w.Zb[4], nullptr, nullptr, nullptr, B, 0, grad + OFF_B4, 0);
+  colpart(s, w, w.Hh[4], nullptr, w.Pb, nullptr, B, 1, 2);                                 // gw5 += H4^T Pb
+  wgrad2(s, w, Bi, w.D[4], w.Ub3, q, 0, w.Zb[4], w.Hh[3], 0, q, grad + OFF_W4);           // gW4 = D4^T Ub3 + Zb4^T H3
+  colpart(s, w, w.Zb[4], nullptr, nullptr, nullptr, B, 0, 3);
   gemm<false, false>(s, w, Bi, H, H, w.Zb[4], H, P + OFF_W4, H, w.Hb, H, 0.0f, nullptr, 0, q,
                      epi_zbacc(w.Z[3], w.Zb[3]));                                              // Hb3 = Zb4 W4
-  gemm<true, false>(s, w, H, H, Bi, w.Zb[3], H, w.Hh[2], H, grad + OFF_W3, H, 1.0f, nullptr, 0, q);
-  colsum(s, w, w.Zb[3], nullptr, nullptr, nullptr, B, 0, grad + OFF_B3, 0);
+  wgrad2(s, w, Bi, w.D[3], w.Ub2, q, 0, w.Zb[3], w.Hh[2], 0, q, grad + OFF_W3);           // gW3 = D3^T Ub2 + Zb3^T H2
+  colpart(s, w, w.Zb[3], nullptr, nullptr, nullptr, B, 0, 4);
   gemm<false, false>(s, w, Bi, H, H, w.Zb[3], H, P + OFF_W3, H, w.Hb, H, 0.0f, nullptr, 0, q,
                      epi_zbacc(w.Z[2], w.Zb[2]));
-  gemm<true, false>(s, w, H, H, Bi, w.Zb[2], H, w.Hh[1], H, grad + OFF_W2, H, 1.0f, nullptr, 0, q);
-  colsum(s, w, w.Zb[2], nullptr, nullptr, nullptr, B, 0, grad + OFF_B2, 0);
+  wgrad2(s, w, Bi, w.D[2], w.Ub, q, 0, w.Zb[2], w.Hh[1], 0, q, grad + OFF_W2);            // gW2 = D2^T Ub1 + Zb2^T H1
+  colpart(s, w, w.Zb[2], nullptr, nullptr, nullptr, B, 0, 5);
   gemm<false, false>(s, w, Bi, H, H, w.Zb[2], H, P + OFF_W2, H, w.Hb, H, 0.0f, nullptr, 0, q,
                      epi_zbacc(w.Z[1], w.Zb[1]));
-  colsum(s, w, w.Zb[1], nullptr, nullptr, x, B, 3, grad + OFF_W1, 1);                                // gW1 += Zb1^T X
-  colsum(s, w, w.Zb[1], nullptr, nullptr, nullptr, B, 0, grad + OFF_B1, 0);
+  colpart(s, w, w.Zb[1], nullptr, nullptr, x, B, 3, 6);                                     // gW1 += Zb1^T X
+  colpart(s, w, w.Zb[1], nullptr, nullptr, nullptr, B, 0, 7);
+  ColJobs J{};
+  const int slot_a[kColJobs] = {0, 1, 3, 4, 5, 7, -1}, slot_b[kColJobs] = {6, 2, -1, -1, -1, -1, -1};
+  const int64_t outs[kColJobs] = {OFF_W1, OFF_W5, OFF_B4, OFF_B3, OFF_B2, OFF_B1, OFF_B5};
+  for (int j = 0; j < kColJobs; ++j) {
+    J.part[j][0] = slot_a[j] >= 0 ? col_slot(w, B, slot_a[j]) : w.pbsum;
+    J.part[j][1] = slot_b[j] >= 0 ? col_slot(w, B, slot_b[j]) : nullptr;
+    J.out[j] = grad + outs[j];
+    J.nj[j] = j == 0 ? 3 : (j == kColJobs - 1 ? 0 : 1);
+  }
+  J.chunks = col_chunks(B);
+  J.n0 = (int)loss_blocks;
+  k_colfinal_all<<<dim3(H / 32, kColJobs), 256, 0, s>>>(J);
 }
 
 // ---------------------------------------------------------------- device-driven training

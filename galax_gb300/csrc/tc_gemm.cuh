@@ -66,19 +66,74 @@ struct Args {
   int kchunk;  // K per blockIdx.z, a multiple of BK
   float* part;  // gridDim.z > 1: partial tiles [z][M][N]
   int* err;
+  // Optional second product of the same shape and K, added into the same C:
+  // slices blockIdx.z >= z2 compute A2(m, k) B2(n, k) over their K range
+  // (slice z - z2); only with gridDim.z > 1 (partial tiles)
+  const float* A2;
+  int64_t sam2, sak2;
+  const float* B2;
+  int64_t sbn2, sbk2;
+  int split_a2, split_b2;
+  int z2;
   // Elementwise work of the next training step fused into the store of C
   // (same layout as C, v = the stored value of C[m][n]):
   //   EPI_SILU : o1 = silu(v)                                  (q1: rounded to bf16)
   //   EPI_DMUL : o1 = silu'(e1) v                              (q1: silu' rounded, q2: o1 rounded)
   //   EPI_DD   : o1 = silu'(e1) v (q1: silu' rounded), o2 = silu''(e1) e2 v; C not stored
   //   EPI_ZBACC: o1 += silu'(e1) v; C not stored
+  //   EPI_SILU_D4: o1 = silu(v) (q1: rounded), o2 = silu'(v) cvec[n] (q2: rounded)
+  //   EPI_ZB4  : o1 = silu''(e1) cvec[n] v + silu'(e1) rvec[m] cvec[n]
   int epi;
   const float *e1, *e2;
   float *o1, *o2;
+  const float* cvec;  // per column n
+  const float* rvec;  // per row m
   int q1, q2;
 };
 
-enum { EPI_NONE = 0, EPI_SILU = 1, EPI_DMUL = 2, EPI_DD = 3, EPI_ZBACC = 4 };
+enum { EPI_NONE = 0, EPI_SILU = 1, EPI_DMUL = 2, EPI_DD = 3, EPI_ZBACC = 4, EPI_SILU_D4 = 5, EPI_ZB4 = 6 };
+
+template <int EPI>
+constexpr bool epi_stores_c() {
+  return EPI != EPI_DD && EPI != EPI_ZBACC;
+}
+template <int EPI>
+constexpr bool epi_reads_e1() {
+  return EPI == EPI_DMUL || EPI == EPI_DD || EPI == EPI_ZBACC || EPI == EPI_ZB4;
+}
+template <int EPI>
+constexpr bool epi_writes_o2() {
+  return EPI == EPI_DD || EPI == EPI_SILU_D4;
+}
+
+// The fused step for one element: v = C[m][n] (beta and bias applied), x1 =
+// e1, x2 = e2, xo = o1 at the same place, cv = cvec[n], rv = rvec[m].
+template <int EPI>
+__device__ __forceinline__ void fused_step(const Args& a, float v, float x1, float x2, float xo, float cv, float rv,
+                                           float& r1, float& r2) {
+  if constexpr (EPI == EPI_SILU || EPI == EPI_SILU_D4) {
+    const float h = mlp::silu(v);
+    r1 = a.q1 ? mlp::bf16r(h) : h;
+    if constexpr (EPI == EPI_SILU_D4) {
+      const float d = mlp::dsilu(v) * cv;
+      r2 = a.q2 ? mlp::bf16r(d) : d;
+    }
+  } else if constexpr (EPI == EPI_DMUL) {
+    float sd = mlp::dsilu(x1);
+    if (a.q1) sd = mlp::bf16r(sd);
+    const float d = sd * v;
+    r1 = a.q2 ? mlp::bf16r(d) : d;
+  } else if constexpr (EPI == EPI_DD) {
+    float sd = mlp::dsilu(x1);
+    if (a.q1) sd = mlp::bf16r(sd);
+    r1 = sd * v;
+    r2 = mlp::d2silu(x1) * x2 * v;
+  } else if constexpr (EPI == EPI_ZBACC) {
+    r1 = xo + mlp::dsilu(x1) * v;
+  } else if constexpr (EPI == EPI_ZB4) {
+    r1 = mlp::d2silu(x1) * cv * v + mlp::dsilu(x1) * rv * cv;
+  }
+}
 
 __device__ __forceinline__ uint16_t bf16_bits(float f) {
   uint32_t r;
@@ -158,7 +213,7 @@ __device__ __forceinline__ void prefetch_l2(const float* p) { asm volatile("pref
 // there.
 template <int EPI>
 __device__ __forceinline__ void prefetch_epilogue(const Args& a, int m0, int n0) {
-  if constexpr (EPI == EPI_DMUL || EPI == EPI_DD || EPI == EPI_ZBACC) {
+  if constexpr (epi_reads_e1<EPI>()) {
     for (int i = threadIdx.x; i < BM * (BN / 32); i += NTHREADS) {
       const int m = m0 + (i >> 2), n = n0 + (i & 3) * 32;
       if (m >= a.M || n >= a.N) continue;
@@ -168,37 +223,6 @@ __device__ __forceinline__ void prefetch_epilogue(const Args& a, int m0, int n0)
       if constexpr (EPI == EPI_ZBACC) prefetch_l2(a.o1 + idx);
     }
   }
-}
-
-// v: four consecutive outputs C[m][n..n+3] (beta and bias applied); x1, x2,
-// xo: the fused step's operands at the same places. Stores what EPI asks.
-template <int EPI>
-__device__ __forceinline__ void finish4(const Args& a, int64_t idx, const float (&v)[4], const float (&x1)[4],
-                                        const float (&x2)[4], const float (&xo)[4]) {
-  float r1[4], r2[4];
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    if constexpr (EPI == EPI_SILU) {
-      const float h = mlp::silu(v[k]);
-      r1[k] = a.q1 ? mlp::bf16r(h) : h;
-    } else if constexpr (EPI == EPI_DMUL) {
-      float sd = mlp::dsilu(x1[k]);
-      if (a.q1) sd = mlp::bf16r(sd);
-      const float d = sd * v[k];
-      r1[k] = a.q2 ? mlp::bf16r(d) : d;
-    } else if constexpr (EPI == EPI_DD) {
-      float sd = mlp::dsilu(x1[k]);
-      if (a.q1) sd = mlp::bf16r(sd);
-      r1[k] = sd * v[k];
-      r2[k] = mlp::d2silu(x1[k]) * x2[k] * v[k];
-    } else if constexpr (EPI == EPI_ZBACC) {
-      r1[k] = xo[k] + mlp::dsilu(x1[k]) * v[k];
-    }
-  }
-  if constexpr (EPI == EPI_NONE || EPI == EPI_SILU || EPI == EPI_DMUL)
-    *reinterpret_cast<float4*>(a.C + idx) = make_float4(v[0], v[1], v[2], v[3]);
-  if constexpr (EPI != EPI_NONE) *reinterpret_cast<float4*>(a.o1 + idx) = make_float4(r1[0], r1[1], r1[2], r1[3]);
-  if constexpr (EPI == EPI_DD) *reinterpret_cast<float4*>(a.o2 + idx) = make_float4(r2[0], r2[1], r2[2], r2[3]);
 }
 
 __device__ __forceinline__ void ld4(const float* p, float (&x)[4]) {
@@ -220,17 +244,19 @@ __device__ __forceinline__ void store_tile(const Args& a, const float* out, int 
   constexpr int WARPS = NTHREADS / 32, RG = 4;
   const bool partial = gridDim.z > 1;
   const bool ld_c = !partial && a.beta != 0.0f;
-  constexpr bool ld_e1 = EPI == EPI_DMUL || EPI == EPI_DD || EPI == EPI_ZBACC;
+  constexpr bool ld_e1 = epi_reads_e1<EPI>();
+  constexpr bool use_cv = EPI == EPI_SILU_D4 || EPI == EPI_ZB4, use_rv = EPI == EPI_ZB4;
   if (vec) {
     const int c = 4 * lane, n = n0 + c;
     if (n >= a.N) return;
-    float bias[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-    if (!partial && a.bias) {
+    float bias[4] = {0.0f, 0.0f, 0.0f, 0.0f}, cv[4] = {0.0f, 0.0f, 0.0f, 0.0f};
 #pragma unroll
-      for (int k = 0; k < 4; ++k) bias[k] = a.bias[n + k];
+    for (int k = 0; k < 4; ++k) {
+      if (!partial && a.bias) bias[k] = a.bias[n + k];
+      if constexpr (use_cv) cv[k] = a.cvec[n + k];
     }
     for (int g = 0; g < BM / WARPS; g += RG) {
-      float xc[RG][4], x1[RG][4], x2[RG][4], xo[RG][4];
+      float xc[RG][4], x1[RG][4], x2[RG][4], xo[RG][4], rv[RG];
 #pragma unroll
       for (int i = 0; i < RG; ++i) {
         const int m = m0 + warp + (g + i) * WARPS;
@@ -238,6 +264,8 @@ __device__ __forceinline__ void store_tile(const Args& a, const float* out, int 
         const bool in = m < a.M;
 #pragma unroll
         for (int k = 0; k < 4; ++k) xc[i][k] = x1[i][k] = x2[i][k] = xo[i][k] = 0.0f;
+        rv[i] = 0.0f;
+        if constexpr (use_rv) if (in) rv[i] = a.rvec[m];
         if (in && ld_c) ld4(a.C + idx, xc[i]);
         if constexpr (ld_e1) if (in) ld4(a.e1 + idx, x1[i]);
         if constexpr (EPI == EPI_DD) if (in) ld4(a.e2 + idx, x2[i]);
@@ -253,12 +281,19 @@ __device__ __forceinline__ void store_tile(const Args& a, const float* out, int 
           *reinterpret_cast<float4*>(a.part + ((int64_t)blockIdx.z * a.M + m) * a.N + n) = t;
           continue;
         }
+        float r1[4], r2[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
           if (ld_c) v[k] = fmaf(a.beta, xc[i][k], v[k]);
           v[k] += bias[k];
+          fused_step<EPI>(a, v[k], x1[i][k], x2[i][k], xo[i][k], cv[k], rv[i], r1[k], r2[k]);
         }
-        finish4<EPI>(a, (int64_t)m * a.ldc + n, v, x1[i], x2[i], xo[i]);
+        const int64_t idx = (int64_t)m * a.ldc + n;
+        if constexpr (epi_stores_c<EPI>()) *reinterpret_cast<float4*>(a.C + idx) = make_float4(v[0], v[1], v[2], v[3]);
+        if constexpr (EPI != EPI_NONE)
+          *reinterpret_cast<float4*>(a.o1 + idx) = make_float4(r1[0], r1[1], r1[2], r1[3]);
+        if constexpr (epi_writes_o2<EPI>())
+          *reinterpret_cast<float4*>(a.o2 + idx) = make_float4(r2[0], r2[1], r2[2], r2[3]);
       }
     }
     return;
@@ -277,28 +312,15 @@ __device__ __forceinline__ void store_tile(const Args& a, const float* out, int 
       const int64_t idx = (int64_t)m * a.ldc + n;
       if (ld_c) v = fmaf(a.beta, a.C[idx], v);
       if (a.bias) v += a.bias[n];
-      if constexpr (EPI == EPI_NONE) {
-        a.C[idx] = v;
-      } else if constexpr (EPI == EPI_SILU) {
-        a.C[idx] = v;
-        const float h = mlp::silu(v);
-        a.o1[idx] = a.q1 ? mlp::bf16r(h) : h;
-      } else if constexpr (EPI == EPI_DMUL) {
-        a.C[idx] = v;
-        float sd = mlp::dsilu(a.e1[idx]);
-        if (a.q1) sd = mlp::bf16r(sd);
-        const float d = sd * v;
-        a.o1[idx] = a.q2 ? mlp::bf16r(d) : d;
-      } else if constexpr (EPI == EPI_DD) {
-        const float z = a.e1[idx];
-        float sd = mlp::dsilu(z);
-        if (a.q1) sd = mlp::bf16r(sd);
-        const float ee = a.e2[idx];
-        a.o1[idx] = sd * v;
-        a.o2[idx] = mlp::d2silu(z) * ee * v;
-      } else {  // EPI_ZBACC
-        a.o1[idx] += mlp::dsilu(a.e1[idx]) * v;
-      }
+      const float x1 = ld_e1 ? a.e1[idx] : 0.0f;
+      const float x2 = EPI == EPI_DD ? a.e2[idx] : 0.0f;
+      const float xo = EPI == EPI_ZBACC ? a.o1[idx] : 0.0f;
+      const float cv = use_cv ? a.cvec[n] : 0.0f, rv = use_rv ? a.rvec[m] : 0.0f;
+      float r1 = 0.0f, r2 = 0.0f;
+      fused_step<EPI>(a, v, x1, x2, xo, cv, rv, r1, r2);
+      if constexpr (epi_stores_c<EPI>()) a.C[idx] = v;
+      if constexpr (EPI != EPI_NONE) a.o1[idx] = r1;
+      if constexpr (epi_writes_o2<EPI>()) a.o2[idx] = r2;
     }
   }
 }
@@ -312,7 +334,13 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_tc_gemm(Args a) {
   __shared__ int fail_s;
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
   const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
-  const int kbeg = blockIdx.z * a.kchunk;
+  const bool second = a.A2 != nullptr && (int)blockIdx.z >= a.z2;
+  const float* const A = second ? a.A2 : a.A;
+  const float* const Bm = second ? a.B2 : a.B;
+  const int64_t sam = second ? a.sam2 : a.sam, sak = second ? a.sak2 : a.sak;
+  const int64_t sbn = second ? a.sbn2 : a.sbn, sbk = second ? a.sbk2 : a.sbk;
+  const int split_a = second ? a.split_a2 : a.split_a, split_b = second ? a.split_b2 : a.split_b;
+  const int kbeg = (second ? (int)blockIdx.z - a.z2 : (int)blockIdx.z) * a.kchunk;
   const int kend = min(a.K, kbeg + a.kchunk);
   const int nk = kend > kbeg ? (kend - kbeg + BK - 1) / BK : 0;
   if (t == 0) {
@@ -335,8 +363,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_tc_gemm(Args a) {
   Frag<BM> fa;
   Frag<BN> fb;
   if (nk > 0) {
-    fetch<BM>(fa, a.A, a.sam, a.sak, m0, a.M, kbeg, kend);
-    fetch<BN>(fb, a.B, a.sbn, a.sbk, n0, a.N, kbeg, kend);
+    fetch<BM>(fa, A, sam, sak, m0, a.M, kbeg, kend);
+    fetch<BN>(fb, Bm, sbn, sbk, n0, a.N, kbeg, kend);
   }
   for (int kb = 0; kb < nk; ++kb) {
     const int s = kb & 1;
@@ -344,12 +372,12 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_tc_gemm(Args a) {
     if (kb >= 2 && !tc::mbar_wait(&done[s], (uint32_t)((kb / 2 - 1) & 1), WAIT_LIMIT)) fail_s = 1;
     __syncthreads();
     if (fail_s) break;
-    put<BM>(fa, st, st + A_BLK, a.sak == 1, a.split_a);
-    put<BN>(fb, st + 2 * A_BLK, st + 2 * A_BLK + B_BLK, a.sbk == 1, a.split_b);
+    put<BM>(fa, st, st + A_BLK, sak == 1, split_a);
+    put<BN>(fb, st + 2 * A_BLK, st + 2 * A_BLK + B_BLK, sbk == 1, split_b);
     if (kb + 1 < nk) {  // the next block's loads in flight across the barrier and the product issue
       const int k1 = kbeg + (kb + 1) * BK;
-      fetch<BM>(fa, a.A, a.sam, a.sak, m0, a.M, k1, kend);
-      fetch<BN>(fb, a.B, a.sbn, a.sbk, n0, a.N, k1, kend);
+      fetch<BM>(fa, A, sam, sak, m0, a.M, k1, kend);
+      fetch<BN>(fb, Bm, sbn, sbk, n0, a.N, k1, kend);
     }
     tc::fence_proxy_async_smem();
     __syncthreads();
@@ -359,8 +387,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_tc_gemm(Args a) {
 #pragma unroll
       for (int ks = 0; ks < 4; ++ks) {
         tc::mma_bf16(tmem, tc::desc_sw128(ah + ks * 32), tc::desc_sw128(bh + ks * 32), idesc, (kb | ks) != 0);
-        if (a.split_b) tc::mma_bf16(tmem, tc::desc_sw128(ah + ks * 32), tc::desc_sw128(bl + ks * 32), idesc, 1);
-        if (a.split_a) tc::mma_bf16(tmem, tc::desc_sw128(al + ks * 32), tc::desc_sw128(bh + ks * 32), idesc, 1);
+        if (split_b) tc::mma_bf16(tmem, tc::desc_sw128(ah + ks * 32), tc::desc_sw128(bl + ks * 32), idesc, 1);
+        if (split_a) tc::mma_bf16(tmem, tc::desc_sw128(al + ks * 32), tc::desc_sw128(bh + ks * 32), idesc, 1);
       }
       tc::mma_commit(&done[s]);
     }

@@ -37,6 +37,9 @@ WORKLOADS = {
               "radii log-uniform 0.5-100 kpc, durations log-uniform 0.1-5 Gyr, 10-1000 saves/orbit, "
               "one persistent launch",
     "plain": "plain small: MilkyWayPotential, Dopri8 fixed dt=1 Myr over 1 Gyr, 100 uniform saves",
+    "train": "surrogate training alone: MLP 3-256-256-256-256-1 SiLU fitted to the subhalo remainder beyond "
+             "12 kpc (potential and gradient, exact second-order loss gradient, Adam), batch 8192, "
+             "one CUDA graph per step, tensor-core products (bf16, split bf16x3 where FP32 accuracy is needed)",
     "subhalos": "plain FP64 direct sum: MilkyWayPotential + 512 Plummer subhalos (the learned surrogate's tables), "
                 "Dopri5 fixed dt=1 Myr over 1 Gyr, disk-like orbits at 4-20 kpc, final state saved",
     "grad": "differentiation: MilkyWayPotential, Dopri8 fixed dt=0.5 Myr over 2 Gyr, squared-distance loss, "
@@ -55,7 +58,7 @@ WORKLOADS = {
            "(random weights), fused tensor-core kernel",
 }
 DEFAULT_ORBITS = {"uneven": 262_144, "plain": 1024, "subhalos": 65_536, "grad": 65_536, "surrogate": 1_048_576,
-                  "mlp": 1_048_576, "stream": 3000}
+                  "mlp": 1_048_576, "stream": 3000, "train": 0}
 
 
 def dist_env():
@@ -184,6 +187,8 @@ def run_ours(args) -> dict | None:
         return run_plain(args, n, rank, world, dist)
     if args.workload == "subhalos":
         return run_subhalos(args, n, rank, world, dist)
+    if args.workload == "train":
+        return run_train(args, rank, world, dist)
     if args.workload == "surrogate":
         return run_surrogate(args, n, rank, world, dist)
     if args.workload == "mlp":
@@ -701,6 +706,65 @@ def run_subhalos(args, n, rank, world, dist) -> dict | None:
                          "frac_of_issue_ceiling": achieved / peak["issue_ceiling_tflops"],
                          "frac": achieved / peak["tflops"], "flops_per_step": STEP_FLOPS_MW_SUBHALOS[5]},
             "clocks": clk, "gpu_launches": args.steps}
+
+
+# algorithmic flops of one training step (batch b): 18 products of 2 b 256^2
+# (forward 3, input gradient 3, second-order pass 6, weight gradients 6 terms)
+# plus the 3-wide and 1-wide first/last-layer products
+def train_step_flops(b: int) -> float:
+    return b * (18 * 2 * 256 * 256 + 6 * 2 * 3 * 256 + 4 * 2 * 256)
+
+
+def run_train(args, rank, world, dist) -> dict | None:
+    """Surrogate training alone: training steps/s of the device-driven loop
+    (gal_mlp_train, one CUDA graph per step) on the surrogate workload's data."""
+    import torch
+
+    from galax_gb300 import surrogate as S
+    from galax_gb300 import workloads as W
+
+    _, sub, _ = subhalo_tables()
+    npts, batch = args.train_points, 8192
+    xt = torch.as_tensor(W.training_points(npts, seed=30), device="cuda")
+    phi_t, g_t = sub.potential(xt), sub.gradient(xt)
+    near = S.ShortRange(sub, args.split_radius) if args.split_radius > 0 else None
+    if near is not None:
+        ps, gs = near.evaluate(xt)
+        phi_t, g_t = phi_t - ps, g_t - gs
+    stream = torch.cuda.current_stream()
+
+    def step():
+        return S.train(xt, phi_t, g_t, length_scale=50.0, epochs=args.train_epochs, batch=batch, lr=2e-3)
+
+    for _ in range(args.warmup):
+        step()
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", 0)))
+    clocks.start()
+    ms = _max_over_ranks(_timed(step, args.steps, stream), dist)
+    clk = clocks.stop()
+    _, rep = step()
+    if rank != 0:
+        return None
+    nsteps = (npts // batch) * args.train_epochs
+    per_step_ms = ms / nsteps
+    peaks = measured_peaks()
+    achieved = train_step_flops(batch) / (per_step_ms * 1e-3) / 1e12
+    return {"metric": "training steps/s", "value": world * nsteps / (ms * 1e-3), "unit": "steps/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16 / bf16x3, f32 accumulate",
+            "data": "synthetic", "ms_per_training_step": per_step_ms,
+            "seconds_for_400_epochs_on_4M_points": per_step_ms * 1e-3 * (4_194_304 // batch) * 400,
+            "config": {"workload": WORKLOADS["train"], "train_points": npts, "train_epochs": args.train_epochs,
+                       "batch": batch, "training_steps_per_bench_step": nsteps,
+                       "loss_first_last": [rep.loss[0], rep.loss[-1]]},
+            "roofline": {"bound": "latency (kernel chain)", "achieved": achieved, "peak": peaks.get("bf16_tflops"),
+                         "unit": "TFLOP/s", "frac": achieved / peaks["bf16_tflops"] if peaks.get("bf16_tflops") else None,
+                         "flops_per_training_step": train_step_flops(batch),
+                         "note": "algorithmic flops; the 8192-row products are too small to fill the tensor cores, so "
+                                 "the step is set by the chain of ~30 dependent kernels"},
+            # per training step: gather, 9 forward/input-gradient kernels, 23 of the second-order pass
+            # (12 products, 3 split-K sums, 8 column-sum and loss kernels), Adam and the step counter
+            "clocks": clk, "gpu_launches": args.steps * nsteps * 35}
 
 
 def run_surrogate(args, n, rank, world, dist) -> dict | None:

@@ -166,6 +166,8 @@ __global__ void __launch_bounds__(256) k_layer1(const float* __restrict__ X, con
                                                 const float* __restrict__ b1, const float* __restrict__ Z,
                                                 const float* __restrict__ U, float* __restrict__ o1,
                                                 float* __restrict__ o2, int64_t rows, int q) {
+  tc::pdl_wait();
+  tc::pdl_trigger();
   const int c = threadIdx.x;
   const float w0 = W1[3 * c], w1 = W1[3 * c + 1], w2 = W1[3 * c + 2];
   const float bc = MODE == 0 ? b1[c] : 0.0f;
@@ -209,6 +211,8 @@ constexpr int kColRows = 64;
 template <int mode>
 __global__ void __launch_bounds__(256) k_colpart(const float* X, const float* Y, const float* v, const float* V,
                                                  int64_t rows, float* part) {
+  tc::pdl_wait();
+  tc::pdl_trigger();
   __shared__ float red[3][8][H];
   const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
   const int64_t b0 = (int64_t)blockIdx.x * kColRows + wp * 8;
@@ -279,8 +283,8 @@ __global__ void __launch_bounds__(256) k_colpart(const float* X, const float* Y,
 // the chunks of part[j][0] (and then those of part[j][1], when set) for each
 // of its H * nj outputs and stores the total (first + second) to out[j];
 // a job with nj = 0 is the sum of n0 scalars part[j][0][0..n0) (the output
-// bias gradient from the loss kernel's per-block sums).
-constexpr int kColJobs = 7;
+// bias gradient and the loss from the loss kernel's per-block sums).
+constexpr int kColJobs = 8;
 struct ColJobs {
   const float* part[kColJobs][2];
   float* out[kColJobs];
@@ -292,6 +296,8 @@ struct ColJobs {
 // grid (H / 32, jobs): 32 columns per block; the 8 warps sum interleaved
 // chunks, then one warp adds the 8 partial sums in a fixed order.
 __global__ void __launch_bounds__(256) k_colfinal_all(ColJobs J) {
+  tc::pdl_wait();
+  tc::pdl_trigger();
   __shared__ float red[8][32][3];
   const int job = blockIdx.y;
   const int cl = threadIdx.x & 31, g = threadIdx.x >> 5;
@@ -343,6 +349,8 @@ __global__ void __launch_bounds__(256) k_colfinal_all(ColJobs J) {
 // (coalesced), a fixed-order shuffle reduction.
 __global__ void __launch_bounds__(256) k_rowdot(const float* X, const float* W, const float* bias, int64_t rows,
                                                 int ncol, float* out) {
+  tc::pdl_wait();
+  tc::pdl_trigger();
   const int lane = threadIdx.x & 31;
   const int64_t b = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
   if (b >= rows) return;
@@ -361,10 +369,12 @@ __global__ void __launch_bounds__(256) k_rowdot(const float* X, const float* W, 
 
 // residuals, their loss weights and the loss value
 // (optional per-point weights wt[b] multiply both terms of point b)
-// pbsum[block] = the block's sum of Pb (added in a fixed order: the output
-// bias gradient)
+// lpart[block] = the block's share of the loss and pbsum[block] its sum of Pb
+// (the output bias gradient), both added up in a fixed order afterwards
 __global__ void k_loss(const float* out, const float* G, const float* phi_t, const float* g_t, const float* wt,
-                       int64_t B, float alpha, float beta, float* Pb, float* Eb, float* loss, float* pbsum) {
+                       int64_t B, float alpha, float beta, float* Pb, float* Eb, float* lpart, float* pbsum) {
+  tc::pdl_wait();
+  tc::pdl_trigger();
   float s = 0.0f, ps = 0.0f;
   GRID_STRIDE(b, B) {
     const float w = wt ? wt[b] : 1.0f;
@@ -391,13 +401,15 @@ __global__ void k_loss(const float* out, const float* G, const float* phi_t, con
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    atomicAdd(loss, red[0][0] / (float)B);
+    lpart[blockIdx.x] = red[0][0] / (float)B;
     pbsum[blockIdx.x] = red[1][0];
   }
 }
 
 __global__ void k_adam(float* p, const float* g, float* m, float* v, int64_t n, float lr, float b1, float b2,
                        float eps, float c1, float c2) {
+  tc::pdl_wait();
+  tc::pdl_trigger();
   GRID_STRIDE(i, n) {
     const float gi = g[i];
     const float mi = b1 * m[i] + (1.0f - b1) * gi;
@@ -412,6 +424,7 @@ struct Ws {
   float *Z[5], *Hh[5], *D[5], *U[4], *Zb[5], *Db, *Ub, *Ub2, *Ub3, *Hb, *out, *G, *Pb, *Eb;  // Ub1, Ub2, Ub3
   float* colpart;  // [kColSlots][chunks][H][3] partial column sums, one slot per column sum of a step
   float* pbsum;    // [kLossBlocks] per-block sums of Pb
+  float* lpart;    // [kLossBlocks] per-block shares of the loss
   float* splitk;   // [kMaxSplits][H][H] partial tiles of the tensor-core weight gradients
   int* err;  // set by a tensor-core product that gave up waiting (gal_mlp_workspace_error)
 };
@@ -424,7 +437,7 @@ constexpr int kLossBlocks = 4096;  // k_loss's largest grid (ew_grid)
 static size_t ws_bytes(int64_t B) {
   const size_t big = sizeof(float) * (size_t)B * H;
   return big * (4 + 4 + 4 + 3 + 4 + 5) + sizeof(float) * (size_t)B * (1 + 3 + 1 + 3) +
-         sizeof(float) * (size_t)kColSlots * col_chunks(B) * H * 3 + sizeof(float) * kLossBlocks +
+         sizeof(float) * (size_t)kColSlots * col_chunks(B) * H * 3 + sizeof(float) * 2 * kLossBlocks +
          sizeof(float) * (size_t)kMaxSplits * H * H + 64 * 256;
 }
 
@@ -456,6 +469,7 @@ static Ws carve(void* ws, int64_t B) {
   w.err = reinterpret_cast<int*>(take(256));
   w.colpart = take(sizeof(float) * (size_t)kColSlots * col_chunks(B) * H * 3);
   w.pbsum = take(sizeof(float) * kLossBlocks);
+  w.lpart = take(sizeof(float) * kLossBlocks);
   w.splitk = take(sizeof(float) * (size_t)kMaxSplits * H * H);
   return w;
 }
@@ -476,6 +490,25 @@ struct Epi {
   int q1 = 0, q2 = 0;
 };
 
+// Launch with programmatic stream serialization (the kernel calls
+// tc::pdl_wait() before touching global memory): its blocks may be scheduled,
+// and run their set-up, while the kernel before it in the stream finishes.
+template <typename... KArgs, typename... Args>
+static void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                       Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
 // the tensor-core product kernels' shared-memory opt-in, once per device
 static bool tc_configure() {
   static std::atomic<int> configured[64] = {};
@@ -487,7 +520,7 @@ static bool tc_configure() {
                          (const void*)tcg::k_tc_gemm<tcg::EPI_ZBACC>, (const void*)tcg::k_tc_gemm<tcg::EPI_SILU_D4>,
                          (const void*)tcg::k_tc_gemm<tcg::EPI_ZB4>};
     for (const void* f : fns)
-      if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tcg::SMEM_ALLOC) != cudaSuccess)
+      if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tcg::SMEM_MAX) != cudaSuccess)
         return false;
     configured[dev].store(1);
   }
@@ -534,8 +567,11 @@ static bool tc_wgrad2(cudaStream_t s, int K, const float* A1, const float* B1, i
   const int z = (K + a.kchunk - 1) / a.kchunk;
   a.z2 = z;
   const dim3 grid(H / tcg::BN, H / tcg::BM, 2 * z);
-  tcg::k_tc_gemm<tcg::EPI_NONE><<<grid, tcg::NTHREADS, tcg::SMEM_ALLOC, s>>>(a);
-  tcg::k_splitk_sum<<<(unsigned)((H * H + 255) / 256), 256, 0, s>>>(part, 2 * z, H, H, C, H, 0.0f);
+  const uint32_t st1 = tcg::stage_bytes(split_a1, split_b1), st2 = tcg::stage_bytes(split_a2, split_b2);
+  a.stage = st1 > st2 ? st1 : st2;
+  launch_pdl(tcg::k_tc_gemm<tcg::EPI_NONE>, grid, tcg::NTHREADS, tcg::smem_alloc(a.stage), s, a);
+  launch_pdl(tcg::k_splitk_sum, dim3((H * H + 255) / 256), 256, 0, s, (const float*)part, 2 * z, (int)H, (int)H, C,
+             (int64_t)H, 0.0f);
   return true;
 }
 
@@ -587,18 +623,21 @@ static bool tc_gemm(cudaStream_t s, bool TA, bool TB, int M, int N, int K, const
       a.part = part;
     }
   }
+  a.stage = tcg::stage_bytes(split_a, split_b);
+  const uint32_t smem = tcg::smem_alloc(a.stage);
   switch (epi.mode) {
-    case tcg::EPI_SILU: tcg::k_tc_gemm<tcg::EPI_SILU><<<grid, tcg::NTHREADS, tcg::SMEM_ALLOC, s>>>(a); break;
-    case tcg::EPI_DMUL: tcg::k_tc_gemm<tcg::EPI_DMUL><<<grid, tcg::NTHREADS, tcg::SMEM_ALLOC, s>>>(a); break;
-    case tcg::EPI_DD: tcg::k_tc_gemm<tcg::EPI_DD><<<grid, tcg::NTHREADS, tcg::SMEM_ALLOC, s>>>(a); break;
-    case tcg::EPI_ZBACC: tcg::k_tc_gemm<tcg::EPI_ZBACC><<<grid, tcg::NTHREADS, tcg::SMEM_ALLOC, s>>>(a); break;
-    case tcg::EPI_SILU_D4: tcg::k_tc_gemm<tcg::EPI_SILU_D4><<<grid, tcg::NTHREADS, tcg::SMEM_ALLOC, s>>>(a); break;
-    case tcg::EPI_ZB4: tcg::k_tc_gemm<tcg::EPI_ZB4><<<grid, tcg::NTHREADS, tcg::SMEM_ALLOC, s>>>(a); break;
-    default: tcg::k_tc_gemm<tcg::EPI_NONE><<<grid, tcg::NTHREADS, tcg::SMEM_ALLOC, s>>>(a); break;
+    case tcg::EPI_SILU: launch_pdl(tcg::k_tc_gemm<tcg::EPI_SILU>, grid, tcg::NTHREADS, smem, s, a); break;
+    case tcg::EPI_DMUL: launch_pdl(tcg::k_tc_gemm<tcg::EPI_DMUL>, grid, tcg::NTHREADS, smem, s, a); break;
+    case tcg::EPI_DD: launch_pdl(tcg::k_tc_gemm<tcg::EPI_DD>, grid, tcg::NTHREADS, smem, s, a); break;
+    case tcg::EPI_ZBACC: launch_pdl(tcg::k_tc_gemm<tcg::EPI_ZBACC>, grid, tcg::NTHREADS, smem, s, a); break;
+    case tcg::EPI_SILU_D4: launch_pdl(tcg::k_tc_gemm<tcg::EPI_SILU_D4>, grid, tcg::NTHREADS, smem, s, a); break;
+    case tcg::EPI_ZB4: launch_pdl(tcg::k_tc_gemm<tcg::EPI_ZB4>, grid, tcg::NTHREADS, smem, s, a); break;
+    default: launch_pdl(tcg::k_tc_gemm<tcg::EPI_NONE>, grid, tcg::NTHREADS, smem, s, a); break;
   }
   if (grid.z > 1) {
     const int64_t mn = (int64_t)M * N;
-    tcg::k_splitk_sum<<<(unsigned)((mn + 255) / 256), 256, 0, s>>>(part, (int)grid.z, M, N, C, ldc, beta);
+    launch_pdl(tcg::k_splitk_sum, dim3((unsigned)((mn + 255) / 256)), 256, 0, s, (const float*)part, (int)grid.z, M,
+               N, C, (int64_t)ldc, beta);
   }
   return true;
 }
@@ -658,10 +697,10 @@ static void colpart(cudaStream_t s, const Ws& w, const float* X, const float* Y,
   const unsigned g = (unsigned)col_chunks(B);
   float* part = col_slot(w, B, slot);
   switch (mode) {
-    case 0: k_colpart<0><<<g, H, 0, s>>>(X, Y, v, V, B, part); break;
-    case 1: k_colpart<1><<<g, H, 0, s>>>(X, Y, v, V, B, part); break;
-    case 2: k_colpart<2><<<g, H, 0, s>>>(X, Y, v, V, B, part); break;
-    default: k_colpart<3><<<g, H, 0, s>>>(X, Y, v, V, B, part); break;
+    case 0: launch_pdl(k_colpart<0>, g, H, 0, s, X, Y, v, V, B, part); break;
+    case 1: launch_pdl(k_colpart<1>, g, H, 0, s, X, Y, v, V, B, part); break;
+    case 2: launch_pdl(k_colpart<2>, g, H, 0, s, X, Y, v, V, B, part); break;
+    default: launch_pdl(k_colpart<3>, g, H, 0, s, X, Y, v, V, B, part); break;
   }
 }
 
@@ -744,14 +783,16 @@ static Epi epi_zb4(const float* z, const float* w5, const float* pb, float* zb) 
 static void forward_backward(cudaStream_t s, const float* P, const float* x, int64_t B, const Ws& w, int q) {
   const int Bi = (int)B;
   const unsigned l1_blocks = (unsigned)((B + kL1Rows - 1) / kL1Rows);
-  k_layer1<0><<<l1_blocks, H, 0, s>>>(x, P + OFF_W1, P + OFF_B1, nullptr, nullptr, w.Z[1], w.Hh[1], B, q);
+  launch_pdl(k_layer1<0>, l1_blocks, H, 0, s, x, P + OFF_W1, P + OFF_B1, (const float*)nullptr, (const float*)nullptr,
+             w.Z[1], w.Hh[1], B, q);
   gemm<false, true>(s, w, Bi, H, H, w.Hh[1], H, P + OFF_W2, H, w.Z[2], H, 0.0f, P + OFF_B2, q, q,
                     epi_silu(w.Hh[2], q));
   gemm<false, true>(s, w, Bi, H, H, w.Hh[2], H, P + OFF_W3, H, w.Z[3], H, 0.0f, P + OFF_B3, q, q,
                     epi_silu(w.Hh[3], q));
   gemm<false, true>(s, w, Bi, H, H, w.Hh[3], H, P + OFF_W4, H, w.Z[4], H, 0.0f, P + OFF_B4, q, q,
                     epi_silu_d4(w.Hh[4], 0, P + OFF_W5, w.D[4], q));  // and D4 = silu'(Z4) w5
-  k_rowdot<<<(unsigned)((B + 7) / 8), 256, 0, s>>>(w.Hh[4], P + OFF_W5, P + OFF_B5, B, 1, w.out);
+  launch_pdl(k_rowdot, dim3((unsigned)((B + 7) / 8)), 256, 0, s, (const float*)w.Hh[4], P + OFF_W5, P + OFF_B5, B, 1,
+             w.out);
   // input gradient
   gemm<false, false>(s, w, Bi, H, H, w.D[4], H, P + OFF_W4, H, w.U[3], H, 0.0f, nullptr, q, q,
                      epi_dmul(w.Z[3], w.D[3], q, q));
@@ -759,7 +800,65 @@ static void forward_backward(cudaStream_t s, const float* P, const float* x, int
                      epi_dmul(w.Z[2], w.D[2], q, q));
   gemm<false, false>(s, w, Bi, H, H, w.D[2], H, P + OFF_W2, H, w.U[1], H, 0.0f, nullptr, q, q,
                      epi_dmul(w.Z[1], w.D[1], 0, 0));
-  k_rowdot<<<(unsigned)((B + 7) / 8), 256, 0, s>>>(w.D[1], P + OFF_W1, nullptr, B, 3, w.G);
+  launch_pdl(k_rowdot, dim3((unsigned)((B + 7) / 8)), 256, 0, s, (const float*)w.D[1], P + OFF_W1,
+             (const float*)nullptr, B, 3, w.G);
+}
+
+// A second stream for the work of a training step that is off its critical
+// path: the weight gradients and column sums run beside the chain of
+// input-gradient products, on SMs and shared memory those leave free. Stream
+// and fork/join events are created once per thread and device and reused (an
+// event is re-recorded by every step, and a wait takes the record current at
+// the time of the wait, so a set is never shared between threads). Without
+// them everything runs on the caller's stream, in the same order.
+constexpr int kSideEvents = 5;
+struct SideStream {
+  cudaStream_t st[64] = {};
+  cudaEvent_t ev[64][kSideEvents] = {};
+  ~SideStream() {
+    for (int d = 0; d < 64; ++d) {
+      for (cudaEvent_t e : ev[d])
+        if (e) cudaEventDestroy(e);
+      if (st[d]) cudaStreamDestroy(st[d]);
+    }
+  }
+};
+
+struct Side {
+  cudaStream_t main, side;  // side == main when no second stream could be made
+  cudaEvent_t* ev;
+  void fork(int k) const {
+    if (side == main) return;
+    cudaEventRecord(ev[k], main);
+    cudaStreamWaitEvent(side, ev[k], 0);
+  }
+  void join(int k) const {
+    if (side == main) return;
+    cudaEventRecord(ev[k], side);
+    cudaStreamWaitEvent(main, ev[k], 0);
+  }
+};
+
+static Side side_of(cudaStream_t s) {
+  thread_local SideStream cache;
+  Side r{s, s, nullptr};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return r;
+  if (!cache.st[dev]) {
+    cudaStream_t st = nullptr;
+    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return r;
+    for (int k = 0; k < kSideEvents; ++k)
+      if (cudaEventCreateWithFlags(&cache.ev[dev][k], cudaEventDisableTiming) != cudaSuccess) {
+        for (int j = 0; j <= k; ++j)
+          if (cache.ev[dev][j]) cudaEventDestroy(cache.ev[dev][j]), cache.ev[dev][j] = nullptr;
+        cudaStreamDestroy(st);
+        return r;
+      }
+    cache.st[dev] = st;
+  }
+  r.side = cache.st[dev];
+  r.ev = cache.ev[dev];
+  return r;
 }
 
 static void loss_grads(cudaStream_t s, const float* P, const float* x, const float* phi_t, const float* g_t,
@@ -767,16 +866,23 @@ static void loss_grads(cudaStream_t s, const float* P, const float* x, const flo
                        int q) {
   const int Bi = (int)B;
   forward_backward(s, P, x, B, w, q);
-  cudaMemsetAsync(loss, 0, sizeof(float), s);
   const unsigned loss_blocks = ew_grid(B);
-  k_loss<<<loss_blocks, 256, 0, s>>>(w.out, w.G, phi_t, g_t, wt, B, alpha, beta, w.Pb, w.Eb, loss, w.pbsum);
+  launch_pdl(k_loss, loss_blocks, 256, 0, s, (const float*)w.out, (const float*)w.G, phi_t, g_t, wt, B, alpha, beta,
+             w.Pb, w.Eb, w.lpart, w.pbsum);
   // Column sums go to slots of their own; one launch at the end finishes them all:
   //   0 + 6: gW1 = D1^T Eb + Zb1^T X   1 + 2: gw5 = sum silu'(Z4) Db4 + H4^T Pb
   //   3, 4, 5, 7: gb4, gb3, gb2, gb1   gb5 = sum Pb from k_loss's block sums
+  // The weight gradients and column sums go to the side stream (t), forked
+  // after the products whose results they read; the caller's stream (s)
+  // carries the chain of input-gradient products.
+  const Side sd = side_of(s);
+  const cudaStream_t t = sd.side;
+  sd.fork(0);
+  colpart(t, w, w.D[1], nullptr, nullptr, w.Eb, B, 3, 0);                                     // gW1 = D1^T Eb
+  colpart(t, w, w.Hh[4], nullptr, w.Pb, nullptr, B, 1, 2);                                 // gw5 += H4^T Pb
   // ---- through the input-gradient graph, layer 1 up to 4
-  colpart(s, w, w.D[1], nullptr, nullptr, w.Eb, B, 3, 0);                                     // gW1 = D1^T Eb
-  k_layer1<1><<<(unsigned)((B + kL1Rows - 1) / kL1Rows), H, 0, s>>>(w.Eb, P + OFF_W1, nullptr, w.Z[1], w.U[1], w.Ub,
-                                                                   w.Zb[1], B, 0);           // Db1 = Eb W1^T
+  launch_pdl(k_layer1<1>, dim3((unsigned)((B + kL1Rows - 1) / kL1Rows)), H, 0, s, (const float*)w.Eb, P + OFF_W1,
+             (const float*)nullptr, (const float*)w.Z[1], (const float*)w.U[1], w.Ub, w.Zb[1], B, 0);  // Db1 = Eb W1^T
   // Ub1, Ub2, Ub3 in buffers of their own: each stays until the weight gradient
   // that pairs it with a forward-graph term (gWk = Dk^T Ub(k-1) + Zbk^T H(k-1))
   gemm<false, true>(s, w, Bi, H, H, w.Ub, H, P + OFF_W2, H, w.Db, H, 0.0f, nullptr, 0, q,
@@ -785,35 +891,42 @@ static void loss_grads(cudaStream_t s, const float* P, const float* x, const flo
                     epi_dd(w.Z[3], w.U[3], w.Ub3, w.Zb[3], q));                               // Db3 = Ub2 W3^T
   gemm<false, true>(s, w, Bi, H, H, w.Ub3, H, P + OFF_W4, H, w.Db, H, 0.0f, nullptr, 0, q,
                     epi_zb4(w.Z[4], P + OFF_W5, w.Pb, w.Zb[4]));                              // Db4 = Ub3 W4^T, Zb4
-  colpart(s, w, w.Z[4], w.Db, nullptr, nullptr, B, 2, 1);                                 // gw5 = sum silu'(Z4) Db4
+  sd.fork(1);
+  colpart(t, w, w.Z[4], w.Db, nullptr, nullptr, B, 2, 1);                                 // gw5 = sum silu'(Z4) Db4
   // ---- potential term and the forward graph, layer 4 down to 1
-  colpart(s, w, w.Hh[4], nullptr, w.Pb, nullptr, B, 1, 2);                                 // gw5 += H4^T Pb
-  wgrad2(s, w, Bi, w.D[4], w.Ub3, q, 0, w.Zb[4], w.Hh[3], 0, q, grad + OFF_W4);           // gW4 = D4^T Ub3 + Zb4^T H3
-  colpart(s, w, w.Zb[4], nullptr, nullptr, nullptr, B, 0, 3);
+  wgrad2(t, w, Bi, w.D[4], w.Ub3, q, 0, w.Zb[4], w.Hh[3], 0, q, grad + OFF_W4);           // gW4 = D4^T Ub3 + Zb4^T H3
+  colpart(t, w, w.Zb[4], nullptr, nullptr, nullptr, B, 0, 3);
   gemm<false, false>(s, w, Bi, H, H, w.Zb[4], H, P + OFF_W4, H, w.Hb, H, 0.0f, nullptr, 0, q,
                      epi_zbacc(w.Z[3], w.Zb[3]));                                              // Hb3 = Zb4 W4
-  wgrad2(s, w, Bi, w.D[3], w.Ub2, q, 0, w.Zb[3], w.Hh[2], 0, q, grad + OFF_W3);           // gW3 = D3^T Ub2 + Zb3^T H2
-  colpart(s, w, w.Zb[3], nullptr, nullptr, nullptr, B, 0, 4);
+  sd.fork(2);
+  wgrad2(t, w, Bi, w.D[3], w.Ub2, q, 0, w.Zb[3], w.Hh[2], 0, q, grad + OFF_W3);           // gW3 = D3^T Ub2 + Zb3^T H2
+  colpart(t, w, w.Zb[3], nullptr, nullptr, nullptr, B, 0, 4);
   gemm<false, false>(s, w, Bi, H, H, w.Zb[3], H, P + OFF_W3, H, w.Hb, H, 0.0f, nullptr, 0, q,
                      epi_zbacc(w.Z[2], w.Zb[2]));
-  wgrad2(s, w, Bi, w.D[2], w.Ub, q, 0, w.Zb[2], w.Hh[1], 0, q, grad + OFF_W2);            // gW2 = D2^T Ub1 + Zb2^T H1
-  colpart(s, w, w.Zb[2], nullptr, nullptr, nullptr, B, 0, 5);
+  sd.fork(3);
+  wgrad2(t, w, Bi, w.D[2], w.Ub, q, 0, w.Zb[2], w.Hh[1], 0, q, grad + OFF_W2);            // gW2 = D2^T Ub1 + Zb2^T H1
+  colpart(t, w, w.Zb[2], nullptr, nullptr, nullptr, B, 0, 5);
   gemm<false, false>(s, w, Bi, H, H, w.Zb[2], H, P + OFF_W2, H, w.Hb, H, 0.0f, nullptr, 0, q,
                      epi_zbacc(w.Z[1], w.Zb[1]));
   colpart(s, w, w.Zb[1], nullptr, nullptr, x, B, 3, 6);                                     // gW1 += Zb1^T X
   colpart(s, w, w.Zb[1], nullptr, nullptr, nullptr, B, 0, 7);
   ColJobs J{};
-  const int slot_a[kColJobs] = {0, 1, 3, 4, 5, 7, -1}, slot_b[kColJobs] = {6, 2, -1, -1, -1, -1, -1};
-  const int64_t outs[kColJobs] = {OFF_W1, OFF_W5, OFF_B4, OFF_B3, OFF_B2, OFF_B1, OFF_B5};
-  for (int j = 0; j < kColJobs; ++j) {
-    J.part[j][0] = slot_a[j] >= 0 ? col_slot(w, B, slot_a[j]) : w.pbsum;
+  const int slot_a[kColJobs - 2] = {0, 1, 3, 4, 5, 7}, slot_b[kColJobs - 2] = {6, 2, -1, -1, -1, -1};
+  const int64_t outs[kColJobs - 2] = {OFF_W1, OFF_W5, OFF_B4, OFF_B3, OFF_B2, OFF_B1};
+  for (int j = 0; j < kColJobs - 2; ++j) {
+    J.part[j][0] = col_slot(w, B, slot_a[j]);
     J.part[j][1] = slot_b[j] >= 0 ? col_slot(w, B, slot_b[j]) : nullptr;
     J.out[j] = grad + outs[j];
-    J.nj[j] = j == 0 ? 3 : (j == kColJobs - 1 ? 0 : 1);
+    J.nj[j] = j == 0 ? 3 : 1;
   }
+  J.part[6][0] = w.pbsum;  // gb5
+  J.out[6] = grad + OFF_B5;
+  J.part[7][0] = w.lpart;  // the loss
+  J.out[7] = loss;
   J.chunks = col_chunks(B);
   J.n0 = (int)loss_blocks;
-  k_colfinal_all<<<dim3(H / 32, kColJobs), 256, 0, s>>>(J);
+  sd.join(4);
+  launch_pdl(k_colfinal_all, dim3(H / 32, kColJobs), 256, 0, s, J);
 }
 
 // ---------------------------------------------------------------- device-driven training
@@ -864,11 +977,13 @@ struct TrainRun {
   uint64_t seed;
   float *ub, *pb, *gb, *wb;  // this step's batch
   long long* step;           // device step counter (0-based)
-  const float* loss;         // this step's loss (written by k_loss)
+  const float* loss;         // this step's loss (written by k_colfinal_all)
   float* loss_per_epoch;
 };
 
 __global__ void k_gather(TrainRun r) {
+  tc::pdl_wait();
+  tc::pdl_trigger();
   const long long s = *r.step;
   const int64_t e = s / r.steps_per_epoch, b = s % r.steps_per_epoch;
   const uint32_t key = fmix32((uint32_t)r.seed ^ fmix32((uint32_t)e + 0x632be5abu + (uint32_t)(r.seed >> 32)));
@@ -887,6 +1002,8 @@ __global__ void k_gather(TrainRun r) {
 // Adam with the step's cosine learning rate and bias corrections (step t = s + 1).
 __global__ void k_adam_run(float* p, const float* g, float* m, float* v, int64_t np, const long long* step,
                            int64_t total, float lr, float lr_final, float b1, float b2, float eps) {
+  tc::pdl_wait();
+  tc::pdl_trigger();
   const float t = (float)(*step + 1);
   const float lr_t = lr_final + 0.5f * (lr - lr_final) * (1.0f + cosf(3.14159265358979f * t / (float)total));
   const float c1 = 1.0f - powf(b1, t), c2 = 1.0f - powf(b2, t);
@@ -901,6 +1018,8 @@ __global__ void k_adam_run(float* p, const float* g, float* m, float* v, int64_t
 }
 
 __global__ void k_step_end(TrainRun r) {
+  tc::pdl_wait();
+  tc::pdl_trigger();
   const long long s = *r.step;
   if (r.loss_per_epoch) r.loss_per_epoch[s / r.steps_per_epoch] += *r.loss / (float)r.steps_per_epoch;
   *r.step = s + 1;
@@ -996,8 +1115,8 @@ gal_status gal_mlp_train_step(float* params, float* grad, float* adam_m, float* 
   if (st != GAL_OK) return st;
   if (!adam_m || !adam_v || step < 1) return fail(GAL_ERR_INVALID_ARGUMENT, "Adam state and step >= 1 required");
   const float c1 = 1.0f - powf(beta1, (float)step), c2 = 1.0f - powf(beta2, (float)step);
-  k_adam<<<ew_grid(NPARAM), 256, 0, (cudaStream_t)stream>>>(params, grad, adam_m, adam_v, NPARAM, lr, beta1, beta2,
-                                                            eps, c1, c2);
+  launch_pdl(k_adam, ew_grid(NPARAM), 256, 0, (cudaStream_t)stream, params, (const float*)grad, adam_m, adam_v,
+             NPARAM, lr, beta1, beta2, eps, c1, c2);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? GAL_OK : cuda_fail(e, "MLP Adam update");
 }
@@ -1060,11 +1179,11 @@ gal_status gal_mlp_train(float* params, float* adam_m, float* adam_v, const floa
   if (e == cudaSuccess) e = cudaMemsetAsync(ws + RL.state, 0, 256, s);
   if (e == cudaSuccess && loss_per_epoch) e = cudaMemsetAsync(loss_per_epoch, 0, sizeof(float) * epochs, s);
   auto one_step = [&]() {
-    k_gather<<<ew_grid(batch), 256, 0, s>>>(r);
+    launch_pdl(k_gather, ew_grid(batch), 256, 0, s, r);
     loss_grads(s, params, r.ub, r.pb, r.gb, weights ? r.wb : nullptr, batch, alpha, beta, grad, loss, w, q);
-    k_adam_run<<<ew_grid(NPARAM), 256, 0, s>>>(params, grad, adam_m, adam_v, NPARAM, r.step, r.total, lr, lr_final,
-                                               beta1, beta2, eps);
-    k_step_end<<<1, 1, 0, s>>>(r);
+    launch_pdl(k_adam_run, ew_grid(NPARAM), 256, 0, s, params, (const float*)grad, adam_m, adam_v, NPARAM,
+               (const long long*)r.step, r.total, lr, lr_final, beta1, beta2, eps);
+    launch_pdl(k_step_end, 1, 1, 0, s, r);
   };
   if (e == cudaSuccess) {
     // the first step runs uncaptured: it configures the tensor-core kernel

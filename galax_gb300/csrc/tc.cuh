@@ -55,6 +55,15 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
+// Programmatic dependent launch: a kernel launched with programmatic stream
+// serialization may start while the kernel before it in the stream finishes.
+// pdl_wait() blocks until that kernel has completed and its writes are
+// visible, so a kernel calls it before its first global-memory access; then
+// pdl_trigger() lets the next such kernel be scheduled onto free SMs. Both
+// are no-ops for a kernel launched the ordinary way.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 __device__ __forceinline__ void fence_barrier_init() {
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }

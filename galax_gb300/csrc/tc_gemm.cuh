@@ -16,8 +16,9 @@
 //
 // One CTA of 256 threads computes a 128 x 128 tile of C (so the 8192 x 256
 // products of a training batch spread over 128 CTAs); K runs in blocks of 64
-// through two shared-memory stages (64 KB each: A and B hi/lo, 128 x 64,
-// K-major, 128-byte swizzle, the layout of the inference kernel's operands).
+// through two shared-memory stages (A and B hi, and lo for split operands:
+// 32-64 KB; 128 x 64, K-major, 128-byte swizzle, the layout of the inference
+// kernel's operands).
 // All threads load and convert; thread 0 issues the products and commits them
 // to the stage's mbarrier, which frees the stage for the block after next. The
 // accumulator (128 TMEM columns) drains through shared memory so that C is
@@ -44,13 +45,23 @@ constexpr int BM = 128, BN = 128, BK = 64;
 constexpr int NTHREADS = 256;
 constexpr uint32_t A_BLK = BM * 128;  // 16 KB: 128 rows x 64 bf16
 constexpr uint32_t B_BLK = BN * 128;  // 16 KB
-constexpr uint32_t STAGE_BYTES = 2 * A_BLK + 2 * B_BLK;  // hi and lo of both
-constexpr uint32_t SMEM_BAR = 2 * STAGE_BYTES;            // 128 KB
-constexpr uint32_t SMEM_ALLOC = SMEM_BAR + 64 + 1024;     // barriers, TMEM address, alignment slack
 constexpr int OUT_STRIDE = BN + 4;  // floats per staged output row: rows 16-byte aligned, float4 access conflict-free
+constexpr uint32_t OUT_BYTES = (uint32_t)BM * OUT_STRIDE * 4;  // the staged output tile (reuses the stages)
 constexpr uint32_t WAIT_LIMIT = 1u << 24;
-static_assert(SMEM_ALLOC <= 227 * 1024, "shared memory budget");
-static_assert((uint32_t)BM * OUT_STRIDE * 4 <= SMEM_BAR, "output staging fits in the operand stages");
+// A stage holds A hi [, A lo], B hi [, B lo] (the lo parts only for split
+// operands), so products without split operands need half the shared memory
+// and several CTAs (of this or a concurrent product) fit on an SM.
+__host__ __device__ constexpr uint32_t stage_bytes(int split_a, int split_b) {
+  return A_BLK * (1 + (split_a ? 1 : 0)) + B_BLK * (1 + (split_b ? 1 : 0));
+}
+__host__ __device__ constexpr uint32_t bar_offset(uint32_t stage) {
+  return 2 * stage > OUT_BYTES ? 2 * stage : (OUT_BYTES + 1023) / 1024 * 1024;
+}
+__host__ __device__ constexpr uint32_t smem_alloc(uint32_t stage) {
+  return bar_offset(stage) + 64 + 1024;  // barriers, TMEM address, alignment slack
+}
+constexpr uint32_t SMEM_MAX = smem_alloc(stage_bytes(1, 1));
+static_assert(SMEM_MAX <= 227 * 1024, "shared memory budget");
 
 struct Args {
   int M, N, K;
@@ -63,6 +74,7 @@ struct Args {
   float beta;
   const float* bias;
   int split_a, split_b;
+  uint32_t stage;  // bytes per pipeline stage: stage_bytes() of the launch's most split source
   int kchunk;  // K per blockIdx.z, a multiple of BK
   float* part;  // gridDim.z > 1: partial tiles [z][M][N]
   int* err;
@@ -329,7 +341,7 @@ template <int EPI>
 __global__ void __launch_bounds__(NTHREADS, 1) k_tc_gemm(Args a) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = smem_raw + ((1024 - (tc::smem_u32(smem_raw) & 1023)) & 1023);
-  uint64_t* done = reinterpret_cast<uint64_t*>(smem + SMEM_BAR);  // [2] stage free again
+  uint64_t* done = reinterpret_cast<uint64_t*>(smem + bar_offset(a.stage));  // [2] stage free again
   uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(done + 2);
   __shared__ int fail_s;
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
@@ -341,6 +353,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_tc_gemm(Args a) {
   const int64_t sbn = second ? a.sbn2 : a.sbn, sbk = second ? a.sbk2 : a.sbk;
   const int split_a = second ? a.split_a2 : a.split_a, split_b = second ? a.split_b2 : a.split_b;
   const int kbeg = (second ? (int)blockIdx.z - a.z2 : (int)blockIdx.z) * a.kchunk;
+  const uint32_t b_off = A_BLK * (split_a ? 2u : 1u);  // B hi within a stage
   const int kend = min(a.K, kbeg + a.kchunk);
   const int nk = kend > kbeg ? (kend - kbeg + BK - 1) / BK : 0;
   if (t == 0) {
@@ -357,6 +370,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_tc_gemm(Args a) {
   __syncthreads();
   tc::tc_fence_after();
   const uint32_t tmem = *tmem_holder;
+  // set-up done; now the previous kernel's results are needed
+  tc::pdl_wait();
   constexpr uint32_t idesc = tc::idesc_bf16(BM, BN);
   int committed = 0;  // k blocks whose products were issued (the same count in every thread)
   prefetch_epilogue<EPI>(a, m0, n0);
@@ -368,12 +383,12 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_tc_gemm(Args a) {
   }
   for (int kb = 0; kb < nk; ++kb) {
     const int s = kb & 1;
-    uint8_t* st = smem + s * STAGE_BYTES;
+    uint8_t* st = smem + s * a.stage;
     if (kb >= 2 && !tc::mbar_wait(&done[s], (uint32_t)((kb / 2 - 1) & 1), WAIT_LIMIT)) fail_s = 1;
     __syncthreads();
     if (fail_s) break;
     put<BM>(fa, st, st + A_BLK, sak == 1, split_a);
-    put<BN>(fb, st + 2 * A_BLK, st + 2 * A_BLK + B_BLK, sbk == 1, split_b);
+    put<BN>(fb, st + b_off, st + b_off + B_BLK, sbk == 1, split_b);
     if (kb + 1 < nk) {  // the next block's loads in flight across the barrier and the product issue
       const int k1 = kbeg + (kb + 1) * BK;
       fetch<BM>(fa, A, sam, sak, m0, a.M, k1, kend);
@@ -383,7 +398,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_tc_gemm(Args a) {
     __syncthreads();
     if (t == 0) {
       tc::tc_fence_after();
-      const uint32_t ah = tc::smem_u32(st), al = ah + A_BLK, bh = ah + 2 * A_BLK, bl = bh + B_BLK;
+      const uint32_t ah = tc::smem_u32(st), al = ah + A_BLK, bh = ah + b_off, bl = bh + B_BLK;
 #pragma unroll
       for (int ks = 0; ks < 4; ++ks) {
         tc::mma_bf16(tmem, tc::desc_sw128(ah + ks * 32), tc::desc_sw128(bh + ks * 32), idesc, (kb | ks) != 0);
@@ -394,6 +409,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_tc_gemm(Args a) {
     }
     committed = kb + 1;
   }
+  // the next kernel may be scheduled once every CTA is draining its tile
+  tc::pdl_trigger();
   // the last commit arrives once every product issued by this CTA has completed
   if (committed > 0) {
     const int last = committed - 1;
@@ -440,6 +457,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_tc_gemm(Args a) {
 
 // C[m][n] = beta C[m][n] + sum_z part[z][m][n], the slices added in z order.
 __global__ void k_splitk_sum(const float* part, int splits, int M, int N, float* C, int64_t ldc, float beta) {
+  tc::pdl_wait();
+  tc::pdl_trigger();
   const int64_t mn = (int64_t)M * N;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < mn; i += (int64_t)gridDim.x * blockDim.x) {
     float s = 0.0f;

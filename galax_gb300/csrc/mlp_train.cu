@@ -426,19 +426,51 @@ struct Ws {
   float* pbsum;    // [kLossBlocks] per-block sums of Pb
   float* lpart;    // [kLossBlocks] per-block shares of the loss
   float* splitk;   // [kMaxSplits][H][H] partial tiles of the tensor-core weight gradients
+  uint8_t* wimg;   // bf16 images of W2, W3, W4 as a product's B operand, both orientations (wimg())
   int* err;  // set by a tensor-core product that gave up waiting (gal_mlp_workspace_error)
 };
 
 static int64_t col_chunks(int64_t B) { return (B + kColRows - 1) / kColRows; }
 constexpr int kMaxSplits = 32;
 constexpr int kColSlots = 8;      // column sums per training step
+// B-operand images of the three 256 x 256 layers: per matrix two orientations
+// (B(n, k) = W[n][k] for the forward products, W[k][n] for the backward ones)
+// of two 64 KB column blocks
+constexpr size_t kWimgOne = 2 * tcg::BIMG_BYTES;  // one orientation of one matrix
+constexpr size_t kWimgBytes = 3 * 2 * kWimgOne;
 constexpr int kLossBlocks = 4096;  // k_loss's largest grid (ew_grid)
+
+// The bf16 B-operand images of W2, W3, W4, rounded to nearest as put() rounds
+// a quantised operand: image (matrix m, orientation o) at wimg + (2 m + o) *
+// kWimgOne, column block nb at + nb * BIMG_BYTES, laid out by tc::sw128_offset
+// for 128 rows (n) x 256 K; o = 0: B(n, k) = W[n][k], o = 1: B(n, k) = W[k][n].
+// One thread per 16-byte chunk (8 consecutive k).
+__global__ void __launch_bounds__(256) k_wimg(const float* P, uint8_t* wimg) {
+  tc::pdl_wait();
+  tc::pdl_trigger();
+  const int i = blockIdx.x * 256 + threadIdx.x;
+  const int chunk = i & 31, row = (i >> 5) & 127, nb = (i >> 12) & 1, o = (i >> 13) & 1, m = i >> 14;
+  if (m >= 3) return;
+  const float* W = P + (m == 0 ? OFF_W2 : (m == 1 ? OFF_W3 : OFF_W4));
+  const int n = nb * 128 + row, k0 = chunk * 8;
+  uint32_t h[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int k = k0 + 2 * j;
+    const float v0 = o ? W[k * H + n] : W[n * H + k];
+    const float v1 = o ? W[(k + 1) * H + n] : W[n * H + k + 1];
+    h[j] = (uint32_t)tcg::bf16_bits(v0) | ((uint32_t)tcg::bf16_bits(v1) << 16);
+  }
+  *reinterpret_cast<uint4*>(wimg + (size_t)(2 * m + o) * kWimgOne + (size_t)nb * tcg::BIMG_BYTES +
+                            tc::sw128_offset(128, row, k0)) = make_uint4(h[0], h[1], h[2], h[3]);
+}
+constexpr int kWimgBlocks = 3 * 2 * 2 * 128 * 32 / 256;
 
 static size_t ws_bytes(int64_t B) {
   const size_t big = sizeof(float) * (size_t)B * H;
   return big * (4 + 4 + 4 + 3 + 4 + 5) + sizeof(float) * (size_t)B * (1 + 3 + 1 + 3) +
          sizeof(float) * (size_t)kColSlots * col_chunks(B) * H * 3 + sizeof(float) * 2 * kLossBlocks +
-         sizeof(float) * (size_t)kMaxSplits * H * H + 64 * 256;
+         sizeof(float) * (size_t)kMaxSplits * H * H + kWimgBytes + 64 * 256;
 }
 
 static Ws carve(void* ws, int64_t B) {
@@ -471,6 +503,7 @@ static Ws carve(void* ws, int64_t B) {
   w.pbsum = take(sizeof(float) * kLossBlocks);
   w.lpart = take(sizeof(float) * kLossBlocks);
   w.splitk = take(sizeof(float) * (size_t)kMaxSplits * H * H);
+  w.wimg = reinterpret_cast<uint8_t*>(take(kWimgBytes));
   return w;
 }
 
@@ -507,6 +540,12 @@ static void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t s
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
+// the image of layer `layer` (2..4) as B operand: orientation 0 for B(n, k) =
+// W[n][k] (forward and second-order passes), 1 for W[k][n] (input gradient)
+static const uint8_t* wimg_of(const Ws& w, int layer, int orient) {
+  return w.wimg + (size_t)(2 * (layer - 2) + orient) * kWimgOne;
 }
 
 // the tensor-core product kernels' shared-memory opt-in, once per device
@@ -569,7 +608,8 @@ static bool tc_wgrad2(cudaStream_t s, int K, const float* A1, const float* B1, i
   const dim3 grid(H / tcg::BN, H / tcg::BM, 2 * z);
   const uint32_t st1 = tcg::stage_bytes(split_a1, split_b1), st2 = tcg::stage_bytes(split_a2, split_b2);
   a.stage = st1 > st2 ? st1 : st2;
-  launch_pdl(tcg::k_tc_gemm<tcg::EPI_NONE>, grid, tcg::NTHREADS, tcg::smem_alloc(a.stage), s, a);
+  a.bar_off = tcg::bar_offset(a.stage);
+  launch_pdl(tcg::k_tc_gemm<tcg::EPI_NONE>, grid, tcg::NTHREADS, tcg::smem_alloc_at(a.bar_off), s, a);
   launch_pdl(tcg::k_splitk_sum, dim3((H * H + 255) / 256), 256, 0, s, (const float*)part, 2 * z, (int)H, (int)H, C,
              (int64_t)H, 0.0f);
   return true;
@@ -577,7 +617,7 @@ static bool tc_wgrad2(cudaStream_t s, int K, const float* A1, const float* B1, i
 
 static bool tc_gemm(cudaStream_t s, bool TA, bool TB, int M, int N, int K, const float* A, int lda, const float* B,
                     int ldb, float* C, int ldc, float beta, const float* bias, int split_a, int split_b, int* err,
-                    float* part, const Epi& epi) {
+                    float* part, const Epi& epi, const uint8_t* bimg) {
   if (!tc_configure()) return false;
   tcg::Args a{};
   a.M = M;
@@ -623,8 +663,16 @@ static bool tc_gemm(cudaStream_t s, bool TA, bool TB, int M, int N, int K, const
       a.part = part;
     }
   }
-  a.stage = tcg::stage_bytes(split_a, split_b);
-  const uint32_t smem = tcg::smem_alloc(a.stage);
+  if (bimg && !split_b && N == H && K == H && grid.z == 1) {
+    // B from its bf16 image: the stages hold A only
+    a.bimg = bimg;
+    a.stage = tcg::stage_bytes(split_a, 0) - tcg::B_BLK;
+    a.bar_off = tcg::bar_offset_img(a.stage);
+  } else {
+    a.stage = tcg::stage_bytes(split_a, split_b);
+    a.bar_off = tcg::bar_offset(a.stage);
+  }
+  const uint32_t smem = tcg::smem_alloc_at(a.bar_off);
   switch (epi.mode) {
     case tcg::EPI_SILU: launch_pdl(tcg::k_tc_gemm<tcg::EPI_SILU>, grid, tcg::NTHREADS, smem, s, a); break;
     case tcg::EPI_DMUL: launch_pdl(tcg::k_tc_gemm<tcg::EPI_DMUL>, grid, tcg::NTHREADS, smem, s, a); break;
@@ -645,14 +693,16 @@ static bool tc_gemm(cudaStream_t s, bool TA, bool TB, int M, int N, int K, const
 // Products run on the tensor cores when they have 256 output columns and
 // K >= 64, else on the FP32 kernel. qa / qb: the operand is rounded to bf16
 // (one bf16 part on the tensor cores); otherwise it enters unrounded (two parts).
+// bimg: B's bf16 image (wimg()), used when B is rounded (qb).
 static void epi_fallback(cudaStream_t s, const Epi& e, const float* C, int64_t n);
 
 template <bool TA, bool TB>
 static void gemm(cudaStream_t s, const Ws& w, int M, int N, int K, const float* A, int lda, const float* B, int ldb,
                  float* C, int ldc, float beta = 0.0f, const float* bias = nullptr, int qa = 0, int qb = 0,
-                 const Epi& epi = Epi()) {
+                 const Epi& epi = Epi(), const uint8_t* bimg = nullptr) {
   if (N == H && K >= tcg::BK &&
-      tc_gemm(s, TA, TB, M, N, K, A, lda, B, ldb, C, ldc, beta, bias, qa ? 0 : 1, qb ? 0 : 1, w.err, w.splitk, epi))
+      tc_gemm(s, TA, TB, M, N, K, A, lda, B, ldb, C, ldc, beta, bias, qa ? 0 : 1, qb ? 0 : 1, w.err, w.splitk, epi,
+              qb ? bimg : nullptr))
     return;
   if (epi.mode != tcg::EPI_NONE) {  // FP32 product, then the elementwise step on its own
     gemm<TA, TB>(s, w, M, N, K, A, lda, B, ldb, C, ldc, beta, bias, qa, qb);
@@ -783,23 +833,25 @@ static Epi epi_zb4(const float* z, const float* w5, const float* pb, float* zb) 
 static void forward_backward(cudaStream_t s, const float* P, const float* x, int64_t B, const Ws& w, int q) {
   const int Bi = (int)B;
   const unsigned l1_blocks = (unsigned)((B + kL1Rows - 1) / kL1Rows);
+  // quantised: the layers' weights enter every product rounded to bf16, from their images
+  if (q) launch_pdl(k_wimg, dim3(kWimgBlocks), 256, 0, s, P, w.wimg);
   launch_pdl(k_layer1<0>, l1_blocks, H, 0, s, x, P + OFF_W1, P + OFF_B1, (const float*)nullptr, (const float*)nullptr,
              w.Z[1], w.Hh[1], B, q);
   gemm<false, true>(s, w, Bi, H, H, w.Hh[1], H, P + OFF_W2, H, w.Z[2], H, 0.0f, P + OFF_B2, q, q,
-                    epi_silu(w.Hh[2], q));
+                    epi_silu(w.Hh[2], q), wimg_of(w, 2, 0));
   gemm<false, true>(s, w, Bi, H, H, w.Hh[2], H, P + OFF_W3, H, w.Z[3], H, 0.0f, P + OFF_B3, q, q,
-                    epi_silu(w.Hh[3], q));
+                    epi_silu(w.Hh[3], q), wimg_of(w, 3, 0));
   gemm<false, true>(s, w, Bi, H, H, w.Hh[3], H, P + OFF_W4, H, w.Z[4], H, 0.0f, P + OFF_B4, q, q,
-                    epi_silu_d4(w.Hh[4], 0, P + OFF_W5, w.D[4], q));  // and D4 = silu'(Z4) w5
+                    epi_silu_d4(w.Hh[4], 0, P + OFF_W5, w.D[4], q), wimg_of(w, 4, 0));  // and D4 = silu'(Z4) w5
   launch_pdl(k_rowdot, dim3((unsigned)((B + 7) / 8)), 256, 0, s, (const float*)w.Hh[4], P + OFF_W5, P + OFF_B5, B, 1,
              w.out);
   // input gradient
   gemm<false, false>(s, w, Bi, H, H, w.D[4], H, P + OFF_W4, H, w.U[3], H, 0.0f, nullptr, q, q,
-                     epi_dmul(w.Z[3], w.D[3], q, q));
+                     epi_dmul(w.Z[3], w.D[3], q, q), wimg_of(w, 4, 1));
   gemm<false, false>(s, w, Bi, H, H, w.D[3], H, P + OFF_W3, H, w.U[2], H, 0.0f, nullptr, q, q,
-                     epi_dmul(w.Z[2], w.D[2], q, q));
+                     epi_dmul(w.Z[2], w.D[2], q, q), wimg_of(w, 3, 1));
   gemm<false, false>(s, w, Bi, H, H, w.D[2], H, P + OFF_W2, H, w.U[1], H, 0.0f, nullptr, q, q,
-                     epi_dmul(w.Z[1], w.D[1], 0, 0));
+                     epi_dmul(w.Z[1], w.D[1], 0, 0), wimg_of(w, 2, 1));
   launch_pdl(k_rowdot, dim3((unsigned)((B + 7) / 8)), 256, 0, s, (const float*)w.D[1], P + OFF_W1,
              (const float*)nullptr, B, 3, w.G);
 }
@@ -886,28 +938,28 @@ static void loss_grads(cudaStream_t s, const float* P, const float* x, const flo
   // Ub1, Ub2, Ub3 in buffers of their own: each stays until the weight gradient
   // that pairs it with a forward-graph term (gWk = Dk^T Ub(k-1) + Zbk^T H(k-1))
   gemm<false, true>(s, w, Bi, H, H, w.Ub, H, P + OFF_W2, H, w.Db, H, 0.0f, nullptr, 0, q,
-                    epi_dd(w.Z[2], w.U[2], w.Ub2, w.Zb[2], q));                               // Db2 = Ub1 W2^T
+                    epi_dd(w.Z[2], w.U[2], w.Ub2, w.Zb[2], q), wimg_of(w, 2, 0));             // Db2 = Ub1 W2^T
   gemm<false, true>(s, w, Bi, H, H, w.Ub2, H, P + OFF_W3, H, w.Db, H, 0.0f, nullptr, 0, q,
-                    epi_dd(w.Z[3], w.U[3], w.Ub3, w.Zb[3], q));                               // Db3 = Ub2 W3^T
+                    epi_dd(w.Z[3], w.U[3], w.Ub3, w.Zb[3], q), wimg_of(w, 3, 0));             // Db3 = Ub2 W3^T
   gemm<false, true>(s, w, Bi, H, H, w.Ub3, H, P + OFF_W4, H, w.Db, H, 0.0f, nullptr, 0, q,
-                    epi_zb4(w.Z[4], P + OFF_W5, w.Pb, w.Zb[4]));                              // Db4 = Ub3 W4^T, Zb4
+                    epi_zb4(w.Z[4], P + OFF_W5, w.Pb, w.Zb[4]), wimg_of(w, 4, 0));            // Db4 = Ub3 W4^T, Zb4
   sd.fork(1);
   colpart(t, w, w.Z[4], w.Db, nullptr, nullptr, B, 2, 1);                                 // gw5 = sum silu'(Z4) Db4
   // ---- potential term and the forward graph, layer 4 down to 1
   wgrad2(t, w, Bi, w.D[4], w.Ub3, q, 0, w.Zb[4], w.Hh[3], 0, q, grad + OFF_W4);           // gW4 = D4^T Ub3 + Zb4^T H3
   colpart(t, w, w.Zb[4], nullptr, nullptr, nullptr, B, 0, 3);
   gemm<false, false>(s, w, Bi, H, H, w.Zb[4], H, P + OFF_W4, H, w.Hb, H, 0.0f, nullptr, 0, q,
-                     epi_zbacc(w.Z[3], w.Zb[3]));                                              // Hb3 = Zb4 W4
+                     epi_zbacc(w.Z[3], w.Zb[3]), wimg_of(w, 4, 1));                            // Hb3 = Zb4 W4
   sd.fork(2);
   wgrad2(t, w, Bi, w.D[3], w.Ub2, q, 0, w.Zb[3], w.Hh[2], 0, q, grad + OFF_W3);           // gW3 = D3^T Ub2 + Zb3^T H2
   colpart(t, w, w.Zb[3], nullptr, nullptr, nullptr, B, 0, 4);
   gemm<false, false>(s, w, Bi, H, H, w.Zb[3], H, P + OFF_W3, H, w.Hb, H, 0.0f, nullptr, 0, q,
-                     epi_zbacc(w.Z[2], w.Zb[2]));
+                     epi_zbacc(w.Z[2], w.Zb[2]), wimg_of(w, 3, 1));
   sd.fork(3);
   wgrad2(t, w, Bi, w.D[2], w.Ub, q, 0, w.Zb[2], w.Hh[1], 0, q, grad + OFF_W2);            // gW2 = D2^T Ub1 + Zb2^T H1
   colpart(t, w, w.Zb[2], nullptr, nullptr, nullptr, B, 0, 5);
   gemm<false, false>(s, w, Bi, H, H, w.Zb[2], H, P + OFF_W2, H, w.Hb, H, 0.0f, nullptr, 0, q,
-                     epi_zbacc(w.Z[1], w.Zb[1]));
+                     epi_zbacc(w.Z[1], w.Zb[1]), wimg_of(w, 2, 1));
   colpart(s, w, w.Zb[1], nullptr, nullptr, x, B, 3, 6);                                     // gW1 += Zb1^T X
   colpart(s, w, w.Zb[1], nullptr, nullptr, nullptr, B, 0, 7);
   ColJobs J{};

@@ -57,9 +57,15 @@ __host__ __device__ constexpr uint32_t stage_bytes(int split_a, int split_b) {
 __host__ __device__ constexpr uint32_t bar_offset(uint32_t stage) {
   return 2 * stage > OUT_BYTES ? 2 * stage : (OUT_BYTES + 1023) / 1024 * 1024;
 }
-__host__ __device__ constexpr uint32_t smem_alloc(uint32_t stage) {
-  return bar_offset(stage) + 64 + 1024;  // barriers, TMEM address, alignment slack
+constexpr uint32_t BIMG_BYTES = 4 * B_BLK;  // the B image of one column block (K = 256)
+// image mode: the two A stages, then B whole
+__host__ __device__ constexpr uint32_t bar_offset_img(uint32_t stage) {
+  return 2 * stage + BIMG_BYTES > OUT_BYTES ? 2 * stage + BIMG_BYTES : (OUT_BYTES + 1023) / 1024 * 1024;
 }
+__host__ __device__ constexpr uint32_t smem_alloc_at(uint32_t bar_off) {
+  return bar_off + 64 + 1024;  // barriers, TMEM address, alignment slack
+}
+__host__ __device__ constexpr uint32_t smem_alloc(uint32_t stage) { return smem_alloc_at(bar_offset(stage)); }
 constexpr uint32_t SMEM_MAX = smem_alloc(stage_bytes(1, 1));
 static_assert(SMEM_MAX <= 227 * 1024, "shared memory budget");
 
@@ -74,7 +80,13 @@ struct Args {
   float beta;
   const float* bias;
   int split_a, split_b;
-  uint32_t stage;  // bytes per pipeline stage: stage_bytes() of the launch's most split source
+  uint32_t stage;    // bytes per pipeline stage: stage_bytes() of the launch's most split source
+  uint32_t bar_off;  // shared-memory offset of the barriers (bar_offset())
+  // Optional: B as a pre-swizzled bf16 image (K = 256, B not split, one K
+  // range): for CTA column block nb the 64 KB at bimg + nb * 64 KB, the four
+  // 16 KB K blocks exactly as put() would lay them out; bulk-copied into
+  // shared memory at the start instead of staged through registers.
+  const uint8_t* bimg;
   int kchunk;  // K per blockIdx.z, a multiple of BK
   float* part;  // gridDim.z > 1: partial tiles [z][M][N]
   int* err;
@@ -341,8 +353,11 @@ template <int EPI>
 __global__ void __launch_bounds__(NTHREADS, 1) k_tc_gemm(Args a) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = smem_raw + ((1024 - (tc::smem_u32(smem_raw) & 1023)) & 1023);
-  uint64_t* done = reinterpret_cast<uint64_t*>(smem + bar_offset(a.stage));  // [2] stage free again
-  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(done + 2);
+  // done[0..1]: stage free again; done[2]: the B image has landed
+  uint64_t* done = reinterpret_cast<uint64_t*>(smem + a.bar_off);
+  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(done + 3);
+  const bool bim = a.bimg != nullptr;
+  uint8_t* const bsm = smem + 2 * a.stage;  // image mode: B, four 16 KB K blocks
   __shared__ int fail_s;
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
   const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
@@ -360,6 +375,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_tc_gemm(Args a) {
     fail_s = 0;
     tc::mbar_init(&done[0], 1);
     tc::mbar_init(&done[1], 1);
+    tc::mbar_init(&done[2], 1);
     tc::fence_barrier_init();
   }
   if (warp == 0) {
@@ -372,6 +388,11 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_tc_gemm(Args a) {
   const uint32_t tmem = *tmem_holder;
   // set-up done; now the previous kernel's results are needed
   tc::pdl_wait();
+  if (bim && t == 0 && nk > 0) {
+    tc::mbar_expect_tx(&done[2], (uint32_t)nk * B_BLK);
+    for (int kb = 0; kb < nk; ++kb)
+      tc::bulk_g2s(bsm + kb * B_BLK, a.bimg + (size_t)blockIdx.x * BIMG_BYTES + (size_t)kb * B_BLK, B_BLK, &done[2]);
+  }
   constexpr uint32_t idesc = tc::idesc_bf16(BM, BN);
   int committed = 0;  // k blocks whose products were issued (the same count in every thread)
   prefetch_epilogue<EPI>(a, m0, n0);
@@ -379,7 +400,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_tc_gemm(Args a) {
   Frag<BN> fb;
   if (nk > 0) {
     fetch<BM>(fa, A, sam, sak, m0, a.M, kbeg, kend);
-    fetch<BN>(fb, Bm, sbn, sbk, n0, a.N, kbeg, kend);
+    if (!bim) fetch<BN>(fb, Bm, sbn, sbk, n0, a.N, kbeg, kend);
   }
   for (int kb = 0; kb < nk; ++kb) {
     const int s = kb & 1;
@@ -388,22 +409,29 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_tc_gemm(Args a) {
     __syncthreads();
     if (fail_s) break;
     put<BM>(fa, st, st + A_BLK, sak == 1, split_a);
-    put<BN>(fb, st + b_off, st + b_off + B_BLK, sbk == 1, split_b);
+    if (!bim) put<BN>(fb, st + b_off, st + b_off + B_BLK, sbk == 1, split_b);
     if (kb + 1 < nk) {  // the next block's loads in flight across the barrier and the product issue
       const int k1 = kbeg + (kb + 1) * BK;
       fetch<BM>(fa, A, sam, sak, m0, a.M, k1, kend);
-      fetch<BN>(fb, Bm, sbn, sbk, n0, a.N, k1, kend);
+      if (!bim) fetch<BN>(fb, Bm, sbn, sbk, n0, a.N, k1, kend);
     }
     tc::fence_proxy_async_smem();
     __syncthreads();
     if (t == 0) {
-      tc::tc_fence_after();
-      const uint32_t ah = tc::smem_u32(st), al = ah + A_BLK, bh = ah + b_off, bl = bh + B_BLK;
+      // image mode: B must have landed before the first product
+      const bool b_ok = !bim || kb > 0 || tc::mbar_wait(&done[2], 0, WAIT_LIMIT);
+      if (!b_ok) {
+        fail_s = 1;  // seen by every thread after the next barrier; the commit below still arrives
+      } else {
+        tc::tc_fence_after();
+        const uint32_t ah = tc::smem_u32(st), al = ah + A_BLK;
+        const uint32_t bh = bim ? tc::smem_u32(bsm) + (uint32_t)kb * B_BLK : ah + b_off, bl = bh + B_BLK;
 #pragma unroll
-      for (int ks = 0; ks < 4; ++ks) {
-        tc::mma_bf16(tmem, tc::desc_sw128(ah + ks * 32), tc::desc_sw128(bh + ks * 32), idesc, (kb | ks) != 0);
-        if (split_b) tc::mma_bf16(tmem, tc::desc_sw128(ah + ks * 32), tc::desc_sw128(bl + ks * 32), idesc, 1);
-        if (split_a) tc::mma_bf16(tmem, tc::desc_sw128(al + ks * 32), tc::desc_sw128(bh + ks * 32), idesc, 1);
+        for (int ks = 0; ks < 4; ++ks) {
+          tc::mma_bf16(tmem, tc::desc_sw128(ah + ks * 32), tc::desc_sw128(bh + ks * 32), idesc, (kb | ks) != 0);
+          if (split_b) tc::mma_bf16(tmem, tc::desc_sw128(ah + ks * 32), tc::desc_sw128(bl + ks * 32), idesc, 1);
+          if (split_a) tc::mma_bf16(tmem, tc::desc_sw128(al + ks * 32), tc::desc_sw128(bh + ks * 32), idesc, 1);
+        }
       }
       tc::mma_commit(&done[s]);
     }

@@ -49,7 +49,7 @@ constexpr uint32_t A_BYTES = TILE * 256 * 2;            // 64 KB: one operand ti
 constexpr uint32_t SMEM_A = 0;                          // two operand tiles, ping-pong
 constexpr uint32_t SMEM_RING = 2 * A_BYTES;
 constexpr uint32_t SMEM_SMALL = SMEM_RING + STAGES * HALF_BYTES;
-constexpr int SMALL_FLOATS = H * 4 + 4 * H + 1;         // (W1 row, b1) per unit, b2, b3, b4, w5, b5
+constexpr int SMALL_FLOATS = H * 4 + 4 * H + 1;         // (W1 row, b1) per unit, b2, b3, b4 (halved), w5, b5
 constexpr uint32_t SMEM_PART = SMEM_SMALL + ((SMALL_FLOATS * 4 + 255) / 256) * 256;
 constexpr uint32_t SMEM_READY = SMEM_PART + TILE * 4 * 4;
 constexpr uint32_t SMEM_BAR = SMEM_READY + TILE * 4;
@@ -70,7 +70,7 @@ struct InferArgs {
   double* grad;          // [3][n] or NULL
   int32_t accumulate;    // grad += (1) or = (0)
   double* phi;           // [n] or NULL
-  const float* small;    // {W1[c][0..2], b1[c]} for each unit c, then b2, b3, b4, w5, b5 (SMALL_FLOATS)
+  const float* small;    // {W1[c][0..2], b1[c]} / 2 for each unit c, then b2 / 2, b3 / 2, b4 / 2, w5, b5
   const uint8_t* wimg;   // 24 pre-swizzled 32 KB K-blocks
   int* err;
 };
@@ -89,8 +89,19 @@ __device__ __forceinline__ void set_abort(volatile int* abort_flag, int* err, in
   if (err) atomicExch(err, code);
 }
 
-// sigmoid from one SFU operation: 1 / (1 + e^-z) = (1 + tanh(z / 2)) / 2
-__device__ __forceinline__ float sig(float z) { return fmaf(0.5f, tc::tanh_approx(0.5f * z), 0.5f); }
+// SiLU from one SFU operation. With hz = z / 2 and t = tanh(hz): the sigmoid
+// is s = (1 + t) / 2, silu(z) = z s = hz + hz t, and silu'(z) = s + silu (1 - s)
+// with 1 - s = (1 - t) / 2. The biases and the first layer's weights are kept
+// halved in shared memory (exact), so hz comes straight out of the sums.
+struct Silu {
+  float h, d;  // silu(z), silu'(z)
+};
+__device__ __forceinline__ float silu_h(float hz, float t) { return fmaf(hz, t, hz); }
+__device__ __forceinline__ Silu silu_hd(float hz) {
+  const float t = tc::tanh_approx(hz);
+  const float h = silu_h(hz, t);
+  return {h, fmaf(h, fmaf(-0.5f, t, 0.5f), fmaf(0.5f, t, 0.5f))};
+}
 
 // write 32 consecutive hidden units [c, c+32) of row `row` into an operand tile
 __device__ __forceinline__ void store_row32(uint8_t* tile, int row, int c, const float (&v)[32]) {
@@ -260,9 +271,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
 #pragma unroll
           for (int k = 0; k < 32; ++k) {
             const int cc = c + k;
-            const float4 l1 = sL1[cc];
-            const float z = fmaf(l1.x, u[0], fmaf(l1.y, u[1], fmaf(l1.z, u[2], l1.w)));
-            v[k] = z * sig(z);
+            const float4 l1 = sL1[cc];  // halved
+            const float hz = fmaf(l1.x, u[0], fmaf(l1.y, u[1], fmaf(l1.z, u[2], l1.w)));
+            v[k] = silu_h(hz, tc::tanh_approx(hz));
           }
           store_row32(tiles, row, c, v);
         }
@@ -300,28 +311,37 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
             const int cc0 = c + 32 * half;
             float v[32];
             if (g <= 1) {  // z2 / z3: h = silu(z) -> operand tile, silu'(z) -> TMEM
-              const float* bb = g == 0 ? sb2 : sb3;
+              const float4* hb = reinterpret_cast<const float4*>((g == 0 ? sb2 : sb3) + cc0);  // halved biases
               uint32_t spk[16];
 #pragma unroll
-              for (int k = 0; k < 32; k += 2) {
-                const float z0 = __uint_as_float(acc[k]) + bb[cc0 + k];
-                const float z1 = __uint_as_float(acc[k + 1]) + bb[cc0 + k + 1];
-                const float s0 = sig(z0), s1 = sig(z1);
-                v[k] = z0 * s0;
-                v[k + 1] = z1 * s1;
-                // silu'(z) = s (1 + z (1 - s)) = s + silu(z) (1 - s)
-                spk[k / 2] = tc::pack_bf16x2(fmaf(v[k], 1.f - s0, s0), fmaf(v[k + 1], 1.f - s1, s1));
+              for (int k = 0; k < 32; k += 4) {
+                const float4 b4 = hb[k / 4];
+                const Silu r0 = silu_hd(fmaf(0.5f, __uint_as_float(acc[k]), b4.x));
+                const Silu r1 = silu_hd(fmaf(0.5f, __uint_as_float(acc[k + 1]), b4.y));
+                const Silu r2 = silu_hd(fmaf(0.5f, __uint_as_float(acc[k + 2]), b4.z));
+                const Silu r3 = silu_hd(fmaf(0.5f, __uint_as_float(acc[k + 3]), b4.w));
+                v[k] = r0.h;
+                v[k + 1] = r1.h;
+                v[k + 2] = r2.h;
+                v[k + 3] = r3.h;
+                spk[k / 2] = tc::pack_bf16x2(r0.d, r1.d);
+                spk[k / 2 + 1] = tc::pack_bf16x2(r2.d, r3.d);
               }
               tc::tmem_st16(tmem + lane_base + (uint32_t)((g == 0 ? COL_S2 : COL_S3) + cc0 / 2), spk);
               store_row32(tile_out, row, cc0, v);
             } else if (g == 2) {  // z4: d4 = silu'(z4) w5 -> operand tile; out = w5 . silu(z4)
+              const float4* hb = reinterpret_cast<const float4*>(sb4 + cc0);  // halved
+              const float4* w5 = reinterpret_cast<const float4*>(sw5 + cc0);
 #pragma unroll
-              for (int k = 0; k < 32; ++k) {
-                const float z = __uint_as_float(acc[k]) + sb4[cc0 + k];
-                const float sg = sig(z);
-                const float hz = z * sg;
-                ppart = fmaf(hz, sw5[cc0 + k], ppart);
-                v[k] = fmaf(hz, 1.f - sg, sg) * sw5[cc0 + k];
+              for (int k = 0; k < 32; k += 4) {
+                const float4 b4 = hb[k / 4], w4 = w5[k / 4];
+                const float bq[4] = {b4.x, b4.y, b4.z, b4.w}, wq[4] = {w4.x, w4.y, w4.z, w4.w};
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                  const Silu r = silu_hd(fmaf(0.5f, __uint_as_float(acc[k + j]), bq[j]));
+                  ppart = fmaf(r.h, wq[j], ppart);
+                  v[k + j] = r.d * wq[j];
+                }
               }
               store_row32(tile_out, row, cc0, v);
             } else if (g <= 4) {  // u3 / u2: d = silu'(z) u -> operand tile
@@ -335,10 +355,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
 #pragma unroll
               for (int k = 0; k < 32; ++k) {
                 const int cc = cc0 + k;
-                const float4 l1 = sL1[cc];
-                const float z = fmaf(l1.x, u[0], fmaf(l1.y, u[1], fmaf(l1.z, u[2], l1.w)));
-                const float sg = sig(z);
-                const float d1 = sg * fmaf(z, 1.f - sg, 1.f) * __uint_as_float(acc[k]);
+                const float4 l1 = sL1[cc];  // halved: gpart is half the sum, doubled at the end
+                const float hz = fmaf(l1.x, u[0], fmaf(l1.y, u[1], fmaf(l1.z, u[2], l1.w)));
+                const float d1 = silu_hd(hz).d * __uint_as_float(acc[k]);
                 gpart[0] = fmaf(d1, l1.x, gpart[0]);
                 gpart[1] = fmaf(d1, l1.y, gpart[1]);
                 gpart[2] = fmaf(d1, l1.z, gpart[2]);
@@ -374,7 +393,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
         if (valid) {
 #pragma unroll
           for (int j = 0; j < 3; ++j) {
-            const double gj = a.gscale * (double)(gpart[j] + part[row * 4 + j]);
+            const double gj = 2.0 * a.gscale * (double)(gpart[j] + part[row * 4 + j]);  // halved W1
             if (a.grad) a.grad[j * a.n + gi] = a.accumulate ? a.grad[j * a.n + gi] + gj : gj;
           }
           if (a.phi) a.phi[gi] = a.pscale * (double)(ppart + part[row * 4 + 3] + sw5[H]);
@@ -397,7 +416,7 @@ using namespace gal;
 using namespace gal::mlp;
 
 struct gal_mlp {
-  float* d_small;      // {W1 row, b1} per unit, b2, b3, b4, w5, b5
+  float* d_small;      // {W1 row, b1} per unit, b2, b3, b4 (halved), w5, b5
   uint8_t* d_wimg;     // 24 x 32 KB pre-swizzled bf16 K-blocks
   int* d_err;
   double length_scale, phi_scale;
@@ -421,13 +440,17 @@ gal_status gal_mlp_create(const float* params_host, double length_scale, double 
     *out = nullptr;
     const float* P = params_host;
     std::vector<float> small(SMALL_FLOATS);
+    // the first layer's weights and biases and the hidden biases halved (exact):
+    // the kernel's sums then give z / 2, the argument of its tanh
     for (int c = 0; c < H; ++c) {
-      for (int j = 0; j < 3; ++j) small[4 * c + j] = P[OFF_W1 + 3 * c + j];
-      small[4 * c + 3] = P[OFF_B1 + c];
+      for (int j = 0; j < 3; ++j) small[4 * c + j] = 0.5f * P[OFF_W1 + 3 * c + j];
+      small[4 * c + 3] = 0.5f * P[OFF_B1 + c];
     }
-    std::memcpy(small.data() + 4 * H, P + OFF_B2, sizeof(float) * H);
-    std::memcpy(small.data() + 5 * H, P + OFF_B3, sizeof(float) * H);
-    std::memcpy(small.data() + 6 * H, P + OFF_B4, sizeof(float) * H);
+    for (int c = 0; c < H; ++c) {
+      small[4 * H + c] = 0.5f * P[OFF_B2 + c];
+      small[5 * H + c] = 0.5f * P[OFF_B3 + c];
+      small[6 * H + c] = 0.5f * P[OFF_B4 + c];
+    }
     std::memcpy(small.data() + 7 * H, P + OFF_W5, sizeof(float) * H);
     small[8 * H] = P[OFF_B5];
     // B operands, K-major: product "A x B^T" with B[n][k]. Forward z = h W^T uses

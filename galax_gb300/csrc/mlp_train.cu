@@ -426,7 +426,8 @@ struct Ws {
   float* pbsum;    // [kLossBlocks] per-block sums of Pb
   float* lpart;    // [kLossBlocks] per-block shares of the loss
   float* splitk;   // [kMaxSplits][H][H] partial tiles of the tensor-core weight gradients
-  uint8_t* wimg;   // bf16 images of W2, W3, W4 as a product's B operand, both orientations (wimg())
+  uint8_t* wimg;   // bf16 images of W2, W3, W4 as a product's B operand, both orientations (wimg_of())
+  uint8_t* aimg[2];  // bf16 A-operand images passed between the quantised forward / input-gradient products
   int* err;  // set by a tensor-core product that gave up waiting (gal_mlp_workspace_error)
 };
 
@@ -465,12 +466,14 @@ __global__ void __launch_bounds__(256) k_wimg(const float* P, uint8_t* wimg) {
                             tc::sw128_offset(128, row, k0)) = make_uint4(h[0], h[1], h[2], h[3]);
 }
 constexpr int kWimgBlocks = 3 * 2 * 2 * 128 * 32 / 256;
+// an A-operand image of a [B][256] activation: 64 KB per 128-row block
+static size_t aimg_bytes(int64_t B) { return (size_t)((B + 127) / 128) * tcg::BIMG_BYTES; }
 
 static size_t ws_bytes(int64_t B) {
   const size_t big = sizeof(float) * (size_t)B * H;
   return big * (4 + 4 + 4 + 3 + 4 + 5) + sizeof(float) * (size_t)B * (1 + 3 + 1 + 3) +
          sizeof(float) * (size_t)kColSlots * col_chunks(B) * H * 3 + sizeof(float) * 2 * kLossBlocks +
-         sizeof(float) * (size_t)kMaxSplits * H * H + kWimgBytes + 64 * 256;
+         sizeof(float) * (size_t)kMaxSplits * H * H + kWimgBytes + 2 * aimg_bytes(B) + 64 * 256;
 }
 
 static Ws carve(void* ws, int64_t B) {
@@ -504,6 +507,7 @@ static Ws carve(void* ws, int64_t B) {
   w.lpart = take(sizeof(float) * kLossBlocks);
   w.splitk = take(sizeof(float) * (size_t)kMaxSplits * H * H);
   w.wimg = reinterpret_cast<uint8_t*>(take(kWimgBytes));
+  for (auto& im : w.aimg) im = reinterpret_cast<uint8_t*>(take(aimg_bytes(B)));
   return w;
 }
 
@@ -521,6 +525,8 @@ struct Epi {
   const float* cvec = nullptr;
   const float* rvec = nullptr;
   int q1 = 0, q2 = 0;
+  uint8_t* img = nullptr;  // also write a bf16 A-operand image of o1 (img_src 1) or o2 (2)
+  int img_src = 0;
 };
 
 // Launch with programmatic stream serialization (the kernel calls
@@ -617,7 +623,7 @@ static bool tc_wgrad2(cudaStream_t s, int K, const float* A1, const float* B1, i
 
 static bool tc_gemm(cudaStream_t s, bool TA, bool TB, int M, int N, int K, const float* A, int lda, const float* B,
                     int ldb, float* C, int ldc, float beta, const float* bias, int split_a, int split_b, int* err,
-                    float* part, const Epi& epi, const uint8_t* bimg) {
+                    float* part, const Epi& epi, const uint8_t* bimg, const uint8_t* aimg) {
   if (!tc_configure()) return false;
   tcg::Args a{};
   a.M = M;
@@ -645,6 +651,8 @@ static bool tc_gemm(cudaStream_t s, bool TA, bool TB, int M, int N, int K, const
   a.rvec = epi.rvec;
   a.q1 = epi.q1;
   a.q2 = epi.q2;
+  a.img_out = epi.img;
+  a.img_src = epi.img_src;
   dim3 grid((N + tcg::BN - 1) / tcg::BN, (M + tcg::BM - 1) / tcg::BM, 1);
   a.kchunk = ((K + tcg::BK - 1) / tcg::BK) * tcg::BK;
   // few output tiles and a long K (the weight gradients, K = batch): split K
@@ -664,9 +672,11 @@ static bool tc_gemm(cudaStream_t s, bool TA, bool TB, int M, int N, int K, const
     }
   }
   if (bimg && !split_b && N == H && K == H && grid.z == 1) {
-    // B from its bf16 image: the stages hold A only
+    // B from its bf16 image: the stages hold A only; with A's image too, A's
+    // four K blocks take the place of the two stages
     a.bimg = bimg;
-    a.stage = tcg::stage_bytes(split_a, 0) - tcg::B_BLK;
+    a.aimg = aimg && !split_a ? aimg : nullptr;
+    a.stage = a.aimg ? 2 * tcg::A_BLK : tcg::stage_bytes(split_a, 0) - tcg::B_BLK;
     a.bar_off = tcg::bar_offset_img(a.stage);
   } else {
     a.stage = tcg::stage_bytes(split_a, split_b);
@@ -693,17 +703,24 @@ static bool tc_gemm(cudaStream_t s, bool TA, bool TB, int M, int N, int K, const
 // Products run on the tensor cores when they have 256 output columns and
 // K >= 64, else on the FP32 kernel. qa / qb: the operand is rounded to bf16
 // (one bf16 part on the tensor cores); otherwise it enters unrounded (two parts).
-// bimg: B's bf16 image (wimg()), used when B is rounded (qb).
+// bimg: B's bf16 image (wimg_of()), used when B is rounded (qb); aimg: A's, the
+// image a previous product wrote (Epi::img), used with bimg when A is rounded (qa).
 static void epi_fallback(cudaStream_t s, const Epi& e, const float* C, int64_t n);
 
 template <bool TA, bool TB>
 static void gemm(cudaStream_t s, const Ws& w, int M, int N, int K, const float* A, int lda, const float* B, int ldb,
                  float* C, int ldc, float beta = 0.0f, const float* bias = nullptr, int qa = 0, int qb = 0,
-                 const Epi& epi = Epi(), const uint8_t* bimg = nullptr) {
+                 const Epi& epi = Epi(), const uint8_t* bimg = nullptr, const uint8_t* aimg = nullptr) {
   if (N == H && K >= tcg::BK &&
       tc_gemm(s, TA, TB, M, N, K, A, lda, B, ldb, C, ldc, beta, bias, qa ? 0 : 1, qb ? 0 : 1, w.err, w.splitk, epi,
-              qb ? bimg : nullptr))
+              qb ? bimg : nullptr, qa ? aimg : nullptr))
     return;
+  if (epi.img) {  // the consumer's A image is not written on this path: it falls back to the array
+    Epi e = epi;
+    e.img = nullptr;
+    gemm<TA, TB>(s, w, M, N, K, A, lda, B, ldb, C, ldc, beta, bias, qa, qb, e);
+    return;
+  }
   if (epi.mode != tcg::EPI_NONE) {  // FP32 product, then the elementwise step on its own
     gemm<TA, TB>(s, w, M, N, K, A, lda, B, ldb, C, ldc, beta, bias, qa, qb);
     epi_fallback(s, epi, C, (int64_t)M * N);
@@ -829,6 +846,12 @@ static Epi epi_zb4(const float* z, const float* w5, const float* pb, float* zb) 
   return e;
 }
 
+static Epi with_img(Epi e, uint8_t* img, int src) {
+  e.img = img;
+  e.img_src = src;
+  return e;
+}
+
 // forward and input-gradient pass; leaves Z, H, D, U, out, G in the workspace
 static void forward_backward(cudaStream_t s, const float* P, const float* x, int64_t B, const Ws& w, int q) {
   const int Bi = (int)B;
@@ -837,21 +860,25 @@ static void forward_backward(cudaStream_t s, const float* P, const float* x, int
   if (q) launch_pdl(k_wimg, dim3(kWimgBlocks), 256, 0, s, P, w.wimg);
   launch_pdl(k_layer1<0>, l1_blocks, H, 0, s, x, P + OFF_W1, P + OFF_B1, (const float*)nullptr, (const float*)nullptr,
              w.Z[1], w.Hh[1], B, q);
+  // quantised, each product's A image is written by the product before it (im0 / im1 alternate)
+  uint8_t* const im0 = q ? w.aimg[0] : nullptr;
+  uint8_t* const im1 = q ? w.aimg[1] : nullptr;
   gemm<false, true>(s, w, Bi, H, H, w.Hh[1], H, P + OFF_W2, H, w.Z[2], H, 0.0f, P + OFF_B2, q, q,
-                    epi_silu(w.Hh[2], q), wimg_of(w, 2, 0));
+                    with_img(epi_silu(w.Hh[2], q), im0, 1), wimg_of(w, 2, 0));                    // H2
   gemm<false, true>(s, w, Bi, H, H, w.Hh[2], H, P + OFF_W3, H, w.Z[3], H, 0.0f, P + OFF_B3, q, q,
-                    epi_silu(w.Hh[3], q), wimg_of(w, 3, 0));
+                    with_img(epi_silu(w.Hh[3], q), im1, 1), wimg_of(w, 3, 0), im0);               // H3
   gemm<false, true>(s, w, Bi, H, H, w.Hh[3], H, P + OFF_W4, H, w.Z[4], H, 0.0f, P + OFF_B4, q, q,
-                    epi_silu_d4(w.Hh[4], 0, P + OFF_W5, w.D[4], q), wimg_of(w, 4, 0));  // and D4 = silu'(Z4) w5
+                    with_img(epi_silu_d4(w.Hh[4], 0, P + OFF_W5, w.D[4], q), im0, 2), wimg_of(w, 4, 0),
+                    im1);  // H4 and D4 = silu'(Z4) w5
   launch_pdl(k_rowdot, dim3((unsigned)((B + 7) / 8)), 256, 0, s, (const float*)w.Hh[4], P + OFF_W5, P + OFF_B5, B, 1,
              w.out);
   // input gradient
   gemm<false, false>(s, w, Bi, H, H, w.D[4], H, P + OFF_W4, H, w.U[3], H, 0.0f, nullptr, q, q,
-                     epi_dmul(w.Z[3], w.D[3], q, q), wimg_of(w, 4, 1));
+                     with_img(epi_dmul(w.Z[3], w.D[3], q, q), im1, 1), wimg_of(w, 4, 1), im0);   // D3
   gemm<false, false>(s, w, Bi, H, H, w.D[3], H, P + OFF_W3, H, w.U[2], H, 0.0f, nullptr, q, q,
-                     epi_dmul(w.Z[2], w.D[2], q, q), wimg_of(w, 3, 1));
+                     with_img(epi_dmul(w.Z[2], w.D[2], q, q), im0, 1), wimg_of(w, 3, 1), im1);   // D2
   gemm<false, false>(s, w, Bi, H, H, w.D[2], H, P + OFF_W2, H, w.U[1], H, 0.0f, nullptr, q, q,
-                     epi_dmul(w.Z[1], w.D[1], 0, 0), wimg_of(w, 2, 1));
+                     epi_dmul(w.Z[1], w.D[1], 0, 0), wimg_of(w, 2, 1), im0);                    // D1
   launch_pdl(k_rowdot, dim3((unsigned)((B + 7) / 8)), 256, 0, s, (const float*)w.D[1], P + OFF_W1,
              (const float*)nullptr, B, 3, w.G);
 }

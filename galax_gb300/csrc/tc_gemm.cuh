@@ -87,6 +87,14 @@ struct Args {
   // 16 KB K blocks exactly as put() would lay them out; bulk-copied into
   // shared memory at the start instead of staged through registers.
   const uint8_t* bimg;
+  // Optional, with bimg: A as a bf16 image of the same layout (row block mb
+  // of 128 rows at aimg + mb * 64 KB); then the product is fed by bulk copies
+  // alone (split_a = 0, K = 256).
+  const uint8_t* aimg;
+  // Optional: the store phase also writes a bf16 image (the layout of aimg)
+  // of o1 (img_src = 1) or o2 (img_src = 2), for the next product's A.
+  uint8_t* img_out;
+  int img_src;
   int kchunk;  // K per blockIdx.z, a multiple of BK
   float* part;  // gridDim.z > 1: partial tiles [z][M][N]
   int* err;
@@ -318,6 +326,11 @@ __device__ __forceinline__ void store_tile(const Args& a, const float* out, int 
           *reinterpret_cast<float4*>(a.o1 + idx) = make_float4(r1[0], r1[1], r1[2], r1[3]);
         if constexpr (epi_writes_o2<EPI>())
           *reinterpret_cast<float4*>(a.o2 + idx) = make_float4(r2[0], r2[1], r2[2], r2[3]);
+        if (a.img_out) {  // 4 consecutive K of row m: 8 bytes of one 16-byte chunk
+          const float* r = a.img_src == 2 ? r2 : r1;
+          *reinterpret_cast<uint2*>(a.img_out + (size_t)(m >> 7) * BIMG_BYTES + tc::sw128_offset(128, m & 127, n)) =
+              make_uint2(tc::pack_bf16x2(r[0], r[1]), tc::pack_bf16x2(r[2], r[3]));
+        }
       }
     }
     return;
@@ -345,6 +358,9 @@ __device__ __forceinline__ void store_tile(const Args& a, const float* out, int 
       if constexpr (epi_stores_c<EPI>()) a.C[idx] = v;
       if constexpr (EPI != EPI_NONE) a.o1[idx] = r1;
       if constexpr (epi_writes_o2<EPI>()) a.o2[idx] = r2;
+      if (a.img_out)
+        *reinterpret_cast<uint16_t*>(a.img_out + (size_t)(m >> 7) * BIMG_BYTES +
+                                     tc::sw128_offset(128, m & 127, n)) = bf16_bits(a.img_src == 2 ? r2 : r1);
     }
   }
 }
@@ -357,7 +373,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_tc_gemm(Args a) {
   uint64_t* done = reinterpret_cast<uint64_t*>(smem + a.bar_off);
   uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(done + 3);
   const bool bim = a.bimg != nullptr;
-  uint8_t* const bsm = smem + 2 * a.stage;  // image mode: B, four 16 KB K blocks
+  const bool aim = bim && a.aimg != nullptr;  // both operands from images: no staging at all
+  uint8_t* const bsm = smem + 2 * a.stage;  // image mode: B, four 16 KB K blocks (A's image below it)
   __shared__ int fail_s;
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
   const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
@@ -389,20 +406,42 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_tc_gemm(Args a) {
   // set-up done; now the previous kernel's results are needed
   tc::pdl_wait();
   if (bim && t == 0 && nk > 0) {
-    tc::mbar_expect_tx(&done[2], (uint32_t)nk * B_BLK);
-    for (int kb = 0; kb < nk; ++kb)
+    tc::mbar_expect_tx(&done[2], (uint32_t)nk * (aim ? A_BLK + B_BLK : B_BLK));
+    for (int kb = 0; kb < nk; ++kb) {
       tc::bulk_g2s(bsm + kb * B_BLK, a.bimg + (size_t)blockIdx.x * BIMG_BYTES + (size_t)kb * B_BLK, B_BLK, &done[2]);
+      if (aim)
+        tc::bulk_g2s(smem + kb * A_BLK, a.aimg + (size_t)blockIdx.y * BIMG_BYTES + (size_t)kb * A_BLK, A_BLK,
+                     &done[2]);
+    }
   }
   constexpr uint32_t idesc = tc::idesc_bf16(BM, BN);
   int committed = 0;  // k blocks whose products were issued (the same count in every thread)
   prefetch_epilogue<EPI>(a, m0, n0);
   Frag<BM> fa;
   Frag<BN> fb;
-  if (nk > 0) {
+  if (aim) {
+    // both operands arrive by bulk copy: thread 0 waits for them and issues every product
+    if (t == 0 && nk > 0) {
+      if (!tc::mbar_wait(&done[2], 0, WAIT_LIMIT)) {
+        fail_s = 1;
+      } else {
+        tc::tc_fence_after();
+        const uint32_t ab = tc::smem_u32(smem), bb = tc::smem_u32(bsm);
+        for (int kb = 0; kb < nk; ++kb)
+#pragma unroll
+          for (int ks = 0; ks < 4; ++ks)
+            tc::mma_bf16(tmem, tc::desc_sw128(ab + kb * A_BLK + ks * 32), tc::desc_sw128(bb + kb * B_BLK + ks * 32),
+                         idesc, (kb | ks) != 0);
+      }
+      tc::mma_commit(&done[0]);
+    }
+    committed = nk;
+  }
+  if (!aim && nk > 0) {
     fetch<BM>(fa, A, sam, sak, m0, a.M, kbeg, kend);
     if (!bim) fetch<BN>(fb, Bm, sbn, sbk, n0, a.N, kbeg, kend);
   }
-  for (int kb = 0; kb < nk; ++kb) {
+  for (int kb = 0; kb < (aim ? 0 : nk); ++kb) {
     const int s = kb & 1;
     uint8_t* st = smem + s * a.stage;
     if (kb >= 2 && !tc::mbar_wait(&done[s], (uint32_t)((kb / 2 - 1) & 1), WAIT_LIMIT)) fail_s = 1;
@@ -442,7 +481,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_tc_gemm(Args a) {
   // the last commit arrives once every product issued by this CTA has completed
   if (committed > 0) {
     const int last = committed - 1;
-    if (!tc::mbar_wait(&done[last & 1], (uint32_t)((last / 2) & 1), WAIT_LIMIT)) fail_s = 1;
+    uint64_t* bar = aim ? &done[0] : &done[last & 1];
+    if (!tc::mbar_wait(bar, aim ? 0u : (uint32_t)((last / 2) & 1), WAIT_LIMIT)) fail_s = 1;
   }
   tc::tc_fence_after();
   __syncthreads();

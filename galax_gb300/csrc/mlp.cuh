@@ -22,7 +22,17 @@ constexpr int64_t OFF_W5 = OFF_B4 + H;          // [H]
 constexpr int64_t OFF_B5 = OFF_W5 + H;          // [1]
 constexpr int64_t NPARAM = OFF_B5 + 1;          // 198,657
 
-__host__ __device__ __forceinline__ float sigmoidf_(float z) { return 1.0f / (1.0f + expf(-z)); }
+// On the device the exponential and the reciprocal come from the SFU
+// (__expf, __frcp_rn: a few units in the last place, ~1e-6 relative at
+// worst), which keeps the elementwise work of the training products short;
+// the network's activations are rounded to bfloat16 anyway.
+__host__ __device__ __forceinline__ float sigmoidf_(float z) {
+#ifdef __CUDA_ARCH__
+  return __frcp_rn(1.0f + __expf(-z));
+#else
+  return 1.0f / (1.0f + expf(-z));
+#endif
+}
 __host__ __device__ __forceinline__ float silu(float z) { return z * sigmoidf_(z); }
 __host__ __device__ __forceinline__ float dsilu(float z) {
   const float s = sigmoidf_(z);

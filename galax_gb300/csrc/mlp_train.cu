@@ -151,57 +151,11 @@ __global__ void k_zb_acc(const float* Z, const float* Hb, float* Zb, int64_t n) 
   GRID_STRIDE(i, n) { Zb[i] += dsilu(Z[i]) * Hb[i]; }
 }
 
-// The first layer's 3-wide products with the elementwise step that follows:
-//   MODE 0: Z1 = X W1^T + b1 and H1 = silu(Z1) (bf16-rounded when q) -> o1 = Z1, o2 = H1
-//   MODE 1: Db1 = X W1^T (X = the gradient residual weights), then
-//           o1 = Ub = silu'(Z1) Db1, o2 = Zb1 = silu''(Z1) U1 Db1 (Db1 itself is not stored)
-// Thread c owns column c (row c of W1 in registers); a block takes kL1Rows rows,
-// all of whose loads are issued before the first store.
-// The sum is fma(w0, x0, fma(w1, x1, fma(w2, x2, b1))), the inference
-// kernel's order, so both compute the same first layer.
-constexpr int kL1Rows = 8;
-
-template <int MODE>
-__global__ void __launch_bounds__(256) k_layer1(const float* __restrict__ X, const float* __restrict__ W1,
-                                                const float* __restrict__ b1, const float* __restrict__ Z,
-                                                const float* __restrict__ U, float* __restrict__ o1,
-                                                float* __restrict__ o2, int64_t rows, int q) {
-  tc::pdl_wait();
-  tc::pdl_trigger();
-  const int c = threadIdx.x;
-  const float w0 = W1[3 * c], w1 = W1[3 * c + 1], w2 = W1[3 * c + 2];
-  const float bc = MODE == 0 ? b1[c] : 0.0f;
-  const int64_t b0 = (int64_t)blockIdx.x * kL1Rows;
-  float v[kL1Rows], z[kL1Rows], u[kL1Rows];
-#pragma unroll
-  for (int i = 0; i < kL1Rows; ++i) {
-    const int64_t b = b0 + i < rows ? b0 + i : rows - 1;  // rows past the end repeat the last (not stored)
-    v[i] = fmaf(w0, X[3 * b], fmaf(w1, X[3 * b + 1], fmaf(w2, X[3 * b + 2], bc)));
-    if constexpr (MODE == 1) {
-      z[i] = Z[b * H + c];
-      u[i] = U[b * H + c];
-    }
-  }
-#pragma unroll
-  for (int i = 0; i < kL1Rows; ++i) {
-    const int64_t b = b0 + i;
-    if (b >= rows) break;
-    const int64_t idx = b * H + c;
-    if constexpr (MODE == 0) {
-      const float h = silu(v[i]);
-      o1[idx] = v[i];
-      o2[idx] = q ? bf16r(h) : h;
-    } else {
-      o1[idx] = dsilu(z[i]) * v[i];
-      o2[idx] = d2silu(z[i]) * u[i] * v[i];
-    }
-  }
-}
-
 // Column sums over the B rows of a [B][H] array in two deterministic passes:
 // k_colpart sums f(b, c) over 64-row chunks, k_colfinal_all adds the chunks in
 // order. f: mode 0 X[b,c]; 1 X[b,c] v[b]; 2 silu'(X[b,c]) Y[b,c];
-// 3 X[b,c] V[b][j] for j = 0..2, out[c][3] (the first layer's weight gradient).
+// 3 X[b,c] V[b][j] for j = 0..2, out[c][3] (the first layer's weight gradient);
+// 4 both mode 3 (into part) and mode 0 (into part2) from one read of X.
 // In k_colpart warp w sums rows w*8 .. w*8+7 of the chunk, lane l columns
 // 4l..4l+3 and 128+4l..128+4l+3 (two float4 per row: a warp reads whole
 // rows); the eight loads of each operand are issued together, and the eight
@@ -210,15 +164,15 @@ constexpr int kColRows = 64;
 
 template <int mode>
 __global__ void __launch_bounds__(256) k_colpart(const float* X, const float* Y, const float* v, const float* V,
-                                                 int64_t rows, float* part) {
+                                                 int64_t rows, float* part, float* part2) {
   tc::pdl_wait();
   tc::pdl_trigger();
-  __shared__ float red[3][8][H];
+  __shared__ float red[4][8][H];
   const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
   const int64_t b0 = (int64_t)blockIdx.x * kColRows + wp * 8;
-  float s[3][8];
+  float s[4][8];
 #pragma unroll
-  for (int j = 0; j < 3; ++j)
+  for (int j = 0; j < 4; ++j)
 #pragma unroll
     for (int e = 0; e < 8; ++e) s[j][e] = 0.0f;
   // all of the thread's loads first, then the sums
@@ -238,7 +192,7 @@ __global__ void __launch_bounds__(256) k_colpart(const float* X, const float* Y,
       yb[i] = in ? yr[32 + lane] : z4;
     }
     if constexpr (mode == 1) sc[i][0] = in ? v[b] : 0.0f;
-    if constexpr (mode == 3)
+    if constexpr (mode >= 3)
 #pragma unroll
       for (int j = 0; j < 3; ++j) sc[i][j] = in ? V[b * 3 + j] : 0.0f;
   }
@@ -260,11 +214,14 @@ __global__ void __launch_bounds__(256) k_colpart(const float* X, const float* Y,
       for (int j = 0; j < 3; ++j)
 #pragma unroll
         for (int e = 0; e < 8; ++e) s[j][e] = fmaf(x[e], sc[i][j], s[j][e]);
+      if constexpr (mode == 4)
+#pragma unroll
+        for (int e = 0; e < 8; ++e) s[3][e] += x[e];
     }
   }
-  constexpr int nj = mode == 3 ? 3 : 1;
+  constexpr int nj = mode >= 3 ? 3 : 1, nr = mode == 4 ? 4 : nj;
 #pragma unroll
-  for (int j = 0; j < nj; ++j)
+  for (int j = 0; j < nr; ++j)
 #pragma unroll
     for (int e = 0; e < 8; ++e) red[j][wp][(e < 4 ? 0 : 128) + 4 * lane + (e & 3)] = s[j][e];
   __syncthreads();
@@ -276,6 +233,15 @@ __global__ void __launch_bounds__(256) k_colpart(const float* X, const float* Y,
 #pragma unroll
       for (int q = 0; q < 8; ++q) t += red[j][q][c];
     p[j] = t;
+  }
+  if constexpr (mode == 4) {
+    float t = 0.0f;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) t += red[3][q][c];
+    float* p2 = part2 + ((int64_t)blockIdx.x * H + c) * 3;
+    p2[0] = t;
+    p2[1] = 0.0f;
+    p2[2] = 0.0f;
   }
 }
 
@@ -446,10 +412,7 @@ constexpr int kLossBlocks = 4096;  // k_loss's largest grid (ew_grid)
 // kWimgOne, column block nb at + nb * BIMG_BYTES, laid out by tc::sw128_offset
 // for 128 rows (n) x 256 K; o = 0: B(n, k) = W[n][k], o = 1: B(n, k) = W[k][n].
 // One thread per 16-byte chunk (8 consecutive k).
-__global__ void __launch_bounds__(256) k_wimg(const float* P, uint8_t* wimg) {
-  tc::pdl_wait();
-  tc::pdl_trigger();
-  const int i = blockIdx.x * 256 + threadIdx.x;
+__device__ __forceinline__ void wimg_chunk(const float* P, uint8_t* wimg, int i) {
   const int chunk = i & 31, row = (i >> 5) & 127, nb = (i >> 12) & 1, o = (i >> 13) & 1, m = i >> 14;
   if (m >= 3) return;
   const float* W = P + (m == 0 ? OFF_W2 : (m == 1 ? OFF_W3 : OFF_W4));
@@ -466,6 +429,61 @@ __global__ void __launch_bounds__(256) k_wimg(const float* P, uint8_t* wimg) {
                             tc::sw128_offset(128, row, k0)) = make_uint4(h[0], h[1], h[2], h[3]);
 }
 constexpr int kWimgBlocks = 3 * 2 * 2 * 128 * 32 / 256;
+
+// The first layer's 3-wide products with the elementwise step that follows:
+//   MODE 0: Z1 = X W1^T + b1 and H1 = silu(Z1) (bf16-rounded when q) -> o1 = Z1, o2 = H1
+//   MODE 1: Db1 = X W1^T (X = the gradient residual weights), then
+//           o1 = Ub = silu'(Z1) Db1, o2 = Zb1 = silu''(Z1) U1 Db1 (Db1 itself is not stored)
+// Thread c owns column c (row c of W1 in registers); a block takes kL1Rows rows,
+// all of whose loads are issued before the first store.
+// The sum is fma(w0, x0, fma(w1, x1, fma(w2, x2, b1))), the inference
+// kernel's order, so both compute the same first layer.
+constexpr int kL1Rows = 8;
+
+// MODE 0 with wimg set: blocks from nrow_blocks on build the layers' weight
+// images instead (wimg_chunk), in the same launch.
+template <int MODE>
+__global__ void __launch_bounds__(256) k_layer1(const float* __restrict__ X, const float* __restrict__ W1,
+                                                const float* __restrict__ b1, const float* __restrict__ Z,
+                                                const float* __restrict__ U, float* __restrict__ o1,
+                                                float* __restrict__ o2, int64_t rows, int q, const float* P,
+                                                uint8_t* wimg, unsigned nrow_blocks) {
+  tc::pdl_wait();
+  tc::pdl_trigger();
+  if (MODE == 0 && wimg && blockIdx.x >= nrow_blocks) {
+    wimg_chunk(P, wimg, (int)(blockIdx.x - nrow_blocks) * 256 + threadIdx.x);
+    return;
+  }
+  const int c = threadIdx.x;
+  const float w0 = W1[3 * c], w1 = W1[3 * c + 1], w2 = W1[3 * c + 2];
+  const float bc = MODE == 0 ? b1[c] : 0.0f;
+  const int64_t b0 = (int64_t)blockIdx.x * kL1Rows;
+  float v[kL1Rows], z[kL1Rows], u[kL1Rows];
+#pragma unroll
+  for (int i = 0; i < kL1Rows; ++i) {
+    const int64_t b = b0 + i < rows ? b0 + i : rows - 1;  // rows past the end repeat the last (not stored)
+    v[i] = fmaf(w0, X[3 * b], fmaf(w1, X[3 * b + 1], fmaf(w2, X[3 * b + 2], bc)));
+    if constexpr (MODE == 1) {
+      z[i] = Z[b * H + c];
+      u[i] = U[b * H + c];
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < kL1Rows; ++i) {
+    const int64_t b = b0 + i;
+    if (b >= rows) break;
+    const int64_t idx = b * H + c;
+    if constexpr (MODE == 0) {
+      const float h = silu(v[i]);
+      o1[idx] = v[i];
+      o2[idx] = q ? bf16r(h) : h;
+    } else {
+      o1[idx] = dsilu(z[i]) * v[i];
+      o2[idx] = d2silu(z[i]) * u[i] * v[i];
+    }
+  }
+}
+
 // an A-operand image of a [B][256] activation: 64 KB per 128-row block
 static size_t aimg_bytes(int64_t B) { return (size_t)((B + 127) / 128) * tcg::BIMG_BYTES; }
 
@@ -758,16 +776,19 @@ static float* col_slot(const Ws& w, int64_t B, int slot) {
   return w.colpart + (size_t)slot * col_chunks(B) * H * 3;
 }
 
-// the chunk sums of one column sum into its slot (finished by k_colfinal_all)
+// the chunk sums of one column sum into its slot (finished by k_colfinal_all);
+// mode 4 also writes mode 0's sums into slot2
 static void colpart(cudaStream_t s, const Ws& w, const float* X, const float* Y, const float* v, const float* V,
-                    int64_t B, int mode, int slot) {
+                    int64_t B, int mode, int slot, int slot2 = -1) {
   const unsigned g = (unsigned)col_chunks(B);
   float* part = col_slot(w, B, slot);
+  float* part2 = slot2 >= 0 ? col_slot(w, B, slot2) : nullptr;
   switch (mode) {
-    case 0: launch_pdl(k_colpart<0>, g, H, 0, s, X, Y, v, V, B, part); break;
-    case 1: launch_pdl(k_colpart<1>, g, H, 0, s, X, Y, v, V, B, part); break;
-    case 2: launch_pdl(k_colpart<2>, g, H, 0, s, X, Y, v, V, B, part); break;
-    default: launch_pdl(k_colpart<3>, g, H, 0, s, X, Y, v, V, B, part); break;
+    case 0: launch_pdl(k_colpart<0>, g, H, 0, s, X, Y, v, V, B, part, part2); break;
+    case 1: launch_pdl(k_colpart<1>, g, H, 0, s, X, Y, v, V, B, part, part2); break;
+    case 2: launch_pdl(k_colpart<2>, g, H, 0, s, X, Y, v, V, B, part, part2); break;
+    case 3: launch_pdl(k_colpart<3>, g, H, 0, s, X, Y, v, V, B, part, part2); break;
+    default: launch_pdl(k_colpart<4>, g, H, 0, s, X, Y, v, V, B, part, part2); break;
   }
 }
 
@@ -856,10 +877,10 @@ static Epi with_img(Epi e, uint8_t* img, int src) {
 static void forward_backward(cudaStream_t s, const float* P, const float* x, int64_t B, const Ws& w, int q) {
   const int Bi = (int)B;
   const unsigned l1_blocks = (unsigned)((B + kL1Rows - 1) / kL1Rows);
-  // quantised: the layers' weights enter every product rounded to bf16, from their images
-  if (q) launch_pdl(k_wimg, dim3(kWimgBlocks), 256, 0, s, P, w.wimg);
-  launch_pdl(k_layer1<0>, l1_blocks, H, 0, s, x, P + OFF_W1, P + OFF_B1, (const float*)nullptr, (const float*)nullptr,
-             w.Z[1], w.Hh[1], B, q);
+  // quantised: the layers' weights enter every product rounded to bf16, from their images (built by
+  // extra blocks of the first-layer launch)
+  launch_pdl(k_layer1<0>, dim3(l1_blocks + (q ? kWimgBlocks : 0)), H, 0, s, x, P + OFF_W1, P + OFF_B1,
+             (const float*)nullptr, (const float*)nullptr, w.Z[1], w.Hh[1], B, q, P, q ? w.wimg : nullptr, l1_blocks);
   // quantised, each product's A image is written by the product before it (im0 / im1 alternate)
   uint8_t* const im0 = q ? w.aimg[0] : nullptr;
   uint8_t* const im1 = q ? w.aimg[1] : nullptr;
@@ -961,7 +982,8 @@ static void loss_grads(cudaStream_t s, const float* P, const float* x, const flo
   colpart(t, w, w.Hh[4], nullptr, w.Pb, nullptr, B, 1, 2);                                 // gw5 += H4^T Pb
   // ---- through the input-gradient graph, layer 1 up to 4
   launch_pdl(k_layer1<1>, dim3((unsigned)((B + kL1Rows - 1) / kL1Rows)), H, 0, s, (const float*)w.Eb, P + OFF_W1,
-             (const float*)nullptr, (const float*)w.Z[1], (const float*)w.U[1], w.Ub, w.Zb[1], B, 0);  // Db1 = Eb W1^T
+             (const float*)nullptr, (const float*)w.Z[1], (const float*)w.U[1], w.Ub, w.Zb[1], B, 0,
+             (const float*)nullptr, (uint8_t*)nullptr, 0u);  // Db1 = Eb W1^T
   // Ub1, Ub2, Ub3 in buffers of their own: each stays until the weight gradient
   // that pairs it with a forward-graph term (gWk = Dk^T Ub(k-1) + Zbk^T H(k-1))
   gemm<false, true>(s, w, Bi, H, H, w.Ub, H, P + OFF_W2, H, w.Db, H, 0.0f, nullptr, 0, q,
@@ -987,8 +1009,7 @@ static void loss_grads(cudaStream_t s, const float* P, const float* x, const flo
   colpart(t, w, w.Zb[2], nullptr, nullptr, nullptr, B, 0, 5);
   gemm<false, false>(s, w, Bi, H, H, w.Zb[2], H, P + OFF_W2, H, w.Hb, H, 0.0f, nullptr, 0, q,
                      epi_zbacc(w.Z[1], w.Zb[1]), wimg_of(w, 2, 1));
-  colpart(s, w, w.Zb[1], nullptr, nullptr, x, B, 3, 6);                                     // gW1 += Zb1^T X
-  colpart(s, w, w.Zb[1], nullptr, nullptr, nullptr, B, 0, 7);
+  colpart(s, w, w.Zb[1], nullptr, nullptr, x, B, 4, 6, 7);                                  // gW1 += Zb1^T X; gb1
   ColJobs J{};
   const int slot_a[kColJobs - 2] = {0, 1, 3, 4, 5, 7}, slot_b[kColJobs - 2] = {6, 2, -1, -1, -1, -1};
   const int64_t outs[kColJobs - 2] = {OFF_W1, OFF_W5, OFF_B4, OFF_B3, OFF_B2, OFF_B1};

@@ -761,10 +761,12 @@ def run_train(args, rank, world, dist) -> dict | None:
                          "unit": "TFLOP/s", "frac": achieved / peaks["bf16_tflops"] if peaks.get("bf16_tflops") else None,
                          "flops_per_training_step": train_step_flops(batch),
                          "note": "algorithmic flops; the 8192-row products are too small to fill the tensor cores, so "
-                                 "the step is set by the chain of ~30 dependent kernels"},
-            # per training step: gather, 9 forward/input-gradient kernels, 23 of the second-order pass
-            # (12 products, 3 split-K sums, 8 column-sum and loss kernels), Adam and the step counter
-            "clocks": clk, "gpu_launches": args.steps * nsteps * 35}
+                                 "the step is set by its chain of ~25 dependent kernels"},
+            # per training step: gather, 9 forward/input-gradient kernels (first layer with the weight
+            # images, 6 products, 2 row sums), 22 of the second-order pass (9 products, 3 two-term
+            # weight-gradient products and their 3 split-K sums, 7 column-sum and loss kernels), Adam
+            # and the step counter
+            "clocks": clk, "gpu_launches": args.steps * nsteps * 34}
 
 
 def run_surrogate(args, n, rank, world, dist) -> dict | None:

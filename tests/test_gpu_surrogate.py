@@ -81,6 +81,29 @@ def test_weighted_training_gradient_matches_numpy(env):
         assert np.linalg.norm(got - ref) <= 3e-4 * np.linalg.norm(ref) + 1e-7, k
 
 
+def test_quantised_training_gradient_is_close_to_fp32(env):
+    """The quantised pass (bf16 weights and activations, the products fed from
+    bf16 images, the fused store phases, the two-term weight gradients) gives
+    the FP32 gradient up to the bf16 rounding of its operands: a wrong image,
+    orientation or term would be off by O(1)."""
+    gx, S = env
+    p = _params(S, seed=5)
+    rng = np.random.default_rng(17)
+    B = 4096  # several row blocks and the split-K weight gradients
+    u = rng.normal(size=(B, 3)).astype(np.float32)
+    pt = rng.normal(size=B).astype(np.float32)
+    gt = rng.normal(size=(B, 3)).astype(np.float32)
+    loss_q, grad_q = S.loss_grads(p, u, pt, gt, 0.7, 1.3, quantize=True)
+    L_ref, g_ref = M.loss_and_grads(_as_oracle(S, p), u.astype(np.float64), pt.astype(np.float64),
+                                    gt.astype(np.float64), 0.7, 1.3)
+    assert abs(loss_q - L_ref) <= 2e-2 * abs(L_ref)
+    gd = S.unpack(grad_q)
+    for k in M.NAMES:
+        ref = g_ref[k].reshape(-1)
+        got = gd[k].reshape(-1).astype(np.float64)
+        assert np.linalg.norm(got - ref) <= 5e-2 * np.linalg.norm(ref) + 1e-6, k
+
+
 def test_quantised_fp32_forward_matches_numpy_bf16(env):
     gx, S = env
     p = _params(S)

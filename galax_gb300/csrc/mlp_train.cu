@@ -14,9 +14,17 @@
 // the forward and backward passes, and the weight gradients with K = batch)
 // runs on the tensor cores (tc_gemm.cuh): operands the quantised passes round
 // to bf16 enter as one bf16 part, all others as two (hi + lo), so the
-// gradients keep FP32-level accuracy. The products with 3 or 1 columns or K = 3
-// (first and last layers) stay on a tiled FP32 kernel; elementwise work runs in
-// small grid-stride kernels.
+// gradients keep FP32-level accuracy. The elementwise step after each product
+// runs in its store phase; in the quantised passes the weights, and the
+// activations passed from product to product, travel as bf16 operand images
+// fed by bulk copies. The first layer (K = 3) is one fused kernel, the
+// 1-column and 3-column products are warp row sums, the column sums of the
+// bias and first-layer gradients go through per-chunk partials finished in
+// one launch, and the weight gradients and column sums run on a second
+// stream beside the chain of input-gradient products. Every reduction adds in
+// a fixed order, so training is deterministic. The FP32 tiled kernel and the
+// grid-stride elementwise kernels remain as the path for products the tensor
+// cores do not take.
 #include <cuda_runtime.h>
 
 #include <atomic>

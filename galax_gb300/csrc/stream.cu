@@ -853,11 +853,71 @@ __device__ Dual<N> log1p(const Dual<N>& a) {
   return r;
 }
 
+// The power law with cutoff's radial factors g (grad Phi = g x) and g'(r)/r,
+// and their partial derivatives in r^2, G m, r_c and alpha, at the
+// component's parameters (cc's folded constants: 1 / r_c^2, 1 / Gamma(a1),
+// psi(a1)). With x = r^2 / r_c^2, a1 = 3/2 - alpha/2, P = gamma(a1, x) /
+// Gamma(a1) and eN = x^a1 e^-x / Gamma(a1):
+//   g = G m P r^-3,  g'/r = 2 G m eN r^-5 - 3 g r^-2,
+//   dP/dx = eN / x,  deN/dx = eN (a1 / x - 1),  deN/da1 = eN (log x - psi(a1)),
+//   dP/da1 from the series or continued fraction's a-derivative (as in plc_g).
+struct PlcHess {
+  double g, gpr;
+  double g_r2, g_gm, g_rc, g_al;      // dg / d(r^2, G m, r_c, alpha)
+  double p_r2, p_gm, p_rc, p_al;      // d(g'/r) / d(...)
+};
+
+__device__ __noinline__ PlcHess plc_hess(const DevComp& c, double Gm, double rc, double r2) {
+  const double a1 = fma(-0.5, c.l2, 1.5);
+  const double irc2 = c.inv_l1;
+  const double x = r2 * irc2;
+  const IncGamma ig = inc_gamma(a1, x, true);
+  const double eN = ig.e * c.l2sq;
+  const double P = ig.series ? eN * ig.sum : 1.0 - eN * ig.sum;
+  const double dPda = ig.series ? fma(eN, fma(ig.lx, ig.sum, ig.dsum), -P * c.aux0)
+                                : -fma(eN, fma(ig.lx, ig.sum, ig.dsum), -(1.0 - P) * c.aux0);
+  const double ir = 1.0 / ::sqrt(r2), ir2 = ir * ir, ir3 = ir2 * ir, ir5 = ir3 * ir2, ir7 = ir5 * ir2;
+  const double dPdx = eN / x, deNdx = eN * (a1 / x - 1.0), deNda = eN * (ig.lx - c.aux0);
+  PlcHess o;
+  o.g = Gm * P * ir3;
+  o.gpr = 2.0 * Gm * eN * ir5 - 3.0 * o.g * ir2;
+  o.g_r2 = Gm * (dPdx * irc2 * ir3 - 1.5 * P * ir5);
+  o.g_gm = P * ir3;
+  o.g_rc = Gm * eN * (-2.0 / rc) * ir3;          // dx/dr_c = -2 x / r_c
+  o.g_al = Gm * dPda * (-0.5) * ir3;              // da1/dalpha = -1/2
+  o.p_r2 = 2.0 * Gm * (deNdx * irc2 * ir5 - 2.5 * eN * ir7) - 3.0 * (o.g_r2 * ir2 - o.g * ir2 * ir2);
+  o.p_gm = 2.0 * eN * ir5 - 3.0 * o.g_gm * ir2;
+  o.p_rc = 2.0 * Gm * deNdx * (-2.0 * x / rc) * ir5 - 3.0 * o.g_rc * ir2;
+  o.p_al = 2.0 * Gm * deNda * (-0.5) * ir5 - 3.0 * o.g_al * ir2;
+  return o;
+}
+
+__device__ __forceinline__ void plc_radial(const DevComp& c, double Gm, double rc, double al, double r2, double& g,
+                                           double& gpr) {
+  const PlcHess h = plc_hess(c, Gm, rc, r2);
+  g = h.g;
+  gpr = h.gpr;
+}
+template <int N>
+__device__ void plc_radial(const DevComp& c, const Dual<N>& Gm, const Dual<N>& rc, const Dual<N>& al,
+                           const Dual<N>& r2, Dual<N>& g, Dual<N>& gpr) {
+  const PlcHess h = plc_hess(c, Gm.v, rc.v, r2.v);
+  g = Dual<N>(h.g);
+  gpr = Dual<N>(h.gpr);
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    g.d[i] = h.g_r2 * r2.d[i] + h.g_gm * Gm.d[i] + h.g_rc * rc.d[i] + h.g_al * al.d[i];
+    gpr.d[i] = h.p_r2 * r2.d[i] + h.p_gm * Gm.d[i] + h.p_rc * rc.d[i] + h.p_al * al.d[i];
+  }
+}
+
 // Hessian of one component at offset d from its centre (same closed forms as
 // comp_hessian), generic in the number type so parameters and positions can
-// carry tangents.
+// carry tangents. cc: the component (the power law with cutoff reads its
+// folded constants; its parameters' tangents come from Gm, l1, l2).
 template <class T>
-__device__ void comp_hessian_t(int kind, const T& Gm, const T& l1, const T& l2, const T* d, T* H) {
+__device__ void comp_hessian_t(const DevComp& cc, int kind, const T& Gm, const T& l1, const T& l2, const T* d,
+                               T* H) {
   if (kind == MIYAMOTO_NAGAI) {
     const T zb = sqrt(d[2] * d[2] + l2 * l2);
     const T s = zb + l1;
@@ -895,6 +955,8 @@ __device__ void comp_hessian_t(int kind, const T& Gm, const T& l1, const T& l2, 
     const T q = r2 + l1 * l1;
     g = Gm / q;
     gpr = -2.0 * g / q;
+  } else if (kind == POWERLAW_CUTOFF) {
+    plc_radial(cc, Gm, l1, l2, r2, g, gpr);
   } else {  // PLUMMER
     const T s2 = r2 + l1 * l1, s = sqrt(s2);
     g = Gm / (s2 * s);
@@ -1134,7 +1196,7 @@ __global__ void __launch_bounds__(128) k_stream_release_adj(StreamDev a, const D
   for (int c = 0; c < a.ncomp; ++c) {
     const DevComp& cc = s_comps[c];
     const Dual<3> dd[3] = {X[0] - cc.ox, X[1] - cc.oy, X[2] - cc.oz};
-    comp_hessian_t<Dual<3>>(cc.kind, Dual<3>(cc.Gm), Dual<3>(cc.l1), Dual<3>(cc.l2), dd, Hd);
+    comp_hessian_t<Dual<3>>(cc, cc.kind, Dual<3>(cc.Gm), Dual<3>(cc.l1), Dual<3>(cc.l2), dd, Hd);
   }
   const Dual<3> prr = contract_rhat(Hd, RH);
   const double D = om * om - prr.v;
@@ -1153,7 +1215,7 @@ __global__ void __launch_bounds__(128) k_stream_release_adj(StreamDev a, const D
     dd[1] = Dual<2>(x[1] - cc.oy);
     dd[2] = Dual<2>(x[2] - cc.oz);
     for (int j = 0; j < 3; ++j) rhd[j] = Dual<2>(rh[j]);
-    comp_hessian_t<Dual<2>>(cc.kind, Dual<2>(cc.Gm), l1, l2, dd, Hc);
+    comp_hessian_t<Dual<2>>(cc, cc.kind, Dual<2>(cc.Gm), l1, l2, dd, Hc);
     const Dual<2> pc = contract_rhat(Hc, rhd);
     a.gp_all[(int64_t)(3 * c + 0) * a.ncol + a.np + r] = prr_b * pc.v * cc.inv_m;
     a.gp_all[(int64_t)(3 * c + 1) * a.ncol + a.np + r] = prr_b * pc.d[0];
@@ -1535,9 +1597,6 @@ gal_status gal_stream_grad(const gal_potential* pot, const gal_stream_config* cf
   gal_status st = stream_validate(pot, cfg);
   if (st != GAL_OK) return st;
   if (!noise || !target || !grad_params) return fail(GAL_ERR_INVALID_ARGUMENT, "NULL noise, target or gradient");
-  for (int c = 0; c < pot->n; ++c)
-    if (pot->comps[c].kind == GAL_POWERLAW_CUTOFF)  // the release-map adjoint has no third derivatives for it
-      return fail(GAL_ERR_UNSUPPORTED, "stream gradients do not support the power law with cutoff");
   const StreamLayout L = stream_layout(pot->n, *cfg, true);
   if (!workspace || workspace_bytes < L.total) return fail(GAL_ERR_WORKSPACE, "workspace too small");
   char* ws = static_cast<char*>(workspace);

@@ -3,7 +3,9 @@
 
 Forward: progenitor track, release conditions and final particle states agree
 with the oracle to 1e-9 relative (constant steps on both sides), for both
-release models (Gaussian offsets, galax's Fardal 2015 and Chen 2024 DFs). Gradient: the
+release models (Gaussian offsets, galax's Fardal 2015 and Chen 2024 DFs), for
+the Milky Way, a table and BovyMWPotential2014 (with its power law with
+cutoff). Gradient: the
 discrete adjoint of the whole pipeline (particles, tidal-radius release map,
 progenitor orbit) against central finite differences of the oracle with one
 Richardson extrapolation, 1e-6 relative for the halo mass and scale radius,
@@ -67,7 +69,10 @@ def _relmax(a, b):
 HOSTS = {
     "milky_way": O.milky_way(),
     "table": O.comps([(O.NFW, 8e11, 16.0, 0.0), (O.HERNQUIST, 3e10, 0.8, 0.0), (O.MIYAMOTO_NAGAI, 5e10, 2.5, 0.3)]),
+    # BovyMWPotential2014: Miyamoto-Nagai disk, power law with cutoff bulge, NFW halo
+    "bovy2014": O.bovy_mw_2014(),
 }
+SHAPED = (O.MIYAMOTO_NAGAI, O.POWERLAW_CUTOFF)  # components with a second shape parameter (l2)
 
 
 @pytest.mark.parametrize("df", [0, 1, 2])
@@ -83,8 +88,9 @@ def test_forward_matches_oracle(S, host, method, df):
     assert _relmax(got.final, ref["final"]) < 1e-9
 
 
-@pytest.mark.parametrize("k_ckpt,df", [(64, 0), (0, 0), (0, 1), (64, 2)])
-@pytest.mark.parametrize("host", list(HOSTS))
+@pytest.mark.parametrize("host,k_ckpt,df", [(h, k, d) for h in ("milky_way", "table")
+                                             for k, d in [(64, 0), (0, 0), (0, 1), (64, 2)]]
+                         + [("bovy2014", 64, 0), ("bovy2014", 0, 1)])
 def test_gradient_matches_finite_differences(S, host, k_ckpt, df):
     comps = HOSTS[host]
     s = _setup(comps, df=df)
@@ -95,7 +101,7 @@ def test_gradient_matches_finite_differences(S, host, k_ckpt, df):
     assert g.loss == pytest.approx(float(np.sum((ref["final"] - target) ** 2)), rel=1e-7)
     fields = ("m", "l1", "l2")
     params = [(c, f) for c in range(len(comps)) for f in fields
-              if not (f == "l2" and comps[c]["kind"] != O.MIYAMOTO_NAGAI)]
+              if not (f == "l2" and comps[c]["kind"] not in SHAPED)]
     fd1 = O.stream_fd_grad(comps, s, target, params, rel_h=1e-4)
     fd2 = O.stream_fd_grad(comps, s, target, params, rel_h=1e-5)
     for (c, f), a, b in zip(params, fd1, fd2):
@@ -104,9 +110,9 @@ def test_gradient_matches_finite_differences(S, host, k_ckpt, df):
         halo = comps[c]["kind"] == O.NFW
         tol = 1e-6 * abs(a) + (0.0 if halo else 10 * spread)
         assert abs(got - a) <= tol, (c, f, got, a, b)
-    # parameters that do not exist (l2 of spherical components) get exactly zero
+    # parameters that do not exist (l2 of the other spherical components) get exactly zero
     for c in range(len(comps)):
-        if comps[c]["kind"] != O.MIYAMOTO_NAGAI:
+        if comps[c]["kind"] not in SHAPED:
             assert g.grad_params[c][2] == 0.0
 
 

@@ -81,15 +81,17 @@ def test_weighted_training_gradient_matches_numpy(env):
         assert np.linalg.norm(got - ref) <= 3e-4 * np.linalg.norm(ref) + 1e-7, k
 
 
-def test_quantised_training_gradient_is_close_to_fp32(env):
+@pytest.mark.parametrize("B", [1000, 4096])
+def test_quantised_training_gradient_is_close_to_fp32(env, B):
     """The quantised pass (bf16 weights and activations, the products fed from
     bf16 images, the fused store phases, the two-term weight gradients) gives
     the FP32 gradient up to the bf16 rounding of its operands: a wrong image,
-    orientation or term would be off by O(1)."""
+    orientation or term would be off by O(1). B = 1000 ends in a partial
+    128-row block and a partial 64-row column-sum chunk; 4096 has several row
+    blocks and the split-K weight gradients."""
     gx, S = env
     p = _params(S, seed=5)
     rng = np.random.default_rng(17)
-    B = 4096  # several row blocks and the split-K weight gradients
     u = rng.normal(size=(B, 3)).astype(np.float32)
     pt = rng.normal(size=B).astype(np.float32)
     gt = rng.normal(size=(B, 3)).astype(np.float32)

@@ -96,6 +96,7 @@ SIGNATURES = {
                                         _DP, _I32P, _I64P, _I32P, C.c_int64, C.c_void_p]),
     "gal_set_launch": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
     "gal_set_team": (C.c_int, [C.c_int32]),
+    "gal_set_split_fraction": (C.c_int, [C.c_double]),
     "gal_set_table_lanes": (C.c_int, [C.c_int32]),
     "gal_dense_coef_per_step": (C.c_int32, [C.c_int32]),
     "gal_integrate_dense": (C.c_int, [C.c_void_p, C.POINTER(SolverConfig), _DP, _DP, _DP, C.c_int64, C.c_int64, _DP,

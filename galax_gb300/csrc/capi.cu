@@ -22,6 +22,9 @@ thread_local std::string g_last_error;
 // SMs given to four-warp teams for the longest orbits (gal_set_team); atomic
 // because calls on other threads may read it while it is set
 static std::atomic<int> g_team_blocks{32};
+// Fraction of every span the first pass of the two-pass schedule covers
+// (gal_set_split_fraction), in millionths
+static std::atomic<int> g_split_ppm{100000};
 
 // One library-owned stream per device for the team kernel, created on first use.
 static cudaError_t team_stream(cudaStream_t* out) {
@@ -265,7 +268,6 @@ gal_status validate_cfg(const gal_solver_config* c) {
 
 // ---- two-phase schedule: order parked orbits by estimated remaining work
 constexpr int kBuckets = 64;
-constexpr double kSplitFrac = 0.1;
 
 __global__ void k_sched_keys(const OrbitResume* __restrict__ r, int64_t n, unsigned* __restrict__ hist,
                              int* __restrict__ bucket) {
@@ -545,6 +547,12 @@ gal_status gal_set_team(int32_t blocks) {
   return GAL_OK;
 }
 
+gal_status gal_set_split_fraction(double fraction) {
+  if (!(fraction >= 1e-3 && fraction <= 0.9)) return fail(GAL_ERR_INVALID_ARGUMENT, "fraction must be in [0.001, 0.9]");
+  g_split_ppm.store((int)(fraction * 1e6 + 0.5), std::memory_order_relaxed);
+  return GAL_OK;
+}
+
 gal_status gal_set_table_lanes(int32_t lanes) {
   if (lanes != 0 && lanes != 1 && lanes != 32) return fail(GAL_ERR_INVALID_ARGUMENT, "lanes must be 0, 1 or 32");
   g_table_lanes.store(lanes, std::memory_order_relaxed);
@@ -627,7 +635,7 @@ gal_status gal_integrate(const gal_potential* p, const gal_solver_config* cfg, c
     e = launch();
     return e == cudaSuccess ? GAL_OK : cuda_fail(e, "integrate kernel launch");
   }
-  // two phases: first tenth of every span, then longest remaining work first
+  // two phases: a fraction of every span (a tenth by default), then longest remaining work first
   const SchedLayout L = sched_layout(n);
   auto* qlen = reinterpret_cast<unsigned long long*>(ws + 8);
   auto* hist = reinterpret_cast<unsigned*>(ws + 16);
@@ -637,7 +645,7 @@ gal_status gal_integrate(const gal_potential* p, const gal_solver_config* cfg, c
   auto* order2 = reinterpret_cast<int32_t*>(ws + L.order);
   cudaError_t e = cudaMemsetAsync(ws, 0, L.resume + sizeof(OrbitResume) * (size_t)n, s);
   if (e != cudaSuccess) return cuda_fail(e, "clearing the schedule scratch");
-  a.split_frac = kSplitFrac;
+  a.split_frac = 1e-6 * g_split_ppm.load(std::memory_order_relaxed);
   a.resume = resume;
   e = launch();
   if (e != cudaSuccess) return cuda_fail(e, "integrate kernel launch (first pass)");

@@ -257,6 +257,11 @@ GAL_API gal_status gal_set_launch(int32_t method, int32_t adaptive, int32_t bloc
  * gal_set_launch. Results are bitwise identical either way; the teams cut the
  * serial latency of the longest orbits. Process-wide. */
 GAL_API gal_status gal_set_team(int32_t blocks);
+/* Fraction of every orbit's span that the first pass of the two-pass schedule
+ * (cfg->schedule = 1) covers before the orbits are ordered by their remaining
+ * work (default 0.1, allowed [0.001, 0.9]). Results are bitwise identical for
+ * any value; it only moves work between the passes. Process-wide. */
+GAL_API gal_status gal_set_split_fraction(double fraction);
 /* Orbits per thread or warp for component tables (composites other than the
  * specialised Milky Way kernel) in gal_integrate: 1 runs one thread per orbit;
  * 32 runs one warp per orbit, its lanes splitting the components and reducing

@@ -106,6 +106,8 @@ def test_validation_without_gpu(lib):
     assert lib.gal_set_launch(8, 0, 100, 0, 0) == 1  # not a multiple of 32
     assert lib.gal_set_launch(8, 0, 128, 0, 3) == 1  # unknown register variant
     assert lib.gal_set_launch(8, 0, 256, 0, 0) == 1  # variant 0 takes at most 128 threads
+    assert lib.gal_set_split_fraction(C.c_double(0.0)) == 1 and lib.gal_set_split_fraction(C.c_double(0.95)) == 1
+    assert lib.gal_set_split_fraction(C.c_double(0.1)) == 0
 
 
 def test_python_api_rejects_unsupported_inputs():

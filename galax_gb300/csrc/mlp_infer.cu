@@ -93,14 +93,33 @@ __device__ __forceinline__ void set_abort(volatile int* abort_flag, int* err, in
 // is s = (1 + t) / 2, silu(z) = z s = hz + hz t, and silu'(z) = s + silu (1 - s)
 // with 1 - s = (1 - t) / 2. The biases and the first layer's weights are kept
 // halved in shared memory (exact), so hz comes straight out of the sums.
-struct Silu {
-  float h, d;  // silu(z), silu'(z)
+//
+// The epilogues work on two columns at a time: Blackwell's packed FP32
+// instructions (fma.rn.f32x2, mul.rn.f32x2) do two IEEE single-precision
+// operations per instruction, rounded as the scalar ones, so they issue half
+// the arithmetic instructions for the same results.
+__device__ __forceinline__ float2 f2(float x, float y) { return make_float2(x, y); }
+__device__ __forceinline__ float2 f2u(uint32_t x, uint32_t y) {
+  return make_float2(__uint_as_float(x), __uint_as_float(y));
+}
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+struct Silu2 {
+  float2 h, d;  // silu(z), silu'(z) of two columns
 };
-__device__ __forceinline__ float silu_h(float hz, float t) { return fmaf(hz, t, hz); }
-__device__ __forceinline__ Silu silu_hd(float hz) {
-  const float t = tc::tanh_approx(hz);
-  const float h = silu_h(hz, t);
-  return {h, fmaf(h, fmaf(-0.5f, t, 0.5f), fmaf(0.5f, t, 0.5f))};
+__device__ __forceinline__ float2 tanh2(float2 hz) { return f2(tc::tanh_approx(hz.x), tc::tanh_approx(hz.y)); }
+__device__ __forceinline__ float2 silu_h2(float2 hz, float2 t) { return fma2(hz, t, hz); }
+__device__ __forceinline__ Silu2 silu_hd2(float2 hz) {
+  const float2 t = tanh2(hz);
+  const float2 h = silu_h2(hz, t);
+  const float2 half = f2(0.5f, 0.5f);
+  return {h, fma2(h, fma2(f2(-0.5f, -0.5f), t, half), fma2(half, t, half))};
+}
+// layer 1 for two units from their interleaved parameters {x0, x1, y0, y1},
+// {z0, z1, w0, w1} (W1 row {x, y, z}, bias w, all halved): half the argument
+__device__ __forceinline__ float2 layer1_hz2(const float4& pxy, const float4& pzw, float2 u0, float2 u1,
+                                             float2 u2) {
+  return fma2(f2(pxy.x, pxy.y), u0, fma2(f2(pxy.z, pxy.w), u1, fma2(f2(pzw.x, pzw.y), u2, f2(pzw.z, pzw.w))));
 }
 
 // write 32 consecutive hidden units [c, c+32) of row `row` into an operand tile
@@ -134,7 +153,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
   uint8_t* tiles = smem + SMEM_A;  // [2][A_BYTES]
   uint8_t* ring = smem + SMEM_RING;
   float* sm = reinterpret_cast<float*>(smem + SMEM_SMALL);
-  const float4* sL1 = reinterpret_cast<const float4*>(sm);  // {W1 row, b1} per unit: one 16-byte load
+  // {W1 row, b1} of units 2p, 2p+1 interleaved: {x0, x1, y0, y1} at 2p, {z0, z1, w0, w1} at 2p + 1
+  const float4* sL1 = reinterpret_cast<const float4*>(sm);
   const float* sb2 = sm + 4 * H;
   const float* sb3 = sb2 + H;
   const float* sb4 = sb3 + H;
@@ -153,7 +173,11 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
 
   const int t = threadIdx.x;
   const int warp = t >> 5, lane = t & 31;
-  for (int i = t; i < SMALL_FLOATS; i += NTHREADS) sm[i] = a.small[i];
+  for (int i = t; i < SMALL_FLOATS; i += NTHREADS) {
+    int src = i;  // the first 4H floats ({W1 row, b1} per unit) are interleaved by unit pairs
+    if (i < 4 * H) src = 8 * (i >> 3) + ((i & 7) >> 1) + 4 * (i & 1);
+    sm[i] = a.small[src];
+  }
   for (int i = t; i < TILE; i += NTHREADS) ready[i] = 0;
   if (t == 0) {
     abort_s = 0;
@@ -263,17 +287,18 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
 #pragma unroll
         for (int j = 0; j < 3; ++j) u[j] = (float)(a.x[j * a.n + gi] * a.inv_length);
       }
+      const float2 u0 = f2(u[0], u[0]), u1 = f2(u[1], u[1]), u2 = f2(u[2], u[2]);
       // layer 1 on CUDA cores: h1 = silu(W1 u + b1) -> operand tile 0, half by half
       for (int h = 0; h < 2; ++h) {
         const int cbase = h * 128 + qq * 64;
         for (int c = cbase; c < cbase + 64; c += 32) {
           float v[32];
 #pragma unroll
-          for (int k = 0; k < 32; ++k) {
-            const int cc = c + k;
-            const float4 l1 = sL1[cc];  // halved
-            const float hz = fmaf(l1.x, u[0], fmaf(l1.y, u[1], fmaf(l1.z, u[2], l1.w)));
-            v[k] = silu_h(hz, tc::tanh_approx(hz));
+          for (int k = 0; k < 32; k += 2) {
+            const float2 hz = layer1_hz2(sL1[c + k], sL1[c + k + 1], u0, u1, u2);  // units c+k, c+k+1
+            const float2 hv = silu_h2(hz, tanh2(hz));
+            v[k] = hv.x;
+            v[k + 1] = hv.y;
           }
           store_row32(tiles, row, c, v);
         }
@@ -282,8 +307,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
         __syncwarp();
         if (lane == 0) tc::mbar_arrive(&op_ready[h]);
       }
-      float gpart[3] = {0.f, 0.f, 0.f};
-      float ppart = 0.f;
+      float2 gpart2[3] = {f2(0.f, 0.f), f2(0.f, 0.f), f2(0.f, 0.f)};  // even and odd columns apart
+      float2 ppart2 = f2(0.f, 0.f);
       bool ok = true;
       for (int g = 0; g < GEMMS && ok; ++g) {
         uint8_t* tile_out = tiles + (size_t)((g + 1) & 1) * A_BYTES;
@@ -316,16 +341,14 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
 #pragma unroll
               for (int k = 0; k < 32; k += 4) {
                 const float4 b4 = hb[k / 4];
-                const Silu r0 = silu_hd(fmaf(0.5f, __uint_as_float(acc[k]), b4.x));
-                const Silu r1 = silu_hd(fmaf(0.5f, __uint_as_float(acc[k + 1]), b4.y));
-                const Silu r2 = silu_hd(fmaf(0.5f, __uint_as_float(acc[k + 2]), b4.z));
-                const Silu r3 = silu_hd(fmaf(0.5f, __uint_as_float(acc[k + 3]), b4.w));
-                v[k] = r0.h;
-                v[k + 1] = r1.h;
-                v[k + 2] = r2.h;
-                v[k + 3] = r3.h;
-                spk[k / 2] = tc::pack_bf16x2(r0.d, r1.d);
-                spk[k / 2 + 1] = tc::pack_bf16x2(r2.d, r3.d);
+                const Silu2 r0 = silu_hd2(fma2(f2(0.5f, 0.5f), f2u(acc[k], acc[k + 1]), f2(b4.x, b4.y)));
+                const Silu2 r1 = silu_hd2(fma2(f2(0.5f, 0.5f), f2u(acc[k + 2], acc[k + 3]), f2(b4.z, b4.w)));
+                v[k] = r0.h.x;
+                v[k + 1] = r0.h.y;
+                v[k + 2] = r1.h.x;
+                v[k + 3] = r1.h.y;
+                spk[k / 2] = tc::pack_bf16x2(r0.d.x, r0.d.y);
+                spk[k / 2 + 1] = tc::pack_bf16x2(r1.d.x, r1.d.y);
               }
               tc::tmem_st16(tmem + lane_base + (uint32_t)((g == 0 ? COL_S2 : COL_S3) + cc0 / 2), spk);
               store_row32(tile_out, row, cc0, v);
@@ -335,32 +358,36 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
 #pragma unroll
               for (int k = 0; k < 32; k += 4) {
                 const float4 b4 = hb[k / 4], w4 = w5[k / 4];
-                const float bq[4] = {b4.x, b4.y, b4.z, b4.w}, wq[4] = {w4.x, w4.y, w4.z, w4.w};
-#pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                  const Silu r = silu_hd(fmaf(0.5f, __uint_as_float(acc[k + j]), bq[j]));
-                  ppart = fmaf(r.h, wq[j], ppart);
-                  v[k + j] = r.d * wq[j];
-                }
+                const float2 wa = f2(w4.x, w4.y), wb = f2(w4.z, w4.w);
+                const Silu2 r0 = silu_hd2(fma2(f2(0.5f, 0.5f), f2u(acc[k], acc[k + 1]), f2(b4.x, b4.y)));
+                const Silu2 r1 = silu_hd2(fma2(f2(0.5f, 0.5f), f2u(acc[k + 2], acc[k + 3]), f2(b4.z, b4.w)));
+                ppart2 = fma2(r0.h, wa, ppart2);
+                ppart2 = fma2(r1.h, wb, ppart2);
+                const float2 d0 = mul2(r0.d, wa), d1 = mul2(r1.d, wb);
+                v[k] = d0.x;
+                v[k + 1] = d0.y;
+                v[k + 2] = d1.x;
+                v[k + 3] = d1.y;
               }
               store_row32(tile_out, row, cc0, v);
             } else if (g <= 4) {  // u3 / u2: d = silu'(z) u -> operand tile
 #pragma unroll
               for (int k = 0; k < 32; k += 2) {
-                v[k] = tc::bf16_lo(sp[k / 2]) * __uint_as_float(acc[k]);
-                v[k + 1] = tc::bf16_hi(sp[k / 2]) * __uint_as_float(acc[k + 1]);
+                const float2 d = mul2(f2(tc::bf16_lo(sp[k / 2]), tc::bf16_hi(sp[k / 2])), f2u(acc[k], acc[k + 1]));
+                v[k] = d.x;
+                v[k + 1] = d.y;
               }
               store_row32(tile_out, row, cc0, v);
             } else {  // u1: grad_u out = sum_c silu'(z1_c) u1_c W1[c]
 #pragma unroll
-              for (int k = 0; k < 32; ++k) {
-                const int cc = cc0 + k;
-                const float4 l1 = sL1[cc];  // halved: gpart is half the sum, doubled at the end
-                const float hz = fmaf(l1.x, u[0], fmaf(l1.y, u[1], fmaf(l1.z, u[2], l1.w)));
-                const float d1 = silu_hd(hz).d * __uint_as_float(acc[k]);
-                gpart[0] = fmaf(d1, l1.x, gpart[0]);
-                gpart[1] = fmaf(d1, l1.y, gpart[1]);
-                gpart[2] = fmaf(d1, l1.z, gpart[2]);
+              for (int k = 0; k < 32; k += 2) {
+                // units cc0+k, cc0+k+1; W1 halved: gpart is half the sum, doubled at the end
+                const float4 pxy = sL1[cc0 + k], pzw = sL1[cc0 + k + 1];
+                const float2 hz = layer1_hz2(pxy, pzw, u0, u1, u2);
+                const float2 d1 = mul2(silu_hd2(hz).d, f2u(acc[k], acc[k + 1]));
+                gpart2[0] = fma2(d1, f2(pxy.x, pxy.y), gpart2[0]);
+                gpart2[1] = fma2(d1, f2(pxy.z, pxy.w), gpart2[1]);
+                gpart2[2] = fma2(d1, f2(pzw.x, pzw.y), gpart2[2]);
               }
             }
           }
@@ -374,6 +401,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
         }
       }
       if (!ok) break;
+      const float gpart[3] = {gpart2[0].x + gpart2[0].y, gpart2[1].x + gpart2[1].y, gpart2[2].x + gpart2[2].y};
+      const float ppart = ppart2.x + ppart2.y;
       // combine the two column quarters of each row (bounded hand-off through shared memory)
       if (qq == 1) {
         part[row * 4 + 0] = gpart[0];

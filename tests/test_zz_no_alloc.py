@@ -96,6 +96,47 @@ def test_noalloc_matches_workspace_path_on_consecutive_calls(env, schedule):
         np.testing.assert_array_equal(got[0], ref[0])
 
 
+def test_noalloc_replays_from_a_cuda_graph(env):
+    """Captured once into a CUDA graph (the use this entry point is made for),
+    the two-pass schedule with its team fork/join replays to the workspace
+    path's result bitwise, replay after replay."""
+    import torch
+
+    gx, _lib, L = env
+    mw = gx.MilkyWayPotential()
+    cfg = gx.Integrator(solver=gx.Dopri5(), stepsize_controller=gx.PIDController(rtol=1e-8, atol=1e-10),
+                        max_steps=2**16, schedule=True).config()
+    n = 2500
+    inputs = _device_inputs(_batch(n, 13))
+    ref = _run(L, _lib, mw, cfg, inputs, n, noalloc=False)
+    y0, t0, t1, offs, ts = inputs
+    total = ts.numel()
+    out = torch.empty((6, total), dtype=torch.float64, device="cuda")
+    status = torch.empty((n,), dtype=torch.int32, device="cuda")
+    steps = torch.empty((n,), dtype=torch.int64, device="cuda")
+
+    def call(stream):
+        return L.gal_integrate_noalloc(mw.handle(), C.byref(cfg), y0.data_ptr(), t0.data_ptr(), t1.data_ptr(),
+                                       offs.data_ptr(), ts.data_ptr(), total, out.data_ptr(), status.data_ptr(),
+                                       steps.data_ptr(), None, n, stream)
+
+    _lib.check(call(torch.cuda.current_stream().cuda_stream), "gal_integrate_noalloc (eager)")
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        rc = call(torch.cuda.current_stream().cuda_stream)
+    _lib.check(rc, "gal_integrate_noalloc (captured)")
+    for _ in range(2):
+        out.fill_(-1.0)
+        status.fill_(-1)
+        steps.fill_(-1)
+        g.replay()
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(status.cpu().numpy(), ref[1])
+        np.testing.assert_array_equal(steps.cpu().numpy(), ref[2])
+        np.testing.assert_array_equal(out.cpu().numpy(), ref[0])
+
+
 def test_noalloc_rejects_calls_beyond_its_scratch(env):
     gx, _lib, L = env
     mw = gx.MilkyWayPotential()

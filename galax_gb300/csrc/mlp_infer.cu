@@ -15,7 +15,9 @@
 // the epilogue of one half overlaps the tensor cores' work on the other, and
 // two operand tiles alternate so that an epilogue writes the next product's
 // operand while the current one is still read. The next product starts on K
-// 0..127 once the epilogue of half 0 has written those columns. Weights stream
+// 0..127 once the epilogue of half 0 has written those columns. A tile's layer
+// 1 is computed while the tensor cores run the previous tile's last product,
+// so its first product follows that product's epilogue directly. Weights stream
 // through a ring of 16 KB N-halves of K-blocks (bulk copies from pre-swizzled
 // global images) run by their own warp ahead of the products. The numerics
 // are those of the training kernels' quantised forward/backward (mlp_train.cu).
@@ -277,18 +279,23 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
     const int qq = e >= 4 ? 1 : 0;  // which 64-column quarter of each half
     const uint32_t lane_base = (uint32_t)(quad * 32) << 16;
     int64_t q = 0;  // acc_full phases
-    for (int64_t it = 0; it < my_tiles; ++it) {
-      if (*abort_flag) break;
-      const int64_t tile = blockIdx.x + it * gridDim.x;
-      const int64_t gi = tile * TILE + row;
-      const bool valid = gi < a.n;
-      float u[3] = {0.f, 0.f, 0.f};
-      if (valid) {
+    // network input of this thread's point of tile `it` (zero past the end)
+    auto load_u = [&](int64_t it, float (&u)[3]) {
+      const int64_t gi = (blockIdx.x + it * gridDim.x) * TILE + row;
 #pragma unroll
-        for (int j = 0; j < 3; ++j) u[j] = (float)(a.x[j * a.n + gi] * a.inv_length);
-      }
+      for (int j = 0; j < 3; ++j) u[j] = gi < a.n ? (float)(a.x[j * a.n + gi] * a.inv_length) : 0.f;
+    };
+    // operand half h written and accumulator half h drained: one arrival per warp
+    auto signal = [&](int h) {
+      tc::fence_proxy_async_smem();
+      tc::tc_fence_before();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&op_ready[h]);
+    };
+    // layer 1 on CUDA cores: h1 = silu(W1 u + b1) -> operand tile 0, this thread's columns of
+    // both halves; with `each`, every half is signalled as soon as it is written
+    auto layer1 = [&](const float (&u)[3], bool each) {
       const float2 u0 = f2(u[0], u[0]), u1 = f2(u[1], u[1]), u2 = f2(u[2], u[2]);
-      // layer 1 on CUDA cores: h1 = silu(W1 u + b1) -> operand tile 0, half by half
       for (int h = 0; h < 2; ++h) {
         const int cbase = h * 128 + qq * 64;
         for (int c = cbase; c < cbase + 64; c += 32) {
@@ -302,17 +309,33 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
           }
           store_row32(tiles, row, c, v);
         }
-        tc::fence_proxy_async_smem();
-        tc::tc_fence_before();
-        __syncwarp();
-        if (lane == 0) tc::mbar_arrive(&op_ready[h]);
+        if (each) signal(h);
       }
+    };
+    // The first tile's layer 1 runs here; every later tile's runs while the tensor cores
+    // work on the previous tile's last product (operand tile 0 is free once product 4 has
+    // completed), so the next tile's first product starts as soon as that product's
+    // epilogue has drained the accumulator.
+    float u[3] = {0.f, 0.f, 0.f}, un[3] = {0.f, 0.f, 0.f};
+    if (my_tiles > 0) {
+      load_u(0, u);
+      layer1(u, true);
+    }
+    for (int64_t it = 0; it < my_tiles; ++it) {
+      if (*abort_flag) break;
+      const int64_t tile = blockIdx.x + it * gridDim.x;
+      const int64_t gi = tile * TILE + row;
+      const bool valid = gi < a.n;
+      const bool has_next = it + 1 < my_tiles;
+      if (has_next) load_u(it + 1, un);
+      const float2 u0 = f2(u[0], u[0]), u1 = f2(u[1], u[1]), u2 = f2(u[2], u[2]);
       float2 gpart2[3] = {f2(0.f, 0.f), f2(0.f, 0.f), f2(0.f, 0.f)};  // even and odd columns apart
       float2 ppart2 = f2(0.f, 0.f);
       bool ok = true;
       for (int g = 0; g < GEMMS && ok; ++g) {
         uint8_t* tile_out = tiles + (size_t)((g + 1) & 1) * A_BYTES;
         for (int h = 0; h < 2; ++h, ++q) {
+          if (g == GEMMS - 1 && h == 0 && has_next) layer1(un, false);  // the next tile's, unsignalled
           if (!wait_bar(&acc_full[h], (uint32_t)((q >> 1) & 1), abort_flag)) {
             if (!*abort_flag) set_abort(abort_flag, a.err, 2);
             ok = false;
@@ -392,12 +415,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
             }
           }
           if (g <= 1) tc::tmem_wait_st();
-          if (g < GEMMS - 1) {  // this half of the next operand written, this half of the accumulator drained
-            tc::fence_proxy_async_smem();
-            tc::tc_fence_before();
-            __syncwarp();
-            if (lane == 0) tc::mbar_arrive(&op_ready[h]);
-          }
+          // this half of the next operand (the next product's, or the next tile's layer 1)
+          // written, this half of the accumulator drained
+          if (g < GEMMS - 1 || has_next) signal(h);
         }
       }
       if (!ok) break;
@@ -428,6 +448,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
           if (a.phi) a.phi[gi] = a.pscale * (double)(ppart + part[row * 4 + 3] + sw5[H]);
         }
       }
+#pragma unroll
+      for (int j = 0; j < 3; ++j) u[j] = un[j];
     }
   }
   tc::tc_fence_before();

@@ -332,7 +332,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
       float2 gpart2[3] = {f2(0.f, 0.f), f2(0.f, 0.f), f2(0.f, 0.f)};  // even and odd columns apart
       float2 ppart2 = f2(0.f, 0.f);
       bool ok = true;
-      for (int g = 0; g < GEMMS && ok; ++g) {
+#pragma unroll
+      for (int g = 0; g < GEMMS; ++g) {
+        if (!ok) break;
         uint8_t* tile_out = tiles + (size_t)((g + 1) & 1) * A_BYTES;
         for (int h = 0; h < 2; ++h, ++q) {
           if (g == GEMMS - 1 && h == 0 && has_next) layer1(un, false);  // the next tile's, unsignalled

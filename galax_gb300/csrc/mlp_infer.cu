@@ -336,6 +336,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
       for (int g = 0; g < GEMMS; ++g) {
         if (!ok) break;
         uint8_t* tile_out = tiles + (size_t)((g + 1) & 1) * A_BYTES;
+#pragma unroll
         for (int h = 0; h < 2; ++h, ++q) {
           if (g == GEMMS - 1 && h == 0 && has_next) layer1(un, false);  // the next tile's, unsignalled
           if (!wait_bar(&acc_full[h], (uint32_t)((q >> 1) & 1), abort_flag)) {

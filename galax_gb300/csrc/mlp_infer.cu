@@ -61,7 +61,7 @@ constexpr uint32_t WAIT_LIMIT = 1u << 24;
 constexpr uint32_t TMEM_COLS = 512;
 constexpr uint32_t COL_S2 = 256, COL_S3 = 384;          // packed silu'(z2), silu'(z3)
 static_assert(SMEM_ALLOC <= 227 * 1024, "shared memory budget");
-static_assert(2 * STAGES + 5 <= 32, "barriers fit their 256 bytes");
+static_assert(2 * STAGES + 7 <= 32, "barriers fit their 256 bytes");
 
 struct InferArgs {
   const double* x;       // [3][n]
@@ -167,8 +167,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
   uint64_t* full = bars;
   uint64_t* empty = bars + STAGES;
   uint64_t* acc_full = bars + 2 * STAGES;  // [2]
-  uint64_t* op_ready = acc_full + 2;       // [2]
-  uint64_t* drain = op_ready + 2;
+  uint64_t* op_ready = acc_full + 2;       // [2 halves][2 sub-chunks]
+  uint64_t* drain = op_ready + 4;
   uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(drain + 1);
   __shared__ int abort_s;
   volatile int* abort_flag = &abort_s;
@@ -187,10 +187,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
       tc::mbar_init(&full[s], 1);
       tc::mbar_init(&empty[s], 1);
     }
-    for (int h = 0; h < 2; ++h) {
-      tc::mbar_init(&acc_full[h], 1);
-      tc::mbar_init(&op_ready[h], EPI_WARPS);
-    }
+    for (int h = 0; h < 2; ++h) tc::mbar_init(&acc_full[h], 1);
+    for (int c = 0; c < 4; ++c) tc::mbar_init(&op_ready[c], EPI_WARPS);
     tc::mbar_init(drain, 1);
     tc::fence_barrier_init();
   }
@@ -251,16 +249,39 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
         }
         return true;
       };
+      // N half 0 over one half oh of K (K-blocks 2 oh, 2 oh + 1: ring entries j, j + 1), in two
+      // steps of two K slices each as the epilogue writes the operand's sub-chunks
+      // (op_ready[2 oh + c]: columns 128 oh + 64 qq + 32 c .. + 31 of both column quarters qq)
+      auto half0 = [&](uint32_t a_base, int oh) -> bool {
+        for (int d = 0; d < 2; ++d) {
+          const int64_t jj = j + d;
+          if (!wait_bar(&full[jj % STAGES], (uint32_t)((jj / STAGES) & 1), abort_flag)) return false;
+        }
+        for (int c = 0; c < 2; ++c) {
+          if (!wait_bar(&op_ready[2 * oh + c], (uint32_t)(q & 1), abort_flag)) return false;
+          tc::tc_fence_after();
+#pragma unroll
+          for (int d = 0; d < 2; ++d) {
+            const int kb = 2 * oh + d;
+            const uint32_t b_base = tc::smem_u32(ring + (size_t)((j + d) % STAGES) * HALF_BYTES);
+#pragma unroll
+            for (int ks = 2 * c; ks < 2 * c + 2; ++ks) {
+              const uint64_t ad = tc::desc_sw128(a_base + kb * (TILE * 128) + ks * 32);
+              const uint64_t bd = tc::desc_sw128(b_base + ks * 32);
+              tc::mma_bf16(tmem, ad, bd, idesc, (kb | ks) != 0);
+            }
+          }
+        }
+        tc::mma_commit(&empty[j % STAGES]);  // both stages free once these products complete
+        tc::mma_commit(&empty[(j + 1) % STAGES]);
+        j += 2;
+        return true;
+      };
       for (int64_t it = 0; it < my_tiles && ok; ++it) {
         for (int g = 0; g < GEMMS && ok; ++g, ++q) {
           const uint32_t a_base = tc::smem_u32(tiles + (size_t)(g & 1) * A_BYTES);
-          // half 0 over K 0..127 as soon as the first half of the operand is written
-          if (!wait_bar(&op_ready[0], (uint32_t)(q & 1), abort_flag)) { ok = false; break; }
-          tc::tc_fence_after();
-          if (!run_blocks(a_base, 0, 0, 2)) { ok = false; break; }
-          if (!wait_bar(&op_ready[1], (uint32_t)(q & 1), abort_flag)) { ok = false; break; }
-          tc::tc_fence_after();
-          if (!run_blocks(a_base, 0, 2, 4)) { ok = false; break; }
+          // N half 0 slice by slice as the operand is written, then N half 1 over all of K
+          if (!half0(a_base, 0) || !half0(a_base, 1)) { ok = false; break; }
           tc::mma_commit(&acc_full[0]);
           if (!run_blocks(a_base, 1, 0, 4)) { ok = false; break; }
           tc::mma_commit(&acc_full[1]);
@@ -285,12 +306,13 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
 #pragma unroll
       for (int j = 0; j < 3; ++j) u[j] = gi < a.n ? (float)(a.x[j * a.n + gi] * a.inv_length) : 0.f;
     };
-    // operand half h written and accumulator half h drained: one arrival per warp
-    auto signal = [&](int h) {
+    // sub-chunk c (this thread's columns 32 c .. 32 c + 31) of operand half h written and
+    // accumulator half h drained: one arrival per warp
+    auto signal = [&](int h, int c) {
       tc::fence_proxy_async_smem();
       tc::tc_fence_before();
       __syncwarp();
-      if (lane == 0) tc::mbar_arrive(&op_ready[h]);
+      if (lane == 0) tc::mbar_arrive(&op_ready[2 * h + c]);
     };
     // layer 1 on CUDA cores: h1 = silu(W1 u + b1) -> operand tile 0, this thread's columns of
     // both halves; with `each`, every half is signalled as soon as it is written
@@ -308,8 +330,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
             v[k + 1] = hv.y;
           }
           store_row32(tiles, row, c, v);
+          if (each) signal(h, (c - cbase) >> 5);
         }
-        if (each) signal(h);
       }
     };
     // The first tile's layer 1 runs here; every later tile's runs while the tensor cores
@@ -355,6 +377,12 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
             tc::tmem_ld16(tmem + lane_base + cs + 16, sp1);
           }
           tc::tmem_wait_ld();
+          // the last product: the next tile's operand (its layer 1) is written already, so its
+          // first product may start as soon as this half of the accumulator is drained
+          if (g == GEMMS - 1 && has_next) {
+            signal(h, 0);
+            signal(h, 1);
+          }
 #pragma unroll
           for (int half = 0; half < 2; ++half) {
             const uint32_t(&acc)[32] = half ? acc1 : acc0;
@@ -416,11 +444,11 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
                 gpart2[2] = fma2(d1, f2(pzw.x, pzw.y), gpart2[2]);
               }
             }
+            // this sub-chunk of the next product's operand written (the accumulator half was
+            // drained by the loads above): the product warp may issue its K slices
+            if (g < GEMMS - 1) signal(h, half);
           }
           if (g <= 1) tc::tmem_wait_st();
-          // this half of the next operand (the next product's, or the next tile's layer 1)
-          // written, this half of the accumulator drained
-          if (g < GEMMS - 1 || has_next) signal(h);
         }
       }
       if (!ok) break;

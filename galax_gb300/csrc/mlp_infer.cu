@@ -377,6 +377,12 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
             tc::tmem_ld16(tmem + lane_base + cs + 16, sp1);
           }
           tc::tmem_wait_ld();
+          tc::tmem_regs_after_wait(acc0);
+          tc::tmem_regs_after_wait(acc1);
+          if (g == 3 || g == 4) {
+            tc::tmem_regs_after_wait(sp0);
+            tc::tmem_regs_after_wait(sp1);
+          }
           // the last product: the next tile's operand (its layer 1) is written already, so its
           // first product may start as soon as this half of the accumulator is drained
           if (g == GEMMS - 1 && has_next) {

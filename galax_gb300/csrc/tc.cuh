@@ -153,6 +153,16 @@ __device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t (&r)[16
 }
 
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+// The registers of a tcgen05.ld hold their values only once tcgen05.wait::ld has
+// returned. To the compiler they are defined by the load's asm statement, so
+// each is passed through an empty volatile asm after the wait: volatile asm
+// statements keep their order, so no use of the registers can be scheduled
+// above the wait.
+template <int N>
+__device__ __forceinline__ void tmem_regs_after_wait(uint32_t (&r)[N]) {
+#pragma unroll
+  for (int i = 0; i < N; ++i) asm volatile("" : "+r"(r[i]));
+}
 __device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
 // K-major, 128-byte-swizzled operand: rows 128 bytes apart, 8-row groups 1024 bytes apart.

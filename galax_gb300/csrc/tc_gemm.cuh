@@ -502,6 +502,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_tc_gemm(Args a) {
       if (committed > 0) {
         tc::tmem_ld32(tmem + lane_base + (uint32_t)c, r);
         tc::tmem_wait_ld();
+        tc::tmem_regs_after_wait(r);
       } else {
 #pragma unroll
         for (int j = 0; j < 32; ++j) r[j] = 0u;

@@ -42,8 +42,11 @@ def set_launch(method: int, adaptive: bool, block: int, per_sm: int, variant: in
 
 
 # SMs given to four-warp teams for the longest orbits (second pass of a
-# two-pass Dopri5 Milky Way batch, gal_set_team)
-DEFAULT_TEAMS = (16, 32, 48)
+# two-pass Dopri5 Milky Way batch, gal_set_team). On the 262,144-orbit
+# headline batch the step time has a narrow minimum (ms: 24 -> 1,253,
+# 28 -> 1,171, 30 -> 1,172, 32 -> 1,183, 36 -> 1,211, 40 -> 1,241), so the
+# candidates are spaced closely around it.
+DEFAULT_TEAMS = (24, 28, 32, 40)
 
 
 def set_team(blocks: int) -> None:

@@ -461,6 +461,7 @@ def run_uneven_dopri8(steps: int = 2, warmup: int = 1) -> dict:
         return integrate(mw, y0, t0, t1, sts, cfg, save_offsets=offs, order=order, soa=True, workspace=ws)
 
     L = _lib.load()
+    _lib.check(L.gal_set_split_fraction(0.1), "gal_set_split_fraction")  # the library's default
     res = {}
     for team in (32, 0):
         _lib.check(L.gal_set_team(team), "gal_set_team")

@@ -54,6 +54,19 @@ def set_team(blocks: int) -> None:
     _lib.check(L.gal_set_team(int(blocks)), "gal_set_team")
 
 
+# Fraction of every orbit's span covered by the first pass of the two-pass
+# schedule (gal_set_split_fraction; the library's default is 0.1). The first
+# pass's progress is what orders the second pass longest first: too short a
+# first pass misorders the longest orbits (headline batch, 28 team SMs, ms:
+# 0.06 -> 1,243-1,251, 0.08 -> 1,156, 0.1 -> 1,171, 0.13 -> 1,192).
+DEFAULT_SPLITS = (0.08, 0.1, 0.12)
+
+
+def set_split_fraction(frac: float) -> None:
+    L = _lib.load()
+    _lib.check(L.gal_set_split_fraction(float(frac)), "gal_set_split_fraction")
+
+
 def _worst_ms(run: Callable[[], object], repeats: int) -> float:
     import torch
 
@@ -72,10 +85,11 @@ def _worst_ms(run: Callable[[], object], repeats: int) -> float:
 
 def tune(run: Callable[[], object], method: int, adaptive: bool,
          candidates: Iterable[tuple[int, int, int]] = DEFAULT_CANDIDATES, repeats: int = 2,
-         teams: Iterable[int] = DEFAULT_TEAMS) -> dict:
+         teams: Iterable[int] = DEFAULT_TEAMS, splits: Iterable[float] = DEFAULT_SPLITS) -> dict:
     """Run ``run()`` under each launch-shape candidate ``repeats`` times and keep
     the one whose slowest run is fastest; then, for adaptive Dopri5, the same
-    over the number of SMs given to four-warp teams. Returns the timings."""
+    over the number of SMs given to four-warp teams and, with the best of those,
+    over the first pass's split fraction. Returns the timings."""
     timings = {}
     for cand in candidates:
         set_launch(method, adaptive, *cand)
@@ -93,4 +107,13 @@ def tune(run: Callable[[], object], method: int, adaptive: bool,
         set_team(tbest)
         out["best"]["team_blocks"] = tbest
         out["team_ms"] = {str(k): round(v, 3) for k, v in tt.items()}
+        if splits:
+            sp = {}
+            for frac in splits:
+                set_split_fraction(frac)
+                sp[frac] = _worst_ms(run, repeats)
+            fbest = min(sp, key=sp.get)
+            set_split_fraction(fbest)
+            out["best"]["split_fraction"] = fbest
+            out["split_ms"] = {str(k): round(v, 3) for k, v in sp.items()}
     return out

@@ -436,7 +436,8 @@ def _sensitivity(b, idx, per_orbit, saves_o, starts, lens, tol, n_control: int =
 def run_uneven_dopri8(steps: int = 2, warmup: int = 1) -> dict:
     """The headline batch (262,144 uneven orbits, PID rtol 1e-8 atol 1e-10) with
     Dopri8, galax's default method, with the longest orbits on four-warp teams
-    (the library's default) and, once, without them."""
+    (team SM count and split fraction picked by the autotuner, launch shape the
+    library's) and, once, without them."""
     import torch
 
     import galax_gb300 as gx
@@ -460,23 +461,29 @@ def run_uneven_dopri8(steps: int = 2, warmup: int = 1) -> dict:
         order = torch.argsort((t1 - t0).abs() * torch.sqrt(a / r), descending=True).to(torch.int32)
         return integrate(mw, y0, t0, t1, sts, cfg, save_offsets=offs, order=order, soa=True, workspace=ws)
 
+    from galax_gb300.autotune import tune
+
     L = _lib.load()
-    _lib.check(L.gal_set_split_fraction(0.1), "gal_set_split_fraction")  # the library's default
+    step()  # first call: lazy set-up outside any measurement
+    torch.cuda.synchronize()
+    tuning = tune(step, 8, True, candidates=())
+    team = tuning["best"]["team_blocks"]
     res = {}
-    for team in (32, 0):
-        _lib.check(L.gal_set_team(team), "gal_set_team")
+    for blocks in (team, 0):
+        _lib.check(L.gal_set_team(blocks), "gal_set_team")
         for _ in range(warmup):
             _, st, acc = step()
-        ms = _timed(step, steps if team else 1, stream)
-        res[team] = (ms, int(acc.sum()), int((st != 0).sum()))
-    _lib.check(L.gal_set_team(32), "gal_set_team")
-    ms, accepted, bad = res[32]
+        ms = _timed(step, steps if blocks else 1, stream)
+        res[blocks] = (ms, int(acc.sum()), int((st != 0).sum()))
+    _lib.check(L.gal_set_team(32), "gal_set_team")  # the library's defaults again
+    _lib.check(L.gal_set_split_fraction(0.1), "gal_set_split_fraction")
+    ms, accepted, bad = res[team]
     peak = fp64_peak()
     achieved = accepted * STEP_FLOPS_MW[8] / (ms * 1e-3) / 1e12
     return {"metric": "orbit-steps/s", "value": accepted / (ms * 1e-3), "unit": "orbit-steps/s",
             "ms_per_step": ms, "steps": steps, "warmup": warmup,
             "config": {"workload": WORKLOADS["uneven"].replace("Dopri5", "Dopri8"), "accepted_steps": accepted,
-                       "orbits_not_finished": bad},
+                       "orbits_not_finished": bad, "autotune": tuning},
             "without_teams": {"ms_per_step": res[0][0], "value": res[0][1] / (res[0][0] * 1e-3)},
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak["tflops"], "unit": "TFLOP/s",
                      "issue_ceiling": peak["issue_ceiling_tflops"],

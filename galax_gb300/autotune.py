@@ -42,11 +42,12 @@ def set_launch(method: int, adaptive: bool, block: int, per_sm: int, variant: in
 
 
 # SMs given to four-warp teams for the longest orbits (second pass of a
-# two-pass Dopri5 Milky Way batch, gal_set_team). On the 262,144-orbit
-# headline batch the step time has a narrow minimum (ms: 24 -> 1,253,
-# 28 -> 1,171, 30 -> 1,172, 32 -> 1,183, 36 -> 1,211, 40 -> 1,241), so the
-# candidates are spaced closely around it.
-DEFAULT_TEAMS = (24, 28, 32, 40)
+# two-pass adaptive Milky Way batch, gal_set_team), per method. On the
+# 262,144-orbit headline batch the step time has a narrow minimum, so the
+# candidates are spaced closely around it (ms, Dopri5: 24 -> 1,253,
+# 28 -> 1,171, 30 -> 1,172, 32 -> 1,183, 36 -> 1,211, 40 -> 1,241; Dopri8:
+# 24 -> 1,551, 28 -> 1,579, 32 -> 1,609, 40 -> 1,680).
+DEFAULT_TEAMS = {5: (24, 28, 32, 40), 8: (16, 20, 24, 28, 32)}
 
 
 def set_team(blocks: int) -> None:
@@ -85,20 +86,25 @@ def _worst_ms(run: Callable[[], object], repeats: int) -> float:
 
 def tune(run: Callable[[], object], method: int, adaptive: bool,
          candidates: Iterable[tuple[int, int, int]] = DEFAULT_CANDIDATES, repeats: int = 2,
-         teams: Iterable[int] = DEFAULT_TEAMS, splits: Iterable[float] = DEFAULT_SPLITS) -> dict:
+         teams: Iterable[int] | None = None, splits: Iterable[float] = DEFAULT_SPLITS) -> dict:
     """Run ``run()`` under each launch-shape candidate ``repeats`` times and keep
-    the one whose slowest run is fastest; then, for adaptive Dopri5, the same
-    over the number of SMs given to four-warp teams and, with the best of those,
-    over the first pass's split fraction. Returns the timings."""
+    the one whose slowest run is fastest (no candidates: the shape is left as
+    it is); then, for adaptive batches, the same over the number of SMs given to
+    four-warp teams (``teams``, by default the method's candidates) and, with the
+    best of those, over the first pass's split fraction. Returns the timings."""
     timings = {}
     for cand in candidates:
         set_launch(method, adaptive, *cand)
         timings[cand] = _worst_ms(run, repeats)
-    best = min(timings, key=timings.get)
-    set_launch(method, adaptive, *best)
-    out = {"best": {"block_threads": best[0], "blocks_per_sm": best[1], "variant": best[2]},
-           "ms": {f"{b}x{s}v{v}": round(t, 3) for (b, s, v), t in timings.items()}}
-    if method == 5 and adaptive and teams:
+    out = {"best": {}, "ms": {}}
+    if timings:
+        best = min(timings, key=timings.get)
+        set_launch(method, adaptive, *best)
+        out = {"best": {"block_threads": best[0], "blocks_per_sm": best[1], "variant": best[2]},
+               "ms": {f"{b}x{s}v{v}": round(t, 3) for (b, s, v), t in timings.items()}}
+    if teams is None:
+        teams = DEFAULT_TEAMS.get(method, ()) if adaptive else ()
+    if adaptive and teams:
         tt = {}
         for blocks in teams:
             set_team(blocks)

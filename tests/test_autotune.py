@@ -16,7 +16,7 @@ def fake(monkeypatch):
     state = {"launch": None, "team": None, "split": None, "calls": []}
     # step time as a function of the current settings (ms); two runs each, the second slower
     launch_ms = {(128, 1, 2): 1200.0, (64, 2, 2): 1190.0, (128, 0, 0): 1300.0}
-    team_ms = {24: 40.0, 28: 0.0, 32: 10.0, 40: 60.0}
+    team_ms = {16: 80.0, 20: 50.0, 24: 40.0, 28: 0.0, 32: 10.0, 40: 60.0}
     split_ms = {0.08: -15.0, 0.1: 0.0, 0.12: 20.0}
 
     def set_launch(method, adaptive, block, per_sm, variant):
@@ -50,7 +50,7 @@ def test_adaptive_dopri5_tunes_shape_then_teams_then_split(fake):
     assert out["best"] == {"block_threads": 64, "blocks_per_sm": 2, "variant": 2, "team_blocks": 28,
                            "split_fraction": 0.08}
     assert state["launch"] == (64, 2, 2) and state["team"] == 28 and state["split"] == 0.08
-    assert set(out["team_ms"]) == {str(t) for t in A.DEFAULT_TEAMS}
+    assert set(out["team_ms"]) == {str(t) for t in A.DEFAULT_TEAMS[5]}
     assert set(out["split_ms"]) == {str(f) for f in A.DEFAULT_SPLITS}
     # the split fraction is tuned with the chosen team count in place
     kinds = [c[0] for c in state["calls"]]
@@ -58,11 +58,21 @@ def test_adaptive_dopri5_tunes_shape_then_teams_then_split(fake):
     assert state["calls"][last_team] == ("team", 28) and kinds.index("split") > last_team
 
 
-def test_other_methods_tune_the_launch_shape_only(fake):
+def test_fixed_step_batches_tune_the_launch_shape_only(fake):
     A, state, cands = fake
-    for method, adaptive in ((8, True), (5, False)):
+    for method in (5, 8):
         state["calls"].clear()
-        out = A.tune(lambda: None, method, adaptive, candidates=cands)
+        out = A.tune(lambda: None, method, False, candidates=cands)
         assert set(out["best"]) == {"block_threads", "blocks_per_sm", "variant"}
         assert "team_ms" not in out and "split_ms" not in out
         assert all(c[0] == "launch" for c in state["calls"])
+
+
+def test_adaptive_dopri8_teams_without_shape_candidates(fake):
+    A, state, _ = fake
+    state["launch"] = (128, 1, 2)  # left as it is
+    out = A.tune(lambda: None, 8, True, candidates=())
+    assert out["ms"] == {} and "block_threads" not in out["best"]
+    assert set(out["team_ms"]) == {str(t) for t in A.DEFAULT_TEAMS[8]}
+    assert out["best"]["team_blocks"] == 28 and state["team"] == 28 and state["launch"] == (128, 1, 2)
+    assert all(c[0] != "launch" for c in state["calls"])

@@ -16,7 +16,7 @@ def fake(monkeypatch):
     state = {"launch": None, "team": None, "split": None, "calls": []}
     # step time as a function of the current settings (ms); two runs each, the second slower
     launch_ms = {(128, 1, 2): 1200.0, (64, 2, 2): 1190.0, (128, 0, 0): 1300.0}
-    team_ms = {16: 80.0, 20: 50.0, 24: 40.0, 28: 0.0, 32: 10.0, 40: 60.0}
+    team_ms = {8: 90.0, 12: 30.0, 16: 80.0, 20: 50.0, 24: 40.0, 28: 0.0, 32: 10.0, 40: 60.0}
     split_ms = {0.08: -15.0, 0.1: 0.0, 0.12: 20.0}
 
     def set_launch(method, adaptive, block, per_sm, variant):
@@ -74,5 +74,5 @@ def test_adaptive_dopri8_teams_without_shape_candidates(fake):
     out = A.tune(lambda: None, 8, True, candidates=())
     assert out["ms"] == {} and "block_threads" not in out["best"]
     assert set(out["team_ms"]) == {str(t) for t in A.DEFAULT_TEAMS[8]}
-    assert out["best"]["team_blocks"] == 28 and state["team"] == 28 and state["launch"] == (128, 1, 2)
+    assert out["best"]["team_blocks"] == 12 and state["team"] == 12 and state["launch"] == (128, 1, 2)
     assert all(c[0] != "launch" for c in state["calls"])

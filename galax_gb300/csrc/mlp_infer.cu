@@ -14,10 +14,11 @@
 // Every product runs as two N halves of 128 columns, committed separately, so
 // the epilogue of one half overlaps the tensor cores' work on the other, and
 // two operand tiles alternate so that an epilogue writes the next product's
-// operand while the current one is still read. The next product starts on K
-// 0..127 once the epilogue of half 0 has written those columns. A tile's layer
-// 1 is computed while the tensor cores run the previous tile's last product,
-// so its first product follows that product's epilogue directly. Weights stream
+// operand while the current one is still read. The next product's first N half
+// proceeds in K slices as the epilogues write the operand, 32 columns at a time,
+// so after an epilogue only the last slices remain. A tile's layer 1 is computed
+// while the tensor cores run the previous tile's last product, so its first
+// product starts as soon as that product's accumulator is drained. Weights stream
 // through a ring of 16 KB N-halves of K-blocks (bulk copies from pre-swizzled
 // global images) run by their own warp ahead of the products. The numerics
 // are those of the training kernels' quantised forward/backward (mlp_train.cu).
@@ -146,8 +147,9 @@ __device__ __forceinline__ void store_row32(uint8_t* tile, int row, int c, const
 //              only touch its TMEM lane quadrant (warp id % 4), so each quadrant has two warps
 // Each product splits into its two N halves, committed separately (acc_full[h]), so the
 // epilogue of half 0 runs while half 1 is on the tensor cores; the epilogue writes the next
-// product's operand into the other of two operand tiles, half by half (op_ready[h]), and the
-// next product starts on the K range of half 0 while the epilogue of half 1 still runs.
+// product's operand into the other of two operand tiles, 32 columns per thread at a time
+// (op_ready[2 h + c]: sub-chunk c of operand half h from all eight warps), and the product
+// warp issues the next product's first N half two K slices at a time as those arrive.
 // Every wait is bounded.
 __global__ void __launch_bounds__(NTHREADS, 1) k_mlp_infer(InferArgs a) {
   extern __shared__ uint8_t smem_raw[];

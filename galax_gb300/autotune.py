@@ -46,9 +46,9 @@ def set_launch(method: int, adaptive: bool, block: int, per_sm: int, variant: in
 # 262,144-orbit headline batch the step time has a narrow minimum, so the
 # candidates are spaced closely around it (ms, Dopri5: 24 -> 1,253,
 # 28 -> 1,171, 30 -> 1,172, 32 -> 1,183, 36 -> 1,211, 40 -> 1,241; Dopri8:
-# 16 -> 1,495, 20 -> 1,524, 24 -> 1,549, 28 -> 1,578, 32 -> 1,610, none ->
-# 1,852).
-DEFAULT_TEAMS = {5: (24, 28, 32, 40), 8: (8, 12, 16, 20, 24)}
+# 2 -> 1,590, 4 -> 1,525, 6 -> 1,500, 8 -> 1,454, 12 -> 1,474, 16 -> 1,499,
+# 24 -> 1,549, 32 -> 1,609, none -> 1,852).
+DEFAULT_TEAMS = {5: (24, 28, 32, 40), 8: (6, 8, 10, 12, 16)}
 
 
 def set_team(blocks: int) -> None:

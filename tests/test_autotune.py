@@ -16,7 +16,8 @@ def fake(monkeypatch):
     state = {"launch": None, "team": None, "split": None, "calls": []}
     # step time as a function of the current settings (ms); two runs each, the second slower
     launch_ms = {(128, 1, 2): 1200.0, (64, 2, 2): 1190.0, (128, 0, 0): 1300.0}
-    team_ms = {8: 90.0, 12: 30.0, 16: 80.0, 20: 50.0, 24: 40.0, 28: 0.0, 32: 10.0, 40: 60.0}
+    team_ms = {6: 70.0, 8: 90.0, 10: 55.0, 12: 30.0, 16: 80.0, 20: 50.0, 24: 40.0, 28: 0.0, 32: 10.0,
+               40: 60.0}
     split_ms = {0.08: -15.0, 0.1: 0.0, 0.12: 20.0}
 
     def set_launch(method, adaptive, block, per_sm, variant):
